@@ -1,0 +1,193 @@
+/*
+ * vecgeom_gb300 — C ABI of the GB300 (sm_103a) implementation of VecGeom's data-parallel
+ * query path: per-track SoA shape queries and the BVH navigation step.
+ *
+ * Conventions shared by every entry point
+ *  - Functions return VG_OK (0) or a negative VG_E* code; vg_last_error() describes the
+ *    last failure of the calling thread.
+ *  - Query arrays are DEVICE pointers owned by the caller (structure-of-arrays, FP64, like
+ *    vecgeom::SOA3D<double>, VecGeom/base/SOA3D.h:36-41). `stream` is a cudaStream_t
+ *    (NULL = the legacy default stream); calls are asynchronous with respect to the host.
+ *  - Results follow the reference's value conventions: Inside -> 1 inside, 2 surface,
+ *    3 outside (EnumInside, VecGeom/base/Global.h:71-79); a miss is 1.7976931348623157e308
+ *    (kInfLength); DistanceToOut of an outside point is -1; SafetyToIn is negative inside
+ *    and SafetyToOut negative outside.
+ *  - Placed-volume and logical-volume ids are assigned in creation order exactly as the
+ *    reference does (VPlacedVolume ids: source/PlacedVolume.cpp:32; child ids:
+ *    source/LogicalVolume.cpp:142-148), so states are comparable across implementations.
+ */
+#ifndef VECGEOM_GB300_H
+#define VECGEOM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+#define VG_OK 0
+#define VG_EINVAL (-1)   /* invalid argument / id / state                   */
+#define VG_ECUDA (-2)    /* CUDA runtime error (see vg_last_error)          */
+#define VG_ESTATE (-3)   /* geometry not closed, already closed, no world   */
+#define VG_ENOMEM (-4)   /* allocation failed                               */
+
+/* Per-track status written by navigation entry points (nullable `status` arrays). */
+#define VG_TRACK_OK 0
+#define VG_TRACK_ERR_STACK 1 /* BVH traversal stack bound reached */
+#define VG_TRACK_ERR_ITER 2  /* locate/relocate loop bound reached */
+#define VG_TRACK_ERR_STATE 3 /* input state outside the world       */
+
+/* Shape type tags */
+#define VG_SHAPE_BOX 1
+#define VG_SHAPE_TUBE 2
+#define VG_SHAPE_CONE 3
+#define VG_SHAPE_POLYCONE 4
+#define VG_SHAPE_POLYHEDRON 5
+#define VG_SHAPE_TORUS2 6
+#define VG_SHAPE_TRD 7
+#define VG_SHAPE_BOOLEAN_SUBTRACTION 8
+
+/* Precision flags for queries and navigation */
+#define VG_PREC_FP64 0u  /* plain FP64: results identical to the reference's FP64 path          */
+#define VG_PREC_MIXED 1u /* FP32 bulk arithmetic with FP64 guard band and FP64 recompute        */
+
+/* Navigation state: bit-identical to vecgeom::NavStateIndex {NavIndex_t fNavInd;
+ * NavIndex_t fLastExited; bool fOnBoundary;} (VecGeom/navigation/NavStateIndex.h:39-41). */
+typedef struct vg_navstate {
+  uint32_t nav_ind;
+  uint32_t last_exited;
+  uint8_t on_boundary;
+  uint8_t pad[3];
+} vg_navstate;
+
+typedef struct vg_geom vg_geom; /* opaque geometry handle */
+
+const char *vg_last_error(void);
+const char *vg_version(void);
+
+/* ---------------------------------------------------------------- geometry construction
+ * Replaces the construction half of the reference API: UnplacedBox/UnplacedTube/...
+ * constructors, LogicalVolume (VecGeom/volumes/LogicalVolume.h:87-203),
+ * LogicalVolume::PlaceDaughter (source/LogicalVolume.cpp:125-155), LogicalVolume::Place,
+ * GeoManager::SetWorld + CloseGeometry (source/GeoManager.cpp:192-240) and
+ * BVHManager::Init (source/BVHManager.cpp:24-30). Closing builds the daughter boxes, one
+ * BVH per logical volume with daughters, the NavIndex table, and uploads the flattened
+ * geometry to the current CUDA device (this replaces CudaManager::LoadGeometry/Synchronize,
+ * management/CudaManager.h:115-124). A closed geometry is immutable and may be shared by
+ * concurrent calls on different streams. */
+int vg_geom_create(vg_geom **out);
+void vg_geom_destroy(vg_geom *g);
+
+/* Shape constructors; return the shape id (>= 0) or a negative VG_E* code.
+ * Units: mm and radians. Parameter meaning follows the reference constructors cited. */
+/* UnplacedBox(dx, dy, dz): half-lengths (VecGeom/volumes/BoxStruct.h:19-27) */
+int32_t vg_geom_add_box(vg_geom *g, double dx, double dy, double dz);
+/* UnplacedTube(rmin, rmax, dz, sphi, dphi) (VecGeom/volumes/UnplacedTube.h:28-34) */
+int32_t vg_geom_add_tube(vg_geom *g, double rmin, double rmax, double dz, double sphi, double dphi);
+/* UnplacedCone(rmin1, rmax1, rmin2, rmax2, dz, sphi, dphi) (VecGeom/volumes/ConeStruct.h:327-336) */
+int32_t vg_geom_add_cone(vg_geom *g, double rmin1, double rmax1, double rmin2, double rmax2, double dz, double sphi,
+                         double dphi);
+/* UnplacedPolycone(sphi, dphi, nz, z[], rmin[], rmax[]) (VecGeom/volumes/UnplacedPolycone.h) */
+int32_t vg_geom_add_polycone(vg_geom *g, double sphi, double dphi, int32_t nz, const double *z, const double *rmin,
+                             const double *rmax);
+/* UnplacedPolyhedron(phistart, phidelta, nsides, nz, z[], rmin[], rmax[]) (VecGeom/volumes/UnplacedPolyhedron.h) */
+int32_t vg_geom_add_polyhedron(vg_geom *g, double phistart, double phidelta, int32_t nsides, int32_t nz,
+                               const double *z, const double *rmin, const double *rmax);
+/* UnplacedTorus2(rmin, rmax, rtor, sphi, dphi) (VecGeom/volumes/TorusStruct2.h) */
+int32_t vg_geom_add_torus2(vg_geom *g, double rmin, double rmax, double rtor, double sphi, double dphi);
+/* UnplacedTrd(dx1, dx2, dy1, dy2, dz) (VecGeom/volumes/TrdStruct.h:20-39) */
+int32_t vg_geom_add_trd(vg_geom *g, double dx1, double dx2, double dy1, double dy2, double dz);
+/* UnplacedBooleanVolume<kSubtraction>(left, right): operands are placed volumes created
+ * with vg_geom_place (VecGeom/volumes/BooleanStruct.h:19-33) */
+int32_t vg_geom_add_boolean_subtraction(vg_geom *g, int32_t left_pv, int32_t right_pv);
+
+/* LogicalVolume(shape); returns the logical-volume id. */
+int32_t vg_geom_add_logical_volume(vg_geom *g, int32_t shape_id);
+/* LogicalVolume::Place(transformation): a placed volume with no mother (world, boolean
+ * operands). trans[3], rot[9] as Transformation3D(tx,ty,tz,r0..r8): p_master = R p_local + t
+ * with R row-major. Returns the placed-volume id. */
+int32_t vg_geom_place(vg_geom *g, int32_t lv, const double trans[3], const double rot[9]);
+/* mother_lv.PlaceDaughter(lv, transformation); returns the placed-volume id. */
+int32_t vg_geom_place_daughter(vg_geom *g, int32_t mother_lv, int32_t lv, const double trans[3], const double rot[9]);
+/* GeoManager::SetWorld */
+int vg_geom_set_world(vg_geom *g, int32_t world_pv);
+/* Host half of the close: daughter boxes (source/ABBoxManager.cpp:109-140), the BVHs
+ * (source/BVH.cpp:48-87) and the NavIndex table (source/NavIndexTable.cpp:9-84), without
+ * touching the GPU; the introspection calls below need only this. */
+int vg_geom_build(vg_geom *g);
+/* GeoManager::CloseGeometry + BVHManager::Init + device upload (builds first if needed) */
+int vg_geom_close(vg_geom *g);
+/* Introspection of a built geometry (host copies). */
+int vg_geom_info(const vg_geom *g, int32_t *n_shapes, int32_t *n_lv, int32_t *n_pv, int32_t *max_depth,
+                 size_t *nav_table_words, size_t *device_bytes);
+int vg_geom_nav_table(const vg_geom *g, uint32_t *out, size_t words);
+int vg_geom_bvh_sizes(const vg_geom *g, int32_t lv, int32_t *n_nodes, int32_t *n_prims, int32_t *depth);
+int vg_geom_bvh_arrays(const vg_geom *g, int32_t lv, int32_t *prim_id, int32_t *offset, int32_t *nchild,
+                       double *node_box6, double *prim_box6);
+int vg_geom_shape_extent(const vg_geom *g, int32_t shape_id, double lo[3], double hi[3]);
+
+/* ---------------------------------------------------------------- SoA shape queries
+ * Replace the SoA virtuals of VPlacedVolume (VecGeom/volumes/PlacedVolume.h:271-425):
+ *   Inside(SOA3D const&, Inside_t*)                        -> vg_placed_inside        (:299)
+ *   Contains(SOA3D const&, bool*)                          -> vg_placed_contains      (:273)
+ *   DistanceToIn(SOA3D const&, SOA3D const&, Precision const* step_max, Precision*)
+ *                                                          -> vg_placed_distance_to_in  (:332)
+ *   DistanceToOut(SOA3D const&, SOA3D const&, step_max*, out*) -> vg_placed_distance_to_out (:372)
+ *   SafetyToIn(SOA3D const&, Precision*)                   -> vg_placed_safety_to_in  (:405)
+ *   SafetyToOut(SOA3D const&, Precision*)                  -> vg_placed_safety_to_out (:421)
+ * Inside, Contains, DistanceToIn and SafetyToIn take points in the mother frame (the placed
+ * volume's transformation is applied); DistanceToOut and SafetyToOut take local points, as
+ * in the reference (VecGeom/volumes/PlacedVolImplHelper.h:70-123). `step_max` may be NULL
+ * (the shapes ignore it, as the reference's do). `flags`: VG_PREC_FP64 or VG_PREC_MIXED. */
+int vg_placed_inside(const vg_geom *g, int32_t pv, const double *x, const double *y, const double *z, size_t n,
+                     int32_t *out, uint32_t flags, void *stream);
+int vg_placed_contains(const vg_geom *g, int32_t pv, const double *x, const double *y, const double *z, size_t n,
+                       uint8_t *out, uint32_t flags, void *stream);
+int vg_placed_distance_to_in(const vg_geom *g, int32_t pv, const double *x, const double *y, const double *z,
+                             const double *dx, const double *dy, const double *dz, const double *step_max, size_t n,
+                             double *out, uint32_t flags, void *stream);
+int vg_placed_distance_to_out(const vg_geom *g, int32_t pv, const double *x, const double *y, const double *z,
+                              const double *dx, const double *dy, const double *dz, const double *step_max, size_t n,
+                              double *out, uint32_t flags, void *stream);
+int vg_placed_safety_to_in(const vg_geom *g, int32_t pv, const double *x, const double *y, const double *z, size_t n,
+                           double *out, uint32_t flags, void *stream);
+int vg_placed_safety_to_out(const vg_geom *g, int32_t pv, const double *x, const double *y, const double *z, size_t n,
+                            double *out, uint32_t flags, void *stream);
+
+/* ---------------------------------------------------------------- navigation
+ * vg_nav_locate_point replaces GlobalLocator::LocateGlobalPoint(world, p, state, true)
+ * (VecGeom/navigation/GlobalLocator.h:35-82) with BVHLevelLocator on every logical volume
+ * (VecGeom/navigation/BVHLevelLocator.h:44-48). Points outside the world give nav_ind 0. */
+int vg_nav_locate_point(const vg_geom *g, const double *x, const double *y, const double *z, size_t n,
+                        vg_navstate *out, void *stream);
+
+/* vg_nav_compute_step_and_next_volume replaces the SoA navigator call
+ * VNavigator::ComputeStepsAndPropagatedStates(SOA3D const&, SOA3D const&, Precision const*
+ * step_limits, NavigationState const* const* in, NavigationState** out, Precision* steps)
+ * (VecGeom/navigation/VNavigator.h:128-132) for BVHNavigator<false>, i.e. per track
+ * VNavigatorHelper::ComputeStepAndPropagatedState (VNavigator.h:436-492): DistanceToOut of
+ * the current volume, BVH daughter intersection, PrepareOutState, relocation after the
+ * boundary. The "next volume" is out[i] (its Top()). `step_limit` may be NULL (no physics
+ * limit: kInfLength). `status` (nullable) receives VG_TRACK_* per track. `flags`:
+ * VG_PREC_FP64 or VG_PREC_MIXED (same out states; steps within 1e-9 mm of FP64). */
+int vg_nav_compute_step_and_next_volume(const vg_geom *g, const double *x, const double *y, const double *z,
+                                        const double *dx, const double *dy, const double *dz,
+                                        const double *step_limit, const vg_navstate *in, vg_navstate *out,
+                                        double *step, int32_t *status, size_t n, uint32_t flags, void *stream);
+
+/* Same step with HOST arrays, the form the reference's own SoA navigator interface takes
+ * (VNavigator::ComputeStepsAndPropagatedStates, VNavigator.h:128-132): inputs are copied to
+ * device staging buffers owned by the handle (allocated on first use, grown on demand,
+ * serialised by a lock), the kernel runs on `stream`, results are copied back and the call
+ * returns after the stream has synchronised. Pinned host memory gives full copy bandwidth. */
+int vg_nav_compute_step_and_next_volume_host(vg_geom *g, const double *x, const double *y, const double *z,
+                                             const double *dx, const double *dy, const double *dz,
+                                             const double *step_limit, const vg_navstate *in, vg_navstate *out,
+                                             double *step, int32_t *status, size_t n, uint32_t flags, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VECGEOM_GB300_H */

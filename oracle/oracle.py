@@ -1,0 +1,201 @@
+"""ctypes wrapper of the oracle (TEST INFRASTRUCTURE ONLY — see ref_base.h).
+
+Mirrors the construction methods of ``vecgeom_gb300.Geometry`` so that the same builder
+function (vecgeom_gb300.workloads) produces identical geometries on both sides, and
+exposes batched CPU queries on numpy arrays. Only tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg use it.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+_dp = ctypes.POINTER(ctypes.c_double)
+_vp = ctypes.c_void_p
+NAVSTATE_DTYPE = np.dtype([("nav_ind", "<u4"), ("last_exited", "<u4"), ("on_boundary", "u1"), ("pad", "u1", 3)])
+
+
+def load():
+    global _lib
+    if _lib is None:
+        path = _build.LIB if os.path.exists(_build.LIB) else _build.build()
+        lib = ctypes.CDLL(path)
+        sig = {
+            "oracle_geom_create": (_vp, []),
+            "oracle_geom_destroy": (None, [_vp]),
+            "oracle_add_shape": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.c_int]),
+            "oracle_add_lv": (ctypes.c_int, [_vp, ctypes.c_int]),
+            "oracle_place": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp]),
+            "oracle_place_daughter": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp, _dp]),
+            "oracle_set_world": (None, [_vp, ctypes.c_int]),
+            "oracle_close": (ctypes.c_int, [_vp]),
+            "oracle_shape_extent": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp]),
+            "oracle_placed_query": (ctypes.c_double, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_size_t] + [_vp] * 6 +
+                                    [ctypes.c_double, _vp, _vp, ctypes.c_int]),
+            "oracle_nav_table_words": (ctypes.c_size_t, [_vp]),
+            "oracle_nav_table": (None, [_vp, _vp]),
+            "oracle_max_depth": (ctypes.c_int, [_vp]),
+            "oracle_bvh_sizes": (ctypes.c_int, [_vp, ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 3),
+            "oracle_bvh_arrays": (ctypes.c_int, [_vp, ctypes.c_int] + [_vp] * 5),
+            "oracle_nav_locate": (ctypes.c_double, [_vp, ctypes.c_size_t, _vp, _vp, _vp, _vp, ctypes.c_int]),
+            "oracle_nav_step": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 11 + [ctypes.c_int]),
+            "oracle_nav_step_safety": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 11 + [ctypes.c_int]),
+            "oracle_nav_transport": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 7 +
+                                     [ctypes.c_int, _vp, _vp, _vp, _vp, ctypes.c_int]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(_vp)
+
+
+def _d(v):
+    a = np.ascontiguousarray(np.asarray(v, dtype=np.float64))
+    return a, a.ctypes.data_as(_dp)
+
+
+class OracleGeometry:
+    """Same construction surface as vecgeom_gb300.Geometry, evaluated on the CPU."""
+
+    def __init__(self):
+        load()
+        self._h = _lib.oracle_geom_create()
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.oracle_geom_destroy(self._h)
+            self._h = None
+
+    def _shape(self, t, params):
+        a, p = _d(params)
+        r = _lib.oracle_add_shape(self._h, t, p, a.size)
+        if r < 0:
+            raise RuntimeError("oracle: unsupported shape type %d" % t)
+        return r
+
+    def add_box(self, dx, dy, dz):
+        return self._shape(1, [dx, dy, dz])
+
+    def add_tube(self, rmin, rmax, dz, sphi, dphi):
+        return self._shape(2, [rmin, rmax, dz, sphi, dphi])
+
+    def add_cone(self, rmin1, rmax1, rmin2, rmax2, dz, sphi, dphi):
+        return self._shape(3, [rmin1, rmax1, rmin2, rmax2, dz, sphi, dphi])
+
+    def add_polycone(self, sphi, dphi, z, rmin, rmax):
+        return self._shape(4, [sphi, dphi, len(z), *z, *rmin, *rmax])
+
+    def add_polyhedron(self, phistart, phidelta, nsides, z, rmin, rmax):
+        return self._shape(5, [phistart, phidelta, nsides, len(z), *z, *rmin, *rmax])
+
+    def add_torus2(self, rmin, rmax, rtor, sphi, dphi):
+        return self._shape(6, [rmin, rmax, rtor, sphi, dphi])
+
+    def add_trd(self, dx1, dx2, dy1, dy2, dz):
+        return self._shape(7, [dx1, dx2, dy1, dy2, dz])
+
+    def add_boolean_subtraction(self, left_pv, right_pv):
+        return self._shape(8, [left_pv, right_pv])
+
+    def add_logical_volume(self, shape):
+        return _lib.oracle_add_lv(self._h, shape)
+
+    def place(self, lv, trans=(0.0, 0.0, 0.0), rot=(1.0, 0, 0, 0, 1.0, 0, 0, 0, 1.0)):
+        t, tp = _d(trans)
+        r, rp = _d(rot)
+        return _lib.oracle_place(self._h, lv, tp, rp)
+
+    def place_daughter(self, mother_lv, lv, trans=(0.0, 0.0, 0.0), rot=(1.0, 0, 0, 0, 1.0, 0, 0, 0, 1.0)):
+        t, tp = _d(trans)
+        r, rp = _d(rot)
+        return _lib.oracle_place_daughter(self._h, mother_lv, lv, tp, rp)
+
+    def set_world(self, pv):
+        _lib.oracle_set_world(self._h, pv)
+
+    def close(self):
+        if _lib.oracle_close(self._h) != 0:
+            raise RuntimeError("oracle close failed")
+
+    def shape_extent(self, shape):
+        lo, lp = _d(np.zeros(3))
+        hi, hp = _d(np.zeros(3))
+        _lib.oracle_shape_extent(self._h, shape, lp, hp)
+        return lo, hi
+
+    # ------------------------------------------------------------ queries (numpy, CPU)
+    def query(self, pv, q, x, y, z, dx=None, dy=None, dz=None, step_max=np.finfo(np.float64).max, nthreads=1):
+        """q: 0 Inside, 1 Contains, 2 DistanceToIn, 3 DistanceToOut, 4 SafetyToIn, 5 SafetyToOut."""
+        n = len(x)
+        outd = np.empty(n, np.float64)
+        outi = np.empty(n, np.int32)
+        t = _lib.oracle_placed_query(self._h, pv, q, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), step_max,
+                                     _p(outd), _p(outi), nthreads)
+        return (outi if q in (0, 1) else outd), t
+
+    def nav_table(self):
+        n = _lib.oracle_nav_table_words(self._h)
+        out = np.zeros(n, np.uint32)
+        _lib.oracle_nav_table(self._h, _p(out))
+        return out
+
+    def max_depth(self):
+        return _lib.oracle_max_depth(self._h)
+
+    def bvh(self, lv):
+        nn, npr, dep = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        if _lib.oracle_bvh_sizes(self._h, lv, ctypes.byref(nn), ctypes.byref(npr), ctypes.byref(dep)) != 0:
+            return None
+        prim = np.zeros(npr.value, np.int32)
+        off = np.zeros(nn.value, np.int32)
+        nch = np.zeros(nn.value, np.int32)
+        nodes = np.zeros((nn.value, 6))
+        boxes = np.zeros((npr.value, 6))
+        _lib.oracle_bvh_arrays(self._h, lv, _p(prim), _p(off), _p(nch), _p(nodes), _p(boxes))
+        return dict(depth=dep.value, prim=prim, offset=off, nchild=nch, nodes=nodes, boxes=boxes)
+
+    def locate(self, x, y, z, nthreads=1):
+        out = np.zeros(len(x), NAVSTATE_DTYPE)
+        t = _lib.oracle_nav_locate(self._h, len(x), _p(x), _p(y), _p(z), _p(out), nthreads)
+        return out, t
+
+    def step(self, x, y, z, dx, dy, dz, states, step_limit=None, nthreads=1, count_nodes=False):
+        n = len(x)
+        if step_limit is None:
+            step_limit = np.full(n, np.finfo(np.float64).max)
+        out = np.zeros(n, NAVSTATE_DTYPE)
+        step = np.zeros(n)
+        nv = np.zeros(n, np.int32) if count_nodes else None
+        t = _lib.oracle_nav_step(self._h, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(step_limit),
+                                 _p(states), _p(out), _p(step), _p(nv), nthreads)
+        return out, step, nv, t
+
+    def step_safety(self, x, y, z, dx, dy, dz, states, step_limit=None, nthreads=1):
+        n = len(x)
+        if step_limit is None:
+            step_limit = np.full(n, np.finfo(np.float64).max)
+        out = np.zeros(n, NAVSTATE_DTYPE)
+        step = np.zeros(n)
+        saf = np.zeros(n)
+        t = _lib.oracle_nav_step_safety(self._h, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(step_limit),
+                                        _p(states), _p(out), _p(step), _p(saf), nthreads)
+        return out, step, saf, t
+
+    def transport(self, x, y, z, dx, dy, dz, states, max_steps, trace=False, nthreads=1):
+        n = len(x)
+        nsteps = np.zeros(n, np.int32)
+        final = np.zeros(n, NAVSTATE_DTYPE)
+        tr = np.zeros((n, max_steps), np.uint32) if trace else None
+        trs = np.zeros((n, max_steps)) if trace else None
+        t = _lib.oracle_nav_transport(self._h, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(states),
+                                      max_steps, _p(nsteps), _p(final), _p(tr), _p(trs), nthreads)
+        return nsteps, final, tr, trs, t

@@ -1,0 +1,218 @@
+// ORACLE — TEST INFRASTRUCTURE ONLY (see ref_base.h).
+//
+// extern "C" surface of the oracle for ctypes (tests, smoke check, bench cpu_baseline).
+// Geometry is described with the same call sequence as the product's C-ABI, so both
+// sides assign identical placed-volume ids and child ids. Batched queries split the
+// track range into contiguous chunks over std::thread workers.
+#include "ref_nav.h"
+#include <chrono>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+using namespace oracle;
+
+namespace {
+template <class F>
+double ParallelFor(size_t n, int nthreads, F &&f)
+{
+  auto t0 = std::chrono::steady_clock::now();
+  if (nthreads <= 1 || n < 1024) {
+    f(0, n);
+  } else {
+    std::vector<std::thread> th;
+    const size_t chunk = (n + nthreads - 1) / nthreads;
+    for (int t = 0; t < nthreads; ++t) {
+      const size_t b = t * chunk, e = std::min(n, b + chunk);
+      if (b >= e) break;
+      th.emplace_back([&f, b, e]() { f(b, e); });
+    }
+    for (auto &t : th) t.join();
+  }
+  return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+} // namespace
+
+extern "C" {
+
+void *oracle_geom_create() { return new Geometry(); }
+void oracle_geom_destroy(void *g) { delete static_cast<Geometry *>(g); }
+
+// type: 1 Box, 2 Tube, 3 Cone, 4 Polycone, 5 Polyhedron, 6 Torus2, 7 Trd, 8 BooleanSubtraction
+int oracle_add_shape(void *gp, int type, const double *p, int np)
+{
+  Geometry *g = static_cast<Geometry *>(gp);
+  UnplacedShape *s = nullptr;
+  switch (type) {
+  case 1: s = new Box(p[0], p[1], p[2]); break;
+  case 2: s = new Tube(p[0], p[1], p[2], p[3], p[4]); break;
+  case 3: s = new Cone(p[0], p[1], p[2], p[3], p[4], p[5], p[6]); break;
+  default: return -1;
+  }
+  (void)np;
+  return g->AddShape(s);
+}
+int oracle_add_lv(void *g, int shape) { return static_cast<Geometry *>(g)->AddLogicalVolume(shape); }
+int oracle_place(void *g, int lv, const double *tr, const double *rot)
+{
+  return static_cast<Geometry *>(g)->Place(lv, tr, rot);
+}
+int oracle_place_daughter(void *g, int mother, int lv, const double *tr, const double *rot)
+{
+  return static_cast<Geometry *>(g)->PlaceDaughter(mother, lv, tr, rot);
+}
+void oracle_set_world(void *g, int pv) { static_cast<Geometry *>(g)->world = static_cast<Geometry *>(g)->pvs.at(pv).get(); }
+int oracle_close(void *g)
+{
+  try {
+    static_cast<Geometry *>(g)->Close();
+  } catch (...) {
+    return -1;
+  }
+  return 0;
+}
+int oracle_shape_extent(void *gp, int shape, double *lo, double *hi)
+{
+  Vec3 a, b;
+  static_cast<Geometry *>(gp)->shapes.at(shape)->Extent(a, b);
+  for (int i = 0; i < 3; ++i) lo[i] = a[i], hi[i] = b[i];
+  return 0;
+}
+
+// q: 0 Inside, 1 Contains, 2 DistanceToIn, 3 DistanceToOut, 4 SafetyToIn, 5 SafetyToOut.
+// Returns the wall time of the batched loop (seconds).
+double oracle_placed_query(void *gp, int pv, int q, size_t n, const double *x, const double *y, const double *z,
+                           const double *dx, const double *dy, const double *dz, double step_max, double *outd,
+                           int *outi, int nthreads)
+{
+  Geometry *g           = static_cast<Geometry *>(gp);
+  PlacedVolume const *v = g->pvs.at(pv).get();
+  return ParallelFor(n, nthreads, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i) {
+      const Vec3 p(x[i], y[i], z[i]);
+      switch (q) {
+      case 0: outi[i] = v->Inside(p); break;
+      case 1: outi[i] = v->Contains(p) ? 1 : 0; break;
+      case 2: outd[i] = v->DistanceToIn(p, Vec3(dx[i], dy[i], dz[i]), step_max); break;
+      case 3: outd[i] = v->DistanceToOut(p, Vec3(dx[i], dy[i], dz[i]), step_max); break;
+      case 4: outd[i] = v->SafetyToIn(p); break;
+      case 5: outd[i] = v->SafetyToOut(p); break;
+      }
+    }
+  });
+}
+
+size_t oracle_nav_table_words(void *g) { return static_cast<Geometry *>(g)->tableWords; }
+void oracle_nav_table(void *gp, uint32_t *out)
+{
+  Geometry *g = static_cast<Geometry *>(gp);
+  std::memcpy(out, g->table, g->tableWords * sizeof(uint32_t));
+}
+int oracle_max_depth(void *g) { return static_cast<Geometry *>(g)->maxDepth; }
+
+// BVH arrays of logical volume `lv` (daughters > 0): sizes first, then the arrays.
+int oracle_bvh_sizes(void *gp, int lv, int *nnodes, int *nprims, int *depth)
+{
+  Geometry *g = static_cast<Geometry *>(gp);
+  BVH *b      = g->lvs.at(lv)->bvh;
+  if (!b) return -1;
+  *nnodes = (int)b->nodes.size();
+  *nprims = (int)b->primId.size();
+  *depth  = b->depth;
+  return 0;
+}
+int oracle_bvh_arrays(void *gp, int lv, int *primId, int *offset, int *nchild, double *nodes6, double *aabbs6)
+{
+  Geometry *g = static_cast<Geometry *>(gp);
+  BVH *b      = g->lvs.at(lv)->bvh;
+  if (!b) return -1;
+  for (size_t i = 0; i < b->primId.size(); ++i) primId[i] = b->primId[i];
+  for (size_t i = 0; i < b->nodes.size(); ++i) {
+    offset[i] = b->offset[i];
+    nchild[i] = b->nchild[i];
+    for (int k = 0; k < 3; ++k) nodes6[6 * i + k] = b->nodes[i].mn[k], nodes6[6 * i + 3 + k] = b->nodes[i].mx[k];
+  }
+  for (size_t i = 0; i < b->aabbs.size(); ++i)
+    for (int k = 0; k < 3; ++k) aabbs6[6 * i + k] = b->aabbs[i].mn[k], aabbs6[6 * i + 3 + k] = b->aabbs[i].mx[k];
+  return 0;
+}
+
+// GlobalLocator::LocateGlobalPoint(world, p, state, true) per track.
+double oracle_nav_locate(void *gp, size_t n, const double *x, const double *y, const double *z, NavState *out,
+                         int nthreads)
+{
+  Geometry *g = static_cast<Geometry *>(gp);
+  return ParallelFor(n, nthreads, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i) {
+      NavState s;
+      g->LocateGlobalPoint(g->world, Vec3(x[i], y[i], z[i]), s, true);
+      out[i] = s;
+    }
+  });
+}
+
+// One ComputeStepAndPropagatedState per track. nvisited (nullable) receives the BVH nodes popped.
+double oracle_nav_step(void *gp, size_t n, const double *x, const double *y, const double *z, const double *dx,
+                       const double *dy, const double *dz, const double *step_limit, const NavState *in,
+                       NavState *out, double *step, int *nvisited, int nthreads)
+{
+  Geometry *g = static_cast<Geometry *>(gp);
+  return ParallelFor(n, nthreads, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i) {
+      int nv = 0;
+      if (in[i].navInd == 0) { // outside the world: the reference would dereference a null volume
+        out[i]  = in[i];
+        step[i] = 0.;
+        if (nvisited) nvisited[i] = 0;
+        continue;
+      }
+      step[i] = g->ComputeStepAndPropagatedState(Vec3(x[i], y[i], z[i]), Vec3(dx[i], dy[i], dz[i]), step_limit[i],
+                                                 in[i], out[i], nvisited ? &nv : nullptr);
+      if (nvisited) nvisited[i] = nv;
+    }
+  });
+}
+
+// Step + safety (VNavigator.h:1014-1064).
+double oracle_nav_step_safety(void *gp, size_t n, const double *x, const double *y, const double *z,
+                              const double *dx, const double *dy, const double *dz, const double *step_limit,
+                              const NavState *in, NavState *out, double *step, double *safety, int nthreads)
+{
+  Geometry *g = static_cast<Geometry *>(gp);
+  return ParallelFor(n, nthreads, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i)
+      step[i] = g->ComputeStepAndSafetyAndPropagatedState(Vec3(x[i], y[i], z[i]), Vec3(dx[i], dy[i], dz[i]),
+                                                          step_limit[i], in[i], out[i], safety[i]);
+  });
+}
+
+// Full transport of straight tracks: step (with the step limit kInfLength) and move the
+// point by the step, until the state leaves the world or max_steps is reached.
+// Records per track the number of steps and the final state; `trace` (nullable, size
+// n*max_steps) receives the nav index after each step, `trace_step` the step lengths.
+double oracle_nav_transport(void *gp, size_t n, const double *x, const double *y, const double *z, const double *dx,
+                            const double *dy, const double *dz, const NavState *in, int max_steps, int *nsteps,
+                            NavState *final_state, uint32_t *trace, double *trace_step, int nthreads)
+{
+  Geometry *g = static_cast<Geometry *>(gp);
+  return ParallelFor(n, nthreads, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i) {
+      Vec3 p(x[i], y[i], z[i]);
+      const Vec3 d(dx[i], dy[i], dz[i]);
+      NavState s = in[i], o;
+      int k      = 0;
+      while (s.navInd != 0 && k < max_steps) {
+        const double st = g->ComputeStepAndPropagatedState(p, d, kInfLength, s, o);
+        if (trace) trace[i * (size_t)max_steps + k] = o.navInd;
+        if (trace_step) trace_step[i * (size_t)max_steps + k] = st;
+        p = p + st * d;
+        s = o;
+        ++k;
+      }
+      nsteps[i]      = k;
+      final_state[i] = s;
+    }
+  });
+}
+
+} // extern "C"

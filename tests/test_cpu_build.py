@@ -1,0 +1,97 @@
+"""CPU tests: the C-ABI library loads and exports every declared symbol, and the product's
+host geometry builder reproduces the oracle's daughter boxes, BVHs and NavIndex table
+bit-for-bit (no GPU needed: vg_geom_build flattens on the host only)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+import __graft_entry__
+
+__graft_entry__.build()
+
+import vecgeom_gb300 as vg  # noqa: E402
+from vecgeom_gb300 import workloads as W  # noqa: E402
+from oracle.oracle import OracleGeometry  # noqa: E402
+
+
+def declared_symbols():
+    names = []
+    inc = os.path.join(ROOT, "include")
+    for f in sorted(os.listdir(inc)):
+        if f.endswith(".h"):
+            src = open(os.path.join(inc, f)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names += re.findall(r"\b(vg_[a-z0-9_]+)\s*\(", src)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ctypes.CDLL(vg.LIB_PATH)
+    names = declared_symbols()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_the_abi():
+    bound = set(vg._SIGS)
+    assert set(declared_symbols()) <= bound | set()
+
+
+class HostOnly:
+    """Forwards construction calls; close() only flattens on the host (no GPU)."""
+
+    def __init__(self, g):
+        self.g = g
+
+    def __getattr__(self, n):
+        return getattr(self.g, n)
+
+    def close(self):
+        self.g.build()
+
+
+def compare_builders(builder, **kw):
+    p, o = vg.Geometry(), OracleGeometry()
+    builder(HostOnly(p), **kw)
+    builder(o, **kw)
+    assert np.array_equal(p.nav_table(), o.nav_table())
+    info = p.info()
+    assert info["max_depth"] == o.max_depth()
+    nbvh = 0
+    for lv in range(info["n_lv"]):
+        ob = o.bvh(lv)
+        if ob is None:
+            continue
+        pb = p.bvh(lv)
+        nbvh += 1
+        assert pb["depth"] == ob["depth"]
+        for k in ("prim", "offset", "nchild", "nodes", "boxes"):
+            assert np.array_equal(pb[k], ob[k]), (lv, k)
+    return info, nbvh
+
+
+def test_barrel_tables_match_oracle():
+    info, nbvh = compare_builders(W.build_barrel)
+    assert info["n_pv"] > 3500 and info["max_depth"] == 4 and nbvh == 12
+
+
+def test_small_barrel_variants_match_oracle():
+    for seed in (1, 2, 3):
+        compare_builders(W.build_barrel, seed=seed, nlayers=4, n0=20, n1=300)
+
+
+def test_builder_rejects_bad_ids():
+    g = vg.Geometry()
+    with pytest.raises(vg.VGError):
+        g.add_logical_volume(5)
+    s = g.add_box(1, 1, 1)
+    lv = g.add_logical_volume(s)
+    with pytest.raises(vg.VGError):
+        g.place_daughter(7, lv)
+    with pytest.raises(vg.VGError):
+        g.set_world(3)

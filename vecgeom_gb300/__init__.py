@@ -1,0 +1,299 @@
+"""Python binding of libvecgeom_gb300 (ctypes over the C-ABI in include/vecgeom_gb300.h).
+
+The names mirror the reference's API for the query path: a ``Geometry`` is assembled
+with shape constructors, logical volumes and placements (UnplacedBox, LogicalVolume,
+PlaceDaughter, GeoManager::SetWorldAndClose), after which its placed volumes answer the
+SoA queries of VPlacedVolume (Inside, Contains, DistanceToIn/Out, SafetyToIn/Out) and the
+BVH navigator answers LocatePoint and ComputeStepAndNextVolume, all on the GPU.
+
+Query methods take CUDA tensors (torch is used only for device memory and streams) and
+launch on torch's current stream. There is no CPU fallback: if the CUDA library is not
+built, loading fails with an error that says so.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+__all__ = ["Geometry", "load_library", "NAVSTATE_DTYPE", "PREC_FP64", "PREC_MIXED", "VGError",
+           "kInside", "kSurface", "kOutside", "kInfLength", "IDENTITY_ROT", "ZERO_TRANS"]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libvecgeom_gb300.so")
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+kInside, kSurface, kOutside = 1, 2, 3
+kInfLength = np.finfo(np.float64).max
+IDENTITY_ROT = (1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0)
+ZERO_TRANS = (0.0, 0.0, 0.0)
+
+# vg_navstate / vecgeom::NavStateIndex {uint32 nav_ind; uint32 last_exited; bool on_boundary}
+NAVSTATE_DTYPE = np.dtype([("nav_ind", "<u4"), ("last_exited", "<u4"), ("on_boundary", "u1"), ("pad", "u1", 3)])
+assert NAVSTATE_DTYPE.itemsize == 12
+
+SHAPE_BOX, SHAPE_TUBE, SHAPE_CONE, SHAPE_POLYCONE, SHAPE_POLYHEDRON, SHAPE_TORUS2, SHAPE_TRD, SHAPE_BOOLMINUS = range(1, 9)
+
+
+class VGError(RuntimeError):
+    pass
+
+
+_lib = None
+_c_dp = ctypes.POINTER(ctypes.c_double)
+_c_vp = ctypes.c_void_p
+
+# name -> (restype, argtypes)
+_SIGS = {
+    "vg_last_error": (ctypes.c_char_p, []),
+    "vg_version": (ctypes.c_char_p, []),
+    "vg_geom_create": (ctypes.c_int, [ctypes.POINTER(_c_vp)]),
+    "vg_geom_destroy": (None, [_c_vp]),
+    "vg_geom_add_box": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 3),
+    "vg_geom_add_tube": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 5),
+    "vg_geom_add_cone": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 7),
+    "vg_geom_add_polycone": (ctypes.c_int32, [_c_vp, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
+                                              _c_dp, _c_dp, _c_dp]),
+    "vg_geom_add_polyhedron": (ctypes.c_int32, [_c_vp, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
+                                                ctypes.c_int32, _c_dp, _c_dp, _c_dp]),
+    "vg_geom_add_torus2": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 5),
+    "vg_geom_add_trd": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 5),
+    "vg_geom_add_boolean_subtraction": (ctypes.c_int32, [_c_vp, ctypes.c_int32, ctypes.c_int32]),
+    "vg_geom_add_logical_volume": (ctypes.c_int32, [_c_vp, ctypes.c_int32]),
+    "vg_geom_place": (ctypes.c_int32, [_c_vp, ctypes.c_int32, _c_dp, _c_dp]),
+    "vg_geom_place_daughter": (ctypes.c_int32, [_c_vp, ctypes.c_int32, ctypes.c_int32, _c_dp, _c_dp]),
+    "vg_geom_set_world": (ctypes.c_int, [_c_vp, ctypes.c_int32]),
+    "vg_geom_close": (ctypes.c_int, [_c_vp]),
+    "vg_geom_build": (ctypes.c_int, [_c_vp]),
+    "vg_geom_info": (ctypes.c_int, [_c_vp] + [ctypes.POINTER(ctypes.c_int32)] * 4 +
+                     [ctypes.POINTER(ctypes.c_size_t)] * 2),
+    "vg_geom_nav_table": (ctypes.c_int, [_c_vp, _c_vp, ctypes.c_size_t]),
+    "vg_geom_bvh_sizes": (ctypes.c_int, [_c_vp, ctypes.c_int32] + [ctypes.POINTER(ctypes.c_int32)] * 3),
+    "vg_geom_bvh_arrays": (ctypes.c_int, [_c_vp, ctypes.c_int32] + [_c_vp] * 5),
+    "vg_geom_shape_extent": (ctypes.c_int, [_c_vp, ctypes.c_int32, _c_dp, _c_dp]),
+    "vg_placed_inside": (ctypes.c_int, [_c_vp, ctypes.c_int32, _c_vp, _c_vp, _c_vp, ctypes.c_size_t, _c_vp,
+                                        ctypes.c_uint32, _c_vp]),
+    "vg_placed_contains": (ctypes.c_int, [_c_vp, ctypes.c_int32, _c_vp, _c_vp, _c_vp, ctypes.c_size_t, _c_vp,
+                                          ctypes.c_uint32, _c_vp]),
+    "vg_placed_distance_to_in": (ctypes.c_int, [_c_vp, ctypes.c_int32] + [_c_vp] * 7 +
+                                 [ctypes.c_size_t, _c_vp, ctypes.c_uint32, _c_vp]),
+    "vg_placed_distance_to_out": (ctypes.c_int, [_c_vp, ctypes.c_int32] + [_c_vp] * 7 +
+                                  [ctypes.c_size_t, _c_vp, ctypes.c_uint32, _c_vp]),
+    "vg_placed_safety_to_in": (ctypes.c_int, [_c_vp, ctypes.c_int32, _c_vp, _c_vp, _c_vp, ctypes.c_size_t, _c_vp,
+                                              ctypes.c_uint32, _c_vp]),
+    "vg_placed_safety_to_out": (ctypes.c_int, [_c_vp, ctypes.c_int32, _c_vp, _c_vp, _c_vp, ctypes.c_size_t,
+                                               _c_vp, ctypes.c_uint32, _c_vp]),
+    "vg_nav_locate_point": (ctypes.c_int, [_c_vp, _c_vp, _c_vp, _c_vp, ctypes.c_size_t, _c_vp, _c_vp]),
+    "vg_nav_compute_step_and_next_volume": (ctypes.c_int, [_c_vp] + [_c_vp] * 12 +
+                                            [ctypes.c_size_t, ctypes.c_uint32, _c_vp]),
+    "vg_nav_compute_step_and_next_volume_host": (ctypes.c_int, [_c_vp] + [_c_vp] * 12 +
+                                                 [ctypes.c_size_t, ctypes.c_uint32, _c_vp]),
+}
+
+
+def load_library(path=None):
+    """Load libvecgeom_gb300.so (built in-tree by ``__graft_entry__.build()``)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise VGError("libvecgeom_gb300.so is not built (%s); run `python -c \"import __graft_entry__ as g; "
+                      "g.build()\"` first — there is no CPU fallback" % p)
+    lib = ctypes.CDLL(p)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _check(rc, what):
+    if rc < 0:
+        msg = _lib.vg_last_error().decode()
+        raise VGError("%s failed (%d): %s" % (what, rc, msg))
+    return rc
+
+
+def _darr(v, n=None):
+    a = np.ascontiguousarray(np.asarray(v, dtype=np.float64))
+    if n is not None:
+        assert a.size == n, (a.size, n)
+    return a, a.ctypes.data_as(_c_dp)
+
+
+def _ptr(t):
+    """Device pointer of a CUDA tensor (or None)."""
+    if t is None:
+        return None
+    if not t.is_cuda or not t.is_contiguous():
+        raise VGError("query arrays must be contiguous CUDA tensors")
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream():
+    import torch
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class Geometry:
+    """A geometry handle: construction API + device queries (see module docstring)."""
+
+    def __init__(self):
+        load_library()
+        h = ctypes.c_void_p()
+        _check(_lib.vg_geom_create(ctypes.byref(h)), "vg_geom_create")
+        self._h = h
+        self.closed = False
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.vg_geom_destroy(self._h)
+            self._h = None
+
+    # ---------------------------------------------------------------- construction
+    def add_box(self, dx, dy, dz):
+        return _check(_lib.vg_geom_add_box(self._h, dx, dy, dz), "add_box")
+
+    def add_tube(self, rmin, rmax, dz, sphi, dphi):
+        return _check(_lib.vg_geom_add_tube(self._h, rmin, rmax, dz, sphi, dphi), "add_tube")
+
+    def add_cone(self, rmin1, rmax1, rmin2, rmax2, dz, sphi, dphi):
+        return _check(_lib.vg_geom_add_cone(self._h, rmin1, rmax1, rmin2, rmax2, dz, sphi, dphi), "add_cone")
+
+    def add_polycone(self, sphi, dphi, z, rmin, rmax):
+        n = len(z)
+        za, zp = _darr(z, n)
+        ra, rp = _darr(rmin, n)
+        sa, sp = _darr(rmax, n)
+        return _check(_lib.vg_geom_add_polycone(self._h, sphi, dphi, n, zp, rp, sp), "add_polycone")
+
+    def add_polyhedron(self, phistart, phidelta, nsides, z, rmin, rmax):
+        n = len(z)
+        za, zp = _darr(z, n)
+        ra, rp = _darr(rmin, n)
+        sa, sp = _darr(rmax, n)
+        return _check(_lib.vg_geom_add_polyhedron(self._h, phistart, phidelta, nsides, n, zp, rp, sp),
+                      "add_polyhedron")
+
+    def add_torus2(self, rmin, rmax, rtor, sphi, dphi):
+        return _check(_lib.vg_geom_add_torus2(self._h, rmin, rmax, rtor, sphi, dphi), "add_torus2")
+
+    def add_trd(self, dx1, dx2, dy1, dy2, dz):
+        return _check(_lib.vg_geom_add_trd(self._h, dx1, dx2, dy1, dy2, dz), "add_trd")
+
+    def add_boolean_subtraction(self, left_pv, right_pv):
+        return _check(_lib.vg_geom_add_boolean_subtraction(self._h, left_pv, right_pv), "add_boolean_subtraction")
+
+    def add_logical_volume(self, shape):
+        return _check(_lib.vg_geom_add_logical_volume(self._h, shape), "add_logical_volume")
+
+    def place(self, lv, trans=ZERO_TRANS, rot=IDENTITY_ROT):
+        t, tp = _darr(trans, 3)
+        r, rp = _darr(rot, 9)
+        return _check(_lib.vg_geom_place(self._h, lv, tp, rp), "place")
+
+    def place_daughter(self, mother_lv, lv, trans=ZERO_TRANS, rot=IDENTITY_ROT):
+        t, tp = _darr(trans, 3)
+        r, rp = _darr(rot, 9)
+        return _check(_lib.vg_geom_place_daughter(self._h, mother_lv, lv, tp, rp), "place_daughter")
+
+    def set_world(self, pv):
+        _check(_lib.vg_geom_set_world(self._h, pv), "set_world")
+
+    def build(self):
+        """Host-side flattening only (BVHs, NavIndex table); needs no GPU."""
+        _check(_lib.vg_geom_build(self._h), "build")
+
+    def close(self):
+        _check(_lib.vg_geom_close(self._h), "close")
+        self.closed = True
+
+    # ---------------------------------------------------------------- introspection
+    def info(self):
+        a, b, c, d = (ctypes.c_int32() for _ in range(4))
+        e, f = ctypes.c_size_t(), ctypes.c_size_t()
+        _check(_lib.vg_geom_info(self._h, *(ctypes.byref(v) for v in (a, b, c, d, e, f))), "info")
+        return dict(n_shapes=a.value, n_lv=b.value, n_pv=c.value, max_depth=d.value, nav_words=e.value,
+                    device_bytes=f.value)
+
+    def nav_table(self):
+        n = self.info()["nav_words"]
+        out = np.zeros(n, dtype=np.uint32)
+        _check(_lib.vg_geom_nav_table(self._h, out.ctypes.data_as(_c_vp), n), "nav_table")
+        return out
+
+    def bvh(self, lv):
+        nn, npr, dep = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        _check(_lib.vg_geom_bvh_sizes(self._h, lv, ctypes.byref(nn), ctypes.byref(npr), ctypes.byref(dep)),
+               "bvh_sizes")
+        prim = np.zeros(npr.value, np.int32)
+        off = np.zeros(nn.value, np.int32)
+        nch = np.zeros(nn.value, np.int32)
+        nodes = np.zeros((nn.value, 6))
+        boxes = np.zeros((npr.value, 6))
+        _check(_lib.vg_geom_bvh_arrays(self._h, lv, *(a.ctypes.data_as(_c_vp) for a in (prim, off, nch, nodes, boxes))),
+               "bvh_arrays")
+        return dict(depth=dep.value, prim=prim, offset=off, nchild=nch, nodes=nodes, boxes=boxes)
+
+    def shape_extent(self, shape):
+        lo, lp = _darr(np.zeros(3))
+        hi, hp = _darr(np.zeros(3))
+        _check(_lib.vg_geom_shape_extent(self._h, shape, lp, hp), "shape_extent")
+        return lo, hi
+
+    # ---------------------------------------------------------------- SoA queries (CUDA tensors)
+    def inside(self, pv, x, y, z, out, flags=PREC_FP64):
+        _check(_lib.vg_placed_inside(self._h, pv, _ptr(x), _ptr(y), _ptr(z), x.numel(), _ptr(out), flags,
+                                     _stream()), "vg_placed_inside")
+
+    def contains(self, pv, x, y, z, out, flags=PREC_FP64):
+        _check(_lib.vg_placed_contains(self._h, pv, _ptr(x), _ptr(y), _ptr(z), x.numel(), _ptr(out), flags,
+                                       _stream()), "vg_placed_contains")
+
+    def distance_to_in(self, pv, x, y, z, dx, dy, dz, out, step_max=None, flags=PREC_FP64):
+        _check(_lib.vg_placed_distance_to_in(self._h, pv, _ptr(x), _ptr(y), _ptr(z), _ptr(dx), _ptr(dy), _ptr(dz),
+                                             _ptr(step_max), x.numel(), _ptr(out), flags, _stream()),
+               "vg_placed_distance_to_in")
+
+    def distance_to_out(self, pv, x, y, z, dx, dy, dz, out, step_max=None, flags=PREC_FP64):
+        _check(_lib.vg_placed_distance_to_out(self._h, pv, _ptr(x), _ptr(y), _ptr(z), _ptr(dx), _ptr(dy),
+                                              _ptr(dz), _ptr(step_max), x.numel(), _ptr(out), flags, _stream()),
+               "vg_placed_distance_to_out")
+
+    def safety_to_in(self, pv, x, y, z, out, flags=PREC_FP64):
+        _check(_lib.vg_placed_safety_to_in(self._h, pv, _ptr(x), _ptr(y), _ptr(z), x.numel(), _ptr(out), flags,
+                                           _stream()), "vg_placed_safety_to_in")
+
+    def safety_to_out(self, pv, x, y, z, out, flags=PREC_FP64):
+        _check(_lib.vg_placed_safety_to_out(self._h, pv, _ptr(x), _ptr(y), _ptr(z), x.numel(), _ptr(out), flags,
+                                            _stream()), "vg_placed_safety_to_out")
+
+    # ---------------------------------------------------------------- navigation (CUDA tensors)
+    def locate_point(self, x, y, z, out_states):
+        """GlobalLocator::LocateGlobalPoint(world, p, state, true); out_states: uint8 tensor (n*12)."""
+        _check(_lib.vg_nav_locate_point(self._h, _ptr(x), _ptr(y), _ptr(z), x.numel(), _ptr(out_states),
+                                        _stream()), "vg_nav_locate_point")
+
+    def compute_step_and_next_volume(self, x, y, z, dx, dy, dz, in_states, out_states, step, step_limit=None,
+                                     status=None, flags=PREC_FP64):
+        _check(_lib.vg_nav_compute_step_and_next_volume(
+            self._h, _ptr(x), _ptr(y), _ptr(z), _ptr(dx), _ptr(dy), _ptr(dz), _ptr(step_limit), _ptr(in_states),
+            _ptr(out_states), _ptr(step), _ptr(status), x.numel(), flags, _stream()),
+            "vg_nav_compute_step_and_next_volume")
+
+    def compute_step_and_next_volume_host(self, x, y, z, dx, dy, dz, in_states, out_states, step, step_limit=None,
+                                          status=None, flags=PREC_FP64, stream=None):
+        """Host-array variant (numpy arrays or pinned CPU tensors): copies in, steps, copies out."""
+        def hp(a):
+            if a is None:
+                return None
+            if hasattr(a, "data_ptr"):
+                return ctypes.c_void_p(a.data_ptr())
+            return a.ctypes.data_as(_c_vp)
+        _check(_lib.vg_nav_compute_step_and_next_volume_host(
+            self._h, hp(x), hp(y), hp(z), hp(dx), hp(dy), hp(dz), hp(step_limit), hp(in_states), hp(out_states),
+            hp(step), hp(status), len(x), flags, stream if stream is not None else _stream()),
+            "vg_nav_compute_step_and_next_volume_host")

@@ -1,0 +1,360 @@
+// extern "C" entry points declared in include/vecgeom_gb300.h.
+#include "../../include/vecgeom_gb300.h"
+#include "geom.h"
+#include "launch.h"
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+
+struct vg_geom {
+  vg::Geometry geo;
+  // device staging buffers of the host-pointer entry points (grown on demand, reused)
+  std::mutex staging_mutex;
+  void *staging       = nullptr;
+  size_t staging_size = 0;
+  ~vg_geom()
+  {
+    if (staging) cudaFree(staging);
+  }
+};
+
+namespace {
+thread_local std::string g_last_error;
+
+int fail(int code, std::string const &msg)
+{
+  g_last_error = msg;
+  return code;
+}
+int cuda_fail(cudaError_t e, const char *what)
+{
+  return fail(VG_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+bool built_ok(const vg_geom *g)
+{
+  if (!g) {
+    g_last_error = "null geometry handle";
+    return false;
+  }
+  if (!g->geo.built) {
+    g_last_error = "geometry is not built (call vg_geom_build or vg_geom_close first)";
+    return false;
+  }
+  return true;
+}
+bool closed_ok(const vg_geom *g)
+{
+  if (!g) {
+    g_last_error = "null geometry handle";
+    return false;
+  }
+  if (!g->geo.closed) {
+    g_last_error = "geometry is not closed (call vg_geom_close first)";
+    return false;
+  }
+  return true;
+}
+int32_t add_shape(vg_geom *g, int type, const double *p, int np)
+{
+  if (!g) return fail(VG_EINVAL, "null geometry handle");
+  std::string err;
+  const int32_t id = g->geo.add_shape(type, p, np, err);
+  return id < 0 ? fail(g->geo.closed ? VG_ESTATE : VG_EINVAL, err) : id;
+}
+
+enum Query { kQInside = 0, kQContains = 1, kQDistIn = 2, kQDistOut = 3, kQSafIn = 4, kQSafOut = 5 };
+
+int placed_query(const vg_geom *g, int32_t pv, int q, const double *x, const double *y, const double *z,
+                 const double *dx, const double *dy, const double *dz, size_t n, void *out, uint32_t flags,
+                 void *stream)
+{
+  if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
+  vg::Geometry const &geo = g->geo;
+  if (pv < 0 || pv >= (int32_t)geo.pvs.size()) return fail(VG_EINVAL, "invalid placed-volume id");
+  if (flags > VG_PREC_MIXED) return fail(VG_EINVAL, "invalid precision flags");
+  if (n > 0 && (!x || !y || !z || !out || ((q == kQDistIn || q == kQDistOut) && (!dx || !dy || !dz))))
+    return fail(VG_EINVAL, "null input/output array");
+  const int32_t shape = geo.lvs[geo.pvs[pv].lv].shape;
+  vg::QueryArgs a{x, y, z, dx, dy, dz, n, out};
+  const cudaError_t e = vg::launch_shape_query_fp64(geo.shapes[shape].type, geo.shape_rec(shape),
+                                                    geo.pvs[pv].xf.m, 1, q, a, (cudaStream_t)stream);
+  if (e == cudaErrorNotSupported) return fail(VG_EINVAL, "shape type not supported by this query path");
+  return e == cudaSuccess ? VG_OK : cuda_fail(e, "shape query launch");
+}
+} // namespace
+
+extern "C" {
+
+const char *vg_last_error(void) { return g_last_error.c_str(); }
+const char *vg_version(void) { return "vecgeom_gb300 0.1 (sm_103a)"; }
+
+int vg_geom_create(vg_geom **out)
+{
+  if (!out) return fail(VG_EINVAL, "null output pointer");
+  *out = new (std::nothrow) vg_geom();
+  return *out ? VG_OK : fail(VG_ENOMEM, "out of host memory");
+}
+void vg_geom_destroy(vg_geom *g) { delete g; }
+
+int32_t vg_geom_add_box(vg_geom *g, double dx, double dy, double dz)
+{
+  const double p[3] = {dx, dy, dz};
+  return add_shape(g, vg::kShapeBox, p, 3);
+}
+int32_t vg_geom_add_tube(vg_geom *g, double rmin, double rmax, double dz, double sphi, double dphi)
+{
+  const double p[5] = {rmin, rmax, dz, sphi, dphi};
+  return add_shape(g, vg::kShapeTube, p, 5);
+}
+int32_t vg_geom_add_cone(vg_geom *g, double rmin1, double rmax1, double rmin2, double rmax2, double dz, double sphi,
+                         double dphi)
+{
+  const double p[7] = {rmin1, rmax1, rmin2, rmax2, dz, sphi, dphi};
+  return add_shape(g, vg::kShapeCone, p, 7);
+}
+int32_t vg_geom_add_polycone(vg_geom *g, double sphi, double dphi, int32_t nz, const double *z, const double *rmin,
+                             const double *rmax)
+{
+  if (nz < 2 || nz > 1024 || !z || !rmin || !rmax) return fail(VG_EINVAL, "polycone needs 2..1024 z planes");
+  std::vector<double> p{sphi, dphi, (double)nz};
+  p.insert(p.end(), z, z + nz);
+  p.insert(p.end(), rmin, rmin + nz);
+  p.insert(p.end(), rmax, rmax + nz);
+  return add_shape(g, vg::kShapePolycone, p.data(), (int)p.size());
+}
+int32_t vg_geom_add_polyhedron(vg_geom *g, double phistart, double phidelta, int32_t nsides, int32_t nz,
+                               const double *z, const double *rmin, const double *rmax)
+{
+  if (nz < 2 || nz > 1024 || nsides < 1 || nsides > 1024 || !z || !rmin || !rmax)
+    return fail(VG_EINVAL, "polyhedron needs 2..1024 z planes and 1..1024 sides");
+  std::vector<double> p{phistart, phidelta, (double)nsides, (double)nz};
+  p.insert(p.end(), z, z + nz);
+  p.insert(p.end(), rmin, rmin + nz);
+  p.insert(p.end(), rmax, rmax + nz);
+  return add_shape(g, vg::kShapePolyhedron, p.data(), (int)p.size());
+}
+int32_t vg_geom_add_torus2(vg_geom *g, double rmin, double rmax, double rtor, double sphi, double dphi)
+{
+  const double p[5] = {rmin, rmax, rtor, sphi, dphi};
+  return add_shape(g, vg::kShapeTorus2, p, 5);
+}
+int32_t vg_geom_add_trd(vg_geom *g, double dx1, double dx2, double dy1, double dy2, double dz)
+{
+  const double p[5] = {dx1, dx2, dy1, dy2, dz};
+  return add_shape(g, vg::kShapeTrd, p, 5);
+}
+int32_t vg_geom_add_boolean_subtraction(vg_geom *g, int32_t left_pv, int32_t right_pv)
+{
+  const double p[2] = {(double)left_pv, (double)right_pv};
+  return add_shape(g, vg::kShapeBoolMinus, p, 2);
+}
+
+int32_t vg_geom_add_logical_volume(vg_geom *g, int32_t shape_id)
+{
+  if (!g) return fail(VG_EINVAL, "null geometry handle");
+  std::string err;
+  const int32_t id = g->geo.add_lv(shape_id, err);
+  return id < 0 ? fail(g->geo.closed ? VG_ESTATE : VG_EINVAL, err) : id;
+}
+int32_t vg_geom_place(vg_geom *g, int32_t lv, const double trans[3], const double rot[9])
+{
+  if (!g || !trans || !rot) return fail(VG_EINVAL, "null argument");
+  std::string err;
+  const int32_t id = g->geo.place(lv, trans, rot, -1, err);
+  return id < 0 ? fail(g->geo.closed ? VG_ESTATE : VG_EINVAL, err) : id;
+}
+int32_t vg_geom_place_daughter(vg_geom *g, int32_t mother_lv, int32_t lv, const double trans[3], const double rot[9])
+{
+  if (!g || !trans || !rot) return fail(VG_EINVAL, "null argument");
+  if (mother_lv < 0) return fail(VG_EINVAL, "invalid mother logical volume id");
+  std::string err;
+  const int32_t id = g->geo.place(lv, trans, rot, mother_lv, err);
+  return id < 0 ? fail(g->geo.closed ? VG_ESTATE : VG_EINVAL, err) : id;
+}
+int vg_geom_set_world(vg_geom *g, int32_t world_pv)
+{
+  if (!g) return fail(VG_EINVAL, "null geometry handle");
+  if (g->geo.closed) return fail(VG_ESTATE, "geometry is closed");
+  if (world_pv < 0 || world_pv >= (int32_t)g->geo.pvs.size()) return fail(VG_EINVAL, "invalid placed-volume id");
+  g->geo.world = world_pv;
+  return VG_OK;
+}
+int vg_geom_close(vg_geom *g)
+{
+  if (!g) return fail(VG_EINVAL, "null geometry handle");
+  std::string err;
+  if (g->geo.close(err) != 0) return fail(g->geo.closed ? VG_ESTATE : VG_ECUDA, err);
+  return VG_OK;
+}
+int vg_geom_build(vg_geom *g)
+{
+  if (!g) return fail(VG_EINVAL, "null geometry handle");
+  std::string err;
+  if (g->geo.build_host(err) != 0) return fail(g->geo.closed ? VG_ESTATE : VG_EINVAL, err);
+  return VG_OK;
+}
+int vg_geom_info(const vg_geom *g, int32_t *n_shapes, int32_t *n_lv, int32_t *n_pv, int32_t *max_depth,
+                 size_t *nav_table_words, size_t *device_bytes)
+{
+  if (!g) return fail(VG_EINVAL, "null geometry handle");
+  if (n_shapes) *n_shapes = (int32_t)g->geo.shapes.size();
+  if (n_lv) *n_lv = (int32_t)g->geo.lvs.size();
+  if (n_pv) *n_pv = (int32_t)g->geo.pvs.size();
+  if (max_depth) *max_depth = g->geo.max_depth;
+  if (nav_table_words) *nav_table_words = g->geo.nav_words;
+  if (device_bytes) *device_bytes = g->geo.arena_bytes;
+  return VG_OK;
+}
+int vg_geom_nav_table(const vg_geom *g, uint32_t *out, size_t words)
+{
+  if (!built_ok(g)) return VG_ESTATE;
+  if (!out || words < g->geo.nav_words) return fail(VG_EINVAL, "output buffer too small");
+  std::memcpy(out, g->geo.nav.data(), g->geo.nav_words * sizeof(uint32_t));
+  return VG_OK;
+}
+int vg_geom_bvh_sizes(const vg_geom *g, int32_t lv, int32_t *n_nodes, int32_t *n_prims, int32_t *depth)
+{
+  if (!built_ok(g)) return VG_ESTATE;
+  if (lv < 0 || lv >= (int32_t)g->geo.lvs.size() || g->geo.lv_bvh[lv] < 0)
+    return fail(VG_EINVAL, "logical volume has no BVH");
+  vg::HostBVH const &b = g->geo.bvhs[g->geo.lv_bvh[lv]];
+  *n_nodes = (int32_t)b.nchild.size();
+  *n_prims = (int32_t)b.prim.size();
+  *depth   = b.depth;
+  return VG_OK;
+}
+int vg_geom_bvh_arrays(const vg_geom *g, int32_t lv, int32_t *prim_id, int32_t *offset, int32_t *nchild,
+                       double *node_box6, double *prim_box6)
+{
+  if (!built_ok(g)) return VG_ESTATE;
+  if (lv < 0 || lv >= (int32_t)g->geo.lvs.size() || g->geo.lv_bvh[lv] < 0)
+    return fail(VG_EINVAL, "logical volume has no BVH");
+  vg::HostBVH const &b = g->geo.bvhs[g->geo.lv_bvh[lv]];
+  std::memcpy(prim_id, b.prim.data(), b.prim.size() * sizeof(int32_t));
+  std::memcpy(offset, b.offset.data(), b.offset.size() * sizeof(int32_t));
+  std::memcpy(nchild, b.nchild.data(), b.nchild.size() * sizeof(int32_t));
+  std::memcpy(node_box6, b.node_box.data(), b.node_box.size() * sizeof(double));
+  std::memcpy(prim_box6, b.prim_box.data(), b.prim_box.size() * sizeof(double));
+  return VG_OK;
+}
+int vg_geom_shape_extent(const vg_geom *g, int32_t shape_id, double lo[3], double hi[3])
+{
+  if (!g || shape_id < 0 || shape_id >= (int32_t)g->geo.shapes.size()) return fail(VG_EINVAL, "invalid shape id");
+  for (int k = 0; k < 3; ++k) lo[k] = g->geo.shapes[shape_id].lo[k], hi[k] = g->geo.shapes[shape_id].hi[k];
+  return VG_OK;
+}
+
+int vg_placed_inside(const vg_geom *g, int32_t pv, const double *x, const double *y, const double *z, size_t n,
+                     int32_t *out, uint32_t flags, void *stream)
+{
+  return placed_query(g, pv, kQInside, x, y, z, nullptr, nullptr, nullptr, n, out, flags, stream);
+}
+int vg_placed_contains(const vg_geom *g, int32_t pv, const double *x, const double *y, const double *z, size_t n,
+                       uint8_t *out, uint32_t flags, void *stream)
+{
+  return placed_query(g, pv, kQContains, x, y, z, nullptr, nullptr, nullptr, n, out, flags, stream);
+}
+int vg_placed_distance_to_in(const vg_geom *g, int32_t pv, const double *x, const double *y, const double *z,
+                             const double *dx, const double *dy, const double *dz, const double *step_max, size_t n,
+                             double *out, uint32_t flags, void *stream)
+{
+  (void)step_max;
+  return placed_query(g, pv, kQDistIn, x, y, z, dx, dy, dz, n, out, flags, stream);
+}
+int vg_placed_distance_to_out(const vg_geom *g, int32_t pv, const double *x, const double *y, const double *z,
+                              const double *dx, const double *dy, const double *dz, const double *step_max, size_t n,
+                              double *out, uint32_t flags, void *stream)
+{
+  (void)step_max;
+  return placed_query(g, pv, kQDistOut, x, y, z, dx, dy, dz, n, out, flags, stream);
+}
+int vg_placed_safety_to_in(const vg_geom *g, int32_t pv, const double *x, const double *y, const double *z, size_t n,
+                           double *out, uint32_t flags, void *stream)
+{
+  return placed_query(g, pv, kQSafIn, x, y, z, nullptr, nullptr, nullptr, n, out, flags, stream);
+}
+int vg_placed_safety_to_out(const vg_geom *g, int32_t pv, const double *x, const double *y, const double *z, size_t n,
+                            double *out, uint32_t flags, void *stream)
+{
+  return placed_query(g, pv, kQSafOut, x, y, z, nullptr, nullptr, nullptr, n, out, flags, stream);
+}
+
+int vg_nav_locate_point(const vg_geom *g, const double *x, const double *y, const double *z, size_t n,
+                        vg_navstate *out, void *stream)
+{
+  if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
+  if (g->geo.world < 0) return fail(VG_ESTATE, "geometry has no world volume");
+  if (n > 0 && (!x || !y || !z || !out)) return fail(VG_EINVAL, "null input/output array");
+  const cudaError_t e = vg::launch_locate_fp64(g->geo.dev, x, y, z, n, reinterpret_cast<vg::NavState *>(out),
+                                               (cudaStream_t)stream);
+  return e == cudaSuccess ? VG_OK : cuda_fail(e, "locate launch");
+}
+
+int vg_nav_compute_step_and_next_volume(const vg_geom *g, const double *x, const double *y, const double *z,
+                                        const double *dx, const double *dy, const double *dz,
+                                        const double *step_limit, const vg_navstate *in, vg_navstate *out,
+                                        double *step, int32_t *status, size_t n, uint32_t flags, void *stream)
+{
+  if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
+  if (g->geo.world < 0) return fail(VG_ESTATE, "geometry has no world volume");
+  if (flags > VG_PREC_MIXED) return fail(VG_EINVAL, "invalid precision flags");
+  if (n > 0 && (!x || !y || !z || !dx || !dy || !dz || !in || !out || !step))
+    return fail(VG_EINVAL, "null input/output array");
+  vg::StepArgs a{x,   y,   z,   dx,  dy,  dz, step_limit, reinterpret_cast<const vg::NavState *>(in),
+                 reinterpret_cast<vg::NavState *>(out), step, status, nullptr, n};
+  const cudaError_t e = vg::launch_step(g->geo.dev, a, flags, (cudaStream_t)stream);
+  return e == cudaSuccess ? VG_OK : cuda_fail(e, "navigation step launch");
+}
+
+int vg_nav_compute_step_and_next_volume_host(vg_geom *g, const double *x, const double *y, const double *z,
+                                             const double *dx, const double *dy, const double *dz,
+                                             const double *step_limit, const vg_navstate *in, vg_navstate *out,
+                                             double *step, int32_t *status, size_t n, uint32_t flags, void *stream)
+{
+  if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
+  if (n == 0) return VG_OK;
+  if (!x || !y || !z || !dx || !dy || !dz || !in || !out || !step) return fail(VG_EINVAL, "null input/output array");
+  std::lock_guard<std::mutex> lock(g->staging_mutex);
+  const size_t nd = n * sizeof(double), ns = n * sizeof(vg_navstate), ni = n * sizeof(int32_t);
+  const size_t need = 8 * nd + 2 * ns + ni + 16 * 256;
+  if (g->staging_size < need) {
+    if (g->staging) cudaFree(g->staging);
+    g->staging      = nullptr;
+    g->staging_size = 0;
+    const cudaError_t e = cudaMalloc(&g->staging, need);
+    if (e != cudaSuccess) return cuda_fail(e, "staging allocation");
+    g->staging_size = need;
+  }
+  unsigned char *p = static_cast<unsigned char *>(g->staging);
+  size_t off       = 0;
+  auto take = [&](size_t bytes) {
+    void *q = p + off;
+    off += (bytes + 255) & ~size_t(255);
+    return q;
+  };
+  double *d[8];
+  for (int k = 0; k < 8; ++k) d[k] = static_cast<double *>(take(nd));
+  vg_navstate *din  = static_cast<vg_navstate *>(take(ns));
+  vg_navstate *dout = static_cast<vg_navstate *>(take(ns));
+  int32_t *dst      = static_cast<int32_t *>(take(ni));
+  cudaStream_t s    = (cudaStream_t)stream;
+  const double *src[7] = {x, y, z, dx, dy, dz, step_limit};
+  cudaError_t e        = cudaSuccess;
+  for (int k = 0; k < 7 && e == cudaSuccess; ++k)
+    if (src[k]) e = cudaMemcpyAsync(d[k], src[k], nd, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(din, in, ns, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "host-to-device copy");
+  vg::StepArgs a{d[0], d[1], d[2], d[3], d[4], d[5], step_limit ? d[6] : nullptr,
+                 reinterpret_cast<const vg::NavState *>(din), reinterpret_cast<vg::NavState *>(dout), d[7],
+                 status ? dst : nullptr, nullptr, n};
+  e = vg::launch_step(g->geo.dev, a, flags, s);
+  if (e != cudaSuccess) return cuda_fail(e, "navigation step launch");
+  e = cudaMemcpyAsync(out, dout, ns, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(step, d[7], nd, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && status) e = cudaMemcpyAsync(status, dst, ni, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e == cudaSuccess ? VG_OK : cuda_fail(e, "device-to-host copy");
+}
+
+} // extern "C"

@@ -1,0 +1,707 @@
+// Host geometry builder (see geom.h). Compiled with -ffp-contract=off so that the
+// precomputed records, daughter boxes and cached global matrices round exactly as the
+// reference's host code does.
+#include "geom.h"
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <cuda_runtime.h>
+#include <numeric>
+#include <utility>
+
+namespace vg {
+
+// ---------------------------------------------------------------- transformations
+HostXform HostXform::Identity()
+{
+  HostXform x;
+  for (int i = 0; i < 3; ++i) x.m.t[i] = 0.;
+  for (int i = 0; i < 9; ++i) x.m.r[i] = (i % 4 == 0) ? 1. : 0.;
+  return x;
+}
+
+// Transformation3D(tx,ty,tz,r0..r8) + SetProperties (source/Transformation3D.cpp:54-62,118-126,174-185)
+HostXform HostXform::FromArrays(const double *t, const double *r)
+{
+  HostXform x;
+  std::memcpy(x.m.t, t, sizeof(x.m.t));
+  std::memcpy(x.m.r, r, sizeof(x.m.r));
+  x.has_trans = std::fabs(t[0]) > kTolerance || std::fabs(t[1]) > kTolerance || std::fabs(t[2]) > kTolerance;
+  int code    = 0;
+  for (int i = 0; i < 9; ++i) code |= (std::fabs(r[i]) > kTolerance) << i;
+  x.has_rot  = !(code == 0x111 && r[0] == 1. && r[4] == 1. && r[8] == 1.);
+  x.identity = !x.has_trans && !x.has_rot;
+  return x;
+}
+
+// Transformation3D::MultiplyFromRight (Transformation3D.h:878-942): this <- this * rhs
+void HostXform::MultiplyFromRight(HostXform const &rhs)
+{
+  if (rhs.identity) return;
+  identity = false;
+  double *t = m.t, *r = m.r;
+  const double *rt = rhs.m.t, *rr = rhs.m.r;
+  if (rhs.has_trans) {
+    has_trans = true;
+    for (int row = 0; row < 3; ++row) {
+      t[row] += r[3 * row] * rt[0];
+      t[row] += r[3 * row + 1] * rt[1];
+      t[row] += r[3 * row + 2] * rt[2];
+    }
+  }
+  if (rhs.has_rot) {
+    has_rot = true;
+    for (int row = 0; row < 3; ++row) {
+      const double a = r[3 * row], b = r[3 * row + 1], c = r[3 * row + 2];
+      for (int col = 0; col < 3; ++col) r[3 * row + col] = a * rr[col];
+      for (int col = 0; col < 3; ++col) r[3 * row + col] += b * rr[3 + col];
+      for (int col = 0; col < 3; ++col) r[3 * row + col] += c * rr[6 + col];
+    }
+  }
+}
+
+// InverseTransform (Transformation3D.h:797-826): master = t + R local
+void HostXform::InverseTransform(const double *l, double *out) const
+{
+  for (int row = 0; row < 3; ++row) {
+    double v = m.t[row];
+    v += l[0] * m.r[3 * row];
+    v += l[1] * m.r[3 * row + 1];
+    v += l[2] * m.r[3 * row + 2];
+    out[row] = v;
+  }
+}
+
+// ---------------------------------------------------------------- shape records
+namespace {
+template <class T>
+void pack(HostShape &s, T const &rec)
+{
+  static_assert(sizeof(T) % sizeof(double) == 0, "records are double-sized");
+  s.rec.resize(sizeof(T) / sizeof(double));
+  std::memcpy(s.rec.data(), &rec, sizeof(T));
+}
+
+// Wedge constructor (source/Wedge_Evolution.cpp)
+WedgeRec make_wedge(double dphi, double sphi)
+{
+  WedgeRec w;
+  w.dphi = dphi;
+  w.a1x  = std::cos(sphi);
+  w.a1y  = std::sin(sphi);
+  w.a2x  = std::cos(sphi + dphi);
+  w.a2y  = std::sin(sphi + dphi);
+  w.n1x  = -std::sin(sphi);
+  w.n1y  = std::cos(sphi);
+  w.n2x  = std::sin(sphi + dphi);
+  w.n2y  = -std::cos(sphi + dphi);
+  return w;
+}
+bool wedge_contains(WedgeRec const &w, double x, double y)
+{
+  const double startCheck = (-x * w.a1y + y * w.a1x);
+  const double endCheck   = (-w.a2x * y + w.a2y * x);
+  bool out                = startCheck < 0.;
+  out                     = (w.dphi < kPi) ? (out || endCheck < 0.) : (out && endCheck < 0.);
+  return !out;
+}
+
+// Extent of a phi section of radii [rin, rout] (UnplacedTube.cpp:214-266, UnplacedCone.cpp:149-211)
+void phi_section_extent(WedgeRec const &w, double sphi, double dphi, double rin, double rout, double halfz, double *lo,
+                        double *hi)
+{
+  lo[0] = -rout, lo[1] = -rout, lo[2] = -halfz;
+  hi[0] = rout, hi[1] = rout, hi[2] = halfz;
+  if (dphi == kTwoPi) return;
+  const double Rin     = 0.5 * (rout + rin);
+  const bool phi0out   = !wedge_contains(w, Rin, 0);
+  const bool phi90out  = !wedge_contains(w, 0, Rin);
+  const bool phi180out = !wedge_contains(w, -Rin, 0);
+  const bool phi270out = !wedge_contains(w, 0, -Rin);
+  if (!(phi0out || phi90out || phi180out || phi270out)) return;
+  const double Cx = rout * std::cos(sphi), Dx = rout * std::cos(sphi + dphi);
+  const double Cy = rout * std::sin(sphi), Dy = rout * std::sin(sphi + dphi);
+  auto mx = [](double a, double b) { return a > b ? a : b; };
+  auto mn = [](double a, double b) { return a < b ? a : b; };
+  if (phi0out) hi[0] = mx(Cx, Dx);
+  if (phi90out) hi[1] = mx(Cy, Dy);
+  if (phi180out) lo[0] = mn(Cx, Dx);
+  if (phi270out) lo[1] = mn(Cy, Dy);
+  if (dphi >= kPi) return;
+  const double Ax = rin * std::cos(sphi), Bx = rin * std::cos(sphi + dphi);
+  const double Ay = rin * std::sin(sphi), By = rin * std::sin(sphi + dphi);
+  double t;
+  t     = mx(Ax, Bx);
+  hi[0] = t > hi[0] ? t : hi[0];
+  t     = mx(Ay, By);
+  hi[1] = t > hi[1] ? t : hi[1];
+  t     = mn(Ax, Bx);
+  lo[0] = t < lo[0] ? t : lo[0];
+  t     = mn(Ay, By);
+  lo[1] = t < lo[1] ? t : lo[1];
+}
+double nonzero(double x) { return x + std::copysign(1.0e-30, x); }
+} // namespace
+
+void make_box(const double *p, HostShape &s)
+{
+  BoxRec b{p[0], p[1], p[2]};
+  s.type = kShapeBox;
+  pack(s, b);
+  for (int i = 0; i < 3; ++i) s.lo[i] = -p[i], s.hi[i] = p[i];
+}
+
+// TubeStruct constructor + CalculateCached (VecGeom/volumes/TubeStruct.h:41-179)
+void make_tube(const double *p, HostShape &s)
+{
+  TubeRec t;
+  t.rmin      = p[0] < 0.0 ? 0.0 : p[0];
+  t.rmax      = p[1];
+  t.z         = p[2];
+  t.sphi      = p[3];
+  t.dphi      = p[4];
+  t.tolIz     = t.z - kHalfTolerance;
+  t.tolOz     = t.z + kHalfTolerance;
+  t.rmin2     = t.rmin * t.rmin;
+  t.tolOrmin  = t.rmin - kHalfTolerance;
+  t.tolIrmin  = t.rmin + kHalfTolerance;
+  t.tolOrmin2 = t.tolOrmin * t.tolOrmin;
+  t.tolIrmin2 = t.tolIrmin * t.tolIrmin;
+  t.rmax2     = t.rmax * t.rmax;
+  t.tolOrmax  = t.rmax + kHalfTolerance;
+  t.tolIrmax  = t.rmax - kHalfTolerance;
+  t.tolOrmax2 = t.tolOrmax * t.tolOrmax;
+  t.tolIrmax2 = t.tolIrmax * t.tolIrmax;
+  t.a1x       = std::cos(t.sphi);
+  t.a1y       = std::sin(t.sphi);
+  t.a2x       = std::cos(t.sphi + t.dphi);
+  t.a2y       = std::sin(t.sphi + t.dphi);
+  t.maxVal    = t.rmax > t.z ? t.rmax : t.z;
+  t.w         = make_wedge(p[4], p[3]);
+  s.type      = kShapeTube;
+  pack(s, t);
+  phi_section_extent(t.w, t.sphi, t.dphi, t.rmin, t.rmax, t.z, s.lo, s.hi);
+}
+
+// ConeStruct constructor, SetAndCheck{D,S}PhiAngle and CalculateCached (ConeStruct.h:85-336)
+void make_cone(const double *p, HostShape &s)
+{
+  ConeRec c;
+  c.rmin1  = p[0] < 0.0 ? 0.0 : p[0];
+  c.rmax1  = p[1];
+  c.rmin2  = p[2] < 0.0 ? 0.0 : p[2];
+  c.rmax2  = p[3];
+  c.dz     = p[4];
+  c.sphi   = p[5];
+  c.dphi   = p[6];
+  c.frmin1 = p[0], c.frmax1 = p[1], c.frmin2 = p[2], c.frmax2 = p[3];
+  c.w      = make_wedge(p[6], p[5]); // the wedge keeps its construction angles
+  const double dPhi = p[6], sPhi = p[5];
+  if (dPhi >= kTwoPi - 0.5 * kAngTolerance) {
+    c.dphi = kTwoPi;
+    c.sphi = 0;
+  } else if (dPhi > 0) {
+    c.dphi = dPhi;
+  }
+  c.w.dphi = c.dphi;
+  c.sphi   = sPhi < 0 ? kTwoPi - std::fmod(std::fabs(sPhi), kTwoPi) : std::fmod(sPhi, kTwoPi);
+  if (c.sphi + c.dphi > kTwoPi) c.sphi -= kTwoPi;
+  c.a1x = std::cos(c.sphi);
+  c.a1y = std::sin(c.sphi);
+  c.a2x = std::cos(c.sphi + c.dphi);
+  c.a2y = std::sin(c.sphi + c.dphi);
+
+  c.origRmax1 = c.rmax1;
+  c.origRmax2 = c.rmax2;
+  if (c.rmin1 == c.rmax1) c.rmax1 += kConeTolerance;
+  if (c.rmin2 == c.rmax2) c.rmax2 += kConeTolerance;
+  c.sqRmin1    = c.rmin1 * c.rmin1;
+  c.sqRmax1    = c.rmax1 * c.rmax1;
+  c.sqRmin2    = c.rmin2 * c.rmin2;
+  c.sqRmax2    = c.rmax2 * c.rmax2;
+  c.tanRMin    = (c.rmin2 - c.rmin1) * 0.5 / c.dz;
+  c.secRMin    = std::sqrt(1.0 + c.tanRMin * c.tanRMin);
+  c.invSecRMin = 1. / nonzero(c.secRMin);
+  c.tanRMax    = (c.rmax2 - c.rmax1) * 0.5 / c.dz;
+  c.secRMax    = std::sqrt(1.0 + c.tanRMax * c.tanRMax);
+  c.invSecRMax = 1. / nonzero(c.secRMax);
+  c.innerSlope  = -(c.rmin1 - c.rmin2) / (2. * c.dz);
+  c.outerSlope  = -(c.rmax1 - c.rmax2) / (2. * c.dz);
+  c.innerOffset = c.rmin2 - c.innerSlope * c.dz;
+  c.outerOffset = c.rmax2 - c.outerSlope * c.dz;
+  c.innerTol    = kConeTolerance * c.secRMin;
+  c.outerTol    = kConeTolerance * c.secRMax;
+  if (c.rmin2 > c.rmin1) {
+    c.innerApex    = 2 * c.dz * c.rmin1 / (c.rmin2 - c.rmin1);
+    c.tanInnerApex = c.rmin2 / (2 * c.dz + c.innerApex);
+  } else {
+    c.innerApex    = 2 * c.dz * c.rmin2 / nonzero(c.rmin1 - c.rmin2);
+    c.tanInnerApex = c.rmin1 / (2 * c.dz + c.innerApex);
+  }
+  if (c.rmin1 == 0. || c.rmin2 == 0.) c.innerApex = 0.;
+  if (c.rmin1 == 0.) c.tanInnerApex = c.rmin2 / (2 * c.dz);
+  if (c.rmin2 == 0.) c.tanInnerApex = c.rmin1 / (2 * c.dz);
+  if (c.rmax2 > c.rmax1) {
+    c.outerApex    = 2 * c.dz * c.rmax1 / (c.rmax2 - c.rmax1);
+    c.tanOuterApex = c.rmax2 / (2 * c.dz + c.outerApex);
+  } else {
+    c.outerApex    = 2 * c.dz * c.rmax2 / nonzero(c.rmax1 - c.rmax2);
+    c.tanOuterApex = c.rmax1 / (2 * c.dz + c.outerApex);
+  }
+  if (c.rmax1 == 0. || c.rmax2 == 0.) c.outerApex = 0.;
+  if (c.rmax1 == 0.) c.tanOuterApex = c.rmax2 / (2 * c.dz);
+  if (c.rmax2 == 0.) c.tanOuterApex = c.rmax1 / (2 * c.dz);
+  c.zNormInner = c.tanRMin / nonzero(c.secRMin);
+  c.zNormOuter = -c.tanRMax / nonzero(c.secRMax);
+  c.tolIz      = c.dz - kHalfTolerance;
+  c.tolOz      = c.dz + kHalfTolerance;
+  s.type       = kShapeCone;
+  pack(s, c);
+  const double rout = c.frmax1 > c.frmax2 ? c.frmax1 : c.frmax2;
+  const double rin  = c.frmin1 > c.frmin2 ? c.frmin2 : c.frmin1;
+  phi_section_extent(c.w, c.sphi, c.dphi, rin, rout, c.dz, s.lo, s.hi);
+}
+
+// ---------------------------------------------------------------- registry
+Geometry::~Geometry()
+{
+  if (arena) cudaFree(arena);
+}
+
+int32_t Geometry::add_shape(int32_t type, const double *p, int np, std::string &err)
+{
+  if (closed) {
+    err = "geometry is closed";
+    return -1;
+  }
+  HostShape s;
+  auto need = [&](int k) {
+    if (np < k) {
+      err = "too few shape parameters";
+      return false;
+    }
+    return true;
+  };
+  switch (type) {
+  case kShapeBox:
+    if (!need(3)) return -1;
+    make_box(p, s);
+    break;
+  case kShapeTube:
+    if (!need(5)) return -1;
+    make_tube(p, s);
+    break;
+  case kShapeCone:
+    if (!need(7)) return -1;
+    make_cone(p, s);
+    break;
+  default:
+    err = "unknown shape type " + std::to_string(type);
+    return -1;
+  }
+  shapes.push_back(std::move(s));
+  return (int32_t)shapes.size() - 1;
+}
+
+int32_t Geometry::add_lv(int32_t shape, std::string &err)
+{
+  if (closed || shape < 0 || shape >= (int32_t)shapes.size()) {
+    err = closed ? "geometry is closed" : "invalid shape id";
+    return -1;
+  }
+  lvs.push_back(HostLV{shape, {}});
+  return (int32_t)lvs.size() - 1;
+}
+
+// LogicalVolume::Place / PlaceDaughter (source/LogicalVolume.cpp:125-155): ids in creation order.
+int32_t Geometry::place(int32_t lv, const double *t, const double *r, int32_t mother_lv, std::string &err)
+{
+  if (closed || lv < 0 || lv >= (int32_t)lvs.size() || mother_lv >= (int32_t)lvs.size()) {
+    err = closed ? "geometry is closed" : "invalid logical volume id";
+    return -1;
+  }
+  if (lvs[lv].daughters.size() >= 65535 || (mother_lv >= 0 && lvs[mother_lv].daughters.size() >= 65534)) {
+    err = "more than 65535 daughters in one logical volume";
+    return -1;
+  }
+  HostPV pv{lv, HostXform::FromArrays(t, r), -1};
+  pvs.push_back(pv);
+  const int32_t id = (int32_t)pvs.size() - 1;
+  if (mother_lv >= 0) {
+    pvs[id].child = (int32_t)lvs[mother_lv].daughters.size();
+    lvs[mother_lv].daughters.push_back(id);
+  }
+  return id;
+}
+
+// ABBoxManager::ComputeABBox (source/ABBoxManager.cpp:109-140): the 8 corners of the
+// shape's extent mapped to the mother frame, widened by 1e-3 mm.
+void Geometry::daughter_box(int32_t pvid, double *box) const
+{
+  HostPV const &pv    = pvs[pvid];
+  HostShape const &sh = shapes[lvs[pv.lv].shape];
+  const double delta[3] = {sh.hi[0] - sh.lo[0], sh.hi[1] - sh.lo[1], sh.hi[2] - sh.lo[2]};
+  double mn[3] = {kInfLength, kInfLength, kInfLength}, mx[3] = {-kInfLength, -kInfLength, -kInfLength};
+  for (int x = 0; x <= 1; ++x)
+    for (int y = 0; y <= 1; ++y)
+      for (int z = 0; z <= 1; ++z) {
+        const double corner[3] = {sh.lo[0] + x * delta[0], sh.lo[1] + y * delta[1], sh.lo[2] + z * delta[2]};
+        double tc[3];
+        pv.xf.InverseTransform(corner, tc);
+        for (int k = 0; k < 3; ++k) {
+          mn[k] = std::min(mn[k], tc[k]);
+          mx[k] = std::max(mx[k], tc[k]);
+        }
+      }
+  for (int k = 0; k < 3; ++k) box[k] = mn[k] - 1E-3, box[3 + k] = mx[k] + 1E-3;
+}
+
+// ---------------------------------------------------------------- BVH (source/BVH.cpp:48-385)
+namespace {
+struct Box6 {
+  double lo[3], hi[3];
+};
+inline double surface_area(Box6 const &b)
+{
+  const double e0 = b.hi[0] - b.lo[0], e1 = b.hi[1] - b.lo[1], e2 = b.hi[2] - b.lo[2];
+  return 2. * (e0 * e1 + e1 * e2 + e2 * e0);
+}
+inline Box6 merge(Box6 const &a, Box6 const &b)
+{
+  Box6 r;
+  for (int k = 0; k < 3; ++k) {
+    r.lo[k] = a.lo[k] < b.lo[k] ? a.lo[k] : b.lo[k];
+    r.hi[k] = a.hi[k] > b.hi[k] ? a.hi[k] : b.hi[k];
+  }
+  return r;
+}
+// Sort key of a primitive: its centroid pushed 1% further from its lower corner; keys are
+// compared lexicographically starting at the sort axis (BVH.cpp:194-202, 261-268).
+struct SahKey {
+  double k[3];
+};
+inline bool key_less(SahKey const &a, SahKey const &b, int ax)
+{
+  const int a1 = (ax + 1) % 3, a2 = (ax + 2) % 3;
+  return a.k[ax] < b.k[ax] ||
+         (a.k[ax] == b.k[ax] && (a.k[a1] < b.k[a1] || (a.k[a1] == b.k[a1] && a.k[a2] < b.k[a2])));
+}
+
+// Surface-area-heuristic split of prims[b, e); returns the pivot (BVH.cpp:254-306).
+int *sah_split(std::vector<Box6> const &boxes, std::vector<SahKey> const &keys, int *b, int *e)
+{
+  const long n  = e - b;
+  double best   = (double)n;
+  int bestAxis  = -1;
+  int bestObj   = -1;
+  std::vector<double> leftArea(n), rightArea(n);
+  for (int axis = 0; axis < 3; ++axis) {
+    std::sort(b, e, [&](int x, int y) { return key_less(keys[x], keys[y], axis); });
+    Box6 acc     = boxes[b[0]];
+    leftArea[0]  = 0.;
+    for (long i = 1; i < n; ++i) {
+      leftArea[i] = surface_area(acc);
+      acc         = merge(acc, boxes[b[i]]);
+    }
+    Box6 racc = boxes[b[n - 1]];
+    for (long i = n - 1; i >= 0; --i) {
+      racc         = merge(racc, boxes[b[i]]);
+      rightArea[i] = surface_area(racc);
+    }
+    const double total = rightArea[0];
+    for (long i = 0; i < n; ++i) {
+      const double metric = (leftArea[i] / total) * i + (rightArea[i] / total) * (n - i) + 0.1 * std::labs(n / 2 - i / n);
+      if (metric < best) {
+        best     = metric;
+        bestAxis = axis;
+        bestObj  = b[i];
+      }
+    }
+  }
+  if (bestAxis < 0) return e;
+  SahKey const pivotKey = keys[bestObj];
+  return std::partition(b, e, [&](size_t x) { return key_less(keys[(int)x], pivotKey, bestAxis); });
+}
+} // namespace
+
+void Geometry::build_bvh(int32_t lvid, HostBVH &out) const
+{
+  HostLV const &lv = lvs[lvid];
+  const int n      = (int)lv.daughters.size();
+  std::vector<Box6> boxes(n);
+  std::vector<SahKey> keys(n);
+  out.prim_box.resize(6 * (size_t)n);
+  for (int i = 0; i < n; ++i) {
+    daughter_box(lv.daughters[i], &out.prim_box[6 * (size_t)i]);
+    std::memcpy(boxes[i].lo, &out.prim_box[6 * (size_t)i], 3 * sizeof(double));
+    std::memcpy(boxes[i].hi, &out.prim_box[6 * (size_t)i + 3], 3 * sizeof(double));
+    for (int k = 0; k < 3; ++k) {
+      const double c = 0.5 * (boxes[i].hi[k] + boxes[i].lo[k]);
+      keys[i].k[k]   = c + 0.01 * (c - boxes[i].lo[k]);
+    }
+  }
+  const int half = n / 2;
+  out.depth      = std::min(half > 0 ? std::max(0, (int)std::log2(half)) : 0, 32);
+  const int nn   = (2 << out.depth) - 1;
+  out.prim.resize(n);
+  std::iota(out.prim.begin(), out.prim.end(), 0);
+  out.nchild.assign(nn, 0);
+  out.offset.assign(nn, -1);
+  out.node_box.assign(6 * (size_t)nn, 0.);
+  // Work list of (node, first, last) ranges; the two halves of a split are disjoint, so the
+  // processing order does not change the result.
+  struct Item {
+    int node, first, last;
+  };
+  std::vector<Item> work{{0, 0, n}};
+  while (!work.empty()) {
+    const Item it = work.back();
+    work.pop_back();
+    if (it.node >= nn) continue;
+    out.nchild[it.node] = it.last - it.first;
+    out.offset[it.node] = it.first;
+    if (it.first == it.last) continue;
+    Box6 nb = boxes[out.prim[it.first]];
+    for (int i = it.first + 1; i < it.last; ++i) nb = merge(nb, boxes[out.prim[i]]);
+    std::memcpy(&out.node_box[6 * (size_t)it.node], nb.lo, 3 * sizeof(double));
+    std::memcpy(&out.node_box[6 * (size_t)it.node + 3], nb.hi, 3 * sizeof(double));
+    if (it.last - it.first == 1) continue;
+    int *base  = out.prim.data();
+    int *pivot = sah_split(boxes, keys, base + it.first, base + it.last);
+    const int p = (int)(pivot - base);
+    work.push_back({2 * it.node + 2, p, it.last});
+    work.push_back({2 * it.node + 1, it.first, p});
+  }
+  for (int id = 0; id < nn / 2; ++id)
+    if (out.nchild[id] > 8 && out.nchild[id] == out.nchild[2 * id + 1] + out.nchild[2 * id + 2]) out.nchild[id] = -1;
+}
+
+// ---------------------------------------------------------------- NavIndex table
+// Layout per touchable (source/NavIndexTable.cpp:9-84): [mother, placed-volume id,
+// (level u8, has-matrix u8, ndaughters u16), daughter indices..., pad to even], then the
+// node's global matrix (3 translation + 9 rotation doubles) 8-byte aligned. Nodes are in
+// depth-first pre-order; index 0 is the "outside" state.
+void Geometry::build_nav_table()
+{
+  struct Frame {
+    int32_t pv;
+    int level;
+    uint32_t mother;
+    int dind;
+    HostXform mat;
+  };
+  // Pass 1: size (matches the reference's two-pass allocation: 4 bytes + nodes, +1 word).
+  size_t bytes = sizeof(uint32_t);
+  {
+    std::vector<std::pair<int32_t, int>> st{{world, 0}};
+    int maxlev = 0;
+    while (!st.empty()) {
+      auto [pv, lev] = st.back();
+      st.pop_back();
+      maxlev             = std::max(maxlev, lev);
+      const size_t nd    = lvs[pvs[pv].lv].daughters.size();
+      bytes += (3 + nd + ((nd + 1) & 1)) * sizeof(uint32_t) + 12 * sizeof(double);
+      for (int32_t d : lvs[pvs[pv].lv].daughters) st.push_back({d, lev + 1});
+    }
+    max_depth = maxlev + 1;
+  }
+  nav_words = bytes / sizeof(uint32_t) + 1;
+  nav.assign(nav_words + 1, 0u);
+  uint32_t cur = 1;
+  std::vector<Frame> st;
+  st.push_back({world, 0, 0u, 0, HostXform::Identity()});
+  while (!st.empty()) {
+    Frame f = st.back();
+    st.pop_back();
+    const std::vector<int32_t> &ds = lvs[pvs[f.pv].lv].daughters;
+    const uint16_t nd              = (uint16_t)ds.size();
+    const uint32_t self            = cur;
+    nav[cur]                       = f.mother;
+    if (f.mother > 0) nav[f.mother + 3 + f.dind] = cur;
+    nav[cur + 1]          = (uint32_t)f.pv;
+    HostXform mat         = f.mat;
+    if (f.level > 0) mat.MultiplyFromRight(pvs[f.pv].xf); // the world's own placement is not applied
+    unsigned char *meta   = reinterpret_cast<unsigned char *>(&nav[cur + 2]);
+    meta[0]               = (unsigned char)f.level;
+    meta[1]               = (unsigned char)(0x04 + 0x02 * (int)mat.has_trans + (int)mat.has_rot);
+    std::memcpy(meta + 2, &nd, 2);
+    cur += 3 + nd + ((nd + 1) & 1);
+    if (cur & 1u) ++cur;
+    std::memcpy(&nav[cur], mat.m.t, 3 * sizeof(double));
+    std::memcpy(&nav[cur + 6], mat.m.r, 9 * sizeof(double));
+    cur += 24;
+    // push daughters in reverse so that they are visited in order
+    for (int i = (int)ds.size() - 1; i >= 0; --i) st.push_back({ds[i], f.level + 1, self, i, mat});
+  }
+  nav.resize(nav_words);
+}
+
+// ---------------------------------------------------------------- close + upload
+int Geometry::build_host(std::string &err)
+{
+  if (closed) {
+    err = "geometry already closed";
+    return -1;
+  }
+  if (built) return 0;
+  lv_bvh.assign(lvs.size(), -1);
+  bvhs.clear();
+  if (world >= 0) {
+    for (size_t l = 0; l < lvs.size(); ++l) {
+      if (lvs[l].daughters.empty()) continue;
+      HostBVH b;
+      build_bvh((int32_t)l, b);
+      lv_bvh[l] = (int32_t)bvhs.size();
+      bvhs.push_back(std::move(b));
+    }
+    build_nav_table();
+    if (max_depth > 255) {
+      err = "geometry deeper than 255 levels";
+      return -1;
+    }
+  }
+  built = true;
+  return 0;
+}
+
+int Geometry::close(std::string &err)
+{
+  if (build_host(err) != 0) return -1;
+  if (upload(err) != 0) return -1;
+  closed = true;
+  return 0;
+}
+
+namespace {
+float round_down(double x)
+{
+  float f = (float)x;
+  if ((double)f > x) f = std::nextafter(f, -INFINITY);
+  return f;
+}
+float round_up(double x)
+{
+  float f = (float)x;
+  if ((double)f < x) f = std::nextafter(f, INFINITY);
+  return f;
+}
+struct Arena {
+  std::vector<unsigned char> host;
+  size_t add(const void *p, size_t bytes)
+  {
+    const size_t off = (host.size() + 255) & ~size_t(255);
+    host.resize(off + bytes);
+    if (bytes) std::memcpy(host.data() + off, p, bytes);
+    return off;
+  }
+  template <class T>
+  size_t add(std::vector<T> const &v)
+  {
+    return add(v.data(), v.size() * sizeof(T));
+  }
+};
+} // namespace
+
+int Geometry::upload(std::string &err)
+{
+  Arena a;
+  // shapes
+  std::vector<double> sdata;
+  std::vector<int32_t> stype, soff;
+  for (auto const &s : shapes) {
+    while (sdata.size() % 4) sdata.push_back(0.); // 32-byte aligned records
+    stype.push_back(s.type);
+    soff.push_back((int32_t)sdata.size());
+    sdata.insert(sdata.end(), s.rec.begin(), s.rec.end());
+  }
+  std::vector<int32_t> lv_shape, lv_dstart, lv_nd, daughters;
+  for (auto const &lv : lvs) {
+    lv_shape.push_back(lv.shape);
+    lv_dstart.push_back((int32_t)daughters.size());
+    lv_nd.push_back((int32_t)lv.daughters.size());
+    daughters.insert(daughters.end(), lv.daughters.begin(), lv.daughters.end());
+  }
+  std::vector<int32_t> pv_lv, pv_child;
+  std::vector<Xform> pv_xf;
+  for (auto const &pv : pvs) {
+    pv_lv.push_back(pv.lv);
+    pv_child.push_back(pv.child);
+    pv_xf.push_back(pv.xf.m);
+  }
+  // BVH arrays: node arrays concatenated; prim slots follow the LV daughter layout.
+  std::vector<int32_t> bvh_node0, bvh_prim0, node_nchild, node_offset, prim_id(daughters.size(), 0);
+  std::vector<double> node_box, prim_box(6 * daughters.size(), 0.);
+  std::vector<NodeF> node_f;
+  std::vector<float> prim_box_f(6 * daughters.size(), 0.f);
+  for (size_t l = 0; l < lvs.size(); ++l) {
+    if (lv_bvh[l] < 0) continue;
+    HostBVH const &b   = bvhs[lv_bvh[l]];
+    const int32_t base = lv_dstart[l];
+    bvh_node0.push_back((int32_t)node_nchild.size());
+    bvh_prim0.push_back(base);
+    for (size_t i = 0; i < b.nchild.size(); ++i) {
+      node_nchild.push_back(b.nchild[i]);
+      node_offset.push_back(b.offset[i] < 0 ? -1 : base + b.offset[i]);
+      NodeF nf;
+      for (int k = 0; k < 3; ++k) {
+        node_box.push_back(b.node_box[6 * i + k]);
+        nf.lo[k] = round_down(b.node_box[6 * i + k]);
+        nf.hi[k] = round_up(b.node_box[6 * i + 3 + k]);
+      }
+      for (int k = 0; k < 3; ++k) node_box.push_back(b.node_box[6 * i + 3 + k]);
+      nf.nchild = b.nchild[i];
+      nf.offset = b.offset[i] < 0 ? -1 : base + b.offset[i];
+      node_f.push_back(nf);
+    }
+    for (size_t i = 0; i < b.prim.size(); ++i) prim_id[base + i] = b.prim[i];
+    for (size_t i = 0; i < 6 * b.prim.size(); ++i) {
+      prim_box[6 * (size_t)base + i]   = b.prim_box[i];
+      prim_box_f[6 * (size_t)base + i] = (i % 6 < 3) ? round_down(b.prim_box[i]) : round_up(b.prim_box[i]);
+    }
+  }
+  const size_t o_sdata = a.add(sdata), o_stype = a.add(stype), o_soff = a.add(soff);
+  const size_t o_lvs = a.add(lv_shape), o_lvd = a.add(lv_dstart), o_lvn = a.add(lv_nd), o_lvb = a.add(lv_bvh);
+  const size_t o_dau = a.add(daughters), o_pvl = a.add(pv_lv), o_pvc = a.add(pv_child), o_pvx = a.add(pv_xf);
+  const size_t o_bn0 = a.add(bvh_node0), o_bp0 = a.add(bvh_prim0), o_nnc = a.add(node_nchild);
+  const size_t o_nof = a.add(node_offset), o_nbx = a.add(node_box), o_pid = a.add(prim_id);
+  const size_t o_pbx = a.add(prim_box), o_nf = a.add(node_f), o_pbf = a.add(prim_box_f), o_nav = a.add(nav);
+
+  cudaError_t e = cudaGetDevice(&device);
+  if (e == cudaSuccess) e = cudaMalloc(&arena, a.host.size() ? a.host.size() : 256);
+  if (e == cudaSuccess) e = cudaMemcpy(arena, a.host.data(), a.host.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    err = std::string("CUDA error during geometry upload: ") + cudaGetErrorString(e);
+    return -1;
+  }
+  arena_bytes      = a.host.size();
+  unsigned char *d = static_cast<unsigned char *>(arena);
+  auto P = [d](size_t off) { return d + off; };
+  dev.shape_data  = reinterpret_cast<const double *>(P(o_sdata));
+  dev.shape_type  = reinterpret_cast<const int32_t *>(P(o_stype));
+  dev.shape_off   = reinterpret_cast<const int32_t *>(P(o_soff));
+  dev.lv_shape    = reinterpret_cast<const int32_t *>(P(o_lvs));
+  dev.lv_dstart   = reinterpret_cast<const int32_t *>(P(o_lvd));
+  dev.lv_nd       = reinterpret_cast<const int32_t *>(P(o_lvn));
+  dev.lv_bvh      = reinterpret_cast<const int32_t *>(P(o_lvb));
+  dev.daughters   = reinterpret_cast<const int32_t *>(P(o_dau));
+  dev.pv_lv       = reinterpret_cast<const int32_t *>(P(o_pvl));
+  dev.pv_child    = reinterpret_cast<const int32_t *>(P(o_pvc));
+  dev.pv_xf       = reinterpret_cast<const Xform *>(P(o_pvx));
+  dev.bvh_node0   = reinterpret_cast<const int32_t *>(P(o_bn0));
+  dev.bvh_prim0   = reinterpret_cast<const int32_t *>(P(o_bp0));
+  dev.node_nchild = reinterpret_cast<const int32_t *>(P(o_nnc));
+  dev.node_offset = reinterpret_cast<const int32_t *>(P(o_nof));
+  dev.node_box    = reinterpret_cast<const double *>(P(o_nbx));
+  dev.prim_id     = reinterpret_cast<const int32_t *>(P(o_pid));
+  dev.prim_box    = reinterpret_cast<const double *>(P(o_pbx));
+  dev.node_f      = reinterpret_cast<const NodeF *>(P(o_nf));
+  dev.prim_box_f  = reinterpret_cast<const float *>(P(o_pbf));
+  dev.nav         = reinterpret_cast<const uint32_t *>(P(o_nav));
+  dev.world_pv    = world;
+  dev.max_depth   = max_depth;
+  dev.n_pv        = (int32_t)pvs.size();
+  dev.n_lv        = (int32_t)lvs.size();
+  return 0;
+}
+
+} // namespace vg

@@ -1,0 +1,149 @@
+// Plain-FP64 kernels: SoA shape queries (one instantiation per shape type and query,
+// the shape record passed by value so every lane reads it from the constant bank) and the
+// one-thread-per-track navigation kernels. Compiled with --fmad=false.
+#include "launch.h"
+#include "nav_fp64.cuh"
+
+namespace vg {
+namespace {
+
+using f64::V3;
+
+// Grid: enough CTAs to fill the 152 SMs several times over, then grid-stride.
+inline unsigned grid_for(size_t n, int block)
+{
+  size_t blocks       = (n + block - 1) / block;
+  const size_t maxgrd = 152 * 16;
+  if (blocks > maxgrd) blocks = maxgrd;
+  return (unsigned)(blocks ? blocks : 1);
+}
+
+template <class R>
+struct ShapeOps;
+#define VG_OPS(R, PFX)                                                                              \
+  template <>                                                                                       \
+  struct ShapeOps<R> {                                                                              \
+    __device__ static int inside(const R &r, V3 p) { return f64::PFX##_inside(r, p); }              \
+    __device__ static bool contains(const R &r, V3 p) { return f64::PFX##_contains(r, p); }         \
+    __device__ static double dist_in(const R &r, V3 p, V3 d) { return f64::PFX##_dist_in(r, p, d); }   \
+    __device__ static double dist_out(const R &r, V3 p, V3 d) { return f64::PFX##_dist_out(r, p, d); } \
+    __device__ static double safety_in(const R &r, V3 p) { return f64::PFX##_safety_in(r, p); }     \
+    __device__ static double safety_out(const R &r, V3 p) { return f64::PFX##_safety_out(r, p); }   \
+  };
+VG_OPS(BoxRec, box)
+VG_OPS(TubeRec, tube)
+VG_OPS(ConeRec, cone)
+#undef VG_OPS
+
+// Q: 0 Inside, 1 Contains, 2 DistanceToIn, 3 DistanceToOut, 4 SafetyToIn, 5 SafetyToOut
+template <class R, int Q>
+__global__ void __launch_bounds__(256) k_shape_query(const R rec, const Xform xf, const int apply_xf,
+                                                     const double *__restrict__ x, const double *__restrict__ y,
+                                                     const double *__restrict__ z, const double *__restrict__ dx,
+                                                     const double *__restrict__ dy, const double *__restrict__ dz,
+                                                     size_t n, void *__restrict__ out)
+{
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    V3 p{__ldg(x + i), __ldg(y + i), __ldg(z + i)};
+    const bool framed = apply_xf && (Q == 0 || Q == 1 || Q == 2 || Q == 4);
+    if (framed) p = f64::to_local(xf, p);
+    if (Q == 0) static_cast<int32_t *>(out)[i] = ShapeOps<R>::inside(rec, p);
+    if (Q == 1) static_cast<uint8_t *>(out)[i] = ShapeOps<R>::contains(rec, p) ? 1 : 0;
+    if (Q == 2 || Q == 3) {
+      V3 d{__ldg(dx + i), __ldg(dy + i), __ldg(dz + i)};
+      if (framed) d = f64::rotate(xf, d);
+      static_cast<double *>(out)[i] = (Q == 2) ? ShapeOps<R>::dist_in(rec, p, d) : ShapeOps<R>::dist_out(rec, p, d);
+    }
+    if (Q == 4) static_cast<double *>(out)[i] = ShapeOps<R>::safety_in(rec, p);
+    if (Q == 5) static_cast<double *>(out)[i] = ShapeOps<R>::safety_out(rec, p);
+  }
+}
+
+template <class R>
+cudaError_t launch_typed(const double *recp, const Xform &xf, int apply_xf, int q, const QueryArgs &a,
+                         cudaStream_t s)
+{
+  R rec;
+  memcpy(&rec, recp, sizeof(R));
+  const int block = 256;
+  const unsigned grid = grid_for(a.n, block);
+  switch (q) {
+  case 0: k_shape_query<R, 0><<<grid, block, 0, s>>>(rec, xf, apply_xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out); break;
+  case 1: k_shape_query<R, 1><<<grid, block, 0, s>>>(rec, xf, apply_xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out); break;
+  case 2: k_shape_query<R, 2><<<grid, block, 0, s>>>(rec, xf, apply_xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out); break;
+  case 3: k_shape_query<R, 3><<<grid, block, 0, s>>>(rec, xf, apply_xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out); break;
+  case 4: k_shape_query<R, 4><<<grid, block, 0, s>>>(rec, xf, apply_xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out); break;
+  case 5: k_shape_query<R, 5><<<grid, block, 0, s>>>(rec, xf, apply_xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out); break;
+  default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- navigation kernels
+__global__ void __launch_bounds__(256) k_locate(const DevGeom g, const double *__restrict__ x,
+                                                const double *__restrict__ y, const double *__restrict__ z, size_t n,
+                                                NavState *__restrict__ out)
+{
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    NavState s{0u, 0u, 0, {0, 0, 0}};
+    int status = 0;
+    f64::locate_global_point(g, g.world_pv, V3{__ldg(x + i), __ldg(y + i), __ldg(z + i)}, s.navInd, true, status);
+    out[i] = s;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_step(const DevGeom g, const double *__restrict__ x,
+                                              const double *__restrict__ y, const double *__restrict__ z,
+                                              const double *__restrict__ dx, const double *__restrict__ dy,
+                                              const double *__restrict__ dz, const double *__restrict__ limit,
+                                              const NavState *__restrict__ in, NavState *__restrict__ out,
+                                              double *__restrict__ step, int32_t *__restrict__ status,
+                                              int32_t *__restrict__ nvisited, size_t n)
+{
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const NavState s = in[i];
+    NavState o;
+    int st = 0, nv = 0;
+    const double lim = limit ? __ldg(limit + i) : kInfLength;
+    step[i] = f64::compute_step(g, V3{__ldg(x + i), __ldg(y + i), __ldg(z + i)},
+                                V3{__ldg(dx + i), __ldg(dy + i), __ldg(dz + i)}, lim, s, o, st, nvisited ? &nv : nullptr);
+    out[i] = o;
+    if (status) status[i] = st;
+    if (nvisited) nvisited[i] = nv;
+  }
+}
+
+} // namespace
+
+cudaError_t launch_shape_query_fp64(int type, const double *rec, const Xform &xf, int apply_xf, int q,
+                                    const QueryArgs &a, cudaStream_t s)
+{
+  if (a.n == 0) return cudaSuccess;
+  switch (type) {
+  case kShapeBox: return launch_typed<BoxRec>(rec, xf, apply_xf, q, a, s);
+  case kShapeTube: return launch_typed<TubeRec>(rec, xf, apply_xf, q, a, s);
+  case kShapeCone: return launch_typed<ConeRec>(rec, xf, apply_xf, q, a, s);
+  default: return cudaErrorNotSupported;
+  }
+}
+
+cudaError_t launch_locate_fp64(const DevGeom &g, const double *x, const double *y, const double *z, size_t n,
+                               NavState *out, cudaStream_t s)
+{
+  if (n == 0) return cudaSuccess;
+  k_locate<<<grid_for(n, 256), 256, 0, s>>>(g, x, y, z, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step_fp64(const DevGeom &g, const StepArgs &a, cudaStream_t s)
+{
+  if (a.n == 0) return cudaSuccess;
+  k_step<<<grid_for(a.n, 256), 256, 0, s>>>(g, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.limit, a.in, a.out, a.step,
+                                            a.status, a.nvisited, a.n);
+  return cudaGetLastError();
+}
+
+} // namespace vg

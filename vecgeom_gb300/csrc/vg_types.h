@@ -1,0 +1,130 @@
+// Plain-old-data records of the flattened device geometry, shared by the host builder
+// (geom.cpp) and the CUDA kernels. One record per unplaced shape, holding the user
+// parameters plus every quantity the reference precomputes at construction time
+// (VecGeom/volumes/*Struct.h), so no kernel evaluates a transcendental function.
+#pragma once
+#include <cstdint>
+
+#ifdef __CUDACC__
+#define VG_HD __host__ __device__
+#else
+#define VG_HD
+#endif
+
+namespace vg {
+
+// Shape type tags (also the C-ABI's VG_SHAPE_* values).
+enum ShapeType : int32_t {
+  kShapeBox        = 1,
+  kShapeTube       = 2,
+  kShapeCone       = 3,
+  kShapePolycone   = 4,
+  kShapePolyhedron = 5,
+  kShapeTorus2     = 6,
+  kShapeTrd        = 7,
+  kShapeBoolMinus  = 8,
+};
+
+// VecGeom/base/Math.h:27-52 (double precision)
+constexpr double kTolerance     = 1e-9;
+constexpr double kHalfTolerance = 0.5 * kTolerance;
+constexpr double kConeTolerance = 1e-7;
+constexpr double kPushTolerance = 1e-6;
+constexpr double kAngTolerance  = 1e-9;
+constexpr double kPi            = 3.14159265358979323846;
+constexpr double kTwoPi         = 2. * kPi;
+constexpr double kInfLength     = 1.7976931348623157e308; // DBL_MAX
+constexpr double kEpsilon       = 2.220446049250313e-16;  // DBL_EPSILON
+constexpr double kMinimum       = 2.2250738585072014e-308; // DBL_MIN
+
+// EnumInside (VecGeom/base/Global.h:71-79)
+constexpr int32_t kInside = 1, kSurface = 2, kOutside = 3;
+
+// Phi wedge (VecGeom/volumes/Wedge_Evolution.h): along and normal vectors of both planes.
+struct WedgeRec {
+  double dphi;
+  double a1x, a1y, a2x, a2y;
+  double n1x, n1y, n2x, n2y;
+};
+
+struct BoxRec {
+  double dx, dy, dz;
+};
+
+// VecGeom/volumes/TubeStruct.h:15-41
+struct TubeRec {
+  double rmin, rmax, z, sphi, dphi;
+  double rmin2, rmax2, a1x, a1y, a2x, a2y;
+  double tolIrmin2, tolOrmin2, tolIrmax2, tolOrmax2, tolIz, tolOz;
+  double tolIrmin, tolOrmin, tolIrmax, tolOrmax, maxVal;
+  WedgeRec w;
+};
+
+// VecGeom/volumes/ConeStruct.h:23-83
+struct ConeRec {
+  double rmin1, rmax1, rmin2, rmax2, dz, sphi, dphi;
+  double frmin1, frmin2, frmax1, frmax2; // construction values (used by Extent)
+  double a1x, a1y, a2x, a2y;
+  double innerSlope, outerSlope, innerOffset, outerOffset, innerTol, outerTol;
+  double sqRmin1, sqRmin2, sqRmax1, sqRmax2, tolIz, tolOz;
+  double innerApex, tanInnerApex, outerApex, tanOuterApex;
+  double secRMin, secRMax, invSecRMin, invSecRMax, tanRMin, tanRMax, zNormInner, zNormOuter;
+  double origRmax1, origRmax2;
+  WedgeRec w;
+};
+
+// Compact placed-volume transformation: p_local = R^T (p - t) with the reference's
+// component order (VecGeom/base/Transformation3D.h:640-651).
+struct Xform {
+  double t[3];
+  double r[9];
+};
+
+// Navigation state: bit-identical to NavStateIndex (VecGeom/navigation/NavStateIndex.h:39-41).
+struct NavState {
+  uint32_t navInd;
+  uint32_t lastExited;
+  uint8_t onBoundary;
+  uint8_t pad[3];
+};
+static_assert(sizeof(NavState) == 12, "NavState layout");
+
+// FP32 BVH node record for the mixed-precision traversal: 32 bytes, 32-byte aligned.
+struct alignas(32) NodeF {
+  float lo[3];
+  float hi[3];
+  int32_t nchild; // >= 0: leaf with nchild prims; -1: internal
+  int32_t offset; // first prim slot (absolute index into the prim arrays)
+};
+static_assert(sizeof(NodeF) == 32, "NodeF layout");
+
+// Pointers into the device copy of a closed geometry. Passed by value to kernels.
+struct DevGeom {
+  const double *shape_data; // packed shape records (double-aligned)
+  const int32_t *shape_type;
+  const int32_t *shape_off;  // record offset (in doubles) per shape id
+  const int32_t *lv_shape;
+  const int32_t *lv_dstart;  // first entry of the LV's daughters in `daughters`
+  const int32_t *lv_nd;
+  const int32_t *lv_bvh;     // BVH index of the LV, -1 without daughters
+  const int32_t *daughters;  // placed-volume ids in daughter order
+  const int32_t *pv_lv;
+  const int32_t *pv_child;
+  const Xform *pv_xf;
+  const int32_t *bvh_node0;  // first node of each BVH in the node arrays
+  const int32_t *bvh_prim0;  // first prim slot of each BVH (== lv_dstart of its LV)
+  const int32_t *node_nchild;
+  const int32_t *node_offset; // absolute prim slot
+  const double *node_box;     // 6 doubles per node (lo xyz, hi xyz)
+  const int32_t *prim_id;     // daughter index (relative to the LV) per prim slot
+  const double *prim_box;     // 6 doubles per daughter slot (indexed lv_dstart + daughter index)
+  const NodeF *node_f;        // FP32 node records (bounds rounded outward)
+  const float *prim_box_f;    // FP32 daughter boxes (6 floats per slot, rounded outward)
+  const uint32_t *nav;        // NavIndex table
+  int32_t world_pv;
+  int32_t max_depth;
+  int32_t n_pv;
+  int32_t n_lv;
+};
+
+} // namespace vg

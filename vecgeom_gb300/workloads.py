@@ -1,0 +1,236 @@
+"""Seeded synthetic workloads: the shapes, geometries and track samples the benchmarks and
+tests run on.
+
+Every builder takes a ``geo`` object with the construction surface of
+``vecgeom_gb300.Geometry`` (add_box, add_tube, ..., place_daughter, set_world, close) and
+issues the same call sequence to it, so two implementations fed by the same builder get
+identical placed-volume ids. Random numbers come from numpy's Philox generator keyed by
+SplitMix64-derived sub-seeds; all arrays are FP64 and generated once on the host.
+"""
+import math
+
+import numpy as np
+
+MASK64 = (1 << 64) - 1
+TWO_PI = 2.0 * math.pi
+
+
+def splitmix64(x):
+    """One SplitMix64 output for state x (the published constants of the generator)."""
+    z = (x + 0x9E3779B97F4A7C15) & MASK64
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & MASK64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & MASK64
+    return z ^ (z >> 31)
+
+
+def rng(seed, stream=0):
+    """Independent Philox stream `stream` of master seed `seed`."""
+    return np.random.Generator(np.random.Philox(key=splitmix64((seed * 0x100000001B3 + stream) & MASK64)))
+
+
+def isotropic(g, n):
+    """Isotropic unit vectors: z = 2u - 1, phi = 2 pi v."""
+    cz = 2.0 * g.random(n) - 1.0
+    ph = TWO_PI * g.random(n)
+    s = np.sqrt(np.maximum(0.0, 1.0 - cz * cz))
+    return s * np.cos(ph), s * np.sin(ph), cz
+
+
+def rot_z(phi):
+    """Row-major rotation about z by phi (p_master = R p_local)."""
+    c, s = math.cos(phi), math.sin(phi)
+    return (c, -s, 0.0, s, c, 0.0, 0.0, 0.0, 1.0)
+
+
+IDENT = (1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0)
+
+# ---------------------------------------------------------------------- shape catalogue
+# Config 1: plain FP64 shape queries (Box, full-phi Tube, Cone), 2^20 points each.
+SHAPES_CFG1 = {
+    "box": ("box", (10.0, 20.0, 30.0)),
+    "tube": ("tube", (10.0, 20.0, 30.0, 0.0, TWO_PI)),
+    "cone": ("cone", (5.0, 10.0, 8.0, 15.0, 25.0, 0.0, TWO_PI)),
+}
+
+
+def _polycone_cfg2(seed=0x5EED):
+    """12 z-planes evenly in [-500, 500]; rmin in [50,120], rmax in [150,400] from a seeded
+    monotone random walk (increasing with z)."""
+    g = rng(seed, 17)
+    z = np.linspace(-500.0, 500.0, 12)
+    rmin = np.sort(50.0 + 70.0 * g.random(12))
+    rmax = np.sort(150.0 + 250.0 * g.random(12))
+    return (0.0, TWO_PI, tuple(z), tuple(rmin), tuple(rmax))
+
+
+def _polyhedron_cfg2():
+    """8 sides, 6 z-planes, full phi; the z/r values chosen here are recorded with the
+    benchmark output."""
+    z = (-300.0, -200.0, -100.0, 100.0, 200.0, 300.0)
+    rmin = (50.0, 60.0, 70.0, 70.0, 60.0, 50.0)
+    rmax = (150.0, 180.0, 200.0, 200.0, 180.0, 150.0)
+    return (0.0, TWO_PI, 8, z, rmin, rmax)
+
+
+SHAPES_CFG2 = {
+    "tube_phi": ("tube", (10.0, 20.0, 30.0, 0.3, 1.8)),
+    "polycone": ("polycone", _polycone_cfg2()),
+    "polyhedron": ("polyhedron", _polyhedron_cfg2()),
+    "torus2": ("torus2", (5.0, 15.0, 100.0, 0.0, TWO_PI)),
+    "trd": ("trd", (30.0, 10.0, 40.0, 15.0, 60.0)),
+    # Box(5,5,5) minus Tube(0.5,2,2,0,2pi) placed at (-2.5,0,0): the reference's own benchmark
+    # pair (test/benchmark/BoxMinusHollowTubeBenchmark_virtual.cpp:22-31).
+    "box_minus_tube": ("boolminus", None),
+}
+
+
+def add_shape(geo, kind, params):
+    """Create one shape on `geo`; returns the shape id (boolean operands placed first)."""
+    if kind == "boolminus":
+        lb = geo.add_logical_volume(geo.add_box(5.0, 5.0, 5.0))
+        lt = geo.add_logical_volume(geo.add_tube(0.5, 2.0, 2.0, 0.0, TWO_PI))
+        left = geo.place(lb)
+        right = geo.place(lt, (-2.5, 0.0, 0.0), IDENT)
+        return geo.add_boolean_subtraction(left, right)
+    return getattr(geo, "add_" + kind)(*params)
+
+
+def build_single_shape(geo, kind, params):
+    """One shape placed with the identity transformation: returns (shape id, placed id)."""
+    s = add_shape(geo, kind, params)
+    pv = geo.place(geo.add_logical_volume(s))
+    geo.close()
+    return s, pv
+
+
+def shape_points_box(lo, hi, n, seed, scale=1.2):
+    """Points uniform in the extent box scaled `scale` about its centre, isotropic directions."""
+    g = rng(seed, 1)
+    lo, hi = np.asarray(lo), np.asarray(hi)
+    c, h = 0.5 * (lo + hi), 0.5 * (hi - lo) * scale
+    pts = [c[k] + h[k] * (2.0 * g.random(n) - 1.0) for k in range(3)]
+    d = isotropic(rng(seed, 2), n)
+    return tuple(pts), d
+
+
+# ---------------------------------------------------------------------- navigation geometries
+def barrel_layers(nlayers, r0, r1, n0, n1):
+    radii = np.linspace(r0, r1, nlayers)
+    counts = np.round(np.linspace(n0, n1, nlayers)).astype(int)
+    return radii, counts
+
+
+MODULE_HALF = (1.0, 10.0, 50.0)   # 2 x 20 x 100 mm module, thin along the radius
+SENSOR_HALF = (0.5, 9.0, 49.0)
+TANGENTIAL_PITCH = 22.0
+Z_PITCH = 104.0
+
+
+def _place_barrel_layer(geo, world_lv, module_lv, r, n, g, jitter):
+    """One layer: a Tube holding n phi-rotated modules arranged in z-rings; returns the pv."""
+    per_ring = max(1, int(math.floor(TWO_PI * r / TANGENTIAL_PITCH)))
+    rings = int(math.ceil(n / per_ring))
+    halfz = 0.5 * rings * Z_PITCH + 4.0
+    rmin = r - MODULE_HALF[0] - jitter - 1.0
+    rout = r + MODULE_HALF[0] + jitter + 1.0
+    rmax = math.sqrt(rout * rout + (MODULE_HALF[1] + 1.0) ** 2) + 1.0
+    layer_lv = geo.add_logical_volume(geo.add_tube(rmin, rmax, halfz, 0.0, TWO_PI))
+    placed = 0
+    for ring in range(rings):
+        m = min(per_ring, n - placed)
+        zc = -0.5 * rings * Z_PITCH + (ring + 0.5) * Z_PITCH
+        for k in range(m):
+            phi = TWO_PI * k / per_ring + (0.5 * TWO_PI / per_ring) * (ring & 1)
+            dr, dz = jitter * (2.0 * g.random(2) - 1.0)
+            rr = r + dr
+            t = (rr * math.cos(phi), rr * math.sin(phi), zc + dz)
+            geo.place_daughter(layer_lv, module_lv, t, rot_z(phi))
+        placed += m
+    return geo.place_daughter(world_lv, layer_lv)
+
+
+def build_barrel(geo, seed=0xBA44E1, nlayers=10, r0=50.0, r1=1200.0, n0=64, n1=640, jitter=1.0, close=True):
+    """Config 3 barrel: world box 2000 x 2000 x 3000 mm half-lengths, 10 tube layers
+    (r 50..1200 mm) holding 64..640 phi-rotated 2x20x100 mm box modules with +-1 mm seeded
+    radial/z jitter, each module holding one sensor box (nesting depth 4). Modules are laid
+    out in 104 mm z-rings at 22 mm tangential pitch, so no two volumes overlap."""
+    g = rng(seed, 3)
+    world_lv = geo.add_logical_volume(geo.add_box(2000.0, 2000.0, 3000.0))
+    sensor_lv = geo.add_logical_volume(geo.add_box(*SENSOR_HALF))
+    module_lv = geo.add_logical_volume(geo.add_box(*MODULE_HALF))
+    geo.place_daughter(module_lv, sensor_lv)
+    radii, counts = barrel_layers(nlayers, r0, r1, n0, n1)
+    for r, n in zip(radii, counts):
+        _place_barrel_layer(geo, world_lv, module_lv, float(r), int(n), g, jitter)
+    world = geo.place(world_lv)
+    geo.set_world(world)
+    if close:
+        geo.close()
+    return world
+
+
+def build_detector(geo, seed=0xDE7EC7, nlayers=20, total_modules=150000, wedges_per_side=2000, ndisks=12,
+                   close=True):
+    """Config 4 detector: a 20-layer barrel totalling `total_modules` box modules (counts
+    proportional to radius, r 100..1150 mm) plus two endcaps of `ndisks` Polycone holders
+    (8 z-planes each) carrying `wedges_per_side` Trd wedges per side."""
+    g = rng(seed, 4)
+    world_lv = geo.add_logical_volume(geo.add_box(2000.0, 2000.0, 3000.0))
+    sensor_lv = geo.add_logical_volume(geo.add_box(*SENSOR_HALF))
+    module_lv = geo.add_logical_volume(geo.add_box(*MODULE_HALF))
+    geo.place_daughter(module_lv, sensor_lv)
+    radii = np.linspace(100.0, 1150.0, nlayers)
+    counts = np.floor(total_modules * radii / radii.sum()).astype(int)
+    counts[-1] += total_modules - counts.sum()
+    for r, n in zip(radii, counts):
+        _place_barrel_layer(geo, world_lv, module_lv, float(r), int(n), g, 1.0)
+    # endcaps: Polycone holders (an annulus r 290..1100 with a stepped outer profile) with
+    # Trd wedges pointing radially (local z -> radial, local y -> global z).
+    zs = (-20.0, -15.0, -10.0, -5.0, 5.0, 10.0, 15.0, 20.0)
+    rmins = (290.0,) * 8
+    rmaxs = (1100.0, 1105.0, 1110.0, 1110.0, 1110.0, 1110.0, 1105.0, 1100.0)
+    holder_lv = geo.add_logical_volume(geo.add_polycone(0.0, TWO_PI, zs, rmins, rmaxs))
+    per_disk = int(math.ceil(wedges_per_side / ndisks))
+    dphi = TWO_PI / per_disk
+    rin, rout = 310.0, 1080.0
+    dx1 = 0.45 * rin * dphi
+    dx2 = 0.45 * rout * dphi
+    wedge_lv = geo.add_logical_volume(geo.add_trd(dx1, dx2, 5.0, 5.0, 0.5 * (rout - rin)))
+    rc = 0.5 * (rin + rout)
+    for k in range(per_disk):
+        phi = k * dphi
+        c, s = math.cos(phi), math.sin(phi)
+        rot = (-s, 0.0, c, c, 0.0, s, 0.0, 1.0, 0.0)
+        geo.place_daughter(holder_lv, wedge_lv, (rc * c, rc * s, 0.0), rot)
+    for side in (-1.0, 1.0):
+        for d in range(ndisks):
+            z = side * (2300.0 + 55.0 * d)
+            geo.place_daughter(world_lv, holder_lv, (0.0, 0.0, z))
+    world = geo.place(world_lv)
+    geo.set_world(world)
+    if close:
+        geo.close()
+    return world
+
+
+def tracks_in_cylinder(n, seed, rmax=30.0, halfz=500.0):
+    """Config 3 track starts: uniform in the cylinder r < rmax, |z| < halfz, isotropic."""
+    g = rng(seed, 5)
+    r = rmax * np.sqrt(g.random(n))
+    ph = TWO_PI * g.random(n)
+    z = halfz * (2.0 * g.random(n) - 1.0)
+    d = isotropic(rng(seed, 6), n)
+    return (r * np.cos(ph), r * np.sin(ph), z), d
+
+
+def primaries_eta_phi(n, seed, eta_max=3.0):
+    """Config 5 primaries from the origin: pseudorapidity uniform in [-eta_max, eta_max],
+    phi uniform."""
+    g = rng(seed, 7)
+    eta = eta_max * (2.0 * g.random(n) - 1.0)
+    ph = TWO_PI * g.random(n)
+    theta = 2.0 * np.arctan(np.exp(-eta))
+    st = np.sin(theta)
+    d = (st * np.cos(ph), st * np.sin(ph), np.cos(theta))
+    z = np.zeros(n)
+    return (z.copy(), z.copy(), z.copy()), d
