@@ -95,3 +95,24 @@ def test_builder_rejects_bad_ids():
         g.place_daughter(7, lv)
     with pytest.raises(vg.VGError):
         g.set_world(3)
+
+
+def declared_arity():
+    """Parameter count of every vg_* function declared in include/*.h."""
+    out = {}
+    inc = os.path.join(ROOT, "include")
+    for f in sorted(os.listdir(inc)):
+        if f.endswith(".h"):
+            src = re.sub(r"/\*.*?\*/", "", open(os.path.join(inc, f)).read(), flags=re.S)
+            for name, params in re.findall(r"\b(vg_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", src, flags=re.S):
+                params = params.strip()
+                out[name] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_binding_arity_matches_header():
+    ar = declared_arity()
+    assert len(ar) >= 25
+    for name, (res, args) in vg._SIGS.items():
+        assert name in ar, name
+        assert len(args) == ar[name], (name, len(args), ar[name])

@@ -84,9 +84,9 @@ _SIGS = {
     "vg_placed_safety_to_out": (ctypes.c_int, [_c_vp, ctypes.c_int32, _c_vp, _c_vp, _c_vp, ctypes.c_size_t,
                                                _c_vp, ctypes.c_uint32, _c_vp]),
     "vg_nav_locate_point": (ctypes.c_int, [_c_vp, _c_vp, _c_vp, _c_vp, ctypes.c_size_t, _c_vp, _c_vp]),
-    "vg_nav_compute_step_and_next_volume": (ctypes.c_int, [_c_vp] + [_c_vp] * 12 +
+    "vg_nav_compute_step_and_next_volume": (ctypes.c_int, [_c_vp] + [_c_vp] * 11 +
                                             [ctypes.c_size_t, ctypes.c_uint32, _c_vp]),
-    "vg_nav_compute_step_and_next_volume_host": (ctypes.c_int, [_c_vp] + [_c_vp] * 12 +
+    "vg_nav_compute_step_and_next_volume_host": (ctypes.c_int, [_c_vp] + [_c_vp] * 11 +
                                                  [ctypes.c_size_t, ctypes.c_uint32, _c_vp]),
 }
 
