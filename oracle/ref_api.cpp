@@ -5,6 +5,7 @@
 // sides assign identical placed-volume ids and child ids. Batched queries split the
 // track range into contiguous chunks over std::thread workers.
 #include "ref_nav.h"
+#include "ref_shapes_more.h"
 #include <chrono>
 #include <cstring>
 #include <thread>
@@ -47,6 +48,14 @@ int oracle_add_shape(void *gp, int type, const double *p, int np)
   case 1: s = new Box(p[0], p[1], p[2]); break;
   case 2: s = new Tube(p[0], p[1], p[2], p[3], p[4]); break;
   case 3: s = new Cone(p[0], p[1], p[2], p[3], p[4], p[5], p[6]); break;
+  case 4: {
+    const int nz = (int)p[2];
+    s            = new Polycone(p[0], p[1], nz, p + 3, p + 3 + nz, p + 3 + 2 * nz);
+    break;
+  }
+  case 6: s = new Torus2(p[0], p[1], p[2], p[3], p[4]); break;
+  case 7: s = new Trd(p[0], p[1], p[2], p[3], p[4]); break;
+  case 8: s = new BooleanMinus(g->pvs.at((int)p[0]).get(), g->pvs.at((int)p[1]).get()); break;
   default: return -1;
   }
   (void)np;

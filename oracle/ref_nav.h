@@ -38,6 +38,11 @@ struct PlacedVolume {
     return Shape()->DistanceToIn(T.Transform(p), T.TransformDirection(d), s);
   }
   double DistanceToOut(Vec3 const &p, Vec3 const &d, double s) const { return Shape()->DistanceToOut(p, d, s); }
+  // PlacedDistanceToOut (SpecializedPlacedVolImplHelper.h:148-163): mother-frame input
+  double PlacedDistanceToOut(Vec3 const &p, Vec3 const &d, double s) const
+  {
+    return Shape()->DistanceToOut(T.Transform(p), T.TransformDirection(d), s);
+  }
   double SafetyToIn(Vec3 const &p) const { return Shape()->SafetyToIn(T.Transform(p)); }
   double SafetyToOut(Vec3 const &p) const { return Shape()->SafetyToOut(p); }
 };

@@ -1,0 +1,628 @@
+// ORACLE — TEST INFRASTRUCTURE ONLY (see ref_base.h).
+#include "ref_shapes_more.h"
+#include "ref_nav.h"
+#include <cmath>
+
+namespace oracle {
+
+constexpr double kTiny = 1e-30;
+
+// ====================================================================== Trd
+// TrdStruct.h:68-86 CalculateCached
+Trd::Trd(double x1, double x2, double y1, double y2, double z) : fDX1(x1), fDX2(x2), fDY1(y1), fDY2(y2), fDZ(z)
+{
+  fX2minusX1    = fDX2 - fDX1;
+  fY2minusY1    = fDY2 - fDY1;
+  fHalfX1plusX2 = 0.5 * (fDX1 + fDX2);
+  fHalfY1plusY2 = 0.5 * (fDY1 + fDY2);
+  fFx           = 0.5 * (fDX1 - fDX2) / fDZ;
+  fFy           = 0.5 * (fDY1 - fDY2) / fDZ;
+  fSecxz        = std::sqrt(1 + fFx * fFx);
+  fSecyz        = std::sqrt(1 + fFy * fFy);
+  fCalfX        = 1. / Sqrt(1.0 + fFx * fFx);
+  fCalfY        = 1. / Sqrt(1.0 + fFy * fFy);
+  fToleranceX   = kTolerance * Sqrt(fX2minusX1 * fX2minusX1 + 4 * fDZ * fDZ);
+  // the reference uses the x extent for the y tolerance as well (TrdStruct.h:85)
+  fToleranceY = kTolerance * Sqrt(fX2minusX1 * fX2minusX1 + 4 * fDZ * fDZ);
+}
+
+// TrdImplementation.h:138-173 UnplacedInside (UniversalTrd: the y faces always take the
+// cross-product test, HasVaryingY<UniversalTrd> is kUnknown)
+void Trd::UnplacedInside(Vec3 const &point, bool surfaceT, bool &cin, bool &cout) const
+{
+  const double pzPlusDz = point.z() + fDZ;
+  cout                  = Abs(point.z()) > (surfaceT ? fDZ + kHalfTolerance : fDZ);
+  if (surfaceT) cin = Abs(point.z()) < fDZ - kHalfTolerance;
+  double cross = fX2minusX1 * pzPlusDz - (2.0 * fDZ) * (Abs(point.x()) - fDX1);
+  if (surfaceT) {
+    cout = cout || (cross < -fToleranceX);
+    cin  = cin && (cross > fToleranceX);
+  } else {
+    cout = cout || (cross < 0);
+  }
+  cross = fY2minusY1 * pzPlusDz - (2.0 * fDZ) * (Abs(point.y()) - fDY1);
+  if (surfaceT) {
+    cout = cout || (cross < -fToleranceY);
+    cin  = cin && (cross > fToleranceY);
+  } else {
+    cout = cout || (cross < 0);
+  }
+}
+
+// TrdImplementation.h:243-287 Inside (outside overrides inside), Contains
+int Trd::Inside(Vec3 const &p) const
+{
+  bool in = false, out = false;
+  UnplacedInside(p, true, in, out);
+  int r = kSurface;
+  if (in) r = kInside;
+  if (out) r = kOutside;
+  return r;
+}
+bool Trd::Contains(Vec3 const &p) const
+{
+  bool in = false, out = false;
+  UnplacedInside(p, false, in, out);
+  return !out;
+}
+
+// TrdImplementation.h:69-117 FaceTrajectoryIntersection
+void Trd::Face(Vec3 const &pos, Vec3 const &dir, bool forY, bool mirrored, bool toInside, double &dist, bool &ok) const
+{
+  double alongV, posV, dirV, posK, dirK, fV, fK, halfKplus, v1, ndotv;
+  if (forY) {
+    alongV = fY2minusY1, v1 = fDY1, posV = pos.y(), posK = pos.x(), dirV = dir.y(), dirK = dir.x();
+    fK = fFx, fV = fFy, halfKplus = fHalfX1plusX2;
+  } else {
+    alongV = fX2minusX1, v1 = fDX1, posV = pos.x(), posK = pos.y(), dirV = dir.x(), dirK = dir.y();
+    fK = fFy, fV = fFx, halfKplus = fHalfY1plusY2;
+  }
+  if (mirrored) {
+    posV *= -1.;
+    dirV *= -1.;
+  }
+  ndotv = dirV + fV * dir.z();
+  ok    = toInside ? (ndotv < 0.) : (ndotv > 0.);
+  if (!ok) return;
+  const double alongZ = 2.0 * fDZ;
+  dist = (alongZ * (posV - v1) - alongV * (pos.z() + fDZ)) / (dir.z() * alongV - dirV * alongZ + kTiny);
+  ok   = ok && (dist > -kHalfTolerance);
+  if (ok) {
+    const double hitz = pos.z() + dist * dir.z();
+    ok                = ok && (Abs(hitz) <= fDZ);
+    const double hitk = posK + dist * dirK;
+    const double dK   = halfKplus - fK * hitz;
+    ok                = ok && (Abs(hitk) <= dK);
+    if (ok && Abs(dist) < kHalfTolerance) dist = 0.0;
+  }
+}
+
+// TrdImplementation.h:118-137 Safety
+double Trd::Safety(Vec3 const &pos, bool inside) const
+{
+  double dist        = fDZ - Abs(pos.z());
+  const double distx = fHalfX1plusX2 - fFx * pos.z();
+  const double safx  = (distx - Abs(pos.x())) * fCalfX;
+  if (distx >= 0 && safx < dist) dist = safx;
+  if (VaryingY()) {
+    const double disty = fHalfY1plusY2 - fFy * pos.z();
+    const double safy  = (disty - Abs(pos.y())) * fCalfY;
+    if (disty >= 0 && safy < dist) dist = safy;
+  } else {
+    const double safy = fDY1 - Abs(pos.y());
+    if (safy < dist) dist = safy;
+  }
+  return inside ? dist : -dist;
+}
+
+// TrdImplementation.h:288-370 DistanceToIn
+double Trd::DistanceToIn(Vec3 const &point, Vec3 const &direction, double) const
+{
+  double distance = kInfLength;
+  const bool inz  = Abs(point.z()) < fDZ - kHalfTolerance;
+  double distx    = fHalfX1plusX2 - fFx * point.z();
+  const bool inx  = (distx - Abs(point.x())) * fCalfX > kHalfTolerance;
+  double disty;
+  bool iny;
+  if (VaryingY()) {
+    disty = fHalfY1plusY2 - fFy * point.z();
+    iny   = (disty - Abs(point.y())) * fCalfY > kHalfTolerance;
+  } else {
+    disty = Abs(point.y()) - fDY1;
+    iny   = disty < -kHalfTolerance;
+  }
+  const bool inside = inx && iny && inz;
+  if (inside) distance = -1.;
+  bool done = inside;
+  bool okz  = point.z() * direction.z() < 0.;
+  okz       = okz && !inz;
+  if (okz) {
+    const double distz = (Abs(point.z()) - fDZ) / Abs(direction.z());
+    const double hitx  = Abs(point.x() + distz * direction.x());
+    const double hity  = Abs(point.y() + distz * direction.y());
+    const bool okzt    = point.z() > (fDZ - kHalfTolerance) && hitx <= fDX2 && hity <= fDY2;
+    const bool okzb    = point.z() < (-fDZ + kHalfTolerance) && hitx <= fDX1 && hity <= fDY1;
+    okz                = okz && (okzt || okzb);
+    if (okz) distance = distz;
+  }
+  done = done || okz;
+  if (done) {
+    if (Abs(distance) < kHalfTolerance) distance = 0.0;
+    return distance;
+  }
+  bool okx = false;
+  if (!inx) {
+    Face(point, direction, false, false, true, distx, okx);
+    if (okx) distance = distx;
+    Face(point, direction, false, true, true, distx, okx);
+    if (okx) distance = distx;
+  }
+  done = done || okx;
+  if (done) {
+    if (Abs(distance) < kHalfTolerance) distance = 0.0;
+    return distance;
+  }
+  bool oky = false;
+  if (VaryingY()) {
+    if (!iny) {
+      Face(point, direction, true, false, true, disty, oky);
+      if (oky) distance = disty;
+      Face(point, direction, true, true, true, disty, oky);
+      if (oky) distance = disty;
+    }
+  } else {
+    if (!iny) {
+      disty /= Abs(direction.y());
+      const double zhit = point.z() + disty * direction.z();
+      const double xhit = point.x() + disty * direction.x();
+      const double dx   = fHalfX1plusX2 - fFx * zhit;
+      oky = point.y() * direction.y() < 0 && disty > -kHalfTolerance && Abs(xhit) < dx && Abs(zhit) < fDZ;
+      if (oky) distance = disty;
+    }
+  }
+  if (Abs(distance) < kHalfTolerance) distance = 0.0;
+  return distance;
+}
+
+// TrdImplementation.h:371-470 DistanceToOut
+double Trd::DistanceToOut(Vec3 const &point, Vec3 const &dir, double) const
+{
+  double distance     = 0.0;
+  const double invdir = 1. / Abs(dir.z() + kTiny);
+  const double safz   = fDZ - Abs(point.z());
+  bool out            = safz < -kHalfTolerance;
+  double distx        = fHalfX1plusX2 - fFx * point.z();
+  out                 = out || ((distx - Abs(point.x())) * fCalfX < -kHalfTolerance);
+  double disty;
+  if (VaryingY()) {
+    disty = fHalfY1plusY2 - fFy * point.z();
+    out   = out || ((disty - Abs(point.y())) * fCalfY < -kHalfTolerance);
+  } else {
+    disty = fDY1 - Abs(point.y());
+    out   = out || (disty < -kHalfTolerance);
+  }
+  if (out) return -1.;
+  auto clamp = [](double d) { return Abs(d) < kHalfTolerance ? 0.0 : d; };
+  if (dir.z() > 0.) {
+    const double distz = (fDZ - point.z()) * invdir;
+    const double hitx  = Abs(point.x() + distz * dir.x());
+    const double hity  = Abs(point.y() + distz * dir.y());
+    if (hitx <= fDX2 && hity <= fDY2) return clamp(distz);
+  }
+  if (dir.z() < 0.) {
+    const double distz = (point.z() + fDZ) * invdir;
+    const double hitx  = Abs(point.x() + distz * dir.x());
+    const double hity  = Abs(point.y() + distz * dir.y());
+    if (hitx <= fDX1 && hity <= fDY1) return clamp(distz);
+  }
+  bool okx;
+  Face(point, dir, false, false, false, distx, okx);
+  if (okx) return clamp(distx);
+  Face(point, dir, false, true, false, distx, okx);
+  if (okx) return clamp(distx);
+  bool oky;
+  if (VaryingY()) {
+    Face(point, dir, true, false, false, disty, oky);
+    if (oky) return clamp(disty);
+    Face(point, dir, true, true, false, disty, oky);
+    if (oky) distance = disty;
+  } else {
+    double plane = fDY1;
+    if (dir.y() < 0.) plane = -fDY1;
+    disty             = (plane - point.y()) / dir.y();
+    const double zhit = point.z() + disty * dir.z();
+    const double xhit = point.x() + disty * dir.x();
+    const double dx   = fHalfX1plusX2 - fFx * zhit;
+    oky               = Abs(xhit) < dx && Abs(zhit) < fDZ;
+    if (oky) distance = disty;
+  }
+  return clamp(distance);
+}
+
+// source/UnplacedTrd / UnplacedTrd.h:218-222 Extent
+void Trd::Extent(Vec3 &lo, Vec3 &hi) const
+{
+  lo = Vec3(-Max(fDX1, fDX2), -Max(fDY1, fDY2), -fDZ);
+  hi = Vec3(Max(fDX1, fDX2), Max(fDY1, fDY2), fDZ);
+}
+
+// ====================================================================== Polycone
+// PolyconeStruct.h:124-239 Init (sections are ConeStruct(prevRmin, prevRmax, rMin, rMax,
+// dz, phiStart, phiTotal) shifted to the middle of their z range)
+Polycone::Polycone(double phiStart, double phiTotal, int nz, const double *zPlane, const double *rInner,
+                   const double *rOuter)
+{
+  // SetAndCheckDPhiAngle / SetAndCheckSPhiAngle
+  if (phiTotal >= kTwoPi - 0.5 * kAngTolerance) {
+    fDeltaPhi = kTwoPi;
+    fStartPhi = 0;
+  } else if (phiTotal > 0) {
+    fDeltaPhi = phiTotal;
+  }
+  fStartPhi = phiStart < 0 ? kTwoPi - std::fmod(std::fabs(phiStart), kTwoPi) : std::fmod(phiStart, kTwoPi);
+  if (fStartPhi + fDeltaPhi > kTwoPi) fStartPhi -= kTwoPi;
+  std::vector<double> z(zPlane, zPlane + nz), rin(rInner, rInner + nz), rout(rOuter, rOuter + nz);
+  if (zPlane[0] > zPlane[nz - 1])
+    for (int i = 0; i < nz; ++i) z[i] = zPlane[nz - 1 - i], rin[i] = rInner[nz - 1 - i], rout[i] = rOuter[nz - 1 - i];
+  if (phiTotal <= 0. || phiTotal > kTwoPi - kTolerance) {
+    fStartPhi = 0;
+    fDeltaPhi = kTwoPi;
+  } else {
+    fStartPhi = phiStart;
+    while (fStartPhi < 0) fStartPhi += kTwoPi;
+  }
+  double prevZ = z[0], prevRmax = 0, prevRmin = 0;
+  int dirZ = 1;
+  if (z[1] < z[0]) dirZ = -1;
+  for (int i = 0; i < nz; ++i) {
+    const double rMin = rin[i], rMax = rout[i], zz = z[i];
+    if (i > 0) {
+      if (((zz > prevZ + kTolerance) && (dirZ > 0)) || ((zz < prevZ - kTolerance) && (dirZ < 0))) {
+        const double dz = (zz - prevZ) / 2;
+        fSolids.emplace_back(new Cone(prevRmin, prevRmax, rMin, rMax, dz, phiStart, phiTotal));
+        fZs.push_back(zz);
+        const int zi = (int)fZs.size() - 1;
+        fShift.push_back(fZs[zi - 1] + 0.5 * (fZs[zi] - fZs[zi - 1]));
+      }
+    } else {
+      fZs.push_back(zz);
+    }
+    prevZ    = zz;
+    prevRmin = rMin;
+    prevRmax = rMax;
+  }
+}
+
+// PolyconeStruct.h:246-253 GetSectionIndex
+int Polycone::GetSectionIndex(double zposition) const
+{
+  if (zposition < fZs[0]) return -1;
+  for (int i = 0; i < NSections(); ++i)
+    if (zposition >= fZs[i] && zposition <= fZs[i + 1]) return i;
+  return -2;
+}
+
+// PolyconeImplementation.h:58-79 GenericKernelForASection
+void Polycone::SectionKernel(int isect, Vec3 const &p, bool forInside, bool &cin, bool &cout) const
+{
+  if (isect < 0) {
+    cin  = false;
+    cout = true;
+    return;
+  }
+  fSolids[isect]->ContainsAndInside(Local(p, isect), forInside, cin, cout);
+}
+
+// PolyconeImplementation.h:103-147 GenericKernelForContainsAndInside
+void Polycone::ContainsAndInside(Vec3 const &p, bool forInside, bool &cin, bool &cout) const
+{
+  const int indexLow  = GetSectionIndex(p.z() - kTolerance);
+  const int indexHigh = GetSectionIndex(p.z() + kTolerance);
+  if (indexLow < 0 && indexHigh < 0) {
+    cout = true;
+    return;
+  }
+  if (indexLow < 0 && indexHigh == 0) {
+    SectionKernel(0, p, forInside, cin, cout);
+    return;
+  }
+  if (indexHigh < 0 && indexLow == (NSections() - 1)) {
+    SectionKernel(NSections() - 1, p, forInside, cin, cout);
+    return;
+  }
+  if (indexLow >= 0 && indexHigh >= 0) {
+    if (indexLow == indexHigh) {
+      SectionKernel(indexLow, p, forInside, cin, cout);
+      return;
+    }
+    bool inLow = false, outLow = false, inHigh = false, outHigh = false;
+    SectionKernel(indexLow, p, forInside, inLow, outLow);
+    SectionKernel(indexHigh, p, forInside, inHigh, outHigh);
+    const bool surfLow  = !inLow && !outLow;
+    const bool surfHigh = !inHigh && !outHigh;
+    if (surfLow && surfHigh) {
+      cin = true;
+      return;
+    }
+    if (outLow && outHigh) {
+      cout = true;
+      return;
+    }
+  }
+}
+
+int Polycone::Inside(Vec3 const &p) const
+{
+  bool cin = false, cout = false;
+  ContainsAndInside(p, true, cin, cout);
+  int r = kSurface;
+  if (cout) r = kOutside;
+  if (cin) r = kInside;
+  return r;
+}
+bool Polycone::Contains(Vec3 const &p) const
+{
+  bool cin = false, cout = false;
+  ContainsAndInside(p, false, cin, cout);
+  return !cout;
+}
+
+// PolyconeImplementation.h:148-180 DistanceToIn
+double Polycone::DistanceToIn(Vec3 const &p, Vec3 const &v, double smax) const
+{
+  double distance = kInfLength;
+  int increment   = (v.z() > 0) ? 1 : -1;
+  if (std::fabs(v.z()) < kTolerance) increment = 0;
+  int index = GetSectionIndex(p.z());
+  if (index == -1) index = 0;
+  if (index == -2) index = NSections() - 1;
+  do {
+    distance = fSolids[index]->DistanceToIn(Local(p, index), v, smax);
+    if (distance < kInfLength || !increment) break;
+    index += increment;
+  } while (index >= 0 && index < NSections());
+  return distance;
+}
+
+// PolyconeImplementation.h:181-300 DistanceToOut
+double Polycone::DistanceToOut(Vec3 const &point, Vec3 const &dir, double smax) const
+{
+  double distance = kInfLength;
+  Vec3 pn         = point;
+  if (NSections() == 1) return fSolids[0]->DistanceToOut(Local(point, 0), dir, smax);
+  const int indexLow  = GetSectionIndex(point.z() - kTolerance);
+  const int indexHigh = GetSectionIndex(point.z() + kTolerance);
+  int index           = 0;
+  if (indexLow < 0 && indexHigh < 0) {
+    return -1;
+  } else if (indexLow < 0 && indexHigh >= 0) {
+    index = indexHigh;
+    if (fSolids[index]->Inside(Local(point, index)) == kOutside) return -1;
+  } else if (indexLow != indexHigh && (indexLow >= 0)) {
+    if (fSolids[indexLow]->Inside(Local(point, indexLow)) == kOutside)
+      index = indexHigh;
+    else
+      index = indexLow;
+  } else {
+    index = indexLow;
+    if (index < 0) index = GetSectionIndex(point.z());
+  }
+  if (index < 0) return 0.;
+  if (fSolids[index]->Inside(Local(point, index)) == kOutside) return -1;
+  double totalDistance = 0.;
+  double dist;
+  int increment = (dir.z() > 0) ? 1 : -1;
+  if (std::fabs(dir.z()) < kTolerance) increment = 0;
+  int istep = 0;
+  do {
+    if ((totalDistance != 0) || (istep < 2)) {
+      pn = point + totalDistance * dir;
+      pn[2] -= fShift[index];
+      if (fSolids[index]->Inside(pn) == kOutside) break;
+    } else {
+      pn[2] -= fShift[index];
+    }
+    istep++;
+    dist = fSolids[index]->DistanceToOut(pn, dir, smax);
+    if (dist == -1) return distance;
+    if (std::fabs(dist) < 0.5 * kTolerance) {
+      int index1 = index;
+      if ((index > 0) && (index < NSections() - 1)) {
+        index1 += increment;
+      } else {
+        if ((index == 0) && (increment > 0)) index1 += increment;
+        if ((index == NSections() - 1) && (increment < 0)) index1 += increment;
+      }
+      Vec3 pte = point + (totalDistance + dist) * dir;
+      pte[2] -= fShift[index1];
+      const int inside22 = fSolids[index1]->Inside(pte);
+      if (inside22 == 3 || (increment == 0)) break;
+    }
+    totalDistance += dist;
+    index += increment;
+  } while (increment != 0 && index >= 0 && index < NSections());
+  return totalDistance;
+}
+
+// PolyconeImplementation.h:301-354 SafetyToIn
+double Polycone::SafetyToIn(Vec3 const &p) const
+{
+  int index  = GetSectionIndex(p.z());
+  bool needZ = false;
+  if (index < 0) {
+    needZ = true;
+    if (index == -1) index = 0;
+    if (index == -2) index = NSections() - 1;
+  }
+  double safety = fSolids[index]->SafetyToIn(Local(p, index));
+  if (needZ) return safety;
+  if (safety < kTolerance) return safety;
+  double minSafety = safety;
+  double zbase     = fZs[index + 1];
+  for (int i = index + 1; i < NSections(); ++i) {
+    const double dz = fZs[i] - zbase;
+    if (dz >= minSafety) break;
+    safety = fSolids[i]->SafetyToIn(Local(p, i));
+    if (safety < minSafety) minSafety = safety;
+  }
+  if (index > 0) {
+    zbase = fZs[index - 1];
+    for (int i = index - 1; i >= 0; --i) {
+      const double dz = zbase - fZs[i];
+      if (dz >= minSafety) break;
+      safety = fSolids[i]->SafetyToIn(Local(p, i));
+      if (safety < minSafety) minSafety = safety;
+    }
+  }
+  return minSafety;
+}
+
+// PolyconeImplementation.h:355-410 SafetyToOut
+double Polycone::SafetyToOut(Vec3 const &point) const
+{
+  bool compIn = false, compOut = false;
+  ContainsAndInside(point, true, compIn, compOut);
+  if (compOut) return -1;
+  const int index = GetSectionIndex(point.z());
+  if (index < 0) return -1;
+  double safety    = fSolids[index]->SafetyToOut(Local(point, index));
+  double minSafety = safety;
+  if (minSafety == kInfLength) return 0.;
+  if (minSafety < kTolerance) return 0.;
+  double zbase = fZs[index + 1];
+  for (int i = index + 1; i < NSections(); ++i) {
+    const double dz = fZs[i] - zbase;
+    if (dz >= minSafety) break;
+    safety = fSolids[i]->SafetyToIn(Local(point, i));
+    if (safety < minSafety) minSafety = safety;
+  }
+  if (index > 0) {
+    zbase = fZs[index - 1];
+    for (int i = index - 1; i >= 0; --i) {
+      const double dz = zbase - fZs[i];
+      if (dz >= minSafety) break;
+      safety = fSolids[i]->SafetyToIn(Local(point, i));
+      if (safety < minSafety) minSafety = safety;
+    }
+  }
+  return minSafety;
+}
+
+// source/UnplacedPolycone.cpp:865-902 Extent (the xy part is a cone's extent over the radius range)
+void Polycone::Extent(Vec3 &aMin, Vec3 &aMax) const
+{
+  double maxR = 0, minR = kInfLength;
+  for (auto const &s : fSolids) {
+    maxR = Max(maxR, Max(s->_frmax1, s->_frmax2));
+    minR = Min(minR, Min(s->_frmin1, s->_frmin2));
+  }
+  double zlo, zhi;
+  if (fZs[0] > fZs[NSections()]) {
+    zhi = fZs[0];
+    zlo = fZs[NSections()];
+  } else {
+    zlo = fZs[0];
+    zhi = fZs[NSections()];
+  }
+  Cone tempCone(minR, maxR, minR, maxR, 1, fStartPhi, fDeltaPhi);
+  tempCone.Extent(aMin, aMax);
+  aMin[2] = zlo;
+  aMax[2] = zhi;
+}
+
+// ====================================================================== Boolean subtraction
+// BooleanImplementation.h:64-72 Contains
+bool BooleanMinus::Contains(Vec3 const &p) const
+{
+  if (!fLeft->Contains(p)) return false;
+  return !fRight->Contains(p);
+}
+
+// BooleanImplementation.h:73-107 Inside
+int BooleanMinus::Inside(Vec3 const &p) const
+{
+  const int a = fLeft->Inside(p);
+  if (a == kOutside) return kOutside;
+  const int b = fRight->Inside(p);
+  if (a == kInside && b == kOutside) return kInside;
+  if ((a == kInside && b == kSurface) || (b == kOutside && a == kSurface)) return kSurface;
+  return kOutside;
+}
+
+// BooleanImplementation.h:108-147 DistanceToIn (push loop with kPushTolerance)
+double BooleanMinus::DistanceToIn(Vec3 const &p, Vec3 const &dir, double stepMax) const
+{
+  double d1, d2, snxt = 0.;
+  Vec3 hitpoint      = p;
+  bool insideRight   = fRight->Contains(p);
+  const double epsil = kPushTolerance;
+  while (true) {
+    if (insideRight) {
+      d1 = fRight->PlacedDistanceToOut(hitpoint, dir, stepMax);
+      snxt += (d1 >= 0. && d1 < kInfLength) ? (d1 + epsil) : 0.;
+      hitpoint = hitpoint + ((d1 >= 0. && d1 < kInfLength) ? (d1 + epsil) * dir : 0. * dir);
+      if (fLeft->Contains(hitpoint)) {
+        const double check = fLeft->PlacedDistanceToOut(hitpoint, dir, kInfLength);
+        if (check > epsil) return snxt;
+      }
+    }
+    d2 = fLeft->DistanceToIn(hitpoint, dir, stepMax);
+    d2 = Max(d2, 0.);
+    if (d2 == kInfLength) return kInfLength;
+    d1 = fRight->DistanceToIn(hitpoint, dir, stepMax);
+    if (d2 < d1 - kTolerance) {
+      snxt += d2 + epsil;
+      return snxt;
+    }
+    snxt += (d1 >= 0. && d1 < kInfLength) ? d1 + epsil : 0.;
+    hitpoint    = hitpoint + ((d1 >= 0. && d1 < kInfLength) ? (d1 + epsil) * dir : epsil * dir);
+    insideRight = true;
+  }
+}
+
+// BooleanImplementation.h:148-157 DistanceToOut
+double BooleanMinus::DistanceToOut(Vec3 const &p, Vec3 const &d, double stepMax) const
+{
+  const double distancel = fLeft->PlacedDistanceToOut(p, d, stepMax);
+  const double dinright  = fRight->DistanceToIn(p, d, stepMax);
+  return Min(distancel, dinright);
+}
+
+// BooleanImplementation.h:158-170 SafetyToIn
+double BooleanMinus::SafetyToIn(Vec3 const &p) const
+{
+  if (fLeft->Contains(p) && fRight->Contains(p)) return fRight->SafetyToOut(fRight->T.Transform(p));
+  return fLeft->SafetyToIn(p);
+}
+
+// BooleanImplementation.h:171-178 SafetyToOut (the left operand is queried in the
+// boolean's own frame, as the reference does)
+double BooleanMinus::SafetyToOut(Vec3 const &p) const
+{
+  const double sl = fLeft->SafetyToOut(p);
+  const double sr = fRight->SafetyToIn(p);
+  return Min(sl, sr);
+}
+
+// source/UnplacedBooleanVolume.cpp:403-458 TransformedExtent of the left operand
+void BooleanMinus::Extent(Vec3 &aMin, Vec3 &aMax) const
+{
+  Vec3 lower, upper;
+  fLeft->Shape()->Extent(lower, upper);
+  const Vec3 delta = upper - lower;
+  double mn[3] = {kInfLength, kInfLength, kInfLength}, mx[3] = {-kInfLength, -kInfLength, -kInfLength};
+  for (int x = 0; x <= 1; ++x)
+    for (int y = 0; y <= 1; ++y)
+      for (int z = 0; z <= 1; ++z) {
+        Vec3 c(lower.x() + x * delta.x(), lower.y() + y * delta.y(), lower.z() + z * delta.z());
+        const Vec3 t = fLeft->T.InverseTransform(c);
+        for (int k = 0; k < 3; ++k) {
+          mn[k] = std::min(mn[k], t[k]);
+          mx[k] = std::max(mx[k], t[k]);
+        }
+      }
+  aMin = Vec3(mn[0], mn[1], mn[2]);
+  aMax = Vec3(mx[0], mx[1], mx[2]);
+}
+
+} // namespace oracle

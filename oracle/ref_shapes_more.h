@@ -1,0 +1,85 @@
+// ORACLE — TEST INFRASTRUCTURE ONLY (see ref_base.h).
+// Trd, Polycone, Polyhedron, Torus2 and the boolean subtraction.
+#pragma once
+#include "ref_shapes.h"
+#include <memory>
+#include <vector>
+
+namespace oracle {
+
+struct PlacedVolume;
+
+// VecGeom/volumes/TrdStruct.h, VecGeom/volumes/kernel/TrdImplementation.h (UniversalTrd)
+struct Trd : UnplacedShape {
+  double fDX1, fDX2, fDY1, fDY2, fDZ;
+  double fX2minusX1, fY2minusY1, fHalfX1plusX2, fHalfY1plusY2, fCalfX, fCalfY, fSecxz, fSecyz;
+  double fToleranceX, fToleranceY, fFx, fFy;
+  Trd(double x1, double x2, double y1, double y2, double z);
+  bool VaryingY() const { return fDY1 != fDY2; }
+  void UnplacedInside(Vec3 const &p, bool surfaceT, bool &cin, bool &cout) const;
+  void Face(Vec3 const &pos, Vec3 const &dir, bool forY, bool mirrored, bool toInside, double &dist, bool &ok) const;
+  double Safety(Vec3 const &p, bool inside) const;
+  int Inside(Vec3 const &p) const override;
+  bool Contains(Vec3 const &p) const override;
+  double DistanceToIn(Vec3 const &p, Vec3 const &d, double) const override;
+  double DistanceToOut(Vec3 const &p, Vec3 const &d, double) const override;
+  double SafetyToIn(Vec3 const &p) const override { return Safety(p, false); }
+  double SafetyToOut(Vec3 const &p) const override { return Safety(p, true); }
+  void Extent(Vec3 &lo, Vec3 &hi) const override;
+};
+
+// VecGeom/volumes/PolyconeStruct.h (Init), VecGeom/volumes/kernel/PolyconeImplementation.h
+struct Polycone : UnplacedShape {
+  double fStartPhi = 0, fDeltaPhi = 0;
+  std::vector<std::unique_ptr<Cone>> fSolids;
+  std::vector<double> fShift;
+  std::vector<double> fZs;
+  Polycone(double phiStart, double phiTotal, int nz, const double *z, const double *rmin, const double *rmax);
+  int NSections() const { return (int)fSolids.size(); }
+  int GetSectionIndex(double z) const;
+  Vec3 Local(Vec3 const &p, int i) const { return Vec3(p.x(), p.y(), p.z() - fShift[i]); }
+  void SectionKernel(int isect, Vec3 const &p, bool forInside, bool &cin, bool &cout) const;
+  void ContainsAndInside(Vec3 const &p, bool forInside, bool &cin, bool &cout) const;
+  int Inside(Vec3 const &p) const override;
+  bool Contains(Vec3 const &p) const override;
+  double DistanceToIn(Vec3 const &p, Vec3 const &d, double) const override;
+  double DistanceToOut(Vec3 const &p, Vec3 const &d, double) const override;
+  double SafetyToIn(Vec3 const &p) const override;
+  double SafetyToOut(Vec3 const &p) const override;
+  void Extent(Vec3 &lo, Vec3 &hi) const override;
+};
+
+// VecGeom/volumes/kernel/BooleanImplementation.h (kSubtraction); operands are placed volumes.
+struct BooleanMinus : UnplacedShape {
+  PlacedVolume const *fLeft, *fRight;
+  BooleanMinus(PlacedVolume const *l, PlacedVolume const *r) : fLeft(l), fRight(r) {}
+  int Inside(Vec3 const &p) const override;
+  bool Contains(Vec3 const &p) const override;
+  double DistanceToIn(Vec3 const &p, Vec3 const &d, double smax) const override;
+  double DistanceToOut(Vec3 const &p, Vec3 const &d, double smax) const override;
+  double SafetyToIn(Vec3 const &p) const override;
+  double SafetyToOut(Vec3 const &p) const override;
+  void Extent(Vec3 &lo, Vec3 &hi) const override;
+};
+
+} // namespace oracle
+
+namespace oracle {
+// VecGeom/volumes/TorusStruct2.h, VecGeom/volumes/kernel/TorusImplementation2.h
+struct Torus2 : UnplacedShape {
+  double fRmin, fRmax, fRtor, fSphi, fDphi, fRmin2, fRmax2, fRtor2;
+  Wedge fPhiWedge;
+  Tube fBoundingTube;
+  Torus2(double rmin, double rmax, double rtor, double sphi, double dphi);
+  void ContainsAndInside(Vec3 const &p, bool forInside, bool notForDisk, bool &cin, bool &cout) const;
+  double ToBoundary(Vec3 const &pt, Vec3 const &dir, double radius, bool out) const;
+  double DistSqrToTorusR(Vec3 const &p, Vec3 const &d, double dist) const;
+  int Inside(Vec3 const &p) const override;
+  bool Contains(Vec3 const &p) const override;
+  double DistanceToIn(Vec3 const &p, Vec3 const &d, double smax) const override;
+  double DistanceToOut(Vec3 const &p, Vec3 const &d, double smax) const override;
+  double SafetyToIn(Vec3 const &p) const override;
+  double SafetyToOut(Vec3 const &p) const override;
+  void Extent(Vec3 &lo, Vec3 &hi) const override { fBoundingTube.Extent(lo, hi); }
+};
+} // namespace oracle

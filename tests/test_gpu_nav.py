@@ -103,3 +103,63 @@ def test_transport_sequence_matches(cuda, barrel):
         ref_st = np.where(alive, ref_out, ref_st)
         st_h = ref_st.copy()
         st = cuda.from_numpy(st_h.view(np.uint8).reshape(-1).copy()).to("cuda:0")
+
+
+@pytest.fixture(scope="module")
+def detector(cuda):
+    import vecgeom_gb300 as vg
+    from oracle.oracle import OracleGeometry
+    from vecgeom_gb300 import workloads as W
+
+    g, o = vg.Geometry(), OracleGeometry()
+    W.build_detector(g)
+    W.build_detector(o)
+    return g, o
+
+
+def test_detector_locate_step_transport(cuda, detector):
+    """Config-4 detector (150k box modules, Polycone holders with Trd wedges): straight
+    tracks from the origin are transported step by step; every step's state and length
+    agree with the oracle."""
+    from vecgeom_gb300 import workloads as W
+    g, o = detector
+    n = 8192
+    (x, y, z), dirs = W.primaries_eta_phi(n, seed=51)
+    st, st_h = gpu_locate(cuda, g, (x, y, z))
+    ref_st, _ = o.locate(x, y, z)
+    assert np.array_equal(st_h, ref_st)
+    for k in range(40):
+        alive = ref_st["nav_ind"] != 0
+        if not alive.any():
+            break
+        out, step, status = gpu_step(cuda, g, (x, y, z), dirs, st)
+        ref_out, ref_step, _, _ = o.step(x, y, z, *dirs, ref_st, nthreads=8)
+        assert (status[alive] == 0).all()
+        assert np.array_equal(out[alive], ref_out[alive]), k
+        assert not dist_mismatch(step[alive], ref_step[alive]).any(), k
+        x = np.where(alive, x + ref_step * dirs[0], x)
+        y = np.where(alive, y + ref_step * dirs[1], y)
+        z = np.where(alive, z + ref_step * dirs[2], z)
+        ref_st = np.where(alive, ref_out, ref_st)
+        st = cuda.from_numpy(ref_st.view(np.uint8).reshape(-1).copy()).to("cuda:0")
+
+
+def test_detector_random_points(cuda, detector):
+    """Track starts spread over the detector volume (barrel and endcaps)."""
+    from vecgeom_gb300 import workloads as W
+    g, o = detector
+    n = 1 << 16
+    gg = W.rng(61, 1)
+    r = 1150.0 * np.sqrt(gg.random(n))
+    ph = 2 * np.pi * gg.random(n)
+    z = 2950.0 * (2 * gg.random(n) - 1)
+    pts = (r * np.cos(ph), r * np.sin(ph), z)
+    dirs = W.isotropic(W.rng(61, 2), n)
+    st, st_h = gpu_locate(cuda, g, pts)
+    ref_st, _ = o.locate(*pts, nthreads=8)
+    assert np.array_equal(st_h, ref_st)
+    out, step, status = gpu_step(cuda, g, pts, dirs, st)
+    ref_out, ref_step, _, _ = o.step(*pts, *dirs, ref_st, nthreads=8)
+    assert (status == 0).all()
+    assert np.array_equal(out, ref_out)
+    assert not dist_mismatch(step, ref_step).any()

@@ -125,3 +125,33 @@ def test_placed_transform_parity(cuda):
     assert np.array_equal(got[0], ref[0])
     for q in (2, 3, 4, 5):
         assert not dist_mismatch(got[q], ref[q]).any(), q
+
+
+# Stated per-shape tolerance of the FP64 path against the FP64 oracle. Torus2's cubic
+# resolvent calls cbrt/pow/cos/atan2, whose CUDA and libm results differ in the last ulps;
+# the Newton polish then stops within kTolerance (1e-9 mm) of the root, so its distances are
+# compared at 1e-8 mm. Every other shape uses only +,-,*,/ and sqrt and meets 1e-9 + 1e-12 rel.
+CFG2_TOL = {"torus2": 1e-8}
+
+
+@pytest.mark.parametrize("name", ["tube_phi", "polycone", "torus2", "trd", "box_minus_tube"])
+def test_cfg2_shape_parity(cuda, name):
+    import vecgeom_gb300 as vg
+    from oracle.oracle import OracleGeometry
+    from vecgeom_gb300 import workloads as W
+
+    kind, params = W.SHAPES_CFG2[name]
+    g, o = vg.Geometry(), OracleGeometry()
+    s, pv = W.build_single_shape(g, kind, params)
+    W.build_single_shape(o, kind, params)
+    lo, hi = g.shape_extent(s)
+    pts, dirs = W.shape_points_mixed(lo, hi, 3 * 8192, 77, lambda x, y, z: o.query(pv, 0, x, y, z)[0],
+                                     lambda *a: o.query(pv, 3, *a)[0])
+    got = run_all_queries(cuda, g, pv, pts, dirs)
+    ref = oracle_all(o, pv, pts, dirs)
+    tol = CFG2_TOL.get(name, 1e-9)
+    assert np.array_equal(got[0], ref[0]), ("Inside", int((got[0] != ref[0]).sum()))
+    assert np.array_equal(got[1], ref[1]), ("Contains", int((got[1] != ref[1]).sum()))
+    for q in (2, 3, 4, 5):
+        bad = dist_mismatch(got[q], ref[q], abs_tol=tol)
+        assert not bad.any(), (q, int(bad.sum()), got[q][bad][:4], ref[q][bad][:4])

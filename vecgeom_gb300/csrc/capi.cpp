@@ -76,9 +76,13 @@ int placed_query(const vg_geom *g, int32_t pv, int q, const double *x, const dou
   if (n > 0 && (!x || !y || !z || !out || ((q == kQDistIn || q == kQDistOut) && (!dx || !dy || !dz))))
     return fail(VG_EINVAL, "null input/output array");
   const int32_t shape = geo.lvs[geo.pvs[pv].lv].shape;
+  const int32_t type  = geo.shapes[shape].type;
   vg::QueryArgs a{x, y, z, dx, dy, dz, n, out};
-  const cudaError_t e = vg::launch_shape_query_fp64(geo.shapes[shape].type, geo.shape_rec(shape),
-                                                    geo.pvs[pv].xf.m, 1, q, a, (cudaStream_t)stream);
+  const bool composite = type == vg::kShapePolycone || type == vg::kShapePolyhedron || type == vg::kShapeBoolMinus;
+  const cudaError_t e  = composite ? vg::launch_shape_query_dyn_fp64(geo.dev, shape, geo.pvs[pv].xf.m, q, a,
+                                                                    (cudaStream_t)stream)
+                                  : vg::launch_shape_query_fp64(type, geo.shape_rec(shape), geo.pvs[pv].xf.m, 1, q,
+                                                                a, (cudaStream_t)stream);
   if (e == cudaErrorNotSupported) return fail(VG_EINVAL, "shape type not supported by this query path");
   return e == cudaSuccess ? VG_OK : cuda_fail(e, "shape query launch");
 }

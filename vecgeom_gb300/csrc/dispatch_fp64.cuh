@@ -1,51 +1,177 @@
-// Run-time shape dispatch for the navigator (one switch per query on the shape tag of
-// the flattened record). The per-shape SoA kernels do not use it: they are instantiated
-// per shape type.
+// Run-time shape dispatch (one switch per query on the shape tag of the flattened record)
+// used by the navigator and by the SoA kernel of variable-length shapes, plus the boolean
+// subtraction, whose operands are placed primitive shapes.
 #pragma once
 #include "shapes_fp64.cuh"
+#include "shapes_more_fp64.cuh"
+#include "shapes_torus_fp64.cuh"
 
 namespace vg {
+
+
 namespace f64 {
 
-#define VG_SHAPE_CASES(FN, ...)                                                     \
-  switch (g.shape_type[shape]) {                                                    \
-  case kShapeBox: return box_##FN(rec<BoxRec>(g, shape), __VA_ARGS__);              \
-  case kShapeTube: return tube_##FN(rec<TubeRec>(g, shape), __VA_ARGS__);           \
-  case kShapeCone: return cone_##FN(rec<ConeRec>(g, shape), __VA_ARGS__);           \
-  default: break;                                                                   \
+#define VG_PRIM_CASES(FN, ...)                                                               \
+  switch (g.shape_type[shape]) {                                                             \
+  case kShapeBox: return box_##FN(rec<BoxRec>(g, shape), __VA_ARGS__);                       \
+  case kShapeTube: return tube_##FN(rec<TubeRec>(g, shape), __VA_ARGS__);                    \
+  case kShapeCone: return cone_##FN(rec<ConeRec>(g, shape), __VA_ARGS__);                    \
+  case kShapeTrd: return trd_##FN(rec<TrdRec>(g, shape), __VA_ARGS__);                       \
+  case kShapePolycone: return polycone_##FN(rec<PolyconeRec>(g, shape), __VA_ARGS__);        \
+  case kShapeTorus2: return torus_##FN(rec<TorusRec>(g, shape), __VA_ARGS__);                \
+  default: break;                                                                            \
   }
 
+__device__ inline bool prim_contains(const DevGeom &g, int shape, V3 p)
+{
+  VG_PRIM_CASES(contains, p)
+  return false;
+}
+__device__ inline int prim_inside(const DevGeom &g, int shape, V3 p)
+{
+  VG_PRIM_CASES(inside, p)
+  return kOutside;
+}
+__device__ inline double prim_dist_in(const DevGeom &g, int shape, V3 p, V3 d)
+{
+  VG_PRIM_CASES(dist_in, p, d)
+  return kInfLength;
+}
+__device__ inline double prim_dist_out(const DevGeom &g, int shape, V3 p, V3 d)
+{
+  VG_PRIM_CASES(dist_out, p, d)
+  return -1.;
+}
+__device__ inline double prim_safety_in(const DevGeom &g, int shape, V3 p)
+{
+  VG_PRIM_CASES(safety_in, p)
+  return kInfLength;
+}
+__device__ inline double prim_safety_out(const DevGeom &g, int shape, V3 p)
+{
+  VG_PRIM_CASES(safety_out, p)
+  return -1.;
+}
+#undef VG_PRIM_CASES
+
+// ---------------------------------------------------------------- boolean subtraction
+// Placed-operand helpers (SpecializedPlacedVolImplHelper.h:98-170): mother-frame input.
+struct Operand {
+  const Xform *xf;
+  int shape;
+  __device__ Operand(const DevGeom &g, double pv) : xf(&g.pv_xf[(int)pv]), shape(g.lv_shape[g.pv_lv[(int)pv]]) {}
+  __device__ bool contains(const DevGeom &g, V3 p) const { return prim_contains(g, shape, to_local(*xf, p)); }
+  __device__ int inside(const DevGeom &g, V3 p) const { return prim_inside(g, shape, to_local(*xf, p)); }
+  __device__ double dist_in(const DevGeom &g, V3 p, V3 d) const
+  {
+    return prim_dist_in(g, shape, to_local(*xf, p), rotate(*xf, d));
+  }
+  __device__ double placed_dist_out(const DevGeom &g, V3 p, V3 d) const
+  {
+    return prim_dist_out(g, shape, to_local(*xf, p), rotate(*xf, d));
+  }
+};
+
+// BooleanImplementation.h:64-72
+__device__ inline bool boolminus_contains(const DevGeom &g, const BoolRec &b, V3 p)
+{
+  if (!Operand(g, b.left_pv).contains(g, p)) return false;
+  return !Operand(g, b.right_pv).contains(g, p);
+}
+// BooleanImplementation.h:73-107
+__device__ inline int boolminus_inside(const DevGeom &g, const BoolRec &b, V3 p)
+{
+  const int a = Operand(g, b.left_pv).inside(g, p);
+  if (a == kOutside) return kOutside;
+  const int c = Operand(g, b.right_pv).inside(g, p);
+  if (a == kInside && c == kOutside) return kInside;
+  if ((a == kInside && c == kSurface) || (c == kOutside && a == kSurface)) return kSurface;
+  return kOutside;
+}
+// BooleanImplementation.h:108-147 (push loop bounded by kBoolMaxPush; a track that hits the
+// bound gets kInfLength)
+__device__ inline double boolminus_dist_in(const DevGeom &g, const BoolRec &b, V3 p, V3 dir)
+{
+  const Operand L(g, b.left_pv), R(g, b.right_pv);
+  double snxt = 0.;
+  V3 hit      = p;
+  bool inR    = R.contains(g, p);
+  for (int it = 0; it < kBoolMaxPush; ++it) {
+    if (inR) {
+      const double d1 = R.placed_dist_out(g, hit, dir);
+      const bool okd  = d1 >= 0. && d1 < kInfLength;
+      snxt += okd ? (d1 + kPushTolerance) : 0.;
+      const double s = okd ? (d1 + kPushTolerance) : 0.;
+      hit            = V3{hit.x + s * dir.x, hit.y + s * dir.y, hit.z + s * dir.z};
+      if (L.contains(g, hit) && L.placed_dist_out(g, hit, dir) > kPushTolerance) return snxt;
+    }
+    double d2 = L.dist_in(g, hit, dir);
+    d2        = dmax(d2, 0.);
+    if (d2 == kInfLength) return kInfLength;
+    const double d1 = R.dist_in(g, hit, dir);
+    if (d2 < d1 - kTolerance) return snxt + (d2 + kPushTolerance);
+    const bool okd = d1 >= 0. && d1 < kInfLength;
+    snxt += okd ? d1 + kPushTolerance : 0.;
+    const double s = okd ? (d1 + kPushTolerance) : kPushTolerance;
+    hit            = V3{hit.x + s * dir.x, hit.y + s * dir.y, hit.z + s * dir.z};
+    inR            = true;
+  }
+  return kInfLength;
+}
+// BooleanImplementation.h:148-157
+__device__ inline double boolminus_dist_out(const DevGeom &g, const BoolRec &b, V3 p, V3 d)
+{
+  const double dl = Operand(g, b.left_pv).placed_dist_out(g, p, d);
+  const double dr = Operand(g, b.right_pv).dist_in(g, p, d);
+  return dmin(dl, dr);
+}
+// BooleanImplementation.h:158-170
+__device__ inline double boolminus_safety_in(const DevGeom &g, const BoolRec &b, V3 p)
+{
+  const Operand L(g, b.left_pv), R(g, b.right_pv);
+  if (L.contains(g, p) && R.contains(g, p)) return prim_safety_out(g, R.shape, to_local(*R.xf, p));
+  return prim_safety_in(g, L.shape, to_local(*L.xf, p));
+}
+// BooleanImplementation.h:171-178 (left operand queried in the boolean's frame)
+__device__ inline double boolminus_safety_out(const DevGeom &g, const BoolRec &b, V3 p)
+{
+  const Operand L(g, b.left_pv), R(g, b.right_pv);
+  const double sl = prim_safety_out(g, L.shape, p);
+  const double sr = prim_safety_in(g, R.shape, to_local(*R.xf, p));
+  return dmin(sl, sr);
+}
+
+// ---------------------------------------------------------------- full dispatch
 __device__ inline bool shape_contains(const DevGeom &g, int shape, V3 p)
 {
-  VG_SHAPE_CASES(contains, p)
-  return false;
+  if (g.shape_type[shape] == kShapeBoolMinus) return boolminus_contains(g, rec<BoolRec>(g, shape), p);
+  return prim_contains(g, shape, p);
 }
 __device__ inline int shape_inside(const DevGeom &g, int shape, V3 p)
 {
-  VG_SHAPE_CASES(inside, p)
-  return kOutside;
+  if (g.shape_type[shape] == kShapeBoolMinus) return boolminus_inside(g, rec<BoolRec>(g, shape), p);
+  return prim_inside(g, shape, p);
 }
 __device__ inline double shape_dist_in(const DevGeom &g, int shape, V3 p, V3 d)
 {
-  VG_SHAPE_CASES(dist_in, p, d)
-  return kInfLength;
+  if (g.shape_type[shape] == kShapeBoolMinus) return boolminus_dist_in(g, rec<BoolRec>(g, shape), p, d);
+  return prim_dist_in(g, shape, p, d);
 }
 __device__ inline double shape_dist_out(const DevGeom &g, int shape, V3 p, V3 d)
 {
-  VG_SHAPE_CASES(dist_out, p, d)
-  return -1.;
+  if (g.shape_type[shape] == kShapeBoolMinus) return boolminus_dist_out(g, rec<BoolRec>(g, shape), p, d);
+  return prim_dist_out(g, shape, p, d);
 }
 __device__ inline double shape_safety_in(const DevGeom &g, int shape, V3 p)
 {
-  VG_SHAPE_CASES(safety_in, p)
-  return kInfLength;
+  if (g.shape_type[shape] == kShapeBoolMinus) return boolminus_safety_in(g, rec<BoolRec>(g, shape), p);
+  return prim_safety_in(g, shape, p);
 }
 __device__ inline double shape_safety_out(const DevGeom &g, int shape, V3 p)
 {
-  VG_SHAPE_CASES(safety_out, p)
-  return -1.;
+  if (g.shape_type[shape] == kShapeBoolMinus) return boolminus_safety_out(g, rec<BoolRec>(g, shape), p);
+  return prim_safety_out(g, shape, p);
 }
-#undef VG_SHAPE_CASES
 
 } // namespace f64
 } // namespace vg

@@ -262,6 +262,117 @@ void make_cone(const double *p, HostShape &s)
   phi_section_extent(c.w, c.sphi, c.dphi, rin, rout, c.dz, s.lo, s.hi);
 }
 
+// TrdStruct.h:68-86 CalculateCached (the y tolerance uses the x extent, as the reference does)
+void make_trd(const double *p, HostShape &s)
+{
+  TrdRec t{};
+  t.dx1 = p[0], t.dx2 = p[1], t.dy1 = p[2], t.dy2 = p[3], t.dz = p[4];
+  t.x2minusx1    = t.dx2 - t.dx1;
+  t.y2minusy1    = t.dy2 - t.dy1;
+  t.halfx1plusx2 = 0.5 * (t.dx1 + t.dx2);
+  t.halfy1plusy2 = 0.5 * (t.dy1 + t.dy2);
+  t.fx           = 0.5 * (t.dx1 - t.dx2) / t.dz;
+  t.fy           = 0.5 * (t.dy1 - t.dy2) / t.dz;
+  t.calfx        = 1. / std::sqrt(1.0 + t.fx * t.fx);
+  t.calfy        = 1. / std::sqrt(1.0 + t.fy * t.fy);
+  t.tolx         = kTolerance * std::sqrt(t.x2minusx1 * t.x2minusx1 + 4 * t.dz * t.dz);
+  t.toly         = kTolerance * std::sqrt(t.x2minusx1 * t.x2minusx1 + 4 * t.dz * t.dz);
+  s.type         = kShapeTrd;
+  pack(s, t);
+  const double mx = t.dx1 > t.dx2 ? t.dx1 : t.dx2, my = t.dy1 > t.dy2 ? t.dy1 : t.dy2;
+  s.lo[0] = -mx, s.lo[1] = -my, s.lo[2] = -t.dz;
+  s.hi[0] = mx, s.hi[1] = my, s.hi[2] = t.dz;
+}
+
+// PolyconeStruct.h:124-239 Init: one ConeStruct(prevRmin, prevRmax, rMin, rMax, dz, phiStart,
+// phiTotal) per z interval longer than kTolerance, shifted to the interval's middle.
+bool make_polycone(const double *p, int np, HostShape &s, std::string &err)
+{
+  const double phiStart = p[0], phiTotal = p[1];
+  const int nz = (int)p[2];
+  if (nz < 2 || np < 3 + 3 * nz) {
+    err = "polycone needs at least 2 z planes";
+    return false;
+  }
+  const double *zPlane = p + 3, *rInner = p + 3 + nz, *rOuter = p + 3 + 2 * nz;
+  std::vector<double> z(zPlane, zPlane + nz), rin(rInner, rInner + nz), rout(rOuter, rOuter + nz);
+  if (zPlane[0] > zPlane[nz - 1])
+    for (int i = 0; i < nz; ++i) z[i] = zPlane[nz - 1 - i], rin[i] = rInner[nz - 1 - i], rout[i] = rOuter[nz - 1 - i];
+  double deltaPhi = 0, startPhi = 0;
+  if (phiTotal <= 0. || phiTotal > kTwoPi - kTolerance) {
+    startPhi = 0;
+    deltaPhi = kTwoPi;
+  } else {
+    deltaPhi = phiTotal;
+    startPhi = phiStart;
+    while (startPhi < 0) startPhi += kTwoPi;
+  }
+  std::vector<double> zs, shifts;
+  std::vector<HostShape> cones;
+  double prevZ = z[0], prevRmax = 0, prevRmin = 0;
+  const int dirZ = z[1] < z[0] ? -1 : 1;
+  double maxR = 0, minR = kInfLength;
+  for (int i = 0; i < nz; ++i) {
+    if (i > 0) {
+      if (((z[i] > prevZ + kTolerance) && dirZ > 0) || ((z[i] < prevZ - kTolerance) && dirZ < 0)) {
+        const double cp[7] = {prevRmin, prevRmax, rin[i], rout[i], (z[i] - prevZ) / 2, phiStart, phiTotal};
+        HostShape c;
+        make_cone(cp, c);
+        cones.push_back(std::move(c));
+        zs.push_back(z[i]);
+        const size_t zi = zs.size() - 1;
+        shifts.push_back(zs[zi - 1] + 0.5 * (zs[zi] - zs[zi - 1]));
+        const ConeRec &cr = *reinterpret_cast<const ConeRec *>(cones.back().rec.data());
+        maxR = std::max(maxR, std::max(cr.frmax1, cr.frmax2));
+        minR = std::min(minR, std::min(cr.frmin1, cr.frmin2));
+      }
+    } else {
+      zs.push_back(z[i]);
+    }
+    prevZ = z[i], prevRmin = rin[i], prevRmax = rout[i];
+  }
+  const int nsec = (int)cones.size();
+  if (nsec < 1) {
+    err = "polycone has no section longer than the tolerance";
+    return false;
+  }
+  const int base = polycone_section_base(nsec);
+  std::vector<double> r(base + nsec * kPolyconeSectionDoubles, 0.);
+  r[0] = nsec, r[1] = startPhi, r[2] = deltaPhi;
+  for (int i = 0; i <= nsec; ++i) r[4 + i] = zs[i];
+  for (int i = 0; i < nsec; ++i) {
+    double *sec = r.data() + base + i * kPolyconeSectionDoubles;
+    sec[0]      = shifts[i];
+    std::memcpy(sec + 4, cones[i].rec.data(), sizeof(ConeRec));
+  }
+  s.type = kShapePolycone;
+  s.rec  = std::move(r);
+  // source/UnplacedPolycone.cpp:865-902: xy extent of a Cone(minR, maxR, minR, maxR, 1, sphi, dphi)
+  const double tp[7] = {minR, maxR, minR, maxR, 1, startPhi, deltaPhi};
+  HostShape tmp;
+  make_cone(tp, tmp);
+  for (int k = 0; k < 2; ++k) s.lo[k] = tmp.lo[k], s.hi[k] = tmp.hi[k];
+  s.lo[2] = zs[0] > zs[nsec] ? zs[nsec] : zs[0];
+  s.hi[2] = zs[0] > zs[nsec] ? zs[0] : zs[nsec];
+  return true;
+}
+
+// TorusStruct2.h:36-43; bounding tube from UnplacedTorus2.h:64-74
+void make_torus2(const double *p, HostShape &s)
+{
+  TorusRec t{};
+  t.rmin = p[0], t.rmax = p[1], t.rtor = p[2], t.sphi = p[3], t.dphi = p[4];
+  t.rmin2 = t.rmin * t.rmin, t.rmax2 = t.rmax * t.rmax, t.rtor2 = t.rtor * t.rtor;
+  t.w                = make_wedge(t.dphi, t.sphi);
+  const double bp[5] = {t.rtor - t.rmax - kTolerance, t.rtor + t.rmax + kTolerance, t.rmax, t.sphi, t.dphi};
+  HostShape bt;
+  make_tube(bp, bt);
+  std::memcpy(&t.bt, bt.rec.data(), sizeof(TubeRec));
+  s.type = kShapeTorus2;
+  pack(s, t);
+  for (int k = 0; k < 3; ++k) s.lo[k] = bt.lo[k], s.hi[k] = bt.hi[k];
+}
+
 // ---------------------------------------------------------------- registry
 Geometry::~Geometry()
 {
@@ -295,6 +406,49 @@ int32_t Geometry::add_shape(int32_t type, const double *p, int np, std::string &
     if (!need(7)) return -1;
     make_cone(p, s);
     break;
+  case kShapeTrd:
+    if (!need(5)) return -1;
+    make_trd(p, s);
+    break;
+  case kShapeTorus2:
+    if (!need(5)) return -1;
+    make_torus2(p, s);
+    break;
+  case kShapePolycone:
+    if (!need(3) || !make_polycone(p, np, s, err)) return -1;
+    break;
+  case kShapeBoolMinus: {
+    if (!need(2)) return -1;
+    const int32_t l = (int32_t)p[0], r = (int32_t)p[1];
+    if (l < 0 || r < 0 || l >= (int32_t)pvs.size() || r >= (int32_t)pvs.size()) {
+      err = "invalid boolean operand placed-volume id";
+      return -1;
+    }
+    for (int32_t op : {l, r})
+      if (shapes[lvs[pvs[op].lv].shape].type == kShapeBoolMinus) {
+        err = "boolean operands must be primitive shapes";
+        return -1;
+      }
+    BoolRec b{(double)l, (double)r, 0., 0.};
+    s.type     = kShapeBoolMinus;
+    s.left_pv  = l;
+    s.right_pv = r;
+    pack(s, b);
+    // source/UnplacedBooleanVolume.cpp:403-458: extent of the left operand in this frame
+    HostShape const &ls = shapes[lvs[pvs[l].lv].shape];
+    const double delta[3] = {ls.hi[0] - ls.lo[0], ls.hi[1] - ls.lo[1], ls.hi[2] - ls.lo[2]};
+    double mn[3] = {kInfLength, kInfLength, kInfLength}, mx[3] = {-kInfLength, -kInfLength, -kInfLength};
+    for (int x = 0; x <= 1; ++x)
+      for (int y = 0; y <= 1; ++y)
+        for (int z = 0; z <= 1; ++z) {
+          const double c[3] = {ls.lo[0] + x * delta[0], ls.lo[1] + y * delta[1], ls.lo[2] + z * delta[2]};
+          double t[3];
+          pvs[l].xf.InverseTransform(c, t);
+          for (int k = 0; k < 3; ++k) mn[k] = std::min(mn[k], t[k]), mx[k] = std::max(mx[k], t[k]);
+        }
+    for (int k = 0; k < 3; ++k) s.lo[k] = mn[k], s.hi[k] = mx[k];
+    break;
+  }
   default:
     err = "unknown shape type " + std::to_string(type);
     return -1;

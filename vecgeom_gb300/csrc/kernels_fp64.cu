@@ -33,6 +33,8 @@ struct ShapeOps;
 VG_OPS(BoxRec, box)
 VG_OPS(TubeRec, tube)
 VG_OPS(ConeRec, cone)
+VG_OPS(TrdRec, trd)
+VG_OPS(TorusRec, torus)
 #undef VG_OPS
 
 // Q: 0 Inside, 1 Contains, 2 DistanceToIn, 3 DistanceToOut, 4 SafetyToIn, 5 SafetyToOut
@@ -78,6 +80,32 @@ cudaError_t launch_typed(const double *recp, const Xform &xf, int apply_xf, int 
   default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
+}
+
+// Variable-length and composite shapes (polycone, polyhedron, boolean): the record stays in
+// the geometry arena and the query goes through the run-time dispatch.
+template <int Q>
+__global__ void __launch_bounds__(256) k_shape_query_dyn(const DevGeom g, const int shape, const Xform xf,
+                                                         const double *__restrict__ x, const double *__restrict__ y,
+                                                         const double *__restrict__ z, const double *__restrict__ dx,
+                                                         const double *__restrict__ dy, const double *__restrict__ dz,
+                                                         size_t n, void *__restrict__ out)
+{
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    V3 p{__ldg(x + i), __ldg(y + i), __ldg(z + i)};
+    const bool framed = (Q == 0 || Q == 1 || Q == 2 || Q == 4);
+    if (framed) p = f64::to_local(xf, p);
+    if (Q == 0) static_cast<int32_t *>(out)[i] = f64::shape_inside(g, shape, p);
+    if (Q == 1) static_cast<uint8_t *>(out)[i] = f64::shape_contains(g, shape, p) ? 1 : 0;
+    if (Q == 2 || Q == 3) {
+      V3 d{__ldg(dx + i), __ldg(dy + i), __ldg(dz + i)};
+      if (framed) d = f64::rotate(xf, d);
+      static_cast<double *>(out)[i] = (Q == 2) ? f64::shape_dist_in(g, shape, p, d) : f64::shape_dist_out(g, shape, p, d);
+    }
+    if (Q == 4) static_cast<double *>(out)[i] = f64::shape_safety_in(g, shape, p);
+    if (Q == 5) static_cast<double *>(out)[i] = f64::shape_safety_out(g, shape, p);
+  }
 }
 
 // ---------------------------------------------------------------- navigation kernels
@@ -126,8 +154,29 @@ cudaError_t launch_shape_query_fp64(int type, const double *rec, const Xform &xf
   case kShapeBox: return launch_typed<BoxRec>(rec, xf, apply_xf, q, a, s);
   case kShapeTube: return launch_typed<TubeRec>(rec, xf, apply_xf, q, a, s);
   case kShapeCone: return launch_typed<ConeRec>(rec, xf, apply_xf, q, a, s);
+  case kShapeTrd: return launch_typed<TrdRec>(rec, xf, apply_xf, q, a, s);
+  case kShapeTorus2: return launch_typed<TorusRec>(rec, xf, apply_xf, q, a, s);
   default: return cudaErrorNotSupported;
   }
+}
+
+cudaError_t launch_shape_query_dyn_fp64(const DevGeom &g, int shape, const Xform &xf, int q, const QueryArgs &a,
+                                        cudaStream_t s)
+{
+  if (a.n == 0) return cudaSuccess;
+  const unsigned grid = grid_for(a.n, 256);
+#define VG_DYN(Q) k_shape_query_dyn<Q><<<grid, 256, 0, s>>>(g, shape, xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out)
+  switch (q) {
+  case 0: VG_DYN(0); break;
+  case 1: VG_DYN(1); break;
+  case 2: VG_DYN(2); break;
+  case 3: VG_DYN(3); break;
+  case 4: VG_DYN(4); break;
+  case 5: VG_DYN(5); break;
+  default: return cudaErrorInvalidValue;
+  }
+#undef VG_DYN
+  return cudaGetLastError();
 }
 
 cudaError_t launch_locate_fp64(const DevGeom &g, const double *x, const double *y, const double *z, size_t n,

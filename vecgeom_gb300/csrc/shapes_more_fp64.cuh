@@ -1,0 +1,358 @@
+// FP64 device kernels of Trd and Polycone (same compilation rules as shapes_fp64.cuh).
+#pragma once
+#include "shapes_fp64.cuh"
+
+namespace vg {
+
+
+
+namespace f64 {
+
+constexpr double kTiny = 1e-30;
+
+// ================================================================ Trd
+// TrdImplementation.h:138-173 (y faces always take the cross-product test)
+__device__ __forceinline__ void trd_classify(const TrdRec &t, V3 p, bool surfaceT, bool &cin, bool &cout)
+{
+  const double pzPlusDz = p.z + t.dz;
+  cout                  = fabs(p.z) > (surfaceT ? t.dz + kHalfTolerance : t.dz);
+  if (surfaceT) cin = fabs(p.z) < t.dz - kHalfTolerance;
+  const double cx = t.x2minusx1 * pzPlusDz - (2.0 * t.dz) * (fabs(p.x) - t.dx1);
+  const double cy = t.y2minusy1 * pzPlusDz - (2.0 * t.dz) * (fabs(p.y) - t.dy1);
+  if (surfaceT) {
+    cout = cout || (cx < -t.tolx) || (cy < -t.toly);
+    cin  = cin && (cx > t.tolx) && (cy > t.toly);
+  } else {
+    cout = cout || (cx < 0) || (cy < 0);
+  }
+}
+__device__ __forceinline__ int trd_inside(const TrdRec &t, V3 p)
+{
+  bool in = false, out = false;
+  trd_classify(t, p, true, in, out);
+  return out ? kOutside : (in ? kInside : kSurface);
+}
+__device__ __forceinline__ bool trd_contains(const TrdRec &t, V3 p)
+{
+  bool in = false, out = false;
+  trd_classify(t, p, false, in, out);
+  return !out;
+}
+// TrdImplementation.h:69-117 FaceTrajectoryIntersection
+__device__ __forceinline__ bool trd_face(const TrdRec &t, V3 pos, V3 dir, bool forY, bool mirrored, bool toInside,
+                                         double &dist)
+{
+  const double alongV = forY ? t.y2minusy1 : t.x2minusx1;
+  const double v1     = forY ? t.dy1 : t.dx1;
+  double posV         = forY ? pos.y : pos.x;
+  double dirV         = forY ? dir.y : dir.x;
+  const double posK   = forY ? pos.x : pos.y;
+  const double dirK   = forY ? dir.x : dir.y;
+  const double fK     = forY ? t.fx : t.fy;
+  const double fV     = forY ? t.fy : t.fx;
+  const double halfK  = forY ? t.halfx1plusx2 : t.halfy1plusy2;
+  if (mirrored) {
+    posV = -posV;
+    dirV = -dirV;
+  }
+  const double ndotv = dirV + fV * dir.z;
+  if (toInside ? !(ndotv < 0.) : !(ndotv > 0.)) return false;
+  const double alongZ = 2.0 * t.dz;
+  dist = (alongZ * (posV - v1) - alongV * (pos.z + t.dz)) / (dir.z * alongV - dirV * alongZ + kTiny);
+  if (!(dist > -kHalfTolerance)) return false;
+  const double hitz = pos.z + dist * dir.z;
+  const double hitk = posK + dist * dirK;
+  const bool ok     = fabs(hitz) <= t.dz && fabs(hitk) <= halfK - fK * hitz;
+  if (ok && fabs(dist) < kHalfTolerance) dist = 0.0;
+  return ok;
+}
+__device__ __forceinline__ double trd_clamp(double d) { return fabs(d) < kHalfTolerance ? 0.0 : d; }
+// TrdImplementation.h:288-370
+__device__ __noinline__ double trd_dist_in(const TrdRec &t, V3 p, V3 d)
+{
+  double distance  = kInfLength;
+  const bool inz   = fabs(p.z) < t.dz - kHalfTolerance;
+  double distx     = t.halfx1plusx2 - t.fx * p.z;
+  const bool inx   = (distx - fabs(p.x)) * t.calfx > kHalfTolerance;
+  const bool vary  = t.dy1 != t.dy2;
+  double disty     = vary ? t.halfy1plusy2 - t.fy * p.z : fabs(p.y) - t.dy1;
+  const bool iny   = vary ? (disty - fabs(p.y)) * t.calfy > kHalfTolerance : disty < -kHalfTolerance;
+  if (inx && iny && inz) return -1.;
+  if (p.z * d.z < 0. && !inz) {
+    const double distz = (fabs(p.z) - t.dz) / fabs(d.z);
+    const double hitx  = fabs(p.x + distz * d.x);
+    const double hity  = fabs(p.y + distz * d.y);
+    const bool okzt    = p.z > (t.dz - kHalfTolerance) && hitx <= t.dx2 && hity <= t.dy2;
+    const bool okzb    = p.z < (-t.dz + kHalfTolerance) && hitx <= t.dx1 && hity <= t.dy1;
+    if (okzt || okzb) return trd_clamp(distz);
+  }
+  bool okx = false;
+  if (!inx) {
+    if (trd_face(t, p, d, false, false, true, distx)) distance = distx;
+    okx = trd_face(t, p, d, false, true, true, distx);
+    if (okx) distance = distx;
+  }
+  if (okx) return trd_clamp(distance);
+  if (!iny) {
+    if (vary) {
+      if (trd_face(t, p, d, true, false, true, disty)) distance = disty;
+      if (trd_face(t, p, d, true, true, true, disty)) distance = disty;
+    } else {
+      disty /= fabs(d.y);
+      const double zhit = p.z + disty * d.z;
+      const double xhit = p.x + disty * d.x;
+      const double dx   = t.halfx1plusx2 - t.fx * zhit;
+      if (p.y * d.y < 0 && disty > -kHalfTolerance && fabs(xhit) < dx && fabs(zhit) < t.dz) distance = disty;
+    }
+  }
+  return trd_clamp(distance);
+}
+// TrdImplementation.h:371-470
+__device__ __noinline__ double trd_dist_out(const TrdRec &t, V3 p, V3 d)
+{
+  const double invdir = 1. / fabs(d.z + kTiny);
+  const bool vary     = t.dy1 != t.dy2;
+  double distx        = t.halfx1plusx2 - t.fx * p.z;
+  double disty        = vary ? t.halfy1plusy2 - t.fy * p.z : t.dy1 - fabs(p.y);
+  const bool out      = (t.dz - fabs(p.z) < -kHalfTolerance) || ((distx - fabs(p.x)) * t.calfx < -kHalfTolerance) ||
+                   (vary ? ((disty - fabs(p.y)) * t.calfy < -kHalfTolerance) : (disty < -kHalfTolerance));
+  if (out) return -1.;
+  if (d.z > 0.) {
+    const double distz = (t.dz - p.z) * invdir;
+    if (fabs(p.x + distz * d.x) <= t.dx2 && fabs(p.y + distz * d.y) <= t.dy2) return trd_clamp(distz);
+  }
+  if (d.z < 0.) {
+    const double distz = (p.z + t.dz) * invdir;
+    if (fabs(p.x + distz * d.x) <= t.dx1 && fabs(p.y + distz * d.y) <= t.dy1) return trd_clamp(distz);
+  }
+  if (trd_face(t, p, d, false, false, false, distx)) return trd_clamp(distx);
+  if (trd_face(t, p, d, false, true, false, distx)) return trd_clamp(distx);
+  double distance = 0.0;
+  if (vary) {
+    if (trd_face(t, p, d, true, false, false, disty)) return trd_clamp(disty);
+    if (trd_face(t, p, d, true, true, false, disty)) distance = disty;
+  } else {
+    const double plane = d.y < 0. ? -t.dy1 : t.dy1;
+    disty              = (plane - p.y) / d.y;
+    const double zhit  = p.z + disty * d.z;
+    const double xhit  = p.x + disty * d.x;
+    const double dx    = t.halfx1plusx2 - t.fx * zhit;
+    if (fabs(xhit) < dx && fabs(zhit) < t.dz) distance = disty;
+  }
+  return trd_clamp(distance);
+}
+// TrdImplementation.h:118-137
+__device__ __forceinline__ double trd_safety(const TrdRec &t, V3 p, bool inside)
+{
+  double dist        = t.dz - fabs(p.z);
+  const double distx = t.halfx1plusx2 - t.fx * p.z;
+  const double safx  = (distx - fabs(p.x)) * t.calfx;
+  if (distx >= 0 && safx < dist) dist = safx;
+  if (t.dy1 != t.dy2) {
+    const double disty = t.halfy1plusy2 - t.fy * p.z;
+    const double safy  = (disty - fabs(p.y)) * t.calfy;
+    if (disty >= 0 && safy < dist) dist = safy;
+  } else {
+    const double safy = t.dy1 - fabs(p.y);
+    if (safy < dist) dist = safy;
+  }
+  return inside ? dist : -dist;
+}
+__device__ __forceinline__ double trd_safety_in(const TrdRec &t, V3 p) { return trd_safety(t, p, false); }
+__device__ __forceinline__ double trd_safety_out(const TrdRec &t, V3 p) { return trd_safety(t, p, true); }
+
+// ================================================================ Polycone
+struct PolyconeView {
+  const double *r;
+  int nsec;
+  __device__ PolyconeView(const PolyconeRec &rec) : r(&rec.nsec), nsec((int)rec.nsec) {}
+  __device__ double z(int i) const { return r[4 + i]; }
+  __device__ const double *sec(int i) const { return r + polycone_section_base(nsec) + i * kPolyconeSectionDoubles; }
+  __device__ double shift(int i) const { return sec(i)[0]; }
+  __device__ const ConeRec &cone(int i) const { return *reinterpret_cast<const ConeRec *>(sec(i) + 4); }
+  __device__ V3 local(V3 p, int i) const { return V3{p.x, p.y, p.z - shift(i)}; }
+  // PolyconeStruct.h:246-253 GetSectionIndex
+  __device__ int index(double zp) const
+  {
+    if (zp < z(0)) return -1;
+    for (int i = 0; i < nsec; ++i)
+      if (zp >= z(i) && zp <= z(i + 1)) return i;
+    return -2;
+  }
+};
+
+// PolyconeImplementation.h:58-147
+__device__ __forceinline__ void pc_section(const PolyconeView &v, int i, V3 p, bool forInside, bool &cin, bool &cout)
+{
+  if (i < 0) {
+    cin  = false;
+    cout = true;
+    return;
+  }
+  cone_classify(v.cone(i), v.local(p, i), forInside, cin, cout);
+}
+__device__ __noinline__ void polycone_classify(const PolyconeRec &rec, V3 p, bool forInside, bool &cin, bool &cout)
+{
+  const PolyconeView v(rec);
+  const int lo = v.index(p.z - kTolerance);
+  const int hi = v.index(p.z + kTolerance);
+  if (lo < 0 && hi < 0) {
+    cout = true;
+    return;
+  }
+  if (lo < 0 && hi == 0) return pc_section(v, 0, p, forInside, cin, cout);
+  if (hi < 0 && lo == v.nsec - 1) return pc_section(v, v.nsec - 1, p, forInside, cin, cout);
+  if (lo >= 0 && hi >= 0) {
+    if (lo == hi) return pc_section(v, lo, p, forInside, cin, cout);
+    bool inL = false, outL = false, inH = false, outH = false;
+    pc_section(v, lo, p, forInside, inL, outL);
+    pc_section(v, hi, p, forInside, inH, outH);
+    if (!inL && !outL && !inH && !outH) {
+      cin = true;
+      return;
+    }
+    if (outL && outH) cout = true;
+  }
+}
+__device__ __forceinline__ int polycone_inside(const PolyconeRec &r, V3 p)
+{
+  bool cin = false, cout = false;
+  polycone_classify(r, p, true, cin, cout);
+  return cin ? kInside : (cout ? kOutside : kSurface);
+}
+__device__ __forceinline__ bool polycone_contains(const PolyconeRec &r, V3 p)
+{
+  bool cin = false, cout = false;
+  polycone_classify(r, p, false, cin, cout);
+  return !cout;
+}
+// PolyconeImplementation.h:148-180
+__device__ __noinline__ double polycone_dist_in(const PolyconeRec &rec, V3 p, V3 d)
+{
+  const PolyconeView v(rec);
+  double distance = kInfLength;
+  int increment   = (d.z > 0) ? 1 : -1;
+  if (fabs(d.z) < kTolerance) increment = 0;
+  int index = v.index(p.z);
+  if (index == -1) index = 0;
+  if (index == -2) index = v.nsec - 1;
+  do {
+    distance = cone_dist_in(v.cone(index), v.local(p, index), d);
+    if (distance < kInfLength || !increment) break;
+    index += increment;
+  } while (index >= 0 && index < v.nsec);
+  return distance;
+}
+// PolyconeImplementation.h:181-300
+__device__ __noinline__ double polycone_dist_out(const PolyconeRec &rec, V3 point, V3 dir)
+{
+  const PolyconeView v(rec);
+  if (v.nsec == 1) return cone_dist_out(v.cone(0), v.local(point, 0), dir);
+  const int lo = v.index(point.z - kTolerance);
+  const int hi = v.index(point.z + kTolerance);
+  int index    = 0;
+  if (lo < 0 && hi < 0) return -1;
+  if (lo < 0 && hi >= 0) {
+    index = hi;
+    if (cone_inside(v.cone(index), v.local(point, index)) == kOutside) return -1;
+  } else if (lo != hi && lo >= 0) {
+    index = (cone_inside(v.cone(lo), v.local(point, lo)) == kOutside) ? hi : lo;
+  } else {
+    index = lo;
+    if (index < 0) index = v.index(point.z);
+  }
+  if (index < 0) return 0.;
+  if (cone_inside(v.cone(index), v.local(point, index)) == kOutside) return -1;
+  double total  = 0.;
+  int increment = (dir.z > 0) ? 1 : -1;
+  if (fabs(dir.z) < kTolerance) increment = 0;
+  int istep = 0;
+  V3 pn     = point;
+  do {
+    if ((total != 0) || (istep < 2)) {
+      pn = V3{point.x + total * dir.x, point.y + total * dir.y, point.z + total * dir.z};
+      pn.z -= v.shift(index);
+      if (cone_inside(v.cone(index), pn) == kOutside) break;
+    } else {
+      pn.z -= v.shift(index);
+    }
+    istep++;
+    const double dist = cone_dist_out(v.cone(index), pn, dir);
+    if (dist == -1) return kInfLength;
+    if (fabs(dist) < 0.5 * kTolerance) {
+      int index1 = index;
+      if ((index > 0) && (index < v.nsec - 1)) {
+        index1 += increment;
+      } else {
+        if ((index == 0) && (increment > 0)) index1 += increment;
+        if ((index == v.nsec - 1) && (increment < 0)) index1 += increment;
+      }
+      const double s = total + dist;
+      V3 pte{point.x + s * dir.x, point.y + s * dir.y, point.z + s * dir.z};
+      pte.z -= v.shift(index1);
+      if (cone_inside(v.cone(index1), pte) == 3 || increment == 0) break;
+    }
+    total += dist;
+    index += increment;
+  } while (increment != 0 && index >= 0 && index < v.nsec);
+  return total;
+}
+// PolyconeImplementation.h:301-354
+__device__ __noinline__ double polycone_safety_in(const PolyconeRec &rec, V3 p)
+{
+  const PolyconeView v(rec);
+  int index  = v.index(p.z);
+  bool needZ = false;
+  if (index < 0) {
+    needZ = true;
+    index = (index == -1) ? 0 : v.nsec - 1;
+  }
+  double safety = cone_safety_in(v.cone(index), v.local(p, index));
+  if (needZ || safety < kTolerance) return safety;
+  double minSafety = safety;
+  double zbase     = v.z(index + 1);
+  for (int i = index + 1; i < v.nsec; ++i) {
+    if (v.z(i) - zbase >= minSafety) break;
+    safety = cone_safety_in(v.cone(i), v.local(p, i));
+    if (safety < minSafety) minSafety = safety;
+  }
+  if (index > 0) {
+    zbase = v.z(index - 1);
+    for (int i = index - 1; i >= 0; --i) {
+      if (zbase - v.z(i) >= minSafety) break;
+      safety = cone_safety_in(v.cone(i), v.local(p, i));
+      if (safety < minSafety) minSafety = safety;
+    }
+  }
+  return minSafety;
+}
+// PolyconeImplementation.h:355-410
+__device__ __noinline__ double polycone_safety_out(const PolyconeRec &rec, V3 p)
+{
+  const PolyconeView v(rec);
+  bool cin = false, cout = false;
+  polycone_classify(rec, p, true, cin, cout);
+  if (cout) return -1;
+  const int index = v.index(p.z);
+  if (index < 0) return -1;
+  double minSafety = cone_safety_out(v.cone(index), v.local(p, index));
+  if (minSafety == kInfLength || minSafety < kTolerance) return 0.;
+  double zbase = v.z(index + 1);
+  for (int i = index + 1; i < v.nsec; ++i) {
+    if (v.z(i) - zbase >= minSafety) break;
+    const double s = cone_safety_in(v.cone(i), v.local(p, i));
+    if (s < minSafety) minSafety = s;
+  }
+  if (index > 0) {
+    zbase = v.z(index - 1);
+    for (int i = index - 1; i >= 0; --i) {
+      if (zbase - v.z(i) >= minSafety) break;
+      const double s = cone_safety_in(v.cone(i), v.local(p, i));
+      if (s < minSafety) minSafety = s;
+    }
+  }
+  return minSafety;
+}
+
+} // namespace f64
+} // namespace vg

@@ -73,6 +73,37 @@ struct ConeRec {
   WedgeRec w;
 };
 
+// VecGeom/volumes/TrdStruct.h:15-86
+struct TrdRec {
+  double dx1, dx2, dy1, dy2, dz;
+  double x2minusx1, y2minusy1, halfx1plusx2, halfy1plusy2, calfx, calfy, fx, fy, tolx, toly, pad;
+};
+
+// Polycone record: header, section boundaries, then one (shift, cone) block per section
+// (VecGeom/volumes/PolyconeStruct.h:26-36, PolyconeSection.h). Variable length; the views
+// below address it in place.
+struct PolyconeRec {
+  double nsec, sphi, dphi, reserved;
+  double data[1]; // zs[nsec+1], pad to a multiple of 4, then nsec x (shift, 3 pad, ConeRec, pad)
+};
+constexpr int kPolyconeSectionDoubles = 4 + ((int)(sizeof(ConeRec) / sizeof(double)) + 3) / 4 * 4;
+VG_HD inline int polycone_section_base(int nsec) { return ((4 + nsec + 1) + 3) / 4 * 4; }
+
+// VecGeom/volumes/TorusStruct2.h:26-43 (+ the bounding tube of UnplacedTorus2.h:64-74)
+struct TorusRec {
+  double rmin, rmax, rtor, sphi, dphi, rmin2, rmax2, rtor2;
+  WedgeRec w;
+  double pad[3];
+  TubeRec bt;
+};
+
+// Boolean subtraction record (VecGeom/volumes/BooleanStruct.h:19-33): operand placed-volume ids.
+struct BoolRec {
+  double left_pv, right_pv, reserved0, reserved1;
+};
+// Bound of the reference's unbounded push loop in DistanceToIn (BooleanImplementation.h:116-146).
+constexpr int kBoolMaxPush = 1000;
+
 // Compact placed-volume transformation: p_local = R^T (p - t) with the reference's
 // component order (VecGeom/base/Transformation3D.h:640-651).
 struct Xform {

@@ -234,3 +234,36 @@ def primaries_eta_phi(n, seed, eta_max=3.0):
     d = (st * np.cos(ph), st * np.sin(ph), np.cos(theta))
     z = np.zeros(n)
     return (z.copy(), z.copy(), z.copy()), d
+
+
+def shape_points_mixed(lo, hi, n, seed, inside_fn, dist_out_fn, surface_band=1e-6):
+    """Config-2 point mix for one shape: a third strictly inside, a third outside (uniform in
+    the 1.2x extent box, classified with `inside_fn`), and a third within `surface_band` mm
+    of the surface (an inside point moved along a random direction to where `dist_out_fn`
+    puts the boundary, then offset by U(-band, band) along that direction). Directions are
+    isotropic. `inside_fn(x, y, z)` and `dist_out_fn(x, y, z, dx, dy, dz)` evaluate the shape
+    (on the GPU in the benchmark, on the CPU checker in tests)."""
+    n3 = n // 3
+    ins, outs = [], []
+    it = 0
+    while (sum(len(a[0]) for a in ins) < n - 2 * n3 + n3 or sum(len(a[0]) for a in outs) < n3) and it < 64:
+        m = max(4 * n, 1024)
+        (x, y, z), _ = shape_points_box(lo, hi, m, seed + 1000 * it)
+        cls = np.asarray(inside_fn(x, y, z))
+        ins.append((x[cls == 1], y[cls == 1], z[cls == 1]))
+        outs.append((x[cls == 3], y[cls == 3], z[cls == 3]))
+        it += 1
+    ix, iy, iz = (np.concatenate([a[k] for a in ins]) for k in range(3))
+    ox, oy, oz = (np.concatenate([a[k] for a in outs]) for k in range(3))
+    n_in = n - 2 * n3
+    g = rng(seed, 11)
+    sx, sy, sz = ix[n_in:n_in + n3], iy[n_in:n_in + n3], iz[n_in:n_in + n3]
+    sdx, sdy, sdz = isotropic(rng(seed, 12), len(sx))
+    d = np.asarray(dist_out_fn(sx, sy, sz, sdx, sdy, sdz))
+    d = np.where((d > 0) & (d < 1e30), d, 0.0) + surface_band * (2.0 * g.random(len(sx)) - 1.0)
+    px = np.concatenate([ix[:n_in], ox[:n3], sx + d * sdx])
+    py = np.concatenate([iy[:n_in], oy[:n3], sy + d * sdy])
+    pz = np.concatenate([iz[:n_in], oz[:n3], sz + d * sdz])
+    perm = rng(seed, 13).permutation(len(px))
+    dirs = isotropic(rng(seed, 14), len(px))
+    return (px[perm].copy(), py[perm].copy(), pz[perm].copy()), dirs
