@@ -1,13 +1,17 @@
 """Benchmark: navigation steps per second on one GB300.
 
 A step is one ComputeStepAndNextVolume (DistanceToOut of the current volume, BVH daughter
-intersection, boundary relocation) for every track of the batch. Inputs (points,
-directions, located states) are resident in HBM when the timed region starts; `e2e`
-repeats the measurement through the host-array C-ABI entry point with the host<->device
-copies inside the timed region. The CPU baseline is the oracle (a scalar restatement of
-the reference's CPU path) on the host cores over a bounded sample of the same tracks.
+intersection, boundary relocation) for every track of the batch. The default workload is
+the config-4 detector (150k box modules in a 20-layer barrel + two endcaps of Polycone
+holders with Trd wedges); the 2^22 step inputs are drawn from straight-track transport
+histories generated on the GPU, so they cover every kind of volume. Inputs are resident in
+HBM when the timed region starts; `e2e` repeats the measurement through the host-array
+C-ABI entry point with the host<->device copies inside the timed region. The CPU baseline
+is the oracle (a scalar restatement of the reference's CPU path) on the host cores over a
+bounded sample of the same step inputs.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                       [--workload detector|barrel]
 For N > 1 (torchrun) every rank runs an independent replica of the workload (the path has
 no exchange step) and rank 0 reports the aggregate.
 """
@@ -34,10 +38,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="barrel", choices=["barrel"])
+    ap.add_argument("--workload", default="detector", choices=["detector", "barrel"])
     ap.add_argument("--tracks", type=int, default=1 << 22)
+    ap.add_argument("--primaries", type=int, default=1 << 20)
     ap.add_argument("--seed", type=int, default=0xC0FFEE)
-    ap.add_argument("--cpu-sample", type=int, default=1 << 18)
+    ap.add_argument("--cpu-sample", type=int, default=1 << 17)
     return ap.parse_args()
 
 
@@ -47,8 +52,7 @@ def dist_setup(args):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if ws > 1:
         import torch.distributed as dist
-        backend = "nccl" if args.impl == "ours" else "gloo"
-        dist.init_process_group(backend)
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
     return ws, rank, local
 
 
@@ -69,8 +73,7 @@ class ClockSampler:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
-            self.t.start()
+            threading.Thread(target=self._read, daemon=True).start()
         except OSError:
             self.proc = None
         return self
@@ -107,48 +110,94 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_workload(args, geo_factory):
+def builder(name):
     from vecgeom_gb300 import workloads as W
-    geo = geo_factory()
-    W.build_barrel(geo)
+    return W.build_detector if name == "detector" else W.build_barrel
+
+
+def config_of(args, total_pool=None):
+    if args.workload == "detector":
+        cfg = {"workload": "detector nav step (config 4 geometry: 150k box modules in 20 barrel layers, "
+                           "2x12 Polycone holders x 167 Trd wedges; 150,213 placed volumes, depth 4)",
+               "tracks": args.tracks,
+               "track_sample": "uniform draw from straight-track transport histories of %d primaries "
+                               "(eta in [-3,3], phi uniform, from the origin)" % args.primaries}
+    else:
+        cfg = {"workload": "barrel nav step (config 3: 1e4 placed volumes, depth 4)", "tracks": args.tracks,
+               "track_sample": "r<30 mm, |z|<500 mm, isotropic"}
+    cfg["seed"] = args.seed
+    if total_pool:
+        cfg["sample_pool"] = total_pool
+    return cfg
+
+
+def make_inputs(args, geo, torch, dev):
+    from vecgeom_gb300 import workloads as W
+    if args.workload == "detector":
+        t, st, total = W.sample_transport_steps(geo, args.tracks, args.seed, torch, dev, n_primaries=args.primaries)
+        return t, st, total
     pts, dirs = W.tracks_in_cylinder(args.tracks, seed=args.seed)
-    cfg = {"workload": "barrel nav step (1e4 placed volumes, depth 4)", "geometry": "10 tube layers x 64..640 box "
-           "modules + sensors, world 4x4x6 m", "tracks": args.tracks, "track_start": "r<30 mm, |z|<500 mm, isotropic",
-           "seed": args.seed}
-    return geo, pts, dirs, cfg
+    t = [torch.from_numpy(a).to(dev) for a in (*pts, *dirs)]
+    st = torch.empty(args.tracks * 12, dtype=torch.uint8, device=dev)
+    geo.locate_point(t[0], t[1], t[2], st)
+    return t, st, None
 
 
-def cpu_baseline(args, pts, dirs, nthreads):
-    """Oracle port on the host cores over a bounded sample of the same tracks."""
+def cpu_time_steps(args, host_inputs, host_states, nthreads, reps=3):
+    """Oracle port timing on the host cores over the given sample."""
     from oracle.oracle import OracleGeometry
-    from vecgeom_gb300 import workloads as W
     o = OracleGeometry()
-    W.build_barrel(o)
-    m = min(args.cpu_sample, len(pts[0]))
-    sub = [np.ascontiguousarray(a[:m]) for a in (*pts, *dirs)]
-    st, _ = o.locate(*sub[:3], nthreads=nthreads)
+    builder(args.workload)(o)
+    st = np.frombuffer(host_states.tobytes(), dtype=[("nav_ind", "<u4"), ("last_exited", "<u4"),
+                                                    ("on_boundary", "u1"), ("pad", "u1", 3)]).copy()
     best = None
-    for _ in range(3):
-        _, _, _, t = o.step(*sub, st, nthreads=nthreads)
+    for _ in range(reps):
+        _, _, _, t = o.step(*host_inputs, st, nthreads=nthreads)
         best = t if best is None else min(best, t)
-    return {"value": m / best, "unit": "nav steps/s", "cores": nthreads, "kind": "port",
-            "sample": "%d of the %d tracks, one step each, best of 3" % (m, len(pts[0]))}
+    return len(host_inputs[0]) / best
+
+
+def oracle_sample_steps(o, m, seed, nthreads, max_steps=400):
+    """The detector workload's step inputs generated on the CPU: m primaries transported by
+    the oracle, every pre-step (point, direction, state) pooled, m of them drawn uniformly."""
+    from vecgeom_gb300 import workloads as W
+    (x, y, z), (dx, dy, dz) = W.primaries_eta_phi(m, seed)
+    st, _ = o.locate(x, y, z, nthreads=nthreads)
+    pool = [[] for _ in range(7)]
+    for _ in range(max_steps):
+        alive = st["nav_ind"] != 0
+        if not alive.any():
+            break
+        for k, a in enumerate((x, y, z, dx, dy, dz, st)):
+            pool[k].append(a[alive])
+        out, step, _, _ = o.step(x, y, z, dx, dy, dz, st, nthreads=nthreads)
+        x = np.where(alive, x + step * dx, x)
+        y = np.where(alive, y + step * dy, y)
+        z = np.where(alive, z + step * dz, z)
+        st = np.where(alive, out, st)
+    cat = [np.concatenate(p) for p in pool]
+    pick = W.rng(seed, 21).permutation(len(cat[0]))[:m]
+    return [np.ascontiguousarray(c[pick]) for c in cat[:6]], np.ascontiguousarray(cat[6][pick])
 
 
 def run_reference(args, ws, rank):
     """CPU implementation of the path (the oracle port; the reference itself needs VecCore,
-    which is not available) on all host cores, same metric/config, bounded per step."""
+    which is not available) on all host cores, same metric and config, each step a bounded
+    sample of the batch."""
     if rank != 0:
         return
+    nthreads = os.cpu_count() or 1
     from oracle.oracle import OracleGeometry
     from vecgeom_gb300 import workloads as W
-    nthreads = os.cpu_count() or 1
     o = OracleGeometry()
-    W.build_barrel(o)
-    pts, dirs = W.tracks_in_cylinder(args.tracks, seed=args.seed)
+    builder(args.workload)(o)
     m = min(args.cpu_sample, args.tracks)
-    sub = [np.ascontiguousarray(a[:m]) for a in (*pts, *dirs)]
-    st, _ = o.locate(*sub[:3], nthreads=nthreads)
+    if args.workload == "detector":
+        sub, st = oracle_sample_steps(o, m, args.seed, nthreads)
+    else:
+        pts, dirs = W.tracks_in_cylinder(m, seed=args.seed)
+        sub = [np.ascontiguousarray(a) for a in (*pts, *dirs)]
+        st, _ = o.locate(*sub[:3], nthreads=nthreads)
     for _ in range(args.warmup):
         o.step(*sub, st, nthreads=nthreads)
     times = []
@@ -157,14 +206,13 @@ def run_reference(args, ws, rank):
         times.append(t)
     tot = sum(times)
     value = m * args.steps / tot
-    _, _, _, cfg = None, None, None, {"workload": "barrel nav step (1e4 placed volumes, depth 4)",
-                                       "tracks": args.tracks, "seed": args.seed}
     line = {"metric": "nav steps/s", "value": value, "unit": "nav steps/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": cfg,
-            "impl": "reference",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": config_of(args), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "nav steps/s", "cores": nthreads, "kind": "port",
-                             "sample": "%d tracks per step of the %d-track batch" % (m, args.tracks)},
+                             "sample": "%d tracks per step (first steps of the primaries) of the %d-track batch"
+                                       % (m, args.tracks)},
             "e2e": {"value": value, "unit": "nav steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -182,11 +230,10 @@ def main():
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    geo, pts, dirs, cfg = make_workload(args, vg.Geometry)
+    geo = vg.Geometry()
+    builder(args.workload)(geo)
+    t, st, pool = make_inputs(args, geo, torch, dev)
     n = args.tracks
-    t = [torch.from_numpy(a).to(dev) for a in (*pts, *dirs)]
-    st = torch.empty(n * 12, dtype=torch.uint8, device=dev)
-    geo.locate_point(t[0], t[1], t[2], st)
     out = torch.empty_like(st)
     step = torch.empty(n, dtype=torch.float64, device=dev)
     status = torch.empty(n, dtype=torch.int32, device=dev)
@@ -218,22 +265,26 @@ def main():
             ms = float(v.item())
         return ms / args.steps
 
+    ms_fp64 = timed(vg.PREC_FP64)
+    out64, step64 = out.clone(), step.clone()
     with ClockSampler(local) as clocks:
-        ms_fp64 = timed(vg.PREC_FP64)
+        ms_mixed = timed(vg.PREC_MIXED)
     n_err = int((status != 0).sum().item())
+    ids_equal = bool(torch.equal(out64, out))
+    step_err = float((step64 - step).abs().max().item())
 
-    # e2e: host arrays through the C-ABI host entry point (pinned), copies inside the timed region
-    hp = [torch.from_numpy(a).pin_memory() for a in (*pts, *dirs)]
+    # e2e: host arrays through the host-pointer C-ABI entry point, copies inside the timed region
+    hp = [a.cpu().pin_memory() for a in t]
     hst = st.cpu().pin_memory()
     hout = torch.empty_like(hst).pin_memory()
     hstep = torch.empty(n, dtype=torch.float64).pin_memory()
     for _ in range(2):
-        geo.compute_step_and_next_volume_host(*hp, hst, hout, hstep)
+        geo.compute_step_and_next_volume_host(*hp, hst, hout, hstep, flags=vg.PREC_MIXED)
     barrier()
-    t0 = time.perf_counter()
     ke = max(3, args.steps // 4)
+    t0 = time.perf_counter()
     for _ in range(ke):
-        geo.compute_step_and_next_volume_host(*hp, hst, hout, hstep)
+        geo.compute_step_and_next_volume_host(*hp, hst, hout, hstep, flags=vg.PREC_MIXED)
     torch.cuda.synchronize()
     barrier()
     e2e_s = (time.perf_counter() - t0) / ke
@@ -244,26 +295,38 @@ def main():
     except (OSError, ValueError):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    value = ws * n / (ms_fp64 * 1e-3)
-    achieved = STEP_BYTES * n / (ms_fp64 * 1e-3) / 1e9
+    value = ws * n / (ms_mixed * 1e-3)
+    achieved = STEP_BYTES * n / (ms_mixed * 1e-3) / 1e9
     line = {
         "metric": "nav steps/s", "value": value, "unit": "nav steps/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_fp64, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, generated on the host)",
-        "config": dict(cfg, precision="plain FP64", l2="inputs 240 MB > L2 (129 MB); geometry L2-resident by design",
+        "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 (mixed: FP32 pruning, FP64 decisions)",
+        "data": "synthetic (seeded; geometry built in code, tracks generated on the GPU)",
+        "config": dict(config_of(args, pool), precision="VG_PREC_MIXED",
+                       l2="inputs %.0f MB > L2 (129 MB); geometry L2/HBM-resident by design" % (n * 60 / 1e6),
                        parallelism="replicas" if ws > 1 else "single GPU"),
+        "plain_fp64": {"value": ws * n / (ms_fp64 * 1e-3), "ms_per_step": ms_fp64},
+        "speedup_vs_plain_fp64": ms_fp64 / ms_mixed,
+        "ids_identical_to_fp64": ids_equal, "max_step_diff_vs_fp64_mm": step_err,
         "e2e": {"value": ws * n / e2e_s, "unit": "nav steps/s", "h2d_bytes_per_step": n * (48 + 12),
                 "d2h_bytes_per_step": n * (12 + 8)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": None,
-                     "note": "algorithmic bytes %d B/step; FP64-issue bound kernel (GB300 FP64 ~1.2 TF/s), "
-                             "peak %s" % (STEP_BYTES, "of measured" if peaks else "of fallback")},
+                     "note": "algorithmic bytes %d B/step; the kernel is issue/latency bound (FP64 pipe for "
+                             "the plain path), see profiles/; peak %s" % (STEP_BYTES,
+                                                                        "of measured" if peaks else "of fallback")},
         "gpu_launches": args.steps,
         "track_errors": n_err,
         "clocks": clocks.summary(),
     }
     if rank == 0:
-        line["cpu_baseline"] = cpu_baseline(args, pts, dirs, os.cpu_count() or 1)
+        m = min(args.cpu_sample, n)
+        hin = [a[:m].cpu().numpy() for a in t]
+        hs = st[: m * 12].cpu().numpy()
+        nthreads = os.cpu_count() or 1
+        cv = cpu_time_steps(args, hin, hs, nthreads)
+        line["cpu_baseline"] = {"value": cv, "unit": "nav steps/s", "cores": nthreads, "kind": "port",
+                                "sample": "%d of the %d step inputs, best of 3" % (m, n)}
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist

@@ -818,7 +818,45 @@ int Geometry::upload(std::string &err)
   const size_t o_dau = a.add(daughters), o_pvl = a.add(pv_lv), o_pvc = a.add(pv_child), o_pvx = a.add(pv_xf);
   const size_t o_bn0 = a.add(bvh_node0), o_bp0 = a.add(bvh_prim0), o_nnc = a.add(node_nchild);
   const size_t o_nof = a.add(node_offset), o_nbx = a.add(node_box), o_pid = a.add(prim_id);
+  // FP32 bounding descriptors of the shapes (mixed-precision navigator): kind 0 = box
+  // (lo, hi; flag 1 when the box is the shape itself), kind 1 = cylindrical shell (rmin,
+  // rmax, zlo, zhi; flag 1 when the shell is the shape itself). Radii and z are rounded
+  // outward to FP32.
+  std::vector<float> lbd(8 * shapes.size(), 0.f);
+  for (size_t i = 0; i < shapes.size(); ++i) {
+    HostShape const &s = shapes[i];
+    float *d           = &lbd[8 * i];
+    auto shell = [&](double rmin, double rmax, double zlo, double zhi, bool exact) {
+      d[0] = 1.f, d[1] = exact ? 1.f : 0.f;
+      d[2] = round_down(rmin < 0 ? 0 : rmin), d[3] = round_up(rmax), d[4] = round_down(zlo), d[5] = round_up(zhi);
+    };
+    if (s.type == kShapeTube) {
+      const TubeRec &t = *reinterpret_cast<const TubeRec *>(s.rec.data());
+      shell(t.rmin, t.rmax, -t.z, t.z, t.dphi >= kTwoPi);
+    } else if (s.type == kShapeCone) {
+      const ConeRec &c = *reinterpret_cast<const ConeRec *>(s.rec.data());
+      shell(std::min(c.rmin1, c.rmin2), std::max(std::max(c.rmax1, c.rmax2), std::max(c.origRmax1, c.origRmax2)),
+            -c.dz, c.dz, false);
+    } else if (s.type == kShapePolycone) {
+      const int nsec = (int)s.rec[0];
+      double rmin = kInfLength, rmax = 0.;
+      for (int k = 0; k < nsec; ++k) {
+        const ConeRec &c =
+            *reinterpret_cast<const ConeRec *>(s.rec.data() + polycone_section_base(nsec) + k * kPolyconeSectionDoubles + 4);
+        rmin = std::min(rmin, std::min(c.rmin1, c.rmin2));
+        rmax = std::max(rmax, std::max(std::max(c.rmax1, c.rmax2), std::max(c.origRmax1, c.origRmax2)));
+      }
+      shell(rmin, rmax, s.rec[4], s.rec[4 + nsec], false);
+    } else if (s.type == kShapeTorus2) {
+      const TorusRec &t = *reinterpret_cast<const TorusRec *>(s.rec.data());
+      shell(t.rtor - t.rmax, t.rtor + t.rmax, -t.rmax, t.rmax, false);
+    } else {
+      d[0] = 0.f, d[1] = (s.type == kShapeBox) ? 1.f : 0.f;
+      for (int k = 0; k < 3; ++k) d[2 + k] = round_down(s.lo[k]), d[5 + k] = round_up(s.hi[k]);
+    }
+  }
   const size_t o_pbx = a.add(prim_box), o_nf = a.add(node_f), o_pbf = a.add(prim_box_f), o_nav = a.add(nav);
+  const size_t o_lbd = a.add(lbd);
 
   cudaError_t e = cudaGetDevice(&device);
   if (e == cudaSuccess) e = cudaMalloc(&arena, a.host.size() ? a.host.size() : 256);
@@ -851,6 +889,7 @@ int Geometry::upload(std::string &err)
   dev.node_f      = reinterpret_cast<const NodeF *>(P(o_nf));
   dev.prim_box_f  = reinterpret_cast<const float *>(P(o_pbf));
   dev.nav         = reinterpret_cast<const uint32_t *>(P(o_nav));
+  dev.shape_lbd   = reinterpret_cast<const float *>(P(o_lbd));
   dev.world_pv    = world;
   dev.max_depth   = max_depth;
   dev.n_pv        = (int32_t)pvs.size();

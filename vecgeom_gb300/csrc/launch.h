@@ -29,11 +29,13 @@ cudaError_t launch_shape_query_dyn_fp64(const DevGeom &g, int shape, const Xform
 cudaError_t launch_locate_fp64(const DevGeom &g, const double *x, const double *y, const double *z, size_t n,
                                NavState *out, cudaStream_t s);
 cudaError_t launch_step_fp64(const DevGeom &g, const StepArgs &a, cudaStream_t s);
-// flags: VG_PREC_FP64 or VG_PREC_MIXED
+cudaError_t launch_step_mixed(const DevGeom &g, const StepArgs &a, cudaStream_t s);
+cudaError_t launch_locate_mixed(const DevGeom &g, const double *x, const double *y, const double *z, size_t n,
+                                NavState *out, cudaStream_t s);
+// flags: VG_PREC_FP64 (0) or VG_PREC_MIXED (1)
 inline cudaError_t launch_step(const DevGeom &g, const StepArgs &a, uint32_t flags, cudaStream_t s)
 {
-  (void)flags;
-  return launch_step_fp64(g, a, s);
+  return (flags & 1u) ? launch_step_mixed(g, a, s) : launch_step_fp64(g, a, s);
 }
 
 } // namespace vg

@@ -1,0 +1,422 @@
+// Mixed-precision navigator (VG_PREC_MIXED). The reference algorithm and its FP64
+// arithmetic decide every result: the global-to-local transform, the mother's
+// DistanceToOut, the DistanceToIn of every daughter that can still win, and every
+// relocation Contains that is not certain. FP32 is used only to prune work that cannot
+// change the result:
+//   * BVH node and daughter boxes are tested in FP32 against copies inflated by kBoxPad
+//     (rounded outward), so a box the FP64 test enters is always entered;
+//   * each daughter surviving the box test gets an FP32 lower bound of its DistanceToIn
+//     from a conservative descriptor of its shape (bounding box, or cylindrical shell for
+//     tubes/cones/polycones/tori); only daughters whose bound is below the current step get
+//     the exact FP64 DistanceToIn, lowest bound first, so the step shrinks as early as it can;
+//   * Contains in relocation is decided in FP32 when the point is farther than kBoxPad from
+//     the descriptor's boundary, else in FP64.
+// A lower bound never exceeds the FP64 distance and a certain decision never disagrees
+// with FP64, so out-states and steps equal the FP64 path's; only exact ties between two
+// daughters could resolve differently (both sides keep the first one they evaluate).
+#pragma once
+#include "nav_fp64.cuh"
+
+namespace vg {
+namespace mixed {
+
+using f64::V3;
+
+// Pad (mm) added to every FP32 box/descriptor on each side. FP32 rounding of coordinates
+// up to 4 m is <= 2.4e-4 mm, and slab parameters carry <= ~1e-6 relative error, so a 4 um
+// pad keeps every FP32 inclusion test a superset of the FP64 one.
+constexpr float kBoxPad = 4e-3f;
+// Relative shrink applied to every FP32 lower bound (covers the FP32 rounding of the
+// quotient and square-root chains; 2^-16 is ~500 FP32 ulps).
+constexpr float kLbRel = 1.52587890625e-5f;
+
+struct F3 {
+  float x, y, z;
+};
+__device__ __forceinline__ F3 f3(V3 v) { return F3{(float)v.x, (float)v.y, (float)v.z}; }
+
+// Descriptor of a shape for FP32 bounds (host-built, 8 floats):
+//   kind 0: box lo[3], hi[3] (extent, local frame), flag: box is the shape itself
+//   kind 1: cylindrical shell rmin, rmax, zlo, zhi (local frame), flag: shell is the shape
+struct ShapeLB {
+  float kind, flag, a0, a1, a2, a3, a4, a5;
+};
+
+__device__ __forceinline__ float inv_dir(float d) { return 1.0f / (d + copysignf(1e-30f, d)); }
+
+// FP32 slab interval of a box padded by kBoxPad.
+__device__ __forceinline__ void slab_f(const float *lo, const float *hi, F3 p, F3 inv, float &tmin, float &tmax)
+{
+  float t0x = (lo[0] - kBoxPad - p.x) * inv.x, t1x = (hi[0] + kBoxPad - p.x) * inv.x;
+  float t0y = (lo[1] - kBoxPad - p.y) * inv.y, t1y = (hi[1] + kBoxPad - p.y) * inv.y;
+  float t0z = (lo[2] - kBoxPad - p.z) * inv.z, t1z = (hi[2] + kBoxPad - p.z) * inv.z;
+  tmin = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fminf(t0z, t1z));
+  tmax = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fmaxf(t0z, t1z));
+}
+__device__ __forceinline__ bool box_contains_f(const float *lo, const float *hi, F3 p)
+{
+  return p.x >= lo[0] - kBoxPad && p.x <= hi[0] + kBoxPad && p.y >= lo[1] - kBoxPad && p.y <= hi[1] + kBoxPad &&
+         p.z >= lo[2] - kBoxPad && p.z <= hi[2] + kBoxPad;
+}
+
+// Lower bound of DistanceToIn for a shell rmin <= r <= rmax, zlo <= z <= zhi (already
+// padded) from p along unit d; +inf when the ray certainly misses.
+__device__ __forceinline__ float shell_lb(float rmin, float rmax, float zlo, float zhi, F3 p, F3 d)
+{
+  // z slab
+  float tz = 0.f;
+  if (p.z < zlo) {
+    if (d.z <= 0.f) return INFINITY;
+    tz = (zlo - p.z) / d.z;
+  } else if (p.z > zhi) {
+    if (d.z >= 0.f) return INFINITY;
+    tz = (zhi - p.z) / d.z;
+  }
+  // radial
+  const float a  = fmaf(d.x, d.x, d.y * d.y);
+  const float b  = fmaf(p.x, d.x, p.y * d.y);
+  const float r2 = fmaf(p.x, p.x, p.y * p.y);
+  float tr       = 0.f;
+  if (r2 > rmax * rmax) {
+    const float c   = r2 - rmax * rmax;
+    const float err = (r2 + rmax * rmax) * 1e-6f + 1e-6f;
+    if (b >= 0.f && c > err) return INFINITY; // outside and not approaching the axis
+    const float disc = fmaf(b, b, -a * c);
+    const float derr = (b * b + a * (r2 + rmax * rmax)) * 1e-6f + 1e-12f;
+    if (disc + derr < 0.f) return INFINITY;
+    if (a <= 0.f) return 0.f;
+    tr = (-b - sqrtf(disc + derr)) / (a * (1.f + 1e-6f));
+  } else if (rmin > 0.f && r2 < rmin * rmin) {
+    const float c    = r2 - rmin * rmin; // < 0
+    const float disc = fmaf(b, b, -a * c);
+    const float derr = (b * b + a * (r2 + rmin * rmin)) * 1e-6f + 1e-12f;
+    const float dl   = fmaxf(disc - derr, 0.f);
+    if (a <= 1e-30f) return INFINITY;
+    tr = (-b + sqrtf(dl)) / (a * (1.f + 1e-6f));
+  }
+  return fmaxf(fmaxf(tz, tr), 0.f) * (1.f - kLbRel) - kBoxPad;
+}
+
+// Lower bound of DistanceToIn of a placed daughter (p, d in the mother frame). The
+// daughter's frame offset (p - t) is formed in FP64, the rotation in FP32.
+__device__ __forceinline__ float daughter_lb(const DevGeom &g, const ShapeLB *lbs, int pv, V3 p, V3 d)
+{
+  const Xform &m = g.pv_xf[pv];
+  const F3 q{(float)(p.x - m.t[0]), (float)(p.y - m.t[1]), (float)(p.z - m.t[2])};
+  const F3 dd = f3(d);
+  F3 lp, ld;
+  lp.x = fmaf(q.x, (float)m.r[0], fmaf(q.y, (float)m.r[3], q.z * (float)m.r[6]));
+  lp.y = fmaf(q.x, (float)m.r[1], fmaf(q.y, (float)m.r[4], q.z * (float)m.r[7]));
+  lp.z = fmaf(q.x, (float)m.r[2], fmaf(q.y, (float)m.r[5], q.z * (float)m.r[8]));
+  ld.x = fmaf(dd.x, (float)m.r[0], fmaf(dd.y, (float)m.r[3], dd.z * (float)m.r[6]));
+  ld.y = fmaf(dd.x, (float)m.r[1], fmaf(dd.y, (float)m.r[4], dd.z * (float)m.r[7]));
+  ld.z = fmaf(dd.x, (float)m.r[2], fmaf(dd.y, (float)m.r[5], dd.z * (float)m.r[8]));
+  const ShapeLB s = lbs[g.lv_shape[g.pv_lv[pv]]];
+  if (s.kind == 0.f) {
+    const float lo[3] = {s.a0, s.a1, s.a2}, hi[3] = {s.a3, s.a4, s.a5};
+    const F3 inv{inv_dir(ld.x), inv_dir(ld.y), inv_dir(ld.z)};
+    float tmin, tmax;
+    slab_f(lo, hi, lp, inv, tmin, tmax);
+    if (!(tmin <= tmax) || tmax < 0.f) return INFINITY;
+    if (tmin <= 0.f) return -INFINITY; // inside the padded box: the distance may be <= 0
+    return tmin * (1.f - kLbRel) - kBoxPad;
+  }
+  const float rmin = fmaxf(s.a0 - kBoxPad, 0.f), rmax = s.a1 + kBoxPad;
+  const float zlo = s.a2 - kBoxPad, zhi = s.a3 + kBoxPad;
+  const float r2  = fmaf(lp.x, lp.x, lp.y * lp.y);
+  if (lp.z >= zlo && lp.z <= zhi && r2 <= rmax * rmax && r2 >= rmin * rmin) return -INFINITY;
+  return shell_lb(rmin, rmax, zlo, zhi, lp, ld);
+}
+
+// Contains with an FP32 certain-outside / certain-inside test before the FP64 one.
+// Returns the daughter-local FP64 point in `lp` when it returns true.
+__device__ __forceinline__ bool pv_contains_mixed(const DevGeom &g, const ShapeLB *lbs, int pv, V3 p, V3 &lp)
+{
+  const Xform &m  = g.pv_xf[pv];
+  const V3 q{p.x - m.t[0], p.y - m.t[1], p.z - m.t[2]};
+  const F3 qf     = f3(q);
+  const F3 l{fmaf(qf.x, (float)m.r[0], fmaf(qf.y, (float)m.r[3], qf.z * (float)m.r[6])),
+             fmaf(qf.x, (float)m.r[1], fmaf(qf.y, (float)m.r[4], qf.z * (float)m.r[7])),
+             fmaf(qf.x, (float)m.r[2], fmaf(qf.y, (float)m.r[5], qf.z * (float)m.r[8]))};
+  const int shape = g.lv_shape[g.pv_lv[pv]];
+  const ShapeLB s = lbs[shape];
+  if (s.kind == 0.f) {
+    const float lo[3] = {s.a0, s.a1, s.a2}, hi[3] = {s.a3, s.a4, s.a5};
+    if (!box_contains_f(lo, hi, l)) return false;
+    if (s.flag != 0.f && l.x > lo[0] + kBoxPad && l.x < hi[0] - kBoxPad && l.y > lo[1] + kBoxPad &&
+        l.y < hi[1] - kBoxPad && l.z > lo[2] + kBoxPad && l.z < hi[2] - kBoxPad) {
+      lp = f64::to_local(m, p);
+      return true;
+    }
+  } else {
+    const float r2 = fmaf(l.x, l.x, l.y * l.y);
+    const float ro = s.a1 + kBoxPad, ri = fmaxf(s.a0 - kBoxPad, 0.f);
+    if (l.z < s.a2 - kBoxPad || l.z > s.a3 + kBoxPad || r2 > ro * ro || r2 < ri * ri) return false;
+    const float ro_in = s.a1 - kBoxPad, ri_in = s.a0 + kBoxPad;
+    if (s.flag != 0.f && l.z > s.a2 + kBoxPad && l.z < s.a3 - kBoxPad && r2 < ro_in * ro_in && r2 > ri_in * ri_in) {
+      lp = f64::to_local(m, p);
+      return true;
+    }
+  }
+  return f64::pv_contains(g, pv, p, lp);
+}
+
+// BVH::CheckDaughterIntersections with FP32 pruning (see file comment). Candidates wait in
+// a small buffer sorted by lower bound; when it is full the lowest is evaluated in FP64,
+// which tightens the step and drops every candidate that can no longer win.
+constexpr int kCandBuf = 8;
+
+__device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, const ShapeLB *lbs, int lv, V3 lp, V3 ld,
+                                                     double &step, int last_pv, int &hit_pv, int *nvisited)
+{
+  const int b = g.lv_bvh[lv];
+  if (b < 0) return kTrackOk;
+  const int node0 = g.bvh_node0[b];
+  const int dbase = g.lv_dstart[lv];
+  const F3 pf     = f3(lp);
+  const F3 ldf    = f3(ld);
+  const F3 inv{inv_dir(ldf.x), inv_dir(ldf.y), inv_dir(ldf.z)};
+  float bound = __double2float_ru(step);
+  float cl[kCandBuf] = {};
+  int cp[kCandBuf]   = {};
+  int nc = 0;
+  auto evaluate_first = [&]() {
+    const float lb = cl[0];
+    const int vol  = cp[0];
+    for (int k = 1; k < nc; ++k) cl[k - 1] = cl[k], cp[k - 1] = cp[k];
+    --nc;
+    if (lb >= bound) {
+      nc = 0;
+      return;
+    }
+    const double dist = f64::pv_dist_in(g, vol, lp, ld);
+    if (dist < step && !(dist <= 0.0 && vol == last_pv)) {
+      step   = dist;
+      hit_pv = vol;
+      bound  = __double2float_ru(step);
+      while (nc > 0 && cl[nc - 1] >= bound) --nc;
+    }
+  };
+  auto add = [&](float lb, int vol) {
+    if (!(lb < bound)) return;
+    if (nc == kCandBuf) {
+      evaluate_first();
+      if (!(lb < bound)) return;
+    }
+    int k = nc++;
+    while (k > 0 && cl[k - 1] > lb) cl[k] = cl[k - 1], cp[k] = cp[k - 1], --k;
+    cl[k] = lb, cp[k] = vol;
+  };
+  unsigned stack[32];
+  int sp     = 1;
+  stack[0]   = 0;
+  int visits = 0;
+  do {
+    const unsigned id = stack[--sp];
+    ++visits;
+    const NodeF nd = g.node_f[node0 + id];
+    if (nd.nchild >= 0) {
+      for (int i = 0; i < nd.nchild; ++i) {
+        const int prim = __ldg(&g.prim_id[nd.offset + i]);
+        const float *bx = g.prim_box_f + 6 * (size_t)(dbase + prim);
+        float tmin, tmax;
+        slab_f(bx, bx + 3, pf, inv, tmin, tmax);
+        if (tmin <= tmax && tmax >= 0.f && tmin < bound) {
+          const int vol = __ldg(&g.daughters[dbase + prim]);
+          add(daughter_lb(g, lbs, vol, lp, ld), vol);
+        }
+      }
+    } else {
+      const unsigned cl_ = 2 * id + 1, cr_ = 2 * id + 2;
+      const NodeF L = g.node_f[node0 + cl_], R = g.node_f[node0 + cr_];
+      float tminL, tmaxL, tminR, tmaxR;
+      slab_f(L.lo, L.hi, pf, inv, tminL, tmaxL);
+      slab_f(R.lo, R.hi, pf, inv, tminR, tmaxR);
+      const bool tl = tminL <= tmaxL && tmaxL >= 0.f && tminL < bound;
+      const bool tr = tminR <= tmaxR && tmaxR >= 0.f && tminR < bound;
+      if (sp + 2 > 32) {
+        if (nvisited) *nvisited = visits;
+        return kTrackErrStack;
+      }
+      if (tminR < tminL) {
+        if (tr) stack[sp++] = cr_;
+        if (tl) stack[sp++] = cl_;
+      } else {
+        if (tl) stack[sp++] = cl_;
+        if (tr) stack[sp++] = cr_;
+      }
+    }
+  } while (sp > 0);
+  while (nc > 0) evaluate_first();
+  if (nvisited) *nvisited = visits;
+  return kTrackOk;
+}
+
+// BVH::LevelLocate with FP32 box tests (padded) and mixed Contains.
+__device__ __forceinline__ bool level_locate_mixed(const DevGeom &g, const ShapeLB *lbs, int lv, int excl_pv, V3 lp,
+                                                   int &pv, V3 &dlp, int &status)
+{
+  const int b     = g.lv_bvh[lv];
+  const int node0 = g.bvh_node0[b];
+  const int dbase = g.lv_dstart[lv];
+  const F3 pf     = f3(lp);
+  unsigned stack[32];
+  int sp   = 1;
+  stack[0] = 0;
+  do {
+    const unsigned id = stack[--sp];
+    const NodeF nd    = g.node_f[node0 + id];
+    if (nd.nchild >= 0) {
+      for (int i = 0; i < nd.nchild; ++i) {
+        const int prim  = __ldg(&g.prim_id[nd.offset + i]);
+        const float *bx = g.prim_box_f + 6 * (size_t)(dbase + prim);
+        if (box_contains_f(bx, bx + 3, pf)) {
+          const int vol = __ldg(&g.daughters[dbase + prim]);
+          if (vol != excl_pv && pv_contains_mixed(g, lbs, vol, lp, dlp)) {
+            pv = vol;
+            return true;
+          }
+        }
+      }
+    } else {
+      if (sp + 2 > 32) {
+        status = kTrackErrStack;
+        return false;
+      }
+      const unsigned cl = 2 * id + 1, cr = 2 * id + 2;
+      const NodeF L = g.node_f[node0 + cl], R = g.node_f[node0 + cr];
+      if (box_contains_f(L.lo, L.hi, pf)) stack[sp++] = cl;
+      if (box_contains_f(R.lo, R.hi, pf)) stack[sp++] = cr;
+    }
+  } while (sp > 0);
+  return false;
+}
+
+__device__ __forceinline__ bool shape_contains_mixed(const DevGeom &g, const ShapeLB *lbs, int shape, V3 p)
+{
+  const ShapeLB s = lbs[shape];
+  const F3 l      = f3(p);
+  if (s.kind == 0.f) {
+    const float lo[3] = {s.a0, s.a1, s.a2}, hi[3] = {s.a3, s.a4, s.a5};
+    if (!box_contains_f(lo, hi, l)) return false;
+    if (s.flag != 0.f && l.x > lo[0] + kBoxPad && l.x < hi[0] - kBoxPad && l.y > lo[1] + kBoxPad &&
+        l.y < hi[1] - kBoxPad && l.z > lo[2] + kBoxPad && l.z < hi[2] - kBoxPad)
+      return true;
+  } else {
+    const float r2 = fmaf(l.x, l.x, l.y * l.y);
+    const float ro = s.a1 + kBoxPad, ri = fmaxf(s.a0 - kBoxPad, 0.f);
+    if (l.z < s.a2 - kBoxPad || l.z > s.a3 + kBoxPad || r2 > ro * ro || r2 < ri * ri) return false;
+    const float ro_in = s.a1 - kBoxPad, ri_in = s.a0 + kBoxPad;
+    if (s.flag != 0.f && l.z > s.a2 + kBoxPad && l.z < s.a3 - kBoxPad && r2 < ro_in * ro_in && r2 > ri_in * ri_in)
+      return true;
+  }
+  return f64::shape_contains(g, shape, p);
+}
+
+__device__ __forceinline__ int locate_global_point_mixed(const DevGeom &g, const ShapeLB *lbs, int vol, V3 p,
+                                                         uint32_t &nav, bool top, int &status)
+{
+  int cand = vol;
+  if (top) cand = shape_contains_mixed(g, lbs, f64::pv_shape(g, vol), p) ? vol : -1;
+  if (cand < 0) return -1;
+  nav    = f64::nav_push(g, nav, cand);
+  int lv = g.pv_lv[cand];
+  for (int level = 0; level < 256; ++level) {
+    if (g.lv_nd[lv] == 0) return f64::nav_top(g, nav);
+    int pv = -1;
+    V3 tp;
+    if (!level_locate_mixed(g, lbs, lv, -1, p, pv, tp, status)) return f64::nav_top(g, nav);
+    nav  = f64::nav_push(g, nav, pv);
+    cand = f64::nav_top(g, nav);
+    lv   = g.pv_lv[cand];
+    p    = tp;
+  }
+  status = kTrackErrIter;
+  return f64::nav_top(g, nav);
+}
+
+__device__ __forceinline__ void locate_excl_mixed(const DevGeom &g, const ShapeLB *lbs, int vol, int excl, V3 p,
+                                                  uint32_t &nav, int &status)
+{
+  int cand = vol;
+  nav      = f64::nav_push(g, nav, cand);
+  int lv   = g.pv_lv[cand];
+  for (int level = 0; level < 256; ++level) {
+    if (g.lv_nd[lv] == 0) return;
+    V3 tp;
+    if (!level_locate_mixed(g, lbs, lv, excl, p, cand, tp, status)) return;
+    lv  = g.pv_lv[cand];
+    p   = tp;
+    nav = f64::nav_push(g, nav, cand);
+  }
+  status = kTrackErrIter;
+}
+
+__device__ __forceinline__ void relocate_force_different_mixed(const DevGeom &g, const ShapeLB *lbs, V3 lp,
+                                                               uint32_t &nav, int &status)
+{
+  int cur         = f64::nav_top(g, nav);
+  const int entry = cur;
+  if (cur < 0) return;
+  for (int level = 0; level < 256 && cur >= 0; ++level) {
+    if (cur == entry || !shape_contains_mixed(g, lbs, f64::pv_shape(g, cur), lp)) {
+      nav = f64::nav_pop(g, nav);
+      lp  = f64::to_master(g.pv_xf[cur], lp);
+      cur = f64::nav_top(g, nav);
+    } else {
+      nav = f64::nav_pop(g, nav);
+      locate_excl_mixed(g, lbs, cur, entry, lp, nav, status);
+      return;
+    }
+  }
+}
+
+// ComputeStepAndPropagatedState with FP32 pruning (same control flow as f64::compute_step).
+__device__ __forceinline__ double compute_step_mixed(const DevGeom &g, const ShapeLB *lbs, V3 gp, V3 gd, double limit,
+                                                     NavState const &in, NavState &out, int &status, int *nvisited)
+{
+  out    = in;
+  status = kTrackOk;
+  if (in.navInd == 0) {
+    status = kTrackErrState;
+    return 0.;
+  }
+  const Xform m = f64::nav_top_matrix(g, in.navInd);
+  const V3 lp   = f64::to_local(m, gp);
+  const V3 ld   = f64::rotate(m, gd);
+  const int pv  = f64::nav_top(g, in.navInd);
+  const int lv  = g.pv_lv[pv];
+  double step   = f64::shape_dist_out(g, g.lv_shape[lv], lp, ld);
+  if (step < 0.) step = 0.;
+  int hit = -1;
+  if (g.lv_nd[lv] > 0) {
+    const int last = f64::nav_top(g, in.lastExited);
+    status         = check_daughters_mixed(g, lbs, lv, lp, ld, step, last, hit, nvisited);
+    if (status != kTrackOk) return 0.;
+  }
+  if (step == kInfLength && limit > 0.) {
+    out.onBoundary = 1;
+    out.navInd     = f64::nav_pop(g, out.navInd);
+    return kTolerance;
+  }
+  if (step > limit) {
+    out.onBoundary = 0;
+    return limit;
+  }
+  out.onBoundary = 1;
+  out.lastExited = out.navInd;
+  if (hit >= 0) out.navInd = f64::nav_push(g, out.navInd, hit);
+  if (step < 0.) step = 0.;
+  const double s = step + 1E-6;
+  const V3 after{lp.x + s * ld.x, lp.y + s * ld.y, lp.z + s * ld.z};
+  if (hit < 0) {
+    relocate_force_different_mixed(g, lbs, after, out.navInd, status);
+  } else {
+    out.navInd = f64::nav_pop(g, out.navInd);
+    locate_global_point_mixed(g, lbs, hit, f64::to_local(g.pv_xf[hit], after), out.navInd, false, status);
+  }
+  return step;
+}
+
+} // namespace mixed
+} // namespace vg

@@ -243,7 +243,7 @@ __device__ __forceinline__ bool tube_contains(const TubeRec &t, V3 p)
 }
 
 // TubeImplementation.h:456-596 DistanceToInKernel
-__device__ __noinline__ double tube_dist_in_kernel(const TubeRec &t, V3 point, V3 dir)
+static __device__ __noinline__ double tube_dist_in_kernel(const TubeRec &t, V3 point, V3 dir)
 {
   double distz = fabs(point.z) - t.z;
   if (distz > kHalfTolerance && point.z * dir.z >= 0) return kInfLength;
@@ -312,7 +312,7 @@ __device__ __forceinline__ double tube_dist_in(const TubeRec &t, V3 p, V3 d)
 }
 
 // TubeImplementation.h:601-697 DistanceToOut
-__device__ __noinline__ double tube_dist_out(const TubeRec &t, V3 point, V3 dir)
+static __device__ __noinline__ double tube_dist_out(const TubeRec &t, V3 point, V3 dir)
 {
   if (t.z - fabs(point.z) < -kHalfTolerance) return -1.;
   const double rsq   = point.x * point.x + point.y * point.y;
@@ -464,7 +464,7 @@ __device__ __forceinline__ void cone_phi_plane(const ConeRec &c, double ax, doub
 }
 
 // ConeUtilities.h:551-684 (scalar DetectIntersectionAndCalculateDistanceToConicalSurface)
-__device__ __noinline__ bool cone_conical(const ConeRec &c, V3 point, V3 dir, bool forDistToIn, bool inner,
+static __device__ __noinline__ bool cone_conical(const ConeRec &c, V3 point, V3 dir, bool forDistToIn, bool inner,
                                           double &distance)
 {
   distance           = kInfLength;
@@ -591,7 +591,7 @@ __device__ __forceinline__ bool cone_contains(const ConeRec &c, V3 p)
 }
 
 // ConeImplementation.h:126-258
-__device__ __noinline__ double cone_dist_in(const ConeRec &c, V3 point, V3 dir)
+static __device__ __noinline__ double cone_dist_in(const ConeRec &c, V3 point, V3 dir)
 {
   double distz = fabs(point.z) - c.dz;
   if ((distz > kConeTolerance && (point.z * dir.z) >= 0.) || (fabs(distz) < kConeTolerance && (point.z * dir.z) > 0.))
@@ -642,7 +642,7 @@ __device__ __noinline__ double cone_dist_in(const ConeRec &c, V3 point, V3 dir)
 }
 
 // ConeImplementation.h:260-370
-__device__ __noinline__ double cone_dist_out(const ConeRec &c, V3 point, V3 dir)
+static __device__ __noinline__ double cone_dist_out(const ConeRec &c, V3 point, V3 dir)
 {
   const double distz    = fabs(point.z) - c.dz;
   const double rsq      = perp2(point);

@@ -68,7 +68,7 @@ __device__ __forceinline__ bool trd_face(const TrdRec &t, V3 pos, V3 dir, bool f
 }
 __device__ __forceinline__ double trd_clamp(double d) { return fabs(d) < kHalfTolerance ? 0.0 : d; }
 // TrdImplementation.h:288-370
-__device__ __noinline__ double trd_dist_in(const TrdRec &t, V3 p, V3 d)
+static __device__ __noinline__ double trd_dist_in(const TrdRec &t, V3 p, V3 d)
 {
   double distance  = kInfLength;
   const bool inz   = fabs(p.z) < t.dz - kHalfTolerance;
@@ -108,7 +108,7 @@ __device__ __noinline__ double trd_dist_in(const TrdRec &t, V3 p, V3 d)
   return trd_clamp(distance);
 }
 // TrdImplementation.h:371-470
-__device__ __noinline__ double trd_dist_out(const TrdRec &t, V3 p, V3 d)
+static __device__ __noinline__ double trd_dist_out(const TrdRec &t, V3 p, V3 d)
 {
   const double invdir = 1. / fabs(d.z + kTiny);
   const bool vary     = t.dy1 != t.dy2;
@@ -191,7 +191,7 @@ __device__ __forceinline__ void pc_section(const PolyconeView &v, int i, V3 p, b
   }
   cone_classify(v.cone(i), v.local(p, i), forInside, cin, cout);
 }
-__device__ __noinline__ void polycone_classify(const PolyconeRec &rec, V3 p, bool forInside, bool &cin, bool &cout)
+static __device__ __noinline__ void polycone_classify(const PolyconeRec &rec, V3 p, bool forInside, bool &cin, bool &cout)
 {
   const PolyconeView v(rec);
   const int lo = v.index(p.z - kTolerance);
@@ -227,7 +227,7 @@ __device__ __forceinline__ bool polycone_contains(const PolyconeRec &r, V3 p)
   return !cout;
 }
 // PolyconeImplementation.h:148-180
-__device__ __noinline__ double polycone_dist_in(const PolyconeRec &rec, V3 p, V3 d)
+static __device__ __noinline__ double polycone_dist_in(const PolyconeRec &rec, V3 p, V3 d)
 {
   const PolyconeView v(rec);
   double distance = kInfLength;
@@ -244,7 +244,7 @@ __device__ __noinline__ double polycone_dist_in(const PolyconeRec &rec, V3 p, V3
   return distance;
 }
 // PolyconeImplementation.h:181-300
-__device__ __noinline__ double polycone_dist_out(const PolyconeRec &rec, V3 point, V3 dir)
+static __device__ __noinline__ double polycone_dist_out(const PolyconeRec &rec, V3 point, V3 dir)
 {
   const PolyconeView v(rec);
   if (v.nsec == 1) return cone_dist_out(v.cone(0), v.local(point, 0), dir);
@@ -298,7 +298,7 @@ __device__ __noinline__ double polycone_dist_out(const PolyconeRec &rec, V3 poin
   return total;
 }
 // PolyconeImplementation.h:301-354
-__device__ __noinline__ double polycone_safety_in(const PolyconeRec &rec, V3 p)
+static __device__ __noinline__ double polycone_safety_in(const PolyconeRec &rec, V3 p)
 {
   const PolyconeView v(rec);
   int index  = v.index(p.z);
@@ -327,7 +327,7 @@ __device__ __noinline__ double polycone_safety_in(const PolyconeRec &rec, V3 p)
   return minSafety;
 }
 // PolyconeImplementation.h:355-410
-__device__ __noinline__ double polycone_safety_out(const PolyconeRec &rec, V3 p)
+static __device__ __noinline__ double polycone_safety_out(const PolyconeRec &rec, V3 p)
 {
   const PolyconeView v(rec);
   bool cin = false, cout = false;

@@ -60,7 +60,7 @@ __device__ __forceinline__ void sort4(double *x)
   cswap(x[1], x[2]);
 }
 // TorusImplementation2.h:84-150
-__device__ __noinline__ int solve_quartic(double a, double b, double c, double d, double *x)
+static __device__ __noinline__ int solve_quartic(double a, double b, double c, double d, double *x)
 {
   const double e = b - 3. * a * a / 8.;
   const double f = c + a * a * a / 8. - 0.5 * a * b;
@@ -176,7 +176,7 @@ __device__ __forceinline__ double quartic_d(double s, double a, double b, double
 }
 
 // TorusImplementation2.h:292-389 ToBoundary
-__device__ __noinline__ double torus_to_boundary(const TorusRec &t, V3 pt, V3 dir, double radius, bool out)
+static __device__ __noinline__ double torus_to_boundary(const TorusRec &t, V3 pt, V3 dir, double radius, bool out)
 {
   const double tol    = 100. * kTolerance;
   const double r0sq   = pt.x * pt.x + pt.y * pt.y + pt.z * pt.z;
@@ -250,7 +250,7 @@ __device__ __noinline__ double torus_to_boundary(const TorusRec &t, V3 pt, V3 di
 }
 
 // TorusImplementation2.h:140-222
-__device__ __noinline__ double torus_dist_out(const TorusRec &t, V3 p, V3 dir)
+static __device__ __noinline__ double torus_dist_out(const TorusRec &t, V3 p, V3 dir)
 {
   const double rsq       = p.x * p.x + p.y * p.y;
   const double outerExcl = t.rtor + t.rmax + kHalfTolerance;
@@ -289,7 +289,7 @@ __device__ __noinline__ double torus_dist_out(const TorusRec &t, V3 p, V3 dir)
 }
 
 // TorusImplementation2.h:421-488 (VECGEOM_NO_SPECIALIZATION branch)
-__device__ __noinline__ double torus_dist_in(const TorusRec &t, V3 p, V3 dir)
+static __device__ __noinline__ double torus_dist_in(const TorusRec &t, V3 p, V3 dir)
 {
   const bool inBounds = tube_contains(t.bt, p);
   const double tubeDistance = inBounds ? 0. : tube_dist_in(t.bt, p, dir);

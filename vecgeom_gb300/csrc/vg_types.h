@@ -151,6 +151,7 @@ struct DevGeom {
   const double *prim_box;     // 6 doubles per daughter slot (indexed lv_dstart + daughter index)
   const NodeF *node_f;        // FP32 node records (bounds rounded outward)
   const float *prim_box_f;    // FP32 daughter boxes (6 floats per slot, rounded outward)
+  const float *shape_lbd;     // FP32 bounding descriptor per shape (8 floats, see nav_mixed.cuh)
   const uint32_t *nav;        // NavIndex table
   int32_t world_pv;
   int32_t max_depth;

@@ -267,3 +267,40 @@ def shape_points_mixed(lo, hi, n, seed, inside_fn, dist_out_fn, surface_band=1e-
     perm = rng(seed, 13).permutation(len(px))
     dirs = isotropic(rng(seed, 14), len(px))
     return (px[perm].copy(), py[perm].copy(), pz[perm].copy()), dirs
+
+
+def sample_transport_steps(geo, n_samples, seed, torch, device, n_primaries=1 << 20, max_steps=200, flags=0):
+    """Realistic step inputs: straight primaries from the origin (config-5 distribution) are
+    transported on the GPU with the FP64 navigator; every (point, direction, state) before
+    a step is a candidate, and `n_samples` of them are drawn uniformly (seeded). Returns
+    device tensors x, y, z, dx, dy, dz (FP64) and states (uint8, 12 B each)."""
+    (x, y, z), (dx, dy, dz) = primaries_eta_phi(n_primaries, seed)
+    t = [torch.from_numpy(a).to(device) for a in (x, y, z, dx, dy, dz)]
+    st = torch.empty(n_primaries * 12, dtype=torch.uint8, device=device)
+    geo.locate_point(t[0], t[1], t[2], st)
+    out = torch.empty_like(st)
+    step = torch.empty(n_primaries, dtype=torch.float64, device=device)
+    pool = [[] for _ in range(7)]
+    px, py, pz, ddx, ddy, ddz = t
+    for _ in range(max_steps):
+        nav = st.view(torch.int32).view(-1, 3)[:, 0]
+        alive = nav != 0
+        if not bool(alive.any()):
+            break
+        idx = alive.nonzero().squeeze(1)
+        for k, a in enumerate((px, py, pz, ddx, ddy, ddz)):
+            pool[k].append(a[idx])
+        pool[6].append(st.view(-1, 12)[idx])
+        geo.compute_step_and_next_volume(px, py, pz, ddx, ddy, ddz, st, out, step, flags=flags)
+        m = alive.to(torch.float64)
+        px = px + m * (step * ddx)
+        py = py + m * (step * ddy)
+        pz = pz + m * (step * ddz)
+        st = torch.where(alive.unsqueeze(1), out.view(-1, 12), st.view(-1, 12)).reshape(-1).contiguous()
+    cat = [torch.cat(p) for p in pool]
+    total = cat[0].numel()
+    gen = torch.Generator(device="cpu").manual_seed(seed & 0x7FFFFFFF)
+    pick = torch.randperm(total, generator=gen)[:n_samples].to(device)
+    res = [c[pick].contiguous() for c in cat[:6]]
+    states = cat[6][pick].reshape(-1).contiguous()
+    return res, states, total
