@@ -30,6 +30,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 STEP_BYTES = 24 + 24 + 12 + 12 + 8  # p, d, state in, state out, step (FP64 SoA + 12 B states)
+# name -> (precision | scheduling flags): 1 = VG_PREC_MIXED, 2 = VG_NAV_SORT, 4 = VG_NAV_QUEUE
+SCHEDULES = {"fp64": 0, "fp64_sort": 2, "mixed": 1, "mixed_sort": 3, "mixed_queue": 5, "mixed_sort_queue": 7}
 
 
 def parse():
@@ -43,6 +45,9 @@ def parse():
     ap.add_argument("--primaries", type=int, default=1 << 20)
     ap.add_argument("--seed", type=int, default=0xC0FFEE)
     ap.add_argument("--cpu-sample", type=int, default=1 << 17)
+    ap.add_argument("--schedule", default="mixed_sort_queue", choices=sorted(SCHEDULES),
+                    help="precision and scheduling of the headline measurement")
+    ap.add_argument("--variants", type=int, default=1, help="also time the other schedules (1/0)")
     return ap.parse_args()
 
 
@@ -265,13 +270,43 @@ def main():
             ms = float(v.item())
         return ms / args.steps
 
+    head = SCHEDULES[args.schedule]
     ms_fp64 = timed(vg.PREC_FP64)
     out64, step64 = out.clone(), step.clone()
+    variants = {"fp64": ms_fp64}
+    identical = True
+    if args.variants:
+        for name, f in sorted(SCHEDULES.items()):
+            if name in ("fp64", args.schedule):
+                continue
+            variants[name] = timed(f)
+            identical &= bool(torch.equal(out64, out)) and bool(torch.equal(step64, step))
     with ClockSampler(local) as clocks:
-        ms_mixed = timed(vg.PREC_MIXED)
+        ms_head = timed(head)
+    variants[args.schedule] = ms_head
     n_err = int((status != 0).sum().item())
     ids_equal = bool(torch.equal(out64, out))
     step_err = float((step64 - step).abs().max().item())
+
+    # the track sort alone (part of every sorted step), to separate the step kernel's time
+    ms_sort = 0.0
+    passes = 0
+    if head & vg.NAV_SORT:
+        order = torch.empty(n, dtype=torch.int32, device=dev)
+        wsp = torch.empty(vg.Geometry.step_workspace_bytes(n, vg.NAV_SORT), dtype=torch.uint8, device=dev)
+        for _ in range(args.warmup):
+            geo.sort_tracks(t[0], t[1], t[2], st, order, workspace=wsp)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(args.steps):
+            geo.sort_tracks(t[0], t[1], t[2], st, order, workspace=wsp)
+        e1.record()
+        torch.cuda.synchronize()
+        ms_sort = e0.elapsed_time(e1) / args.steps
+        _, _, cb, lb = geo.sort_key_params()
+        passes = (lb + 3 * cb + 7) // 8
+    ms_kernel = ms_head - ms_sort
 
     # e2e: host arrays through the host-pointer C-ABI entry point, copies inside the timed region
     hp = [a.cpu().pin_memory() for a in t]
@@ -279,12 +314,12 @@ def main():
     hout = torch.empty_like(hst).pin_memory()
     hstep = torch.empty(n, dtype=torch.float64).pin_memory()
     for _ in range(2):
-        geo.compute_step_and_next_volume_host(*hp, hst, hout, hstep, flags=vg.PREC_MIXED)
+        geo.compute_step_and_next_volume_host(*hp, hst, hout, hstep, flags=head)
     barrier()
     ke = max(3, args.steps // 4)
     t0 = time.perf_counter()
     for _ in range(ke):
-        geo.compute_step_and_next_volume_host(*hp, hst, hout, hstep, flags=vg.PREC_MIXED)
+        geo.compute_step_and_next_volume_host(*hp, hst, hout, hstep, flags=head)
     torch.cuda.synchronize()
     barrier()
     e2e_s = (time.perf_counter() - t0) / ke
@@ -295,27 +330,30 @@ def main():
     except (OSError, ValueError):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    value = ws * n / (ms_mixed * 1e-3)
-    achieved = STEP_BYTES * n / (ms_mixed * 1e-3) / 1e9
+    value = ws * n / (ms_head * 1e-3)
+    achieved = STEP_BYTES * n / (ms_kernel * 1e-3) / 1e9
     line = {
         "metric": "nav steps/s", "value": value, "unit": "nav steps/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": ms_head, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64 (mixed: FP32 pruning, FP64 decisions)",
         "data": "synthetic (seeded; geometry built in code, tracks generated on the GPU)",
-        "config": dict(config_of(args, pool), precision="VG_PREC_MIXED",
+        "config": dict(config_of(args, pool), schedule=args.schedule,
                        l2="inputs %.0f MB > L2 (129 MB); geometry L2/HBM-resident by design" % (n * 60 / 1e6),
                        parallelism="replicas" if ws > 1 else "single GPU"),
         "plain_fp64": {"value": ws * n / (ms_fp64 * 1e-3), "ms_per_step": ms_fp64},
-        "speedup_vs_plain_fp64": ms_fp64 / ms_mixed,
+        "speedup_vs_plain_fp64": ms_fp64 / ms_head,
         "ids_identical_to_fp64": ids_equal, "max_step_diff_vs_fp64_mm": step_err,
+        "schedules_ms_per_step": variants, "all_schedules_identical_to_fp64": identical and ids_equal,
+        "sort_ms_per_step": ms_sort, "step_kernel_ms_per_step": ms_kernel,
         "e2e": {"value": ws * n / e2e_s, "unit": "nav steps/s", "h2d_bytes_per_step": n * (48 + 12),
                 "d2h_bytes_per_step": n * (12 + 8)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": None,
-                     "note": "algorithmic bytes %d B/step; the kernel is issue/latency bound (FP64 pipe for "
-                             "the plain path), see profiles/; peak %s" % (STEP_BYTES,
-                                                                        "of measured" if peaks else "of fallback")},
-        "gpu_launches": args.steps,
+                     "kernel": "k_step_mixed_queue" if head & 4 else ("k_step_mixed" if head & 1 else "k_step"),
+                     "note": "algorithmic bytes %d B/step over the step kernel's time (sort excluded); the "
+                             "kernel is issue/latency bound, not HBM-bound, see profiles/; peak %s"
+                             % (STEP_BYTES, "of measured" if peaks else "of fallback")},
+        "gpu_launches": args.steps * (1 + ((1 + 3 * passes) if head & 2 else 0)),
         "track_errors": n_err,
         "clocks": clocks.summary(),
     }

@@ -53,6 +53,14 @@ extern "C" {
 #define VG_PREC_FP64 0u  /* plain FP64: results identical to the reference's FP64 path          */
 #define VG_PREC_MIXED 1u /* FP32 bulk arithmetic with FP64 guard band and FP64 recompute        */
 
+/* Scheduling flags for the navigation step (OR-ed with a precision flag). They change the
+ * order in which the device visits tracks, never a track's result (outputs stay at each
+ * track's own index). They need a workspace: vg_nav_compute_step_and_next_volume_ws, or
+ * the host entry point, which keeps one in the handle. The reference has no counterpart:
+ * its SoA navigator loops over tracks in input order (VNavigator.h:128-132). */
+#define VG_NAV_SORT 2u  /* radix-sort tracks by (logical volume, Morton cell of the position)   */
+#define VG_NAV_QUEUE 4u /* persistent kernel, warps take 32-track chunks from a global counter  */
+
 /* Navigation state: bit-identical to vecgeom::NavStateIndex {NavIndex_t fNavInd;
  * NavIndex_t fLastExited; bool fOnBoundary;} (VecGeom/navigation/NavStateIndex.h:39-41). */
 typedef struct vg_navstate {
@@ -177,11 +185,35 @@ int vg_nav_compute_step_and_next_volume(const vg_geom *g, const double *x, const
                                         const double *step_limit, const vg_navstate *in, vg_navstate *out,
                                         double *step, int32_t *status, size_t n, uint32_t flags, void *stream);
 
+/* The same step with scheduling flags. `workspace` is device memory of at least
+ * vg_nav_step_workspace_bytes(n, flags) bytes (256-byte aligned), used by this call only
+ * until the stream reaches its end; concurrent calls need separate workspaces. With
+ * flags < VG_NAV_SORT no workspace is needed and the call equals the one above. */
+size_t vg_nav_step_workspace_bytes(size_t n, uint32_t flags);
+int vg_nav_compute_step_and_next_volume_ws(const vg_geom *g, const double *x, const double *y, const double *z,
+                                           const double *dx, const double *dy, const double *dz,
+                                           const double *step_limit, const vg_navstate *in, vg_navstate *out,
+                                           double *step, int32_t *status, size_t n, uint32_t flags, void *workspace,
+                                           size_t workspace_bytes, void *stream);
+
+/* The visiting order VG_NAV_SORT uses, for callers that want to reorder their own track
+ * arrays: key = logical-volume id of the state's top volume << 3*cell_bits | Morton code of
+ * the position's cell (cell_bits per axis over the world box; cell = (float)(c - lo) * scale
+ * truncated and clamped to [0, 2^cell_bits - 1]); states outside the world get 0xffffffff.
+ * `order` receives the track indices sorted stably by key, `keys` (nullable) the sorted
+ * keys. The workspace is sized by vg_nav_step_workspace_bytes(n, VG_NAV_SORT). No
+ * reference counterpart. */
+int vg_nav_sort_tracks(const vg_geom *g, const double *x, const double *y, const double *z, const vg_navstate *in,
+                       size_t n, uint32_t *order, uint32_t *keys, void *workspace, size_t workspace_bytes,
+                       void *stream);
+int vg_nav_sort_key_params(const vg_geom *g, float lo[3], float scale[3], int32_t *cell_bits, int32_t *lv_bits);
+
 /* Same step with HOST arrays, the form the reference's own SoA navigator interface takes
  * (VNavigator::ComputeStepsAndPropagatedStates, VNavigator.h:128-132): inputs are copied to
  * device staging buffers owned by the handle (allocated on first use, grown on demand,
  * serialised by a lock), the kernel runs on `stream`, results are copied back and the call
- * returns after the stream has synchronised. Pinned host memory gives full copy bandwidth. */
+ * returns after the stream has synchronised. Pinned host memory gives full copy bandwidth.
+ * `flags` may include VG_NAV_SORT / VG_NAV_QUEUE (the workspace is part of the staging). */
 int vg_nav_compute_step_and_next_volume_host(vg_geom *g, const double *x, const double *y, const double *z,
                                              const double *dx, const double *dy, const double *dz,
                                              const double *step_limit, const vg_navstate *in, vg_navstate *out,

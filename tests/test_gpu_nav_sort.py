@@ -1,0 +1,130 @@
+"""Track ordering (VG_NAV_SORT) and the persistent work queue (VG_NAV_QUEUE): the sort key
+and stable order match a numpy restatement bit for bit, and every scheduling variant gives
+out-states and steps identical to the plain launch, in FP64 and in mixed precision."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _spread(n, seed, rmax, zmax):
+    from vecgeom_gb300 import workloads as W
+    gg = W.rng(seed, 1)
+    r = rmax * np.sqrt(gg.random(n))
+    ph = 2 * np.pi * gg.random(n)
+    z = zmax * (2 * gg.random(n) - 1)
+    return (r * np.cos(ph), r * np.sin(ph), z), W.isotropic(W.rng(seed, 2), n)
+
+
+@pytest.fixture(scope="module", params=["barrel", "detector"])
+def geo(request, cuda):
+    import vecgeom_gb300 as vg
+    from vecgeom_gb300 import workloads as W
+    g = vg.Geometry()
+    (W.build_barrel if request.param == "barrel" else W.build_detector)(g)
+    zmax = 2950.0 if request.param == "detector" else 400.0
+    # n not a multiple of the 4096-entry sort tile, to cover ragged tiles
+    pts, dirs = _spread((1 << 17) + 1234, 313, 1250.0, zmax)
+    dev = [cuda.from_numpy(np.ascontiguousarray(a)).to("cuda:0") for a in (*pts, *dirs)]
+    st = cuda.empty(len(pts[0]) * 12, dtype=cuda.uint8, device="cuda:0")
+    g.locate_point(*dev[:3], st)
+    return request.param, g, pts, dev, st
+
+
+def _keys_numpy(g, pts, states):
+    """Restatement of the sort key documented for vg_nav_sort_tracks."""
+    lo, sc, cb, lb = g.sort_key_params()
+    nav = g.nav_table()
+    pv_lv = np.asarray(g.pv_lv, dtype=np.uint32)
+    ni = states["nav_ind"].astype(np.int64)
+    key = np.full(len(ni), 0xFFFFFFFF, dtype=np.uint32)
+    ok = ni != 0
+    lv = pv_lv[nav[ni[ok] + 1]]
+    maxc = (1 << cb) - 1
+
+    def cell(c, k):
+        f = (c.astype(np.float32) - np.float32(lo[k])) * np.float32(sc[k])
+        q = np.where(f > 0, np.minimum(f, np.float32(maxc)), 0).astype(np.uint32)
+        return q
+
+    def spread(v):
+        out = np.zeros_like(v)
+        for b in range(cb):
+            out |= ((v >> b) & 1) << (3 * b)
+        return out
+
+    m = spread(cell(pts[0][ok], 0)) | (spread(cell(pts[1][ok], 1)) << 1) | (spread(cell(pts[2][ok], 2)) << 2)
+    key[ok] = (lv.astype(np.uint32) << np.uint32(3 * cb)) | m
+    return key
+
+
+def test_sort_order_is_stable_and_keys_match(cuda, geo):
+    import vecgeom_gb300 as vg
+    name, g, pts, dev, st = geo
+    n = dev[0].numel()
+    order = cuda.empty(n, dtype=cuda.int32, device="cuda:0")
+    keys = cuda.empty(n, dtype=cuda.int32, device="cuda:0")
+    g.sort_tracks(*dev[:3], st, order, keys)
+    o = order.cpu().numpy().view(np.uint32)
+    k = keys.cpu().numpy().view(np.uint32)
+    states = st.cpu().numpy().view(vg.NAVSTATE_DTYPE)
+    ref = _keys_numpy(g, pts, states)
+    assert np.array_equal(np.sort(o), np.arange(n, dtype=np.uint32))
+    assert np.array_equal(k, ref[o])
+    assert np.array_equal(o, np.argsort(ref, kind="stable").astype(np.uint32))
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_scheduling_variants_identical(cuda, geo, prec):
+    import vecgeom_gb300 as vg
+    name, g, pts, dev, st = geo
+    n = dev[0].numel()
+
+    def run(flags):
+        out = cuda.empty(n * 12, dtype=cuda.uint8, device="cuda:0")
+        step = cuda.empty(n, dtype=cuda.float64, device="cuda:0")
+        status = cuda.empty(n, dtype=cuda.int32, device="cuda:0")
+        g.compute_step_and_next_volume(*dev, st, out, step, status=status, flags=flags)
+        return out.cpu().numpy(), step.cpu().numpy(), status.cpu().numpy()
+
+    base = run(prec)
+    variants = [prec | vg.NAV_SORT]
+    if prec == vg.PREC_MIXED:
+        variants += [prec | vg.NAV_QUEUE, prec | vg.NAV_SORT | vg.NAV_QUEUE]
+    for f in variants:
+        got = run(f)
+        for a, b in zip(base, got):
+            assert np.array_equal(a, b), f
+
+
+def test_host_entry_sorted_queue(cuda, geo):
+    import vecgeom_gb300 as vg
+    name, g, pts, dev, st = geo
+    n = dev[0].numel()
+    h = [d.cpu().numpy() for d in dev]
+    sh = st.cpu().numpy()
+    out_d = cuda.empty(n * 12, dtype=cuda.uint8, device="cuda:0")
+    step_d = cuda.empty(n, dtype=cuda.float64, device="cuda:0")
+    g.compute_step_and_next_volume(*dev, st, out_d, step_d, flags=vg.PREC_MIXED)
+    out_h = np.empty(n * 12, dtype=np.uint8)
+    step_h = np.empty(n, dtype=np.float64)
+    status_h = np.empty(n, dtype=np.int32)
+    g.compute_step_and_next_volume_host(*h, sh, out_h, step_h, status=status_h,
+                                        flags=vg.PREC_MIXED | vg.NAV_SORT | vg.NAV_QUEUE)
+    assert np.array_equal(out_h, out_d.cpu().numpy())
+    assert np.array_equal(step_h, step_d.cpu().numpy())
+
+
+def test_scheduling_flag_errors(cuda, geo):
+    import vecgeom_gb300 as vg
+    name, g, pts, dev, st = geo
+    n = dev[0].numel()
+    out = cuda.empty(n * 12, dtype=cuda.uint8, device="cuda:0")
+    step = cuda.empty(n, dtype=cuda.float64, device="cuda:0")
+    with pytest.raises(vg.VGError):  # the work queue exists for the mixed kernel only
+        g.compute_step_and_next_volume(*dev, st, out, step, flags=vg.NAV_QUEUE)
+    with pytest.raises(vg.VGError):  # unknown flag bits
+        g.compute_step_and_next_volume(*dev, st, out, step, flags=vg.PREC_MIXED | 64)
+    small = cuda.empty(256, dtype=cuda.uint8, device="cuda:0")
+    with pytest.raises(vg.VGError):  # workspace too small
+        g.compute_step_and_next_volume(*dev, st, out, step, flags=vg.NAV_SORT, workspace=small)

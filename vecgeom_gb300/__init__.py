@@ -15,7 +15,7 @@ import os
 
 import numpy as np
 
-__all__ = ["Geometry", "load_library", "NAVSTATE_DTYPE", "PREC_FP64", "PREC_MIXED", "VGError",
+__all__ = ["Geometry", "load_library", "NAVSTATE_DTYPE", "PREC_FP64", "PREC_MIXED", "NAV_SORT", "NAV_QUEUE", "VGError",
            "kInside", "kSurface", "kOutside", "kInfLength", "IDENTITY_ROT", "ZERO_TRANS"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -23,6 +23,8 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libvecgeom_gb300.so")
 
 PREC_FP64 = 0
 PREC_MIXED = 1
+NAV_SORT = 2   # visit tracks sorted by (logical volume, Morton cell); results unchanged
+NAV_QUEUE = 4  # persistent step kernel fed from a global work counter (with PREC_MIXED)
 kInside, kSurface, kOutside = 1, 2, 3
 kInfLength = np.finfo(np.float64).max
 IDENTITY_ROT = (1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0)
@@ -88,6 +90,13 @@ _SIGS = {
                                             [ctypes.c_size_t, ctypes.c_uint32, _c_vp]),
     "vg_nav_compute_step_and_next_volume_host": (ctypes.c_int, [_c_vp] + [_c_vp] * 11 +
                                                  [ctypes.c_size_t, ctypes.c_uint32, _c_vp]),
+    "vg_nav_step_workspace_bytes": (ctypes.c_size_t, [ctypes.c_size_t, ctypes.c_uint32]),
+    "vg_nav_sort_tracks": (ctypes.c_int, [_c_vp] * 5 + [ctypes.c_size_t, _c_vp, _c_vp, _c_vp, ctypes.c_size_t,
+                                                        _c_vp]),
+    "vg_nav_sort_key_params": (ctypes.c_int, [_c_vp] * 5),
+    "vg_nav_compute_step_and_next_volume_ws": (ctypes.c_int, [_c_vp] + [_c_vp] * 11 +
+                                               [ctypes.c_size_t, ctypes.c_uint32, _c_vp, ctypes.c_size_t,
+                                                _c_vp]),
 }
 
 
@@ -147,6 +156,7 @@ class Geometry:
         _check(_lib.vg_geom_create(ctypes.byref(h)), "vg_geom_create")
         self._h = h
         self.closed = False
+        self.pv_lv = []  # logical volume of each placed volume, indexed by placed-volume id
 
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:
@@ -193,12 +203,16 @@ class Geometry:
     def place(self, lv, trans=ZERO_TRANS, rot=IDENTITY_ROT):
         t, tp = _darr(trans, 3)
         r, rp = _darr(rot, 9)
-        return _check(_lib.vg_geom_place(self._h, lv, tp, rp), "place")
+        pv = _check(_lib.vg_geom_place(self._h, lv, tp, rp), "place")
+        self.pv_lv.append(lv)
+        return pv
 
     def place_daughter(self, mother_lv, lv, trans=ZERO_TRANS, rot=IDENTITY_ROT):
         t, tp = _darr(trans, 3)
         r, rp = _darr(rot, 9)
-        return _check(_lib.vg_geom_place_daughter(self._h, mother_lv, lv, tp, rp), "place_daughter")
+        pv = _check(_lib.vg_geom_place_daughter(self._h, mother_lv, lv, tp, rp), "place_daughter")
+        self.pv_lv.append(lv)
+        return pv
 
     def set_world(self, pv):
         _check(_lib.vg_geom_set_world(self._h, pv), "set_world")
@@ -278,11 +292,55 @@ class Geometry:
                                         _stream()), "vg_nav_locate_point")
 
     def compute_step_and_next_volume(self, x, y, z, dx, dy, dz, in_states, out_states, step, step_limit=None,
-                                     status=None, flags=PREC_FP64):
+                                     status=None, flags=PREC_FP64, workspace=None):
+        """One navigation step for n tracks (CUDA tensors). With NAV_SORT / NAV_QUEUE in
+        `flags` a device workspace is needed: pass a uint8 CUDA tensor of at least
+        step_workspace_bytes(n, flags) bytes, or leave it to the geometry, which keeps one
+        cached workspace (calls running concurrently on different streams need their own)."""
+        n = x.numel()
+        if flags & (NAV_SORT | NAV_QUEUE):
+            need = int(_lib.vg_nav_step_workspace_bytes(n, flags))
+            if workspace is None:
+                ws = getattr(self, "_ws", None)
+                if ws is None or ws.numel() < need or ws.device != x.device:
+                    import torch
+                    ws = torch.empty(max(need, 256), dtype=torch.uint8, device=x.device)
+                    self._ws = ws
+                workspace = ws
+            _check(_lib.vg_nav_compute_step_and_next_volume_ws(
+                self._h, _ptr(x), _ptr(y), _ptr(z), _ptr(dx), _ptr(dy), _ptr(dz), _ptr(step_limit),
+                _ptr(in_states), _ptr(out_states), _ptr(step), _ptr(status), n, flags, _ptr(workspace),
+                workspace.numel(), _stream()), "vg_nav_compute_step_and_next_volume_ws")
+            return
         _check(_lib.vg_nav_compute_step_and_next_volume(
             self._h, _ptr(x), _ptr(y), _ptr(z), _ptr(dx), _ptr(dy), _ptr(dz), _ptr(step_limit), _ptr(in_states),
-            _ptr(out_states), _ptr(step), _ptr(status), x.numel(), flags, _stream()),
+            _ptr(out_states), _ptr(step), _ptr(status), n, flags, _stream()),
             "vg_nav_compute_step_and_next_volume")
+
+    def sort_tracks(self, x, y, z, in_states, order, keys=None, workspace=None):
+        """The visiting order NAV_SORT uses: `order` (int32/uint32 CUDA tensor of n) gets the
+        track indices sorted stably by key; `keys` (optional) the sorted keys."""
+        n = x.numel()
+        need = int(_lib.vg_nav_step_workspace_bytes(n, NAV_SORT))
+        if workspace is None:
+            import torch
+            workspace = torch.empty(max(need, 256), dtype=torch.uint8, device=x.device)
+        _check(_lib.vg_nav_sort_tracks(self._h, _ptr(x), _ptr(y), _ptr(z), _ptr(in_states), n, _ptr(order),
+                                       _ptr(keys), _ptr(workspace), workspace.numel(), _stream()),
+               "vg_nav_sort_tracks")
+
+    def sort_key_params(self):
+        """(lo[3], scale[3], cell_bits, lv_bits) of the sort key of this closed geometry."""
+        lo = (ctypes.c_float * 3)()
+        sc = (ctypes.c_float * 3)()
+        cb, lb = ctypes.c_int32(), ctypes.c_int32()
+        _check(_lib.vg_nav_sort_key_params(self._h, lo, sc, ctypes.byref(cb), ctypes.byref(lb)),
+               "vg_nav_sort_key_params")
+        return tuple(lo), tuple(sc), cb.value, lb.value
+
+    @staticmethod
+    def step_workspace_bytes(n, flags):
+        return int(_lib.vg_nav_step_workspace_bytes(n, flags))
 
     def compute_step_and_next_volume_host(self, x, y, z, dx, dy, dz, in_states, out_states, step, step_limit=None,
                                           status=None, flags=PREC_FP64, stream=None):

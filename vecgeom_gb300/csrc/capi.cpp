@@ -13,6 +13,7 @@ struct vg_geom {
   std::mutex staging_mutex;
   void *staging       = nullptr;
   size_t staging_size = 0;
+  vg::SortKeyParams sort{}; // set when the geometry is closed
   ~vg_geom()
   {
     if (staging) cudaFree(staging);
@@ -55,6 +56,65 @@ bool closed_ok(const vg_geom *g)
   }
   return true;
 }
+// Sort-key layout for VG_NAV_SORT: the logical-volume id in the high bits, then as many
+// Morton bits per axis of the world box (the frame of global points) as fit in 32 bits.
+vg::SortKeyParams sort_params(const vg::Geometry &geo)
+{
+  vg::SortKeyParams p{};
+  int lvb = 1;
+  while (lvb < 31 && (size_t(1) << lvb) < geo.lvs.size()) ++lvb;
+  p.lv_bits   = lvb;
+  p.cell_bits = (32 - lvb) / 3 > 10 ? 10 : (32 - lvb) / 3;
+  const vg::HostShape &ws = geo.shapes[geo.lvs[geo.pvs[geo.world].lv].shape];
+  for (int k = 0; k < 3; ++k) {
+    const double ext = ws.hi[k] - ws.lo[k];
+    p.lo[k]          = (float)ws.lo[k];
+    p.scale[k]       = ext > 0. ? (float)((double)(1u << p.cell_bits) / ext) : 0.f;
+  }
+  return p;
+}
+
+constexpr uint32_t kNavFlags = VG_PREC_MIXED | VG_NAV_SORT | VG_NAV_QUEUE;
+
+size_t step_workspace_bytes(size_t n, uint32_t flags)
+{
+  size_t b = 0;
+  if (flags & VG_NAV_QUEUE) b += 256;
+  if (flags & VG_NAV_SORT) b += vg::nav_sort_workspace_bytes(n);
+  return b;
+}
+
+// Validated step launch with optional sort and work queue; `ws` holds the counter
+// (256 bytes, first) and the sort arrays.
+int step_launch(const vg_geom *g, vg::StepArgs a, uint32_t flags, void *ws, size_t ws_bytes, cudaStream_t s)
+{
+  if (flags & ~kNavFlags) return fail(VG_EINVAL, "invalid navigation flags");
+  if ((flags & VG_NAV_QUEUE) && !(flags & VG_PREC_MIXED))
+    return fail(VG_EINVAL, "VG_NAV_QUEUE needs VG_PREC_MIXED");
+  if (a.n > 0xffffffffull) return fail(VG_EINVAL, "more than 2^32-1 tracks in one call");
+  const size_t need = step_workspace_bytes(a.n, flags);
+  if (need > 0 && (!ws || ws_bytes < need || (reinterpret_cast<uintptr_t>(ws) & 255u)))
+    return fail(VG_EINVAL, "workspace missing, too small or not 256-byte aligned");
+  unsigned char *w = static_cast<unsigned char *>(ws);
+  unsigned long long *counter = nullptr;
+  if (flags & VG_NAV_QUEUE) {
+    counter = reinterpret_cast<unsigned long long *>(w);
+    w += 256;
+  }
+  cudaError_t e = cudaSuccess;
+  if (flags & VG_NAV_SORT) {
+    const uint32_t *order = nullptr;
+    e = vg::launch_nav_sort(g->geo.dev, g->sort, a.x, a.y, a.z, a.in, a.n, w, &order, s);
+    if (e != cudaSuccess) return cuda_fail(e, "track sort launch");
+    a.order = order;
+  }
+  if (flags & VG_NAV_QUEUE)
+    e = vg::launch_step_mixed_queue(g->geo.dev, a, counter, s);
+  else
+    e = vg::launch_step(g->geo.dev, a, flags & VG_PREC_MIXED, s);
+  return e == cudaSuccess ? VG_OK : cuda_fail(e, "navigation step launch");
+}
+
 int32_t add_shape(vg_geom *g, int type, const double *p, int np)
 {
   if (!g) return fail(VG_EINVAL, "null geometry handle");
@@ -189,6 +249,7 @@ int vg_geom_close(vg_geom *g)
   if (!g) return fail(VG_EINVAL, "null geometry handle");
   std::string err;
   if (g->geo.close(err) != 0) return fail(g->geo.closed ? VG_ESTATE : VG_ECUDA, err);
+  if (g->geo.world >= 0) g->sort = sort_params(g->geo);
   return VG_OK;
 }
 int vg_geom_build(vg_geom *g)
@@ -302,13 +363,66 @@ int vg_nav_compute_step_and_next_volume(const vg_geom *g, const double *x, const
 {
   if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
   if (g->geo.world < 0) return fail(VG_ESTATE, "geometry has no world volume");
-  if (flags > VG_PREC_MIXED) return fail(VG_EINVAL, "invalid precision flags");
+  if (flags > VG_PREC_MIXED)
+    return fail(VG_EINVAL, "invalid precision flags (scheduling flags need vg_nav_compute_step_and_next_volume_ws)");
+  return vg_nav_compute_step_and_next_volume_ws(g, x, y, z, dx, dy, dz, step_limit, in, out, step, status, n, flags,
+                                                nullptr, 0, stream);
+}
+
+size_t vg_nav_step_workspace_bytes(size_t n, uint32_t flags) { return step_workspace_bytes(n, flags); }
+
+int vg_nav_compute_step_and_next_volume_ws(const vg_geom *g, const double *x, const double *y, const double *z,
+                                           const double *dx, const double *dy, const double *dz,
+                                           const double *step_limit, const vg_navstate *in, vg_navstate *out,
+                                           double *step, int32_t *status, size_t n, uint32_t flags, void *workspace,
+                                           size_t workspace_bytes, void *stream)
+{
+  if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
+  if (g->geo.world < 0) return fail(VG_ESTATE, "geometry has no world volume");
   if (n > 0 && (!x || !y || !z || !dx || !dy || !dz || !in || !out || !step))
     return fail(VG_EINVAL, "null input/output array");
   vg::StepArgs a{x,   y,   z,   dx,  dy,  dz, step_limit, reinterpret_cast<const vg::NavState *>(in),
                  reinterpret_cast<vg::NavState *>(out), step, status, nullptr, n};
-  const cudaError_t e = vg::launch_step(g->geo.dev, a, flags, (cudaStream_t)stream);
-  return e == cudaSuccess ? VG_OK : cuda_fail(e, "navigation step launch");
+  return step_launch(g, a, flags, workspace, workspace_bytes, (cudaStream_t)stream);
+}
+
+int vg_nav_sort_tracks(const vg_geom *g, const double *x, const double *y, const double *z, const vg_navstate *in,
+                       size_t n, uint32_t *order, uint32_t *keys, void *workspace, size_t workspace_bytes,
+                       void *stream)
+{
+  if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
+  if (g->geo.world < 0) return fail(VG_ESTATE, "geometry has no world volume");
+  if (n == 0) return VG_OK;
+  if (!x || !y || !z || !in || !order) return fail(VG_EINVAL, "null input/output array");
+  if (n > 0xffffffffull) return fail(VG_EINVAL, "more than 2^32-1 tracks in one call");
+  const size_t need = vg::nav_sort_workspace_bytes(n);
+  if (!workspace || workspace_bytes < need || (reinterpret_cast<uintptr_t>(workspace) & 255u))
+    return fail(VG_EINVAL, "workspace missing, too small or not 256-byte aligned");
+  cudaStream_t s        = (cudaStream_t)stream;
+  const uint32_t *sorted = nullptr;
+  cudaError_t e = vg::launch_nav_sort(g->geo.dev, g->sort, x, y, z, reinterpret_cast<const vg::NavState *>(in), n,
+                                      workspace, &sorted, s);
+  if (e != cudaSuccess) return cuda_fail(e, "track sort launch");
+  e = cudaMemcpyAsync(order, sorted, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess && keys) {
+    // the sorted keys sit in the key buffer paired with the final value buffer
+    const uint32_t *sk = vg::nav_sort_keys_of(sorted, workspace, n);
+    e = cudaMemcpyAsync(keys, sk, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
+  }
+  return e == cudaSuccess ? VG_OK : cuda_fail(e, "order copy");
+}
+
+int vg_nav_sort_key_params(const vg_geom *g, float lo[3], float scale[3], int32_t *cell_bits, int32_t *lv_bits)
+{
+  if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
+  if (g->geo.world < 0) return fail(VG_ESTATE, "geometry has no world volume");
+  for (int k = 0; k < 3; ++k) {
+    if (lo) lo[k] = g->sort.lo[k];
+    if (scale) scale[k] = g->sort.scale[k];
+  }
+  if (cell_bits) *cell_bits = g->sort.cell_bits;
+  if (lv_bits) *lv_bits = g->sort.lv_bits;
+  return VG_OK;
 }
 
 int vg_nav_compute_step_and_next_volume_host(vg_geom *g, const double *x, const double *y, const double *z,
@@ -319,9 +433,11 @@ int vg_nav_compute_step_and_next_volume_host(vg_geom *g, const double *x, const 
   if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
   if (n == 0) return VG_OK;
   if (!x || !y || !z || !dx || !dy || !dz || !in || !out || !step) return fail(VG_EINVAL, "null input/output array");
+  if (flags & ~kNavFlags) return fail(VG_EINVAL, "invalid navigation flags");
   std::lock_guard<std::mutex> lock(g->staging_mutex);
   const size_t nd = n * sizeof(double), ns = n * sizeof(vg_navstate), ni = n * sizeof(int32_t);
-  const size_t need = 8 * nd + 2 * ns + ni + 16 * 256;
+  const size_t wsb  = step_workspace_bytes(n, flags);
+  const size_t need = 8 * nd + 2 * ns + ni + wsb + 16 * 256;
   if (g->staging_size < need) {
     if (g->staging) cudaFree(g->staging);
     g->staging      = nullptr;
@@ -342,6 +458,7 @@ int vg_nav_compute_step_and_next_volume_host(vg_geom *g, const double *x, const 
   vg_navstate *din  = static_cast<vg_navstate *>(take(ns));
   vg_navstate *dout = static_cast<vg_navstate *>(take(ns));
   int32_t *dst      = static_cast<int32_t *>(take(ni));
+  void *dws         = wsb ? take(wsb) : nullptr;
   cudaStream_t s    = (cudaStream_t)stream;
   const double *src[7] = {x, y, z, dx, dy, dz, step_limit};
   cudaError_t e        = cudaSuccess;
@@ -352,8 +469,8 @@ int vg_nav_compute_step_and_next_volume_host(vg_geom *g, const double *x, const 
   vg::StepArgs a{d[0], d[1], d[2], d[3], d[4], d[5], step_limit ? d[6] : nullptr,
                  reinterpret_cast<const vg::NavState *>(din), reinterpret_cast<vg::NavState *>(dout), d[7],
                  status ? dst : nullptr, nullptr, n};
-  e = vg::launch_step(g->geo.dev, a, flags, s);
-  if (e != cudaSuccess) return cuda_fail(e, "navigation step launch");
+  const int rc = step_launch(g, a, flags, dws, wsb, s);
+  if (rc != VG_OK) return rc;
   e = cudaMemcpyAsync(out, dout, ns, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(step, d[7], nd, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess && status) e = cudaMemcpyAsync(status, dst, ni, cudaMemcpyDeviceToHost, s);

@@ -889,6 +889,7 @@ int Geometry::upload(std::string &err)
   dev.node_f      = reinterpret_cast<const NodeF *>(P(o_nf));
   dev.prim_box_f  = reinterpret_cast<const float *>(P(o_pbf));
   dev.nav         = reinterpret_cast<const uint32_t *>(P(o_nav));
+  dev.nav_words   = (uint32_t)nav_words;
   dev.shape_lbd   = reinterpret_cast<const float *>(P(o_lbd));
   dev.world_pv    = world;
   dev.max_depth   = max_depth;

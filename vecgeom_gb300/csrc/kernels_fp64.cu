@@ -122,25 +122,21 @@ __global__ void __launch_bounds__(256) k_locate(const DevGeom g, const double *_
   }
 }
 
-__global__ void __launch_bounds__(256) k_step(const DevGeom g, const double *__restrict__ x,
-                                              const double *__restrict__ y, const double *__restrict__ z,
-                                              const double *__restrict__ dx, const double *__restrict__ dy,
-                                              const double *__restrict__ dz, const double *__restrict__ limit,
-                                              const NavState *__restrict__ in, NavState *__restrict__ out,
-                                              double *__restrict__ step, int32_t *__restrict__ status,
-                                              int32_t *__restrict__ nvisited, size_t n)
+__global__ void __launch_bounds__(256) k_step(const DevGeom g, const StepArgs a)
 {
   const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    const NavState s = in[i];
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+    const size_t t   = a.order ? (size_t)__ldg(a.order + i) : i;
+    const NavState s = a.in[t];
     NavState o;
     int st = 0, nv = 0;
-    const double lim = limit ? __ldg(limit + i) : kInfLength;
-    step[i] = f64::compute_step(g, V3{__ldg(x + i), __ldg(y + i), __ldg(z + i)},
-                                V3{__ldg(dx + i), __ldg(dy + i), __ldg(dz + i)}, lim, s, o, st, nvisited ? &nv : nullptr);
-    out[i] = o;
-    if (status) status[i] = st;
-    if (nvisited) nvisited[i] = nv;
+    const double lim = a.limit ? __ldg(a.limit + t) : kInfLength;
+    a.step[t] = f64::compute_step(g, V3{__ldg(a.x + t), __ldg(a.y + t), __ldg(a.z + t)},
+                                  V3{__ldg(a.dx + t), __ldg(a.dy + t), __ldg(a.dz + t)}, lim, s, o, st,
+                                  a.nvisited ? &nv : nullptr);
+    a.out[t] = o;
+    if (a.status) a.status[t] = st;
+    if (a.nvisited) a.nvisited[t] = nv;
   }
 }
 
@@ -190,8 +186,7 @@ cudaError_t launch_locate_fp64(const DevGeom &g, const double *x, const double *
 cudaError_t launch_step_fp64(const DevGeom &g, const StepArgs &a, cudaStream_t s)
 {
   if (a.n == 0) return cudaSuccess;
-  k_step<<<grid_for(a.n, 256), 256, 0, s>>>(g, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.limit, a.in, a.out, a.step,
-                                            a.status, a.nvisited, a.n);
+  k_step<<<grid_for(a.n, 256), 256, 0, s>>>(g, a);
   return cudaGetLastError();
 }
 

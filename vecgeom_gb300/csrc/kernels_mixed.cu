@@ -16,27 +16,44 @@ inline unsigned grid_for(size_t n, int block)
   return (unsigned)(blocks ? blocks : 1);
 }
 
-__global__ void __launch_bounds__(256) k_step_mixed(const DevGeom g, const double *__restrict__ x,
-                                                    const double *__restrict__ y, const double *__restrict__ z,
-                                                    const double *__restrict__ dx, const double *__restrict__ dy,
-                                                    const double *__restrict__ dz, const double *__restrict__ limit,
-                                                    const NavState *__restrict__ in, NavState *__restrict__ out,
-                                                    double *__restrict__ step, int32_t *__restrict__ status,
-                                                    int32_t *__restrict__ nvisited, size_t n)
+__device__ __forceinline__ void step_one_mixed(const DevGeom &g, const mixed::ShapeLB *lbs, const StepArgs &a,
+                                               size_t t)
+{
+  const NavState s = a.in[t];
+  NavState o;
+  int st = 0, nv = 0;
+  const double lim = a.limit ? __ldg(a.limit + t) : kInfLength;
+  a.step[t] = mixed::compute_step_mixed(g, lbs, f64::V3{__ldg(a.x + t), __ldg(a.y + t), __ldg(a.z + t)},
+                                        f64::V3{__ldg(a.dx + t), __ldg(a.dy + t), __ldg(a.dz + t)}, lim, s, o, st,
+                                        a.nvisited ? &nv : nullptr);
+  a.out[t] = o;
+  if (a.status) a.status[t] = st;
+  if (a.nvisited) a.nvisited[t] = nv;
+}
+
+__global__ void __launch_bounds__(256) k_step_mixed(const DevGeom g, const StepArgs a)
 {
   const mixed::ShapeLB *lbs = reinterpret_cast<const mixed::ShapeLB *>(g.shape_lbd);
   const size_t stride       = (size_t)gridDim.x * blockDim.x;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    const NavState s = in[i];
-    NavState o;
-    int st = 0, nv = 0;
-    const double lim = limit ? __ldg(limit + i) : kInfLength;
-    step[i] = mixed::compute_step_mixed(g, lbs, f64::V3{__ldg(x + i), __ldg(y + i), __ldg(z + i)},
-                                        f64::V3{__ldg(dx + i), __ldg(dy + i), __ldg(dz + i)}, lim, s, o, st,
-                                        nvisited ? &nv : nullptr);
-    out[i] = o;
-    if (status) status[i] = st;
-    if (nvisited) nvisited[i] = nv;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride)
+    step_one_mixed(g, lbs, a, a.order ? (size_t)__ldg(a.order + i) : i);
+}
+
+// Persistent variant: one grid of resident blocks; each warp takes the next 32 entries of
+// the visiting order from a global counter (zeroed before the launch), so warps that drew
+// cheap tracks take more of them.
+__global__ void __launch_bounds__(256) k_step_mixed_queue(const DevGeom g, const StepArgs a,
+                                                          unsigned long long *__restrict__ counter)
+{
+  const mixed::ShapeLB *lbs = reinterpret_cast<const mixed::ShapeLB *>(g.shape_lbd);
+  const int lane            = threadIdx.x & 31;
+  for (;;) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(counter, 32ull);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= a.n) break;
+    const size_t i = (size_t)base + lane;
+    if (i < a.n) step_one_mixed(g, lbs, a, a.order ? (size_t)__ldg(a.order + i) : i);
   }
 }
 
@@ -60,8 +77,29 @@ __global__ void __launch_bounds__(256) k_locate_mixed(const DevGeom g, const dou
 cudaError_t launch_step_mixed(const DevGeom &g, const StepArgs &a, cudaStream_t s)
 {
   if (a.n == 0) return cudaSuccess;
-  k_step_mixed<<<grid_for(a.n, 256), 256, 0, s>>>(g, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.limit, a.in, a.out, a.step,
-                                                  a.status, a.nvisited, a.n);
+  k_step_mixed<<<grid_for(a.n, 256), 256, 0, s>>>(g, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step_mixed_queue(const DevGeom &g, const StepArgs &a, unsigned long long *counter, cudaStream_t s)
+{
+  if (a.n == 0) return cudaSuccess;
+  static int resident = 0; // blocks of 256 per SM (same for every device of this build)
+  if (resident == 0) {
+    int r = 0;
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_step_mixed_queue, 256, 0);
+    if (e != cudaSuccess) return e;
+    resident = r > 0 ? r : 1;
+  }
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  size_t blocks = (size_t)sms * resident, need = (a.n + 255) / 256;
+  if (blocks > need) blocks = need;
+  k_step_mixed_queue<<<(unsigned)blocks, 256, 0, s>>>(g, a, counter);
   return cudaGetLastError();
 }
 

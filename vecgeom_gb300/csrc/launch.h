@@ -20,6 +20,16 @@ struct StepArgs {
   int32_t *status;
   int32_t *nvisited;
   size_t n;
+  const uint32_t *order = nullptr; // optional visiting order (track indices); null: 0..n-1
+};
+
+// Sort key of a track: logical volume of its state above 3*cell_bits Morton bits of its
+// position cell in the world box.
+struct SortKeyParams {
+  float lo[3];    // world box low corner (mm)
+  float scale[3]; // cells per mm along each axis
+  int cell_bits;  // bits per axis (<= 10)
+  int lv_bits;    // bits of the logical-volume id
 };
 
 cudaError_t launch_shape_query_fp64(int type, const double *rec, const Xform &xf, int apply_xf, int q,
@@ -30,8 +40,18 @@ cudaError_t launch_locate_fp64(const DevGeom &g, const double *x, const double *
                                NavState *out, cudaStream_t s);
 cudaError_t launch_step_fp64(const DevGeom &g, const StepArgs &a, cudaStream_t s);
 cudaError_t launch_step_mixed(const DevGeom &g, const StepArgs &a, cudaStream_t s);
+cudaError_t launch_step_mixed_queue(const DevGeom &g, const StepArgs &a, unsigned long long *counter,
+                                    cudaStream_t s);
 cudaError_t launch_locate_mixed(const DevGeom &g, const double *x, const double *y, const double *z, size_t n,
                                 NavState *out, cudaStream_t s);
+size_t nav_sort_workspace_bytes(size_t n);
+int sort_key_bits(const SortKeyParams &p);
+const uint32_t *nav_sort_keys_of(const uint32_t *order, const void *ws, size_t n); // keys paired with `order`
+// Keys + stable radix sort of the n tracks; *order receives the sorted track indices
+// (inside the workspace).
+cudaError_t launch_nav_sort(const DevGeom &g, const SortKeyParams &p, const double *x, const double *y,
+                            const double *z, const NavState *in, size_t n, void *ws, const uint32_t **order,
+                            cudaStream_t s);
 // flags: VG_PREC_FP64 (0) or VG_PREC_MIXED (1)
 inline cudaError_t launch_step(const DevGeom &g, const StepArgs &a, uint32_t flags, cudaStream_t s)
 {

@@ -153,6 +153,7 @@ struct DevGeom {
   const float *prim_box_f;    // FP32 daughter boxes (6 floats per slot, rounded outward)
   const float *shape_lbd;     // FP32 bounding descriptor per shape (8 floats, see nav_mixed.cuh)
   const uint32_t *nav;        // NavIndex table
+  uint32_t nav_words;
   int32_t world_pv;
   int32_t max_depth;
   int32_t n_pv;
