@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--schedule", default="mixed_sort_queue", choices=sorted(SCHEDULES),
                     help="precision and scheduling of the headline measurement")
     ap.add_argument("--variants", type=int, default=1, help="also time the other schedules (1/0)")
+    ap.add_argument("--tune", type=int, default=1,
+                    help="autotune sort-key bits / queue occupancy before timing (untimed; 1/0)")
     return ap.parse_args()
 
 
@@ -271,6 +273,11 @@ def main():
         return ms / args.steps
 
     head = SCHEDULES[args.schedule]
+    tuning = None
+    if args.tune and head & (vg.NAV_SORT | vg.NAV_QUEUE):
+        from vecgeom_gb300.tune import autotune
+        cands = [(head, b, q) for b in (0, 7, 5) for q in ((1, 2) if head & vg.NAV_QUEUE else (1,))]
+        tuning = autotune(geo, t, st, candidates=cands, cache=None)
     ms_fp64 = timed(vg.PREC_FP64)
     out64, step64 = out.clone(), step.clone()
     variants = {"fp64": ms_fp64}
@@ -345,6 +352,7 @@ def main():
         "ids_identical_to_fp64": ids_equal, "max_step_diff_vs_fp64_mm": step_err,
         "schedules_ms_per_step": variants, "all_schedules_identical_to_fp64": identical and ids_equal,
         "sort_ms_per_step": ms_sort, "step_kernel_ms_per_step": ms_kernel,
+        "tuning": None if tuning is None else {k: tuning[k] for k in ("cell_bits", "queue_blocks", "timings")},
         "e2e": {"value": ws * n / e2e_s, "unit": "nav steps/s", "h2d_bytes_per_step": n * (48 + 12),
                 "d2h_bytes_per_step": n * (12 + 8)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",

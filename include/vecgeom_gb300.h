@@ -207,6 +207,12 @@ int vg_nav_sort_tracks(const vg_geom *g, const double *x, const double *y, const
                        size_t n, uint32_t *order, uint32_t *keys, void *workspace, size_t workspace_bytes,
                        void *stream);
 int vg_nav_sort_key_params(const vg_geom *g, float lo[3], float scale[3], int32_t *cell_bits, int32_t *lv_bits);
+/* Tuning knobs of the scheduled step (results never depend on them): `cell_bits`, the
+ * Morton bits per axis of the sort key (1..10; 0 = default, the most that fit beside the
+ * logical-volume id; fewer bits mean fewer radix passes and coarser cells), and
+ * `queue_blocks_per_sm` for VG_NAV_QUEUE (1: full register budget per thread; 2: half the
+ * registers, twice the resident warps; 0 = 1). Set before sorted calls are in flight. */
+int vg_nav_set_tuning(vg_geom *g, int32_t cell_bits, int32_t queue_blocks_per_sm);
 
 /* Same step with HOST arrays, the form the reference's own SoA navigator interface takes
  * (VNavigator::ComputeStepsAndPropagatedStates, VNavigator.h:128-132): inputs are copied to

@@ -94,6 +94,7 @@ _SIGS = {
     "vg_nav_sort_tracks": (ctypes.c_int, [_c_vp] * 5 + [ctypes.c_size_t, _c_vp, _c_vp, _c_vp, ctypes.c_size_t,
                                                         _c_vp]),
     "vg_nav_sort_key_params": (ctypes.c_int, [_c_vp] * 5),
+    "vg_nav_set_tuning": (ctypes.c_int, [_c_vp, ctypes.c_int32, ctypes.c_int32]),
     "vg_nav_compute_step_and_next_volume_ws": (ctypes.c_int, [_c_vp] + [_c_vp] * 11 +
                                                [ctypes.c_size_t, ctypes.c_uint32, _c_vp, ctypes.c_size_t,
                                                 _c_vp]),
@@ -337,6 +338,11 @@ class Geometry:
         _check(_lib.vg_nav_sort_key_params(self._h, lo, sc, ctypes.byref(cb), ctypes.byref(lb)),
                "vg_nav_sort_key_params")
         return tuple(lo), tuple(sc), cb.value, lb.value
+
+    def set_tuning(self, cell_bits=0, queue_blocks_per_sm=0):
+        """Sort-key Morton bits per axis and resident blocks per SM of the work-queue kernel
+        (0: defaults). Results do not depend on them."""
+        _check(_lib.vg_nav_set_tuning(self._h, cell_bits, queue_blocks_per_sm), "vg_nav_set_tuning")
 
     @staticmethod
     def step_workspace_bytes(n, flags):

@@ -14,6 +14,7 @@ struct vg_geom {
   void *staging       = nullptr;
   size_t staging_size = 0;
   vg::SortKeyParams sort{}; // set when the geometry is closed
+  int queue_blocks = 1;     // resident blocks per SM of the work-queue step kernel (1 or 2)
   ~vg_geom()
   {
     if (staging) cudaFree(staging);
@@ -58,13 +59,14 @@ bool closed_ok(const vg_geom *g)
 }
 // Sort-key layout for VG_NAV_SORT: the logical-volume id in the high bits, then as many
 // Morton bits per axis of the world box (the frame of global points) as fit in 32 bits.
-vg::SortKeyParams sort_params(const vg::Geometry &geo)
+vg::SortKeyParams sort_params(const vg::Geometry &geo, int cell_bits)
 {
   vg::SortKeyParams p{};
   int lvb = 1;
   while (lvb < 31 && (size_t(1) << lvb) < geo.lvs.size()) ++lvb;
-  p.lv_bits   = lvb;
-  p.cell_bits = (32 - lvb) / 3 > 10 ? 10 : (32 - lvb) / 3;
+  p.lv_bits    = lvb;
+  const int mx = (32 - lvb) / 3 > 10 ? 10 : (32 - lvb) / 3;
+  p.cell_bits  = (cell_bits > 0 && cell_bits < mx) ? cell_bits : mx;
   const vg::HostShape &ws = geo.shapes[geo.lvs[geo.pvs[geo.world].lv].shape];
   for (int k = 0; k < 3; ++k) {
     const double ext = ws.hi[k] - ws.lo[k];
@@ -109,7 +111,7 @@ int step_launch(const vg_geom *g, vg::StepArgs a, uint32_t flags, void *ws, size
     a.order = order;
   }
   if (flags & VG_NAV_QUEUE)
-    e = vg::launch_step_mixed_queue(g->geo.dev, a, counter, s);
+    e = vg::launch_step_mixed_queue(g->geo.dev, a, counter, g->queue_blocks, s);
   else
     e = vg::launch_step(g->geo.dev, a, flags & VG_PREC_MIXED, s);
   return e == cudaSuccess ? VG_OK : cuda_fail(e, "navigation step launch");
@@ -249,7 +251,7 @@ int vg_geom_close(vg_geom *g)
   if (!g) return fail(VG_EINVAL, "null geometry handle");
   std::string err;
   if (g->geo.close(err) != 0) return fail(g->geo.closed ? VG_ESTATE : VG_ECUDA, err);
-  if (g->geo.world >= 0) g->sort = sort_params(g->geo);
+  if (g->geo.world >= 0) g->sort = sort_params(g->geo, 0);
   return VG_OK;
 }
 int vg_geom_build(vg_geom *g)
@@ -410,6 +412,17 @@ int vg_nav_sort_tracks(const vg_geom *g, const double *x, const double *y, const
     e = cudaMemcpyAsync(keys, sk, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
   }
   return e == cudaSuccess ? VG_OK : cuda_fail(e, "order copy");
+}
+
+int vg_nav_set_tuning(vg_geom *g, int32_t cell_bits, int32_t queue_blocks_per_sm)
+{
+  if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
+  if (g->geo.world < 0) return fail(VG_ESTATE, "geometry has no world volume");
+  if (cell_bits < 0 || cell_bits > 10) return fail(VG_EINVAL, "cell_bits must be in [0, 10]");
+  if (queue_blocks_per_sm < 0 || queue_blocks_per_sm > 2) return fail(VG_EINVAL, "queue_blocks_per_sm must be 0, 1 or 2");
+  g->sort         = sort_params(g->geo, cell_bits);
+  g->queue_blocks = queue_blocks_per_sm ? queue_blocks_per_sm : 1;
+  return VG_OK;
 }
 
 int vg_nav_sort_key_params(const vg_geom *g, float lo[3], float scale[3], int32_t *cell_bits, int32_t *lv_bits)

@@ -42,8 +42,9 @@ __global__ void __launch_bounds__(256) k_step_mixed(const DevGeom g, const StepA
 // Persistent variant: one grid of resident blocks; each warp takes the next 32 entries of
 // the visiting order from a global counter (zeroed before the launch), so warps that drew
 // cheap tracks take more of them.
-__global__ void __launch_bounds__(256) k_step_mixed_queue(const DevGeom g, const StepArgs a,
-                                                          unsigned long long *__restrict__ counter)
+template <int MinBlocks>
+__global__ void __launch_bounds__(256, MinBlocks) k_step_mixed_queue(const DevGeom g, const StepArgs a,
+                                                                     unsigned long long *__restrict__ counter)
 {
   const mixed::ShapeLB *lbs = reinterpret_cast<const mixed::ShapeLB *>(g.shape_lbd);
   const int lane            = threadIdx.x & 31;
@@ -81,13 +82,13 @@ cudaError_t launch_step_mixed(const DevGeom &g, const StepArgs &a, cudaStream_t 
   return cudaGetLastError();
 }
 
-cudaError_t launch_step_mixed_queue(const DevGeom &g, const StepArgs &a, unsigned long long *counter, cudaStream_t s)
+template <int MinBlocks>
+cudaError_t launch_queue(const DevGeom &g, const StepArgs &a, unsigned long long *counter, cudaStream_t s)
 {
-  if (a.n == 0) return cudaSuccess;
   static int resident = 0; // blocks of 256 per SM (same for every device of this build)
   if (resident == 0) {
     int r = 0;
-    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_step_mixed_queue, 256, 0);
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_step_mixed_queue<MinBlocks>, 256, 0);
     if (e != cudaSuccess) return e;
     resident = r > 0 ? r : 1;
   }
@@ -99,8 +100,15 @@ cudaError_t launch_step_mixed_queue(const DevGeom &g, const StepArgs &a, unsigne
   if (e != cudaSuccess) return e;
   size_t blocks = (size_t)sms * resident, need = (a.n + 255) / 256;
   if (blocks > need) blocks = need;
-  k_step_mixed_queue<<<(unsigned)blocks, 256, 0, s>>>(g, a, counter);
+  k_step_mixed_queue<MinBlocks><<<(unsigned)blocks, 256, 0, s>>>(g, a, counter);
   return cudaGetLastError();
+}
+
+cudaError_t launch_step_mixed_queue(const DevGeom &g, const StepArgs &a, unsigned long long *counter,
+                                    int blocks_per_sm, cudaStream_t s)
+{
+  if (a.n == 0) return cudaSuccess;
+  return blocks_per_sm >= 2 ? launch_queue<2>(g, a, counter, s) : launch_queue<1>(g, a, counter, s);
 }
 
 cudaError_t launch_locate_mixed(const DevGeom &g, const double *x, const double *y, const double *z, size_t n,

@@ -41,7 +41,7 @@ cudaError_t launch_locate_fp64(const DevGeom &g, const double *x, const double *
 cudaError_t launch_step_fp64(const DevGeom &g, const StepArgs &a, cudaStream_t s);
 cudaError_t launch_step_mixed(const DevGeom &g, const StepArgs &a, cudaStream_t s);
 cudaError_t launch_step_mixed_queue(const DevGeom &g, const StepArgs &a, unsigned long long *counter,
-                                    cudaStream_t s);
+                                    int blocks_per_sm, cudaStream_t s);
 cudaError_t launch_locate_mixed(const DevGeom &g, const double *x, const double *y, const double *z, size_t n,
                                 NavState *out, cudaStream_t s);
 size_t nav_sort_workspace_bytes(size_t n);

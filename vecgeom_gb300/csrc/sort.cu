@@ -74,17 +74,12 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_hist(const uint32_t *__res
   hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
 }
 
-// In-place exclusive scan of m counts by one block of 1024 threads.
-__global__ void __launch_bounds__(1024) k_scan_exclusive(uint32_t *__restrict__ a, size_t m)
+// Exclusive block-wide scan of one value per thread (blockDim.x a multiple of 32, <= 1024);
+// returns the exclusive prefix and leaves the block total in *total.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *wsum, uint32_t *total)
 {
-  __shared__ uint32_t wsum[32];
-  const size_t per = (m + 1023) / 1024;
-  const size_t b   = (size_t)threadIdx.x * per;
-  const size_t e   = b + per < m ? b + per : m;
-  uint32_t sum     = 0u;
-  for (size_t i = b; i < e; ++i) sum += a[i];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  uint32_t incl  = sum;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  uint32_t incl = v;
   for (int o = 1; o < 32; o <<= 1) {
     const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
     if (lane >= o) incl += t;
@@ -92,20 +87,39 @@ __global__ void __launch_bounds__(1024) k_scan_exclusive(uint32_t *__restrict__ 
   if (lane == 31) wsum[w] = incl;
   __syncthreads();
   if (w == 0) {
-    uint32_t v = wsum[lane], iv = v;
+    const uint32_t x = lane < nw ? wsum[lane] : 0u;
+    uint32_t ix      = x;
     for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t t = __shfl_up_sync(0xffffffffu, iv, o);
-      if (lane >= o) iv += t;
+      const uint32_t t = __shfl_up_sync(0xffffffffu, ix, o);
+      if (lane >= o) ix += t;
     }
-    wsum[lane] = iv - v;
+    if (lane < nw) wsum[lane] = ix - x;
+    if (lane == 31) wsum[32] = ix;
   }
   __syncthreads();
-  uint32_t run = wsum[w] + incl - sum;
-  for (size_t i = b; i < e; ++i) {
-    const uint32_t v = a[i];
-    a[i]             = run;
-    run += v;
+  const uint32_t r = wsum[w] + incl - v;
+  *total           = wsum[32];
+  __syncthreads();
+  return r;
+}
+
+// Row d of the digit-major counts: exclusive scan over the tiles in place (one block per
+// digit); the row total goes to totals[d].
+__global__ void __launch_bounds__(1024) k_scan_rows(uint32_t *__restrict__ hist, unsigned ntiles,
+                                                    uint32_t *__restrict__ totals)
+{
+  __shared__ uint32_t wsum[33];
+  uint32_t *row = hist + (size_t)blockIdx.x * ntiles;
+  uint32_t carry = 0u;
+  for (unsigned c = 0; c < ntiles; c += blockDim.x) {
+    const unsigned i = c + threadIdx.x;
+    const uint32_t v = i < ntiles ? row[i] : 0u;
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_scan(v, wsum, &tot);
+    if (i < ntiles) row[i] = carry + ex;
+    carry += tot;
   }
+  if (threadIdx.x == 0) totals[blockIdx.x] = carry;
 }
 
 // Stable scatter of one digit. Tile positions are (warp, round, lane) in that order, so
@@ -114,9 +128,10 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_scatter(const uint32_t *__
                                                               const uint32_t *__restrict__ vin,
                                                               uint32_t *__restrict__ kout, uint32_t *__restrict__ vout,
                                                               size_t n, int shift, const uint32_t *__restrict__ hist,
-                                                              unsigned ntiles)
+                                                              const uint32_t *__restrict__ totals, unsigned ntiles)
 {
   __shared__ uint32_t cnt[kSortWarps][256];
+  __shared__ uint32_t wsum[33];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int k = threadIdx.x; k < kSortWarps * 256; k += kSortBlock) (&cnt[0][0])[k] = 0u;
   __syncthreads();
@@ -140,7 +155,8 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_scatter(const uint32_t *__
   __syncthreads();
   {
     const uint32_t d = threadIdx.x;
-    uint32_t run     = __ldg(hist + (size_t)d * ntiles + blockIdx.x);
+    uint32_t tot;
+    uint32_t run = block_exclusive_scan(__ldg(totals + d), wsum, &tot) + __ldg(hist + (size_t)d * ntiles + blockIdx.x);
     for (int ww = 0; ww < kSortWarps; ++ww) {
       const uint32_t c = cnt[ww][d];
       cnt[ww][d]       = run;
@@ -172,7 +188,7 @@ inline unsigned grid_for(size_t n, int block)
 size_t nav_sort_workspace_bytes(size_t n)
 {
   const size_t ntiles = (n + kSortTile - 1) / kSortTile;
-  return 4 * align256(n * sizeof(uint32_t)) + align256(256 * ntiles * sizeof(uint32_t));
+  return 4 * align256(n * sizeof(uint32_t)) + align256(256 * ntiles * sizeof(uint32_t)) + 256 * sizeof(uint32_t);
 }
 
 const uint32_t *nav_sort_keys_of(const uint32_t *order, const void *ws, size_t n)
@@ -196,7 +212,8 @@ cudaError_t launch_nav_sort(const DevGeom &g, const SortKeyParams &p, const doub
   const size_t a        = align256(n * sizeof(uint32_t));
   uint32_t *k0 = reinterpret_cast<uint32_t *>(w), *k1 = reinterpret_cast<uint32_t *>(w + a);
   uint32_t *v0 = reinterpret_cast<uint32_t *>(w + 2 * a), *v1 = reinterpret_cast<uint32_t *>(w + 3 * a);
-  uint32_t *hist = reinterpret_cast<uint32_t *>(w + 4 * a);
+  uint32_t *hist   = reinterpret_cast<uint32_t *>(w + 4 * a);
+  uint32_t *totals = reinterpret_cast<uint32_t *>(w + 4 * a + align256(256 * (size_t)ntiles * sizeof(uint32_t)));
   k_sort_keys<<<grid_for(n, 256), 256, 0, s>>>(g, p, x, y, z, in, n, k0);
   // Digits above the key's width are all zero (invalid states carry all-ones keys, which
   // sort last within every pass), so only the passes that cover the key bits are run.
@@ -205,8 +222,8 @@ cudaError_t launch_nav_sort(const DevGeom &g, const SortKeyParams &p, const doub
   uint32_t *kin = k0, *kout = k1, *vin = nullptr, *vout = v0;
   for (int ps = 0; ps < passes; ++ps) {
     k_radix_hist<<<ntiles, kSortBlock, 0, s>>>(kin, n, 8 * ps, hist, ntiles);
-    k_scan_exclusive<<<1, 1024, 0, s>>>(hist, (size_t)256 * ntiles);
-    k_radix_scatter<<<ntiles, kSortBlock, 0, s>>>(kin, vin, kout, vout, n, 8 * ps, hist, ntiles);
+    k_scan_rows<<<256, 1024, 0, s>>>(hist, ntiles, totals);
+    k_radix_scatter<<<ntiles, kSortBlock, 0, s>>>(kin, vin, kout, vout, n, 8 * ps, hist, totals, ntiles);
     uint32_t *tk = kin;
     kin          = kout;
     kout         = tk;
