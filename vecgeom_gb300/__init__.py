@@ -95,6 +95,8 @@ _SIGS = {
                                                         _c_vp]),
     "vg_nav_sort_key_params": (ctypes.c_int, [_c_vp] * 5),
     "vg_nav_set_tuning": (ctypes.c_int, [_c_vp, ctypes.c_int32, ctypes.c_int32]),
+    "vg_nav_compute_step_and_next_volume_noalloc": (ctypes.c_int, [_c_vp] + [_c_vp] * 11 +
+                                                    [ctypes.c_size_t, ctypes.c_uint32, _c_vp]),
     "vg_nav_compute_step_and_next_volume_ws": (ctypes.c_int, [_c_vp] + [_c_vp] * 11 +
                                                [ctypes.c_size_t, ctypes.c_uint32, _c_vp, ctypes.c_size_t,
                                                 _c_vp]),
@@ -317,6 +319,15 @@ class Geometry:
             self._h, _ptr(x), _ptr(y), _ptr(z), _ptr(dx), _ptr(dy), _ptr(dz), _ptr(step_limit), _ptr(in_states),
             _ptr(out_states), _ptr(step), _ptr(status), n, flags, _stream()),
             "vg_nav_compute_step_and_next_volume")
+
+    def compute_step_and_next_volume_noalloc(self, x, y, z, dx, dy, dz, in_states, out_states, step,
+                                             step_limit=None, status=None, flags=PREC_MIXED | NAV_SORT | NAV_QUEUE):
+        """The scheduled step on the library's fixed device scratch (no allocation, at most
+        2^20 tracks per call; overlapping calls race; the first call per device is setup)."""
+        _check(_lib.vg_nav_compute_step_and_next_volume_noalloc(
+            self._h, _ptr(x), _ptr(y), _ptr(z), _ptr(dx), _ptr(dy), _ptr(dz), _ptr(step_limit), _ptr(in_states),
+            _ptr(out_states), _ptr(step), _ptr(status), x.numel(), flags, _stream()),
+            "vg_nav_compute_step_and_next_volume_noalloc")
 
     def sort_tracks(self, x, y, z, in_states, order, keys=None, workspace=None):
         """The visiting order NAV_SORT uses: `order` (int32/uint32 CUDA tensor of n) gets the

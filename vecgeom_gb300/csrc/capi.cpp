@@ -438,6 +438,30 @@ int vg_nav_sort_key_params(const vg_geom *g, float lo[3], float scale[3], int32_
   return VG_OK;
 }
 
+int vg_nav_compute_step_and_next_volume_noalloc(const vg_geom *g, const double *x, const double *y, const double *z,
+                                                const double *dx, const double *dy, const double *dz,
+                                                const double *step_limit, const vg_navstate *in, vg_navstate *out,
+                                                double *step, int32_t *status, size_t n, uint32_t flags,
+                                                void *stream)
+{
+  if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
+  if (g->geo.world < 0) return fail(VG_ESTATE, "geometry has no world volume");
+  if (n > vg::noalloc_max_tracks())
+    return fail(VG_EINVAL, "n = " + std::to_string(n) + " exceeds the fixed scratch capacity of " +
+                               std::to_string(vg::noalloc_max_tracks()) + " tracks of the no-allocation entry point");
+  if (n > 0 && (!x || !y || !z || !dx || !dy || !dz || !in || !out || !step))
+    return fail(VG_EINVAL, "null input/output array");
+  void *ws     = nullptr;
+  size_t bytes = 0;
+  if (flags & (VG_NAV_SORT | VG_NAV_QUEUE)) {
+    const cudaError_t e = vg::noalloc_scratch(&ws, &bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "no-allocation scratch lookup");
+  }
+  vg::StepArgs a{x,   y,   z,   dx,  dy,  dz, step_limit, reinterpret_cast<const vg::NavState *>(in),
+                 reinterpret_cast<vg::NavState *>(out), step, status, nullptr, n};
+  return step_launch(g, a, flags, ws, bytes, (cudaStream_t)stream);
+}
+
 int vg_nav_compute_step_and_next_volume_host(vg_geom *g, const double *x, const double *y, const double *z,
                                              const double *dx, const double *dy, const double *dz,
                                              const double *step_limit, const vg_navstate *in, vg_navstate *out,

@@ -52,6 +52,9 @@ const uint32_t *nav_sort_keys_of(const uint32_t *order, const void *ws, size_t n
 cudaError_t launch_nav_sort(const DevGeom &g, const SortKeyParams &p, const double *x, const double *y,
                             const double *z, const NavState *in, size_t n, void *ws, const uint32_t **order,
                             cudaStream_t s);
+// Fixed scratch of the no-allocation step entry point (noalloc.cu).
+size_t noalloc_max_tracks();
+cudaError_t noalloc_scratch(void **ptr, size_t *bytes);
 // flags: VG_PREC_FP64 (0) or VG_PREC_MIXED (1)
 inline cudaError_t launch_step(const DevGeom &g, const StepArgs &a, uint32_t flags, cudaStream_t s)
 {
