@@ -1,0 +1,91 @@
+"""Known-answer vectors from the reference's shape unit tests (tests/golden/unit_*.json,
+made by tests/golden/extract_unit_vectors.py): loading, shape construction through either
+geometry API (the oracle's or the product's, which share method names), and the tests'
+own comparison rules."""
+import json
+import math
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+FILES = ["Box", "Tube", "Cons", "Polycone", "Torus2", "Trd"]
+QUERY_ID = {"Inside": 0, "DistanceToIn": 2, "DistanceToOut": 3, "SafetyToIn": 4, "SafetyToOut": 5}
+APPROX_TOL = 1e-6   # kApproxEqualTolerance of test/unit_tests/ApproxEqual.h
+RANGE_DELTA = 1e-4  # DELTA of OutRange in test/unit_tests/TestCons.cpp
+
+
+# Soft checks the reference itself does not meet, found by reading its code path:
+# (file, line) -> reason.
+SOFT_EXCEPTIONS = {
+    ("Cons", 591): "point 2.5e-7 mm outside -dz: ConeImplementation::DistanceToOut returns -1 when "
+                   "|z| - dz > kConeTolerance (1e-7), VecGeom/volumes/kernel/ConeImplementation.h:274-284",
+}
+
+
+def excepted(name, case):
+    return case.get("soft", False) and (name, case["line"]) in SOFT_EXCEPTIONS
+
+
+def load(name):
+    with open(os.path.join(GOLDEN, "unit_%s.json" % name)) as f:
+        return json.load(f)
+
+
+def add_shape(geo, spec):
+    t, a = spec["type"], spec["args"]
+    if t == "box":
+        return geo.add_box(*a[:3])
+    if t == "tube":
+        return geo.add_tube(*a[:5])
+    if t == "cone":
+        return geo.add_cone(*a[:7])
+    if t == "torus2":
+        return geo.add_torus2(*a[:5])
+    if t == "trd":
+        if len(a) == 4:  # Trd1 constructor (x1, x2, y, z)
+            return geo.add_trd(a[0], a[1], a[2], a[2], a[3])
+        return geo.add_trd(*a[:5])
+    if t == "polycone":
+        sphi, dphi, nz, z, rmin, rmax = a[:6]
+        nz = int(nz)
+        return geo.add_polycone(sphi, dphi, list(z)[:nz], list(rmin)[:nz], list(rmax)[:nz])
+    raise ValueError(t)
+
+
+def build(geo, spec):
+    """The shape placed alone with the identity transformation; returns its placed id."""
+    pv = geo.place(geo.add_logical_volume(add_shape(geo, spec)))
+    geo.close()
+    return pv
+
+
+def approx_equal(x, y):
+    """ApproxEqual<double> of test/unit_tests/ApproxEqual.h."""
+    if x == y:
+        return True
+    if x * y == 0.0:
+        return abs(x - y) < APPROX_TOL
+    if abs(x) > 1e100 or abs(y) > 1e100:
+        return x * y > 0 and abs(x) > 1e100 and abs(y) > 1e100
+    return abs(x - y) / (abs(x) + abs(y)) < APPROX_TOL
+
+
+def passes(kind, actual, expected):
+    a, e = float(actual), float(expected)
+    if kind == "approx":
+        return approx_equal(a, e)
+    if kind == "range":
+        return not (a < e - RANGE_DELTA or a > e + RANGE_DELTA)
+    return {"==": a == e, "!=": a != e, "<": a < e, "<=": a <= e, ">": a > e, ">=": a >= e}[kind]
+
+
+def grouped(doc):
+    """Cases grouped by (shape, query): arrays of points/directions and the case list."""
+    groups = {}
+    for c in doc["cases"]:
+        groups.setdefault((c["shape"], c["query"]), []).append(c)
+    for (shape, q), cs in groups.items():
+        p = np.array([c["p"] for c in cs], dtype=np.float64)
+        d = np.array([c["d"] if c["d"] else [0.0, 0.0, 1.0] for c in cs], dtype=np.float64)
+        yield shape, q, cs, p, d

@@ -1,0 +1,49 @@
+"""The oracle against the known answers of the reference's own shape unit tests
+(test/unit_tests/Test{Box,Tube,Cons,Polycone,Torus2,Trd}.cpp, extracted as text into
+tests/golden/unit_*.json): every extracted assert passes with the tests' own comparison.
+Soft checks (TestCons prints a mismatch instead of asserting) must pass too, except the
+ones listed in golden_util.SOFT_EXCEPTIONS, where the reference's own code path gives a
+different answer (each entry says why)."""
+import numpy as np
+import pytest
+
+import golden_util as G
+
+
+@pytest.mark.parametrize("name", G.FILES)
+def test_oracle_matches_reference_unit_tests(name):
+    from oracle.oracle import OracleGeometry
+    doc = G.load(name)
+    assert doc["cases"], "no cases extracted"
+    fails = []
+    for shape, q, cs, p, d in G.grouped(doc):
+        o = OracleGeometry()
+        pv = G.build(o, doc["shapes"][shape])
+        qi = G.QUERY_ID[q]
+        if qi in (2, 3):
+            out, _ = o.query(pv, qi, p[:, 0].copy(), p[:, 1].copy(), p[:, 2].copy(), d[:, 0].copy(), d[:, 1].copy(),
+                             d[:, 2].copy())
+        else:
+            out, _ = o.query(pv, qi, p[:, 0].copy(), p[:, 1].copy(), p[:, 2].copy())
+        for c, v in zip(cs, out):
+            if not G.passes(c["kind"], v, c["expected"]) and not G.excepted(name, c):
+                fails.append((c["line"], shape, q, c["p"], c["d"], c["kind"], c["expected"], float(v)))
+    assert not fails, "%d of %d fail, first: %s" % (len(fails), len(doc["cases"]), fails[:5])
+
+
+def test_pin_detects_a_planted_error():
+    """The same checks on an oracle fed shapes 1e-3 mm larger than the tests construct
+    must fail: the known answers are sharp enough to catch a wrong dimension."""
+    from oracle.oracle import OracleGeometry
+    doc = G.load("Box")
+    bad = 0
+    for shape, q, cs, p, d in G.grouped(doc):
+        spec = dict(doc["shapes"][shape])
+        spec["args"] = [a + 1e-3 for a in spec["args"]]
+        o = OracleGeometry()
+        pv = G.build(o, spec)
+        qi = G.QUERY_ID[q]
+        cols = [p[:, k].copy() for k in range(3)] + ([d[:, k].copy() for k in range(3)] if qi in (2, 3) else [])
+        out, _ = o.query(pv, qi, *cols)
+        bad += sum(not G.passes(c["kind"], v, c["expected"]) for c, v in zip(cs, out))
+    assert bad >= 20, bad
