@@ -53,6 +53,11 @@ int oracle_add_shape(void *gp, int type, const double *p, int np)
     s            = new Polycone(p[0], p[1], nz, p + 3, p + 3 + nz, p + 3 + 2 * nz);
     break;
   }
+  case 5: {
+    const int nz = (int)p[3];
+    s            = new Polyhedron(p[0], p[1], (int)p[2], nz, p + 4, p + 4 + nz, p + 4 + 2 * nz);
+    break;
+  }
   case 6: s = new Torus2(p[0], p[1], p[2], p[3], p[4]); break;
   case 7: s = new Trd(p[0], p[1], p[2], p[3], p[4]); break;
   case 8: s = new BooleanMinus(g->pvs.at((int)p[0]).get(), g->pvs.at((int)p[1]).get()); break;

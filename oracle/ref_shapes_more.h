@@ -83,3 +83,72 @@ struct Torus2 : UnplacedShape {
   void Extent(Vec3 &lo, Vec3 &hi) const override { fBoundingTube.Extent(lo, hi); }
 };
 } // namespace oracle
+
+namespace oracle {
+// Set of quadrilaterals (VecGeom/volumes/Quadrilaterals.h, source/Quadrilaterals.cpp):
+// plane (normal, distance), four side planes for the bounds check, four corners.
+struct Quads {
+  std::vector<Vec3> normal;
+  std::vector<double> dist;
+  std::vector<Vec3> sideN[4];
+  std::vector<double> sideD[4];
+  std::vector<Vec3> corner[4];
+  explicit Quads(int n = 0) { Resize(n); }
+  void Resize(int n);
+  int size() const { return (int)dist.size(); }
+  void Set(int i, Vec3 const &c0, Vec3 const &c1, Vec3 const &c2, Vec3 const &c3);
+  void FlipSign(int i)
+  {
+    normal[i] = -normal[i];
+    dist[i]   = -dist[i];
+  }
+  bool Contains(Vec3 const &p) const;
+  int Inside(Vec3 const &p) const;
+  int Inside(Vec3 const &p, int i) const;
+  bool RayHits(int i, Vec3 const &x) const;
+  double DistanceToIn(Vec3 const &p, Vec3 const &d, bool behind) const;
+  double DistanceToOut(Vec3 const &p, Vec3 const &d, double zMin, double zMax) const;
+  double ScalarDistanceSquared(int i, Vec3 const &p) const;
+};
+
+struct ZSegment {
+  Quads outer, phi, inner;
+  bool hasInnerRadius() const { return inner.size() > 0; }
+};
+
+// VecGeom/volumes/PolyhedronStruct.h (construction), VecGeom/volumes/kernel/
+// PolyhedronImplementation.h (scalar kernels), EInnerRadii/EPhiCutout = kGeneric as used by
+// UnplacedPolyhedron (VecGeom/volumes/UnplacedPolyhedron.h:82-84).
+struct Polyhedron : UnplacedShape {
+  int fSideCount;
+  bool fHasInnerRadii = false, fHasPhiCutout, fHasLargePhiCutout;
+  double fPhiStart, fPhiDelta;
+  Wedge fPhiWedge;
+  std::vector<ZSegment> fZSegments;
+  std::vector<double> fZPlanes, fRMin, fRMax;
+  std::vector<bool> fSameZ;
+  std::vector<Vec3> fPhiSections;
+  Tube fBoundingTube;
+  double fBoundingTubeOffset = 0.;
+  Polyhedron(double phiStart, double phiDelta, int sideCount, int nz, const double *z, const double *rmin,
+             const double *rmax);
+  int FindZSegment(double z) const;
+  int FindPhiSegment(Vec3 const &p) const;
+  double DistanceToInZSegment(int s, Vec3 const &p, Vec3 const &d) const;
+  double DistanceToOutZSegment(int s, double zMin, double zMax, Vec3 const &p, Vec3 const &d) const;
+  double SafetyToZSegmentSquared(int s, int &phiIndex, Vec3 const &p, bool ptInside, int &iSurf) const;
+  void DistanceToEndcaps(bool pointInside, Vec3 const &p, Vec3 const &d, double &distance) const;
+  void SafetyToEndcapsSquared(Vec3 const &p, double &distance, int &iz) const;
+  bool InPhiCutoutWedge(ZSegment const &s, Vec3 const &p) const;
+  int InsideSegBorder(Vec3 const &p, int zIndex) const;
+  int InsideSegPhi(Vec3 const &p, int zIndex, int phiIndex) const;
+  double SafetyKernel(Vec3 const &p, bool ptInside) const;
+  int Inside(Vec3 const &p) const override;
+  bool Contains(Vec3 const &p) const override;
+  double DistanceToIn(Vec3 const &p, Vec3 const &d, double smax) const override;
+  double DistanceToOut(Vec3 const &p, Vec3 const &d, double smax) const override;
+  double SafetyToIn(Vec3 const &p) const override { return SafetyKernel(p, false); }
+  double SafetyToOut(Vec3 const &p) const override { return SafetyKernel(p, true); }
+  void Extent(Vec3 &lo, Vec3 &hi) const override;
+};
+} // namespace oracle

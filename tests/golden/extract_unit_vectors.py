@@ -1,6 +1,6 @@
 """Extract known-answer vectors from VecGeom's shape unit tests into JSON fixtures.
 
-Reads test/unit_tests/Test{Box,Tube,Cons,Polycone,Torus2,Trd}.cpp of a VecGeom source
+Reads test/unit_tests/Test{Box,Tube,Cons,Polycone,Torus2,Trd,Polyhedra}.cpp of a VecGeom source
 tree AS TEXT (nothing of it is compiled or run) and records, for every assert that checks
 a query result of a shape constructed in the test:
 
@@ -35,8 +35,9 @@ FILES = {
     "Polycone": ("TestPolycone.cpp", {"Polycone_t": "polycone"}),
     "Torus2": ("TestTorus2.cpp", {"Torus_t": "torus2"}),
     "Trd": ("TestTrd.cpp", {"Trd_t": "trd"}),
+    "Polyhedra": ("TestPolyhedra.cpp", {"Polyhedra_t": "polyhedron"}),
 }
-QUERIES = {"Inside", "DistanceToIn", "DistanceToOut", "SafetyToIn", "SafetyToOut"}
+QUERIES = {"Inside", "Contains", "DistanceToIn", "DistanceToOut", "SafetyToIn", "SafetyToOut"}
 
 
 class V:
@@ -184,6 +185,42 @@ def split_top(s, sep=","):
     return [p.strip() for p in parts]
 
 
+def strip_parens(s):
+    """Remove parentheses that enclose the whole expression."""
+    s = s.strip()
+    while s.startswith("("):
+        depth = 0
+        for k, ch in enumerate(s):
+            depth += ch == "("
+            depth -= ch == ")"
+            if depth == 0:
+                break
+        if k != len(s) - 1:
+            break
+        s = s[1:-1].strip()
+    return s
+
+
+def find_top(s, ops):
+    """First operator of `ops` outside parentheses that is not part of `->`; (index, op)."""
+    depth = 0
+    for k, ch in enumerate(s):
+        depth += ch in "([{"
+        depth -= ch in ")]}"
+        if depth:
+            continue
+        for op in ops:
+            if s.startswith(op, k):
+                if op in (">", ">=") and k > 0 and s[k - 1] == "-":
+                    continue
+                if op == "-" and s.startswith("->", k):
+                    continue
+                if op in ("<", ">") and (s.startswith("<=", k) or s.startswith(">=", k)):
+                    continue
+                return k, op
+    return -1, None
+
+
 def to_py(expr):
     e = expr.strip()
     e = re.sub(r"\bstatic_cast<[^>]*>", "", e)
@@ -240,11 +277,32 @@ class Extractor:
         c = dict(qd, kind=kind, expected=value, line=line, soft=soft)
         self.cases.append(c)
 
+    def handle_fabs(self, term, line):
+        """`fabs(CALL - value) < tol` or `fabs(CALL) < tol` (TestPolyhedra.cpp style)."""
+        m = re.match(r"^(?:std::)?fabs\s*\((.*)\)\s*<\s*(.+)$", term, flags=re.S)
+        if not m:
+            return False
+        inner = strip_parens(m.group(1))
+        k, op = find_top(inner, ["-"])
+        call, val = (strip_parens(inner[:k]), inner[k + 1:].strip()) if k > 0 else (inner, "0")
+        qd = self.results.get(call) if re.match(r"^\w+$", call) else self.query_call(call)
+        if qd is None:
+            return False
+        tol = float(self.ev(m.group(2)))
+        self.emit(qd, "absdiff", float(self.ev(val)), line)
+        self.cases[-1]["tol"] = tol
+        return True
+
     def handle_assert(self, body, line):
+        if len(split_top(body, "|")) > 1:
+            return False  # alternatives: no single known answer
         ok = False
         for term in split_top(body, "&"):
             term = term.strip().strip("&").strip()
             if not term:
+                continue
+            if self.handle_fabs(term, line):
+                ok = True
                 continue
             m = re.match(r"^ApproxEqual(?:<[^>]*>)?\s*\((.*)\)$", term, flags=re.S)
             if m:
@@ -264,11 +322,15 @@ class Extractor:
                 self.emit(qd, "approx", float(val), line)
                 ok = True
                 continue
-            m = re.match(r"^(.*?)\s*(==|!=|<=|>=|<|>)\s*(.*)$", term, flags=re.S)
-            if m:
-                lhs, op, rhs = m.group(1).strip(), m.group(2), m.group(3).strip()
-                lhs = lhs.lstrip("(").strip()
-                rhs = rhs.rstrip(")").strip() if rhs.count(")") > rhs.count("(") else rhs
+            neg = term.startswith("!")
+            qd = self.query_call(strip_parens(term[1:] if neg else term))
+            if qd is not None and qd["query"] == "Contains":
+                self.emit(qd, "==", 0.0 if neg else 1.0, line)
+                ok = True
+                continue
+            k, op = find_top(term, ["==", "!=", "<=", ">=", "<", ">"])
+            if k > 0:
+                lhs, rhs = strip_parens(term[:k]), strip_parens(term[k + len(op):])
                 qd = self.results.get(lhs) if re.match(r"^\w+$", lhs) else self.query_call(lhs)
                 if qd is None:
                     continue
@@ -348,6 +410,21 @@ class Extractor:
             try:
                 self.env[m.group(1)] = [float(self.ev(a)) for a in split_top(m.group(2)) if a]
             except Exception:
+                self.skipped += 1
+            return
+        m = re.match(r"^(?:const\s+)?(?:double|Precision|float)\s+(\w+)\s*\[\s*(\w+)\s*\]$", st)
+        if m:
+            try:
+                self.env[m.group(1)] = [0.0] * int(self.ev(m.group(2)))
+            except Exception:
+                self.skipped += 1
+            return
+        m = re.match(r"^(\w+)\s*\[\s*(\w+)\s*\]\s*=\s*(.*)$", st, flags=re.S)
+        if m and isinstance(self.env.get(m.group(1)), list):
+            try:
+                self.env[m.group(1)][int(self.ev(m.group(2)))] = float(self.ev(m.group(3)))
+            except Exception:
+                self.env.pop(m.group(1), None)
                 self.skipped += 1
             return
         # vector declarations

@@ -9,8 +9,8 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-FILES = ["Box", "Tube", "Cons", "Polycone", "Torus2", "Trd"]
-QUERY_ID = {"Inside": 0, "DistanceToIn": 2, "DistanceToOut": 3, "SafetyToIn": 4, "SafetyToOut": 5}
+FILES = ["Box", "Tube", "Cons", "Polycone", "Torus2", "Trd", "Polyhedra"]
+QUERY_ID = {"Inside": 0, "Contains": 1, "DistanceToIn": 2, "DistanceToOut": 3, "SafetyToIn": 4, "SafetyToOut": 5}
 APPROX_TOL = 1e-6   # kApproxEqualTolerance of test/unit_tests/ApproxEqual.h
 RANGE_DELTA = 1e-4  # DELTA of OutRange in test/unit_tests/TestCons.cpp
 
@@ -46,6 +46,10 @@ def add_shape(geo, spec):
         if len(a) == 4:  # Trd1 constructor (x1, x2, y, z)
             return geo.add_trd(a[0], a[1], a[2], a[2], a[3])
         return geo.add_trd(*a[:5])
+    if t == "polyhedron":
+        sphi, dphi, nsides, nz, z, rmin, rmax = a[:7]
+        nz = int(nz)
+        return geo.add_polyhedron(sphi, dphi, int(nsides), list(z)[:nz], list(rmin)[:nz], list(rmax)[:nz])
     if t == "polycone":
         sphi, dphi, nz, z, rmin, rmax = a[:6]
         nz = int(nz)
@@ -71,8 +75,10 @@ def approx_equal(x, y):
     return abs(x - y) / (abs(x) + abs(y)) < APPROX_TOL
 
 
-def passes(kind, actual, expected):
+def passes(kind, actual, expected, tol=None):
     a, e = float(actual), float(expected)
+    if kind == "absdiff":  # std::fabs(actual - expected) < tol
+        return abs(a - e) < tol
     if kind == "approx":
         return approx_equal(a, e)
     if kind == "range":

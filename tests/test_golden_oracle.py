@@ -1,5 +1,5 @@
 """The oracle against the known answers of the reference's own shape unit tests
-(test/unit_tests/Test{Box,Tube,Cons,Polycone,Torus2,Trd}.cpp, extracted as text into
+(test/unit_tests/Test{Box,Tube,Cons,Polycone,Torus2,Trd,Polyhedra}.cpp, extracted as text into
 tests/golden/unit_*.json): every extracted assert passes with the tests' own comparison.
 Soft checks (TestCons prints a mismatch instead of asserting) must pass too, except the
 ones listed in golden_util.SOFT_EXCEPTIONS, where the reference's own code path gives a
@@ -26,7 +26,7 @@ def test_oracle_matches_reference_unit_tests(name):
         else:
             out, _ = o.query(pv, qi, p[:, 0].copy(), p[:, 1].copy(), p[:, 2].copy())
         for c, v in zip(cs, out):
-            if not G.passes(c["kind"], v, c["expected"]) and not G.excepted(name, c):
+            if not G.passes(c["kind"], v, c["expected"], c.get("tol")) and not G.excepted(name, c):
                 fails.append((c["line"], shape, q, c["p"], c["d"], c["kind"], c["expected"], float(v)))
     assert not fails, "%d of %d fail, first: %s" % (len(fails), len(doc["cases"]), fails[:5])
 
@@ -45,5 +45,5 @@ def test_pin_detects_a_planted_error():
         qi = G.QUERY_ID[q]
         cols = [p[:, k].copy() for k in range(3)] + ([d[:, k].copy() for k in range(3)] if qi in (2, 3) else [])
         out, _ = o.query(pv, qi, *cols)
-        bad += sum(not G.passes(c["kind"], v, c["expected"]) for c, v in zip(cs, out))
+        bad += sum(not G.passes(c["kind"], v, c["expected"], c.get("tol")) for c, v in zip(cs, out))
     assert bad >= 20, bad

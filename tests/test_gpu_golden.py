@@ -19,6 +19,9 @@ def _run(torch, g, pv, qi, p, d):
     if qi == 0:
         out = torch.empty(n, dtype=torch.int32, device="cuda:0")
         g.inside(pv, x, y, z, out)
+    elif qi == 1:
+        out = torch.empty(n, dtype=torch.uint8, device="cuda:0")
+        g.contains(pv, x, y, z, out)
     elif qi in (2, 3):
         out = torch.empty(n, dtype=torch.float64, device="cuda:0")
         f = g.distance_to_in if qi == 2 else g.distance_to_out
@@ -44,10 +47,10 @@ def test_kernels_match_reference_unit_tests(cuda, name):
         cols = [p[:, k].copy() for k in range(3)] + ([d[:, k].copy() for k in range(3)] if qi in (2, 3) else [])
         ref, _ = o.query(opv, qi, *cols)
         for c, v in zip(cs, got):
-            if not G.passes(c["kind"], v, c["expected"]) and not G.excepted(name, c):
+            if not G.passes(c["kind"], v, c["expected"], c.get("tol")) and not G.excepted(name, c):
                 fails.append((c["line"], shape, q, c["expected"], float(v)))
-        if qi == 0:
-            bad = got != ref
+        if qi in (0, 1):
+            bad = got.astype(np.int64) != ref.astype(np.int64)
         elif spec["type"] == "torus2":
             bad = ~((got == ref) | (np.abs(got - ref) <= 1e-8))
         else:

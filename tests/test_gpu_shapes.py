@@ -134,7 +134,7 @@ def test_placed_transform_parity(cuda):
 CFG2_TOL = {"torus2": 1e-8}
 
 
-@pytest.mark.parametrize("name", ["tube_phi", "polycone", "torus2", "trd", "box_minus_tube"])
+@pytest.mark.parametrize("name", ["tube_phi", "polycone", "polyhedron", "torus2", "trd", "box_minus_tube"])
 def test_cfg2_shape_parity(cuda, name):
     import vecgeom_gb300 as vg
     from oracle.oracle import OracleGeometry
@@ -154,4 +154,33 @@ def test_cfg2_shape_parity(cuda, name):
     assert np.array_equal(got[1], ref[1]), ("Contains", int((got[1] != ref[1]).sum()))
     for q in (2, 3, 4, 5):
         bad = dist_mismatch(got[q], ref[q], abs_tol=tol)
+        assert not bad.any(), (q, int(bad.sum()), got[q][bad][:4], ref[q][bad][:4])
+
+
+# Polyhedron variants beyond the config-2 shape: phi cut-outs smaller and larger than pi,
+# a z plane shared by two segments (the border case), inner radii on some segments only.
+POLYHEDRA = [
+    (0.3, 1.8, 5, (-100.0, 0.0, 0.0, 50.0), (0.0, 10.0, 20.0, 5.0), (40.0, 60.0, 50.0, 30.0)),
+    (0.0, 4.5, 3, (-10.0, 10.0), (0.0, 0.0), (20.0, 30.0)),
+    (0.5, 2 * np.pi, 6, (-50.0, -20.0, 30.0, 60.0), (10.0, 0.0, 0.0, 15.0), (40.0, 45.0, 45.0, 20.0)),
+]
+
+
+@pytest.mark.parametrize("k", range(len(POLYHEDRA)))
+def test_polyhedron_variants_parity(cuda, k):
+    import vecgeom_gb300 as vg
+    from oracle.oracle import OracleGeometry
+    from vecgeom_gb300 import workloads as W
+    g, o = vg.Geometry(), OracleGeometry()
+    s, pv = W.build_single_shape(g, "polyhedron", POLYHEDRA[k])
+    W.build_single_shape(o, "polyhedron", POLYHEDRA[k])
+    lo, hi = g.shape_extent(s)
+    pts, dirs = W.shape_points_mixed(lo, hi, 3 * 4096, 91 + k, lambda x, y, z: o.query(pv, 0, x, y, z)[0],
+                                     lambda *a: o.query(pv, 3, *a)[0])
+    got = run_all_queries(cuda, g, pv, pts, dirs)
+    ref = oracle_all(o, pv, pts, dirs)
+    assert np.array_equal(got[0], ref[0]), ("Inside", int((got[0] != ref[0]).sum()))
+    assert np.array_equal(got[1], ref[1]), ("Contains", int((got[1] != ref[1]).sum()))
+    for q in (2, 3, 4, 5):
+        bad = dist_mismatch(got[q], ref[q])
         assert not bad.any(), (q, int(bad.sum()), got[q][bad][:4], ref[q][bad][:4])

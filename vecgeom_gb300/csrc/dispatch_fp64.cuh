@@ -5,6 +5,7 @@
 #include "shapes_fp64.cuh"
 #include "shapes_more_fp64.cuh"
 #include "shapes_torus_fp64.cuh"
+#include "shapes_polyhedron_fp64.cuh"
 
 namespace vg {
 
@@ -18,6 +19,7 @@ namespace f64 {
   case kShapeCone: return cone_##FN(rec<ConeRec>(g, shape), __VA_ARGS__);                    \
   case kShapeTrd: return trd_##FN(rec<TrdRec>(g, shape), __VA_ARGS__);                       \
   case kShapePolycone: return polycone_##FN(rec<PolyconeRec>(g, shape), __VA_ARGS__);        \
+  case kShapePolyhedron: return polyhedron_##FN(rec<PolyhedronRec>(g, shape), __VA_ARGS__);  \
   case kShapeTorus2: return torus_##FN(rec<TorusRec>(g, shape), __VA_ARGS__);                \
   default: break;                                                                            \
   }

@@ -373,6 +373,237 @@ void make_torus2(const double *p, HostShape &s)
   for (int k = 0; k < 3; ++k) s.lo[k] = bt.lo[k], s.hi[k] = bt.hi[k];
 }
 
+// ---------------------------------------------------------------- polyhedron
+// Construction of PolyhedronStruct(phiStart, phiDelta, sideCount, zPlaneCount, zPlanes,
+// rMin, rMax) + Initialize (VecGeom/volumes/PolyhedronStruct.h:112-125, 262-430), with
+// the quadrilateral and plane setters of source/Quadrilaterals.cpp:44-123 and
+// source/Planes.cpp:31-52, evaluated in the same order so the record is bit-identical.
+namespace {
+struct HV {
+  double v[3];
+  double operator[](int i) const { return v[i]; }
+};
+HV hv(double x, double y, double z) { return HV{{x, y, z}}; }
+HV hsub(HV a, HV b) { return hv(a[0] - b[0], a[1] - b[1], a[2] - b[2]); }
+double hdot(HV a, HV b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+double hmag(HV a) { return std::sqrt(hdot(a, a)); }
+HV hscale(HV a, double s) { return hv(a[0] * s, a[1] * s, a[2] * s); }
+HV hcross(HV l, HV r) { return hv(l[1] * r[2] - l[2] * r[1], l[2] * r[0] - l[0] * r[2], l[0] * r[1] - l[1] * r[0]); }
+HV hfix(HV a)
+{
+  for (int i = 0; i < 3; ++i)
+    if (std::fabs(a.v[i]) < kTolerance) a.v[i] = 0.;
+  return a;
+}
+HV hnormalized(HV a) { return hscale(a, 1. / hmag(a)); }
+bool hsame(HV a, HV b)
+{
+  return std::fabs(a[0] - b[0]) < kTolerance && std::fabs(a[1] - b[1]) < kTolerance &&
+         std::fabs(a[2] - b[2]) < kTolerance;
+}
+HV hcyl(double r, double phi, double z) { return hv(r * std::cos(phi), r * std::sin(phi), z); }
+double normalize_angle(double a) { return a + kTwoPi * (double)((a < 0 ? 1 : 0) - (int)(a / kTwoPi)); }
+
+// One quadrilateral (kPolyQuadDoubles doubles) from its four corners.
+void set_quad(double *q, HV c0, HV c1, HV c2, HV c3)
+{
+  const HV cs[4] = {c0, c1, c2, c3};
+  HV ch[4]       = {hv(0, 0, 0), hv(0, 0, 0), hv(0, 0, 0), hv(0, 0, 0)};
+  ch[0]          = c0;
+  int assigned = 1, tested = 1;
+  while (tested < 4) {
+    bool chosen = true;
+    for (int j = 0; j < assigned; ++j)
+      if (hsame(ch[j], cs[tested])) {
+        chosen = false;
+        break;
+      }
+    if (chosen) ch[assigned++] = cs[tested];
+    ++tested;
+  }
+  const double a = ch[0][1] * (ch[1][2] - ch[2][2]) + ch[1][1] * (ch[2][2] - ch[0][2]) + ch[2][1] * (ch[0][2] - ch[1][2]);
+  const double b = ch[0][2] * (ch[1][0] - ch[2][0]) + ch[1][2] * (ch[2][0] - ch[0][0]) + ch[2][2] * (ch[0][0] - ch[1][0]);
+  const double c = ch[0][0] * (ch[1][1] - ch[2][1]) + ch[1][0] * (ch[2][1] - ch[0][1]) + ch[2][0] * (ch[0][1] - ch[1][1]);
+  double d = -ch[0][0] * (ch[1][1] * ch[2][2] - ch[2][1] * ch[1][2]) - ch[1][0] * (ch[2][1] * ch[0][2] - ch[0][1] * ch[2][2]) -
+             ch[2][0] * (ch[0][1] * ch[1][2] - ch[1][1] * ch[0][2]);
+  HV n             = hv(a, b, c);
+  const double inv = 1. / hmag(n);
+  n                = hscale(n, inv);
+  d *= inv;
+  n = hfix(n);
+  q[0] = n[0], q[1] = n[1], q[2] = n[2], q[3] = d;
+  for (int j = 0; j < 4; ++j) {
+    const HV a0 = cs[j], a1 = cs[(j + 1) % 4];
+    double *sp  = q + 4 + 4 * j;
+    if (!hsame(a1, a0)) {
+      const HV sv     = hfix(hnormalized(hcross(n, hsub(a1, a0))));
+      const double il = 1. / hmag(sv);
+      sp[0] = il * sv[0], sp[1] = il * sv[1], sp[2] = il * sv[2];
+      sp[3] = il * -hdot(sv, a0);
+    } else {
+      sp[0] = sp[1] = sp[2] = sp[3] = 0.;
+    }
+  }
+  for (int k = 0; k < 4; ++k)
+    for (int i = 0; i < 3; ++i) q[20 + 3 * k + i] = cs[k][i];
+}
+void flip_quad(double *q)
+{
+  for (int i = 0; i < 4; ++i) q[i] = -q[i];
+}
+} // namespace
+
+bool make_polyhedron(const double *p, int np, HostShape &s, std::string &err)
+{
+  const double phiStartIn = p[0], phiDeltaIn = p[1];
+  const int S = (int)p[2], nz = (int)p[3];
+  if (S < 1 || nz < 2 || np < 4 + 3 * nz || !(phiDeltaIn > 0)) {
+    err = "polyhedron needs >= 1 side, >= 2 z planes and phiDelta > 0";
+    return false;
+  }
+  const double *zp = p + 4, *rmin = p + 4 + nz, *rmax = p + 4 + 2 * nz;
+  for (int i = 0; i < nz; ++i) {
+    if (i + 1 < nz && !(zp[i] <= zp[i + 1])) {
+      err = "polyhedron z planes must be non-decreasing";
+      return false;
+    }
+    if (!(rmin[i] >= 0) || !(rmax[i] >= rmin[i])) {
+      err = "polyhedron radii must satisfy 0 <= rmin <= rmax";
+      return false;
+    }
+  }
+  const int nseg          = nz - 1;
+  const bool hasPhiCutout = phiDeltaIn < kTwoPi, largePhiCutout = phiDeltaIn < kPi;
+  const double fPhiStart  = normalize_angle(phiStartIn);
+  const double fPhiDelta  = phiDeltaIn > kTwoPi ? kTwoPi : phiDeltaIn;
+  // quadrilateral counts per segment
+  std::vector<int> nout(nseg), nphi(nseg), nin(nseg);
+  bool hasInnerRadii = false;
+  for (int i = 0; i < nseg; ++i) {
+    const bool hasInner = rmin[i] > 0 || rmin[i + 1] > 0;
+    nout[i]             = S * ((zp[i] == zp[i + 1] && rmax[i] == rmax[i + 1]) ? 0 : 1);
+    nphi[i]             = hasPhiCutout ? 2 * ((zp[i] == zp[i + 1]) ? 0 : 1) : 0;
+    const int mult      = (zp[i] == zp[i + 1] && rmin[i] == rmin[i + 1]) ? 0 : 1;
+    nin[i]              = (hasInner && mult > 0) ? S * mult : 0;
+    if (nin[i] > 0) hasInnerRadii = true;
+  }
+  // layout
+  const int hdr = ((int)(sizeof(PolyhedronRec) / sizeof(double)) + 3) / 4 * 4;
+  int off       = hdr;
+  auto take     = [&](int n) {
+    const int o = off;
+    off += (n + 3) / 4 * 4;
+    return o;
+  };
+  const int oZ = take(nz), oRmin = take(nz), oRmax = take(nz), oSameZ = take(nz), oPhiSec = take(3 * (S + 1));
+  const int oSeg = take(4 * nseg);
+  std::vector<int> qbase(nseg);
+  for (int i = 0; i < nseg; ++i) qbase[i] = take(kPolyQuadDoubles * (nout[i] + nphi[i] + nin[i]));
+  std::vector<double> rec(off, 0.);
+  PolyhedronRec h{};
+  h.nsides = S, h.nseg = nseg, h.nz = nz;
+  h.flags  = (hasInnerRadii ? kPolyFlagInner : 0) | (hasPhiCutout ? kPolyFlagPhi : 0) |
+            (largePhiCutout ? kPolyFlagLargePhi : 0);
+  h.phiStart = fPhiStart, h.phiDelta = fPhiDelta;
+  h.offZ = oZ, h.offRMin = oRmin, h.offRMax = oRmax, h.offSameZ = oSameZ, h.offPhiSec = oPhiSec, h.offSeg = oSeg;
+  h.w = make_wedge(fPhiDelta, fPhiStart);
+  for (int i = 0; i < nz; ++i) {
+    rec[oZ + i] = zp[i], rec[oRmin + i] = rmin[i], rec[oRmax + i] = rmax[i];
+    rec[oSameZ + i] = (i > 0 && i < nz - 1 && zp[i] == zp[i + 1]) ? 1. : 0.;
+  }
+  for (int i = 0; i < nseg; ++i) {
+    rec[oSeg + 4 * i] = nout[i], rec[oSeg + 4 * i + 1] = nphi[i], rec[oSeg + 4 * i + 2] = nin[i];
+    rec[oSeg + 4 * i + 3] = qbase[i];
+  }
+  // phi of the corners and the phi-section planes
+  const double phiStart = normalize_angle(phiStartIn);
+  const double phiDelta = phiDeltaIn > kTwoPi ? kTwoPi : phiDeltaIn;
+  const double sidePhi  = phiDelta / S;
+  std::vector<double> vphi(S + 1);
+  std::vector<HV> phiSec(S + 1);
+  for (int i = 0; i < S + 1; ++i) {
+    vphi[i]         = normalize_angle(phiStart + i * sidePhi);
+    const HV corner = hfix(hnormalized(hcyl(1., vphi[i], 0)));
+    phiSec[i]       = hcross(hnormalized(corner), hv(0, 0, -1));
+    for (int k = 0; k < 3; ++k) rec[oPhiSec + 3 * i + k] = phiSec[i][k];
+  }
+  if (!hasPhiCutout) vphi[S] = vphi[0];
+  const double cosHalf = std::cos(0.5 * sidePhi);
+  double innerRadius = kInfLength, outerRadius = -kInfLength;
+  for (int i = 0; i < nz; ++i) {
+    if (rmin[i] < innerRadius) innerRadius = rmin[i];
+    if (rmax[i] > outerRadius) outerRadius = rmax[i];
+  }
+  outerRadius /= cosHalf;
+  const double kPhiTolerance = 100 * kTolerance;
+  const double bp[5] = {innerRadius - kHalfTolerance, outerRadius + kHalfTolerance,
+                        0.5 * (zp[nz - 1] - zp[0]) + kTolerance, !hasPhiCutout ? 0 : phiStart - kPhiTolerance,
+                        !hasPhiCutout ? kTwoPi : phiDelta + 2 * kPhiTolerance};
+  HostShape bt;
+  make_tube(bp, bt);
+  std::memcpy(&h.bt, bt.rec.data(), sizeof(TubeRec));
+  h.tubeOffset = 0.5 * (zp[0] + zp[nz - 1]);
+  // vertices and quadrilaterals
+  auto VI = [S](int plane, int corner) { return plane * (S + 1) + corner; };
+  std::vector<HV> ov(nz * (S + 1), hv(0, 0, 0)), iv(nz * (S + 1), hv(0, 0, 0));
+  for (int i = 0; i < nz; ++i) {
+    for (int j = 0, jMax = S + (hasPhiCutout ? 1 : 0); j < jMax; ++j) {
+      ov[VI(i, j)] = hfix(hcyl(rmax[i] / cosHalf, vphi[j], zp[i]));
+      iv[VI(i, j)] = hfix(hcyl(rmin[i] / cosHalf, vphi[j], zp[i]));
+    }
+    if (!hasPhiCutout) {
+      ov[VI(i, S)] = ov[VI(i, 0)];
+      iv[VI(i, S)] = iv[VI(i, 0)];
+    }
+  }
+  auto wrong = [](const double *q, HV c) { return q[0] * c[0] + q[1] * c[1] < 0; };
+  for (int ip = 0; ip < nseg; ++ip) {
+    double *qo = rec.data() + qbase[ip];
+    double *qp = qo + kPolyQuadDoubles * nout[ip];
+    double *qi = qp + kPolyQuadDoubles * nphi[ip];
+    for (int k = 0; k < nout[ip]; ++k) {
+      double *q = qo + kPolyQuadDoubles * k;
+      set_quad(q, ov[VI(ip, k)], ov[VI(ip, k + 1)], ov[VI(ip + 1, k + 1)], ov[VI(ip + 1, k)]);
+      if (wrong(q, ov[VI(ip, k)])) flip_quad(q);
+    }
+    for (int k = 0; k < nin[ip]; ++k) {
+      double *q = qi + kPolyQuadDoubles * k;
+      set_quad(q, iv[VI(ip, k)], iv[VI(ip, k + 1)], iv[VI(ip + 1, k + 1)], iv[VI(ip + 1, k)]);
+      if (wrong(q, iv[VI(ip, k)])) flip_quad(q);
+    }
+    if (hasPhiCutout && nphi[ip] == 2) {
+      set_quad(qp, iv[VI(ip, 0)], iv[VI(ip + 1, 0)], ov[VI(ip + 1, 0)], ov[VI(ip, 0)]);
+      if (hdot(hv(qp[0], qp[1], qp[2]), phiSec[0]) > 0) flip_quad(qp);
+      double *q1 = qp + kPolyQuadDoubles;
+      set_quad(q1, ov[VI(ip, S)], ov[VI(ip + 1, S)], iv[VI(ip + 1, S)], iv[VI(ip, S)]);
+      if (hdot(hv(q1[0], q1[1], q1[2]), phiSec[S]) < 0) flip_quad(q1);
+    }
+  }
+  std::memcpy(rec.data(), &h, sizeof(h));
+  s.type = kShapePolyhedron;
+  s.rec  = std::move(rec);
+  // UnplacedPolyhedron::Extent (source/UnplacedPolyhedron.cpp:273-303)
+  for (int k = 0; k < 3; ++k) s.lo[k] = kInfLength, s.hi[k] = -kInfLength;
+  const double sp   = fPhiDelta / S;
+  const double conv = 1. / std::cos(0.5 * sp);
+  for (int iphi = 0; iphi <= S; ++iphi) {
+    const double phi = fPhiStart + iphi * sp;
+    const double cx = conv * std::cos(phi), cy = conv * std::sin(phi);
+    for (int k = 0; k < nz; ++k) {
+      const double a[3] = {rmin[k] * cx, rmin[k] * cy, zp[k]}, b[3] = {rmax[k] * cx, rmax[k] * cy, zp[k]};
+      for (int i = 0; i < 3; ++i) { // Min(a, b) = a < b ? a : b, Max(a, b) = a > b ? a : b
+        s.lo[i] = s.lo[i] < a[i] ? s.lo[i] : a[i];
+        s.hi[i] = s.hi[i] > a[i] ? s.hi[i] : a[i];
+      }
+      for (int i = 0; i < 3; ++i) {
+        s.lo[i] = s.lo[i] < b[i] ? s.lo[i] : b[i];
+        s.hi[i] = s.hi[i] > b[i] ? s.hi[i] : b[i];
+      }
+    }
+  }
+  return true;
+}
+
 // ---------------------------------------------------------------- registry
 Geometry::~Geometry()
 {
@@ -409,6 +640,12 @@ int32_t Geometry::add_shape(int32_t type, const double *p, int np, std::string &
   case kShapeTrd:
     if (!need(5)) return -1;
     make_trd(p, s);
+    break;
+  case kShapePolyhedron:
+    if (!need(4) || !make_polyhedron(p, np, s, err)) {
+      if (err.empty()) err = "too few polyhedron parameters";
+      return -1;
+    }
     break;
   case kShapeTorus2:
     if (!need(5)) return -1;

@@ -97,6 +97,23 @@ struct TorusRec {
   TubeRec bt;
 };
 
+// Polyhedron record (VecGeom/volumes/PolyhedronStruct.h:52-107): fixed header, then the
+// z planes, radii, same-z flags and phi-section normals, a segment table (n_outer, n_phi,
+// n_inner, first quadrilateral) and the quadrilaterals of all segments (outer, phi, inner
+// in that order), kPolyQuadDoubles each: plane normal + distance, four side planes
+// (normal + distance) and four corners (Quadrilaterals.h:28-37). Offsets in doubles from
+// the record start.
+struct PolyhedronRec {
+  double nsides, nseg, nz, flags; // flags: 1 inner radii, 2 phi cutout, 4 phi cutout > pi
+  double phiStart, phiDelta, tubeOffset, pad0;
+  double offZ, offRMin, offRMax, offSameZ, offPhiSec, offSeg, pad1, pad2;
+  WedgeRec w;
+  double pad3[3];
+  TubeRec bt;
+};
+constexpr int kPolyQuadDoubles = 32; // n[3] d | (sideN[3] sideD) x 4 | corner[3] x 4
+constexpr int kPolyFlagInner = 1, kPolyFlagPhi = 2, kPolyFlagLargePhi = 4;
+
 // Boolean subtraction record (VecGeom/volumes/BooleanStruct.h:19-33): operand placed-volume ids.
 struct BoolRec {
   double left_pv, right_pv, reserved0, reserved1;
