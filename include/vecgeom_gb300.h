@@ -60,6 +60,7 @@ extern "C" {
  * its SoA navigator loops over tracks in input order (VNavigator.h:128-132). */
 #define VG_NAV_SORT 2u  /* radix-sort tracks by (logical volume, Morton cell of the position)   */
 #define VG_NAV_QUEUE 4u /* persistent kernel, warps take 32-track chunks from a global counter  */
+#define VG_NAV_LEARNED 8u /* explore the BVH subtree proposed by the attached model first       */
 
 /* Navigation state: bit-identical to vecgeom::NavStateIndex {NavIndex_t fNavInd;
  * NavIndex_t fLastExited; bool fOnBoundary;} (VecGeom/navigation/NavStateIndex.h:39-41). */
@@ -188,13 +189,15 @@ int vg_nav_compute_step_and_next_volume(const vg_geom *g, const double *x, const
 /* The same step with scheduling flags. `workspace` is device memory of at least
  * vg_nav_step_workspace_bytes(n, flags) bytes (256-byte aligned), used by this call only
  * until the stream reaches its end; concurrent calls need separate workspaces. With
- * flags < VG_NAV_SORT no workspace is needed and the call equals the one above. */
+ * flags < VG_NAV_SORT no workspace is needed and the call equals the one above.
+ * `nodes_visited` (nullable) receives the BVH nodes the daughter search visited per track
+ * (the traversal-cost figure of the learned proposal). */
 size_t vg_nav_step_workspace_bytes(size_t n, uint32_t flags);
 int vg_nav_compute_step_and_next_volume_ws(const vg_geom *g, const double *x, const double *y, const double *z,
                                            const double *dx, const double *dy, const double *dz,
                                            const double *step_limit, const vg_navstate *in, vg_navstate *out,
-                                           double *step, int32_t *status, size_t n, uint32_t flags, void *workspace,
-                                           size_t workspace_bytes, void *stream);
+                                           double *step, int32_t *status, int32_t *nodes_visited, size_t n,
+                                           uint32_t flags, void *workspace, size_t workspace_bytes, void *stream);
 
 /* The scheduled step without any allocation and without a caller workspace: scratch is a
  * fixed device array inside the library (capacity 2^20 tracks per call; larger n is
@@ -226,6 +229,42 @@ int vg_nav_sort_key_params(const vg_geom *g, float lo[3], float scale[3], int32_
  * `queue_blocks_per_sm` for VG_NAV_QUEUE (1: full register budget per thread; 2: half the
  * registers, twice the resident warps; 0 = 1). Set before sorted calls are in flight. */
 int vg_nav_set_tuning(vg_geom *g, int32_t cell_bits, int32_t queue_blocks_per_sm);
+
+/* ---------------------------------------------------------------- learned proposal
+ * No reference counterpart. A small MLP (80 -> 64 -> 64 -> 16, ReLU, BF16 weights for
+ * inference) predicts for a track in a logical volume whose BVH has depth >= 3 which of
+ * the 8 depth-3 BVH subtrees holds the first daughter the ray hits (or none). With
+ * VG_NAV_LEARNED the step explores the proposed subtree first, which tightens the step
+ * bound early; the full traversal still decides, so results do not depend on the model.
+ * vg_learn_features writes 80 FP32 features per track (`feat`, n x 80), the logical volume
+ * (`lv`, -1 where no proposal applies) and, if `label` is given, the training label from
+ * the plain FP64 traversal (0..7 subtree, 8 none, -1 not applicable). Training consumes
+ * only samples with lv >= 0 and 0 <= label <= 8: callers pass that subset. Gradients and
+ * parameters use one flat FP32 layout: W1[64][80], b1[64], W2[64][64], b2[64], W3[16][64],
+ * b3[16], E[n_lv][16]. All arrays are device memory unless stated. */
+typedef struct vg_mlp vg_mlp;
+int vg_mlp_create(const vg_geom *g, uint64_t seed, vg_mlp **out);
+void vg_mlp_destroy(vg_mlp *m);
+size_t vg_mlp_param_count(const vg_mlp *m);
+int vg_mlp_get_params(const vg_mlp *m, float *host, size_t n); /* host buffer */
+int vg_mlp_set_params(vg_mlp *m, const float *host, size_t n); /* host buffer; resets Adam */
+int vg_learn_features(const vg_geom *g, const double *x, const double *y, const double *z, const double *dx,
+                      const double *dy, const double *dz, const vg_navstate *in, size_t n, float *feat, int32_t *lv,
+                      int8_t *label, void *stream);
+/* Forward + backward over all n samples: mean softmax cross-entropy gradients (flat
+ * layout) and the summed loss. Synchronises the stream. */
+int vg_mlp_gradients(vg_mlp *m, const float *feat, const int32_t *lv, const int8_t *label, size_t n, float *grads,
+                     float *loss, void *stream);
+/* Adam (0.9, 0.999, 1e-8) over shuffled mini-batches; epoch_loss (host, nullable) gets the
+ * mean loss of each epoch. Refreshes the BF16 inference copy. Synchronises the stream. */
+int vg_mlp_train(vg_mlp *m, const float *feat, const int32_t *lv, const int8_t *label, size_t n, int32_t epochs,
+                 int32_t batch, float lr, uint64_t seed, float *epoch_loss, void *stream);
+/* Proposals from features: slot 0..7, or -1 for "none" / no proposal; logits (nullable,
+ * n x 16 FP32). flags 0: SIMT kernel. */
+int vg_mlp_infer(const vg_mlp *m, const float *feat, const int32_t *lv, size_t n, int8_t *slot, float *logits,
+                 uint32_t flags, void *stream);
+/* Model used by steps with VG_NAV_LEARNED (NULL detaches). The model must outlive its use. */
+int vg_geom_set_proposer(vg_geom *g, const vg_mlp *m);
 
 /* Same step with HOST arrays, the form the reference's own SoA navigator interface takes
  * (VNavigator::ComputeStepsAndPropagatedStates, VNavigator.h:128-132): inputs are copied to

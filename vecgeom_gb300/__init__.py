@@ -15,7 +15,8 @@ import os
 
 import numpy as np
 
-__all__ = ["Geometry", "load_library", "NAVSTATE_DTYPE", "PREC_FP64", "PREC_MIXED", "NAV_SORT", "NAV_QUEUE", "VGError",
+__all__ = ["Geometry", "load_library", "NAVSTATE_DTYPE", "PREC_FP64", "PREC_MIXED", "NAV_SORT", "NAV_QUEUE",
+           "NAV_LEARNED", "VGError",
            "kInside", "kSurface", "kOutside", "kInfLength", "IDENTITY_ROT", "ZERO_TRANS"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -25,6 +26,7 @@ PREC_FP64 = 0
 PREC_MIXED = 1
 NAV_SORT = 2   # visit tracks sorted by (logical volume, Morton cell); results unchanged
 NAV_QUEUE = 4  # persistent step kernel fed from a global work counter (with PREC_MIXED)
+NAV_LEARNED = 8  # explore the BVH subtree proposed by the attached model first (with PREC_MIXED)
 kInside, kSurface, kOutside = 1, 2, 3
 kInfLength = np.finfo(np.float64).max
 IDENTITY_ROT = (1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0)
@@ -95,9 +97,20 @@ _SIGS = {
                                                         _c_vp]),
     "vg_nav_sort_key_params": (ctypes.c_int, [_c_vp] * 5),
     "vg_nav_set_tuning": (ctypes.c_int, [_c_vp, ctypes.c_int32, ctypes.c_int32]),
+    "vg_mlp_create": (ctypes.c_int, [_c_vp, ctypes.c_uint64, ctypes.POINTER(_c_vp)]),
+    "vg_mlp_destroy": (None, [_c_vp]),
+    "vg_mlp_param_count": (ctypes.c_size_t, [_c_vp]),
+    "vg_mlp_get_params": (ctypes.c_int, [_c_vp, _c_vp, ctypes.c_size_t]),
+    "vg_mlp_set_params": (ctypes.c_int, [_c_vp, _c_vp, ctypes.c_size_t]),
+    "vg_learn_features": (ctypes.c_int, [_c_vp] * 8 + [ctypes.c_size_t, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "vg_mlp_gradients": (ctypes.c_int, [_c_vp] * 4 + [ctypes.c_size_t, _c_vp, _c_vp, _c_vp]),
+    "vg_mlp_train": (ctypes.c_int, [_c_vp] * 4 + [ctypes.c_size_t, ctypes.c_int32, ctypes.c_int32, ctypes.c_float,
+                                                  ctypes.c_uint64, _c_vp, _c_vp]),
+    "vg_mlp_infer": (ctypes.c_int, [_c_vp] * 3 + [ctypes.c_size_t, _c_vp, _c_vp, ctypes.c_uint32, _c_vp]),
+    "vg_geom_set_proposer": (ctypes.c_int, [_c_vp, _c_vp]),
     "vg_nav_compute_step_and_next_volume_noalloc": (ctypes.c_int, [_c_vp] + [_c_vp] * 11 +
                                                     [ctypes.c_size_t, ctypes.c_uint32, _c_vp]),
-    "vg_nav_compute_step_and_next_volume_ws": (ctypes.c_int, [_c_vp] + [_c_vp] * 11 +
+    "vg_nav_compute_step_and_next_volume_ws": (ctypes.c_int, [_c_vp] + [_c_vp] * 12 +
                                                [ctypes.c_size_t, ctypes.c_uint32, _c_vp, ctypes.c_size_t,
                                                 _c_vp]),
 }
@@ -295,13 +308,13 @@ class Geometry:
                                         _stream()), "vg_nav_locate_point")
 
     def compute_step_and_next_volume(self, x, y, z, dx, dy, dz, in_states, out_states, step, step_limit=None,
-                                     status=None, flags=PREC_FP64, workspace=None):
+                                     status=None, flags=PREC_FP64, workspace=None, nodes_visited=None):
         """One navigation step for n tracks (CUDA tensors). With NAV_SORT / NAV_QUEUE in
         `flags` a device workspace is needed: pass a uint8 CUDA tensor of at least
         step_workspace_bytes(n, flags) bytes, or leave it to the geometry, which keeps one
         cached workspace (calls running concurrently on different streams need their own)."""
         n = x.numel()
-        if flags & (NAV_SORT | NAV_QUEUE):
+        if flags & (NAV_SORT | NAV_QUEUE | NAV_LEARNED) or nodes_visited is not None:
             need = int(_lib.vg_nav_step_workspace_bytes(n, flags))
             if workspace is None:
                 ws = getattr(self, "_ws", None)
@@ -312,8 +325,8 @@ class Geometry:
                 workspace = ws
             _check(_lib.vg_nav_compute_step_and_next_volume_ws(
                 self._h, _ptr(x), _ptr(y), _ptr(z), _ptr(dx), _ptr(dy), _ptr(dz), _ptr(step_limit),
-                _ptr(in_states), _ptr(out_states), _ptr(step), _ptr(status), n, flags, _ptr(workspace),
-                workspace.numel(), _stream()), "vg_nav_compute_step_and_next_volume_ws")
+                _ptr(in_states), _ptr(out_states), _ptr(step), _ptr(status), _ptr(nodes_visited), n, flags,
+                _ptr(workspace), workspace.numel(), _stream()), "vg_nav_compute_step_and_next_volume_ws")
             return
         _check(_lib.vg_nav_compute_step_and_next_volume(
             self._h, _ptr(x), _ptr(y), _ptr(z), _ptr(dx), _ptr(dy), _ptr(dz), _ptr(step_limit), _ptr(in_states),

@@ -2,8 +2,13 @@
 #include "../../include/vecgeom_gb300.h"
 #include "geom.h"
 #include "launch.h"
+#include "learn.h"
+#include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <mutex>
+#include <random>
+#include <vector>
 #include <new>
 #include <string>
 
@@ -15,9 +20,30 @@ struct vg_geom {
   size_t staging_size = 0;
   vg::SortKeyParams sort{}; // set when the geometry is closed
   int queue_blocks = 1;     // resident blocks per SM of the work-queue step kernel (1 or 2)
+  const vg_mlp *proposer = nullptr; // learned proposal used by VG_NAV_LEARNED
   ~vg_geom()
   {
     if (staging) cudaFree(staging);
+  }
+};
+
+// Learned-proposal model: FP32 parameters + Adam state + BF16 inference copy, on the
+// device of the geometry it was created for.
+struct vg_mlp {
+  int n_lv       = 0;
+  size_t nparams = 0;
+  float *params = nullptr, *grads = nullptr, *m = nullptr, *v = nullptr, *loss = nullptr;
+  uint16_t *wbf = nullptr;
+  float *ws = nullptr;
+  size_t ws_floats = 0;
+  uint32_t *idx = nullptr;
+  size_t idx_n = 0;
+  int t = 0;
+  ~vg_mlp()
+  {
+    for (void *p : {(void *)params, (void *)grads, (void *)m, (void *)v, (void *)loss, (void *)wbf, (void *)ws,
+                    (void *)idx})
+      if (p) cudaFree(p);
   }
 };
 
@@ -33,6 +59,18 @@ int cuda_fail(cudaError_t e, const char *what)
 {
   return fail(VG_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
+template <class T>
+cudaError_t grow(T *&p, size_t &cap, size_t n)
+{
+  if (cap >= n && p) return cudaSuccess;
+  if (p) cudaFree(p);
+  p   = nullptr;
+  cap = 0;
+  const cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&p), (n ? n : 1) * sizeof(T));
+  if (e == cudaSuccess) cap = n;
+  return e;
+}
+
 bool built_ok(const vg_geom *g)
 {
   if (!g) {
@@ -76,12 +114,13 @@ vg::SortKeyParams sort_params(const vg::Geometry &geo, int cell_bits)
   return p;
 }
 
-constexpr uint32_t kNavFlags = VG_PREC_MIXED | VG_NAV_SORT | VG_NAV_QUEUE;
+constexpr uint32_t kNavFlags = VG_PREC_MIXED | VG_NAV_SORT | VG_NAV_QUEUE | VG_NAV_LEARNED;
 
 size_t step_workspace_bytes(size_t n, uint32_t flags)
 {
   size_t b = 0;
   if (flags & VG_NAV_QUEUE) b += 256;
+  if (flags & VG_NAV_LEARNED) b += (n + 255) & ~size_t(255);
   if (flags & VG_NAV_SORT) b += vg::nav_sort_workspace_bytes(n);
   return b;
 }
@@ -91,8 +130,9 @@ size_t step_workspace_bytes(size_t n, uint32_t flags)
 int step_launch(const vg_geom *g, vg::StepArgs a, uint32_t flags, void *ws, size_t ws_bytes, cudaStream_t s)
 {
   if (flags & ~kNavFlags) return fail(VG_EINVAL, "invalid navigation flags");
-  if ((flags & VG_NAV_QUEUE) && !(flags & VG_PREC_MIXED))
-    return fail(VG_EINVAL, "VG_NAV_QUEUE needs VG_PREC_MIXED");
+  if ((flags & (VG_NAV_QUEUE | VG_NAV_LEARNED)) && !(flags & VG_PREC_MIXED))
+    return fail(VG_EINVAL, "VG_NAV_QUEUE and VG_NAV_LEARNED need VG_PREC_MIXED");
+  if ((flags & VG_NAV_LEARNED) && !g->proposer) return fail(VG_ESTATE, "VG_NAV_LEARNED without a proposer model");
   if (a.n > 0xffffffffull) return fail(VG_EINVAL, "more than 2^32-1 tracks in one call");
   const size_t need = step_workspace_bytes(a.n, flags);
   if (need > 0 && (!ws || ws_bytes < need || (reinterpret_cast<uintptr_t>(ws) & 255u)))
@@ -103,12 +143,22 @@ int step_launch(const vg_geom *g, vg::StepArgs a, uint32_t flags, void *ws, size
     counter = reinterpret_cast<unsigned long long *>(w);
     w += 256;
   }
+  int8_t *slots = nullptr;
+  if (flags & VG_NAV_LEARNED) {
+    slots = reinterpret_cast<int8_t *>(w);
+    w += (a.n + 255) & ~size_t(255);
+  }
   cudaError_t e = cudaSuccess;
   if (flags & VG_NAV_SORT) {
     const uint32_t *order = nullptr;
     e = vg::launch_nav_sort(g->geo.dev, g->sort, a.x, a.y, a.z, a.in, a.n, w, &order, s);
     if (e != cudaSuccess) return cuda_fail(e, "track sort launch");
     a.order = order;
+  }
+  if (flags & VG_NAV_LEARNED) {
+    e = vg::launch_mlp_propose(g->geo.dev, a, g->proposer->wbf, slots, s);
+    if (e != cudaSuccess) return cuda_fail(e, "proposal launch");
+    a.proposal = slots;
   }
   if (flags & VG_NAV_QUEUE)
     e = vg::launch_step_mixed_queue(g->geo.dev, a, counter, g->queue_blocks, s);
@@ -367,8 +417,8 @@ int vg_nav_compute_step_and_next_volume(const vg_geom *g, const double *x, const
   if (g->geo.world < 0) return fail(VG_ESTATE, "geometry has no world volume");
   if (flags > VG_PREC_MIXED)
     return fail(VG_EINVAL, "invalid precision flags (scheduling flags need vg_nav_compute_step_and_next_volume_ws)");
-  return vg_nav_compute_step_and_next_volume_ws(g, x, y, z, dx, dy, dz, step_limit, in, out, step, status, n, flags,
-                                                nullptr, 0, stream);
+  return vg_nav_compute_step_and_next_volume_ws(g, x, y, z, dx, dy, dz, step_limit, in, out, step, status, nullptr, n,
+                                                flags, nullptr, 0, stream);
 }
 
 size_t vg_nav_step_workspace_bytes(size_t n, uint32_t flags) { return step_workspace_bytes(n, flags); }
@@ -376,15 +426,15 @@ size_t vg_nav_step_workspace_bytes(size_t n, uint32_t flags) { return step_works
 int vg_nav_compute_step_and_next_volume_ws(const vg_geom *g, const double *x, const double *y, const double *z,
                                            const double *dx, const double *dy, const double *dz,
                                            const double *step_limit, const vg_navstate *in, vg_navstate *out,
-                                           double *step, int32_t *status, size_t n, uint32_t flags, void *workspace,
-                                           size_t workspace_bytes, void *stream)
+                                           double *step, int32_t *status, int32_t *nodes_visited, size_t n,
+                                           uint32_t flags, void *workspace, size_t workspace_bytes, void *stream)
 {
   if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
   if (g->geo.world < 0) return fail(VG_ESTATE, "geometry has no world volume");
   if (n > 0 && (!x || !y || !z || !dx || !dy || !dz || !in || !out || !step))
     return fail(VG_EINVAL, "null input/output array");
   vg::StepArgs a{x,   y,   z,   dx,  dy,  dz, step_limit, reinterpret_cast<const vg::NavState *>(in),
-                 reinterpret_cast<vg::NavState *>(out), step, status, nullptr, n};
+                 reinterpret_cast<vg::NavState *>(out), step, status, nodes_visited, n};
   return step_launch(g, a, flags, workspace, workspace_bytes, (cudaStream_t)stream);
 }
 
@@ -513,6 +563,160 @@ int vg_nav_compute_step_and_next_volume_host(vg_geom *g, const double *x, const 
   if (e == cudaSuccess && status) e = cudaMemcpyAsync(status, dst, ni, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   return e == cudaSuccess ? VG_OK : cuda_fail(e, "device-to-host copy");
+}
+
+
+int vg_mlp_create(const vg_geom *g, uint64_t seed, vg_mlp **out)
+{
+  if (!out) return fail(VG_EINVAL, "null output handle");
+  *out = nullptr;
+  if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
+  vg_mlp *m = new (std::nothrow) vg_mlp;
+  if (!m) return fail(VG_ENOMEM, "out of host memory");
+  m->n_lv    = (int)g->geo.lvs.size();
+  m->nparams = vg::mlp_param_count(m->n_lv);
+  std::vector<float> h(m->nparams, 0.f);
+  std::mt19937_64 rng(seed);
+  auto fill = [&](int off, int n, float lim) {
+    std::uniform_real_distribution<float> u(-lim, lim);
+    for (int i = 0; i < n; ++i) h[off + i] = u(rng);
+  };
+  fill(vg::kMlpW1, vg::kMlpHid * vg::kMlpIn, std::sqrt(6.f / vg::kMlpIn));
+  fill(vg::kMlpW2, vg::kMlpHid * vg::kMlpHid, std::sqrt(6.f / vg::kMlpHid));
+  fill(vg::kMlpW3, vg::kMlpOut * vg::kMlpHid, std::sqrt(6.f / vg::kMlpHid));
+  fill(vg::kMlpE, m->n_lv * vg::kMlpEmb, 0.1f);
+  const size_t P = m->nparams;
+  cudaError_t e  = cudaMalloc(&m->params, P * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&m->grads, P * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&m->m, P * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&m->v, P * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&m->wbf, P * sizeof(uint16_t));
+  if (e == cudaSuccess) e = cudaMemset(m->m, 0, P * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemset(m->v, 0, P * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemcpy(m->params, h.data(), P * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = vg::launch_mlp_to_bf16(m->params, m->wbf, P, nullptr);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    delete m;
+    return cuda_fail(e, "model allocation");
+  }
+  *out = m;
+  return VG_OK;
+}
+
+void vg_mlp_destroy(vg_mlp *m) { delete m; }
+
+size_t vg_mlp_param_count(const vg_mlp *m) { return m ? m->nparams : 0; }
+
+int vg_mlp_get_params(const vg_mlp *m, float *host, size_t n)
+{
+  if (!m || !host || n < m->nparams) return fail(VG_EINVAL, "null model/output or buffer too small");
+  const cudaError_t e = cudaMemcpy(host, m->params, m->nparams * sizeof(float), cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? VG_OK : cuda_fail(e, "parameter copy");
+}
+
+int vg_mlp_set_params(vg_mlp *m, const float *host, size_t n)
+{
+  if (!m || !host || n != m->nparams) return fail(VG_EINVAL, "null model/input or wrong parameter count");
+  cudaError_t e = cudaMemcpy(m->params, host, n * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(m->m, 0, n * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemset(m->v, 0, n * sizeof(float));
+  if (e == cudaSuccess) e = vg::launch_mlp_to_bf16(m->params, m->wbf, n, nullptr);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  m->t = 0;
+  return e == cudaSuccess ? VG_OK : cuda_fail(e, "parameter upload");
+}
+
+int vg_learn_features(const vg_geom *g, const double *x, const double *y, const double *z, const double *dx,
+                      const double *dy, const double *dz, const vg_navstate *in, size_t n, float *feat, int32_t *lv,
+                      int8_t *label, void *stream)
+{
+  if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
+  if (n > 0 && (!x || !y || !z || !dx || !dy || !dz || !in || !feat || !lv))
+    return fail(VG_EINVAL, "null input/output array");
+  vg::StepArgs a{x, y, z, dx, dy, dz, nullptr, reinterpret_cast<const vg::NavState *>(in), nullptr, nullptr, nullptr,
+                 nullptr, n};
+  const cudaError_t e = vg::launch_learn_features(g->geo.dev, a, feat, lv, label, (cudaStream_t)stream);
+  return e == cudaSuccess ? VG_OK : cuda_fail(e, "feature kernel launch");
+}
+
+int vg_mlp_gradients(vg_mlp *m, const float *feat, const int32_t *lv, const int8_t *label, size_t n, float *grads,
+                     float *loss, void *stream)
+{
+  if (!m || !feat || !lv || !label || !grads || !loss) return fail(VG_EINVAL, "null argument");
+  if (n == 0 || n > (1u << 24)) return fail(VG_EINVAL, "n must be in [1, 2^24]");
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e  = grow(m->ws, m->ws_floats, vg::mlp_train_ws_floats((int)n));
+  if (e == cudaSuccess) e = grow(m->idx, m->idx_n, n);
+  if (e != cudaSuccess) return cuda_fail(e, "scratch allocation");
+  std::vector<uint32_t> id(n);
+  for (size_t i = 0; i < n; ++i) id[i] = (uint32_t)i;
+  e = cudaMemcpyAsync(m->idx, id.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = vg::launch_mlp_grad(m->params, m->n_lv, feat, lv, label, m->idx, (int)n, grads, loss, m->ws, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e == cudaSuccess ? VG_OK : cuda_fail(e, "gradient kernels");
+}
+
+int vg_mlp_train(vg_mlp *m, const float *feat, const int32_t *lv, const int8_t *label, size_t n, int32_t epochs,
+                 int32_t batch, float lr, uint64_t seed, float *epoch_loss, void *stream)
+{
+  if (!m || !feat || !lv || !label) return fail(VG_EINVAL, "null argument");
+  if (n == 0 || n > 0xffffffffull || epochs < 0 || batch < 1 || batch > 65536 || !(lr > 0))
+    return fail(VG_EINVAL, "invalid training parameters");
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t nbatch = (n + batch - 1) / batch;
+  size_t loss_cap     = 0;
+  float *losses       = nullptr;
+  cudaError_t e       = grow(m->ws, m->ws_floats, vg::mlp_train_ws_floats(batch));
+  if (e == cudaSuccess) e = grow(m->idx, m->idx_n, n);
+  if (e == cudaSuccess) e = grow(losses, loss_cap, nbatch);
+  if (e != cudaSuccess) {
+    if (losses) cudaFree(losses);
+    return cuda_fail(e, "scratch allocation");
+  }
+  std::vector<uint32_t> perm(n);
+  std::vector<float> hl(nbatch);
+  std::mt19937_64 rng(seed);
+  for (int ep = 0; ep < epochs && e == cudaSuccess; ++ep) {
+    for (size_t i = 0; i < n; ++i) perm[i] = (uint32_t)i;
+    std::shuffle(perm.begin(), perm.end(), rng);
+    e = cudaMemcpyAsync(m->idx, perm.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
+    for (size_t b = 0; b < nbatch && e == cudaSuccess; ++b) {
+      const size_t b0 = b * batch;
+      const int nb    = (int)std::min<size_t>(batch, n - b0);
+      e = vg::launch_mlp_grad(m->params, m->n_lv, feat, lv, label, m->idx + b0, nb, m->grads, losses + b, m->ws, s);
+      if (e == cudaSuccess)
+        e = vg::launch_mlp_adam(m->params, m->grads, m->m, m->v, m->nparams, lr, 0.9f, 0.999f, 1e-8f, ++m->t, s);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hl.data(), losses, nbatch * sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess && epoch_loss) {
+      double sum = 0.;
+      for (float v : hl) sum += v;
+      epoch_loss[ep] = (float)(sum / (double)n);
+    }
+  }
+  if (e == cudaSuccess) e = vg::launch_mlp_to_bf16(m->params, m->wbf, m->nparams, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(losses);
+  return e == cudaSuccess ? VG_OK : cuda_fail(e, "training");
+}
+
+int vg_mlp_infer(const vg_mlp *m, const float *feat, const int32_t *lv, size_t n, int8_t *slot, float *logits,
+                 uint32_t flags, void *stream)
+{
+  if (!m || (n > 0 && (!feat || !lv || !slot))) return fail(VG_EINVAL, "null argument");
+  if (flags != 0) return fail(VG_EINVAL, "unknown inference flags");
+  const cudaError_t e = vg::launch_mlp_infer_feat(m->wbf, m->n_lv, feat, lv, n, slot, logits, (cudaStream_t)stream);
+  return e == cudaSuccess ? VG_OK : cuda_fail(e, "inference kernel launch");
+}
+
+int vg_geom_set_proposer(vg_geom *g, const vg_mlp *m)
+{
+  if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
+  if (m && m->n_lv != (int)g->geo.lvs.size()) return fail(VG_EINVAL, "model was made for another geometry");
+  g->proposer = m;
+  return VG_OK;
 }
 
 } // extern "C"

@@ -1024,10 +1024,24 @@ int Geometry::upload(std::string &err)
   std::vector<double> node_box, prim_box(6 * daughters.size(), 0.);
   std::vector<NodeF> node_f;
   std::vector<float> prim_box_f(6 * daughters.size(), 0.f);
+  // Learned proposal: BVH depth per LV, and per daughter slot the depth-3 subtree (0..7,
+  // node 7 + k in breadth-first numbering) of the leaf that holds it; -1 where the leaf
+  // sits above depth 3 or the BVH is shallower.
+  std::vector<int32_t> lv_depth(lvs.size(), -1), dau_slot3(daughters.size(), -1);
   for (size_t l = 0; l < lvs.size(); ++l) {
     if (lv_bvh[l] < 0) continue;
     HostBVH const &b   = bvhs[lv_bvh[l]];
     const int32_t base = lv_dstart[l];
+    lv_depth[l]        = b.depth;
+    for (size_t i = 0; i < b.nchild.size(); ++i) {
+      if (b.nchild[i] <= 0) continue;
+      int depth = 0;
+      while ((size_t(2) << depth) - 1 <= i) ++depth; // nodes of depth d: [2^d - 1, 2^(d+1) - 1)
+      if (depth < 3) continue;
+      size_t a = i;
+      for (int d = depth; d > 3; --d) a = (a - 1) / 2;
+      for (int j = 0; j < b.nchild[i]; ++j) dau_slot3[base + b.prim[b.offset[i] + j]] = (int32_t)a - 7;
+    }
     bvh_node0.push_back((int32_t)node_nchild.size());
     bvh_prim0.push_back(base);
     for (size_t i = 0; i < b.nchild.size(); ++i) {
@@ -1055,6 +1069,7 @@ int Geometry::upload(std::string &err)
   const size_t o_dau = a.add(daughters), o_pvl = a.add(pv_lv), o_pvc = a.add(pv_child), o_pvx = a.add(pv_xf);
   const size_t o_bn0 = a.add(bvh_node0), o_bp0 = a.add(bvh_prim0), o_nnc = a.add(node_nchild);
   const size_t o_nof = a.add(node_offset), o_nbx = a.add(node_box), o_pid = a.add(prim_id);
+  const size_t o_lvdp = a.add(lv_depth), o_ds3 = a.add(dau_slot3);
   // FP32 bounding descriptors of the shapes (mixed-precision navigator): kind 0 = box
   // (lo, hi; flag 1 when the box is the shape itself), kind 1 = cylindrical shell (rmin,
   // rmax, zlo, zhi; flag 1 when the shell is the shape itself). Radii and z are rounded
@@ -1127,6 +1142,8 @@ int Geometry::upload(std::string &err)
   dev.prim_box_f  = reinterpret_cast<const float *>(P(o_pbf));
   dev.nav         = reinterpret_cast<const uint32_t *>(P(o_nav));
   dev.nav_words   = (uint32_t)nav_words;
+  dev.lv_depth    = reinterpret_cast<const int32_t *>(P(o_lvdp));
+  dev.dau_slot3   = reinterpret_cast<const int32_t *>(P(o_ds3));
   dev.shape_lbd   = reinterpret_cast<const float *>(P(o_lbd));
   dev.world_pv    = world;
   dev.max_depth   = max_depth;

@@ -25,7 +25,7 @@ __device__ __forceinline__ void step_one_mixed(const DevGeom &g, const mixed::Sh
   const double lim = a.limit ? __ldg(a.limit + t) : kInfLength;
   a.step[t] = mixed::compute_step_mixed(g, lbs, f64::V3{__ldg(a.x + t), __ldg(a.y + t), __ldg(a.z + t)},
                                         f64::V3{__ldg(a.dx + t), __ldg(a.dy + t), __ldg(a.dz + t)}, lim, s, o, st,
-                                        a.nvisited ? &nv : nullptr);
+                                        a.nvisited ? &nv : nullptr, a.proposal ? (int)__ldg(a.proposal + t) : -1);
   a.out[t] = o;
   if (a.status) a.status[t] = st;
   if (a.nvisited) a.nvisited[t] = nv;

@@ -21,6 +21,7 @@ struct StepArgs {
   int32_t *nvisited;
   size_t n;
   const uint32_t *order = nullptr; // optional visiting order (track indices); null: 0..n-1
+  const int8_t *proposal = nullptr; // optional learned first subtree per track (-1: none)
 };
 
 // Sort key of a track: logical volume of its state above 3*cell_bits Morton bits of its
@@ -55,6 +56,8 @@ cudaError_t launch_nav_sort(const DevGeom &g, const SortKeyParams &p, const doub
 // Fixed scratch of the no-allocation step entry point (noalloc.cu).
 size_t noalloc_max_tracks();
 cudaError_t noalloc_scratch(void **ptr, size_t *bytes);
+// Learned proposal per track (features + BF16 MLP, SIMT) into `slot` (n bytes).
+cudaError_t launch_mlp_propose(const DevGeom &g, const StepArgs &a, const uint16_t *wbf, int8_t *slot, cudaStream_t s);
 // flags: VG_PREC_FP64 (0) or VG_PREC_MIXED (1)
 inline cudaError_t launch_step(const DevGeom &g, const StepArgs &a, uint32_t flags, cudaStream_t s)
 {

@@ -167,7 +167,8 @@ __device__ __forceinline__ bool pv_contains_mixed(const DevGeom &g, const ShapeL
 constexpr int kCandBuf = 8;
 
 __device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, const ShapeLB *lbs, int lv, V3 lp, V3 ld,
-                                                     double &step, int last_pv, int &hit_pv, int *nvisited)
+                                                     double &step, int last_pv, int &hit_pv, int *nvisited,
+                                                     int first = -1)
 {
   const int b = g.lv_bvh[lv];
   if (b < 0) return kTrackOk;
@@ -211,7 +212,22 @@ __device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, const Sha
   int sp     = 1;
   stack[0]   = 0;
   int visits = 0;
+  // Learned proposal: explore depth-3 subtree `first` before the rest. When only the root
+  // is left on the stack the subtree is done: its candidates are evaluated now, which
+  // tightens the bound for the remaining traversal, and the subtree is not entered again.
+  unsigned skip = 0xffffffffu;
+  bool flushed  = true;
+  if (first >= 0) {
+    skip     = 7u + (unsigned)first;
+    stack[1] = skip;
+    sp       = 2;
+    flushed  = false;
+  }
   do {
+    if (!flushed && sp == 1) {
+      while (nc > 0) evaluate_first();
+      flushed = true;
+    }
     const unsigned id = stack[--sp];
     ++visits;
     const NodeF nd = g.node_f[node0 + id];
@@ -232,8 +248,8 @@ __device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, const Sha
       float tminL, tmaxL, tminR, tmaxR;
       slab_f(L.lo, L.hi, pf, inv, tminL, tmaxL);
       slab_f(R.lo, R.hi, pf, inv, tminR, tmaxR);
-      const bool tl = tminL <= tmaxL && tmaxL >= 0.f && tminL < bound;
-      const bool tr = tminR <= tmaxR && tmaxR >= 0.f && tminR < bound;
+      const bool tl = tminL <= tmaxL && tmaxL >= 0.f && tminL < bound && cl_ != skip;
+      const bool tr = tminR <= tmaxR && tmaxR >= 0.f && tminR < bound && cr_ != skip;
       if (sp + 2 > 32) {
         if (nvisited) *nvisited = visits;
         return kTrackErrStack;
@@ -373,7 +389,8 @@ __device__ __forceinline__ void relocate_force_different_mixed(const DevGeom &g,
 
 // ComputeStepAndPropagatedState with FP32 pruning (same control flow as f64::compute_step).
 __device__ __forceinline__ double compute_step_mixed(const DevGeom &g, const ShapeLB *lbs, V3 gp, V3 gd, double limit,
-                                                     NavState const &in, NavState &out, int &status, int *nvisited)
+                                                     NavState const &in, NavState &out, int &status, int *nvisited,
+                                                     int proposal = -1)
 {
   out    = in;
   status = kTrackOk;
@@ -391,7 +408,18 @@ __device__ __forceinline__ double compute_step_mixed(const DevGeom &g, const Sha
   int hit = -1;
   if (g.lv_nd[lv] > 0) {
     const int last = f64::nav_top(g, in.lastExited);
-    status         = check_daughters_mixed(g, lbs, lv, lp, ld, step, last, hit, nvisited);
+    int first = -1; // the proposal applies to BVHs of depth >= 3 whose depth-3 node is reachable
+    if (proposal >= 0 && proposal < 8 && g.lv_depth[lv] >= 3) {
+      const int node0 = g.bvh_node0[g.lv_bvh[lv]];
+      int n           = 7 + proposal;
+      bool ok         = true;
+      for (int d = 0; d < 3; ++d) {
+        n  = (n - 1) >> 1;
+        ok = ok && __ldg(&g.node_nchild[node0 + n]) < 0;
+      }
+      if (ok) first = proposal;
+    }
+    status = check_daughters_mixed(g, lbs, lv, lp, ld, step, last, hit, nvisited, first);
     if (status != kTrackOk) return 0.;
   }
   if (step == kInfLength && limit > 0.) {

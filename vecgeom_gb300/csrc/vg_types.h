@@ -171,6 +171,8 @@ struct DevGeom {
   const float *shape_lbd;     // FP32 bounding descriptor per shape (8 floats, see nav_mixed.cuh)
   const uint32_t *nav;        // NavIndex table
   uint32_t nav_words;
+  const int32_t *lv_depth;    // BVH depth per LV (-1: no BVH)
+  const int32_t *dau_slot3;   // depth-3 subtree (0..7) of each daughter slot's leaf, or -1
   int32_t world_pv;
   int32_t max_depth;
   int32_t n_pv;
