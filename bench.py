@@ -31,7 +31,9 @@ sys.path.insert(0, ROOT)
 
 STEP_BYTES = 24 + 24 + 12 + 12 + 8  # p, d, state in, state out, step (FP64 SoA + 12 B states)
 # name -> (precision | scheduling flags): 1 = VG_PREC_MIXED, 2 = VG_NAV_SORT, 4 = VG_NAV_QUEUE
-SCHEDULES = {"fp64": 0, "fp64_sort": 2, "mixed": 1, "mixed_sort": 3, "mixed_queue": 5, "mixed_sort_queue": 7}
+# 8 = VG_NAV_LEARNED (explore the BVH subtree proposed by the trained model first)
+SCHEDULES = {"fp64": 0, "fp64_sort": 2, "mixed": 1, "mixed_sort": 3, "mixed_queue": 5, "mixed_sort_queue": 7,
+             "mixed_sort_queue_learned": 15}
 
 
 def parse():
@@ -45,9 +47,12 @@ def parse():
     ap.add_argument("--primaries", type=int, default=1 << 20)
     ap.add_argument("--seed", type=int, default=0xC0FFEE)
     ap.add_argument("--cpu-sample", type=int, default=1 << 17)
-    ap.add_argument("--schedule", default="mixed_sort_queue", choices=sorted(SCHEDULES),
+    ap.add_argument("--schedule", default="mixed_sort_queue_learned", choices=sorted(SCHEDULES),
                     help="precision and scheduling of the headline measurement")
     ap.add_argument("--variants", type=int, default=1, help="also time the other schedules (1/0)")
+    ap.add_argument("--train-samples", type=int, default=10_000_000,
+                    help="plain-navigator steps sampled to train the learned proposal")
+    ap.add_argument("--train-epochs", type=int, default=3)
     ap.add_argument("--tune", type=int, default=1,
                     help="autotune sort-key bits / queue occupancy before timing (untimed; 1/0)")
     return ap.parse_args()
@@ -148,6 +153,36 @@ def make_inputs(args, geo, torch, dev):
     st = torch.empty(args.tracks * 12, dtype=torch.uint8, device=dev)
     geo.locate_point(t[0], t[1], t[2], st)
     return t, st, None
+
+
+def train_proposer(args, geo, torch, dev):
+    """Train the learned proposal on steps of the plain FP64 navigator (a separate sample of
+    the same transport histories, other seed), keep 10% of the hits for a held-out check,
+    attach the model. Untimed setup; its figures go into the result line."""
+    from vecgeom_gb300 import learned as L
+    from vecgeom_gb300 import workloads as W
+    t0 = time.perf_counter()
+    tt, tst, _ = W.sample_transport_steps(geo, args.train_samples, args.seed ^ 0x5EED5EED, torch, dev,
+                                          n_primaries=args.primaries)
+    feat, lv, lab = L.features(geo, *tt, tst)
+    del tt, tst
+    hits = ((lv >= 0) & (lab >= 0) & (lab <= 7)).nonzero().flatten()
+    gen = torch.Generator(device="cpu").manual_seed(args.seed & 0x7FFFFFFF)
+    hits = hits[torch.randperm(hits.numel(), generator=gen).to(dev)]
+    ntr = hits.numel() * 9 // 10
+    tr, te = hits[:ntr], hits[ntr:]
+    model = L.Proposer(geo, seed=args.seed)
+    losses = model.train(feat[tr].contiguous(), lv[tr].contiguous(), lab[tr].contiguous(), epochs=args.train_epochs,
+                         batch=8192, lr=3e-3, seed=args.seed)
+    pred = model.infer(feat[te].contiguous(), lv[te].contiguous())
+    acc = float((pred.to(torch.int64) == lab[te].to(torch.int64)).float().mean().item())
+    model.attach(geo)
+    info = {"train_steps_sampled": args.train_samples, "train_hit_samples": int(ntr), "epochs": args.train_epochs,
+            "epoch_loss": [round(x, 4) for x in losses], "holdout_top1": round(acc, 4),
+            "train_s": round(time.perf_counter() - t0, 2)}
+    del feat, lv, lab
+    torch.cuda.empty_cache()
+    return model, info
 
 
 def cpu_time_steps(args, host_inputs, host_states, nthreads, reps=3):
@@ -273,6 +308,16 @@ def main():
         return ms / args.steps
 
     head = SCHEDULES[args.schedule]
+    learned_info, model = None, None
+    if any(f & vg.NAV_LEARNED for f in SCHEDULES.values()) and (args.variants or head & vg.NAV_LEARNED):
+        model, learned_info = train_proposer(args, geo, torch, dev)
+        nodes = torch.empty(n, dtype=torch.int32, device=dev)
+        per = {}
+        for name in ("fp64", "mixed_sort_queue", "mixed_sort_queue_learned"):
+            geo.compute_step_and_next_volume(*t, st, out, step, status=status, flags=SCHEDULES[name],
+                                             nodes_visited=nodes)
+            per[name] = round(float(nodes.to(torch.float64).mean().item()), 3)
+        learned_info["bvh_nodes_visited_per_step"] = per
     tuning = None
     if args.tune and head & (vg.NAV_SORT | vg.NAV_QUEUE):
         from vecgeom_gb300.tune import autotune
@@ -313,7 +358,22 @@ def main():
         ms_sort = e0.elapsed_time(e1) / args.steps
         _, _, cb, lb = geo.sort_key_params()
         passes = (lb + 3 * cb + 7) // 8
-    ms_kernel = ms_head - ms_sort
+    # the learned proposal alone (features + MLP inference), also part of the headline step
+    ms_propose = 0.0
+    if head & vg.NAV_LEARNED:
+        from vecgeom_gb300 import learned as L
+        slot = torch.empty(n, dtype=torch.int8, device=dev)
+        for _ in range(args.warmup):
+            L.propose(geo, *t, st, out=slot)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(args.steps):
+            L.propose(geo, *t, st, out=slot)
+        e1.record()
+        torch.cuda.synchronize()
+        ms_propose = e0.elapsed_time(e1) / args.steps
+    ms_kernel = ms_head - ms_sort - ms_propose
 
     # e2e: host arrays through the host-pointer C-ABI entry point, copies inside the timed region
     hp = [a.cpu().pin_memory() for a in t]
@@ -351,17 +411,19 @@ def main():
         "speedup_vs_plain_fp64": ms_fp64 / ms_head,
         "ids_identical_to_fp64": ids_equal, "max_step_diff_vs_fp64_mm": step_err,
         "schedules_ms_per_step": variants, "all_schedules_identical_to_fp64": identical and ids_equal,
-        "sort_ms_per_step": ms_sort, "step_kernel_ms_per_step": ms_kernel,
+        "sort_ms_per_step": ms_sort, "propose_ms_per_step": ms_propose, "step_kernel_ms_per_step": ms_kernel,
         "tuning": None if tuning is None else {k: tuning[k] for k in ("cell_bits", "queue_blocks", "timings")},
+        "learned": learned_info,
         "e2e": {"value": ws * n / e2e_s, "unit": "nav steps/s", "h2d_bytes_per_step": n * (48 + 12),
                 "d2h_bytes_per_step": n * (12 + 8)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": None,
                      "kernel": "k_step_mixed_queue" if head & 4 else ("k_step_mixed" if head & 1 else "k_step"),
+                     "step_kernel_time_note": "sort and proposal kernels excluded" if head & 8 else "sort excluded",
                      "note": "algorithmic bytes %d B/step over the step kernel's time (sort excluded); the "
                              "kernel is issue/latency bound, not HBM-bound, see profiles/; peak %s"
                              % (STEP_BYTES, "of measured" if peaks else "of fallback")},
-        "gpu_launches": args.steps * (1 + ((1 + 3 * passes) if head & 2 else 0)),
+        "gpu_launches": args.steps * (1 + ((1 + 3 * passes) if head & 2 else 0) + (1 if head & 8 else 0)),
         "track_errors": n_err,
         "clocks": clocks.summary(),
     }

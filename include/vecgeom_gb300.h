@@ -260,11 +260,21 @@ int vg_mlp_gradients(vg_mlp *m, const float *feat, const int32_t *lv, const int8
 int vg_mlp_train(vg_mlp *m, const float *feat, const int32_t *lv, const int8_t *label, size_t n, int32_t epochs,
                  int32_t batch, float lr, uint64_t seed, float *epoch_loss, void *stream);
 /* Proposals from features: slot 0..7, or -1 for "none" / no proposal; logits (nullable,
- * n x 16 FP32). flags 0: SIMT kernel. */
+ * n x 16 FP32). flags 0: SIMT kernel; 1: tensor-core kernel (tcgen05, same semantics). */
 int vg_mlp_infer(const vg_mlp *m, const float *feat, const int32_t *lv, size_t n, int8_t *slot, float *logits,
                  uint32_t flags, void *stream);
 /* Model used by steps with VG_NAV_LEARNED (NULL detaches). The model must outlive its use. */
 int vg_geom_set_proposer(vg_geom *g, const vg_mlp *m);
+/* Kernel VG_NAV_LEARNED uses for its proposals: 1 tensor-core (default), 0 SIMT. */
+int vg_nav_set_proposal_kernel(vg_geom *g, int32_t tensor);
+/* Reads and clears the model's error flag: 1 if a tensor-core kernel's bounded wait for its
+ * MMA gave up (its proposals are then incomplete; step results are unaffected). */
+int vg_mlp_error(const vg_mlp *m, int32_t *error);
+/* The proposals VG_NAV_LEARNED computes inside the step (features + attached model), for
+ * n tracks: slot 0..7 or -1. flags 0: SIMT kernel; 1: tensor-core kernel. */
+int vg_nav_propose(const vg_geom *g, const double *x, const double *y, const double *z, const double *dx,
+                   const double *dy, const double *dz, const vg_navstate *in, size_t n, int8_t *slot, uint32_t flags,
+                   void *stream);
 
 /* Same step with HOST arrays, the form the reference's own SoA navigator interface takes
  * (VNavigator::ComputeStepsAndPropagatedStates, VNavigator.h:128-132): inputs are copied to

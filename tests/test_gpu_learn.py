@@ -134,3 +134,39 @@ def test_learned_step_identical_and_visits_fewer_nodes(cuda, barrel, trained):
     assert np.array_equal(s0, s1)
     held = te.cpu().numpy()
     assert n1[held].mean() < n0[held].mean(), (n1[held].mean(), n0[held].mean())
+
+
+def test_tensor_core_inference_matches_simt(cuda, barrel, trained):
+    """tcgen05 inference (BF16 operands in shared memory, FP32 accumulator in tensor memory)
+    against the SIMT kernel on the same features. The two sum in different orders, so a
+    hidden activation next to a BF16 rounding boundary can round to the neighbouring BF16
+    value (a 2^-8 relative step) and move the logits slightly: nearly all logits agree to
+    FP32 rounding, all within 1% of the logit range, and the proposals agree wherever the
+    top two logits are 0.1 apart."""
+    g, t, st, feat, lv, lab = barrel
+    model, _, te = trained
+    sel = te[: (1 << 15) + 77]  # a ragged last tile
+    f, l = feat[sel].contiguous(), lv[sel].contiguous()
+    s0, l0 = model.infer(f, l, logits=True)
+    s1, l1 = model.infer(f, l, logits=True, tensor=True)
+    assert model.error() == 0
+    a, b = l0.cpu().numpy()[:, :9], l1.cpu().numpy()[:, :9]
+    d = np.abs(a - b)
+    scale = max(1.0, np.abs(a).max())
+    assert (d <= 1e-5 * scale).mean() > 0.99, (d <= 1e-5 * scale).mean()
+    assert d.max() <= 1e-2 * scale, d.max()
+    srt = np.sort(a, axis=1)
+    clear = (srt[:, -1] - srt[:, -2]) > 0.1
+    assert (s0.cpu().numpy()[clear] == s1.cpu().numpy()[clear]).all()
+
+
+def test_tensor_core_propose_matches_simt(cuda, barrel, trained):
+    from vecgeom_gb300 import learned as L
+    g, t, st, feat, lv, lab = barrel
+    model, _, te = trained
+    model.attach(g)
+    p0 = L.propose(g, *t, st, tensor=False).cpu().numpy()
+    p1 = L.propose(g, *t, st, tensor=True).cpu().numpy()
+    assert model.error() == 0
+    assert (p0 == p1).mean() > 0.999
+    assert ((p0 == -1) == (lv.cpu().numpy() < 0)).all() or (p0[lv.cpu().numpy() < 0] == -1).all()

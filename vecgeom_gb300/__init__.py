@@ -108,6 +108,9 @@ _SIGS = {
                                                   ctypes.c_uint64, _c_vp, _c_vp]),
     "vg_mlp_infer": (ctypes.c_int, [_c_vp] * 3 + [ctypes.c_size_t, _c_vp, _c_vp, ctypes.c_uint32, _c_vp]),
     "vg_geom_set_proposer": (ctypes.c_int, [_c_vp, _c_vp]),
+    "vg_nav_set_proposal_kernel": (ctypes.c_int, [_c_vp, ctypes.c_int32]),
+    "vg_mlp_error": (ctypes.c_int, [_c_vp, _c_vp]),
+    "vg_nav_propose": (ctypes.c_int, [_c_vp] * 8 + [ctypes.c_size_t, _c_vp, ctypes.c_uint32, _c_vp]),
     "vg_nav_compute_step_and_next_volume_noalloc": (ctypes.c_int, [_c_vp] + [_c_vp] * 11 +
                                                     [ctypes.c_size_t, ctypes.c_uint32, _c_vp]),
     "vg_nav_compute_step_and_next_volume_ws": (ctypes.c_int, [_c_vp] + [_c_vp] * 12 +

@@ -21,6 +21,7 @@ struct vg_geom {
   vg::SortKeyParams sort{}; // set when the geometry is closed
   int queue_blocks = 1;     // resident blocks per SM of the work-queue step kernel (1 or 2)
   const vg_mlp *proposer = nullptr; // learned proposal used by VG_NAV_LEARNED
+  int propose_tensor      = 1;       // proposal kernel of VG_NAV_LEARNED: 1 tcgen05, 0 SIMT
   ~vg_geom()
   {
     if (staging) cudaFree(staging);
@@ -39,10 +40,11 @@ struct vg_mlp {
   uint32_t *idx = nullptr;
   size_t idx_n = 0;
   int t = 0;
+  int *err = nullptr; // set by a tensor-core kernel whose bounded MMA wait gave up
   ~vg_mlp()
   {
     for (void *p : {(void *)params, (void *)grads, (void *)m, (void *)v, (void *)loss, (void *)wbf, (void *)ws,
-                    (void *)idx})
+                    (void *)idx, (void *)err})
       if (p) cudaFree(p);
   }
 };
@@ -156,7 +158,8 @@ int step_launch(const vg_geom *g, vg::StepArgs a, uint32_t flags, void *ws, size
     a.order = order;
   }
   if (flags & VG_NAV_LEARNED) {
-    e = vg::launch_mlp_propose(g->geo.dev, a, g->proposer->wbf, slots, s);
+    e = g->propose_tensor ? vg::launch_mlp_propose_tc(g->geo.dev, a, g->proposer->wbf, slots, g->proposer->err, s)
+                          : vg::launch_mlp_propose(g->geo.dev, a, g->proposer->wbf, slots, s);
     if (e != cudaSuccess) return cuda_fail(e, "proposal launch");
     a.proposal = slots;
   }
@@ -591,6 +594,8 @@ int vg_mlp_create(const vg_geom *g, uint64_t seed, vg_mlp **out)
   if (e == cudaSuccess) e = cudaMalloc(&m->m, P * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&m->v, P * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&m->wbf, P * sizeof(uint16_t));
+  if (e == cudaSuccess) e = cudaMalloc(&m->err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(m->err, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(m->m, 0, P * sizeof(float));
   if (e == cudaSuccess) e = cudaMemset(m->v, 0, P * sizeof(float));
   if (e == cudaSuccess) e = cudaMemcpy(m->params, h.data(), P * sizeof(float), cudaMemcpyHostToDevice);
@@ -706,9 +711,44 @@ int vg_mlp_infer(const vg_mlp *m, const float *feat, const int32_t *lv, size_t n
                  uint32_t flags, void *stream)
 {
   if (!m || (n > 0 && (!feat || !lv || !slot))) return fail(VG_EINVAL, "null argument");
-  if (flags != 0) return fail(VG_EINVAL, "unknown inference flags");
-  const cudaError_t e = vg::launch_mlp_infer_feat(m->wbf, m->n_lv, feat, lv, n, slot, logits, (cudaStream_t)stream);
+  if (flags > 1) return fail(VG_EINVAL, "unknown inference flags");
+  const cudaError_t e =
+      flags ? vg::launch_mlp_infer_feat_tc(m->wbf, feat, lv, n, slot, logits, m->err, (cudaStream_t)stream)
+            : vg::launch_mlp_infer_feat(m->wbf, m->n_lv, feat, lv, n, slot, logits, (cudaStream_t)stream);
   return e == cudaSuccess ? VG_OK : cuda_fail(e, "inference kernel launch");
+}
+
+int vg_nav_propose(const vg_geom *g, const double *x, const double *y, const double *z, const double *dx,
+                   const double *dy, const double *dz, const vg_navstate *in, size_t n, int8_t *slot, uint32_t flags,
+                   void *stream)
+{
+  if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
+  if (!g->proposer) return fail(VG_ESTATE, "no proposer model attached");
+  if (flags > 1) return fail(VG_EINVAL, "unknown proposal flags");
+  if (n > 0 && (!x || !y || !z || !dx || !dy || !dz || !in || !slot)) return fail(VG_EINVAL, "null input/output array");
+  vg::StepArgs a{x, y, z, dx, dy, dz, nullptr, reinterpret_cast<const vg::NavState *>(in), nullptr, nullptr, nullptr,
+                 nullptr, n};
+  const cudaError_t e =
+      flags ? vg::launch_mlp_propose_tc(g->geo.dev, a, g->proposer->wbf, slot, g->proposer->err, (cudaStream_t)stream)
+            : vg::launch_mlp_propose(g->geo.dev, a, g->proposer->wbf, slot, (cudaStream_t)stream);
+  return e == cudaSuccess ? VG_OK : cuda_fail(e, "proposal launch");
+}
+
+int vg_nav_set_proposal_kernel(vg_geom *g, int32_t tensor)
+{
+  if (!g) return fail(VG_EINVAL, "null geometry handle");
+  g->propose_tensor = tensor ? 1 : 0;
+  return VG_OK;
+}
+
+int vg_mlp_error(const vg_mlp *m, int32_t *error)
+{
+  if (!m || !error) return fail(VG_EINVAL, "null argument");
+  int h = 0;
+  cudaError_t e = cudaMemcpy(&h, m->err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemset(m->err, 0, sizeof(int));
+  *error = h;
+  return e == cudaSuccess ? VG_OK : cuda_fail(e, "error flag read");
 }
 
 int vg_geom_set_proposer(vg_geom *g, const vg_mlp *m)

@@ -53,4 +53,11 @@ cudaError_t launch_mlp_to_bf16(const float *params, uint16_t *wbf, size_t n, cud
 cudaError_t launch_mlp_infer_feat(const uint16_t *wbf, int n_lv, const float *feat, const int32_t *lv, size_t n,
                                   int8_t *slot, float *logits, cudaStream_t s);
 
+// Tensor-core (tcgen05) versions: same semantics, `err` (device int) is set to 1 if a
+// bounded wait for an MMA gave up.
+cudaError_t launch_mlp_propose_tc(const DevGeom &g, const StepArgs &a, const uint16_t *wbf, int8_t *slot, int *err,
+                                  cudaStream_t s);
+cudaError_t launch_mlp_infer_feat_tc(const uint16_t *wbf, const float *feat, const int32_t *lv, size_t n, int8_t *slot,
+                                     float *logits, int *err, cudaStream_t s);
+
 } // namespace vg

@@ -78,15 +78,36 @@ class Proposer:
                                    out.ctypes.data, _stream()), "vg_mlp_train")
         return out[:epochs].tolist()
 
-    def infer(self, feat, lv, logits=False):
+    def infer(self, feat, lv, logits=False, tensor=False):
+        """Proposals from features; tensor=True uses the tcgen05 kernel."""
         import torch
         n = lv.numel()
         slot = torch.empty(n, dtype=torch.int8, device=feat.device)
         lg = torch.empty((n, 16), dtype=torch.float32, device=feat.device) if logits else None
-        _check(_lib().vg_mlp_infer(self._h, _ptr(feat), _ptr(lv), n, _ptr(slot), _ptr(lg), 0, _stream()),
-               "vg_mlp_infer")
+        _check(_lib().vg_mlp_infer(self._h, _ptr(feat), _ptr(lv), n, _ptr(slot), _ptr(lg), 1 if tensor else 0,
+                                   _stream()), "vg_mlp_infer")
         return (slot, lg) if logits else slot
 
-    def attach(self, geo):
+    def error(self):
+        """Reads and clears the tensor-core kernels' time-out flag."""
+        e = ctypes.c_int32()
+        _check(_lib().vg_mlp_error(self._h, ctypes.byref(e)), "vg_mlp_error")
+        return e.value
+
+    def attach(self, geo, tensor=True):
+        """Use this model for NAV_LEARNED steps on `geo` (tensor-core proposals by default)."""
         _check(_lib().vg_geom_set_proposer(geo._h, self._h), "vg_geom_set_proposer")
+        _check(_lib().vg_nav_set_proposal_kernel(geo._h, 1 if tensor else 0), "vg_nav_set_proposal_kernel")
         geo._proposer = self  # keep the model alive while attached
+
+
+def propose(geo, x, y, z, dx, dy, dz, states, tensor=True, out=None):
+    """Proposals of the model attached to `geo` for step inputs (what NAV_LEARNED uses);
+    tensor=True uses the tcgen05 kernel."""
+    flags = 1 if tensor else 0
+    import torch
+    n = x.numel()
+    slot = out if out is not None else torch.empty(n, dtype=torch.int8, device=x.device)
+    _check(_lib().vg_nav_propose(geo._h, _ptr(x), _ptr(y), _ptr(z), _ptr(dx), _ptr(dy), _ptr(dz), _ptr(states), n,
+                                 _ptr(slot), flags, _stream()), "vg_nav_propose")
+    return slot
