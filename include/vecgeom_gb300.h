@@ -212,6 +212,22 @@ int vg_nav_compute_step_and_next_volume_noalloc(const vg_geom *g, const double *
                                                 double *step, int32_t *status, size_t n, uint32_t flags,
                                                 void *stream);
 
+/* Transport stream (config-5 style): every track steps until it leaves the world or has made
+ * max_steps steps, as the reference's navigator would be driven by a straight-line
+ * transport loop (per step VNavigator::ComputeStepAndPropagatedState with no physics limit,
+ * then p += step * d). x/y/z and `states` are updated in place; nsteps[i] receives the
+ * steps of track i, status[i] a VG_TRACK_* give-up code (0 normally). Tracks below
+ * trace_tracks record each step's out-state and length at [i * max_steps + k] of
+ * trace_states / trace_steps. Each iteration steps all live tracks with one persistent
+ * kernel (refilled from a compacted list of survivors), after sorting them (VG_NAV_SORT)
+ * and computing proposals (VG_NAV_LEARNED) if asked. *iterations (nullable) receives the
+ * number of iterations. Synchronises the stream. No single reference counterpart. */
+size_t vg_nav_transport_workspace_bytes(size_t n, uint32_t flags);
+int vg_nav_transport(const vg_geom *g, double *x, double *y, double *z, const double *dx, const double *dy,
+                     const double *dz, vg_navstate *states, size_t n, int32_t max_steps, uint32_t flags,
+                     int32_t *nsteps, int32_t *status, vg_navstate *trace_states, double *trace_steps,
+                     size_t trace_tracks, int32_t *iterations, void *workspace, size_t workspace_bytes, void *stream);
+
 /* The visiting order VG_NAV_SORT uses, for callers that want to reorder their own track
  * arrays: key = logical-volume id of the state's top volume << 3*cell_bits | Morton code of
  * the position's cell (cell_bits per axis over the world box; cell = (float)(c - lo) * scale

@@ -93,6 +93,10 @@ _SIGS = {
     "vg_nav_compute_step_and_next_volume_host": (ctypes.c_int, [_c_vp] + [_c_vp] * 11 +
                                                  [ctypes.c_size_t, ctypes.c_uint32, _c_vp]),
     "vg_nav_step_workspace_bytes": (ctypes.c_size_t, [ctypes.c_size_t, ctypes.c_uint32]),
+    "vg_nav_transport_workspace_bytes": (ctypes.c_size_t, [ctypes.c_size_t, ctypes.c_uint32]),
+    "vg_nav_transport": (ctypes.c_int, [_c_vp] * 8 + [ctypes.c_size_t, ctypes.c_int32, ctypes.c_uint32, _c_vp, _c_vp,
+                                                      _c_vp, _c_vp, ctypes.c_size_t, _c_vp, _c_vp, ctypes.c_size_t,
+                                                      _c_vp]),
     "vg_nav_sort_tracks": (ctypes.c_int, [_c_vp] * 5 + [ctypes.c_size_t, _c_vp, _c_vp, _c_vp, ctypes.c_size_t,
                                                         _c_vp]),
     "vg_nav_sort_key_params": (ctypes.c_int, [_c_vp] * 5),
@@ -344,6 +348,25 @@ class Geometry:
             self._h, _ptr(x), _ptr(y), _ptr(z), _ptr(dx), _ptr(dy), _ptr(dz), _ptr(step_limit), _ptr(in_states),
             _ptr(out_states), _ptr(step), _ptr(status), x.numel(), flags, _stream()),
             "vg_nav_compute_step_and_next_volume_noalloc")
+
+    def transport(self, x, y, z, dx, dy, dz, states, max_steps=400, flags=PREC_FP64, trace_tracks=0):
+        """Transport stream: steps every track until it leaves the world or makes max_steps
+        steps. x, y, z and states (CUDA tensors) are updated in place. Returns (nsteps,
+        status, iterations, trace_states, trace_steps); the traces hold the first
+        `trace_tracks` tracks ([track, step] layout) or are None."""
+        import torch
+        n = x.numel()
+        dev = x.device
+        nsteps = torch.empty(n, dtype=torch.int32, device=dev)
+        status = torch.empty(n, dtype=torch.int32, device=dev)
+        tst = torch.zeros(max(trace_tracks, 0) * max_steps * 12, dtype=torch.uint8, device=dev) if trace_tracks else None
+        tsp = torch.zeros(max(trace_tracks, 0) * max_steps, dtype=torch.float64, device=dev) if trace_tracks else None
+        ws = torch.empty(max(int(_lib.vg_nav_transport_workspace_bytes(n, flags)), 256), dtype=torch.uint8, device=dev)
+        it = ctypes.c_int32()
+        _check(_lib.vg_nav_transport(self._h, _ptr(x), _ptr(y), _ptr(z), _ptr(dx), _ptr(dy), _ptr(dz), _ptr(states), n,
+                                     max_steps, flags, _ptr(nsteps), _ptr(status), _ptr(tst), _ptr(tsp), trace_tracks,
+                                     ctypes.byref(it), _ptr(ws), ws.numel(), _stream()), "vg_nav_transport")
+        return nsteps, status, it.value, tst, tsp
 
     def sort_tracks(self, x, y, z, in_states, order, keys=None, workspace=None):
         """The visiting order NAV_SORT uses: `order` (int32/uint32 CUDA tensor of n) gets the

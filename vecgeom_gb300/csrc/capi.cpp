@@ -441,6 +441,86 @@ int vg_nav_compute_step_and_next_volume_ws(const vg_geom *g, const double *x, co
   return step_launch(g, a, flags, workspace, workspace_bytes, (cudaStream_t)stream);
 }
 
+size_t transport_ws_bytes(size_t n, uint32_t flags)
+{
+  const size_t a = (n * sizeof(uint32_t) + 255) & ~size_t(255);
+  size_t b       = 2 * a + 3 * 256; // two track lists, survivor count, live count, queue counter
+  if (flags & VG_NAV_LEARNED) b += (n + 255) & ~size_t(255);
+  if (flags & VG_NAV_SORT) b += vg::nav_sort_workspace_bytes(n);
+  return b;
+}
+
+size_t vg_nav_transport_workspace_bytes(size_t n, uint32_t flags) { return transport_ws_bytes(n, flags); }
+
+int vg_nav_transport(const vg_geom *g, double *x, double *y, double *z, const double *dx, const double *dy,
+                     const double *dz, vg_navstate *states, size_t n, int32_t max_steps, uint32_t flags,
+                     int32_t *nsteps, int32_t *status, vg_navstate *trace_states, double *trace_steps,
+                     size_t trace_tracks, int32_t *iterations, void *workspace, size_t workspace_bytes, void *stream)
+{
+  if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
+  if (g->geo.world < 0) return fail(VG_ESTATE, "geometry has no world volume");
+  if (flags & ~kNavFlags) return fail(VG_EINVAL, "invalid navigation flags");
+  if ((flags & (VG_NAV_QUEUE | VG_NAV_LEARNED)) && !(flags & VG_PREC_MIXED))
+    return fail(VG_EINVAL, "VG_NAV_QUEUE and VG_NAV_LEARNED need VG_PREC_MIXED");
+  if ((flags & VG_NAV_LEARNED) && !g->proposer) return fail(VG_ESTATE, "VG_NAV_LEARNED without a proposer model");
+  if (n > 0xffffffffull || max_steps < 0) return fail(VG_EINVAL, "n or max_steps out of range");
+  if (n > 0 && (!x || !y || !z || !dx || !dy || !dz || !states || !nsteps || !status))
+    return fail(VG_EINVAL, "null input/output array");
+  if (trace_tracks > 0 && (!trace_states || !trace_steps)) return fail(VG_EINVAL, "null trace arrays");
+  if (trace_tracks > n) trace_tracks = n;
+  const size_t need = transport_ws_bytes(n, flags);
+  if (!workspace || workspace_bytes < need || (reinterpret_cast<uintptr_t>(workspace) & 255u))
+    return fail(VG_EINVAL, "workspace missing, too small or not 256-byte aligned");
+  if (iterations) *iterations = 0;
+  if (n == 0) return VG_OK;
+  cudaStream_t s   = (cudaStream_t)stream;
+  unsigned char *w = static_cast<unsigned char *>(workspace);
+  const size_t al  = (n * sizeof(uint32_t) + 255) & ~size_t(255);
+  uint32_t *list[2] = {reinterpret_cast<uint32_t *>(w), reinterpret_cast<uint32_t *>(w + al)};
+  unsigned int *cnt[2] = {reinterpret_cast<unsigned int *>(w + 2 * al), reinterpret_cast<unsigned int *>(w + 2 * al + 256)};
+  unsigned long long *counter = reinterpret_cast<unsigned long long *>(w + 2 * al + 512);
+  unsigned char *rest         = w + 2 * al + 768;
+  int8_t *slots               = nullptr;
+  if (flags & VG_NAV_LEARNED) {
+    slots = reinterpret_cast<int8_t *>(rest);
+    rest += (n + 255) & ~size_t(255);
+  }
+  vg::NavState *st = reinterpret_cast<vg::NavState *>(states);
+  cudaError_t e    = vg::launch_transport_init(st, n, nsteps, status, list[0], cnt[0], s);
+  int cur = 0, it = 0;
+  while (e == cudaSuccess && it < max_steps) {
+    unsigned int live = 0;
+    e = cudaMemcpyAsync(&live, cnt[cur], sizeof(live), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess || live == 0) break;
+    const uint32_t *order = list[cur];
+    if (flags & VG_NAV_SORT) {
+      const uint32_t *sorted = nullptr;
+      e = vg::launch_nav_sort(g->geo.dev, g->sort, x, y, z, st, live, rest, &sorted, s, list[cur]);
+      if (e != cudaSuccess) break;
+      order = sorted;
+    }
+    if (flags & VG_NAV_LEARNED) {
+      vg::StepArgs pa{x, y, z, dx, dy, dz, nullptr, st, nullptr, nullptr, nullptr, nullptr, live};
+      pa.order = order;
+      e = g->propose_tensor ? vg::launch_mlp_propose_tc(g->geo.dev, pa, g->proposer->wbf, slots, g->proposer->err, s)
+                            : vg::launch_mlp_propose(g->geo.dev, pa, g->proposer->wbf, slots, s);
+      if (e != cudaSuccess) break;
+    }
+    e = cudaMemsetAsync(cnt[cur ^ 1], 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) break;
+    vg::TransportArgs ta{x,       y,           z,       dx,          dy,         dz,    st,
+                         nsteps,  status,      (int)max_steps, reinterpret_cast<vg::NavState *>(trace_states),
+                         trace_steps, trace_tracks, order, live, list[cur ^ 1], cnt[cur ^ 1], slots};
+    e = vg::launch_transport_iter(g->geo.dev, ta, (flags & VG_PREC_MIXED) != 0, counter, g->queue_blocks, s);
+    cur ^= 1;
+    ++it;
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (iterations) *iterations = it;
+  return e == cudaSuccess ? VG_OK : cuda_fail(e, "transport stream");
+}
+
 int vg_nav_sort_tracks(const vg_geom *g, const double *x, const double *y, const double *z, const vg_navstate *in,
                        size_t n, uint32_t *order, uint32_t *keys, void *workspace, size_t workspace_bytes,
                        void *stream)

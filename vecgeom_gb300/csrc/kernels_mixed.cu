@@ -73,6 +73,81 @@ __global__ void __launch_bounds__(256) k_locate_mixed(const DevGeom g, const dou
   }
 }
 
+// Transport stream iteration (see TransportArgs): persistent warps take 32-entry chunks of
+// the visiting order from a global counter.
+template <bool Mixed, int MinBlocks>
+__global__ void __launch_bounds__(256, MinBlocks) k_transport_iter(const DevGeom g, const TransportArgs a,
+                                                                   unsigned long long *__restrict__ counter)
+{
+  const mixed::ShapeLB *lbs = reinterpret_cast<const mixed::ShapeLB *>(g.shape_lbd);
+  const int lane            = threadIdx.x & 31;
+  for (;;) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(counter, 32ull);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= a.n) break;
+    const size_t i = (size_t)base + lane;
+    if (i >= a.n) continue;
+    const size_t t = __ldg(a.list + i);
+    const NavState s = a.st[t];
+    NavState o;
+    int st = 0;
+    const f64::V3 p{a.x[t], a.y[t], a.z[t]}, d{__ldg(a.dx + t), __ldg(a.dy + t), __ldg(a.dz + t)};
+    const double step =
+        Mixed ? mixed::compute_step_mixed(g, lbs, p, d, kInfLength, s, o, st, nullptr,
+                                          a.proposal ? (int)__ldg(a.proposal + t) : -1)
+              : f64::compute_step(g, p, d, kInfLength, s, o, st, nullptr);
+    const int k = a.nsteps[t];
+    if (t < a.trace_n) {
+      a.trace_st[t * (size_t)a.max_steps + k]   = o;
+      a.trace_step[t * (size_t)a.max_steps + k] = step;
+    }
+    a.x[t]      = p.x + step * d.x; // OracleTransport: p = p + step * d
+    a.y[t]      = p.y + step * d.y;
+    a.z[t]      = p.z + step * d.z;
+    a.st[t]     = o;
+    a.nsteps[t] = k + 1;
+    if (st != kTrackOk) {
+      a.status[t] = st; // a track that gave up leaves the stream with its status
+      continue;
+    }
+    if (o.navInd != 0 && k + 1 < a.max_steps) a.next[atomicAdd(a.next_count, 1u)] = (uint32_t)t;
+  }
+}
+
+__global__ void k_transport_init(const NavState *__restrict__ st, size_t n, int32_t *__restrict__ nsteps,
+                                 int32_t *__restrict__ status, uint32_t *__restrict__ list,
+                                 unsigned int *__restrict__ count)
+{
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+    nsteps[t] = 0;
+    status[t] = 0;
+    if (st[t].navInd != 0) list[atomicAdd(count, 1u)] = (uint32_t)t;
+  }
+}
+
+template <bool Mixed, int MinBlocks>
+cudaError_t launch_transport(const DevGeom &g, const TransportArgs &a, unsigned long long *counter, cudaStream_t s)
+{
+  static int resident = 0;
+  if (resident == 0) {
+    int r = 0;
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_transport_iter<Mixed, MinBlocks>, 256, 0);
+    if (e != cudaSuccess) return e;
+    resident = r > 0 ? r : 1;
+  }
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  size_t blocks = (size_t)sms * resident, need = (a.n + 255) / 256;
+  if (blocks > need) blocks = need;
+  k_transport_iter<Mixed, MinBlocks><<<(unsigned)blocks, 256, 0, s>>>(g, a, counter);
+  return cudaGetLastError();
+}
+
 } // namespace
 
 cudaError_t launch_step_mixed(const DevGeom &g, const StepArgs &a, cudaStream_t s)
@@ -109,6 +184,25 @@ cudaError_t launch_step_mixed_queue(const DevGeom &g, const StepArgs &a, unsigne
 {
   if (a.n == 0) return cudaSuccess;
   return blocks_per_sm >= 2 ? launch_queue<2>(g, a, counter, s) : launch_queue<1>(g, a, counter, s);
+}
+
+cudaError_t launch_transport_iter(const DevGeom &g, const TransportArgs &a, bool mixed, unsigned long long *counter,
+                                  int blocks_per_sm, cudaStream_t s)
+{
+  if (a.n == 0) return cudaSuccess;
+  if (mixed)
+    return blocks_per_sm >= 2 ? launch_transport<true, 2>(g, a, counter, s) : launch_transport<true, 1>(g, a, counter, s);
+  return launch_transport<false, 1>(g, a, counter, s);
+}
+
+cudaError_t launch_transport_init(const NavState *st, size_t n, int32_t *nsteps, int32_t *status, uint32_t *list,
+                                  unsigned int *count, cudaStream_t s)
+{
+  if (n == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned int), s);
+  if (e != cudaSuccess) return e;
+  k_transport_init<<<grid_for(n, 256), 256, 0, s>>>(st, n, nsteps, status, list, count);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_locate_mixed(const DevGeom &g, const double *x, const double *y, const double *z, size_t n,

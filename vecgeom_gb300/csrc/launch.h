@@ -48,11 +48,35 @@ cudaError_t launch_locate_mixed(const DevGeom &g, const double *x, const double 
 size_t nav_sort_workspace_bytes(size_t n);
 int sort_key_bits(const SortKeyParams &p);
 const uint32_t *nav_sort_keys_of(const uint32_t *order, const void *ws, size_t n); // keys paired with `order`
-// Keys + stable radix sort of the n tracks; *order receives the sorted track indices
-// (inside the workspace).
+// Keys + stable radix sort of the n tracks (or of the n track ids in `list`); *order
+// receives the sorted track indices (inside the workspace).
 cudaError_t launch_nav_sort(const DevGeom &g, const SortKeyParams &p, const double *x, const double *y,
                             const double *z, const NavState *in, size_t n, void *ws, const uint32_t **order,
-                            cudaStream_t s);
+                            cudaStream_t s, const uint32_t *list = nullptr);
+
+// One iteration of the transport stream over the n track ids in `list` (visiting order):
+// step each track, move it (p += step d), store its new state in place, count the step,
+// record the trace of tracks < trace_n, and append the tracks still alive to `next`.
+struct TransportArgs {
+  double *x, *y, *z;
+  const double *dx, *dy, *dz;
+  NavState *st;
+  int32_t *nsteps;
+  int32_t *status;
+  int max_steps;
+  NavState *trace_st;
+  double *trace_step;
+  size_t trace_n;
+  const uint32_t *list;
+  size_t n;
+  uint32_t *next;
+  unsigned int *next_count;
+  const int8_t *proposal;
+};
+cudaError_t launch_transport_iter(const DevGeom &g, const TransportArgs &a, bool mixed, unsigned long long *counter,
+                                  int blocks_per_sm, cudaStream_t s);
+cudaError_t launch_transport_init(const NavState *st, size_t n, int32_t *nsteps, int32_t *status, uint32_t *list,
+                                  unsigned int *count, cudaStream_t s);
 // Fixed scratch of the no-allocation step entry point (noalloc.cu).
 size_t noalloc_max_tracks();
 cudaError_t noalloc_scratch(void **ptr, size_t *bytes);

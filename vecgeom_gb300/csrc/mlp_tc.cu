@@ -25,9 +25,10 @@ constexpr uint32_t kWaitLimit = 1u << 20; // try_wait polls; each may suspend br
 constexpr int kOffW1   = 0;                        // 64 x 80 bf16
 constexpr int kOffW2   = kOffW1 + 64 * 80 * 2;     // 64 x 64
 constexpr int kOffW3   = kOffW2 + 64 * 64 * 2;     // 16 x 64
-constexpr int kOffA    = 22528;                    // 128 x 80 (layer 1 input; layer 3 input 128 x 64)
-constexpr int kOffA2   = kOffA + kTile * 80 * 2;   // 128 x 64 (layer 2 input)
-constexpr int kOffBias = kOffA2 + kTile * 64 * 2;  // b1[64], b2[64], b3[16] as float
+// One operand buffer serves the three layers: each layer's input is written only after the
+// MMA that read the previous contents has completed (its barrier wait).
+constexpr int kOffA    = 22528;                    // 128 x 80 (layer 1), then 128 x 64 (layers 2, 3)
+constexpr int kOffBias = kOffA + kTile * 80 * 2;   // b1[64], b2[64], b3[16] as float
 constexpr int kOffBar  = kOffBias + 144 * 4;       // mbarrier (8 B) + tmem address (4 B)
 constexpr int kSmemBytes = kOffBar + 64;
 static_assert(kOffW3 + 16 * 64 * 2 <= kOffA, "weights overlap the operand tiles");
@@ -97,6 +98,15 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
 }
 
 __device__ __forceinline__ uint16_t tobf(float x) { return __bfloat16_as_ushort(__float2bfloat16_rn(x)); }
+__device__ __forceinline__ uint32_t pack2(uint16_t lo, uint16_t hi) { return (uint32_t)lo | ((uint32_t)hi << 16); }
+
+// 16-byte store of columns [8 kb, 8 kb + 8) of row r of a K-major operand with K columns:
+// one row segment of a core matrix, so a quarter warp (8 rows of one row group) writes
+// 128 contiguous bytes and the store is free of bank conflicts.
+__device__ __forceinline__ void store_chunk(unsigned char *base, int r, int kb, int K, uint4 v)
+{
+  *reinterpret_cast<uint4 *>(base + (r >> 3) * (K >> 3) * 128 + kb * 128 + (r & 7) * 16) = v;
+}
 __device__ __forceinline__ float frombf(uint16_t u) { return __bfloat162float(__ushort_as_bfloat16(u)); }
 
 // Feature source: computed from step inputs (Step = true) or read from a feature array.
@@ -142,7 +152,7 @@ __global__ void __launch_bounds__(kTile) k_mlp_propose_tc(const DevGeom g, const
   bool ok              = true;
 
   const uint32_t aW1 = smem_u32(sm + kOffW1), aW2 = smem_u32(sm + kOffW2), aW3 = smem_u32(sm + kOffW3);
-  const uint32_t aA = smem_u32(sm + kOffA), aA2 = smem_u32(sm + kOffA2);
+  const uint32_t aA = smem_u32(sm + kOffA);
   const size_t ntiles = (n + kTile - 1) / kTile;
   for (size_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     const size_t i = tile * kTile + t;
@@ -163,15 +173,22 @@ __global__ void __launch_bounds__(kTile) k_mlp_propose_tc(const DevGeom g, const
           for (int k = 0; k < kMlpIn; ++k) f[k] = feat[i * kMlpIn + k];
       }
     }
-    // layer-1 operand row
-    for (int k = 0; k < kMlpIn; ++k) {
-      uint16_t v = 0;
-      if (valid) {
-        const bool e = k >= kMlpEmbOff && k < kMlpEmbOff + kMlpEmb;
-        v            = e ? wbf[kMlpE + (size_t)lv * kMlpEmb + (k - kMlpEmbOff)] : tobf(f[k]);
-      }
-      *reinterpret_cast<uint16_t *>(sm + kOffA + kmajor_off(t, k, 80)) = v;
+    // layer-1 operand row: features rounded to BF16, embedding row of the volume
+    uint16_t x[kMlpIn];
+#pragma unroll
+    for (int k = 0; k < kMlpIn; ++k) x[k] = valid ? tobf(f[k]) : (uint16_t)0;
+    if (valid) {
+      const uint4 *er = reinterpret_cast<const uint4 *>(wbf + kMlpE + (size_t)lv * kMlpEmb);
+      const uint4 e0 = __ldg(er), e1 = __ldg(er + 1);
+      const uint32_t ew[8] = {e0.x, e0.y, e0.z, e0.w, e1.x, e1.y, e1.z, e1.w};
+#pragma unroll
+      for (int j = 0; j < kMlpEmb; ++j) x[kMlpEmbOff + j] = (uint16_t)(ew[j >> 1] >> (16 * (j & 1)));
     }
+#pragma unroll
+    for (int kb = 0; kb < kMlpIn / 8; ++kb)
+      store_chunk(sm + kOffA, t, kb, 80,
+                  make_uint4(pack2(x[8 * kb], x[8 * kb + 1]), pack2(x[8 * kb + 2], x[8 * kb + 3]),
+                             pack2(x[8 * kb + 4], x[8 * kb + 5]), pack2(x[8 * kb + 6], x[8 * kb + 7])));
     fence_async_smem();
     __syncthreads();
     if (t == 0) {
@@ -187,8 +204,14 @@ __global__ void __launch_bounds__(kTile) k_mlp_propose_tc(const DevGeom g, const
       for (int c = 0; c < 64; c += 16) {
         float v[16];
         tmem_ld16(tmem + lane0 + c, v);
-        for (int j = 0; j < 16; ++j)
-          *reinterpret_cast<uint16_t *>(sm + kOffA2 + kmajor_off(t, c + j, 64)) = tobf(fmaxf(v[j] + bias[c + j], 0.f));
+        uint16_t h[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) h[j] = tobf(fmaxf(v[j] + bias[c + j], 0.f));
+#pragma unroll
+        for (int q = 0; q < 2; ++q)
+          store_chunk(sm + kOffA, t, c / 8 + q, 64,
+                      make_uint4(pack2(h[8 * q], h[8 * q + 1]), pack2(h[8 * q + 2], h[8 * q + 3]),
+                                 pack2(h[8 * q + 4], h[8 * q + 5]), pack2(h[8 * q + 6], h[8 * q + 7])));
       }
     }
     tc_fence_before();
@@ -198,7 +221,7 @@ __global__ void __launch_bounds__(kTile) k_mlp_propose_tc(const DevGeom g, const
     if (t == 0) {
       tc_fence_after();
       for (int ks = 0; ks < 4; ++ks)
-        mma_bf16(tmem, smem_desc(aA2 + ks * 256, 64), smem_desc(aW2 + ks * 256, 64), idesc_bf16(128, 64), ks > 0);
+        mma_bf16(tmem, smem_desc(aA + ks * 256, 64), smem_desc(aW2 + ks * 256, 64), idesc_bf16(128, 64), ks > 0);
       mma_commit(barA);
     }
     ok = __all_sync(0xffffffffu, bar_wait(barA, parity)); // warp-uniform before tcgen05.ld
@@ -208,9 +231,14 @@ __global__ void __launch_bounds__(kTile) k_mlp_propose_tc(const DevGeom g, const
       for (int c = 0; c < 64; c += 16) {
         float v[16];
         tmem_ld16(tmem + lane0 + c, v);
-        for (int j = 0; j < 16; ++j)
-          *reinterpret_cast<uint16_t *>(sm + kOffA + kmajor_off(t, c + j, 64)) =
-              tobf(fmaxf(v[j] + bias[64 + c + j], 0.f));
+        uint16_t h[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) h[j] = tobf(fmaxf(v[j] + bias[64 + c + j], 0.f));
+#pragma unroll
+        for (int q = 0; q < 2; ++q)
+          store_chunk(sm + kOffA, t, c / 8 + q, 64,
+                      make_uint4(pack2(h[8 * q], h[8 * q + 1]), pack2(h[8 * q + 2], h[8 * q + 3]),
+                                 pack2(h[8 * q + 4], h[8 * q + 5]), pack2(h[8 * q + 6], h[8 * q + 7])));
       }
     }
     tc_fence_before();
@@ -263,11 +291,21 @@ cudaError_t launch_tc(const DevGeom &g, const StepArgs &a, const float *feat, co
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(k_mlp_propose_tc<Step>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          kSmemBytes);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_mlp_propose_tc<Step>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return e;
-    int r = 0;
-    e     = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_mlp_propose_tc<Step>, kTile, kSmemBytes);
+    // resident CTAs per SM from shared memory and registers (tensor memory: at most 6 x 64
+    // of the 512 columns)
+    cudaFuncAttributes fa{};
+    int dev0 = 0, smem_sm = 0;
+    e = cudaFuncGetAttributes(&fa, k_mlp_propose_tc<Step>);
+    if (e == cudaSuccess) e = cudaGetDevice(&dev0);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev0);
     if (e != cudaSuccess) return e;
-    blocks_per_sm = r > 0 ? (r > 4 ? 4 : r) : 1; // 4 x 64 tensor-memory columns per SM at most
+    const int by_smem = smem_sm / (kSmemBytes + 1024);
+    const int by_regs = 65536 / ((fa.numRegs > 0 ? fa.numRegs : 255) * kTile);
+    int r             = by_smem < by_regs ? by_smem : by_regs;
+    blocks_per_sm     = r < 1 ? 1 : (r > 6 ? 6 : r);
     configured    = 1;
   }
   int dev = 0, sms = 0;

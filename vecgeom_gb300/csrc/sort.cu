@@ -35,11 +35,13 @@ __device__ __forceinline__ uint32_t cell(double c, float lo, float scale, uint32
 
 __global__ void __launch_bounds__(256) k_sort_keys(const DevGeom g, const SortKeyParams p, const double *__restrict__ x,
                                                    const double *__restrict__ y, const double *__restrict__ z,
-                                                   const NavState *__restrict__ in, size_t n, uint32_t *__restrict__ keys)
+                                                   const NavState *__restrict__ in, const uint32_t *__restrict__ list,
+                                                   size_t n, uint32_t *__restrict__ keys)
 {
   const uint32_t maxc = (1u << p.cell_bits) - 1u;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+  for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+    const size_t i     = list ? (size_t)__ldg(list + j) : j;
     const uint32_t nav = in[i].navInd;
     uint32_t key       = 0xffffffffu; // outside the world or not a table node: last
     if (nav != 0u && nav + 2u < g.nav_words) {
@@ -52,7 +54,7 @@ __global__ void __launch_bounds__(256) k_sort_keys(const DevGeom g, const SortKe
         key = (lv << (3 * p.cell_bits)) | m;
       }
     }
-    keys[i] = key;
+    keys[j] = key;
   }
 }
 
@@ -128,7 +130,8 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_scatter(const uint32_t *__
                                                               const uint32_t *__restrict__ vin,
                                                               uint32_t *__restrict__ kout, uint32_t *__restrict__ vout,
                                                               size_t n, int shift, const uint32_t *__restrict__ hist,
-                                                              const uint32_t *__restrict__ totals, unsigned ntiles)
+                                                              const uint32_t *__restrict__ totals, unsigned ntiles,
+                                                              const uint32_t *__restrict__ list)
 {
   __shared__ uint32_t cnt[kSortWarps][256];
   __shared__ uint32_t wsum[33];
@@ -143,7 +146,7 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_scatter(const uint32_t *__
     const size_t i  = base + (size_t)r * 32 + lane;
     const bool ok   = i < n;
     key[r]          = ok ? __ldg(kin + i) : 0u;
-    val[r]          = ok ? (vin ? __ldg(vin + i) : (uint32_t)i) : 0u;
+    val[r]          = ok ? (vin ? __ldg(vin + i) : (list ? __ldg(list + i) : (uint32_t)i)) : 0u;
     const uint32_t d  = ok ? (key[r] >> shift) & 255u : 256u;
     const uint32_t pm = __match_any_sync(0xffffffffu, d);
     const uint32_t before = ok ? cnt[w][d] : 0u;
@@ -203,7 +206,7 @@ int sort_key_bits(const SortKeyParams &p) { return p.lv_bits + 3 * p.cell_bits; 
 
 cudaError_t launch_nav_sort(const DevGeom &g, const SortKeyParams &p, const double *x, const double *y,
                             const double *z, const NavState *in, size_t n, void *ws, const uint32_t **order,
-                            cudaStream_t s)
+                            cudaStream_t s, const uint32_t *list)
 {
   *order = nullptr;
   if (n == 0) return cudaSuccess;
@@ -214,7 +217,7 @@ cudaError_t launch_nav_sort(const DevGeom &g, const SortKeyParams &p, const doub
   uint32_t *v0 = reinterpret_cast<uint32_t *>(w + 2 * a), *v1 = reinterpret_cast<uint32_t *>(w + 3 * a);
   uint32_t *hist   = reinterpret_cast<uint32_t *>(w + 4 * a);
   uint32_t *totals = reinterpret_cast<uint32_t *>(w + 4 * a + align256(256 * (size_t)ntiles * sizeof(uint32_t)));
-  k_sort_keys<<<grid_for(n, 256), 256, 0, s>>>(g, p, x, y, z, in, n, k0);
+  k_sort_keys<<<grid_for(n, 256), 256, 0, s>>>(g, p, x, y, z, in, list, n, k0);
   // Digits above the key's width are all zero (invalid states carry all-ones keys, which
   // sort last within every pass), so only the passes that cover the key bits are run.
   const int bits   = sort_key_bits(p);
@@ -223,7 +226,7 @@ cudaError_t launch_nav_sort(const DevGeom &g, const SortKeyParams &p, const doub
   for (int ps = 0; ps < passes; ++ps) {
     k_radix_hist<<<ntiles, kSortBlock, 0, s>>>(kin, n, 8 * ps, hist, ntiles);
     k_scan_rows<<<256, 1024, 0, s>>>(hist, ntiles, totals);
-    k_radix_scatter<<<ntiles, kSortBlock, 0, s>>>(kin, vin, kout, vout, n, 8 * ps, hist, totals, ntiles);
+    k_radix_scatter<<<ntiles, kSortBlock, 0, s>>>(kin, vin, kout, vout, n, 8 * ps, hist, totals, ntiles, list);
     uint32_t *tk = kin;
     kin          = kout;
     kout         = tk;

@@ -269,6 +269,22 @@ def shape_points_mixed(lo, hi, n, seed, inside_fn, dist_out_fn, surface_band=1e-
     return (px[perm].copy(), py[perm].copy(), pz[perm].copy()), dirs
 
 
+def stream_tracks(n, seed, restart_fraction=0.2, world_half=(2000.0, 2000.0, 3000.0)):
+    """Config 5 track starts: primaries from the origin (pseudorapidity uniform in [-3, 3],
+    phi uniform), except a seeded `restart_fraction` that start at a point drawn uniformly in
+    the world box with an isotropic direction (tracks restarting inside random volumes)."""
+    (x, y, z), (dx, dy, dz) = primaries_eta_phi(n, seed)
+    g = rng(seed, 11)
+    restart = g.random(n) < restart_fraction
+    m = int(restart.sum())
+    for arr, h in zip((x, y, z), world_half):
+        arr[restart] = h * (2.0 * g.random(m) - 1.0)
+    rd = isotropic(rng(seed, 12), m)
+    for arr, v in zip((dx, dy, dz), rd):
+        arr[restart] = v
+    return (x, y, z), (dx, dy, dz), restart
+
+
 def sample_transport_steps(geo, n_samples, seed, torch, device, n_primaries=1 << 20, max_steps=200, flags=0):
     """Realistic step inputs: straight primaries from the origin (config-5 distribution) are
     transported on the GPU with the FP64 navigator; every (point, direction, state) before
