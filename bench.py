@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--train-samples", type=int, default=10_000_000,
                     help="plain-navigator steps sampled to train the learned proposal")
     ap.add_argument("--train-epochs", type=int, default=3)
+    ap.add_argument("--stream", type=int, default=1, help="also run the config-5 transport stream (1/0)")
+    ap.add_argument("--stream-tracks", type=int, default=1 << 20)
+    ap.add_argument("--shapes", type=int, default=1, help="also time the config-1/2 shape queries (1/0)")
     ap.add_argument("--tune", type=int, default=1,
                     help="autotune sort-key bits / queue occupancy before timing (untimed; 1/0)")
     return ap.parse_args()
@@ -183,6 +186,123 @@ def train_proposer(args, geo, torch, dev):
     del feat, lv, lab
     torch.cuda.empty_cache()
     return model, info
+
+
+def run_stream(args, geo, torch, dev, head, clocks_cls, local):
+    """Config 5: 2^20 tracks (80% primaries from the origin, 20% restarting at random points
+    of the world) transported until they leave the world, plain FP64 vs the headline
+    schedule; steps/s over all steps, identity of every track's step count, final state and
+    position; the oracle's transport loop on a bounded sample on the host cores."""
+    import vecgeom_gb300 as vg
+    from vecgeom_gb300 import workloads as W
+    n = args.stream_tracks
+    pts, dirs, restart = W.stream_tracks(n, args.seed)
+    res = {}
+    for name, flags in (("fp64", vg.PREC_FP64), ("headline", head)):
+        dv = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (*pts, *dirs)]
+        st = torch.empty(n * 12, dtype=torch.uint8, device=dev)
+        geo.locate_point(*dv[:3], st)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        nsteps, status, iters, _, _ = geo.transport(*dv, st, max_steps=400, flags=flags)
+        torch.cuda.synchronize()
+        sec = time.perf_counter() - t0
+        total = int(nsteps.to(torch.int64).sum().item())
+        res[name] = dict(seconds=sec, steps=total, iterations=iters, nsteps=nsteps.cpu().numpy(),
+                         final=st.cpu().numpy(), pos=[a.cpu().numpy() for a in dv[:3]],
+                         errors=int((status != 0).sum().item()))
+    a, b = res["fp64"], res["headline"]
+    identical = (np.array_equal(a["nsteps"], b["nsteps"]) and np.array_equal(a["final"], b["final"])
+                 and all(np.array_equal(p, q) for p, q in zip(a["pos"], b["pos"])))
+    out = {"tracks": n, "restart_fraction": round(float(restart.mean()), 4), "max_steps": 400,
+           "total_steps": a["steps"], "steps_per_track_max": int(a["nsteps"].max()),
+           "fp64": {"steps_per_s": a["steps"] / a["seconds"], "seconds": round(a["seconds"], 4)},
+           "headline": {"steps_per_s": b["steps"] / b["seconds"], "seconds": round(b["seconds"], 4),
+                        "iterations": b["iterations"]},
+           "speedup": a["seconds"] / b["seconds"], "identical_to_fp64": bool(identical),
+           "track_errors": a["errors"] + b["errors"]}
+    # the oracle's transport loop on the host cores over a bounded sample of the same tracks
+    from oracle.oracle import OracleGeometry
+    o = OracleGeometry()
+    builder(args.workload)(o)
+    m = min(4096, n)
+    sx = [np.ascontiguousarray(v[:m]) for v in (*pts, *dirs)]
+    ost, _ = o.locate(*sx[:3], nthreads=os.cpu_count() or 1)
+    ons, ofin, _, _, osec = o.transport(*sx, ost, 400, nthreads=os.cpu_count() or 1)
+    out["cpu_oracle"] = {"steps_per_s": float(ons.sum()) / osec, "cores": os.cpu_count() or 1,
+                         "sample_tracks": m, "steps_match_gpu": bool(np.array_equal(ons, a["nsteps"][:m]))}
+    return out
+
+
+QUERY_BYTES = {"inside": 28, "contains": 25, "distance_to_in": 56, "distance_to_out": 56, "safety_to_in": 32,
+               "safety_to_out": 32}  # FP64 SoA inputs + output per query (step_max not passed)
+
+
+def shape_rows(args, torch, dev, hbm_peak, reps=5):
+    """Config 1 (Box, Tube, Cone; 2^20 points uniform in the 1.2x extent box) and config 2
+    (2^22 points: thirds inside, outside, within 1e-6 mm of the surface) shape queries per
+    precision: queries/s, algorithmic GB/s and its fraction of the HBM peak, and for the
+    mixed path the largest difference to FP64 per query."""
+    import vecgeom_gb300 as vg
+    from vecgeom_gb300 import workloads as W
+    rows = []
+    cases = [(k, v, 1 << 20, "cfg1") for k, v in W.SHAPES_CFG1.items()] + \
+            [(k, v, 1 << 22, "cfg2") for k, v in W.SHAPES_CFG2.items()]
+    for name, (kind, params), n, cfg in cases:
+        g = vg.Geometry()
+        sid, pv = W.build_single_shape(g, kind, params)
+        lo, hi = g.shape_extent(sid)
+
+        def q_gpu(fn, dtype, *cols):
+            t = [torch.from_numpy(np.ascontiguousarray(c)).to(dev) for c in cols]
+            o = torch.empty(len(cols[0]), dtype=dtype, device=dev)
+            fn(pv, *t, o)
+            return o.cpu().numpy()
+
+        if cfg == "cfg1":
+            pts, dirs = W.shape_points_box(lo, hi, n, args.seed)
+        else:
+            pts, dirs = W.shape_points_mixed(lo, hi, n, args.seed, lambda *c: q_gpu(g.inside, torch.int32, *c),
+                                             lambda *c: q_gpu(g.distance_to_out, torch.float64, *c))
+        t = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (*pts, *dirs)]
+        outs = {"inside": torch.empty(n, dtype=torch.int32, device=dev),
+                "contains": torch.empty(n, dtype=torch.uint8, device=dev)}
+        for prec_name, prec in (("fp64", vg.PREC_FP64), ("mixed", vg.PREC_MIXED)):
+            for q in QUERY_BYTES:
+                o = outs.get(q, None)
+                if o is None:
+                    o = torch.empty(n, dtype=torch.float64, device=dev)
+                fn = getattr(g, q)
+                args_q = (pv, *t, o) if q.startswith("distance") else (pv, *t[:3], o)
+
+                def call():
+                    fn(*args_q, flags=prec)
+
+                for _ in range(2):
+                    call()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                torch.cuda.synchronize()
+                e0.record()
+                for _ in range(reps):
+                    call()
+                e1.record()
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1) / reps
+                gbs = QUERY_BYTES[q] * n / (ms * 1e-3) / 1e9
+                row = {"config": cfg, "shape": name, "query": q, "precision": prec_name, "n": n,
+                       "queries_per_s": n / (ms * 1e-3), "GB_per_s": gbs, "hbm_frac": gbs / hbm_peak}
+                if prec_name == "fp64":
+                    outs[(q, "ref")] = o.clone()
+                else:
+                    ref = outs[(q, "ref")]
+                    if o.dtype == torch.float64:
+                        both = (ref < 1e300) & (o < 1e300)
+                        row["max_abs_diff_vs_fp64"] = float((o - ref)[both].abs().max().item()) if bool(both.any()) else 0.0
+                        row["sentinel_mismatch"] = int(((ref >= 1e300) != (o >= 1e300)).sum().item())
+                    else:
+                        row["mismatch_vs_fp64"] = int((o != ref).sum().item())
+                rows.append(row)
+    return rows
 
 
 def cpu_time_steps(args, host_inputs, host_states, nthreads, reps=3):
@@ -375,6 +495,14 @@ def main():
         ms_propose = e0.elapsed_time(e1) / args.steps
     ms_kernel = ms_head - ms_sort - ms_propose
 
+    stream = run_stream(args, geo, torch, dev, head, ClockSampler, local) if (args.stream and rank == 0) else None
+    peaks_early = {}
+    try:
+        peaks_early = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    shapes = shape_rows(args, torch, dev, peaks_early.get("hbm_gbs", 6800.0)) if (args.shapes and rank == 0) else None
+
     # e2e: host arrays through the host-pointer C-ABI entry point, copies inside the timed region
     hp = [a.cpu().pin_memory() for a in t]
     hst = st.cpu().pin_memory()
@@ -414,6 +542,8 @@ def main():
         "sort_ms_per_step": ms_sort, "propose_ms_per_step": ms_propose, "step_kernel_ms_per_step": ms_kernel,
         "tuning": None if tuning is None else {k: tuning[k] for k in ("cell_bits", "queue_blocks", "timings")},
         "learned": learned_info,
+        "transport_stream": stream,
+        "shape_queries": shapes,
         "e2e": {"value": ws * n / e2e_s, "unit": "nav steps/s", "h2d_bytes_per_step": n * (48 + 12),
                 "d2h_bytes_per_step": n * (12 + 8)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",

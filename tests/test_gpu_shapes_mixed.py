@@ -1,0 +1,77 @@
+"""Mixed-precision shape queries (VG_PREC_MIXED on the placed SoA queries) against the FP64
+kernels on the same points: Inside, Contains, DistanceToIn and DistanceToOut are identical
+for every shape; safeties are identical except Box, whose FP32 safeties never exceed the
+FP64 value and stay within the stated bound 3 * 2^-23 (max|p| + max half-length) below it."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+QUERIES = ["inside", "contains", "distance_to_in", "distance_to_out", "safety_to_in", "safety_to_out"]
+
+
+def _run(torch, g, pv, pts, dirs, flags):
+    t = [torch.from_numpy(np.ascontiguousarray(a)).to("cuda:0") for a in (*pts, *dirs)]
+    n = len(pts[0])
+    res = {}
+    for q in QUERIES:
+        dt = torch.int32 if q == "inside" else (torch.uint8 if q == "contains" else torch.float64)
+        o = torch.empty(n, dtype=dt, device="cuda:0")
+        fn = getattr(g, q)
+        if q.startswith("distance"):
+            fn(pv, *t, o, flags=flags)
+        else:
+            fn(pv, *t[:3], o, flags=flags)
+        res[q] = o.cpu().numpy()
+    return res
+
+
+def _cases():
+    from vecgeom_gb300 import workloads as W
+    c = [(k, v) for k, v in W.SHAPES_CFG1.items()] + [(k, v) for k, v in W.SHAPES_CFG2.items()]
+    c.append(("polyhedron_phi", ("polyhedron", (0.3, 1.8, 5, (-100.0, 0.0, 0.0, 50.0), (0.0, 10.0, 20.0, 5.0),
+                                                (40.0, 60.0, 50.0, 30.0)))))
+    return c
+
+
+@pytest.mark.parametrize("case", _cases(), ids=lambda c: c[0])
+def test_mixed_shape_queries(cuda, case):
+    import vecgeom_gb300 as vg
+    from vecgeom_gb300 import workloads as W
+    name, (kind, params) = case
+    g = vg.Geometry()
+    s, pv = W.build_single_shape(g, kind, params)
+    lo, hi = g.shape_extent(s)
+    inside = lambda x, y, z: _run(cuda, g, pv, (x, y, z), (x, y, z), vg.PREC_FP64)["inside"]
+
+    def dout(x, y, z, dx, dy, dz):
+        return _run(cuda, g, pv, (x, y, z), (dx, dy, dz), vg.PREC_FP64)["distance_to_out"]
+
+    pts, dirs = W.shape_points_mixed(lo, hi, 3 * 8192, 123, inside, dout)
+    a = _run(cuda, g, pv, pts, dirs, vg.PREC_FP64)
+    b = _run(cuda, g, pv, pts, dirs, vg.PREC_MIXED)
+    for q in QUERIES[:4]:
+        assert np.array_equal(a[q], b[q]), (q, int((a[q] != b[q]).sum()))
+    if kind == "box":
+        p = np.abs(np.stack(pts))
+        bound = 3 * 2.0 ** -23 * (p.max(axis=0) + max(params))
+        for q in ("safety_to_in", "safety_to_out"):
+            assert (b[q] <= a[q]).all()
+            assert (a[q] - b[q] <= bound * 1.0001 + 1e-300).all(), q
+    else:
+        for q in ("safety_to_in", "safety_to_out"):
+            assert np.array_equal(a[q], b[q]), q
+
+
+def test_mixed_placed_transform(cuda):
+    """A rotated and translated tube: the FP32 guard works in the local frame."""
+    import vecgeom_gb300 as vg
+    from vecgeom_gb300 import workloads as W
+    g = vg.Geometry()
+    lv = g.add_logical_volume(g.add_tube(10.0, 20.0, 30.0, 0.3, 1.8))
+    pv = g.place(lv, (5.0, -7.0, 11.0), W.rot_z(0.7))
+    g.close()
+    (x, y, z), dirs = W.shape_points_box((-30.0, -35.0, -25.0), (40.0, 25.0, 45.0), 1 << 16, 9)
+    a = _run(cuda, g, pv, (x, y, z), dirs, vg.PREC_FP64)
+    b = _run(cuda, g, pv, (x, y, z), dirs, vg.PREC_MIXED)
+    for q in QUERIES:
+        assert np.array_equal(a[q], b[q]), q

@@ -194,10 +194,12 @@ int placed_query(const vg_geom *g, int32_t pv, int q, const double *x, const dou
   const int32_t type  = geo.shapes[shape].type;
   vg::QueryArgs a{x, y, z, dx, dy, dz, n, out};
   const bool composite = type == vg::kShapePolycone || type == vg::kShapePolyhedron || type == vg::kShapeBoolMinus;
-  const cudaError_t e  = composite ? vg::launch_shape_query_dyn_fp64(geo.dev, shape, geo.pvs[pv].xf.m, q, a,
-                                                                    (cudaStream_t)stream)
+  const bool mixed      = (flags & VG_PREC_MIXED) != 0;
+  const float *lbd      = mixed ? geo.shape_lbd_host.data() + 8 * (size_t)shape : nullptr;
+  const cudaError_t e   = composite ? vg::launch_shape_query_dyn_fp64(geo.dev, shape, geo.pvs[pv].xf.m, q, a,
+                                                                    (cudaStream_t)stream, mixed)
                                   : vg::launch_shape_query_fp64(type, geo.shape_rec(shape), geo.pvs[pv].xf.m, 1, q,
-                                                                a, (cudaStream_t)stream);
+                                                                a, (cudaStream_t)stream, lbd);
   if (e == cudaErrorNotSupported) return fail(VG_EINVAL, "shape type not supported by this query path");
   return e == cudaSuccess ? VG_OK : cuda_fail(e, "shape query launch");
 }

@@ -1109,6 +1109,7 @@ int Geometry::upload(std::string &err)
   }
   const size_t o_pbx = a.add(prim_box), o_nf = a.add(node_f), o_pbf = a.add(prim_box_f), o_nav = a.add(nav);
   const size_t o_lbd = a.add(lbd);
+  shape_lbd_host     = lbd;
 
   cudaError_t e = cudaGetDevice(&device);
   if (e == cudaSuccess) e = cudaMalloc(&arena, a.host.size() ? a.host.size() : 256);

@@ -58,6 +58,7 @@ public:
   std::vector<int32_t> lv_bvh;
   std::vector<uint32_t> nav;
   size_t nav_words = 0;
+  std::vector<float> shape_lbd_host; // FP32 shape descriptors (8 floats per shape) uploaded at close
 
   DevGeom dev{};
   void *arena      = nullptr;

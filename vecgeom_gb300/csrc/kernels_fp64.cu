@@ -3,6 +3,8 @@
 // one-thread-per-track navigation kernels. Compiled with --fmad=false.
 #include "launch.h"
 #include "nav_fp64.cuh"
+#include "shapes_mixed.cuh"
+#include <type_traits>
 
 namespace vg {
 namespace {
@@ -37,71 +39,106 @@ VG_OPS(TrdRec, trd)
 VG_OPS(TorusRec, torus)
 #undef VG_OPS
 
-// Q: 0 Inside, 1 Contains, 2 DistanceToIn, 3 DistanceToOut, 4 SafetyToIn, 5 SafetyToOut
-template <class R, int Q>
+// Q: 0 Inside, 1 Contains, 2 DistanceToIn, 3 DistanceToOut, 4 SafetyToIn, 5 SafetyToOut.
+// M: mixed precision (FP32 guard on the descriptor `lb`, see shapes_mixed.cuh).
+template <class R, int Q, bool M>
 __global__ void __launch_bounds__(256) k_shape_query(const R rec, const Xform xf, const int apply_xf,
-                                                     const double *__restrict__ x, const double *__restrict__ y,
-                                                     const double *__restrict__ z, const double *__restrict__ dx,
-                                                     const double *__restrict__ dy, const double *__restrict__ dz,
-                                                     size_t n, void *__restrict__ out)
+                                                     const mixed::ShapeLB lb, const double *__restrict__ x,
+                                                     const double *__restrict__ y, const double *__restrict__ z,
+                                                     const double *__restrict__ dx, const double *__restrict__ dy,
+                                                     const double *__restrict__ dz, size_t n, void *__restrict__ out)
 {
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     V3 p{__ldg(x + i), __ldg(y + i), __ldg(z + i)};
     const bool framed = apply_xf && (Q == 0 || Q == 1 || Q == 2 || Q == 4);
     if (framed) p = f64::to_local(xf, p);
-    if (Q == 0) static_cast<int32_t *>(out)[i] = ShapeOps<R>::inside(rec, p);
-    if (Q == 1) static_cast<uint8_t *>(out)[i] = ShapeOps<R>::contains(rec, p) ? 1 : 0;
+    if (Q == 0 || Q == 1) {
+      const int c = M ? mixed::lb_classify(lb, p) : 0;
+      if (Q == 0) static_cast<int32_t *>(out)[i] = c ? c : ShapeOps<R>::inside(rec, p);
+      if (Q == 1) static_cast<uint8_t *>(out)[i] = c ? (c == kInside ? 1 : 0) : (ShapeOps<R>::contains(rec, p) ? 1 : 0);
+    }
     if (Q == 2 || Q == 3) {
       V3 d{__ldg(dx + i), __ldg(dy + i), __ldg(dz + i)};
       if (framed) d = f64::rotate(xf, d);
-      static_cast<double *>(out)[i] = (Q == 2) ? ShapeOps<R>::dist_in(rec, p, d) : ShapeOps<R>::dist_out(rec, p, d);
+      double r;
+      if (Q == 2)
+        r = (M && mixed::lb_certain_miss(lb, p, d)) ? kInfLength : ShapeOps<R>::dist_in(rec, p, d);
+      else
+        r = ShapeOps<R>::dist_out(rec, p, d);
+      static_cast<double *>(out)[i] = r;
     }
-    if (Q == 4) static_cast<double *>(out)[i] = ShapeOps<R>::safety_in(rec, p);
-    if (Q == 5) static_cast<double *>(out)[i] = ShapeOps<R>::safety_out(rec, p);
+    if (Q == 4 || Q == 5) {
+      double r;
+      if (M && std::is_same<R, BoxRec>::value && mixed::in_range(mixed::f3(p)))
+        r = mixed::box_safety_mixed(reinterpret_cast<const BoxRec &>(rec), p, Q == 5);
+      else
+        r = (Q == 4) ? ShapeOps<R>::safety_in(rec, p) : ShapeOps<R>::safety_out(rec, p);
+      static_cast<double *>(out)[i] = r;
+    }
   }
 }
 
+template <class R, bool M>
+cudaError_t launch_typed_q(const R &rec, const Xform &xf, int apply_xf, const mixed::ShapeLB &lb, int q,
+                           const QueryArgs &a, cudaStream_t s)
+{
+  const int block     = 256;
+  const unsigned grid = grid_for(a.n, block);
+#define VG_Q(Q)                                                                                                   \
+  k_shape_query<R, Q, M><<<grid, block, 0, s>>>(rec, xf, apply_xf, lb, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out)
+  switch (q) {
+  case 0: VG_Q(0); break;
+  case 1: VG_Q(1); break;
+  case 2: VG_Q(2); break;
+  case 3: VG_Q(3); break;
+  case 4: VG_Q(4); break;
+  case 5: VG_Q(5); break;
+  default: return cudaErrorInvalidValue;
+  }
+#undef VG_Q
+  return cudaGetLastError();
+}
+
 template <class R>
-cudaError_t launch_typed(const double *recp, const Xform &xf, int apply_xf, int q, const QueryArgs &a,
-                         cudaStream_t s)
+cudaError_t launch_typed(const double *recp, const Xform &xf, int apply_xf, const float *lbd, int q,
+                         const QueryArgs &a, cudaStream_t s)
 {
   R rec;
   memcpy(&rec, recp, sizeof(R));
-  const int block = 256;
-  const unsigned grid = grid_for(a.n, block);
-  switch (q) {
-  case 0: k_shape_query<R, 0><<<grid, block, 0, s>>>(rec, xf, apply_xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out); break;
-  case 1: k_shape_query<R, 1><<<grid, block, 0, s>>>(rec, xf, apply_xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out); break;
-  case 2: k_shape_query<R, 2><<<grid, block, 0, s>>>(rec, xf, apply_xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out); break;
-  case 3: k_shape_query<R, 3><<<grid, block, 0, s>>>(rec, xf, apply_xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out); break;
-  case 4: k_shape_query<R, 4><<<grid, block, 0, s>>>(rec, xf, apply_xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out); break;
-  case 5: k_shape_query<R, 5><<<grid, block, 0, s>>>(rec, xf, apply_xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out); break;
-  default: return cudaErrorInvalidValue;
-  }
-  return cudaGetLastError();
+  if (!lbd) return launch_typed_q<R, false>(rec, xf, apply_xf, mixed::ShapeLB{}, q, a, s);
+  mixed::ShapeLB lb;
+  memcpy(&lb, lbd, sizeof(lb));
+  return launch_typed_q<R, true>(rec, xf, apply_xf, lb, q, a, s);
 }
 
 // Variable-length and composite shapes (polycone, polyhedron, boolean): the record stays in
 // the geometry arena and the query goes through the run-time dispatch.
-template <int Q>
+template <int Q, bool M>
 __global__ void __launch_bounds__(256) k_shape_query_dyn(const DevGeom g, const int shape, const Xform xf,
                                                          const double *__restrict__ x, const double *__restrict__ y,
                                                          const double *__restrict__ z, const double *__restrict__ dx,
                                                          const double *__restrict__ dy, const double *__restrict__ dz,
                                                          size_t n, void *__restrict__ out)
 {
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const mixed::ShapeLB lb = M ? reinterpret_cast<const mixed::ShapeLB *>(g.shape_lbd)[shape] : mixed::ShapeLB{};
+  const size_t stride     = (size_t)gridDim.x * blockDim.x;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     V3 p{__ldg(x + i), __ldg(y + i), __ldg(z + i)};
     const bool framed = (Q == 0 || Q == 1 || Q == 2 || Q == 4);
     if (framed) p = f64::to_local(xf, p);
-    if (Q == 0) static_cast<int32_t *>(out)[i] = f64::shape_inside(g, shape, p);
-    if (Q == 1) static_cast<uint8_t *>(out)[i] = f64::shape_contains(g, shape, p) ? 1 : 0;
+    if (Q == 0 || Q == 1) {
+      const int c = M ? mixed::lb_classify(lb, p) : 0;
+      if (Q == 0) static_cast<int32_t *>(out)[i] = c ? c : f64::shape_inside(g, shape, p);
+      if (Q == 1)
+        static_cast<uint8_t *>(out)[i] = c ? (c == kInside ? 1 : 0) : (f64::shape_contains(g, shape, p) ? 1 : 0);
+    }
     if (Q == 2 || Q == 3) {
       V3 d{__ldg(dx + i), __ldg(dy + i), __ldg(dz + i)};
       if (framed) d = f64::rotate(xf, d);
-      static_cast<double *>(out)[i] = (Q == 2) ? f64::shape_dist_in(g, shape, p, d) : f64::shape_dist_out(g, shape, p, d);
+      static_cast<double *>(out)[i] =
+          (Q == 2) ? ((M && mixed::lb_certain_miss(lb, p, d)) ? kInfLength : f64::shape_dist_in(g, shape, p, d))
+                   : f64::shape_dist_out(g, shape, p, d);
     }
     if (Q == 4) static_cast<double *>(out)[i] = f64::shape_safety_in(g, shape, p);
     if (Q == 5) static_cast<double *>(out)[i] = f64::shape_safety_out(g, shape, p);
@@ -143,25 +180,27 @@ __global__ void __launch_bounds__(256) k_step(const DevGeom g, const StepArgs a)
 } // namespace
 
 cudaError_t launch_shape_query_fp64(int type, const double *rec, const Xform &xf, int apply_xf, int q,
-                                    const QueryArgs &a, cudaStream_t s)
+                                    const QueryArgs &a, cudaStream_t s, const float *lbd)
 {
   if (a.n == 0) return cudaSuccess;
   switch (type) {
-  case kShapeBox: return launch_typed<BoxRec>(rec, xf, apply_xf, q, a, s);
-  case kShapeTube: return launch_typed<TubeRec>(rec, xf, apply_xf, q, a, s);
-  case kShapeCone: return launch_typed<ConeRec>(rec, xf, apply_xf, q, a, s);
-  case kShapeTrd: return launch_typed<TrdRec>(rec, xf, apply_xf, q, a, s);
-  case kShapeTorus2: return launch_typed<TorusRec>(rec, xf, apply_xf, q, a, s);
+  case kShapeBox: return launch_typed<BoxRec>(rec, xf, apply_xf, lbd, q, a, s);
+  case kShapeTube: return launch_typed<TubeRec>(rec, xf, apply_xf, lbd, q, a, s);
+  case kShapeCone: return launch_typed<ConeRec>(rec, xf, apply_xf, lbd, q, a, s);
+  case kShapeTrd: return launch_typed<TrdRec>(rec, xf, apply_xf, lbd, q, a, s);
+  case kShapeTorus2: return launch_typed<TorusRec>(rec, xf, apply_xf, lbd, q, a, s);
   default: return cudaErrorNotSupported;
   }
 }
 
 cudaError_t launch_shape_query_dyn_fp64(const DevGeom &g, int shape, const Xform &xf, int q, const QueryArgs &a,
-                                        cudaStream_t s)
+                                        cudaStream_t s, bool mixed)
 {
   if (a.n == 0) return cudaSuccess;
   const unsigned grid = grid_for(a.n, 256);
-#define VG_DYN(Q) k_shape_query_dyn<Q><<<grid, 256, 0, s>>>(g, shape, xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out)
+#define VG_DYN(Q)                                                                                                  \
+  (mixed ? k_shape_query_dyn<Q, true><<<grid, 256, 0, s>>>(g, shape, xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out) \
+         : k_shape_query_dyn<Q, false><<<grid, 256, 0, s>>>(g, shape, xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out))
   switch (q) {
   case 0: VG_DYN(0); break;
   case 1: VG_DYN(1); break;
