@@ -186,6 +186,17 @@ int vg_nav_compute_step_and_next_volume(const vg_geom *g, const double *x, const
                                         const double *step_limit, const vg_navstate *in, vg_navstate *out,
                                         double *step, int32_t *status, size_t n, uint32_t flags, void *stream);
 
+/* vg_nav_compute_step_and_safety replaces VNavigator::ComputeStepAndSafetyAndPropagatedState
+ * (VecGeom/navigation/VNavigator.h:1014-1064) with BVHSafetyEstimator
+ * (VecGeom/navigation/BVHSafetyEstimator.h:38-46): per track the isotropic safety of the
+ * input point in its volume (the mother's SafetyToOut, lowered by BVH::ComputeSafety over
+ * the daughters, VecGeom/base/BVH.h:172-209) and the step as above. The safety is FP64 in
+ * both precisions; `flags` (VG_PREC_FP64 / VG_PREC_MIXED) selects the step's arithmetic. */
+int vg_nav_compute_step_and_safety(const vg_geom *g, const double *x, const double *y, const double *z,
+                                   const double *dx, const double *dy, const double *dz, const double *step_limit,
+                                   const vg_navstate *in, vg_navstate *out, double *step, double *safety,
+                                   int32_t *status, size_t n, uint32_t flags, void *stream);
+
 /* The same step with scheduling flags. `workspace` is device memory of at least
  * vg_nav_step_workspace_bytes(n, flags) bytes (256-byte aligned), used by this call only
  * until the stream reaches its end; concurrent calls need separate workspaces. With

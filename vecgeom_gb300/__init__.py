@@ -93,6 +93,7 @@ _SIGS = {
     "vg_nav_compute_step_and_next_volume_host": (ctypes.c_int, [_c_vp] + [_c_vp] * 11 +
                                                  [ctypes.c_size_t, ctypes.c_uint32, _c_vp]),
     "vg_nav_step_workspace_bytes": (ctypes.c_size_t, [ctypes.c_size_t, ctypes.c_uint32]),
+    "vg_nav_compute_step_and_safety": (ctypes.c_int, [_c_vp] * 13 + [ctypes.c_size_t, ctypes.c_uint32, _c_vp]),
     "vg_nav_transport_workspace_bytes": (ctypes.c_size_t, [ctypes.c_size_t, ctypes.c_uint32]),
     "vg_nav_transport": (ctypes.c_int, [_c_vp] * 8 + [ctypes.c_size_t, ctypes.c_int32, ctypes.c_uint32, _c_vp, _c_vp,
                                                       _c_vp, _c_vp, ctypes.c_size_t, _c_vp, _c_vp, ctypes.c_size_t,
@@ -348,6 +349,14 @@ class Geometry:
             self._h, _ptr(x), _ptr(y), _ptr(z), _ptr(dx), _ptr(dy), _ptr(dz), _ptr(step_limit), _ptr(in_states),
             _ptr(out_states), _ptr(step), _ptr(status), x.numel(), flags, _stream()),
             "vg_nav_compute_step_and_next_volume_noalloc")
+
+    def compute_step_and_safety(self, x, y, z, dx, dy, dz, in_states, out_states, step, safety, step_limit=None,
+                                status=None, flags=PREC_FP64):
+        """Step (as compute_step_and_next_volume) plus the FP64 safety of each input point."""
+        _check(_lib.vg_nav_compute_step_and_safety(
+            self._h, _ptr(x), _ptr(y), _ptr(z), _ptr(dx), _ptr(dy), _ptr(dz), _ptr(step_limit), _ptr(in_states),
+            _ptr(out_states), _ptr(step), _ptr(safety), _ptr(status), x.numel(), flags, _stream()),
+            "vg_nav_compute_step_and_safety")
 
     def transport(self, x, y, z, dx, dy, dz, states, max_steps=400, flags=PREC_FP64, trace_tracks=0):
         """Transport stream: steps every track until it leaves the world or makes max_steps

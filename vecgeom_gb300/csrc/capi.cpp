@@ -597,6 +597,22 @@ int vg_nav_compute_step_and_next_volume_noalloc(const vg_geom *g, const double *
   return step_launch(g, a, flags, ws, bytes, (cudaStream_t)stream);
 }
 
+int vg_nav_compute_step_and_safety(const vg_geom *g, const double *x, const double *y, const double *z,
+                                   const double *dx, const double *dy, const double *dz, const double *step_limit,
+                                   const vg_navstate *in, vg_navstate *out, double *step, double *safety,
+                                   int32_t *status, size_t n, uint32_t flags, void *stream)
+{
+  if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
+  if (g->geo.world < 0) return fail(VG_ESTATE, "geometry has no world volume");
+  if (flags > VG_PREC_MIXED) return fail(VG_EINVAL, "invalid precision flags");
+  if (n > 0 && (!x || !y || !z || !dx || !dy || !dz || !in || !out || !step || !safety))
+    return fail(VG_EINVAL, "null input/output array");
+  vg::StepArgs a{x,   y,   z,   dx,  dy,  dz, step_limit, reinterpret_cast<const vg::NavState *>(in),
+                 reinterpret_cast<vg::NavState *>(out), step, status, nullptr, n};
+  const cudaError_t e = vg::launch_step_safety(g->geo.dev, a, safety, flags & VG_PREC_MIXED, (cudaStream_t)stream);
+  return e == cudaSuccess ? VG_OK : cuda_fail(e, "step-and-safety launch");
+}
+
 int vg_nav_compute_step_and_next_volume_host(vg_geom *g, const double *x, const double *y, const double *z,
                                              const double *dx, const double *dy, const double *dz,
                                              const double *step_limit, const vg_navstate *in, vg_navstate *out,

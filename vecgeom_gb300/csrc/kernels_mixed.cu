@@ -73,6 +73,28 @@ __global__ void __launch_bounds__(256) k_locate_mixed(const DevGeom g, const dou
   }
 }
 
+// ComputeStepAndSafetyAndPropagatedState: the safety of the input state (FP64), then the step
+// (FP64 or mixed). A give-up in either part sets the track's status.
+template <bool Mixed>
+__global__ void __launch_bounds__(256) k_step_safety(const DevGeom g, const StepArgs a, double *__restrict__ safety)
+{
+  const mixed::ShapeLB *lbs = reinterpret_cast<const mixed::ShapeLB *>(g.shape_lbd);
+  const size_t stride       = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+    const NavState s = a.in[i];
+    const f64::V3 p{__ldg(a.x + i), __ldg(a.y + i), __ldg(a.z + i)}, d{__ldg(a.dx + i), __ldg(a.dy + i),
+                                                                       __ldg(a.dz + i)};
+    int st_saf = kTrackOk, st = kTrackOk;
+    safety[i] = f64::safety_of_state(g, p, s.navInd, st_saf);
+    NavState o;
+    const double lim = a.limit ? __ldg(a.limit + i) : kInfLength;
+    a.step[i] = Mixed ? mixed::compute_step_mixed(g, lbs, p, d, lim, s, o, st, nullptr)
+                      : f64::compute_step(g, p, d, lim, s, o, st, nullptr);
+    a.out[i] = o;
+    if (a.status) a.status[i] = st != kTrackOk ? st : st_saf;
+  }
+}
+
 // Transport stream iteration (see TransportArgs): persistent warps take 32-entry chunks of
 // the visiting order from a global counter.
 template <bool Mixed, int MinBlocks>
@@ -184,6 +206,16 @@ cudaError_t launch_step_mixed_queue(const DevGeom &g, const StepArgs &a, unsigne
 {
   if (a.n == 0) return cudaSuccess;
   return blocks_per_sm >= 2 ? launch_queue<2>(g, a, counter, s) : launch_queue<1>(g, a, counter, s);
+}
+
+cudaError_t launch_step_safety(const DevGeom &g, const StepArgs &a, double *safety, bool mixed, cudaStream_t s)
+{
+  if (a.n == 0) return cudaSuccess;
+  if (mixed)
+    k_step_safety<true><<<grid_for(a.n, 256), 256, 0, s>>>(g, a, safety);
+  else
+    k_step_safety<false><<<grid_for(a.n, 256), 256, 0, s>>>(g, a, safety);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_transport_iter(const DevGeom &g, const TransportArgs &a, bool mixed, unsigned long long *counter,

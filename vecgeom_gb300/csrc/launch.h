@@ -82,6 +82,8 @@ cudaError_t launch_transport_init(const NavState *st, size_t n, int32_t *nsteps,
 // Fixed scratch of the no-allocation step entry point (noalloc.cu).
 size_t noalloc_max_tracks();
 cudaError_t noalloc_scratch(void **ptr, size_t *bytes);
+// Step + safety of the input state (ComputeStepAndSafetyAndPropagatedState).
+cudaError_t launch_step_safety(const DevGeom &g, const StepArgs &a, double *safety, bool mixed, cudaStream_t s);
 // Learned proposal per track (features + BF16 MLP, SIMT) into `slot` (n bytes).
 cudaError_t launch_mlp_propose(const DevGeom &g, const StepArgs &a, const uint16_t *wbf, int8_t *slot, cudaStream_t s);
 // flags: VG_PREC_FP64 (0) or VG_PREC_MIXED (1)

@@ -241,6 +241,78 @@ __device__ __forceinline__ void relocate_force_different(const DevGeom &g, V3 lp
   }
 }
 
+// AABB::Safety (VecGeom/base/AABB.h:81): max over axes of |p - centre| - half size, with
+// centre = 0.5 (max + min) and half size = 0.5 (max - min) as the reference forms them.
+__device__ __forceinline__ double aabb_safety(const double *b, V3 p)
+{
+  const double cx = 0.5 * (__ldg(b + 3) + __ldg(b)), cy = 0.5 * (__ldg(b + 4) + __ldg(b + 1));
+  const double cz = 0.5 * (__ldg(b + 5) + __ldg(b + 2));
+  const double hx = 0.5 * (__ldg(b + 3) - __ldg(b)), hy = 0.5 * (__ldg(b + 4) - __ldg(b + 1));
+  const double hz = 0.5 * (__ldg(b + 5) - __ldg(b + 2));
+  return max3(fabs(p.x - cx) - hx, fabs(p.y - cy) - hy, fabs(p.z - cz) - hz);
+}
+
+// BVH::ComputeSafety (VecGeom/base/BVH.h:172-209): minimum of `safety` and the SafetyToIn of
+// every daughter whose box is closer than the current minimum.
+__device__ __forceinline__ double bvh_compute_safety(const DevGeom &g, int lv, V3 lp, double safety, int &status)
+{
+  const int b     = g.lv_bvh[lv];
+  const int node0 = g.bvh_node0[b];
+  const int dbase = g.lv_dstart[lv];
+  unsigned stack[32];
+  int sp   = 1;
+  stack[0] = 0;
+  do {
+    const unsigned id = stack[--sp];
+    const int nch     = __ldg(&g.node_nchild[node0 + id]);
+    if (nch >= 0) {
+      const int off = __ldg(&g.node_offset[node0 + id]);
+      for (int i = 0; i < nch; ++i) {
+        const int prim = __ldg(&g.prim_id[off + i]);
+        if (aabb_safety(g.prim_box + 6 * (size_t)(dbase + prim), lp) < safety) {
+          const int vol     = __ldg(&g.daughters[dbase + prim]);
+          const double dist = shape_safety_in(g, pv_shape(g, vol), to_local(g.pv_xf[vol], lp));
+          if (dist < safety) safety = dist;
+        }
+      }
+    } else {
+      if (sp + 2 > 32) {
+        status = kTrackErrStack;
+        return safety;
+      }
+      const unsigned cl = 2 * id + 1, cr = 2 * id + 2;
+      const double sl = aabb_safety(g.node_box + 6 * (size_t)(node0 + cl), lp);
+      const double sr = aabb_safety(g.node_box + 6 * (size_t)(node0 + cr), lp);
+      const bool tl = sl < safety, tr = sr < safety;
+      if (sr < sl) {
+        if (tr) stack[sp++] = cr;
+        if (tl) stack[sp++] = cl;
+      } else {
+        if (tl) stack[sp++] = cl;
+        if (tr) stack[sp++] = cr;
+      }
+    }
+  } while (sp > 0);
+  return safety;
+}
+
+// Safety part of ComputeStepAndSafetyAndPropagatedState (VNavigator.h:1014-1064) with
+// BVHSafetyEstimator::ComputeSafetyForLocalPoint (BVHSafetyEstimator.h:38-46): the mother's
+// SafetyToOut, lowered by the daughters' SafetyToIn when positive.
+__device__ __forceinline__ double safety_of_state(const DevGeom &g, V3 gp, uint32_t navInd, int &status)
+{
+  if (navInd == 0) {
+    status = kTrackErrState;
+    return 0.;
+  }
+  const Xform m = nav_top_matrix(g, navInd);
+  const V3 lp   = to_local(m, gp);
+  const int lv  = g.pv_lv[nav_top(g, navInd)];
+  double safety = shape_safety_out(g, g.lv_shape[lv], lp);
+  if (safety > 0.0 && g.lv_nd[lv] > 0) safety = bvh_compute_safety(g, lv, lp, safety, status);
+  return safety;
+}
+
 // VNavigatorHelper<BVHNavigator<false>>::ComputeStepAndPropagatedState (VNavigator.h:436-492)
 __device__ __forceinline__ double compute_step(const DevGeom &g, V3 gp, V3 gd, double limit, NavState const &in,
                                                NavState &out, int &status, int *nvisited)
