@@ -56,6 +56,9 @@ def parse():
     ap.add_argument("--stream", type=int, default=1, help="also run the config-5 transport stream (1/0)")
     ap.add_argument("--stream-tracks", type=int, default=1 << 20)
     ap.add_argument("--shapes", type=int, default=1, help="also time the config-1/2 shape queries (1/0)")
+    ap.add_argument("--shape-reps", type=int, default=20, help="graph-captured calls per shape-query timing")
+    ap.add_argument("--section", default="all", choices=["all", "shapes"],
+                    help="'shapes': only the shape-query rows (one JSON line), e.g. for profiling")
     ap.add_argument("--tune", type=int, default=1,
                     help="autotune sort-key bits / queue occupancy before timing (untimed; 1/0)")
     return ap.parse_args()
@@ -69,6 +72,17 @@ def dist_setup(args):
         import torch.distributed as dist
         dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
     return ws, rank, local
+
+
+def max_over_ranks(value, ws, device):
+    """The largest `value` over all ranks (timings are reported as the slowest rank's)."""
+    if ws <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    v = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(v, op=dist.ReduceOp.MAX)
+    return float(v.item())
 
 
 class ClockSampler:
@@ -234,11 +248,42 @@ def run_stream(args, geo, torch, dev, head, clocks_cls, local):
     return out
 
 
+def timed_graph(torch, call, reps):
+    """Device time per call: `reps` calls captured in one CUDA graph and replayed between
+    CUDA events, so host launch overhead is not timed (falls back to an eager loop if the
+    capture is refused)."""
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(2):
+            call()
+    torch.cuda.current_stream().wait_stream(side)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    try:
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            for _ in range(reps):
+                call()
+        graph.replay()
+        torch.cuda.synchronize()
+        e0.record()
+        graph.replay()
+        e1.record()
+    except RuntimeError:
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            call()
+        e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
 QUERY_BYTES = {"inside": 28, "contains": 25, "distance_to_in": 56, "distance_to_out": 56, "safety_to_in": 32,
                "safety_to_out": 32}  # FP64 SoA inputs + output per query (step_max not passed)
 
 
-def shape_rows(args, torch, dev, hbm_peak, reps=5):
+def shape_rows(args, torch, dev, hbm_peak):
     """Config 1 (Box, Tube, Cone; 2^20 points uniform in the 1.2x extent box) and config 2
     (2^22 points: thirds inside, outside, within 1e-6 mm of the surface) shape queries per
     precision: queries/s, algorithmic GB/s and its fraction of the HBM peak, and for the
@@ -278,18 +323,10 @@ def shape_rows(args, torch, dev, hbm_peak, reps=5):
                 def call():
                     fn(*args_q, flags=prec)
 
-                for _ in range(2):
-                    call()
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                torch.cuda.synchronize()
-                e0.record()
-                for _ in range(reps):
-                    call()
-                e1.record()
-                torch.cuda.synchronize()
-                ms = e0.elapsed_time(e1) / reps
+                ms = timed_graph(torch, call, args.shape_reps)
                 gbs = QUERY_BYTES[q] * n / (ms * 1e-3) / 1e9
                 row = {"config": cfg, "shape": name, "query": q, "precision": prec_name, "n": n,
+                       "input_bytes": QUERY_BYTES[q] * n, "l2_resident_inputs": QUERY_BYTES[q] * n < 129e6,
                        "queries_per_s": n / (ms * 1e-3), "GB_per_s": gbs, "hbm_frac": gbs / hbm_peak}
                 if prec_name == "fp64":
                     outs[(q, "ref")] = o.clone()
@@ -373,7 +410,8 @@ def run_reference(args, ws, rank):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": config_of(args), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "nav steps/s", "cores": nthreads, "kind": "port",
-                             "sample": "%d tracks per step (first steps of the primaries) of the %d-track batch"
+                             "sample": "%d step inputs per step (drawn from the oracle's own transport "
+                                       "histories when the workload is the detector) of the %d-track batch"
                                        % (m, args.tracks)},
             "e2e": {"value": value, "unit": "nav steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -392,6 +430,14 @@ def main():
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.section == "shapes":
+        try:
+            hbm = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+        except (OSError, ValueError, KeyError):
+            hbm = 6800.0
+        if rank == 0:
+            print(json.dumps({"section": "shape_queries", "rows": shape_rows(args, torch, dev, hbm)}), flush=True)
+        return
     geo = vg.Geometry()
     builder(args.workload)(geo)
     t, st, pool = make_inputs(args, geo, torch, dev)
@@ -419,12 +465,7 @@ def main():
         e1.record()
         torch.cuda.synchronize()
         barrier()
-        ms = e0.elapsed_time(e1)
-        if ws > 1:
-            import torch.distributed as dist
-            v = torch.tensor([ms], device=dev)
-            dist.all_reduce(v, op=dist.ReduceOp.MAX)
-            ms = float(v.item())
+        ms = max_over_ranks(e0.elapsed_time(e1), ws, dev)
         return ms / args.steps
 
     head = SCHEDULES[args.schedule]

@@ -25,9 +25,40 @@ __device__ __forceinline__ double max3(double a, double b, double c) { return dm
 __device__ __forceinline__ double min3(double a, double b, double c) { return dmin(a, dmin(b, c)); }
 
 // ---------------------------------------------------------------- transformations
-// Generic Transform / TransformDirection / InverseTransform (Transformation3D.h:640-651,797-826)
+// Generic Transform / TransformDirection / InverseTransform (Transformation3D.h:640-651,797-826).
+//
+// With VECGEOM_NO_SPECIALIZATION the reference applies the full 12-double transform to every
+// point, also when the rotation is the identity. Its result is then known exactly without
+// the multiplications: each component is  v + (u * 0) + (w * 0)  with v the component and u,
+// w the other two; for finite inputs that is v itself when v != 0, and a zero that is -0
+// only when v, u and w are all negative zeros. The identity case is recognised on the bit
+// patterns (+1.0 on the diagonal, +0.0 elsewhere) and applied only to finite inputs, so the
+// results are bit-identical to the multiplications they replace, which GB300 would issue on
+// its narrow FP64 pipe.
+__device__ __forceinline__ bool finite_bits(double x)
+{
+  return (__double_as_longlong(x) & 0x7FF0000000000000LL) != 0x7FF0000000000000LL;
+}
+__device__ __forceinline__ bool rot_is_identity(const Xform &m)
+{
+  const long long one = 0x3FF0000000000000LL;
+  return __double_as_longlong(m.r[0]) == one && __double_as_longlong(m.r[4]) == one &&
+         __double_as_longlong(m.r[8]) == one && __double_as_longlong(m.r[1]) == 0 &&
+         __double_as_longlong(m.r[2]) == 0 && __double_as_longlong(m.r[3]) == 0 &&
+         __double_as_longlong(m.r[5]) == 0 && __double_as_longlong(m.r[6]) == 0 &&
+         __double_as_longlong(m.r[7]) == 0;
+}
+// v + (u * 0) + (w * 0) for finite u, w
+__device__ __forceinline__ double zsum3(double v, double u, double w)
+{
+  const long long vb = __double_as_longlong(v);
+  if ((vb & 0x7FFFFFFFFFFFFFFFLL) != 0) return v;
+  return (vb < 0 && __double_as_longlong(u) < 0 && __double_as_longlong(w) < 0) ? -0.0 : 0.0;
+}
 __device__ __forceinline__ V3 rotate(const Xform &m, V3 a)
 {
+  if (rot_is_identity(m) && finite_bits(a.x) && finite_bits(a.y) && finite_bits(a.z))
+    return V3{zsum3(a.x, a.y, a.z), zsum3(a.y, a.x, a.z), zsum3(a.z, a.x, a.y)};
   double lx = a.x * m.r[0], ly = a.x * m.r[1], lz = a.x * m.r[2];
   lx += a.y * m.r[3];
   ly += a.y * m.r[4];
@@ -39,10 +70,15 @@ __device__ __forceinline__ V3 rotate(const Xform &m, V3 a)
 }
 __device__ __forceinline__ V3 to_local(const Xform &m, V3 p)
 {
-  return rotate(m, V3{p.x - m.t[0], p.y - m.t[1], p.z - m.t[2]});
+  // p - (+0.0) is p for every p, so a zero translation needs no subtraction
+  const bool zt = __double_as_longlong(m.t[0]) == 0 && __double_as_longlong(m.t[1]) == 0 &&
+                  __double_as_longlong(m.t[2]) == 0;
+  return rotate(m, zt ? p : V3{p.x - m.t[0], p.y - m.t[1], p.z - m.t[2]});
 }
 __device__ __forceinline__ V3 to_master(const Xform &m, V3 l)
 {
+  if (rot_is_identity(m) && finite_bits(l.x) && finite_bits(l.y) && finite_bits(l.z))
+    return V3{zsum3(m.t[0] + l.x, l.y, l.z), zsum3(m.t[1] + l.y, l.x, l.z), zsum3(m.t[2] + l.z, l.x, l.y)};
   double x = m.t[0];
   x += l.x * m.r[0];
   x += l.y * m.r[1];
