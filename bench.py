@@ -105,6 +105,10 @@ class ClockSampler:
             threading.Thread(target=self._read, daemon=True).start()
         except OSError:
             self.proc = None
+        # the first sample marks the end of nvidia-smi's start-up, which then overlaps no timing
+        t0 = time.perf_counter()
+        while self.proc and not self.lines and self.proc.poll() is None and time.perf_counter() - t0 < 5.0:
+            time.sleep(0.01)
         return self
 
     def _read(self):
@@ -452,20 +456,24 @@ def main():
             import torch.distributed as dist
             dist.barrier()
 
+    spread = {}
+
     def timed(flags):
         for _ in range(args.warmup):
             geo.compute_step_and_next_volume(*t, st, out, step, status=status, flags=flags)
         torch.cuda.synchronize()
         barrier()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
         torch.cuda.synchronize()
-        e0.record()
-        for _ in range(args.steps):
+        evs[0].record()
+        for k in range(args.steps):
             geo.compute_step_and_next_volume(*t, st, out, step, status=status, flags=flags)
-        e1.record()
+            evs[k + 1].record()
         torch.cuda.synchronize()
         barrier()
-        ms = max_over_ranks(e0.elapsed_time(e1), ws, dev)
+        per = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+        spread[flags] = (min(per), max(per))
+        ms = max_over_ranks(evs[0].elapsed_time(evs[-1]), ws, dev)
         return ms / args.steps
 
     head = SCHEDULES[args.schedule]
@@ -482,7 +490,7 @@ def main():
     tuning = None
     if args.tune and head & (vg.NAV_SORT | vg.NAV_QUEUE):
         from vecgeom_gb300.tune import autotune
-        cands = [(head, b, q) for b in (0, 7, 5) for q in ((1, 2) if head & vg.NAV_QUEUE else (1,))]
+        cands = [(head, b, q) for b in (0, 7, 5) for q in ((1, 2, 3) if head & vg.NAV_QUEUE else (1,))]
         tuning = autotune(geo, t, st, candidates=cands, cache=None)
     ms_fp64 = timed(vg.PREC_FP64)
     out64, step64 = out.clone(), step.clone()
@@ -571,6 +579,7 @@ def main():
     line = {
         "metric": "nav steps/s", "value": value, "unit": "nav steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_head, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step_min_max": [round(v, 4) for v in spread.get(head, (ms_head, ms_head))],
         "vs_baseline": None, "dtype": "f64 (mixed: FP32 pruning, FP64 decisions)",
         "data": "synthetic (seeded; geometry built in code, tracks generated on the GPU)",
         "config": dict(config_of(args, pool), schedule=args.schedule,

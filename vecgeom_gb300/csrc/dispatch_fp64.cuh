@@ -101,18 +101,18 @@ __device__ inline double boolminus_dist_in(const DevGeom &g, const BoolRec &b, V
   for (int it = 0; it < kBoolMaxPush; ++it) {
     if (inR) {
       const double d1 = R.placed_dist_out(g, hit, dir);
-      const bool okd  = d1 >= 0. && d1 < kInfLength;
+      const bool okd  = dge(d1, 0.) && dlt(d1, kInfLength);
       snxt += okd ? (d1 + kPushTolerance) : 0.;
       const double s = okd ? (d1 + kPushTolerance) : 0.;
       hit            = V3{hit.x + s * dir.x, hit.y + s * dir.y, hit.z + s * dir.z};
-      if (L.contains(g, hit) && L.placed_dist_out(g, hit, dir) > kPushTolerance) return snxt;
+      if (L.contains(g, hit) && dgt(L.placed_dist_out(g, hit, dir), kPushTolerance)) return snxt;
     }
     double d2 = L.dist_in(g, hit, dir);
     d2        = dmax(d2, 0.);
-    if (d2 == kInfLength) return kInfLength;
+    if (deq(d2, kInfLength)) return kInfLength;
     const double d1 = R.dist_in(g, hit, dir);
-    if (d2 < d1 - kTolerance) return snxt + (d2 + kPushTolerance);
-    const bool okd = d1 >= 0. && d1 < kInfLength;
+    if (dlt(d2, d1 - kTolerance)) return snxt + (d2 + kPushTolerance);
+    const bool okd = dge(d1, 0.) && dlt(d1, kInfLength);
     snxt += okd ? d1 + kPushTolerance : 0.;
     const double s = okd ? (d1 + kPushTolerance) : kPushTolerance;
     hit            = V3{hit.x + s * dir.x, hit.y + s * dir.y, hit.z + s * dir.z};

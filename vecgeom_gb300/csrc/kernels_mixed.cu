@@ -2,6 +2,7 @@
 // kernels; FP32 is used only for conservative pruning (see nav_mixed.cuh). Compiled with
 // --fmad=false like every translation unit; the FP32 code requests fused multiply-adds
 // explicitly.
+#define VG_FP64_INT_COMPARE 0 // latency-bound navigation code (fp64_int.cuh)
 #include "launch.h"
 #include "nav_mixed.cuh"
 
@@ -41,10 +42,12 @@ __global__ void __launch_bounds__(256) k_step_mixed(const DevGeom g, const StepA
 
 // Persistent variant: one grid of resident blocks; each warp takes the next 32 entries of
 // the visiting order from a global counter (zeroed before the launch), so warps that drew
-// cheap tracks take more of them.
-template <int MinBlocks>
-__global__ void __launch_bounds__(256, MinBlocks) k_step_mixed_queue(const DevGeom g, const StepArgs a,
-                                                                     unsigned long long *__restrict__ counter)
+// cheap tracks take more of them. Threads x MinBlocks sets the register budget per thread:
+// 256 x 1 (no spills, 8 warps per SM), 256 x 2 (128 registers, 16 warps) or 128 x 3 (168
+// registers, 12 warps).
+template <int Threads, int MinBlocks>
+__global__ void __launch_bounds__(Threads, MinBlocks) k_step_mixed_queue(const DevGeom g, const StepArgs a,
+                                                                         unsigned long long *__restrict__ counter)
 {
   const mixed::ShapeLB *lbs = reinterpret_cast<const mixed::ShapeLB *>(g.shape_lbd);
   const int lane            = threadIdx.x & 31;
@@ -97,9 +100,9 @@ __global__ void __launch_bounds__(256) k_step_safety(const DevGeom g, const Step
 
 // Transport stream iteration (see TransportArgs): persistent warps take 32-entry chunks of
 // the visiting order from a global counter.
-template <bool Mixed, int MinBlocks>
-__global__ void __launch_bounds__(256, MinBlocks) k_transport_iter(const DevGeom g, const TransportArgs a,
-                                                                   unsigned long long *__restrict__ counter)
+template <bool Mixed, int Threads, int MinBlocks>
+__global__ void __launch_bounds__(Threads, MinBlocks) k_transport_iter(const DevGeom g, const TransportArgs a,
+                                                                       unsigned long long *__restrict__ counter)
 {
   const mixed::ShapeLB *lbs = reinterpret_cast<const mixed::ShapeLB *>(g.shape_lbd);
   const int lane            = threadIdx.x & 31;
@@ -149,13 +152,14 @@ __global__ void k_transport_init(const NavState *__restrict__ st, size_t n, int3
   }
 }
 
-template <bool Mixed, int MinBlocks>
+template <bool Mixed, int Threads, int MinBlocks>
 cudaError_t launch_transport(const DevGeom &g, const TransportArgs &a, unsigned long long *counter, cudaStream_t s)
 {
   static int resident = 0;
   if (resident == 0) {
     int r = 0;
-    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_transport_iter<Mixed, MinBlocks>, 256, 0);
+    const cudaError_t e =
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_transport_iter<Mixed, Threads, MinBlocks>, Threads, 0);
     if (e != cudaSuccess) return e;
     resident = r > 0 ? r : 1;
   }
@@ -164,9 +168,9 @@ cudaError_t launch_transport(const DevGeom &g, const TransportArgs &a, unsigned 
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e == cudaSuccess) e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
-  size_t blocks = (size_t)sms * resident, need = (a.n + 255) / 256;
+  size_t blocks = (size_t)sms * resident, need = (a.n + Threads - 1) / Threads;
   if (blocks > need) blocks = need;
-  k_transport_iter<Mixed, MinBlocks><<<(unsigned)blocks, 256, 0, s>>>(g, a, counter);
+  k_transport_iter<Mixed, Threads, MinBlocks><<<(unsigned)blocks, Threads, 0, s>>>(g, a, counter);
   return cudaGetLastError();
 }
 
@@ -179,13 +183,14 @@ cudaError_t launch_step_mixed(const DevGeom &g, const StepArgs &a, cudaStream_t 
   return cudaGetLastError();
 }
 
-template <int MinBlocks>
+template <int Threads, int MinBlocks>
 cudaError_t launch_queue(const DevGeom &g, const StepArgs &a, unsigned long long *counter, cudaStream_t s)
 {
-  static int resident = 0; // blocks of 256 per SM (same for every device of this build)
+  static int resident = 0; // blocks per SM (same for every device of this build)
   if (resident == 0) {
     int r = 0;
-    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_step_mixed_queue<MinBlocks>, 256, 0);
+    const cudaError_t e =
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_step_mixed_queue<Threads, MinBlocks>, Threads, 0);
     if (e != cudaSuccess) return e;
     resident = r > 0 ? r : 1;
   }
@@ -195,9 +200,9 @@ cudaError_t launch_queue(const DevGeom &g, const StepArgs &a, unsigned long long
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
-  size_t blocks = (size_t)sms * resident, need = (a.n + 255) / 256;
+  size_t blocks = (size_t)sms * resident, need = (a.n + Threads - 1) / Threads;
   if (blocks > need) blocks = need;
-  k_step_mixed_queue<MinBlocks><<<(unsigned)blocks, 256, 0, s>>>(g, a, counter);
+  k_step_mixed_queue<Threads, MinBlocks><<<(unsigned)blocks, Threads, 0, s>>>(g, a, counter);
   return cudaGetLastError();
 }
 
@@ -205,7 +210,8 @@ cudaError_t launch_step_mixed_queue(const DevGeom &g, const StepArgs &a, unsigne
                                     int blocks_per_sm, cudaStream_t s)
 {
   if (a.n == 0) return cudaSuccess;
-  return blocks_per_sm >= 2 ? launch_queue<2>(g, a, counter, s) : launch_queue<1>(g, a, counter, s);
+  if (blocks_per_sm == 3) return launch_queue<128, 3>(g, a, counter, s);
+  return blocks_per_sm == 2 ? launch_queue<256, 2>(g, a, counter, s) : launch_queue<256, 1>(g, a, counter, s);
 }
 
 cudaError_t launch_step_safety(const DevGeom &g, const StepArgs &a, double *safety, bool mixed, cudaStream_t s)
@@ -222,9 +228,10 @@ cudaError_t launch_transport_iter(const DevGeom &g, const TransportArgs &a, bool
                                   int blocks_per_sm, cudaStream_t s)
 {
   if (a.n == 0) return cudaSuccess;
-  if (mixed)
-    return blocks_per_sm >= 2 ? launch_transport<true, 2>(g, a, counter, s) : launch_transport<true, 1>(g, a, counter, s);
-  return launch_transport<false, 1>(g, a, counter, s);
+  if (!mixed) return launch_transport<false, 256, 1>(g, a, counter, s);
+  if (blocks_per_sm == 3) return launch_transport<true, 128, 3>(g, a, counter, s);
+  return blocks_per_sm == 2 ? launch_transport<true, 256, 2>(g, a, counter, s)
+                            : launch_transport<true, 256, 1>(g, a, counter, s);
 }
 
 cudaError_t launch_transport_init(const NavState *st, size_t n, int32_t *nsteps, int32_t *status, uint32_t *list,

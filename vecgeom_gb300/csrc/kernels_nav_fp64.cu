@@ -1,0 +1,71 @@
+// Plain-FP64 navigation kernels: one thread per track, LocatePoint and
+// ComputeStepAndPropagatedState. Compiled with --fmad=false. These divergent kernels are
+// latency-bound, so FP64 compares stay on the FP64 pipe and the exact shortcuts are off
+// (VG_FP64_INT_COMPARE 0, VG_FP64_SHORTCUTS 0, see fp64_int.cuh).
+#define VG_FP64_INT_COMPARE 0
+#define VG_FP64_SHORTCUTS 0
+#include "launch.h"
+#include "nav_fp64.cuh"
+
+namespace vg {
+namespace {
+
+using f64::V3;
+
+inline unsigned grid_for(size_t n, int block)
+{
+  size_t blocks       = (n + block - 1) / block;
+  const size_t maxgrd = 152 * 16;
+  if (blocks > maxgrd) blocks = maxgrd;
+  return (unsigned)(blocks ? blocks : 1);
+}
+
+__global__ void __launch_bounds__(256) k_locate(const DevGeom g, const double *__restrict__ x,
+                                                const double *__restrict__ y, const double *__restrict__ z, size_t n,
+                                                NavState *__restrict__ out)
+{
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    NavState s{0u, 0u, 0, {0, 0, 0}};
+    int status = 0;
+    f64::locate_global_point(g, g.world_pv, V3{__ldg(x + i), __ldg(y + i), __ldg(z + i)}, s.navInd, true, status);
+    out[i] = s;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_step(const DevGeom g, const StepArgs a)
+{
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+    const size_t t   = a.order ? (size_t)__ldg(a.order + i) : i;
+    const NavState s = a.in[t];
+    NavState o;
+    int st = 0, nv = 0;
+    const double lim = a.limit ? __ldg(a.limit + t) : kInfLength;
+    a.step[t] = f64::compute_step(g, V3{__ldg(a.x + t), __ldg(a.y + t), __ldg(a.z + t)},
+                                  V3{__ldg(a.dx + t), __ldg(a.dy + t), __ldg(a.dz + t)}, lim, s, o, st,
+                                  a.nvisited ? &nv : nullptr);
+    a.out[t] = o;
+    if (a.status) a.status[t] = st;
+    if (a.nvisited) a.nvisited[t] = nv;
+  }
+}
+
+} // namespace
+
+cudaError_t launch_locate_fp64(const DevGeom &g, const double *x, const double *y, const double *z, size_t n,
+                               NavState *out, cudaStream_t s)
+{
+  if (n == 0) return cudaSuccess;
+  k_locate<<<grid_for(n, 256), 256, 0, s>>>(g, x, y, z, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step_fp64(const DevGeom &g, const StepArgs &a, cudaStream_t s)
+{
+  if (a.n == 0) return cudaSuccess;
+  k_step<<<grid_for(a.n, 256), 256, 0, s>>>(g, a);
+  return cudaGetLastError();
+}
+
+} // namespace vg

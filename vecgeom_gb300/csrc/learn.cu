@@ -1,6 +1,7 @@
 // Learned proposal: feature/label generation, training kernels (FP32 forward, backward and
 // Adam over the flat parameter vector) and the SIMT BF16 inference kernel used as the
 // reference for the tensor-core one.
+#define VG_FP64_INT_COMPARE 0 // latency-bound navigation code (fp64_int.cuh)
 #include "learn_features.cuh"
 #include <cuda_bf16.h>
 

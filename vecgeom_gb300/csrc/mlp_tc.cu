@@ -11,6 +11,7 @@
 // along K (leading byte offset) and K/8 x 128 bytes apart along M/N (stride byte offset).
 // Every wait on the MMA completion barrier is bounded; on time-out the kernel records an
 // error, drains its outstanding MMA (bounded), frees its tensor memory and returns.
+#define VG_FP64_INT_COMPARE 0 // latency-bound navigation code (fp64_int.cuh)
 #include "learn_features.cuh"
 #include <cuda_bf16.h>
 

@@ -64,17 +64,17 @@ __device__ __forceinline__ Xform nav_top_matrix(const DevGeom &g, uint32_t n)
 // ---------------------------------------------------------------- boxes (VecGeom/base/AABB.h)
 __device__ __forceinline__ bool aabb_contains(const double *b, V3 p)
 {
-  return p.x >= __ldg(b) && p.x <= __ldg(b + 3) && p.y >= __ldg(b + 1) && p.y <= __ldg(b + 4) && p.z >= __ldg(b + 2) &&
-         p.z <= __ldg(b + 5);
+  return dge(p.x, __ldg(b)) && dle(p.x, __ldg(b + 3)) && dge(p.y, __ldg(b + 1)) && dle(p.y, __ldg(b + 4)) &&
+         dge(p.z, __ldg(b + 2)) && dle(p.z, __ldg(b + 5));
 }
 __device__ __forceinline__ void aabb_slab(const double *b, V3 p, V3 inv, double &tmin, double &tmax)
 {
   double t0x = (__ldg(b) - p.x) * inv.x, t1x = (__ldg(b + 3) - p.x) * inv.x;
   double t0y = (__ldg(b + 1) - p.y) * inv.y, t1y = (__ldg(b + 4) - p.y) * inv.y;
   double t0z = (__ldg(b + 2) - p.z) * inv.z, t1z = (__ldg(b + 5) - p.z) * inv.z;
-  if (t0x > t1x) { double s = t0x; t0x = t1x; t1x = s; }
-  if (t0y > t1y) { double s = t0y; t0y = t1y; t1y = s; }
-  if (t0z > t1z) { double s = t0z; t0z = t1z; t1z = s; }
+  if (dgt(t0x, t1x)) { double s = t0x; t0x = t1x; t1x = s; }
+  if (dgt(t0y, t1y)) { double s = t0y; t0y = t1y; t1y = s; }
+  if (dgt(t0z, t1z)) { double s = t0z; t0z = t1z; t1z = s; }
   tmin = max3(t0x, t0y, t0z);
   tmax = min3(t1x, t1y, t1z) * (1. + 2 * kEpsilon);
 }
@@ -114,10 +114,10 @@ __device__ __forceinline__ int bvh_check_daughters(const DevGeom &g, int lv, V3 
         const int prim = __ldg(&g.prim_id[off + i]);
         double tmin, tmax;
         aabb_slab(g.prim_box + 6 * (size_t)(dbase + prim), lp, inv, tmin, tmax);
-        if (tmin <= tmax && tmax >= 0.0 && tmin < step) {
+        if (dle(tmin, tmax) && dge(tmax, 0.0) && dlt(tmin, step)) {
           const int vol     = __ldg(&g.daughters[dbase + prim]);
           const double dist = pv_dist_in(g, vol, lp, ld);
-          if (dist < step && !(dist <= 0.0 && vol == last_pv)) step = dist, hit_pv = vol;
+          if (dlt(dist, step) && !(dle(dist, 0.0) && vol == last_pv)) step = dist, hit_pv = vol;
         }
       }
     } else {
@@ -125,13 +125,13 @@ __device__ __forceinline__ int bvh_check_daughters(const DevGeom &g, int lv, V3 
       double tminL, tmaxL, tminR, tmaxR;
       aabb_slab(g.node_box + 6 * (size_t)(node0 + cl), lp, inv, tminL, tmaxL);
       aabb_slab(g.node_box + 6 * (size_t)(node0 + cr), lp, inv, tminR, tmaxR);
-      const bool tl = tminL <= tmaxL && tmaxL >= 0.0 && tminL < step;
-      const bool tr = tminR <= tmaxR && tmaxR >= 0.0 && tminR < step;
+      const bool tl = dle(tminL, tmaxL) && dge(tmaxL, 0.0) && dlt(tminL, step);
+      const bool tr = dle(tminR, tmaxR) && dge(tmaxR, 0.0) && dlt(tminR, step);
       if (sp + 2 > 32) {
         if (nvisited) *nvisited = visits;
         return kTrackErrStack;
       }
-      if (tminR < tminL) {
+      if (dlt(tminR, tminL)) {
         if (tr) stack[sp++] = cr;
         if (tl) stack[sp++] = cl;
       } else {
@@ -269,10 +269,10 @@ __device__ __forceinline__ double bvh_compute_safety(const DevGeom &g, int lv, V
       const int off = __ldg(&g.node_offset[node0 + id]);
       for (int i = 0; i < nch; ++i) {
         const int prim = __ldg(&g.prim_id[off + i]);
-        if (aabb_safety(g.prim_box + 6 * (size_t)(dbase + prim), lp) < safety) {
+        if (dlt(aabb_safety(g.prim_box + 6 * (size_t)(dbase + prim), lp), safety)) {
           const int vol     = __ldg(&g.daughters[dbase + prim]);
           const double dist = shape_safety_in(g, pv_shape(g, vol), to_local(g.pv_xf[vol], lp));
-          if (dist < safety) safety = dist;
+          if (dlt(dist, safety)) safety = dist;
         }
       }
     } else {
@@ -283,8 +283,8 @@ __device__ __forceinline__ double bvh_compute_safety(const DevGeom &g, int lv, V
       const unsigned cl = 2 * id + 1, cr = 2 * id + 2;
       const double sl = aabb_safety(g.node_box + 6 * (size_t)(node0 + cl), lp);
       const double sr = aabb_safety(g.node_box + 6 * (size_t)(node0 + cr), lp);
-      const bool tl = sl < safety, tr = sr < safety;
-      if (sr < sl) {
+      const bool tl = dlt(sl, safety), tr = dlt(sr, safety);
+      if (dlt(sr, sl)) {
         if (tr) stack[sp++] = cr;
         if (tl) stack[sp++] = cl;
       } else {
@@ -309,7 +309,7 @@ __device__ __forceinline__ double safety_of_state(const DevGeom &g, V3 gp, uint3
   const V3 lp   = to_local(m, gp);
   const int lv  = g.pv_lv[nav_top(g, navInd)];
   double safety = shape_safety_out(g, g.lv_shape[lv], lp);
-  if (safety > 0.0 && g.lv_nd[lv] > 0) safety = bvh_compute_safety(g, lv, lp, safety, status);
+  if (dgt(safety, 0.0) && g.lv_nd[lv] > 0) safety = bvh_compute_safety(g, lv, lp, safety, status);
   return safety;
 }
 
@@ -329,7 +329,7 @@ __device__ __forceinline__ double compute_step(const DevGeom &g, V3 gp, V3 gd, d
   const int pv  = nav_top(g, in.navInd);
   const int lv  = g.pv_lv[pv];
   double step   = shape_dist_out(g, g.lv_shape[lv], lp, ld);
-  if (step < 0.) step = 0.;
+  if (dlt(step, 0.)) step = 0.;
   int hit = -1;
   if (g.lv_nd[lv] > 0) {
     const int last = nav_top(g, in.lastExited);
@@ -337,19 +337,19 @@ __device__ __forceinline__ double compute_step(const DevGeom &g, V3 gp, V3 gd, d
     if (status != kTrackOk) return 0.;
   }
   // PrepareOutState (VNavigator.h:192-235)
-  if (step == kInfLength && limit > 0.) {
+  if (deq(step, kInfLength) && dgt(limit, 0.)) {
     out.onBoundary = 1;
     out.navInd     = nav_pop(g, out.navInd);
     return kTolerance;
   }
-  if (step > limit) {
+  if (dgt(step, limit)) {
     out.onBoundary = 0;
     return limit;
   }
   out.onBoundary = 1;
   out.lastExited = out.navInd;
   if (hit >= 0) out.navInd = nav_push(g, out.navInd, hit);
-  if (step < 0.) step = 0.;
+  if (dlt(step, 0.)) step = 0.;
   // Relocate(MovePointAfterBoundary(...)) (VNavigator.h:168-173, 1070-1091)
   const double s = step + 1E-6;
   const V3 after{lp.x + s * ld.x, lp.y + s * ld.y, lp.z + s * ld.z};

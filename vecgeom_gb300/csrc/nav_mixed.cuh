@@ -20,6 +20,13 @@
 namespace vg {
 namespace mixed {
 
+#if VG_FP64_INT_COMPARE // (otherwise these names are macros)
+using f64::deq;
+using f64::dgt;
+using f64::dle;
+using f64::dlt;
+#endif
+
 using f64::V3;
 
 // Pad (mm) added to every FP32 box/descriptor on each side. FP32 rounding of coordinates
@@ -99,8 +106,16 @@ __device__ __forceinline__ float shell_lb(float rmin, float rmax, float zlo, flo
 
 // Lower bound of DistanceToIn of a placed daughter (p, d in the mother frame). The
 // daughter's frame offset (p - t) is formed in FP64, the rotation in FP32.
-__device__ __forceinline__ float daughter_lb(const DevGeom &g, const ShapeLB *lbs, int pv, V3 p, V3 d)
+//
+// `ub` receives an upper bound of the FP64 DistanceToIn when one is certain, else +inf. It
+// is given for daughters whose shape is their box: if the FP32 ray crosses the box shrunk
+// by 2 kBoxPad over a parameter interval [t0, t1] with t0 > 0, then the FP64 ray (within
+// kBoxPad of the FP32 one) is strictly inside the box at t0, so the box's DistanceToIn is a
+// hit (entry before exit, exit ahead, the far planes ahead by more than kHalfTolerance) at a
+// distance <= t0; the bound adds the FP32 rounding of t0 and 1 um.
+__device__ __forceinline__ float daughter_lb(const DevGeom &g, const ShapeLB *lbs, int pv, V3 p, V3 d, float &ub)
 {
+  ub = INFINITY;
   const Xform &m = g.pv_xf[pv];
   const F3 q{(float)(p.x - m.t[0]), (float)(p.y - m.t[1]), (float)(p.z - m.t[2])};
   const F3 dd = f3(d);
@@ -119,6 +134,17 @@ __device__ __forceinline__ float daughter_lb(const DevGeom &g, const ShapeLB *lb
     slab_f(lo, hi, lp, inv, tmin, tmax);
     if (!(tmin <= tmax) || tmax < 0.f) return INFINITY;
     if (tmin <= 0.f) return -INFINITY; // inside the padded box: the distance may be <= 0
+    if (s.flag != 0.f) {
+      // slab of the box shrunk by 2 kBoxPad (slab_f pads by kBoxPad, so shrink by 3 kBoxPad)
+      const float ls[3] = {lo[0] + 3.f * kBoxPad, lo[1] + 3.f * kBoxPad, lo[2] + 3.f * kBoxPad};
+      const float hs[3] = {hi[0] - 3.f * kBoxPad, hi[1] - 3.f * kBoxPad, hi[2] - 3.f * kBoxPad};
+      if (ls[0] < hs[0] && ls[1] < hs[1] && ls[2] < hs[2]) {
+        float t0, t1;
+        slab_f(ls, hs, lp, inv, t0, t1);
+        const float u = fmaf(t0, 1.f + 2.f * kLbRel, 1e-3f);
+        if (t0 > 0.f && t1 * (1.f - 2.f * kLbRel) > u) ub = u;
+      }
+    }
     return tmin * (1.f - kLbRel) - kBoxPad;
   }
   const float rmin = fmaxf(s.a0 - kBoxPad, 0.f), rmax = s.a1 + kBoxPad;
@@ -191,10 +217,10 @@ __device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, const Sha
       return;
     }
     const double dist = f64::pv_dist_in(g, vol, lp, ld);
-    if (dist < step && !(dist <= 0.0 && vol == last_pv)) {
+    if (dlt(dist, step) && !(dle(dist, 0.0) && vol == last_pv)) {
       step   = dist;
       hit_pv = vol;
-      bound  = __double2float_ru(step);
+      bound  = fminf(bound, __double2float_ru(step));
       while (nc > 0 && cl[nc - 1] >= bound) --nc;
     }
   };
@@ -212,22 +238,17 @@ __device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, const Sha
   int sp     = 1;
   stack[0]   = 0;
   int visits = 0;
-  // Learned proposal: explore depth-3 subtree `first` before the rest. When only the root
-  // is left on the stack the subtree is done: its candidates are evaluated now, which
-  // tightens the bound for the remaining traversal, and the subtree is not entered again.
+  // Learned proposal: explore depth-3 subtree `first` before the rest (and not again), so
+  // the upper bounds of its daughters tighten the bound for the remaining traversal. Exact
+  // FP64 evaluations still wait for the end of the traversal, where the lanes of a warp
+  // reach them together.
   unsigned skip = 0xffffffffu;
-  bool flushed  = true;
   if (first >= 0) {
     skip     = 7u + (unsigned)first;
     stack[1] = skip;
     sp       = 2;
-    flushed  = false;
   }
   do {
-    if (!flushed && sp == 1) {
-      while (nc > 0) evaluate_first();
-      flushed = true;
-    }
     const unsigned id = stack[--sp];
     ++visits;
     const NodeF nd = g.node_f[node0 + id];
@@ -239,7 +260,15 @@ __device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, const Sha
         slab_f(bx, bx + 3, pf, inv, tmin, tmax);
         if (tmin <= tmax && tmax >= 0.f && tmin < bound) {
           const int vol = __ldg(&g.daughters[dbase + prim]);
-          add(daughter_lb(g, lbs, vol, lp, ld), vol);
+          float ub;
+          const float lb = daughter_lb(g, lbs, vol, lp, ld, ub);
+          add(lb, vol);
+          // a certain upper bound of this daughter's distance bounds the step: whatever
+          // starts beyond it can no longer be the first hit
+          if (ub < bound && vol != last_pv) {
+            bound = ub;
+            while (nc > 0 && cl[nc - 1] >= bound) --nc;
+          }
         }
       }
     } else {
@@ -404,7 +433,7 @@ __device__ __forceinline__ double compute_step_mixed(const DevGeom &g, const Sha
   const int pv  = f64::nav_top(g, in.navInd);
   const int lv  = g.pv_lv[pv];
   double step   = f64::shape_dist_out(g, g.lv_shape[lv], lp, ld);
-  if (step < 0.) step = 0.;
+  if (dlt(step, 0.)) step = 0.;
   int hit = -1;
   if (g.lv_nd[lv] > 0) {
     const int last = f64::nav_top(g, in.lastExited);
@@ -422,19 +451,19 @@ __device__ __forceinline__ double compute_step_mixed(const DevGeom &g, const Sha
     status = check_daughters_mixed(g, lbs, lv, lp, ld, step, last, hit, nvisited, first);
     if (status != kTrackOk) return 0.;
   }
-  if (step == kInfLength && limit > 0.) {
+  if (deq(step, kInfLength) && dgt(limit, 0.)) {
     out.onBoundary = 1;
     out.navInd     = f64::nav_pop(g, out.navInd);
     return kTolerance;
   }
-  if (step > limit) {
+  if (dgt(step, limit)) {
     out.onBoundary = 0;
     return limit;
   }
   out.onBoundary = 1;
   out.lastExited = out.navInd;
   if (hit >= 0) out.navInd = f64::nav_push(g, out.navInd, hit);
-  if (step < 0.) step = 0.;
+  if (dlt(step, 0.)) step = 0.;
   const double s = step + 1E-6;
   const V3 after{lp.x + s * ld.x, lp.y + s * ld.y, lp.z + s * ld.z};
   if (hit < 0) {

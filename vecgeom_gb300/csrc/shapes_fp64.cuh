@@ -5,6 +5,7 @@
 // the reference's host build; the evaluation order of every expression follows the
 // reference kernel cited above each function.
 #pragma once
+#include "fp64_int.cuh"
 #include "vg_types.h"
 
 namespace vg {
@@ -14,9 +15,17 @@ struct V3 {
   double x, y, z;
 };
 __device__ __forceinline__ V3 mk(double x, double y, double z) { return V3{x, y, z}; }
-__device__ __forceinline__ double dmin(double a, double b) { return a < b ? a : b; }
-__device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : b; }
-__device__ __forceinline__ double nonzero(double x) { return x + copysign(1.0e-30, x); }
+// x + copysign(1e-30, x). For |x| >= 2^-46 half an ulp of x exceeds 1e-30, so the sum
+// rounds back to x and the FP64 addition is skipped.
+__device__ __forceinline__ double nonzero(double x)
+{
+#if VG_FP64_SHORTCUTS
+  if (dabs_lt(x, 1.4210854715202004e-14)) x = x + copysign(1.0e-30, x);
+  return x;
+#else
+  return x + copysign(1.0e-30, x);
+#endif
+}
 __device__ __forceinline__ double nonzeroabs(double x) { return fabs(x) + 1.0e-30; }
 __device__ __forceinline__ double sgn(double x) { return copysign(1.0, x); }
 __device__ __forceinline__ double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
@@ -39,6 +48,21 @@ __device__ __forceinline__ bool finite_bits(double x)
 {
   return (__double_as_longlong(x) & 0x7FF0000000000000LL) != 0x7FF0000000000000LL;
 }
+// v + (u * +0.0) for finite u: v unless v is a zero, then -0 only when v and u are both -0
+__device__ __forceinline__ double zadd(double v, double u)
+{
+  const long long vb = dbits(v);
+  if ((vb & 0x7FFFFFFFFFFFFFFFLL) != 0) return v;
+  return (vb < 0 && dbits(u) < 0) ? -0.0 : 0.0;
+}
+// Rotation about z: r[2] = r[5] = r[6] = r[7] = +0.0 and r[8] = +1.0 exactly. The terms with
+// a zero factor are then known signed zeros, and the product with 1.0 is the operand.
+__device__ __forceinline__ bool rot_is_z(const Xform &m)
+{
+  return VG_FP64_SHORTCUTS && __double_as_longlong(m.r[8]) == 0x3FF0000000000000LL && __double_as_longlong(m.r[2]) == 0 &&
+         __double_as_longlong(m.r[5]) == 0 && __double_as_longlong(m.r[6]) == 0 &&
+         __double_as_longlong(m.r[7]) == 0;
+}
 __device__ __forceinline__ bool rot_is_identity(const Xform &m)
 {
   const long long one = 0x3FF0000000000000LL;
@@ -57,8 +81,12 @@ __device__ __forceinline__ double zsum3(double v, double u, double w)
 }
 __device__ __forceinline__ V3 rotate(const Xform &m, V3 a)
 {
-  if (rot_is_identity(m) && finite_bits(a.x) && finite_bits(a.y) && finite_bits(a.z))
-    return V3{zsum3(a.x, a.y, a.z), zsum3(a.y, a.x, a.z), zsum3(a.z, a.x, a.y)};
+  const bool fin = finite_bits(a.x) && finite_bits(a.y) && finite_bits(a.z);
+  if (fin && rot_is_identity(m)) return V3{zsum3(a.x, a.y, a.z), zsum3(a.y, a.x, a.z), zsum3(a.z, a.x, a.y)};
+  if (fin && rot_is_z(m)) {
+    const double sx = a.x * m.r[0] + a.y * m.r[3], sy = a.x * m.r[1] + a.y * m.r[4];
+    return V3{zadd(sx, a.z), zadd(sy, a.z), zsum3(a.z, a.x, a.y)};
+  }
   double lx = a.x * m.r[0], ly = a.x * m.r[1], lz = a.x * m.r[2];
   lx += a.y * m.r[3];
   ly += a.y * m.r[4];
@@ -77,8 +105,18 @@ __device__ __forceinline__ V3 to_local(const Xform &m, V3 p)
 }
 __device__ __forceinline__ V3 to_master(const Xform &m, V3 l)
 {
-  if (rot_is_identity(m) && finite_bits(l.x) && finite_bits(l.y) && finite_bits(l.z))
+  const bool fin = finite_bits(l.x) && finite_bits(l.y) && finite_bits(l.z);
+  if (fin && rot_is_identity(m))
     return V3{zsum3(m.t[0] + l.x, l.y, l.z), zsum3(m.t[1] + l.y, l.x, l.z), zsum3(m.t[2] + l.z, l.x, l.y)};
+  if (fin && rot_is_z(m)) {
+    double x = m.t[0];
+    x += l.x * m.r[0];
+    x += l.y * m.r[1];
+    double y = m.t[1];
+    y += l.x * m.r[3];
+    y += l.y * m.r[4];
+    return V3{zadd(x, l.z), zadd(y, l.z), zsum3(m.t[2], l.x, l.y) + l.z};
+  }
   double x = m.t[0];
   x += l.x * m.r[0];
   x += l.y * m.r[1];
@@ -98,19 +136,19 @@ __device__ __forceinline__ V3 to_master(const Xform &m, V3 l)
 // Wedge_Evolution.h:335-347
 __device__ __forceinline__ bool wedge_on_surface(double ax, double ay, double nx, double ny, V3 p)
 {
-  if (!(ax * p.x + ay * p.y >= 0.)) return false;
-  return fabs(nx * p.x + ny * p.y) < kTolerance;
+  if (!dge(ax * p.x + ay * p.y, 0.)) return false;
+  return dabs_lt(nx * p.x + ny * p.y, kTolerance);
 }
 // Wedge_Evolution.h:299-331 (forInside selects the surface-aware variant)
 __device__ __forceinline__ void wedge_classify(const WedgeRec &w, V3 p, bool forInside, bool &cin, bool &cout)
 {
   const double startCheck = (-p.x * w.a1y + p.y * w.a1x);
   const double endCheck   = (-w.a2x * p.y + w.a2y * p.x);
-  cout                    = startCheck < 0.;
-  if (w.dphi < kPi)
-    cout = cout || (endCheck < 0.);
+  cout                    = dlt(startCheck, 0.);
+  if (dlt(w.dphi, kPi))
+    cout = cout || dlt(endCheck, 0.);
   else
-    cout = cout && (endCheck < 0.);
+    cout = cout && dlt(endCheck, 0.);
   if (forInside) {
     const bool onSurface = wedge_on_surface(w.a1x, w.a1y, w.n1x, w.n1y, p) || wedge_on_surface(w.a2x, w.a2y, w.n2x, w.n2y, p);
     cout                 = cout && !onSurface;
@@ -121,13 +159,13 @@ __device__ __forceinline__ double wedge_safety_out(const WedgeRec &w, V3 p)
 {
   const double d1 = p.x * w.n1x + p.y * w.n1y;
   const double d2 = p.x * w.n2x + p.y * w.n2y;
-  return w.dphi < kPi ? dmin(d1, d2) : dmax(d1, d2);
+  return dlt(w.dphi, kPi) ? dmin(d1, d2) : dmax(d1, d2);
 }
 __device__ __forceinline__ double wedge_safety_in(const WedgeRec &w, V3 p)
 {
   const double d1 = p.x * w.n1x + p.y * w.n1y;
   const double d2 = p.x * w.n2x + p.y * w.n2y;
-  return w.dphi < kPi ? dmax(-d1, -d2) : dmin(-d1, -d2);
+  return dlt(w.dphi, kPi) ? dmax(-d1, -d2) : dmin(-d1, -d2);
 }
 
 // ================================================================ Box
@@ -143,28 +181,29 @@ __device__ __forceinline__ double box_safety_out(const BoxRec &b, V3 p)
 __device__ __forceinline__ int box_inside(const BoxRec &b, V3 p)
 {
   const double dist = box_safety_in(b, p);
-  return fabs(dist) < kHalfTolerance ? kSurface : (dist < 0. ? kInside : kOutside);
+  return dabs_lt(dist, kHalfTolerance) ? kSurface : (dlt(dist, 0.) ? kInside : kOutside);
 }
-__device__ __forceinline__ bool box_contains(const BoxRec &b, V3 p) { return box_safety_in(b, p) < 0.; }
+__device__ __forceinline__ bool box_contains(const BoxRec &b, V3 p) { return dlt(box_safety_in(b, p), 0.); }
+// The products with sgn(d) = +-1 are sign flips (flipsign / negflipsign).
 __device__ __forceinline__ double box_dist_in(const BoxRec &b, V3 p, V3 d)
 {
   const double ix = 1.0 / nonzero(d.x), iy = 1.0 / nonzero(d.y), iz = 1.0 / nonzero(d.z);
-  const double sx = sgn(d.x), sy = sgn(d.y), sz = sgn(d.z);
-  const double inx = -sx * b.dx - p.x, iny = -sy * b.dy - p.y, inz = -sz * b.dz - p.z;
-  const double ox = sx * b.dx - p.x, oy = sy * b.dy - p.y, oz = sz * b.dz - p.z;
-  const double absOrthogOut = fabs(min3(sx * ox, sy * oy, sz * oz));
+  const double inx = negflipsign(b.dx, d.x) - p.x, iny = negflipsign(b.dy, d.y) - p.y,
+               inz = negflipsign(b.dz, d.z) - p.z;
+  const double ox = flipsign(b.dx, d.x) - p.x, oy = flipsign(b.dy, d.y) - p.y, oz = flipsign(b.dz, d.z) - p.z;
+  const double absOrthogOut = fabs(min3(flipsign(ox, d.x), flipsign(oy, d.y), flipsign(oz, d.z)));
   const double distOut      = min3(ox * ix, oy * iy, oz * iz);
   const double distance     = max3(inx * ix, iny * iy, inz * iz);
-  const bool miss = distance >= distOut || distOut <= kHalfTolerance || absOrthogOut <= kHalfTolerance;
+  const bool miss = dge(distance, distOut) || dle(distOut, kHalfTolerance) || dle(absOrthogOut, kHalfTolerance);
   return miss ? kInfLength : distance;
 }
 __device__ __forceinline__ double box_dist_out(const BoxRec &b, V3 p, V3 d)
 {
   const double ix = 1.0 / nonzero(d.x), iy = 1.0 / nonzero(d.y), iz = 1.0 / nonzero(d.z);
   const double safetyIn = box_safety_in(b, p);
-  const double ox = sgn(d.x) * b.dx - p.x, oy = sgn(d.y) * b.dy - p.y, oz = sgn(d.z) * b.dz - p.z;
+  const double ox = flipsign(b.dx, d.x) - p.x, oy = flipsign(b.dy, d.y) - p.y, oz = flipsign(b.dz, d.z) - p.z;
   const double distance = min3(ox * ix, oy * iy, oz * iz);
-  return safetyIn > kHalfTolerance ? -1.0 : distance;
+  return dgt(safetyIn, kHalfTolerance) ? -1.0 : distance;
 }
 
 // ================================================================ Tube
@@ -174,26 +213,26 @@ __device__ __forceinline__ bool tube_in_sector(const TubeRec &t, double x, doubl
   const double startCheck = (-x * t.a1y + y * t.a1x);
   const double endCheck   = (-t.a2x * y + t.a2y * x);
   const double tol        = includeSurface ? -kHalfTolerance : kHalfTolerance;
-  if (t.dphi <= kPi) return (startCheck >= tol) && (endCheck >= tol);
-  return (startCheck >= tol) || (endCheck >= tol);
+  if (dle(t.dphi, kPi)) return dge(startCheck, tol) && dge(endCheck, tol);
+  return dge(startCheck, tol) || dge(endCheck, tol);
 }
-__device__ __forceinline__ bool tube_phi(const TubeRec &t) { return t.dphi < kTwoPi; }
-__device__ __forceinline__ bool tube_rmin(const TubeRec &t) { return t.rmin > 0; }
+__device__ __forceinline__ bool tube_phi(const TubeRec &t) { return dlt(t.dphi, kTwoPi); }
+__device__ __forceinline__ bool tube_rmin(const TubeRec &t) { return dgt(t.rmin, 0.); }
 
 // TubeImplementation.h:103-162
 __device__ __forceinline__ void tube_circle(const TubeRec &t, double b, double c, V3 pos, V3 dir, bool largest,
                                             bool insectorCheck, double &dist, bool &ok)
 {
   double delta = b * b - c;
-  ok           = delta > 0. || (largest && delta == 0.);
+  ok           = dgt(delta, 0.) || (largest && deq(delta, 0.));
   if (!ok) delta = 0.;
   delta = sqrt(delta);
   if (!largest) delta = -delta;
   dist = -b + delta;
-  ok   = ok && (dist >= -2 * kTolerance);
+  ok   = ok && dge(dist, -2 * kTolerance);
   if (!ok || !insectorCheck) return;
   const double hitz = pos.z + dist * dir.z;
-  ok                = fabs(hitz) <= t.z;
+  ok                = dabs_le(hitz, t.z);
   if (!ok) return;
   if (tube_phi(t)) {
     const double hitx = pos.x + dist * dir.x;
@@ -207,19 +246,19 @@ __device__ __forceinline__ void tube_phi_plane(const TubeRec &t, double ax, doub
                                                V3 dir, bool insectorCheck, double &dist, bool &ok)
 {
   const double dirDotNorm = dir.x * nx + dir.y * ny;
-  ok                      = insectorCheck ? (dirDotNorm > 0.) : (dirDotNorm < 0.);
+  ok                      = insectorCheck ? dgt(dirDotNorm, 0.) : dlt(dirDotNorm, 0.);
   const double dirDotXY   = (dir.y * ax - dir.x * ay);
   dist                    = (ay * pos.x - ax * pos.y) / nonzero(dirDotXY);
-  ok                      = ok && ((dist * fabs(dirDotNorm)) > -kHalfTolerance);
+  ok                      = ok && dgt(dist * fabs(dirDotNorm), -kHalfTolerance);
   const double hitx       = pos.x + dist * dir.x;
   const double hity       = pos.y + dist * dir.y;
   if (insectorCheck) {
     const double hitz = pos.z + dist * dir.z;
     const double r2   = hitx * hitx + hity * hity;
-    ok                = ok && fabs(hitz) <= t.tolOz && (r2 >= t.tolOrmin2) && (r2 <= t.tolOrmax2);
-    ok                = ok && (hitx * ax + hity * ay) > 0.;
+    ok                = ok && dabs_le(hitz, t.tolOz) && dge(r2, t.tolOrmin2) && dle(r2, t.tolOrmax2);
+    ok                = ok && dgt(hitx * ax + hity * ay, 0.);
   } else {
-    ok = ok && (hitx * ax + hity * ay) >= 0.;
+    ok = ok && dge(hitx * ax + hity * ay, 0.);
   }
 }
 
@@ -227,34 +266,34 @@ __device__ __forceinline__ void tube_phi_plane(const TubeRec &t, double ax, doub
 __device__ __forceinline__ bool tube_moving_in_surface(const TubeRec &t, V3 p, V3 d, bool inner)
 {
   const double rho = perp2(p);
-  const bool zok   = fabs(p.z) < (t.z + kTolerance);
-  const bool on    = inner ? (rho >= t.tolOrmin2 && rho <= t.tolIrmin2 && zok)
-                        : (rho >= t.tolIrmax2 && rho <= t.tolOrmax2 && zok);
+  const bool zok   = dabs_lt(p.z, t.z + kTolerance);
+  const bool on    = inner ? (dge(rho, t.tolOrmin2) && dle(rho, t.tolIrmin2) && zok)
+                        : (dge(rho, t.tolIrmax2) && dle(rho, t.tolOrmax2) && zok);
   const V3 n = inner ? V3{-p.x, -p.y, 0.} : V3{p.x, p.y, 0.};
-  return on && (dot(d, n) <= 0.);
+  return on && dle(dot(d, n), 0.);
 }
 
 // TubeImplementation.h:352-396
 __device__ __forceinline__ void tube_classify(const TubeRec &t, V3 p, bool forInside, bool &cin, bool &cout)
 {
   const double absz = fabs(p.z);
-  cout              = absz > (forInside ? t.z + kHalfTolerance : t.z);
-  if (forInside) cin = absz < t.z - kHalfTolerance;
+  cout              = dgt(absz, forInside ? t.z + kHalfTolerance : t.z);
+  if (forInside) cin = dlt(absz, t.z - kHalfTolerance);
   if (cout) return;
   const double r2 = p.x * p.x + p.y * p.y;
   if (forInside) {
-    cout = r2 > t.rmax * (t.rmax + 2.0 * kTolerance);
-    cin  = cin && (r2 < fabs(t.rmax * (t.rmax - 2.0 * kTolerance)));
+    cout = dgt(r2, t.rmax * (t.rmax + 2.0 * kTolerance));
+    cin  = cin && dlt(r2, fabs(t.rmax * (t.rmax - 2.0 * kTolerance)));
   } else {
-    cout = r2 > t.rmax * t.rmax;
+    cout = dgt(r2, t.rmax * t.rmax);
   }
   if (cout) return;
   if (tube_rmin(t)) {
     if (forInside) {
-      cout = r2 <= fabs(t.rmin * (t.rmin - 2.0 * kTolerance));
-      cin  = cin && (r2 > t.rmin * (t.rmin + 2.0 * kTolerance));
+      cout = dle(r2, fabs(t.rmin * (t.rmin - 2.0 * kTolerance)));
+      cin  = cin && dgt(r2, t.rmin * (t.rmin + 2.0 * kTolerance));
     } else {
-      cout = r2 <= t.rmin * t.rmin;
+      cout = dle(r2, t.rmin * t.rmin);
     }
     if (cout) return;
   }
@@ -282,12 +321,12 @@ __device__ __forceinline__ bool tube_contains(const TubeRec &t, V3 p)
 static __device__ __noinline__ double tube_dist_in_kernel(const TubeRec &t, V3 point, V3 dir)
 {
   double distz = fabs(point.z) - t.z;
-  if (distz > kHalfTolerance && point.z * dir.z >= 0) return kInfLength;
+  if (dgt(distz, kHalfTolerance) && dge(point.z * dir.z, 0.)) return kInfLength;
   const double rsq   = point.x * point.x + point.y * point.y;
   const double rdotn = point.x * dir.x + point.y * dir.y;
-  if (rsq > t.tolIrmax2 && rdotn >= 0) return kInfLength;
-  bool inside = distz < -kHalfTolerance && rsq < t.tolIrmax2;
-  if (tube_rmin(t)) inside = inside && (rsq > t.tolIrmin2);
+  if (dgt(rsq, t.tolIrmax2) && dge(rdotn, 0.)) return kInfLength;
+  bool inside = dlt(distz, -kHalfTolerance) && dlt(rsq, t.tolIrmax2);
+  if (tube_rmin(t)) inside = inside && dgt(rsq, t.tolIrmin2);
   if (tube_phi(t) && inside) inside = tube_in_sector(t, point.x, point.y, false);
   if (inside) return -1.0;
 
@@ -296,8 +335,8 @@ static __device__ __noinline__ double tube_dist_in_kernel(const TubeRec &t, V3 p
   const double hitx = point.x + distz * dir.x;
   const double hity = point.y + distz * dir.y;
   const double r2   = hitx * hitx + hity * hity;
-  bool okz          = distz > -kHalfTolerance && (point.z * dir.z < 0) && (r2 <= t.rmax2);
-  if (tube_rmin(t)) okz = okz && (t.rmin2 <= r2);
+  bool okz          = dgt(distz, -kHalfTolerance) && dlt(point.z * dir.z, 0.) && dle(r2, t.rmax2);
+  if (tube_rmin(t)) okz = okz && dle(t.rmin2, r2);
   if (tube_phi(t) && okz) okz = tube_in_sector(t, hitx, hity, true);
   if (okz) distance = distz;
   bool done = okz;
@@ -315,22 +354,22 @@ static __device__ __noinline__ double tube_dist_in_kernel(const TubeRec &t, V3 p
   double dist_rmax;
   bool ok_rmax;
   tube_circle(t, b, crmax, point, dir, false, true, dist_rmax, ok_rmax);
-  if (ok_rmax && dist_rmax < distance) return dist_rmax;
+  if (ok_rmax && dlt(dist_rmax, distance)) return dist_rmax;
 
   if (tube_rmin(t)) {
     const double crmin = invnsq * (rsq - t.rmin2);
     double dist_rmin;
     bool ok_rmin;
     tube_circle(t, b, crmin, point, dir, true, true, dist_rmin, ok_rmin);
-    if (ok_rmin && dist_rmin < distance) distance = dist_rmin;
+    if (ok_rmin && dlt(dist_rmin, distance)) distance = dist_rmin;
   }
   if (tube_phi(t)) {
     double dist_phi;
     bool ok_phi;
     tube_phi_plane(t, t.a1x, t.a1y, t.w.n1x, t.w.n1y, point, dir, true, dist_phi, ok_phi);
-    if (ok_phi && dist_phi < distance) distance = dist_phi;
+    if (ok_phi && dlt(dist_phi, distance)) distance = dist_phi;
     tube_phi_plane(t, t.a2x, t.a2y, t.w.n2x, t.w.n2y, point, dir, true, dist_phi, ok_phi);
-    if (ok_phi && dist_phi < distance) distance = dist_phi;
+    if (ok_phi && dlt(dist_phi, distance)) distance = dist_phi;
   }
   return distance;
 }
@@ -340,7 +379,7 @@ __device__ __forceinline__ double tube_dist_in(const TubeRec &t, V3 p, V3 d)
 {
   const double ptDist = sqrt(p.x * p.x + p.y * p.y + p.z * p.z);
   double distToMove   = 0.;
-  if (ptDist > 100. * t.maxVal) {
+  if (dgt(ptDist, 100. * t.maxVal)) {
     distToMove = ptDist - 100. * t.maxVal;
     p          = V3{p.x + distToMove * d.x, p.y + distToMove * d.y, p.z + distToMove * d.z};
   }
@@ -350,15 +389,15 @@ __device__ __forceinline__ double tube_dist_in(const TubeRec &t, V3 p, V3 d)
 // TubeImplementation.h:601-697 DistanceToOut
 static __device__ __noinline__ double tube_dist_out(const TubeRec &t, V3 point, V3 dir)
 {
-  if (t.z - fabs(point.z) < -kHalfTolerance) return -1.;
+  if (dlt(t.z - fabs(point.z), -kHalfTolerance)) return -1.;
   const double rsq   = point.x * point.x + point.y * point.y;
   const double rdotn = dir.x * point.x + dir.y * point.y;
   double crmax       = rsq - t.rmax2;
   double crmin       = rsq;
-  if (crmax > 2.0 * kTolerance * t.rmax) return -1.;
+  if (dgt(crmax, 2.0 * kTolerance * t.rmax)) return -1.;
   if (tube_rmin(t)) {
     crmin -= t.rmin2;
-    if (crmin < -2.0 * kTolerance * t.rmin) return -1.;
+    if (dlt(crmin, -2.0 * kTolerance * t.rmin)) return -1.;
   }
   if (tube_phi(t)) {
     bool ci = false, co = false;
@@ -368,8 +407,8 @@ static __device__ __noinline__ double tube_dist_out(const TubeRec &t, V3 point, 
   double distance      = kInfLength;
   const double invdirz = 1. / nonzero(dir.z);
   double distz         = (t.z - point.z) * invdirz;
-  if (dir.z < 0) distz = (-t.z - point.z) * invdirz;
-  if (dir.z != 0. && distz < distance) distance = distz;
+  if (dlt(dir.z, 0.)) distz = (-t.z - point.z) * invdirz;
+  if (dne(dir.z, 0.) && dlt(distz, distance)) distance = distz;
   const double invnsq = 1. / nonzero(1. - dir.z * dir.z);
   const double b      = invnsq * rdotn;
   if (tube_rmin(t)) {
@@ -377,20 +416,20 @@ static __device__ __noinline__ double tube_dist_out(const TubeRec &t, V3 point, 
     bool ok_rmin;
     crmin *= invnsq;
     tube_circle(t, b, crmin, point, dir, false, false, dist_rmin, ok_rmin);
-    if (ok_rmin && dist_rmin < distance) distance = dist_rmin;
+    if (ok_rmin && dlt(dist_rmin, distance)) distance = dist_rmin;
   }
   double dist_rmax;
   bool ok_rmax;
   crmax *= invnsq;
   tube_circle(t, b, crmax, point, dir, true, false, dist_rmax, ok_rmax);
-  if (ok_rmax && dist_rmax < distance) distance = dist_rmax;
+  if (ok_rmax && dlt(dist_rmax, distance)) distance = dist_rmax;
   if (tube_phi(t)) {
     double dist_phi;
     bool ok_phi;
     tube_phi_plane(t, t.a1x, t.a1y, t.w.n1x, t.w.n1y, point, dir, false, dist_phi, ok_phi);
-    if (ok_phi && dist_phi < distance) distance = dist_phi;
+    if (ok_phi && dlt(dist_phi, distance)) distance = dist_phi;
     tube_phi_plane(t, t.a2x, t.a2y, t.w.n2x, t.w.n2y, point, dir, false, dist_phi, ok_phi);
-    if (ok_phi && dist_phi < distance) distance = dist_phi;
+    if (ok_phi && dlt(dist_phi, distance)) distance = dist_phi;
   }
   return distance;
 }
@@ -401,19 +440,19 @@ __device__ __forceinline__ double tube_safety_in(const TubeRec &t, V3 p)
   double safety         = fabs(p.z) - t.z;
   const double r        = sqrt(p.x * p.x + p.y * p.y);
   const double safermax = r - t.rmax;
-  if (safermax > safety) safety = safermax;
+  if (dgt(safermax, safety)) safety = safermax;
   if (tube_rmin(t)) {
     const double safermin = t.rmin - r;
-    if (safermin > safety) safety = safermin;
+    if (dgt(safermin, safety)) safety = safermin;
   }
   if (tube_phi(t)) {
     if (tube_in_sector(t, p.x, p.y, false)) return safety;
-    double safephi = t.dphi > kPi ? sqrt(p.x * p.x + p.y * p.y) : kInfLength;
+    double safephi = dgt(t.dphi, kPi) ? sqrt(p.x * p.x + p.y * p.y) : kInfLength;
     const double phi1 = p.x * t.a1y - p.y * t.a1x;
-    if (phi1 > -kHalfTolerance && phi1 < safephi) safephi = phi1;
+    if (dgt(phi1, -kHalfTolerance) && dlt(phi1, safephi)) safephi = phi1;
     const double phi2 = -(p.x * t.a2y - p.y * t.a2x);
-    if (phi2 > -kHalfTolerance && phi2 < safephi) safephi = phi2;
-    if (safephi < kInfLength && safephi > safety) safety = safephi;
+    if (dgt(phi2, -kHalfTolerance) && dlt(phi2, safephi)) safephi = phi2;
+    if (dlt(safephi, kInfLength) && dgt(safephi, safety)) safety = safephi;
   }
   return safety;
 }
@@ -424,26 +463,26 @@ __device__ __forceinline__ double tube_safety_out(const TubeRec &t, V3 p)
   double safety         = t.z - fabs(p.z);
   const double r        = sqrt(p.x * p.x + p.y * p.y);
   const double safermax = t.rmax - r;
-  if (safermax < safety) safety = safermax;
+  if (dlt(safermax, safety)) safety = safermax;
   if (tube_rmin(t)) {
     const double safermin = r - t.rmin;
-    if (safermin < safety) safety = safermin;
+    if (dlt(safermin, safety)) safety = safermin;
   }
   if (tube_phi(t)) {
     const double safephi = wedge_safety_out(t.w, p);
-    if (safephi < safety) safety = safephi;
+    if (dlt(safephi, safety)) safety = safephi;
   }
   return safety;
 }
 
 // ================================================================ Cone
-__device__ __forceinline__ bool cone_phi(const ConeRec &c) { return c.dphi < kTwoPi; }
-__device__ __forceinline__ bool cone_rmin(const ConeRec &c) { return c.rmin1 > 0 || c.rmin2 > 0; }
+__device__ __forceinline__ bool cone_phi(const ConeRec &c) { return dlt(c.dphi, kTwoPi); }
+__device__ __forceinline__ bool cone_rmin(const ConeRec &c) { return dgt(c.rmin1, 0.) || dgt(c.rmin2, 0.); }
 // ConeUtilities.h:113-131
 __device__ __forceinline__ double cone_radius(const ConeRec &c, double z, bool inner)
 {
-  if (inner) return (c.rmin1 == c.rmin2) ? c.rmin1 : c.innerSlope * z + c.innerOffset;
-  return (c.origRmax1 == c.origRmax2) ? c.origRmax1 : c.outerSlope * z + c.outerOffset;
+  if (inner) return deq(c.rmin1, c.rmin2) ? c.rmin1 : c.innerSlope * z + c.innerOffset;
+  return deq(c.origRmax1, c.origRmax2) ? c.origRmax1 : c.outerSlope * z + c.outerOffset;
 }
 // ConeUtilities.h:70-108 (kConeTolerance band)
 __device__ __forceinline__ bool cone_in_sector(const ConeRec &c, double x, double y, bool includeSurface)
@@ -451,18 +490,18 @@ __device__ __forceinline__ bool cone_in_sector(const ConeRec &c, double x, doubl
   const double startCheck = (-x * c.a1y) + (y * c.a1x);
   const double endCheck   = (-c.a2x * y) + (c.a2y * x);
   const double tol        = includeSurface ? -kConeTolerance : kConeTolerance;
-  if (c.dphi <= kPi) return (startCheck >= tol) && (endCheck >= tol);
-  return (startCheck >= tol) || (endCheck >= tol);
+  if (dle(c.dphi, kPi)) return dge(startCheck, tol) && dge(endCheck, tol);
+  return dge(startCheck, tol) || dge(endCheck, tol);
 }
 // ConeUtilities.h:176-200
 __device__ __forceinline__ V3 cone_normal(const ConeRec &c, V3 p, bool inner)
 {
   const double rho = sqrt(perp2(p));
   if (inner) {
-    if ((c.rmin1 == c.rmin2) && (c.rmin1 != 0.)) return V3{-p.x, -p.y, 0.};
+    if (deq(c.rmin1, c.rmin2) && dne(c.rmin1, 0.)) return V3{-p.x, -p.y, 0.};
     return V3{-p.x, -p.y, c.zNormInner * (rho * c.secRMin)};
   }
-  if ((c.rmax1 == c.rmax2) && (c.rmax1 != 0.)) return V3{p.x, p.y, 0.};
+  if (deq(c.rmax1, c.rmax2) && dne(c.rmax1, 0.)) return V3{p.x, p.y, 0.};
   return V3{p.x, p.y, c.zNormOuter * (rho * c.secRMax)};
 }
 // ConeUtilities.h:204-216
@@ -472,8 +511,8 @@ __device__ __forceinline__ bool cone_on_surface(const ConeRec &c, V3 p, bool inn
   const double coneRad  = cone_radius(c, p.z, inner);
   const double coneRad2 = coneRad * coneRad;
   const double tol      = inner ? c.innerTol : c.outerTol;
-  return (rho >= (coneRad2 - tol * coneRad)) && (rho <= (coneRad2 + tol * coneRad)) &&
-         (fabs(p.z) < (c.dz + kConeTolerance));
+  return dge(rho, coneRad2 - tol * coneRad) && dle(rho, coneRad2 + tol * coneRad) &&
+         dabs_lt(p.z, c.dz + kConeTolerance);
 }
 // ConeUtilities.h:146-174
 __device__ __forceinline__ void cone_phi_plane(const ConeRec &c, double ax, double ay, double nx, double ny, V3 pos,
@@ -481,10 +520,10 @@ __device__ __forceinline__ void cone_phi_plane(const ConeRec &c, double ax, doub
 {
   dist = kInfLength;
   const double dn = (dir.x * nx) + (dir.y * ny);
-  ok              = insectorCheck ? (dn > 0.) : (dn < 0.);
+  ok              = insectorCheck ? dgt(dn, 0.) : dlt(dn, 0.);
   const double dirDotXY = (dir.y * ax) - (dir.x * ay);
-  if (dirDotXY != 0) dist = ((ay * pos.x) - (ax * pos.y)) / nonzero(dirDotXY);
-  ok                = ok && (dist > -kConeTolerance);
+  if (dne(dirDotXY, 0.)) dist = ((ay * pos.x) - (ax * pos.y)) / nonzero(dirDotXY);
+  ok                = ok && dgt(dist, -kConeTolerance);
   const double hitx = pos.x + dist * dir.x;
   const double hity = pos.y + dist * dir.y;
   if (insectorCheck) {
@@ -492,10 +531,10 @@ __device__ __forceinline__ void cone_phi_plane(const ConeRec &c, double ax, doub
     const double r2   = (hitx * hitx) + (hity * hity);
     const double inR  = cone_radius(c, hitz, true) + kTolerance;
     const double outR = cone_radius(c, hitz, false) - kTolerance;
-    ok = ok && fabs(hitz) <= c.tolIz && (r2 >= inR * inR) && (r2 <= outR * outR);
-    ok = ok && ((hitx * ax) + (hity * ay)) > 0.;
+    ok = ok && dabs_le(hitz, c.tolIz) && dge(r2, inR * inR) && dle(r2, outR * outR);
+    ok = ok && dgt((hitx * ax) + (hity * ay), 0.);
   } else {
-    ok = ok && ((hitx * ax) + (hity * ay)) >= 0.;
+    ok = ok && dge((hitx * ax) + (hity * ay), 0.);
   }
 }
 
@@ -506,9 +545,9 @@ static __device__ __noinline__ bool cone_conical(const ConeRec &c, V3 point, V3 
   distance           = kInfLength;
   const bool onCone  = cone_on_surface(c, point, inner);
   const double dn    = dot(dir, cone_normal(c, point, inner));
-  if (onCone && fabs(dn) == 0.) return false;
+  if (onCone && deq(fabs(dn), 0.)) return false;
   if (onCone) {
-    const bool moving = forDistToIn ? (dn <= 0.) : (dn >= 0.);
+    const bool moving = forDistToIn ? dle(dn, 0.) : dge(dn, 0.);
     const bool insec  = cone_phi(c) ? cone_in_sector(c, point.x, point.y, true) : true;
     if (insec && moving) {
       distance = 0.;
@@ -519,12 +558,12 @@ static __device__ __noinline__ bool cone_conical(const ConeRec &c, V3 point, V3 
   const double pDotV2D = point.x * dir.x + point.y * dir.y;
   double a, b, cc;
   if (inner) {
-    if (c.rmin1 == c.rmin2) {
+    if (deq(c.rmin1, c.rmin2)) {
       b  = pDotV2D;
       a  = perp2(dir);
       cc = perp2(point) - c.rmin2 * c.rmin2;
     } else {
-      const double newPz = (c.rmin2 > c.rmin1) ? (point.z + c.dz + c.innerApex) * c.tanInnerApex
+      const double newPz = dgt(c.rmin2, c.rmin1) ? (point.z + c.dz + c.innerApex) * c.tanInnerApex
                                                : (point.z - c.dz - c.innerApex) * c.tanInnerApex;
       const double dirT  = dir.z * c.tanInnerApex;
       a                  = (dir.x * dir.x) + (dir.y * dir.y) - dirT * dirT;
@@ -533,23 +572,23 @@ static __device__ __noinline__ bool cone_conical(const ConeRec &c, V3 point, V3 
     }
     const double b2 = b * b;
     const double ac = a * cc;
-    if (b2 < ac) return false;
+    if (dlt(b2, ac)) return false;
     const double delta = sqrt(b2 - ac);
     if (forDistToIn) {
-      distance = (b >= 0.) ? (cc / nonzero(-b - delta)) : (-b + delta) / nonzero(a);
+      distance = dge(b, 0.) ? (cc / nonzero(-b - delta)) : (-b + delta) / nonzero(a);
     } else {
-      if (b == 0. && delta == 0.) return false;
-      distance = (b >= 0.) ? (-b - delta) / nonzero(a) : (cc / nonzero(-b + delta));
+      if (deq(b, 0.) && deq(delta, 0.)) return false;
+      distance = dge(b, 0.) ? (-b - delta) / nonzero(a) : (cc / nonzero(-b + delta));
     }
-    if (distance < 0.) return false;
-    ok = fabs(point.z + (dir.z * distance)) < c.dz;
+    if (dlt(distance, 0.)) return false;
+    ok = dabs_lt(point.z + (dir.z * distance), c.dz);
   } else {
-    if (c.origRmax1 == c.origRmax2) {
+    if (deq(c.origRmax1, c.origRmax2)) {
       a  = perp2(dir);
       b  = pDotV2D;
       cc = (perp2(point) - c.origRmax2 * c.origRmax2);
     } else {
-      const double newPz = (c.origRmax2 > c.origRmax1) ? (point.z + c.dz + c.outerApex) * c.tanOuterApex
+      const double newPz = dgt(c.origRmax2, c.origRmax1) ? (point.z + c.dz + c.outerApex) * c.tanOuterApex
                                                        : (point.z - c.dz - c.outerApex) * c.tanOuterApex;
       const double dirT  = dir.z * c.tanOuterApex;
       a                  = dir.x * dir.x + dir.y * dir.y - dirT * dirT;
@@ -557,25 +596,25 @@ static __device__ __noinline__ bool cone_conical(const ConeRec &c, V3 point, V3 
       cc                 = (perp2(point) - (newPz * newPz));
     }
     const double d2 = b * b - a * cc;
-    if (d2 < 0) return false;
+    if (dlt(d2, 0.)) return false;
     const double delta = sqrt(d2);
     if (forDistToIn) {
-      if (b == 0. && delta == 0.) return false;
-      distance = (b > 0.) ? (-b - delta) / nonzero(a) : (cc / nonzero(-b + delta));
-      ok       = fabs(point.z + (dir.z * distance)) < c.dz + kHalfTolerance;
+      if (deq(b, 0.) && deq(delta, 0.)) return false;
+      distance = dgt(b, 0.) ? (-b - delta) / nonzero(a) : (cc / nonzero(-b + delta));
+      ok       = dabs_lt(point.z + (dir.z * distance), c.dz + kHalfTolerance);
     } else {
-      distance = (b < 0.) ? (-b + delta) / nonzero(a) : (cc / nonzero(-b - delta));
-      ok       = distance > 0.;
+      distance = dlt(b, 0.) ? (-b + delta) / nonzero(a) : (cc / nonzero(-b - delta));
+      ok       = dgt(distance, 0.);
     }
-    if (distance < 0.) return false;
+    if (dlt(distance, 0.)) return false;
   }
   if (cone_phi(c)) {
     double hitx = 0, hity = 0;
-    if (distance < kInfLength) {
+    if (dlt(distance, kInfLength)) {
       hitx = point.x + distance * dir.x;
       hity = point.y + distance * dir.y;
     }
-    ok = ok && cone_in_sector(c, hitx, hity, true) && (distance < kInfLength);
+    ok = ok && cone_in_sector(c, hitx, hity, true) && dlt(distance, kInfLength);
   }
   return ok;
 }
@@ -584,25 +623,25 @@ static __device__ __noinline__ bool cone_conical(const ConeRec &c, V3 point, V3 
 __device__ __forceinline__ void cone_classify(const ConeRec &c, V3 p, bool forInside, bool &cin, bool &cout)
 {
   const double absz = fabs(p.z);
-  cout              = absz > (forInside ? c.dz + kConeTolerance : c.dz);
-  if (forInside) cin = absz < c.dz - kConeTolerance;
+  cout              = dgt(absz, forInside ? c.dz + kConeTolerance : c.dz);
+  if (forInside) cin = dlt(absz, c.dz - kConeTolerance);
   if (cout) return;
   const double r2   = p.x * p.x + p.y * p.y;
-  const double rmax = (c.origRmax1 == c.origRmax2) ? c.origRmax1 : c.outerSlope * p.z + c.outerOffset;
+  const double rmax = deq(c.origRmax1, c.origRmax2) ? c.origRmax1 : c.outerSlope * p.z + c.outerOffset;
   if (forInside) {
-    cout = r2 > rmax * (rmax + 2.0 * c.outerTol);
-    cin  = cin && (r2 < fabs(rmax * (rmax - 2.0 * c.outerTol)));
+    cout = dgt(r2, rmax * (rmax + 2.0 * c.outerTol));
+    cin  = cin && dlt(r2, fabs(rmax * (rmax - 2.0 * c.outerTol)));
   } else {
-    cout = r2 > rmax * rmax;
+    cout = dgt(r2, rmax * rmax);
   }
   if (cout) return;
   if (cone_rmin(c)) {
     const double rmin = c.innerSlope * p.z + c.innerOffset;
     if (forInside) {
-      cout = r2 <= fabs(rmin * (rmin - 2.0 * c.innerTol));
-      cin  = cin && (r2 > rmin * (rmin + 2.0 * c.innerTol));
+      cout = dle(r2, fabs(rmin * (rmin - 2.0 * c.innerTol)));
+      cin  = cin && dgt(r2, rmin * (rmin + 2.0 * c.innerTol));
     } else {
-      cout = r2 <= rmin * rmin;
+      cout = dle(r2, rmin * rmin);
     }
     if (cout) return;
   }
@@ -630,16 +669,16 @@ __device__ __forceinline__ bool cone_contains(const ConeRec &c, V3 p)
 static __device__ __noinline__ double cone_dist_in(const ConeRec &c, V3 point, V3 dir)
 {
   double distz = fabs(point.z) - c.dz;
-  if ((distz > kConeTolerance && (point.z * dir.z) >= 0.) || (fabs(distz) < kConeTolerance && (point.z * dir.z) > 0.))
+  if ((dgt(distz, kConeTolerance) && dge(point.z * dir.z, 0.)) || (dabs_lt(distz, kConeTolerance) && dgt(point.z * dir.z, 0.)))
     return kInfLength;
   const double outerRad = cone_radius(c, point.z, false);
   const double rsq      = perp2(point);
   const double outerIn  = fabs(outerRad * (outerRad - 2.0 * c.outerTol));
-  if (rsq > outerIn && dot(dir, cone_normal(c, point, false)) >= 0.) return kInfLength;
-  bool inside = distz < -kConeTolerance && rsq < outerIn;
+  if (dgt(rsq, outerIn) && dge(dot(dir, cone_normal(c, point, false)), 0.)) return kInfLength;
+  bool inside = dlt(distz, -kConeTolerance) && dlt(rsq, outerIn);
   if (cone_rmin(c)) {
     const double innerRad = cone_radius(c, point.z, true);
-    inside                = inside && (rsq > innerRad * (innerRad + 2.0 * c.innerTol));
+    inside                = inside && dgt(rsq, innerRad * (innerRad + 2.0 * c.innerTol));
   }
   if (cone_phi(c)) inside = inside && cone_in_sector(c, point.x, point.y, false);
   if (inside) return -1.0;
@@ -649,30 +688,30 @@ static __device__ __noinline__ double cone_dist_in(const ConeRec &c, V3 point, V
   const double hitx = point.x + distz * dir.x;
   const double hity = point.y + distz * dir.y;
   const double r2   = (hitx * hitx) + (hity * hity);
-  bool top          = (point.z >= c.tolIz) && (r2 <= c.sqRmax2 + kTolerance);
-  bool bottom       = (point.z <= -c.tolIz) && (r2 <= c.sqRmax1 + kTolerance);
+  bool top          = dge(point.z, c.tolIz) && dle(r2, c.sqRmax2 + kTolerance);
+  bool bottom       = dle(point.z, -c.tolIz) && dle(r2, c.sqRmax1 + kTolerance);
   bool okz          = top || bottom;
   if (cone_rmin(c)) {
-    top    = top && (r2 >= c.sqRmin2 - kTolerance);
-    bottom = bottom && (r2 >= c.sqRmin1 - kTolerance);
+    top    = top && dge(r2, c.sqRmin2 - kTolerance);
+    bottom = bottom && dge(r2, c.sqRmin1 - kTolerance);
     okz    = okz && (top || bottom);
   }
   if (cone_phi(c)) okz = okz && cone_in_sector(c, hitx, hity, true);
   if (okz) return distz;
 
   double dist_rOuter;
-  if (cone_conical(c, point, dir, true, false, dist_rOuter) && dist_rOuter < distance) return dist_rOuter;
+  if (cone_conical(c, point, dir, true, false, dist_rOuter) && dlt(dist_rOuter, distance)) return dist_rOuter;
   if (cone_rmin(c)) {
     double dist_rInner;
-    if (cone_conical(c, point, dir, true, true, dist_rInner) && dist_rInner < distance) distance = dist_rInner;
+    if (cone_conical(c, point, dir, true, true, dist_rInner) && dlt(dist_rInner, distance)) distance = dist_rInner;
   }
   if (cone_phi(c)) {
     double dist_phi;
     bool ok_phi;
     cone_phi_plane(c, c.a1x, c.a1y, c.w.n1x, c.w.n1y, point, dir, true, dist_phi, ok_phi);
-    if (ok_phi && dist_phi < distance) distance = dist_phi;
+    if (ok_phi && dlt(dist_phi, distance)) distance = dist_phi;
     cone_phi_plane(c, c.a2x, c.a2y, c.w.n2x, c.w.n2y, point, dir, true, dist_phi, ok_phi);
-    if (ok_phi && dist_phi < distance) distance = dist_phi;
+    if (ok_phi && dlt(dist_phi, distance)) distance = dist_phi;
   }
   return distance;
 }
@@ -683,40 +722,40 @@ static __device__ __noinline__ double cone_dist_out(const ConeRec &c, V3 point, 
   const double distz    = fabs(point.z) - c.dz;
   const double rsq      = perp2(point);
   const double outerRad = cone_radius(c, point.z, false);
-  if (distz > kConeTolerance || rsq > outerRad * (outerRad + 2.0 * c.outerTol)) return -1.0;
+  if (dgt(distz, kConeTolerance) || dgt(rsq, outerRad * (outerRad + 2.0 * c.outerTol))) return -1.0;
   if (cone_rmin(c)) {
     const double innerRad = cone_radius(c, point.z, true);
-    if (rsq < fabs(innerRad * (innerRad - 2.0 * c.innerTol))) return -1.0;
+    if (dlt(rsq, fabs(innerRad * (innerRad - 2.0 * c.innerTol)))) return -1.0;
   }
   // (no phi-sector rejection on the scalar path, see ConeImplementation.h:292-296)
-  const bool up   = dir.z > 0.;
-  const bool down = dir.z < 0.;
-  if ((up && point.z > 0. && fabs(distz) < kConeTolerance) || (down && point.z < 0. && fabs(distz) < kConeTolerance))
+  const bool up   = dgt(dir.z, 0.);
+  const bool down = dlt(dir.z, 0.);
+  if ((up && dgt(point.z, 0.) && dabs_lt(distz, kConeTolerance)) || (down && dlt(point.z, 0.) && dabs_lt(distz, kConeTolerance)))
     return distz;
   double distance      = kInfLength;
   const double dirZInv = 1. / nonzero(dir.z);
   if (up) distance = (c.dz - point.z) * dirZInv;
   if (down) distance = (-c.dz - point.z) * dirZInv;
   double dist_rOuter;
-  if (cone_conical(c, point, dir, false, false, dist_rOuter) && dist_rOuter < distance) distance = dist_rOuter;
+  if (cone_conical(c, point, dir, false, false, dist_rOuter) && dlt(dist_rOuter, distance)) distance = dist_rOuter;
   if (cone_rmin(c)) {
     double dist_rInner;
-    if (cone_conical(c, point, dir, false, true, dist_rInner) && dist_rInner < distance) distance = dist_rInner;
+    if (cone_conical(c, point, dir, false, true, dist_rInner) && dlt(dist_rInner, distance)) distance = dist_rInner;
   }
   if (cone_phi(c)) {
     const bool onStart = wedge_on_surface(c.w.a1x, c.w.a1y, c.w.n1x, c.w.n1y, point);
     const bool onEnd   = wedge_on_surface(c.w.a2x, c.w.a2y, c.w.n2x, c.w.n2y, point);
     const double dn1   = dir.x * (-c.w.n1x) + dir.y * (-c.w.n1y) + dir.z * (-0.0);
     const double dn2   = dir.x * (-c.w.n2x) + dir.y * (-c.w.n2y) + dir.z * (-0.0);
-    if ((onStart && dn1 > 0.) || (onEnd && dn2 > 0.)) return 0.;
+    if ((onStart && dgt(dn1, 0.)) || (onEnd && dgt(dn2, 0.))) return 0.;
     double dist_phi;
     bool ok_phi;
     cone_phi_plane(c, c.a1x, c.a1y, c.w.n1x, c.w.n1y, point, dir, false, dist_phi, ok_phi);
-    if (ok_phi && dist_phi < distance) distance = dist_phi;
+    if (ok_phi && dlt(dist_phi, distance)) distance = dist_phi;
     cone_phi_plane(c, c.a2x, c.a2y, c.w.n2x, c.w.n2y, point, dir, false, dist_phi, ok_phi);
-    if (ok_phi && dist_phi < distance) distance = dist_phi;
+    if (ok_phi && dlt(dist_phi, distance)) distance = dist_phi;
   }
-  if (distance < 0. && fabs(distance) < kTolerance) distance = 0.;
+  if (dlt(distance, 0.) && dabs_lt(distance, kTolerance)) distance = 0.;
   return distance;
 }
 
@@ -734,10 +773,10 @@ __device__ __forceinline__ double cone_safety_in(const ConeRec &c, V3 p)
   const double distz    = fabs(p.z) - c.dz;
   const double outerRad = cone_radius(c, p.z, false);
   const double rsq      = perp2(p);
-  bool inside           = distz < -kConeTolerance && rsq < fabs(outerRad * (outerRad - 2.0 * c.outerTol));
+  bool inside           = dlt(distz, -kConeTolerance) && dlt(rsq, fabs(outerRad * (outerRad - 2.0 * c.outerTol)));
   if (cone_rmin(c)) {
     const double innerRad = cone_radius(c, p.z, true);
-    inside                = inside && (rsq > innerRad * (innerRad + 2.0 * c.innerTol));
+    inside                = inside && dgt(rsq, innerRad * (innerRad + 2.0 * c.innerTol));
   }
   if (cone_phi(c) && inside) inside = cone_in_sector(c, p.x, p.y, false);
   if (inside) return -1.0;
@@ -745,7 +784,7 @@ __device__ __forceinline__ double cone_safety_in(const ConeRec &c, V3 p)
   const double safeInner = cone_rmin(c) ? -cone_safe_conical(c, p, true) : -kInfLength;
   double safety          = dmax(distz, dmax(safeOuter, safeInner));
   if (cone_phi(c)) safety = dmax(wedge_safety_in(c.w, p), safety);
-  if (fabs(safety) < kTolerance) safety = 0.;
+  if (dabs_lt(safety, kTolerance)) safety = 0.;
   return safety;
 }
 
@@ -755,17 +794,17 @@ __device__ __forceinline__ double cone_safety_out(const ConeRec &c, V3 p)
   const double distz    = fabs(p.z) - c.dz;
   const double rsq      = perp2(p);
   const double outerRad = cone_radius(c, p.z, false);
-  bool outside          = distz > kConeTolerance || rsq > outerRad * (outerRad + 2.0 * c.outerTol);
+  bool outside          = dgt(distz, kConeTolerance) || dgt(rsq, outerRad * (outerRad + 2.0 * c.outerTol));
   if (cone_rmin(c)) {
     const double innerRad = cone_radius(c, p.z, true);
-    outside               = outside || rsq < fabs(innerRad * (innerRad - 2.0 * c.innerTol));
+    outside               = outside || dlt(rsq, fabs(innerRad * (innerRad - 2.0 * c.innerTol)));
   }
   if (outside) return -1.0;
   const double safeOuter = cone_safe_conical(c, p, false);
   const double safeInner = cone_rmin(c) ? cone_safe_conical(c, p, true) : kInfLength;
   double safety          = dmin(c.dz - fabs(p.z), dmin(safeOuter, safeInner));
   if (cone_phi(c)) safety = dmin(wedge_safety_out(c.w, p), safety);
-  if (fabs(safety) < kTolerance) safety = 0.;
+  if (dabs_lt(safety, kTolerance)) safety = 0.;
   return safety;
 }
 

@@ -15,15 +15,15 @@ constexpr double kTiny = 1e-30;
 __device__ __forceinline__ void trd_classify(const TrdRec &t, V3 p, bool surfaceT, bool &cin, bool &cout)
 {
   const double pzPlusDz = p.z + t.dz;
-  cout                  = fabs(p.z) > (surfaceT ? t.dz + kHalfTolerance : t.dz);
-  if (surfaceT) cin = fabs(p.z) < t.dz - kHalfTolerance;
+  cout                  = dgt(fabs(p.z), surfaceT ? t.dz + kHalfTolerance : t.dz);
+  if (surfaceT) cin = dabs_lt(p.z, t.dz - kHalfTolerance);
   const double cx = t.x2minusx1 * pzPlusDz - (2.0 * t.dz) * (fabs(p.x) - t.dx1);
   const double cy = t.y2minusy1 * pzPlusDz - (2.0 * t.dz) * (fabs(p.y) - t.dy1);
   if (surfaceT) {
-    cout = cout || (cx < -t.tolx) || (cy < -t.toly);
-    cin  = cin && (cx > t.tolx) && (cy > t.toly);
+    cout = cout || dlt(cx, -t.tolx) || dlt(cy, -t.toly);
+    cin  = cin && dgt(cx, t.tolx) && dgt(cy, t.toly);
   } else {
-    cout = cout || (cx < 0) || (cy < 0);
+    cout = cout || dlt(cx, 0.) || dlt(cy, 0.);
   }
 }
 __device__ __forceinline__ int trd_inside(const TrdRec &t, V3 p)
@@ -56,34 +56,34 @@ __device__ __forceinline__ bool trd_face(const TrdRec &t, V3 pos, V3 dir, bool f
     dirV = -dirV;
   }
   const double ndotv = dirV + fV * dir.z;
-  if (toInside ? !(ndotv < 0.) : !(ndotv > 0.)) return false;
+  if (toInside ? !dlt(ndotv, 0.) : !dgt(ndotv, 0.)) return false;
   const double alongZ = 2.0 * t.dz;
   dist = (alongZ * (posV - v1) - alongV * (pos.z + t.dz)) / (dir.z * alongV - dirV * alongZ + kTiny);
-  if (!(dist > -kHalfTolerance)) return false;
+  if (!dgt(dist, -kHalfTolerance)) return false;
   const double hitz = pos.z + dist * dir.z;
   const double hitk = posK + dist * dirK;
-  const bool ok     = fabs(hitz) <= t.dz && fabs(hitk) <= halfK - fK * hitz;
-  if (ok && fabs(dist) < kHalfTolerance) dist = 0.0;
+  const bool ok     = dabs_le(hitz, t.dz) && dabs_le(hitk, halfK - fK * hitz);
+  if (ok && dabs_lt(dist, kHalfTolerance)) dist = 0.0;
   return ok;
 }
-__device__ __forceinline__ double trd_clamp(double d) { return fabs(d) < kHalfTolerance ? 0.0 : d; }
+__device__ __forceinline__ double trd_clamp(double d) { return dabs_lt(d, kHalfTolerance) ? 0.0 : d; }
 // TrdImplementation.h:288-370
 static __device__ __noinline__ double trd_dist_in(const TrdRec &t, V3 p, V3 d)
 {
   double distance  = kInfLength;
-  const bool inz   = fabs(p.z) < t.dz - kHalfTolerance;
+  const bool inz   = dabs_lt(p.z, t.dz - kHalfTolerance);
   double distx     = t.halfx1plusx2 - t.fx * p.z;
-  const bool inx   = (distx - fabs(p.x)) * t.calfx > kHalfTolerance;
-  const bool vary  = t.dy1 != t.dy2;
+  const bool inx   = dgt((distx - fabs(p.x)) * t.calfx, kHalfTolerance);
+  const bool vary  = dne(t.dy1, t.dy2);
   double disty     = vary ? t.halfy1plusy2 - t.fy * p.z : fabs(p.y) - t.dy1;
-  const bool iny   = vary ? (disty - fabs(p.y)) * t.calfy > kHalfTolerance : disty < -kHalfTolerance;
+  const bool iny   = vary ? dgt((disty - fabs(p.y)) * t.calfy, kHalfTolerance) : dlt(disty, -kHalfTolerance);
   if (inx && iny && inz) return -1.;
-  if (p.z * d.z < 0. && !inz) {
+  if (dlt(p.z * d.z, 0.) && !inz) {
     const double distz = (fabs(p.z) - t.dz) / fabs(d.z);
     const double hitx  = fabs(p.x + distz * d.x);
     const double hity  = fabs(p.y + distz * d.y);
-    const bool okzt    = p.z > (t.dz - kHalfTolerance) && hitx <= t.dx2 && hity <= t.dy2;
-    const bool okzb    = p.z < (-t.dz + kHalfTolerance) && hitx <= t.dx1 && hity <= t.dy1;
+    const bool okzt    = dgt(p.z, t.dz - kHalfTolerance) && dle(hitx, t.dx2) && dle(hity, t.dy2);
+    const bool okzb    = dlt(p.z, -t.dz + kHalfTolerance) && dle(hitx, t.dx1) && dle(hity, t.dy1);
     if (okzt || okzb) return trd_clamp(distz);
   }
   bool okx = false;
@@ -102,7 +102,7 @@ static __device__ __noinline__ double trd_dist_in(const TrdRec &t, V3 p, V3 d)
       const double zhit = p.z + disty * d.z;
       const double xhit = p.x + disty * d.x;
       const double dx   = t.halfx1plusx2 - t.fx * zhit;
-      if (p.y * d.y < 0 && disty > -kHalfTolerance && fabs(xhit) < dx && fabs(zhit) < t.dz) distance = disty;
+      if (dlt(p.y * d.y, 0.) && dgt(disty, -kHalfTolerance) && dabs_lt(xhit, dx) && dabs_lt(zhit, t.dz)) distance = disty;
     }
   }
   return trd_clamp(distance);
@@ -111,19 +111,19 @@ static __device__ __noinline__ double trd_dist_in(const TrdRec &t, V3 p, V3 d)
 static __device__ __noinline__ double trd_dist_out(const TrdRec &t, V3 p, V3 d)
 {
   const double invdir = 1. / fabs(d.z + kTiny);
-  const bool vary     = t.dy1 != t.dy2;
+  const bool vary     = dne(t.dy1, t.dy2);
   double distx        = t.halfx1plusx2 - t.fx * p.z;
   double disty        = vary ? t.halfy1plusy2 - t.fy * p.z : t.dy1 - fabs(p.y);
-  const bool out      = (t.dz - fabs(p.z) < -kHalfTolerance) || ((distx - fabs(p.x)) * t.calfx < -kHalfTolerance) ||
-                   (vary ? ((disty - fabs(p.y)) * t.calfy < -kHalfTolerance) : (disty < -kHalfTolerance));
+  const bool out      = dlt(t.dz - fabs(p.z), -kHalfTolerance) || dlt((distx - fabs(p.x)) * t.calfx, -kHalfTolerance) ||
+                   (vary ? dlt((disty - fabs(p.y)) * t.calfy, -kHalfTolerance) : dlt(disty, -kHalfTolerance));
   if (out) return -1.;
-  if (d.z > 0.) {
+  if (dgt(d.z, 0.)) {
     const double distz = (t.dz - p.z) * invdir;
-    if (fabs(p.x + distz * d.x) <= t.dx2 && fabs(p.y + distz * d.y) <= t.dy2) return trd_clamp(distz);
+    if (dabs_le(p.x + distz * d.x, t.dx2) && dabs_le(p.y + distz * d.y, t.dy2)) return trd_clamp(distz);
   }
-  if (d.z < 0.) {
+  if (dlt(d.z, 0.)) {
     const double distz = (p.z + t.dz) * invdir;
-    if (fabs(p.x + distz * d.x) <= t.dx1 && fabs(p.y + distz * d.y) <= t.dy1) return trd_clamp(distz);
+    if (dabs_le(p.x + distz * d.x, t.dx1) && dabs_le(p.y + distz * d.y, t.dy1)) return trd_clamp(distz);
   }
   if (trd_face(t, p, d, false, false, false, distx)) return trd_clamp(distx);
   if (trd_face(t, p, d, false, true, false, distx)) return trd_clamp(distx);
@@ -132,12 +132,12 @@ static __device__ __noinline__ double trd_dist_out(const TrdRec &t, V3 p, V3 d)
     if (trd_face(t, p, d, true, false, false, disty)) return trd_clamp(disty);
     if (trd_face(t, p, d, true, true, false, disty)) distance = disty;
   } else {
-    const double plane = d.y < 0. ? -t.dy1 : t.dy1;
+    const double plane = dlt(d.y, 0.) ? -t.dy1 : t.dy1;
     disty              = (plane - p.y) / d.y;
     const double zhit  = p.z + disty * d.z;
     const double xhit  = p.x + disty * d.x;
     const double dx    = t.halfx1plusx2 - t.fx * zhit;
-    if (fabs(xhit) < dx && fabs(zhit) < t.dz) distance = disty;
+    if (dabs_lt(xhit, dx) && dabs_lt(zhit, t.dz)) distance = disty;
   }
   return trd_clamp(distance);
 }
@@ -147,14 +147,14 @@ __device__ __forceinline__ double trd_safety(const TrdRec &t, V3 p, bool inside)
   double dist        = t.dz - fabs(p.z);
   const double distx = t.halfx1plusx2 - t.fx * p.z;
   const double safx  = (distx - fabs(p.x)) * t.calfx;
-  if (distx >= 0 && safx < dist) dist = safx;
-  if (t.dy1 != t.dy2) {
+  if (dge(distx, 0.) && dlt(safx, dist)) dist = safx;
+  if (dne(t.dy1, t.dy2)) {
     const double disty = t.halfy1plusy2 - t.fy * p.z;
     const double safy  = (disty - fabs(p.y)) * t.calfy;
-    if (disty >= 0 && safy < dist) dist = safy;
+    if (dge(disty, 0.) && dlt(safy, dist)) dist = safy;
   } else {
     const double safy = t.dy1 - fabs(p.y);
-    if (safy < dist) dist = safy;
+    if (dlt(safy, dist)) dist = safy;
   }
   return inside ? dist : -dist;
 }
@@ -174,9 +174,9 @@ struct PolyconeView {
   // PolyconeStruct.h:246-253 GetSectionIndex
   __device__ int index(double zp) const
   {
-    if (zp < z(0)) return -1;
+    if (dlt(zp, z(0))) return -1;
     for (int i = 0; i < nsec; ++i)
-      if (zp >= z(i) && zp <= z(i + 1)) return i;
+      if (dge(zp, z(i)) && dle(zp, z(i + 1))) return i;
     return -2;
   }
 };
@@ -231,14 +231,14 @@ static __device__ __noinline__ double polycone_dist_in(const PolyconeRec &rec, V
 {
   const PolyconeView v(rec);
   double distance = kInfLength;
-  int increment   = (d.z > 0) ? 1 : -1;
-  if (fabs(d.z) < kTolerance) increment = 0;
+  int increment   = dgt(d.z, 0.) ? 1 : -1;
+  if (dabs_lt(d.z, kTolerance)) increment = 0;
   int index = v.index(p.z);
   if (index == -1) index = 0;
   if (index == -2) index = v.nsec - 1;
   do {
     distance = cone_dist_in(v.cone(index), v.local(p, index), d);
-    if (distance < kInfLength || !increment) break;
+    if (dlt(distance, kInfLength) || !increment) break;
     index += increment;
   } while (index >= 0 && index < v.nsec);
   return distance;
@@ -264,12 +264,12 @@ static __device__ __noinline__ double polycone_dist_out(const PolyconeRec &rec, 
   if (index < 0) return 0.;
   if (cone_inside(v.cone(index), v.local(point, index)) == kOutside) return -1;
   double total  = 0.;
-  int increment = (dir.z > 0) ? 1 : -1;
-  if (fabs(dir.z) < kTolerance) increment = 0;
+  int increment = dgt(dir.z, 0.) ? 1 : -1;
+  if (dabs_lt(dir.z, kTolerance)) increment = 0;
   int istep = 0;
   V3 pn     = point;
   do {
-    if ((total != 0) || (istep < 2)) {
+    if (dne(total, 0.) || (istep < 2)) {
       pn = V3{point.x + total * dir.x, point.y + total * dir.y, point.z + total * dir.z};
       pn.z -= v.shift(index);
       if (cone_inside(v.cone(index), pn) == kOutside) break;
@@ -278,8 +278,8 @@ static __device__ __noinline__ double polycone_dist_out(const PolyconeRec &rec, 
     }
     istep++;
     const double dist = cone_dist_out(v.cone(index), pn, dir);
-    if (dist == -1) return kInfLength;
-    if (fabs(dist) < 0.5 * kTolerance) {
+    if (deq(dist, -1.)) return kInfLength;
+    if (dabs_lt(dist, 0.5 * kTolerance)) {
       int index1 = index;
       if ((index > 0) && (index < v.nsec - 1)) {
         index1 += increment;
@@ -308,20 +308,20 @@ static __device__ __noinline__ double polycone_safety_in(const PolyconeRec &rec,
     index = (index == -1) ? 0 : v.nsec - 1;
   }
   double safety = cone_safety_in(v.cone(index), v.local(p, index));
-  if (needZ || safety < kTolerance) return safety;
+  if (needZ || dlt(safety, kTolerance)) return safety;
   double minSafety = safety;
   double zbase     = v.z(index + 1);
   for (int i = index + 1; i < v.nsec; ++i) {
-    if (v.z(i) - zbase >= minSafety) break;
+    if (dge(v.z(i) - zbase, minSafety)) break;
     safety = cone_safety_in(v.cone(i), v.local(p, i));
-    if (safety < minSafety) minSafety = safety;
+    if (dlt(safety, minSafety)) minSafety = safety;
   }
   if (index > 0) {
     zbase = v.z(index - 1);
     for (int i = index - 1; i >= 0; --i) {
-      if (zbase - v.z(i) >= minSafety) break;
+      if (dge(zbase - v.z(i), minSafety)) break;
       safety = cone_safety_in(v.cone(i), v.local(p, i));
-      if (safety < minSafety) minSafety = safety;
+      if (dlt(safety, minSafety)) minSafety = safety;
     }
   }
   return minSafety;
@@ -336,19 +336,19 @@ static __device__ __noinline__ double polycone_safety_out(const PolyconeRec &rec
   const int index = v.index(p.z);
   if (index < 0) return -1;
   double minSafety = cone_safety_out(v.cone(index), v.local(p, index));
-  if (minSafety == kInfLength || minSafety < kTolerance) return 0.;
+  if (deq(minSafety, kInfLength) || dlt(minSafety, kTolerance)) return 0.;
   double zbase = v.z(index + 1);
   for (int i = index + 1; i < v.nsec; ++i) {
-    if (v.z(i) - zbase >= minSafety) break;
+    if (dge(v.z(i) - zbase, minSafety)) break;
     const double s = cone_safety_in(v.cone(i), v.local(p, i));
-    if (s < minSafety) minSafety = s;
+    if (dlt(s, minSafety)) minSafety = s;
   }
   if (index > 0) {
     zbase = v.z(index - 1);
     for (int i = index - 1; i >= 0; --i) {
-      if (zbase - v.z(i) >= minSafety) break;
+      if (dge(zbase - v.z(i), minSafety)) break;
       const double s = cone_safety_in(v.cone(i), v.local(p, i));
-      if (s < minSafety) minSafety = s;
+      if (dlt(s, minSafety)) minSafety = s;
     }
   }
   return minSafety;
