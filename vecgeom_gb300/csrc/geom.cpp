@@ -1107,8 +1107,30 @@ int Geometry::upload(std::string &err)
       for (int k = 0; k < 3; ++k) d[2 + k] = round_down(s.lo[k]), d[5 + k] = round_up(s.hi[k]);
     }
   }
+  // per prim slot: box, placed volume, descriptor and FP32 placement in one record
+  std::vector<LeafRec> leaf_rec(daughters.size());
+  for (size_t l = 0; l < lvs.size(); ++l) {
+    if (lv_bvh[l] < 0) continue;
+    const int32_t base = lv_dstart[l];
+    for (int32_t k = 0; k < lv_nd[l]; ++k) {
+      const size_t slot  = (size_t)base + k;
+      const int32_t prim = prim_id[slot];
+      const int32_t pv   = daughters[(size_t)base + prim];
+      LeafRec &r         = leaf_rec[slot];
+      std::memset(&r, 0, sizeof(r));
+      for (int c = 0; c < 3; ++c) {
+        r.lo[c] = prim_box_f[6 * ((size_t)base + prim) + c];
+        r.hi[c] = prim_box_f[6 * ((size_t)base + prim) + 3 + c];
+      }
+      r.pv = pv;
+      std::memcpy(r.lb, &lbd[8 * (size_t)lvs[pvs[pv].lv].shape], sizeof(r.lb));
+      const Xform &m = pvs[pv].xf.m;
+      for (int c = 0; c < 3; ++c) r.t[c] = m.t[c];
+      for (int c = 0; c < 9; ++c) r.r[c] = (float)m.r[c];
+    }
+  }
   const size_t o_pbx = a.add(prim_box), o_nf = a.add(node_f), o_pbf = a.add(prim_box_f), o_nav = a.add(nav);
-  const size_t o_lbd = a.add(lbd);
+  const size_t o_lbd = a.add(lbd), o_lrec = a.add(leaf_rec);
   shape_lbd_host     = lbd;
 
   cudaError_t e = cudaGetDevice(&device);
@@ -1146,6 +1168,7 @@ int Geometry::upload(std::string &err)
   dev.lv_depth    = reinterpret_cast<const int32_t *>(P(o_lvdp));
   dev.dau_slot3   = reinterpret_cast<const int32_t *>(P(o_ds3));
   dev.shape_lbd   = reinterpret_cast<const float *>(P(o_lbd));
+  dev.leaf_rec    = reinterpret_cast<const LeafRec *>(P(o_lrec));
   dev.world_pv    = world;
   dev.max_depth   = max_depth;
   dev.n_pv        = (int32_t)pvs.size();

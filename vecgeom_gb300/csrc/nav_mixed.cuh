@@ -113,20 +113,44 @@ __device__ __forceinline__ float shell_lb(float rmin, float rmax, float zlo, flo
 // kBoxPad of the FP32 one) is strictly inside the box at t0, so the box's DistanceToIn is a
 // hit (entry before exit, exit ahead, the far planes ahead by more than kHalfTolerance) at a
 // distance <= t0; the bound adds the FP32 rounding of t0 and 1 um.
-__device__ __forceinline__ float daughter_lb(const DevGeom &g, const ShapeLB *lbs, int pv, V3 p, V3 d, float &ub)
+// The record of a prim slot: box and placed volume (first 32 bytes).
+__device__ __forceinline__ void leaf_box(const LeafRec *rp, float lo[3], float hi[3], int &pv)
+{
+  const float4 a = __ldg(reinterpret_cast<const float4 *>(rp));
+  const float4 b = __ldg(reinterpret_cast<const float4 *>(rp) + 1);
+  lo[0] = a.x, lo[1] = a.y, lo[2] = a.z, hi[0] = a.w, hi[1] = b.x, hi[2] = b.y;
+  pv = __float_as_int(b.z);
+}
+__device__ __forceinline__ ShapeLB leaf_lb(const LeafRec *rp)
+{
+  const float4 a = __ldg(reinterpret_cast<const float4 *>(rp) + 2);
+  const float4 b = __ldg(reinterpret_cast<const float4 *>(rp) + 3);
+  return ShapeLB{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+}
+// p - t in FP64 rounded to FP32, then the FP32 rotation (the placement's rotation rounded
+// entry by entry), for a point; the rotation alone for a direction.
+__device__ __forceinline__ F3 leaf_local_point(const LeafRec *rp, V3 p)
+{
+  const F3 q{(float)(p.x - __ldg(&rp->t[0])), (float)(p.y - __ldg(&rp->t[1])), (float)(p.z - __ldg(&rp->t[2]))};
+  const float *r = rp->r;
+  return F3{fmaf(q.x, __ldg(r + 0), fmaf(q.y, __ldg(r + 3), q.z * __ldg(r + 6))),
+            fmaf(q.x, __ldg(r + 1), fmaf(q.y, __ldg(r + 4), q.z * __ldg(r + 7))),
+            fmaf(q.x, __ldg(r + 2), fmaf(q.y, __ldg(r + 5), q.z * __ldg(r + 8)))};
+}
+__device__ __forceinline__ F3 leaf_local_dir(const LeafRec *rp, F3 dd)
+{
+  const float *r = rp->r;
+  return F3{fmaf(dd.x, __ldg(r + 0), fmaf(dd.y, __ldg(r + 3), dd.z * __ldg(r + 6))),
+            fmaf(dd.x, __ldg(r + 1), fmaf(dd.y, __ldg(r + 4), dd.z * __ldg(r + 7))),
+            fmaf(dd.x, __ldg(r + 2), fmaf(dd.y, __ldg(r + 5), dd.z * __ldg(r + 8)))};
+}
+
+__device__ __forceinline__ float daughter_lb(const LeafRec *rp, V3 p, V3 d, float &ub)
 {
   ub = INFINITY;
-  const Xform &m = g.pv_xf[pv];
-  const F3 q{(float)(p.x - m.t[0]), (float)(p.y - m.t[1]), (float)(p.z - m.t[2])};
-  const F3 dd = f3(d);
-  F3 lp, ld;
-  lp.x = fmaf(q.x, (float)m.r[0], fmaf(q.y, (float)m.r[3], q.z * (float)m.r[6]));
-  lp.y = fmaf(q.x, (float)m.r[1], fmaf(q.y, (float)m.r[4], q.z * (float)m.r[7]));
-  lp.z = fmaf(q.x, (float)m.r[2], fmaf(q.y, (float)m.r[5], q.z * (float)m.r[8]));
-  ld.x = fmaf(dd.x, (float)m.r[0], fmaf(dd.y, (float)m.r[3], dd.z * (float)m.r[6]));
-  ld.y = fmaf(dd.x, (float)m.r[1], fmaf(dd.y, (float)m.r[4], dd.z * (float)m.r[7]));
-  ld.z = fmaf(dd.x, (float)m.r[2], fmaf(dd.y, (float)m.r[5], dd.z * (float)m.r[8]));
-  const ShapeLB s = lbs[g.lv_shape[g.pv_lv[pv]]];
+  const F3 lp     = leaf_local_point(rp, p);
+  const F3 ld     = leaf_local_dir(rp, f3(d));
+  const ShapeLB s = leaf_lb(rp);
   if (s.kind == 0.f) {
     const float lo[3] = {s.a0, s.a1, s.a2}, hi[3] = {s.a3, s.a4, s.a5};
     const F3 inv{inv_dir(ld.x), inv_dir(ld.y), inv_dir(ld.z)};
@@ -156,16 +180,11 @@ __device__ __forceinline__ float daughter_lb(const DevGeom &g, const ShapeLB *lb
 
 // Contains with an FP32 certain-outside / certain-inside test before the FP64 one.
 // Returns the daughter-local FP64 point in `lp` when it returns true.
-__device__ __forceinline__ bool pv_contains_mixed(const DevGeom &g, const ShapeLB *lbs, int pv, V3 p, V3 &lp)
+__device__ __forceinline__ bool pv_contains_mixed(const DevGeom &g, const LeafRec *rp, int pv, V3 p, V3 &lp)
 {
   const Xform &m  = g.pv_xf[pv];
-  const V3 q{p.x - m.t[0], p.y - m.t[1], p.z - m.t[2]};
-  const F3 qf     = f3(q);
-  const F3 l{fmaf(qf.x, (float)m.r[0], fmaf(qf.y, (float)m.r[3], qf.z * (float)m.r[6])),
-             fmaf(qf.x, (float)m.r[1], fmaf(qf.y, (float)m.r[4], qf.z * (float)m.r[7])),
-             fmaf(qf.x, (float)m.r[2], fmaf(qf.y, (float)m.r[5], qf.z * (float)m.r[8]))};
-  const int shape = g.lv_shape[g.pv_lv[pv]];
-  const ShapeLB s = lbs[shape];
+  const F3 l      = leaf_local_point(rp, p);
+  const ShapeLB s = leaf_lb(rp);
   if (s.kind == 0.f) {
     const float lo[3] = {s.a0, s.a1, s.a2}, hi[3] = {s.a3, s.a4, s.a5};
     if (!box_contains_f(lo, hi, l)) return false;
@@ -199,7 +218,6 @@ __device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, const Sha
   const int b = g.lv_bvh[lv];
   if (b < 0) return kTrackOk;
   const int node0 = g.bvh_node0[b];
-  const int dbase = g.lv_dstart[lv];
   const F3 pf     = f3(lp);
   const F3 ldf    = f3(ld);
   const F3 inv{inv_dir(ldf.x), inv_dir(ldf.y), inv_dir(ldf.z)};
@@ -254,14 +272,15 @@ __device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, const Sha
     const NodeF nd = g.node_f[node0 + id];
     if (nd.nchild >= 0) {
       for (int i = 0; i < nd.nchild; ++i) {
-        const int prim = __ldg(&g.prim_id[nd.offset + i]);
-        const float *bx = g.prim_box_f + 6 * (size_t)(dbase + prim);
+        const LeafRec *rp = g.leaf_rec + (nd.offset + i);
+        float blo[3], bhi[3];
+        int vol;
+        leaf_box(rp, blo, bhi, vol);
         float tmin, tmax;
-        slab_f(bx, bx + 3, pf, inv, tmin, tmax);
+        slab_f(blo, bhi, pf, inv, tmin, tmax);
         if (tmin <= tmax && tmax >= 0.f && tmin < bound) {
-          const int vol = __ldg(&g.daughters[dbase + prim]);
           float ub;
-          const float lb = daughter_lb(g, lbs, vol, lp, ld, ub);
+          const float lb = daughter_lb(rp, lp, ld, ub);
           add(lb, vol);
           // a certain upper bound of this daughter's distance bounds the step: whatever
           // starts beyond it can no longer be the first hit
@@ -303,7 +322,6 @@ __device__ __forceinline__ bool level_locate_mixed(const DevGeom &g, const Shape
 {
   const int b     = g.lv_bvh[lv];
   const int node0 = g.bvh_node0[b];
-  const int dbase = g.lv_dstart[lv];
   const F3 pf     = f3(lp);
   unsigned stack[32];
   int sp   = 1;
@@ -313,11 +331,12 @@ __device__ __forceinline__ bool level_locate_mixed(const DevGeom &g, const Shape
     const NodeF nd    = g.node_f[node0 + id];
     if (nd.nchild >= 0) {
       for (int i = 0; i < nd.nchild; ++i) {
-        const int prim  = __ldg(&g.prim_id[nd.offset + i]);
-        const float *bx = g.prim_box_f + 6 * (size_t)(dbase + prim);
-        if (box_contains_f(bx, bx + 3, pf)) {
-          const int vol = __ldg(&g.daughters[dbase + prim]);
-          if (vol != excl_pv && pv_contains_mixed(g, lbs, vol, lp, dlp)) {
+        const LeafRec *rp = g.leaf_rec + (nd.offset + i);
+        float blo[3], bhi[3];
+        int vol;
+        leaf_box(rp, blo, bhi, vol);
+        if (box_contains_f(blo, bhi, pf)) {
+          if (vol != excl_pv && pv_contains_mixed(g, rp, vol, lp, dlp)) {
             pv = vol;
             return true;
           }

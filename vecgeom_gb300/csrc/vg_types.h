@@ -146,6 +146,22 @@ struct alignas(32) NodeF {
 };
 static_assert(sizeof(NodeF) == 32, "NodeF layout");
 
+// FP32 record of one BVH prim slot for the mixed-precision traversal, in slot order (the
+// order leaves reference): the daughter's box, placed volume, FP32 shape descriptor and
+// placement, so that a leaf test, a lower/upper distance bound or a Contains pre-test reads
+// one 128-byte line instead of a chain of dependent loads (slot -> daughter -> placed
+// volume -> logical volume -> shape -> descriptor, and the transform).
+struct alignas(16) LeafRec {
+  float lo[3], hi[3]; // daughter box rounded outward (FP32)
+  int32_t pv;         // placed volume
+  int32_t pad0;
+  float lb[8];        // FP32 bounding descriptor of the daughter's shape (shape_lbd)
+  double t[3];        // placement translation
+  float r[9];         // placement rotation, each entry rounded to FP32
+  float pad1;
+};
+static_assert(sizeof(LeafRec) == 128, "LeafRec layout");
+
 // Pointers into the device copy of a closed geometry. Passed by value to kernels.
 struct DevGeom {
   const double *shape_data; // packed shape records (double-aligned)
@@ -169,6 +185,7 @@ struct DevGeom {
   const NodeF *node_f;        // FP32 node records (bounds rounded outward)
   const float *prim_box_f;    // FP32 daughter boxes (6 floats per slot, rounded outward)
   const float *shape_lbd;     // FP32 bounding descriptor per shape (8 floats, see nav_mixed.cuh)
+  const LeafRec *leaf_rec;    // one record per prim slot (absolute slot index)
   const uint32_t *nav;        // NavIndex table
   uint32_t nav_words;
   const int32_t *lv_depth;    // BVH depth per LV (-1: no BVH)
