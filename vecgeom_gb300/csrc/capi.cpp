@@ -159,8 +159,12 @@ int step_launch(const vg_geom *g, vg::StepArgs a, uint32_t flags, void *ws, size
     a.order = order;
   }
   if (flags & VG_NAV_LEARNED) {
-    e = g->propose_tensor ? vg::launch_mlp_propose_tc(g->geo.dev, a, g->proposer->wbf, slots, g->proposer->err, s)
-                          : vg::launch_mlp_propose(g->geo.dev, a, g->proposer->wbf, slots, s);
+    // proposals are stored per track, so they are computed in track order: coalesced
+    // input loads beat the geometry locality of the sorted order
+    vg::StepArgs pa = a;
+    pa.order        = nullptr;
+    e = g->propose_tensor ? vg::launch_mlp_propose_tc(g->geo.dev, pa, g->proposer->wbf, slots, g->proposer->err, s)
+                          : vg::launch_mlp_propose(g->geo.dev, pa, g->proposer->wbf, slots, s);
     if (e != cudaSuccess) return cuda_fail(e, "proposal launch");
     a.proposal = slots;
   }
@@ -505,7 +509,7 @@ int vg_nav_transport(const vg_geom *g, double *x, double *y, double *z, const do
     }
     if (flags & VG_NAV_LEARNED) {
       vg::StepArgs pa{x, y, z, dx, dy, dz, nullptr, st, nullptr, nullptr, nullptr, nullptr, live};
-      pa.order = order;
+      pa.order = list[cur]; // live tracks in (near) track order, see step_launch
       e = g->propose_tensor ? vg::launch_mlp_propose_tc(g->geo.dev, pa, g->proposer->wbf, slots, g->proposer->err, s)
                             : vg::launch_mlp_propose(g->geo.dev, pa, g->proposer->wbf, slots, s);
       if (e != cudaSuccess) break;

@@ -12,47 +12,78 @@ namespace vg {
 
 namespace f64 {
 
-#define VG_PRIM_CASES(FN, ...)                                                               \
-  switch (g.shape_type[shape]) {                                                             \
-  case kShapeBox: return box_##FN(rec<BoxRec>(g, shape), __VA_ARGS__);                       \
-  case kShapeTube: return tube_##FN(rec<TubeRec>(g, shape), __VA_ARGS__);                    \
-  case kShapeCone: return cone_##FN(rec<ConeRec>(g, shape), __VA_ARGS__);                    \
-  case kShapeTrd: return trd_##FN(rec<TrdRec>(g, shape), __VA_ARGS__);                       \
-  case kShapePolycone: return polycone_##FN(rec<PolyconeRec>(g, shape), __VA_ARGS__);        \
-  case kShapePolyhedron: return polyhedron_##FN(rec<PolyhedronRec>(g, shape), __VA_ARGS__);  \
-  case kShapeTorus2: return torus_##FN(rec<TorusRec>(g, shape), __VA_ARGS__);                \
-  default: break;                                                                            \
+// Shapes are addressed either by id (shape) or by (type, off), the tag and record offset
+// the caller already holds (PvRec, LeafRec); both reach the same kernels.
+template <class R>
+__device__ __forceinline__ const R &rec_at(const DevGeom &g, int off)
+{
+  return *reinterpret_cast<const R *>(g.shape_data + off);
+}
+#define VG_PRIM_CASES(FN, ...)                                                                  \
+  switch (type) {                                                                               \
+  case kShapeBox: return box_##FN(rec_at<BoxRec>(g, off), __VA_ARGS__);                         \
+  case kShapeTube: return tube_##FN(rec_at<TubeRec>(g, off), __VA_ARGS__);                      \
+  case kShapeCone: return cone_##FN(rec_at<ConeRec>(g, off), __VA_ARGS__);                      \
+  case kShapeTrd: return trd_##FN(rec_at<TrdRec>(g, off), __VA_ARGS__);                         \
+  case kShapePolycone: return polycone_##FN(rec_at<PolyconeRec>(g, off), __VA_ARGS__);          \
+  case kShapePolyhedron: return polyhedron_##FN(rec_at<PolyhedronRec>(g, off), __VA_ARGS__);    \
+  case kShapeTorus2: return torus_##FN(rec_at<TorusRec>(g, off), __VA_ARGS__);                  \
+  default: break;                                                                               \
   }
 
-__device__ inline bool prim_contains(const DevGeom &g, int shape, V3 p)
+__device__ inline bool prim_contains_to(const DevGeom &g, int type, int off, V3 p)
 {
   VG_PRIM_CASES(contains, p)
   return false;
 }
-__device__ inline int prim_inside(const DevGeom &g, int shape, V3 p)
+__device__ inline bool prim_contains(const DevGeom &g, int shape, V3 p)
+{
+  return prim_contains_to(g, g.shape_type[shape], g.shape_off[shape], p);
+}
+__device__ inline int prim_inside_to(const DevGeom &g, int type, int off, V3 p)
 {
   VG_PRIM_CASES(inside, p)
   return kOutside;
 }
-__device__ inline double prim_dist_in(const DevGeom &g, int shape, V3 p, V3 d)
+__device__ inline int prim_inside(const DevGeom &g, int shape, V3 p)
+{
+  return prim_inside_to(g, g.shape_type[shape], g.shape_off[shape], p);
+}
+__device__ inline double prim_dist_in_to(const DevGeom &g, int type, int off, V3 p, V3 d)
 {
   VG_PRIM_CASES(dist_in, p, d)
   return kInfLength;
 }
-__device__ inline double prim_dist_out(const DevGeom &g, int shape, V3 p, V3 d)
+__device__ inline double prim_dist_in(const DevGeom &g, int shape, V3 p, V3 d)
+{
+  return prim_dist_in_to(g, g.shape_type[shape], g.shape_off[shape], p, d);
+}
+__device__ inline double prim_dist_out_to(const DevGeom &g, int type, int off, V3 p, V3 d)
 {
   VG_PRIM_CASES(dist_out, p, d)
   return -1.;
 }
-__device__ inline double prim_safety_in(const DevGeom &g, int shape, V3 p)
+__device__ inline double prim_dist_out(const DevGeom &g, int shape, V3 p, V3 d)
+{
+  return prim_dist_out_to(g, g.shape_type[shape], g.shape_off[shape], p, d);
+}
+__device__ inline double prim_safety_in_to(const DevGeom &g, int type, int off, V3 p)
 {
   VG_PRIM_CASES(safety_in, p)
   return kInfLength;
 }
-__device__ inline double prim_safety_out(const DevGeom &g, int shape, V3 p)
+__device__ inline double prim_safety_in(const DevGeom &g, int shape, V3 p)
+{
+  return prim_safety_in_to(g, g.shape_type[shape], g.shape_off[shape], p);
+}
+__device__ inline double prim_safety_out_to(const DevGeom &g, int type, int off, V3 p)
 {
   VG_PRIM_CASES(safety_out, p)
   return -1.;
+}
+__device__ inline double prim_safety_out(const DevGeom &g, int shape, V3 p)
+{
+  return prim_safety_out_to(g, g.shape_type[shape], g.shape_off[shape], p);
 }
 #undef VG_PRIM_CASES
 
@@ -144,35 +175,59 @@ __device__ inline double boolminus_safety_out(const DevGeom &g, const BoolRec &b
 }
 
 // ---------------------------------------------------------------- full dispatch
+__device__ inline bool shape_contains_to(const DevGeom &g, int type, int off, V3 p)
+{
+  if (type == kShapeBoolMinus) return boolminus_contains(g, rec_at<BoolRec>(g, off), p);
+  return prim_contains_to(g, type, off, p);
+}
 __device__ inline bool shape_contains(const DevGeom &g, int shape, V3 p)
 {
-  if (g.shape_type[shape] == kShapeBoolMinus) return boolminus_contains(g, rec<BoolRec>(g, shape), p);
-  return prim_contains(g, shape, p);
+  return shape_contains_to(g, g.shape_type[shape], g.shape_off[shape], p);
+}
+__device__ inline int shape_inside_to(const DevGeom &g, int type, int off, V3 p)
+{
+  if (type == kShapeBoolMinus) return boolminus_inside(g, rec_at<BoolRec>(g, off), p);
+  return prim_inside_to(g, type, off, p);
 }
 __device__ inline int shape_inside(const DevGeom &g, int shape, V3 p)
 {
-  if (g.shape_type[shape] == kShapeBoolMinus) return boolminus_inside(g, rec<BoolRec>(g, shape), p);
-  return prim_inside(g, shape, p);
+  return shape_inside_to(g, g.shape_type[shape], g.shape_off[shape], p);
+}
+__device__ inline double shape_dist_in_to(const DevGeom &g, int type, int off, V3 p, V3 d)
+{
+  if (type == kShapeBoolMinus) return boolminus_dist_in(g, rec_at<BoolRec>(g, off), p, d);
+  return prim_dist_in_to(g, type, off, p, d);
 }
 __device__ inline double shape_dist_in(const DevGeom &g, int shape, V3 p, V3 d)
 {
-  if (g.shape_type[shape] == kShapeBoolMinus) return boolminus_dist_in(g, rec<BoolRec>(g, shape), p, d);
-  return prim_dist_in(g, shape, p, d);
+  return shape_dist_in_to(g, g.shape_type[shape], g.shape_off[shape], p, d);
+}
+__device__ inline double shape_dist_out_to(const DevGeom &g, int type, int off, V3 p, V3 d)
+{
+  if (type == kShapeBoolMinus) return boolminus_dist_out(g, rec_at<BoolRec>(g, off), p, d);
+  return prim_dist_out_to(g, type, off, p, d);
 }
 __device__ inline double shape_dist_out(const DevGeom &g, int shape, V3 p, V3 d)
 {
-  if (g.shape_type[shape] == kShapeBoolMinus) return boolminus_dist_out(g, rec<BoolRec>(g, shape), p, d);
-  return prim_dist_out(g, shape, p, d);
+  return shape_dist_out_to(g, g.shape_type[shape], g.shape_off[shape], p, d);
+}
+__device__ inline double shape_safety_in_to(const DevGeom &g, int type, int off, V3 p)
+{
+  if (type == kShapeBoolMinus) return boolminus_safety_in(g, rec_at<BoolRec>(g, off), p);
+  return prim_safety_in_to(g, type, off, p);
 }
 __device__ inline double shape_safety_in(const DevGeom &g, int shape, V3 p)
 {
-  if (g.shape_type[shape] == kShapeBoolMinus) return boolminus_safety_in(g, rec<BoolRec>(g, shape), p);
-  return prim_safety_in(g, shape, p);
+  return shape_safety_in_to(g, g.shape_type[shape], g.shape_off[shape], p);
+}
+__device__ inline double shape_safety_out_to(const DevGeom &g, int type, int off, V3 p)
+{
+  if (type == kShapeBoolMinus) return boolminus_safety_out(g, rec_at<BoolRec>(g, off), p);
+  return prim_safety_out_to(g, type, off, p);
 }
 __device__ inline double shape_safety_out(const DevGeom &g, int shape, V3 p)
 {
-  if (g.shape_type[shape] == kShapeBoolMinus) return boolminus_safety_out(g, rec<BoolRec>(g, shape), p);
-  return prim_safety_out(g, shape, p);
+  return shape_safety_out_to(g, g.shape_type[shape], g.shape_off[shape], p);
 }
 
 } // namespace f64

@@ -1122,15 +1122,31 @@ int Geometry::upload(std::string &err)
         r.lo[c] = prim_box_f[6 * ((size_t)base + prim) + c];
         r.hi[c] = prim_box_f[6 * ((size_t)base + prim) + 3 + c];
       }
-      r.pv = pv;
-      std::memcpy(r.lb, &lbd[8 * (size_t)lvs[pvs[pv].lv].shape], sizeof(r.lb));
+      r.pv              = pv;
+      const int32_t shp = lvs[pvs[pv].lv].shape;
+      r.type            = stype[shp];
+      r.off             = soff[shp];
+      std::memcpy(r.lb, &lbd[8 * (size_t)shp], sizeof(r.lb));
       const Xform &m = pvs[pv].xf.m;
       for (int c = 0; c < 3; ++c) r.t[c] = m.t[c];
       for (int c = 0; c < 9; ++c) r.r[c] = (float)m.r[c];
     }
   }
   const size_t o_pbx = a.add(prim_box), o_nf = a.add(node_f), o_pbf = a.add(prim_box_f), o_nav = a.add(nav);
-  const size_t o_lbd = a.add(lbd), o_lrec = a.add(leaf_rec);
+  std::vector<PvRec> pv_rec(pvs.size());
+  for (size_t i = 0; i < pvs.size(); ++i) {
+    PvRec &r   = pv_rec[i];
+    r.lv       = pvs[i].lv;
+    r.shape    = lvs[r.lv].shape;
+    r.type     = stype[r.shape];
+    r.off      = soff[r.shape];
+    r.nd       = lv_nd[r.lv];
+    const int b = lv_bvh[r.lv];
+    r.node0    = b >= 0 ? bvh_node0[b] : -1;
+    r.depth    = lv_depth[r.lv];
+    r.child    = pvs[i].child;
+  }
+  const size_t o_lbd = a.add(lbd), o_lrec = a.add(leaf_rec), o_pvr = a.add(pv_rec);
   shape_lbd_host     = lbd;
 
   cudaError_t e = cudaGetDevice(&device);
@@ -1169,6 +1185,7 @@ int Geometry::upload(std::string &err)
   dev.dau_slot3   = reinterpret_cast<const int32_t *>(P(o_ds3));
   dev.shape_lbd   = reinterpret_cast<const float *>(P(o_lbd));
   dev.leaf_rec    = reinterpret_cast<const LeafRec *>(P(o_lrec));
+  dev.pv_rec      = reinterpret_cast<const PvRec *>(P(o_pvr));
   dev.world_pv    = world;
   dev.max_depth   = max_depth;
   dev.n_pv        = (int32_t)pvs.size();

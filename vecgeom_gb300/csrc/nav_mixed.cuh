@@ -145,6 +145,14 @@ __device__ __forceinline__ F3 leaf_local_dir(const LeafRec *rp, F3 dd)
             fmaf(dd.x, __ldg(r + 2), fmaf(dd.y, __ldg(r + 5), dd.z * __ldg(r + 8)))};
 }
 
+// The record of placed volume pv (two 16-byte loads).
+__device__ __forceinline__ PvRec pv_rec(const DevGeom &g, int pv)
+{
+  const int4 a = __ldg(reinterpret_cast<const int4 *>(g.pv_rec + pv));
+  const int4 b = __ldg(reinterpret_cast<const int4 *>(g.pv_rec + pv) + 1);
+  return PvRec{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+}
+
 __device__ __forceinline__ float daughter_lb(const LeafRec *rp, V3 p, V3 d, float &ub)
 {
   ub = INFINITY;
@@ -203,7 +211,8 @@ __device__ __forceinline__ bool pv_contains_mixed(const DevGeom &g, const LeafRe
       return true;
     }
   }
-  return f64::pv_contains(g, pv, p, lp);
+  lp = f64::to_local(m, p);
+  return f64::shape_contains_to(g, __ldg(&rp->type), __ldg(&rp->off), lp);
 }
 
 // BVH::CheckDaughterIntersections with FP32 pruning (see file comment). Candidates wait in
@@ -211,30 +220,30 @@ __device__ __forceinline__ bool pv_contains_mixed(const DevGeom &g, const LeafRe
 // which tightens the step and drops every candidate that can no longer win.
 constexpr int kCandBuf = 8;
 
-__device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, const ShapeLB *lbs, int lv, V3 lp, V3 ld,
-                                                     double &step, int last_pv, int &hit_pv, int *nvisited,
-                                                     int first = -1)
+__device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, int node0, V3 lp, V3 ld, double &step,
+                                                     int last_pv, int &hit_pv, int *nvisited, int first = -1)
 {
-  const int b = g.lv_bvh[lv];
-  if (b < 0) return kTrackOk;
-  const int node0 = g.bvh_node0[b];
   const F3 pf     = f3(lp);
   const F3 ldf    = f3(ld);
   const F3 inv{inv_dir(ldf.x), inv_dir(ldf.y), inv_dir(ldf.z)};
   float bound = __double2float_ru(step);
   float cl[kCandBuf] = {};
-  int cp[kCandBuf]   = {};
+  int cp[kCandBuf]   = {}; // prim slots of the candidates
   int nc = 0;
   auto evaluate_first = [&]() {
     const float lb = cl[0];
-    const int vol  = cp[0];
+    const int slot = cp[0];
     for (int k = 1; k < nc; ++k) cl[k - 1] = cl[k], cp[k - 1] = cp[k];
     --nc;
     if (lb >= bound) {
       nc = 0;
       return;
     }
-    const double dist = f64::pv_dist_in(g, vol, lp, ld);
+    const LeafRec *rp = g.leaf_rec + slot;
+    const int vol     = __ldg(&rp->pv);
+    const Xform &m    = g.pv_xf[vol];
+    const double dist =
+        f64::shape_dist_in_to(g, __ldg(&rp->type), __ldg(&rp->off), f64::to_local(m, lp), f64::rotate(m, ld));
     if (dlt(dist, step) && !(dle(dist, 0.0) && vol == last_pv)) {
       step   = dist;
       hit_pv = vol;
@@ -242,7 +251,7 @@ __device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, const Sha
       while (nc > 0 && cl[nc - 1] >= bound) --nc;
     }
   };
-  auto add = [&](float lb, int vol) {
+  auto add = [&](float lb, int slot) {
     if (!(lb < bound)) return;
     if (nc == kCandBuf) {
       evaluate_first();
@@ -250,7 +259,7 @@ __device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, const Sha
     }
     int k = nc++;
     while (k > 0 && cl[k - 1] > lb) cl[k] = cl[k - 1], cp[k] = cp[k - 1], --k;
-    cl[k] = lb, cp[k] = vol;
+    cl[k] = lb, cp[k] = slot;
   };
   unsigned stack[32];
   int sp     = 1;
@@ -272,7 +281,8 @@ __device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, const Sha
     const NodeF nd = g.node_f[node0 + id];
     if (nd.nchild >= 0) {
       for (int i = 0; i < nd.nchild; ++i) {
-        const LeafRec *rp = g.leaf_rec + (nd.offset + i);
+        const int slot    = nd.offset + i;
+        const LeafRec *rp = g.leaf_rec + slot;
         float blo[3], bhi[3];
         int vol;
         leaf_box(rp, blo, bhi, vol);
@@ -281,7 +291,7 @@ __device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, const Sha
         if (tmin <= tmax && tmax >= 0.f && tmin < bound) {
           float ub;
           const float lb = daughter_lb(rp, lp, ld, ub);
-          add(lb, vol);
+          add(lb, slot);
           // a certain upper bound of this daughter's distance bounds the step: whatever
           // starts beyond it can no longer be the first hit
           if (ub < bound && vol != last_pv) {
@@ -317,11 +327,9 @@ __device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, const Sha
 }
 
 // BVH::LevelLocate with FP32 box tests (padded) and mixed Contains.
-__device__ __forceinline__ bool level_locate_mixed(const DevGeom &g, const ShapeLB *lbs, int lv, int excl_pv, V3 lp,
-                                                   int &pv, V3 &dlp, int &status)
+__device__ __forceinline__ bool level_locate_mixed(const DevGeom &g, int node0, int excl_pv, V3 lp, int &pv, V3 &dlp,
+                                                   int &status)
 {
-  const int b     = g.lv_bvh[lv];
-  const int node0 = g.bvh_node0[b];
   const F3 pf     = f3(lp);
   unsigned stack[32];
   int sp   = 1;
@@ -356,9 +364,11 @@ __device__ __forceinline__ bool level_locate_mixed(const DevGeom &g, const Shape
   return false;
 }
 
-__device__ __forceinline__ bool shape_contains_mixed(const DevGeom &g, const ShapeLB *lbs, int shape, V3 p)
+// Contains of placed volume `pv`'s own shape (mother frame of its daughters) with the FP32
+// certain-outside / certain-inside tests first.
+__device__ __forceinline__ bool shape_contains_mixed(const DevGeom &g, const ShapeLB *lbs, const PvRec &r, V3 p)
 {
-  const ShapeLB s = lbs[shape];
+  const ShapeLB s = lbs[r.shape];
   const F3 l      = f3(p);
   if (s.kind == 0.f) {
     const float lo[3] = {s.a0, s.a1, s.a2}, hi[3] = {s.a3, s.a4, s.a5};
@@ -374,44 +384,49 @@ __device__ __forceinline__ bool shape_contains_mixed(const DevGeom &g, const Sha
     if (s.flag != 0.f && l.z > s.a2 + kBoxPad && l.z < s.a3 - kBoxPad && r2 < ro_in * ro_in && r2 > ri_in * ri_in)
       return true;
   }
-  return f64::shape_contains(g, shape, p);
+  return f64::shape_contains_to(g, r.type, r.off, p);
+}
+
+// NavIndex push with the child index already known (NavStateIndex::PushImpl)
+__device__ __forceinline__ uint32_t nav_push_child(const DevGeom &g, uint32_t n, int child)
+{
+  return n > 0 ? __ldg(&g.nav[n + 3 + child]) : 1u;
 }
 
 __device__ __forceinline__ int locate_global_point_mixed(const DevGeom &g, const ShapeLB *lbs, int vol, V3 p,
                                                          uint32_t &nav, bool top, int &status)
 {
-  int cand = vol;
-  if (top) cand = shape_contains_mixed(g, lbs, f64::pv_shape(g, vol), p) ? vol : -1;
+  int cand  = vol;
+  PvRec rec = pv_rec(g, vol);
+  if (top) cand = shape_contains_mixed(g, lbs, rec, p) ? vol : -1;
   if (cand < 0) return -1;
-  nav    = f64::nav_push(g, nav, cand);
-  int lv = g.pv_lv[cand];
+  nav = nav_push_child(g, nav, rec.child);
   for (int level = 0; level < 256; ++level) {
-    if (g.lv_nd[lv] == 0) return f64::nav_top(g, nav);
+    if (rec.nd == 0) return f64::nav_top(g, nav);
     int pv = -1;
     V3 tp;
-    if (!level_locate_mixed(g, lbs, lv, -1, p, pv, tp, status)) return f64::nav_top(g, nav);
-    nav  = f64::nav_push(g, nav, pv);
-    cand = f64::nav_top(g, nav);
-    lv   = g.pv_lv[cand];
-    p    = tp;
+    if (!level_locate_mixed(g, rec.node0, -1, p, pv, tp, status)) return f64::nav_top(g, nav);
+    rec = pv_rec(g, pv);
+    nav = nav_push_child(g, nav, rec.child);
+    p   = tp;
   }
   status = kTrackErrIter;
   return f64::nav_top(g, nav);
 }
 
-__device__ __forceinline__ void locate_excl_mixed(const DevGeom &g, const ShapeLB *lbs, int vol, int excl, V3 p,
-                                                  uint32_t &nav, int &status)
+__device__ __forceinline__ void locate_excl_mixed(const DevGeom &g, int vol, int excl, V3 p, uint32_t &nav,
+                                                  int &status)
 {
-  int cand = vol;
-  nav      = f64::nav_push(g, nav, cand);
-  int lv   = g.pv_lv[cand];
+  PvRec rec = pv_rec(g, vol);
+  nav       = nav_push_child(g, nav, rec.child);
   for (int level = 0; level < 256; ++level) {
-    if (g.lv_nd[lv] == 0) return;
+    if (rec.nd == 0) return;
     V3 tp;
-    if (!level_locate_mixed(g, lbs, lv, excl, p, cand, tp, status)) return;
-    lv  = g.pv_lv[cand];
+    int cand = -1;
+    if (!level_locate_mixed(g, rec.node0, excl, p, cand, tp, status)) return;
+    rec = pv_rec(g, cand);
     p   = tp;
-    nav = f64::nav_push(g, nav, cand);
+    nav = nav_push_child(g, nav, rec.child);
   }
   status = kTrackErrIter;
 }
@@ -423,13 +438,13 @@ __device__ __forceinline__ void relocate_force_different_mixed(const DevGeom &g,
   const int entry = cur;
   if (cur < 0) return;
   for (int level = 0; level < 256 && cur >= 0; ++level) {
-    if (cur == entry || !shape_contains_mixed(g, lbs, f64::pv_shape(g, cur), lp)) {
+    if (cur == entry || !shape_contains_mixed(g, lbs, pv_rec(g, cur), lp)) {
       nav = f64::nav_pop(g, nav);
       lp  = f64::to_master(g.pv_xf[cur], lp);
       cur = f64::nav_top(g, nav);
     } else {
       nav = f64::nav_pop(g, nav);
-      locate_excl_mixed(g, lbs, cur, entry, lp, nav, status);
+      locate_excl_mixed(g, cur, entry, lp, nav, status);
       return;
     }
   }
@@ -446,28 +461,27 @@ __device__ __forceinline__ double compute_step_mixed(const DevGeom &g, const Sha
     status = kTrackErrState;
     return 0.;
   }
-  const Xform m = f64::nav_top_matrix(g, in.navInd);
-  const V3 lp   = f64::to_local(m, gp);
-  const V3 ld   = f64::rotate(m, gd);
-  const int pv  = f64::nav_top(g, in.navInd);
-  const int lv  = g.pv_lv[pv];
-  double step   = f64::shape_dist_out(g, g.lv_shape[lv], lp, ld);
+  const Xform m   = f64::nav_top_matrix(g, in.navInd);
+  const V3 lp     = f64::to_local(m, gp);
+  const V3 ld     = f64::rotate(m, gd);
+  const int pv    = f64::nav_top(g, in.navInd);
+  const PvRec rec = pv_rec(g, pv);
+  double step     = f64::shape_dist_out_to(g, rec.type, rec.off, lp, ld);
   if (dlt(step, 0.)) step = 0.;
   int hit = -1;
-  if (g.lv_nd[lv] > 0) {
+  if (rec.nd > 0) {
     const int last = f64::nav_top(g, in.lastExited);
     int first = -1; // the proposal applies to BVHs of depth >= 3 whose depth-3 node is reachable
-    if (proposal >= 0 && proposal < 8 && g.lv_depth[lv] >= 3) {
-      const int node0 = g.bvh_node0[g.lv_bvh[lv]];
-      int n           = 7 + proposal;
-      bool ok         = true;
+    if (proposal >= 0 && proposal < 8 && rec.depth >= 3) {
+      int n   = 7 + proposal;
+      bool ok = true;
       for (int d = 0; d < 3; ++d) {
         n  = (n - 1) >> 1;
-        ok = ok && __ldg(&g.node_nchild[node0 + n]) < 0;
+        ok = ok && __ldg(&g.node_nchild[rec.node0 + n]) < 0;
       }
       if (ok) first = proposal;
     }
-    status = check_daughters_mixed(g, lbs, lv, lp, ld, step, last, hit, nvisited, first);
+    status = check_daughters_mixed(g, rec.node0, lp, ld, step, last, hit, nvisited, first);
     if (status != kTrackOk) return 0.;
   }
   if (deq(step, kInfLength) && dgt(limit, 0.)) {

@@ -154,13 +154,22 @@ static_assert(sizeof(NodeF) == 32, "NodeF layout");
 struct alignas(16) LeafRec {
   float lo[3], hi[3]; // daughter box rounded outward (FP32)
   int32_t pv;         // placed volume
-  int32_t pad0;
+  int32_t type;       // shape type of the daughter
   float lb[8];        // FP32 bounding descriptor of the daughter's shape (shape_lbd)
   double t[3];        // placement translation
   float r[9];         // placement rotation, each entry rounded to FP32
-  float pad1;
+  int32_t off;        // shape record offset (doubles) of the daughter
 };
 static_assert(sizeof(LeafRec) == 128, "LeafRec layout");
+
+// Per placed volume, what a navigation step needs about it and its logical volume in one
+// 32-byte load (instead of pv -> lv -> shape -> type/offset and lv -> BVH -> first node).
+struct alignas(32) PvRec {
+  int32_t lv, shape, type, off; // logical volume, its shape, the shape's type and record offset
+  int32_t nd, node0, depth;     // daughters, first BVH node (-1: none), BVH depth (-1: none)
+  int32_t child;                // index among the mother's daughters
+};
+static_assert(sizeof(PvRec) == 32, "PvRec layout");
 
 // Pointers into the device copy of a closed geometry. Passed by value to kernels.
 struct DevGeom {
@@ -186,6 +195,7 @@ struct DevGeom {
   const float *prim_box_f;    // FP32 daughter boxes (6 floats per slot, rounded outward)
   const float *shape_lbd;     // FP32 bounding descriptor per shape (8 floats, see nav_mixed.cuh)
   const LeafRec *leaf_rec;    // one record per prim slot (absolute slot index)
+  const PvRec *pv_rec;        // one record per placed volume
   const uint32_t *nav;        // NavIndex table
   uint32_t nav_words;
   const int32_t *lv_depth;    // BVH depth per LV (-1: no BVH)
