@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--shape-reps", type=int, default=20, help="graph-captured calls per shape-query timing")
     ap.add_argument("--section", default="all", choices=["all", "shapes"],
                     help="'shapes': only the shape-query rows (one JSON line), e.g. for profiling")
+    ap.add_argument("--graph", type=int, default=1,
+                    help="time the headline step as replays of a captured CUDA graph (1/0)")
     ap.add_argument("--tune", type=int, default=1,
                     help="autotune sort-key bits / queue occupancy before timing (untimed; 1/0)")
     return ap.parse_args()
@@ -458,16 +460,26 @@ def main():
 
     spread = {}
 
-    def timed(flags):
+    def timed(flags, graph=False):
+        """ms per step; with graph=True the step (all its launches) is captured once into a
+        CUDA graph after the warm-up and each timed step is one replay."""
         for _ in range(args.warmup):
             geo.compute_step_and_next_volume(*t, st, out, step, status=status, flags=flags)
+        torch.cuda.synchronize()
+        run = lambda: geo.compute_step_and_next_volume(*t, st, out, step, status=status, flags=flags)
+        if graph:
+            cg = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(cg):
+                geo.compute_step_and_next_volume(*t, st, out, step, status=status, flags=flags)
+            cg.replay()
+            run = cg.replay
         torch.cuda.synchronize()
         barrier()
         evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
         torch.cuda.synchronize()
         evs[0].record()
         for k in range(args.steps):
-            geo.compute_step_and_next_volume(*t, st, out, step, status=status, flags=flags)
+            run()
             evs[k + 1].record()
         torch.cuda.synchronize()
         barrier()
@@ -502,8 +514,9 @@ def main():
                 continue
             variants[name] = timed(f)
             identical &= bool(torch.equal(out64, out)) and bool(torch.equal(step64, step))
+    ms_head_eager = timed(head) if args.graph else None
     with ClockSampler(local) as clocks:
-        ms_head = timed(head)
+        ms_head = timed(head, graph=bool(args.graph))
     variants[args.schedule] = ms_head
     n_err = int((status != 0).sum().item())
     ids_equal = bool(torch.equal(out64, out))
@@ -580,6 +593,7 @@ def main():
         "metric": "nav steps/s", "value": value, "unit": "nav steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_head, "higher_is_better": True, "scaling": "weak",
         "ms_per_step_min_max": [round(v, 4) for v in spread.get(head, (ms_head, ms_head))],
+        "cuda_graph": bool(args.graph), "ms_per_step_eager": ms_head_eager,
         "vs_baseline": None, "dtype": "f64 (mixed: FP32 pruning, FP64 decisions)",
         "data": "synthetic (seeded; geometry built in code, tracks generated on the GPU)",
         "config": dict(config_of(args, pool), schedule=args.schedule,

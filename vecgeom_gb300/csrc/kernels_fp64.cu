@@ -80,6 +80,92 @@ __global__ void __launch_bounds__(256) k_shape_query(const R rec, const Xform xf
   }
 }
 
+// Mixed-precision SoA distance query with block-level compaction. Each thread first tries to
+// settle its query in FP32 (exact-shape classification with a kBoxPad margin, certain misses of the
+// padded descriptor; see shapes_mixed.cuh). Queries it cannot settle go to a shared-memory
+// queue, and whenever the queue holds a full block's worth, all 256
+// threads evaluate 256 of them in FP64, so the FP64 code runs with full warps instead of the
+// few lanes that needed it. Results are those of the FP64 kernel (k_shape_query<R, Q,
+// false>) for every query.
+template <class R, int Q>
+__global__ void __launch_bounds__(256) k_shape_query_mixed(const R rec, const Xform xf, const int apply_xf,
+                                                           const mixed::ShapeLB lb, const double *__restrict__ x,
+                                                           const double *__restrict__ y, const double *__restrict__ z,
+                                                           const double *__restrict__ dx, const double *__restrict__ dy,
+                                                           const double *__restrict__ dz, size_t n,
+                                                           void *__restrict__ out)
+{
+  __shared__ unsigned long long queue[512];
+  __shared__ int qn;
+  if (threadIdx.x == 0) qn = 0;
+  __syncthreads();
+  static_assert(Q == 2 || Q == 3, "distances only");
+  const bool framed = apply_xf && Q == 2;
+  // FP32 frame: p - t in FP32 (|p|, |t| <= kMaxCoord keep it within 1e-3 mm), FP32 rotation
+  const bool ident = f64::rot_is_identity(xf);
+  const float tf[3] = {(float)xf.t[0], (float)xf.t[1], (float)xf.t[2]};
+  const bool t_ok   = mixed::in_range(mixed::F3{tf[0], tf[1], tf[2]});
+  auto local_f = [&](mixed::F3 v, bool point) {
+    if (!framed) return v;
+    if (point) v = mixed::F3{v.x - tf[0], v.y - tf[1], v.z - tf[2]};
+    if (ident) return v;
+    return mixed::F3{fmaf(v.x, (float)xf.r[0], fmaf(v.y, (float)xf.r[3], v.z * (float)xf.r[6])),
+                     fmaf(v.x, (float)xf.r[1], fmaf(v.y, (float)xf.r[4], v.z * (float)xf.r[7])),
+                     fmaf(v.x, (float)xf.r[2], fmaf(v.y, (float)xf.r[5], v.z * (float)xf.r[8]))};
+  };
+  auto fast = [&](size_t i) -> bool {
+    const mixed::F3 pg{(float)__ldg(x + i), (float)__ldg(y + i), (float)__ldg(z + i)};
+    if (!mixed::in_range(pg) || (framed && !t_ok)) return false;
+    const mixed::F3 l = local_f(pg, true);
+    const int c       = mixed::f32_classify(rec, lb, l);
+    if (Q == 2) {
+      if (c == kInside && mixed::dist_in_inside_is_minus1<R>()) {
+        static_cast<double *>(out)[i] = -1.0;
+        return true;
+      }
+      if (c != kOutside) return false;
+      const mixed::F3 d = local_f(mixed::F3{(float)__ldg(dx + i), (float)__ldg(dy + i), (float)__ldg(dz + i)}, false);
+      if (!mixed::f32_certain_miss(lb, l, d)) return false;
+      static_cast<double *>(out)[i] = kInfLength;
+      return true;
+    }
+    if (Q == 3 && c == kOutside && mixed::dist_out_outside_is_minus1(rec)) {
+      static_cast<double *>(out)[i] = -1.0;
+      return true;
+    }
+    return false;
+  };
+  auto exact = [&](size_t i) {
+    V3 p{__ldg(x + i), __ldg(y + i), __ldg(z + i)};
+    V3 d{__ldg(dx + i), __ldg(dy + i), __ldg(dz + i)};
+    if (framed) p = f64::to_local(xf, p), d = f64::rotate(xf, d);
+    static_cast<double *>(out)[i] = (Q == 2) ? ShapeOps<R>::dist_in(rec, p, d) : ShapeOps<R>::dist_out(rec, p, d);
+  };
+  const int lane      = threadIdx.x & 31;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t base = (size_t)blockIdx.x * blockDim.x; base < n; base += stride) { // uniform over the block
+    const size_t i    = base + threadIdx.x;
+    const bool undec  = i < n && !fast(i);
+    const unsigned bl = __ballot_sync(0xffffffffu, undec);
+    if (bl) {
+      int w = 0;
+      if (lane == 0) w = atomicAdd(&qn, __popc(bl));
+      w = __shfl_sync(0xffffffffu, w, 0);
+      if (undec) queue[w + __popc(bl & ((1u << lane) - 1u))] = i;
+    }
+    __syncthreads();
+    const int q = qn; // < 512: at most 255 left over plus 256 new
+    if (q >= 256) {
+      exact(queue[q - 256 + threadIdx.x]);
+      __syncthreads();
+      if (threadIdx.x == 0) qn = q - 256;
+    }
+    __syncthreads();
+  }
+  const int q = qn;
+  if ((int)threadIdx.x < q) exact(queue[threadIdx.x]);
+}
+
 template <class R, bool M>
 cudaError_t launch_typed_q(const R &rec, const Xform &xf, int apply_xf, const mixed::ShapeLB &lb, int q,
                            const QueryArgs &a, cudaStream_t s)
@@ -87,17 +173,26 @@ cudaError_t launch_typed_q(const R &rec, const Xform &xf, int apply_xf, const mi
   const int block     = 256;
   const unsigned grid = grid_for(a.n, block);
 #define VG_Q(Q)                                                                                                   \
-  k_shape_query<R, Q, M><<<grid, block, 0, s>>>(rec, xf, apply_xf, lb, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out)
+  k_shape_query<R, Q, (M && Q >= 4)><<<grid, block, 0, s>>>(rec, xf, apply_xf, lb, a.x, a.y, a.z, a.dx, a.dy, a.dz, \
+                                                             a.n, a.out)
+#define VG_QM(Q)                                                                                                  \
+  (M ? k_shape_query_mixed<R, Q><<<grid, block, 0, s>>>(rec, xf, apply_xf, lb, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, \
+                                                       a.out)                                                      \
+     : k_shape_query<R, Q, false><<<grid, block, 0, s>>>(rec, xf, apply_xf, lb, a.x, a.y, a.z, a.dx, a.dy, a.dz,   \
+                                                         a.n, a.out))
+  // Inside and Contains are cheaper in the FP64 kernel (integer-pipe compares) than any FP32
+  // pre-classification measured (0.7-0.95x of it), so VG_PREC_MIXED uses it for them.
   switch (q) {
   case 0: VG_Q(0); break;
   case 1: VG_Q(1); break;
-  case 2: VG_Q(2); break;
-  case 3: VG_Q(3); break;
+  case 2: VG_QM(2); break;
+  case 3: VG_QM(3); break;
   case 4: VG_Q(4); break;
   case 5: VG_Q(5); break;
   default: return cudaErrorInvalidValue;
   }
 #undef VG_Q
+#undef VG_QM
   return cudaGetLastError();
 }
 
@@ -171,8 +266,8 @@ cudaError_t launch_shape_query_dyn_fp64(const DevGeom &g, int shape, const Xform
   (mixed ? k_shape_query_dyn<Q, true><<<grid, 256, 0, s>>>(g, shape, xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out) \
          : k_shape_query_dyn<Q, false><<<grid, 256, 0, s>>>(g, shape, xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out))
   switch (q) {
-  case 0: VG_DYN(0); break;
-  case 1: VG_DYN(1); break;
+  case 0: mixed = false, VG_DYN(0); break; // FP64 is the faster classification (see launch_typed_q)
+  case 1: mixed = false, VG_DYN(1); break;
   case 2: VG_DYN(2); break;
   case 3: VG_DYN(3); break;
   case 4: VG_DYN(4); break;

@@ -23,7 +23,10 @@ __device__ __forceinline__ bool slot_reachable(const DevGeom &g, int node0, int 
 __device__ __forceinline__ float safe_inv(float d) { return d != 0.f ? 1.f / d : copysignf(INFINITY, d); }
 
 // Features of a track in state `navInd` at global point/direction (gp, gd). Returns false
-// (and lv = -1) when no proposal applies. lp/ld receive the FP64 local point/direction.
+// (and lv = -1) when no proposal applies. lp/ld receive the FP64 local point/direction
+// (for the training label); the features themselves use an FP32 transform (p - t formed in
+// FP64, the rotation in FP32), the same in training and inference, so that inference,
+// which discards lp/ld, issues almost no FP64 work.
 __device__ __forceinline__ bool features(const DevGeom &g, uint32_t navInd, V3 gp, V3 gd, float *f, int &lv, V3 &lp,
                                          V3 &ld)
 {
@@ -32,6 +35,10 @@ __device__ __forceinline__ bool features(const DevGeom &g, uint32_t navInd, V3 g
   const Xform m = f64::nav_top_matrix(g, navInd);
   lp            = f64::to_local(m, gp);
   ld            = f64::rotate(m, gd);
+  float rf[9];
+  for (int k = 0; k < 9; ++k) rf[k] = (float)m.r[k];
+  const float q[3]  = {(float)(gp.x - m.t[0]), (float)(gp.y - m.t[1]), (float)(gp.z - m.t[2])};
+  const float gf[3] = {(float)gd.x, (float)gd.y, (float)gd.z};
   const int l   = g.pv_lv[f64::nav_top(g, navInd)];
   if (g.lv_depth[l] < 3) return false;
   lv              = l;
@@ -43,8 +50,11 @@ __device__ __forceinline__ bool features(const DevGeom &g, uint32_t navInd, V3 g
     h[k] = fmaxf(0.5f * (root.hi[k] - root.lo[k]), 1e-3f);
     hs   = fmaxf(hs, h[k]);
   }
-  const float p[3] = {(float)lp.x, (float)lp.y, (float)lp.z};
-  const float d[3] = {(float)ld.x, (float)ld.y, (float)ld.z};
+  float p[3], d[3];
+  for (int k = 0; k < 3; ++k) {
+    p[k] = fmaf(q[0], rf[k], fmaf(q[1], rf[3 + k], q[2] * rf[6 + k]));
+    d[k] = fmaf(gf[0], rf[k], fmaf(gf[1], rf[3 + k], gf[2] * rf[6 + k]));
+  }
   const float inv[3] = {safe_inv(d[0]), safe_inv(d[1]), safe_inv(d[2])};
   for (int k = 0; k < 3; ++k) {
     f[k]     = (p[k] - c[k]) / h[k];
