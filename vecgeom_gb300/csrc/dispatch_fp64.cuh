@@ -10,6 +10,10 @@
 namespace vg {
 
 
+#ifndef VG_INLINE_CONTAINS
+#define VG_INLINE_CONTAINS 0
+#endif
+
 namespace f64 {
 
 // Shapes are addressed either by id (shape) or by (type, off), the tag and record offset
@@ -175,7 +179,14 @@ __device__ inline double boolminus_safety_out(const DevGeom &g, const BoolRec &b
 }
 
 // ---------------------------------------------------------------- full dispatch
+// Out of line by default: the scheduled step kernels call it from several places (relocation,
+// Contains fallbacks) and inlining every copy costs them instruction-cache misses (3.6 %
+// slower); the plain-FP64 navigator unit sets VG_INLINE_CONTAINS, where inlining is faster.
+#if VG_INLINE_CONTAINS
 __device__ inline bool shape_contains_to(const DevGeom &g, int type, int off, V3 p)
+#else
+static __device__ __noinline__ bool shape_contains_to(const DevGeom &g, int type, int off, V3 p)
+#endif
 {
   if (type == kShapeBoolMinus) return boolminus_contains(g, rec_at<BoolRec>(g, off), p);
   return prim_contains_to(g, type, off, p);

@@ -4,6 +4,7 @@
 // (VG_FP64_INT_COMPARE 0, VG_FP64_SHORTCUTS 0, see fp64_int.cuh).
 #define VG_FP64_INT_COMPARE 0
 #define VG_FP64_SHORTCUTS 0
+#define VG_INLINE_CONTAINS 1
 #include "launch.h"
 #include "nav_fp64.cuh"
 
