@@ -30,6 +30,14 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 STEP_BYTES = 24 + 24 + 12 + 12 + 8  # p, d, state in, state out, step (FP64 SoA + 12 B states)
+# FP64-pipe thread instructions per scheduled detector step (sort keys 3.0 + proposal 10.2 +
+# step kernel 329.1), counted by ncu (sm__thread_inst_executed_pipe_fp64_pred_on over every
+# launch of one scheduled step on 2^20 detector step inputs; the summary is under profiles/).
+# Per-thread counts do not depend on how lanes group into warps, so they hold at 2^22.
+FP64_OPS_PER_STEP = 342.3
+# DRAM bytes per launch of the step kernel, from the same capture (read 488.4 MB + write
+# 63.4 MB per 2^20 steps), scaled to the 2^22-step launch by the steps it processes.
+STEP_TRAFFIC_PER_STEP = (488.4e6 + 63.4e6) / (1 << 20)
 # name -> (precision | scheduling flags): 1 = VG_PREC_MIXED, 2 = VG_NAV_SORT, 4 = VG_NAV_QUEUE
 # 8 = VG_NAV_LEARNED (explore the BVH subtree proposed by the trained model first)
 SCHEDULES = {"fp64": 0, "fp64_sort": 2, "mixed": 1, "mixed_sort": 3, "mixed_queue": 5, "mixed_sort_queue": 7,
@@ -589,6 +597,16 @@ def main():
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     value = ws * n / (ms_head * 1e-3)
     achieved = STEP_BYTES * n / (ms_kernel * 1e-3) / 1e9
+    # FP64 roofline of the scheduled step (the bound of the navigation rows): FP64 pipe
+    # thread-ops per step x steps/s over this GPU's measured FP64 FMA rate
+    roofline_fp64 = None
+    if head == SCHEDULES["mixed_sort_queue_learned"]:
+        fp64_peak = vg.device_fp64_rate()
+        roofline_fp64 = {"bound": "fp64", "achieved": FP64_OPS_PER_STEP * n / (ms_head * 1e-3), "peak": fp64_peak,
+                         "unit": "FP64 thread-ops/s", "frac": FP64_OPS_PER_STEP * n / (ms_head * 1e-3) / fp64_peak,
+                         "ops_per_step": FP64_OPS_PER_STEP,
+                         "note": "ops per step counted by ncu (summary under profiles/); peak = DFMA "
+                                 "rate of a probe kernel timed in this run"}
     line = {
         "metric": "nav steps/s", "value": value, "unit": "nav steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_head, "higher_is_better": True, "scaling": "weak",
@@ -611,12 +629,16 @@ def main():
         "e2e": {"value": ws * n / e2e_s, "unit": "nav steps/s", "h2d_bytes_per_step": n * (48 + 12),
                 "d2h_bytes_per_step": n * (12 + 8)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None,
+                     "frac": achieved / hbm_peak, "traffic": STEP_TRAFFIC_PER_STEP * n if head & 4 else None,
+                     "traffic_note": "DRAM read + write of one step-kernel launch, ncu on 2^20 steps scaled to %d "
+                                     "(geometry L2 misses and the sorted-order gathers: 526 B/step vs 80 "
+                                     "algorithmic)" % n,
                      "kernel": "k_step_mixed_queue" if head & 4 else ("k_step_mixed" if head & 1 else "k_step"),
                      "step_kernel_time_note": "sort and proposal kernels excluded" if head & 8 else "sort excluded",
                      "note": "algorithmic bytes %d B/step over the step kernel's time (sort excluded); the "
                              "kernel is issue/latency bound, not HBM-bound, see profiles/; peak %s"
                              % (STEP_BYTES, "of measured" if peaks else "of fallback")},
+        "roofline_fp64": roofline_fp64,
         "gpu_launches": args.steps * (1 + ((1 + 3 * passes) if head & 2 else 0) + (1 if head & 8 else 0)),
         "track_errors": n_err,
         "clocks": clocks.summary(),

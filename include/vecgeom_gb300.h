@@ -316,6 +316,12 @@ int vg_nav_compute_step_and_next_volume_host(vg_geom *g, const double *x, const 
                                              const double *step_limit, const vg_navstate *in, vg_navstate *out,
                                              double *step, int32_t *status, size_t n, uint32_t flags, void *stream);
 
+/* ---------------------------------------------------------------- measurement utility
+ * FP64 FMA issue rate of the current device (DFMA instructions per second), timed on
+ * `stream` with CUDA events: the peak against which the navigation kernels' FP64 roofline
+ * is stated. No reference counterpart (a measurement aid, not part of the query path). */
+int vg_device_fp64_rate(double *fma_per_s, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

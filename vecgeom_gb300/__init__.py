@@ -102,6 +102,7 @@ _SIGS = {
                                                         _c_vp]),
     "vg_nav_sort_key_params": (ctypes.c_int, [_c_vp] * 5),
     "vg_nav_set_tuning": (ctypes.c_int, [_c_vp, ctypes.c_int32, ctypes.c_int32]),
+    "vg_device_fp64_rate": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double), _c_vp]),
     "vg_mlp_create": (ctypes.c_int, [_c_vp, ctypes.c_uint64, ctypes.POINTER(_c_vp)]),
     "vg_mlp_destroy": (None, [_c_vp]),
     "vg_mlp_param_count": (ctypes.c_size_t, [_c_vp]),
@@ -169,6 +170,15 @@ def _ptr(t):
 def _stream():
     import torch
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def device_fp64_rate():
+    """FP64 FMA instructions per second of the current CUDA device (a timed probe kernel):
+    the peak for the navigation kernels' FP64 roofline."""
+    load_library()
+    r = ctypes.c_double()
+    _check(_lib.vg_device_fp64_rate(ctypes.byref(r), _stream()), "vg_device_fp64_rate")
+    return r.value
 
 
 class Geometry:

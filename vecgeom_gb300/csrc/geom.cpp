@@ -1128,7 +1128,10 @@ int Geometry::upload(std::string &err)
       r.off             = soff[shp];
       std::memcpy(r.lb, &lbd[8 * (size_t)shp], sizeof(r.lb));
       const Xform &m = pvs[pv].xf.m;
-      for (int c = 0; c < 3; ++c) r.t[c] = m.t[c];
+      for (int c = 0; c < 3; ++c) {
+        r.t[c] = (float)m.t[c];
+        if (!(std::fabs(m.t[c]) <= 4000.)) r.exact_only = 1; // the FP32 pad covers |t| <= 4 m
+      }
       for (int c = 0; c < 9; ++c) r.r[c] = (float)m.r[c];
     }
   }

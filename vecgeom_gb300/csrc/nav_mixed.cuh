@@ -127,11 +127,14 @@ __device__ __forceinline__ ShapeLB leaf_lb(const LeafRec *rp)
   const float4 b = __ldg(reinterpret_cast<const float4 *>(rp) + 3);
   return ShapeLB{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
 }
-// p - t in FP64 rounded to FP32, then the FP32 rotation (the placement's rotation rounded
-// entry by entry), for a point; the rotation alone for a direction.
-__device__ __forceinline__ F3 leaf_local_point(const LeafRec *rp, V3 p)
+// The daughter-frame point and direction in FP32: pf - t and the rotation in FP32 from the
+// FP32 mother-frame point pf and direction df (each converted once per traversal: a
+// double/float conversion takes an FP64-pipe slot on GB300). With |p|, |t| <= kMaxCoord
+// (4 m) the FP32 rounding of pf, t and the difference is at most 3 * 2^-24 * 4000 mm =
+// 7.2e-4 mm per component and the FP32 rotation adds at most ~1.2e-3 mm, within kBoxPad.
+__device__ __forceinline__ F3 leaf_local_point(const LeafRec *rp, F3 pf)
 {
-  const F3 q{(float)(p.x - __ldg(&rp->t[0])), (float)(p.y - __ldg(&rp->t[1])), (float)(p.z - __ldg(&rp->t[2]))};
+  const F3 q{pf.x - __ldg(&rp->t[0]), pf.y - __ldg(&rp->t[1]), pf.z - __ldg(&rp->t[2])};
   const float *r = rp->r;
   return F3{fmaf(q.x, __ldg(r + 0), fmaf(q.y, __ldg(r + 3), q.z * __ldg(r + 6))),
             fmaf(q.x, __ldg(r + 1), fmaf(q.y, __ldg(r + 4), q.z * __ldg(r + 7))),
@@ -144,6 +147,10 @@ __device__ __forceinline__ F3 leaf_local_dir(const LeafRec *rp, F3 dd)
             fmaf(dd.x, __ldg(r + 1), fmaf(dd.y, __ldg(r + 4), dd.z * __ldg(r + 7))),
             fmaf(dd.x, __ldg(r + 2), fmaf(dd.y, __ldg(r + 5), dd.z * __ldg(r + 8)))};
 }
+__device__ __forceinline__ bool f32_coord_ok(F3 l)
+{
+  return fabsf(l.x) <= 4000.f && fabsf(l.y) <= 4000.f && fabsf(l.z) <= 4000.f;
+}
 
 // The record of placed volume pv (two 16-byte loads).
 __device__ __forceinline__ PvRec pv_rec(const DevGeom &g, int pv)
@@ -153,11 +160,12 @@ __device__ __forceinline__ PvRec pv_rec(const DevGeom &g, int pv)
   return PvRec{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
 }
 
-__device__ __forceinline__ float daughter_lb(const LeafRec *rp, V3 p, V3 d, float &ub)
+__device__ __forceinline__ float daughter_lb(const LeafRec *rp, F3 pf, F3 df, float &ub)
 {
   ub = INFINITY;
-  const F3 lp     = leaf_local_point(rp, p);
-  const F3 ld     = leaf_local_dir(rp, f3(d));
+  if (__ldg(&rp->exact_only)) return -INFINITY;
+  const F3 lp     = leaf_local_point(rp, pf);
+  const F3 ld     = leaf_local_dir(rp, df);
   const ShapeLB s = leaf_lb(rp);
   if (s.kind == 0.f) {
     const float lo[3] = {s.a0, s.a1, s.a2}, hi[3] = {s.a3, s.a4, s.a5};
@@ -188,10 +196,14 @@ __device__ __forceinline__ float daughter_lb(const LeafRec *rp, V3 p, V3 d, floa
 
 // Contains with an FP32 certain-outside / certain-inside test before the FP64 one.
 // Returns the daughter-local FP64 point in `lp` when it returns true.
-__device__ __forceinline__ bool pv_contains_mixed(const DevGeom &g, const LeafRec *rp, int pv, V3 p, V3 &lp)
+__device__ __forceinline__ bool pv_contains_mixed(const DevGeom &g, const LeafRec *rp, int pv, V3 p, F3 pf, V3 &lp)
 {
-  const Xform &m  = g.pv_xf[pv];
-  const F3 l      = leaf_local_point(rp, p);
+  const Xform &m = g.pv_xf[pv];
+  if (__ldg(&rp->exact_only)) {
+    lp = f64::to_local(m, p);
+    return f64::shape_contains_to(g, __ldg(&rp->type), __ldg(&rp->off), lp);
+  }
+  const F3 l      = leaf_local_point(rp, pf);
   const ShapeLB s = leaf_lb(rp);
   if (s.kind == 0.f) {
     const float lo[3] = {s.a0, s.a1, s.a2}, hi[3] = {s.a3, s.a4, s.a5};
@@ -215,15 +227,30 @@ __device__ __forceinline__ bool pv_contains_mixed(const DevGeom &g, const LeafRe
   return f64::shape_contains_to(g, __ldg(&rp->type), __ldg(&rp->off), lp);
 }
 
+// Out-of-line FP64 fallbacks for points beyond the FP32 range (rare: keeps their code out of
+// the hot loop).
+static __device__ __noinline__ int check_daughters_far(const DevGeom &g, int lv, V3 lp, V3 ld, double &step,
+                                                       int last_pv, int &hit_pv, int *nvisited)
+{
+  return f64::bvh_check_daughters(g, lv, lp, ld, step, last_pv, hit_pv, nvisited);
+}
+static __device__ __noinline__ bool level_locate_far(const DevGeom &g, int lv, int excl_pv, V3 lp, int &pv, V3 &dlp,
+                                                     int &status)
+{
+  return f64::bvh_level_locate(g, lv, excl_pv, lp, pv, dlp, status);
+}
+
 // BVH::CheckDaughterIntersections with FP32 pruning (see file comment). Candidates wait in
 // a small buffer sorted by lower bound; when it is full the lowest is evaluated in FP64,
 // which tightens the step and drops every candidate that can no longer win.
 constexpr int kCandBuf = 8;
 
-__device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, int node0, V3 lp, V3 ld, double &step,
+__device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, int lv, int node0, V3 lp, V3 ld, double &step,
                                                      int last_pv, int &hit_pv, int *nvisited, int first = -1)
 {
-  const F3 pf     = f3(lp);
+  const F3 pf = f3(lp);
+  // beyond the range the FP32 pad covers, the exact FP64 traversal decides alone
+  if (!f32_coord_ok(pf)) return check_daughters_far(g, lv, lp, ld, step, last_pv, hit_pv, nvisited);
   const F3 ldf    = f3(ld);
   const F3 inv{inv_dir(ldf.x), inv_dir(ldf.y), inv_dir(ldf.z)};
   float bound = __double2float_ru(step);
@@ -290,7 +317,7 @@ __device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, int node0
         slab_f(blo, bhi, pf, inv, tmin, tmax);
         if (tmin <= tmax && tmax >= 0.f && tmin < bound) {
           float ub;
-          const float lb = daughter_lb(rp, lp, ld, ub);
+          const float lb = daughter_lb(rp, pf, ldf, ub);
           add(lb, slot);
           // a certain upper bound of this daughter's distance bounds the step: whatever
           // starts beyond it can no longer be the first hit
@@ -327,10 +354,11 @@ __device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, int node0
 }
 
 // BVH::LevelLocate with FP32 box tests (padded) and mixed Contains.
-__device__ __forceinline__ bool level_locate_mixed(const DevGeom &g, int node0, int excl_pv, V3 lp, int &pv, V3 &dlp,
-                                                   int &status)
+__device__ __forceinline__ bool level_locate_mixed(const DevGeom &g, int lv, int node0, int excl_pv, V3 lp, int &pv,
+                                                   V3 &dlp, int &status)
 {
-  const F3 pf     = f3(lp);
+  const F3 pf = f3(lp);
+  if (!f32_coord_ok(pf)) return level_locate_far(g, lv, excl_pv, lp, pv, dlp, status);
   unsigned stack[32];
   int sp   = 1;
   stack[0] = 0;
@@ -344,7 +372,7 @@ __device__ __forceinline__ bool level_locate_mixed(const DevGeom &g, int node0, 
         int vol;
         leaf_box(rp, blo, bhi, vol);
         if (box_contains_f(blo, bhi, pf)) {
-          if (vol != excl_pv && pv_contains_mixed(g, rp, vol, lp, dlp)) {
+          if (vol != excl_pv && pv_contains_mixed(g, rp, vol, lp, pf, dlp)) {
             pv = vol;
             return true;
           }
@@ -370,6 +398,7 @@ __device__ __forceinline__ bool shape_contains_mixed(const DevGeom &g, const Sha
 {
   const ShapeLB s = lbs[r.shape];
   const F3 l      = f3(p);
+  if (!f32_coord_ok(l)) return f64::shape_contains_to(g, r.type, r.off, p);
   if (s.kind == 0.f) {
     const float lo[3] = {s.a0, s.a1, s.a2}, hi[3] = {s.a3, s.a4, s.a5};
     if (!box_contains_f(lo, hi, l)) return false;
@@ -405,7 +434,7 @@ __device__ __forceinline__ int locate_global_point_mixed(const DevGeom &g, const
     if (rec.nd == 0) return f64::nav_top(g, nav);
     int pv = -1;
     V3 tp;
-    if (!level_locate_mixed(g, rec.node0, -1, p, pv, tp, status)) return f64::nav_top(g, nav);
+    if (!level_locate_mixed(g, rec.lv, rec.node0, -1, p, pv, tp, status)) return f64::nav_top(g, nav);
     rec = pv_rec(g, pv);
     nav = nav_push_child(g, nav, rec.child);
     p   = tp;
@@ -423,7 +452,7 @@ __device__ __forceinline__ void locate_excl_mixed(const DevGeom &g, int vol, int
     if (rec.nd == 0) return;
     V3 tp;
     int cand = -1;
-    if (!level_locate_mixed(g, rec.node0, excl, p, cand, tp, status)) return;
+    if (!level_locate_mixed(g, rec.lv, rec.node0, excl, p, cand, tp, status)) return;
     rec = pv_rec(g, cand);
     p   = tp;
     nav = nav_push_child(g, nav, rec.child);
@@ -481,7 +510,7 @@ __device__ __forceinline__ double compute_step_mixed(const DevGeom &g, const Sha
       }
       if (ok) first = proposal;
     }
-    status = check_daughters_mixed(g, rec.node0, lp, ld, step, last, hit, nvisited, first);
+    status = check_daughters_mixed(g, rec.lv, rec.node0, lp, ld, step, last, hit, nvisited, first);
     if (status != kTrackOk) return 0.;
   }
   if (deq(step, kInfLength) && dgt(limit, 0.)) {

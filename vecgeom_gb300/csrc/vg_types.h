@@ -156,7 +156,9 @@ struct alignas(16) LeafRec {
   int32_t pv;         // placed volume
   int32_t type;       // shape type of the daughter
   float lb[8];        // FP32 bounding descriptor of the daughter's shape (shape_lbd)
-  double t[3];        // placement translation
+  float t[3];         // placement translation rounded to FP32
+  int32_t exact_only; // 1: translation beyond the FP32 range of the pruning (FP64 only)
+  int32_t pad[2];
   float r[9];         // placement rotation, each entry rounded to FP32
   int32_t off;        // shape record offset (doubles) of the daughter
 };
