@@ -494,12 +494,28 @@ int vg_nav_transport(const vg_geom *g, double *x, double *y, double *z, const do
   }
   vg::NavState *st = reinterpret_cast<vg::NavState *>(states);
   cudaError_t e    = vg::launch_transport_init(st, n, nsteps, status, list[0], cnt[0], s);
+  // With VG_NAV_QUEUE, once fewer tracks are alive than the GPU holds threads of the tail
+  // kernel, the rest of the stream runs as one refill pass (launch_transport_drain).
+  unsigned int drain_below = 0;
+  if (flags & VG_NAV_QUEUE) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
+      drain_below = (unsigned int)sms * 512u;
+  }
   int cur = 0, it = 0;
   while (e == cudaSuccess && it < max_steps) {
     unsigned int live = 0;
     e = cudaMemcpyAsync(&live, cnt[cur], sizeof(live), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess || live == 0) break;
+    if (live < drain_below) {
+      vg::TransportArgs ta{x,       y,           z,       dx,          dy,         dz,    st,
+                           nsteps,  status,      (int)max_steps, reinterpret_cast<vg::NavState *>(trace_states),
+                           trace_steps, trace_tracks, list[cur], live, nullptr, nullptr, nullptr};
+      e = vg::launch_transport_drain(g->geo.dev, ta, (flags & VG_PREC_MIXED) != 0, counter, s);
+      ++it;
+      break;
+    }
     const uint32_t *order = list[cur];
     if (flags & VG_NAV_SORT) {
       const uint32_t *sorted = nullptr;

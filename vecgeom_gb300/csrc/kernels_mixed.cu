@@ -140,6 +140,51 @@ __global__ void __launch_bounds__(Threads, MinBlocks) k_transport_iter(const Dev
   }
 }
 
+// Transport stream tail: each thread takes the next live track from a global counter and
+// steps it until it leaves the world, gives up or reaches max_steps, then takes another
+// (refill per lane). Each step is the iteration kernel's step on the same state, so the
+// results are those of running the remaining iterations one by one; what it saves is the
+// per-iteration sort, proposal and host round trip once too few tracks are left to fill
+// the GPU. No proposals (they only reorder the traversal).
+template <bool Mixed>
+__global__ void __launch_bounds__(256, 2) k_transport_drain(const DevGeom g, const TransportArgs a,
+                                                            unsigned long long *__restrict__ counter)
+{
+  const mixed::ShapeLB *lbs = reinterpret_cast<const mixed::ShapeLB *>(g.shape_lbd);
+  for (;;) {
+    const unsigned long long i = atomicAdd(counter, 1ull);
+    if (i >= a.n) break;
+    const size_t t = __ldg(a.list + i);
+    NavState s     = a.st[t];
+    f64::V3 p{a.x[t], a.y[t], a.z[t]};
+    const f64::V3 d{__ldg(a.dx + t), __ldg(a.dy + t), __ldg(a.dz + t)};
+    int k = a.nsteps[t];
+    for (;;) {
+      NavState o;
+      int st = 0;
+      const double step = Mixed ? mixed::compute_step_mixed(g, lbs, p, d, kInfLength, s, o, st, nullptr, -1)
+                                : f64::compute_step(g, p, d, kInfLength, s, o, st, nullptr);
+      if (t < a.trace_n) {
+        a.trace_st[t * (size_t)a.max_steps + k]   = o;
+        a.trace_step[t * (size_t)a.max_steps + k] = step;
+      }
+      p = f64::V3{p.x + step * d.x, p.y + step * d.y, p.z + step * d.z}; // OracleTransport: p += step d
+      s = o;
+      ++k;
+      if (st != kTrackOk) {
+        a.status[t] = st;
+        break;
+      }
+      if (o.navInd == 0 || k >= a.max_steps) break;
+    }
+    a.x[t]      = p.x;
+    a.y[t]      = p.y;
+    a.z[t]      = p.z;
+    a.st[t]     = s;
+    a.nsteps[t] = k;
+  }
+}
+
 __global__ void k_transport_init(const NavState *__restrict__ st, size_t n, int32_t *__restrict__ nsteps,
                                  int32_t *__restrict__ status, uint32_t *__restrict__ list,
                                  unsigned int *__restrict__ count)
@@ -232,6 +277,33 @@ cudaError_t launch_transport_iter(const DevGeom &g, const TransportArgs &a, bool
   if (blocks_per_sm == 3) return launch_transport<true, 128, 3>(g, a, counter, s);
   return blocks_per_sm == 2 ? launch_transport<true, 256, 2>(g, a, counter, s)
                             : launch_transport<true, 256, 1>(g, a, counter, s);
+}
+
+cudaError_t launch_transport_drain(const DevGeom &g, const TransportArgs &a, bool mixed, unsigned long long *counter,
+                                   cudaStream_t s)
+{
+  if (a.n == 0) return cudaSuccess;
+  static int resident[2] = {0, 0};
+  int &r = resident[mixed ? 1 : 0];
+  if (r == 0) {
+    int v = 0;
+    const cudaError_t e = mixed ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_transport_drain<true>, 256, 0)
+                                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_transport_drain<false>, 256, 0);
+    if (e != cudaSuccess) return e;
+    r = v > 0 ? v : 1;
+  }
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  size_t blocks = (size_t)sms * r, need = (a.n + 255) / 256;
+  if (blocks > need) blocks = need;
+  if (mixed)
+    k_transport_drain<true><<<(unsigned)blocks, 256, 0, s>>>(g, a, counter);
+  else
+    k_transport_drain<false><<<(unsigned)blocks, 256, 0, s>>>(g, a, counter);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_transport_init(const NavState *st, size_t n, int32_t *nsteps, int32_t *status, uint32_t *list,

@@ -77,6 +77,9 @@ struct TransportArgs {
 };
 cudaError_t launch_transport_iter(const DevGeom &g, const TransportArgs &a, bool mixed, unsigned long long *counter,
                                   int blocks_per_sm, cudaStream_t s);
+// Transport tail: steps every track of `list` to its end in one launch (refill per lane).
+cudaError_t launch_transport_drain(const DevGeom &g, const TransportArgs &a, bool mixed, unsigned long long *counter,
+                                   cudaStream_t s);
 cudaError_t launch_transport_init(const NavState *st, size_t n, int32_t *nsteps, int32_t *status, uint32_t *list,
                                   unsigned int *count, cudaStream_t s);
 // Fixed scratch of the no-allocation step entry point (noalloc.cu).
