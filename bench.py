@@ -31,13 +31,13 @@ sys.path.insert(0, ROOT)
 
 STEP_BYTES = 24 + 24 + 12 + 12 + 8  # p, d, state in, state out, step (FP64 SoA + 12 B states)
 # FP64-pipe thread instructions per scheduled detector step (sort keys 3.0 + proposal 10.2 +
-# step kernel 329.1), counted by ncu (sm__thread_inst_executed_pipe_fp64_pred_on over every
+# step kernel 289.4), counted by ncu (sm__thread_inst_executed_pipe_fp64_pred_on over every
 # launch of one scheduled step on 2^20 detector step inputs; the summary is under profiles/).
 # Per-thread counts do not depend on how lanes group into warps, so they hold at 2^22.
-FP64_OPS_PER_STEP = 342.3
-# DRAM bytes per launch of the step kernel, from the same capture (read 488.4 MB + write
-# 63.4 MB per 2^20 steps), scaled to the 2^22-step launch by the steps it processes.
-STEP_TRAFFIC_PER_STEP = (488.4e6 + 63.4e6) / (1 << 20)
+FP64_OPS_PER_STEP = 302.6
+# DRAM bytes per launch of the step kernel, from the same capture (read 499.5 MB + write
+# 66.3 MB per 2^20 steps), scaled to the 2^22-step launch by the steps it processes.
+STEP_TRAFFIC_PER_STEP = (499.5e6 + 66.3e6) / (1 << 20)
 # name -> (precision | scheduling flags): 1 = VG_PREC_MIXED, 2 = VG_NAV_SORT, 4 = VG_NAV_QUEUE
 # 8 = VG_NAV_LEARNED (explore the BVH subtree proposed by the trained model first)
 SCHEDULES = {"fp64": 0, "fp64_sort": 2, "mixed": 1, "mixed_sort": 3, "mixed_queue": 5, "mixed_sort_queue": 7,
@@ -631,7 +631,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": STEP_TRAFFIC_PER_STEP * n if head & 4 else None,
                      "traffic_note": "DRAM read + write of one step-kernel launch, ncu on 2^20 steps scaled to %d "
-                                     "(geometry L2 misses and the sorted-order gathers: 526 B/step vs 80 "
+                                     "(geometry L2 misses and the sorted-order gathers: 540 B/step vs 80 "
                                      "algorithmic)" % n,
                      "kernel": "k_step_mixed_queue" if head & 4 else ("k_step_mixed" if head & 1 else "k_step"),
                      "step_kernel_time_note": "sort and proposal kernels excluded" if head & 8 else "sort excluded",

@@ -67,3 +67,28 @@ def test_graph_replay_matches_eager(cuda, detector, flags_name):
     assert cuda.equal(step_g, step_e)
     assert model.error() == 0
     assert int((step_e > 0).sum().item()) > n // 2
+
+
+def test_pipelined_host_entry_matches_device(cuda, detector):
+    """The host-pointer step with a sorted schedule copies its inputs in chunks that overlap
+    the sort keys and proposals of the chunks already arrived; the result equals the
+    device-pointer call."""
+    import vecgeom_gb300 as vg
+    g, model = detector
+    flags = vg.PREC_MIXED | vg.NAV_SORT | vg.NAV_QUEUE | vg.NAV_LEARNED
+    n = (1 << 18) + 77
+    t, st = _inputs(cuda, g, n, 43)
+    out_d = cuda.empty_like(st)
+    step_d = cuda.empty(n, dtype=cuda.float64, device="cuda:0")
+    g.compute_step_and_next_volume(*t, st, out_d, step_d, flags=flags)
+    h = [a.cpu().pin_memory() for a in t]
+    sh = st.cpu().pin_memory()
+    out_h = cuda.empty(n * 12, dtype=cuda.uint8).pin_memory()
+    step_h = cuda.empty(n, dtype=cuda.float64).pin_memory()
+    status_h = cuda.empty(n, dtype=cuda.int32).pin_memory()
+    for _ in range(2):  # the second call reuses the staging buffers and copy stream
+        g.compute_step_and_next_volume_host(*h, sh, out_h, step_h, status=status_h, flags=flags)
+        assert cuda.equal(out_h, out_d.cpu())
+        assert cuda.equal(step_h, step_d.cpu())
+        assert int(status_h.abs().sum().item()) == 0
+    assert model.error() == 0

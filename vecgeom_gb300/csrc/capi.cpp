@@ -23,9 +23,17 @@ struct vg_geom {
                             // threads x resident blocks per SM
   const vg_mlp *proposer = nullptr; // learned proposal used by VG_NAV_LEARNED
   int propose_tensor      = 1;       // proposal kernel of VG_NAV_LEARNED: 1 tcgen05, 0 SIMT
+  // host-pointer step: a copy stream and per-chunk events for overlapping the inputs'
+  // host-to-device copies with the sort keys and proposals of the chunks already arrived
+  static constexpr int kCopyChunks = 4;
+  cudaStream_t copy_stream           = nullptr;
+  cudaEvent_t chunk_ready[kCopyChunks] = {};
   ~vg_geom()
   {
     if (staging) cudaFree(staging);
+    for (cudaEvent_t ev : chunk_ready)
+      if (ev) cudaEventDestroy(ev);
+    if (copy_stream) cudaStreamDestroy(copy_stream);
   }
 };
 
@@ -128,9 +136,44 @@ size_t step_workspace_bytes(size_t n, uint32_t flags)
   return b;
 }
 
+// Workspace of a scheduled step: work-queue counter (256 bytes), proposal slots (n bytes,
+// with VG_NAV_LEARNED), then the sort arrays (keys first).
+struct StepWs {
+  unsigned long long *counter = nullptr;
+  int8_t *slots               = nullptr;
+  unsigned char *sort         = nullptr;
+};
+StepWs step_ws(void *ws, size_t n, uint32_t flags)
+{
+  StepWs r;
+  unsigned char *w = static_cast<unsigned char *>(ws);
+  if (flags & VG_NAV_QUEUE) {
+    r.counter = reinterpret_cast<unsigned long long *>(w);
+    w += 256;
+  }
+  if (flags & VG_NAV_LEARNED) {
+    r.slots = reinterpret_cast<int8_t *>(w);
+    w += (n + 255) & ~size_t(255);
+  }
+  r.sort = w;
+  return r;
+}
+
+cudaError_t propose_launch(const vg_geom *g, const vg::StepArgs &a, int8_t *slots, cudaStream_t s)
+{
+  // proposals are stored per track, so they are computed in track order: coalesced input
+  // loads beat the geometry locality of the sorted order
+  vg::StepArgs pa = a;
+  pa.order        = nullptr;
+  return g->propose_tensor ? vg::launch_mlp_propose_tc(g->geo.dev, pa, g->proposer->wbf, slots, g->proposer->err, s)
+                           : vg::launch_mlp_propose(g->geo.dev, pa, g->proposer->wbf, slots, s);
+}
+
 // Validated step launch with optional sort and work queue; `ws` holds the counter
-// (256 bytes, first) and the sort arrays.
-int step_launch(const vg_geom *g, vg::StepArgs a, uint32_t flags, void *ws, size_t ws_bytes, cudaStream_t s)
+// (256 bytes, first) and the sort arrays. prepared: the sort keys and proposals of all
+// tracks are already in the workspace (the pipelined host-pointer entry point).
+int step_launch(const vg_geom *g, vg::StepArgs a, uint32_t flags, void *ws, size_t ws_bytes, cudaStream_t s,
+                bool prepared = false)
 {
   if (flags & ~kNavFlags) return fail(VG_EINVAL, "invalid navigation flags");
   if ((flags & (VG_NAV_QUEUE | VG_NAV_LEARNED)) && !(flags & VG_PREC_MIXED))
@@ -140,33 +183,21 @@ int step_launch(const vg_geom *g, vg::StepArgs a, uint32_t flags, void *ws, size
   const size_t need = step_workspace_bytes(a.n, flags);
   if (need > 0 && (!ws || ws_bytes < need || (reinterpret_cast<uintptr_t>(ws) & 255u)))
     return fail(VG_EINVAL, "workspace missing, too small or not 256-byte aligned");
-  unsigned char *w = static_cast<unsigned char *>(ws);
-  unsigned long long *counter = nullptr;
-  if (flags & VG_NAV_QUEUE) {
-    counter = reinterpret_cast<unsigned long long *>(w);
-    w += 256;
-  }
-  int8_t *slots = nullptr;
-  if (flags & VG_NAV_LEARNED) {
-    slots = reinterpret_cast<int8_t *>(w);
-    w += (a.n + 255) & ~size_t(255);
-  }
+  const StepWs w = step_ws(ws, a.n, flags);
+  unsigned long long *counter = w.counter;
   cudaError_t e = cudaSuccess;
   if (flags & VG_NAV_SORT) {
     const uint32_t *order = nullptr;
-    e = vg::launch_nav_sort(g->geo.dev, g->sort, a.x, a.y, a.z, a.in, a.n, w, &order, s);
+    e = vg::launch_nav_sort(g->geo.dev, g->sort, a.x, a.y, a.z, a.in, a.n, w.sort, &order, s, nullptr, prepared);
     if (e != cudaSuccess) return cuda_fail(e, "track sort launch");
     a.order = order;
   }
   if (flags & VG_NAV_LEARNED) {
-    // proposals are stored per track, so they are computed in track order: coalesced
-    // input loads beat the geometry locality of the sorted order
-    vg::StepArgs pa = a;
-    pa.order        = nullptr;
-    e = g->propose_tensor ? vg::launch_mlp_propose_tc(g->geo.dev, pa, g->proposer->wbf, slots, g->proposer->err, s)
-                          : vg::launch_mlp_propose(g->geo.dev, pa, g->proposer->wbf, slots, s);
-    if (e != cudaSuccess) return cuda_fail(e, "proposal launch");
-    a.proposal = slots;
+    if (!prepared) {
+      e = propose_launch(g, a, w.slots, s);
+      if (e != cudaSuccess) return cuda_fail(e, "proposal launch");
+    }
+    a.proposal = w.slots;
   }
   if (flags & VG_NAV_QUEUE)
     e = vg::launch_step_mixed_queue(g->geo.dev, a, counter, g->queue_blocks, s);
@@ -671,14 +702,50 @@ int vg_nav_compute_step_and_next_volume_host(vg_geom *g, const double *x, const 
   cudaStream_t s    = (cudaStream_t)stream;
   const double *src[7] = {x, y, z, dx, dy, dz, step_limit};
   cudaError_t e        = cudaSuccess;
-  for (int k = 0; k < 7 && e == cudaSuccess; ++k)
-    if (src[k]) e = cudaMemcpyAsync(d[k], src[k], nd, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(din, in, ns, cudaMemcpyHostToDevice, s);
-  if (e != cudaSuccess) return cuda_fail(e, "host-to-device copy");
   vg::StepArgs a{d[0], d[1], d[2], d[3], d[4], d[5], step_limit ? d[6] : nullptr,
                  reinterpret_cast<const vg::NavState *>(din), reinterpret_cast<vg::NavState *>(dout), d[7],
                  status ? dst : nullptr, nullptr, n};
-  const int rc = step_launch(g, a, flags, dws, wsb, s);
+  // Sorted schedules: the inputs go over in chunks on a copy stream, and the sort keys (and
+  // proposals) of each chunk start as soon as it has arrived, so most of the copy hides
+  // behind that work; the radix passes and the step wait for all chunks.
+  const bool pipelined = (flags & VG_NAV_SORT) && n >= (size_t(1) << 18);
+  if (pipelined) {
+    if (!g->copy_stream) {
+      e = cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking);
+      for (int c = 0; c < vg_geom::kCopyChunks && e == cudaSuccess; ++c)
+        e = cudaEventCreateWithFlags(&g->chunk_ready[c], cudaEventDisableTiming);
+      if (e != cudaSuccess) return cuda_fail(e, "copy stream setup");
+    }
+    const StepWs w = step_ws(dws, n, flags);
+    const size_t per = (n + vg_geom::kCopyChunks - 1) / vg_geom::kCopyChunks;
+    for (int c = 0; c < vg_geom::kCopyChunks && e == cudaSuccess; ++c) {
+      const size_t b = std::min(n, c * per), m = std::min(n, b + per) - b;
+      for (int k = 0; k < 7 && e == cudaSuccess; ++k)
+        if (src[k] && m) e = cudaMemcpyAsync(d[k] + b, src[k] + b, m * sizeof(double), cudaMemcpyHostToDevice, g->copy_stream);
+      if (e == cudaSuccess && m)
+        e = cudaMemcpyAsync(din + b, in + b, m * sizeof(vg_navstate), cudaMemcpyHostToDevice, g->copy_stream);
+      if (e == cudaSuccess) e = cudaEventRecord(g->chunk_ready[c], g->copy_stream);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "host-to-device copy");
+    for (int c = 0; c < vg_geom::kCopyChunks && e == cudaSuccess; ++c) {
+      const size_t b = std::min(n, c * per), m = std::min(n, b + per) - b;
+      e = cudaStreamWaitEvent(s, g->chunk_ready[c], 0);
+      if (e == cudaSuccess)
+        e = vg::launch_nav_sort_keys(g->geo.dev, g->sort, a.x, a.y, a.z, a.in, b, b + m, w.sort, s);
+      if (e == cudaSuccess && (flags & VG_NAV_LEARNED) && m) {
+        vg::StepArgs pa{a.x + b, a.y + b, a.z + b, a.dx + b, a.dy + b, a.dz + b, nullptr, a.in + b,
+                        nullptr,  nullptr, nullptr, nullptr, m};
+        e = propose_launch(g, pa, w.slots + b, s);
+      }
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "key/proposal launch");
+  } else {
+    for (int k = 0; k < 7 && e == cudaSuccess; ++k)
+      if (src[k]) e = cudaMemcpyAsync(d[k], src[k], nd, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(din, in, ns, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(e, "host-to-device copy");
+  }
+  const int rc = step_launch(g, a, flags, dws, wsb, s, pipelined);
   if (rc != VG_OK) return rc;
   e = cudaMemcpyAsync(out, dout, ns, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(step, d[7], nd, cudaMemcpyDeviceToHost, s);

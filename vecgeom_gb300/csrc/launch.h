@@ -51,10 +51,15 @@ size_t nav_sort_workspace_bytes(size_t n);
 int sort_key_bits(const SortKeyParams &p);
 const uint32_t *nav_sort_keys_of(const uint32_t *order, const void *ws, size_t n); // keys paired with `order`
 // Keys + stable radix sort of the n tracks (or of the n track ids in `list`); *order
-// receives the sorted track indices (inside the workspace).
+// receives the sorted track indices (inside the workspace). keys_done: the keys of all n
+// tracks were already written by launch_nav_sort_keys (ranges of tracks, e.g. as their
+// inputs arrive), only the radix passes run.
 cudaError_t launch_nav_sort(const DevGeom &g, const SortKeyParams &p, const double *x, const double *y,
                             const double *z, const NavState *in, size_t n, void *ws, const uint32_t **order,
-                            cudaStream_t s, const uint32_t *list = nullptr);
+                            cudaStream_t s, const uint32_t *list = nullptr, bool keys_done = false);
+cudaError_t launch_nav_sort_keys(const DevGeom &g, const SortKeyParams &p, const double *x, const double *y,
+                                 const double *z, const NavState *in, size_t begin, size_t end, void *ws,
+                                 cudaStream_t s);
 
 // One iteration of the transport stream over the n track ids in `list` (visiting order):
 // step each track, move it (p += step d), store its new state in place, count the step,

@@ -36,11 +36,11 @@ __device__ __forceinline__ uint32_t cell(double c, float lo, float scale, uint32
 __global__ void __launch_bounds__(256) k_sort_keys(const DevGeom g, const SortKeyParams p, const double *__restrict__ x,
                                                    const double *__restrict__ y, const double *__restrict__ z,
                                                    const NavState *__restrict__ in, const uint32_t *__restrict__ list,
-                                                   size_t n, uint32_t *__restrict__ keys)
+                                                   size_t begin, size_t end, uint32_t *__restrict__ keys)
 {
   const uint32_t maxc = (1u << p.cell_bits) - 1u;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+  for (size_t j = begin + (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < end; j += stride) {
     const size_t i     = list ? (size_t)__ldg(list + j) : j;
     const uint32_t nav = in[i].navInd;
     uint32_t key       = 0xffffffffu; // outside the world or not a table node: last
@@ -204,9 +204,19 @@ const uint32_t *nav_sort_keys_of(const uint32_t *order, const void *ws, size_t n
 
 int sort_key_bits(const SortKeyParams &p) { return p.lv_bits + 3 * p.cell_bits; }
 
+cudaError_t launch_nav_sort_keys(const DevGeom &g, const SortKeyParams &p, const double *x, const double *y,
+                                 const double *z, const NavState *in, size_t begin, size_t end, void *ws,
+                                 cudaStream_t s)
+{
+  if (end <= begin) return cudaSuccess;
+  k_sort_keys<<<grid_for(end - begin, 256), 256, 0, s>>>(g, p, x, y, z, in, nullptr, begin, end,
+                                                        static_cast<uint32_t *>(ws));
+  return cudaGetLastError();
+}
+
 cudaError_t launch_nav_sort(const DevGeom &g, const SortKeyParams &p, const double *x, const double *y,
                             const double *z, const NavState *in, size_t n, void *ws, const uint32_t **order,
-                            cudaStream_t s, const uint32_t *list)
+                            cudaStream_t s, const uint32_t *list, bool keys_done)
 {
   *order = nullptr;
   if (n == 0) return cudaSuccess;
@@ -217,7 +227,7 @@ cudaError_t launch_nav_sort(const DevGeom &g, const SortKeyParams &p, const doub
   uint32_t *v0 = reinterpret_cast<uint32_t *>(w + 2 * a), *v1 = reinterpret_cast<uint32_t *>(w + 3 * a);
   uint32_t *hist   = reinterpret_cast<uint32_t *>(w + 4 * a);
   uint32_t *totals = reinterpret_cast<uint32_t *>(w + 4 * a + align256(256 * (size_t)ntiles * sizeof(uint32_t)));
-  k_sort_keys<<<grid_for(n, 256), 256, 0, s>>>(g, p, x, y, z, in, list, n, k0);
+  if (!keys_done) k_sort_keys<<<grid_for(n, 256), 256, 0, s>>>(g, p, x, y, z, in, list, 0, n, k0);
   // Digits above the key's width are all zero (invalid states carry all-ones keys, which
   // sort last within every pass), so only the passes that cover the key bits are run.
   const int bits   = sort_key_bits(p);
