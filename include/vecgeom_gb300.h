@@ -48,6 +48,7 @@ extern "C" {
 #define VG_SHAPE_TORUS2 6
 #define VG_SHAPE_TRD 7
 #define VG_SHAPE_BOOLEAN_SUBTRACTION 8
+#define VG_SHAPE_TRAPEZOID 9
 
 /* Precision flags for queries and navigation */
 #define VG_PREC_FP64 0u  /* plain FP64: results identical to the reference's FP64 path          */
@@ -108,6 +109,14 @@ int32_t vg_geom_add_polyhedron(vg_geom *g, double phistart, double phidelta, int
 int32_t vg_geom_add_torus2(vg_geom *g, double rmin, double rmax, double rtor, double sphi, double dphi);
 /* UnplacedTrd(dx1, dx2, dy1, dy2, dz) (VecGeom/volumes/TrdStruct.h:20-39) */
 int32_t vg_geom_add_trd(vg_geom *g, double dx1, double dx2, double dy1, double dy2, double dz);
+/* UnplacedTrapezoid(dz, theta, phi, dy1, dx1, dx2, alpha1, dy2, dx3, dx4, alpha2), angles in
+ * radians (VecGeom/volumes/UnplacedTrapezoid.h:56-64). The Trd-, box- and parallelepiped-like
+ * constructors of UnplacedTrapezoid.h:90-102 are this call with zero angles / equal sides. */
+int32_t vg_geom_add_trap(vg_geom *g, double dz, double theta, double phi, double dy1, double dx1, double dx2,
+                         double alpha1, double dy2, double dx3, double dx4, double alpha2);
+/* UnplacedTrapezoid(TrapCorners) (VecGeom/volumes/UnplacedTrapezoid.h:84-86): corners[24] = eight
+ * (x, y, z) in the order (---) (+--) (-+-) (++-) (--+) (+-+) (-++) (+++); dz is the last z. */
+int32_t vg_geom_add_trap_corners(vg_geom *g, const double *corners);
 /* UnplacedBooleanVolume<kSubtraction>(left, right): operands are placed volumes created
  * with vg_geom_place (VecGeom/volumes/BooleanStruct.h:19-33) */
 int32_t vg_geom_add_boolean_subtraction(vg_geom *g, int32_t left_pv, int32_t right_pv);

@@ -106,6 +106,13 @@ class OracleGeometry:
     def add_boolean_subtraction(self, left_pv, right_pv):
         return self._shape(8, [left_pv, right_pv])
 
+    def add_trap(self, dz, theta, phi, dy1, dx1, dx2, alpha1, dy2, dx3, dx4, alpha2):
+        return self._shape(9, [dz, theta, phi, dy1, dx1, dx2, alpha1, dy2, dx3, dx4, alpha2])
+
+    def add_trap_corners(self, corners):
+        c = np.asarray(corners, dtype=np.float64).reshape(24)
+        return self._shape(9, list(c))
+
     def add_logical_volume(self, shape):
         return _lib.oracle_add_lv(self._h, shape)
 

@@ -39,7 +39,8 @@ extern "C" {
 void *oracle_geom_create() { return new Geometry(); }
 void oracle_geom_destroy(void *g) { delete static_cast<Geometry *>(g); }
 
-// type: 1 Box, 2 Tube, 3 Cone, 4 Polycone, 5 Polyhedron, 6 Torus2, 7 Trd, 8 BooleanSubtraction
+// type: 1 Box, 2 Tube, 3 Cone, 4 Polycone, 5 Polyhedron, 6 Torus2, 7 Trd, 8 BooleanSubtraction,
+// 9 Trapezoid (11 parameters, or 24 = eight corners x, y, z)
 int oracle_add_shape(void *gp, int type, const double *p, int np)
 {
   Geometry *g = static_cast<Geometry *>(gp);
@@ -61,6 +62,17 @@ int oracle_add_shape(void *gp, int type, const double *p, int np)
   case 6: s = new Torus2(p[0], p[1], p[2], p[3], p[4]); break;
   case 7: s = new Trd(p[0], p[1], p[2], p[3], p[4]); break;
   case 8: s = new BooleanMinus(g->pvs.at((int)p[0]).get(), g->pvs.at((int)p[1]).get()); break;
+  case 9:
+    if (np == 24) {
+      Vec3 c[8];
+      for (int k = 0; k < 8; ++k) c[k] = Vec3(p[3 * k], p[3 * k + 1], p[3 * k + 2]);
+      s = new Trap(c);
+    } else if (np == 11) {
+      s = new Trap(p);
+    } else {
+      return -1;
+    }
+    break;
   default: return -1;
   }
   (void)np;

@@ -246,6 +246,180 @@ void Trd::Extent(Vec3 &lo, Vec3 &hi) const
   hi = Vec3(Max(fDX1, fDX2), Max(fDY1, fDY2), fDZ);
 }
 
+// ====================================================================== Trap
+// UnplacedTrapezoid.h:56-64 (tan of the alphas), TrapezoidStruct.h CalculateCached
+// (tan(theta) cos(phi), tan(theta) sin(phi)), UnplacedTrapezoid.cpp:447-466
+// FromParametersToCorners, then MakePlanes on those corners.
+Trap::Trap(const double *par)
+{
+  const double dz = par[0], theta = par[1], phi = par[2], dy1 = par[3], dx1 = par[4], dx2 = par[5];
+  const double ta1 = std::tan(par[6]), dy2 = par[7], dx3 = par[8], dx4 = par[9], ta2 = std::tan(par[10]);
+  const double tcp = std::tan(theta) * std::cos(phi), tsp = std::tan(theta) * std::sin(phi);
+  fDz                = dz;
+  const double a1    = ta1 * dy1, a2 = ta2 * dy2;
+  const double xz    = tcp * dz, yz = tsp * dz;
+  Vec3 pt[8];
+  pt[0] = Vec3(-xz - a1 - dx1, -yz - dy1, -dz);
+  pt[1] = Vec3(-xz - a1 + dx1, -yz - dy1, -dz);
+  pt[2] = Vec3(-xz + a1 - dx2, -yz + dy1, -dz);
+  pt[3] = Vec3(-xz + a1 + dx2, -yz + dy1, -dz);
+  pt[4] = Vec3(+xz - a2 - dx3, +yz - dy2, +dz);
+  pt[5] = Vec3(+xz - a2 + dx3, +yz - dy2, +dz);
+  pt[6] = Vec3(+xz + a2 - dx4, +yz + dy2, +dz);
+  pt[7] = Vec3(+xz + a2 + dx4, +yz + dy2, +dz);
+  MakePlanes(pt);
+}
+// UnplacedTrapezoid.cpp:496-524 fromCornersToParameters: dz from the last corner, planes
+// straight from the corners (the derived parameters are not used by the queries).
+Trap::Trap(const Vec3 *corners)
+{
+  fDz = corners[7].z();
+  MakePlanes(corners);
+}
+// UnplacedTrapezoid.cpp:630-679 MakePlanes: faces (0,1,5,4) -Y, (2,6,7,3) +Y, (0,4,6,2) -X,
+// (1,3,7,5) +X.
+void Trap::MakePlanes(const Vec3 *pt)
+{
+  MakeAPlane(pt[0], pt[1], pt[5], pt[4], 0);
+  MakeAPlane(pt[2], pt[6], pt[7], pt[3], 1);
+  MakeAPlane(pt[0], pt[4], pt[6], pt[2], 2);
+  MakeAPlane(pt[1], pt[3], pt[7], pt[5], 3);
+}
+// UnplacedTrapezoid.cpp:569-620 MakeAPlane: normal (p3 - p1) x (p4 - p2) scaled by 1/|n|
+// (Vector3D::Normalize), d = -n . (p1 + p2 + p3 + p4) / 4 (summed left to right, times 0.25).
+void Trap::MakeAPlane(Vec3 const &p1, Vec3 const &p2, Vec3 const &p3, Vec3 const &p4, int i)
+{
+  const Vec3 u = p3 - p1, v = p4 - p2;
+  Vec3 n(u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]);
+  const double inv = 1. / n.Mag();
+  n                = n * inv;
+  const Vec3 c     = 0.25 * (((p1 + p2) + p3) + p4);
+  fA[i] = n[0], fB[i] = n[1], fC[i] = n[2], fD[i] = -n.Dot(c);
+}
+// TrapezoidImplementation.h:82-106 + PlaneShell.h GenericKernelForContainsAndInside
+void Trap::ContainsAndInside(Vec3 const &p, bool forInside, bool &cin, bool &cout) const
+{
+  const double h = forInside ? kHalfTolerance : 0.;
+  cout           = Abs(p.z()) > fDz + (forInside ? kHalfTolerance : 0.);
+  if (forInside) cin = Abs(p.z()) < fDz - kHalfTolerance;
+  double dist[4];
+  for (int i = 0; i < 4; ++i) dist[i] = PlaneDist(i, p);
+  for (int i = 0; i < 4; ++i) {
+    cout = cout || dist[i] > 0. + h;
+    if (forInside) cin = cin && dist[i] < 0. - h;
+  }
+}
+// TrapezoidImplementation.h:65-78 Inside (outside assigned first, then inside), :56-64 Contains
+int Trap::Inside(Vec3 const &p) const
+{
+  bool cin = false, cout = false;
+  ContainsAndInside(p, true, cin, cout);
+  int r = kSurface;
+  if (cout) r = kOutside;
+  if (cin) r = kInside;
+  return r;
+}
+bool Trap::Contains(Vec3 const &p) const
+{
+  bool cin = false, cout = false;
+  ContainsAndInside(p, false, cin, cout);
+  return !cout;
+}
+// TrapezoidImplementation.h:107-126 (z slab) + PlaneShell.h DistanceToIn (side planes clip
+// [smin, smax]; early returns with kInfLength)
+double Trap::DistanceToIn(Vec3 const &p, Vec3 const &d, double) const
+{
+  const double sz  = Sign(d.z());
+  const double max = sz * fDz - p.z();
+  if (sz * max < 0.0 + kHalfTolerance) return kInfLength;
+  const double invdir = 1.0 / NonZero(d.z());
+  double smax         = max * invdir;
+  double smin         = -(sz * fDz + p.z()) * invdir;
+  double pdist[4], proj[4], vdist[4];
+  for (int i = 0; i < 4; ++i) {
+    pdist[i] = PlaneDist(i, p);
+    proj[i]  = PlaneProj(i, d);
+    vdist[i] = -pdist[i] / NonZero(proj[i]);
+  }
+  for (int i = 0; i < 4; ++i) {
+    if (pdist[i] > 0. + kHalfTolerance && proj[i] >= 0.) return kInfLength;
+    if (pdist[i] > 0. - kHalfTolerance && proj[i] > 0.) return kInfLength;
+  }
+  for (int i = 0; i < 4; ++i) {
+    const bool posPoint = pdist[i] > 0. - kHalfTolerance;
+    const bool posDir   = proj[i] > 0;
+    const bool fromIn   = !posPoint && posDir;
+    const bool fromOut  = posPoint && !posDir;
+    if ((fromIn && vdist[i] < smin) || (fromOut && vdist[i] > smax)) return kInfLength;
+    if (fromOut && vdist[i] > smin) smin = vdist[i];
+    if (fromIn && vdist[i] < smax) smax = vdist[i];
+  }
+  return smin <= smax ? smin : kInfLength;
+}
+// TrapezoidImplementation.h:151-167 + PlaneShell.h DistanceToOut (planes taken in order:
+// -1 when outside a plane, then any smaller exit distance of a plane the ray leaves by)
+double Trap::DistanceToOut(Vec3 const &p, Vec3 const &d, double) const
+{
+  if (Abs(p.z()) > fDz + kHalfTolerance) return -1.;
+  double distance    = kInfLength;
+  const double distz = (Sign(d.z()) * fDz - p.z()) / NonZero(d.z());
+  if (d.z() != 0.) distance = distz;
+  double out = kInfLength;
+  double pdist[4], proj[4], vdist[4];
+  for (int i = 0; i < 4; ++i) {
+    pdist[i] = PlaneDist(i, p);
+    proj[i]  = PlaneProj(i, d);
+    vdist[i] = -pdist[i] / NonZero(proj[i]);
+  }
+  for (int i = 0; i < 4; ++i) {
+    if (pdist[i] > kHalfTolerance) out = -1.;
+    if (proj[i] > 0. && vdist[i] < out) out = vdist[i];
+  }
+  if (out < distance) distance = out;
+  return distance;
+}
+// TrapezoidImplementation.h:183-200 + PlaneShell.h SafetyToIn (N = 4: sequential maximum)
+double Trap::SafetyToIn(Vec3 const &p) const
+{
+  double safety = Abs(p.z()) - fDz;
+  double dist[4];
+  for (int i = 0; i < 4; ++i) dist[i] = PlaneDist(i, p);
+  for (int i = 0; i < 4; ++i)
+    if (dist[i] > safety) safety = dist[i];
+  return safety;
+}
+// TrapezoidImplementation.h:201-218 + PlaneShell.h SafetyToOut (N = 4: sequential minimum)
+double Trap::SafetyToOut(Vec3 const &p) const
+{
+  double safety = fDz - Abs(p.z());
+  double dist[4];
+  for (int i = 0; i < 4; ++i) dist[i] = -PlaneDist(i, p);
+  for (int i = 0; i < 4; ++i)
+    if (dist[i] < safety) safety = dist[i];
+  return safety;
+}
+// UnplacedTrapezoid.cpp:298-337 Extent on the corners of UnplacedTrapezoid.cpp:468-494
+// fromPlanesToCorners (each corner re-derived from the planes).
+void Trap::Extent(Vec3 &lo, Vec3 &hi) const
+{
+  const double z = fDz;
+  double y[8], x[8];
+  y[0] = y[1] = -(fD[0] - z * fC[0]) / fB[0];
+  y[2] = y[3] = -(fD[1] - z * fC[1]) / fB[1];
+  y[4] = y[5] = -(fD[0] + z * fC[0]) / fB[0];
+  y[6] = y[7] = -(fD[1] + z * fC[1]) / fB[1];
+  // corner k lies on the y plane yp (0 or 1) and the x plane xp (2 or 3), at z = -+fDz
+  for (int k = 0; k < 8; ++k) {
+    const int yp = (k >> 1) & 1, xp = 2 + (k & 1);
+    const double s = (k < 4) ? -z : z;
+    x[k] = ((fB[xp] / fB[yp]) * (fD[yp] + s * fC[yp]) - (fD[xp] + s * fC[xp])) / fA[xp];
+  }
+  auto mx = [](const double *v) { return Max(Max(Max(v[0], v[1]), Max(v[2], v[3])), Max(Max(v[4], v[5]), Max(v[6], v[7]))); };
+  auto mn = [](const double *v) { return Min(Min(Min(v[0], v[1]), Min(v[2], v[3])), Min(Min(v[4], v[5]), Min(v[6], v[7]))); };
+  lo = Vec3(mn(x), mn(y), -fDz);
+  hi = Vec3(mx(x), mx(y), fDz);
+}
+
 // ====================================================================== Polycone
 // PolyconeStruct.h:124-239 Init (sections are ConeStruct(prevRmin, prevRmax, rMin, rMax,
 // dz, phiStart, phiTotal) shifted to the middle of their z range)

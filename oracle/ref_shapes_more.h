@@ -28,6 +28,31 @@ struct Trd : UnplacedShape {
   void Extent(Vec3 &lo, Vec3 &hi) const override;
 };
 
+// VecGeom/volumes/TrapezoidStruct.h, source/UnplacedTrapezoid.cpp (construction),
+// VecGeom/volumes/kernel/TrapezoidImplementation.h with VecGeom/base/PlaneShell.h (the
+// VECGEOM_PLANESHELL build, CMakeLists.txt:156 default ON): two z planes at +-fDz and four
+// side planes a x + b y + c z + d = 0 with outward unit normals, in the order -Y, +Y, -X, +X.
+struct Trap : UnplacedShape {
+  double fDz = 0.;
+  double fA[4] = {}, fB[4] = {}, fC[4] = {}, fD[4] = {};
+  // UnplacedTrapezoid(dz, theta, phi, dy1, dx1, dx2, alpha1, dy2, dx3, dx4, alpha2), angles in radians
+  explicit Trap(const double *par);
+  // UnplacedTrapezoid(TrapCorners): corners p0(---) p1(+--) p2(-+-) p3(++-) p4(--+) p5(+-+) p6(-++) p7(+++)
+  explicit Trap(const Vec3 *corners);
+  void MakePlanes(const Vec3 *pt);
+  void MakeAPlane(Vec3 const &p1, Vec3 const &p2, Vec3 const &p3, Vec3 const &p4, int i);
+  double PlaneDist(int i, Vec3 const &p) const { return fA[i] * p.x() + fB[i] * p.y() + fC[i] * p.z() + fD[i]; }
+  double PlaneProj(int i, Vec3 const &d) const { return fA[i] * d.x() + fB[i] * d.y() + fC[i] * d.z(); }
+  void ContainsAndInside(Vec3 const &p, bool forInside, bool &cin, bool &cout) const;
+  int Inside(Vec3 const &p) const override;
+  bool Contains(Vec3 const &p) const override;
+  double DistanceToIn(Vec3 const &p, Vec3 const &d, double) const override;
+  double DistanceToOut(Vec3 const &p, Vec3 const &d, double) const override;
+  double SafetyToIn(Vec3 const &p) const override;
+  double SafetyToOut(Vec3 const &p) const override;
+  void Extent(Vec3 &lo, Vec3 &hi) const override;
+};
+
 // VecGeom/volumes/PolyconeStruct.h (Init), VecGeom/volumes/kernel/PolyconeImplementation.h
 struct Polycone : UnplacedShape {
   double fStartPhi = 0, fDeltaPhi = 0;

@@ -1,6 +1,6 @@
 """Extract known-answer vectors from VecGeom's shape unit tests into JSON fixtures.
 
-Reads test/unit_tests/Test{Box,Tube,Cons,Polycone,Torus2,Trd,Polyhedra}.cpp of a VecGeom source
+Reads test/unit_tests/Test{Box,Tube,Cons,Polycone,Torus2,Trd,Polyhedra,Trap}.cpp of a VecGeom source
 tree AS TEXT (nothing of it is compiled or run) and records, for every assert that checks
 a query result of a shape constructed in the test:
 
@@ -36,7 +36,10 @@ FILES = {
     "Torus2": ("TestTorus2.cpp", {"Torus_t": "torus2"}),
     "Trd": ("TestTrd.cpp", {"Trd_t": "trd"}),
     "Polyhedra": ("TestPolyhedra.cpp", {"Polyhedra_t": "polyhedron"}),
+    "Trap": ("TestTrap.cpp", {"Trap_t": "trap", "vecgeom::UnplacedTrapezoid": "trap"}),
 }
+# unplaced shapes constructed without a label argument
+NO_LABEL = {"vecgeom::UnplacedTrapezoid"}
 QUERIES = {"Inside", "Contains", "DistanceToIn", "DistanceToOut", "SafetyToIn", "SafetyToOut"}
 
 
@@ -245,6 +248,7 @@ class Extractor:
         self.shape_types = shape_types
         self.env = dict(BASE_ENV)
         self.shapes = {}   # var -> {"type", "args"}
+        self.lvs = {}      # logical-volume var -> shape var
         self.results = {}  # var -> pending query descriptor
         self.cases = []
         self.skipped = 0
@@ -396,8 +400,10 @@ class Extractor:
                 args = split_top(mm.group(2))
                 try:
                     vals = []
-                    for a in args[1:]:
+                    for a in args[0 if m.group(1) in NO_LABEL else 1:]:
                         v = self.ev(a)
+                        if isinstance(v, list):
+                            v = [list(e.v) if isinstance(e, V) else float(e) for e in v]
                         vals.append(v if isinstance(v, list) else float(v))
                     self.shapes[mm.group(1)] = {"type": self.shape_types[m.group(1)], "args": vals}
                 except Exception:
@@ -422,10 +428,33 @@ class Extractor:
         m = re.match(r"^(\w+)\s*\[\s*(\w+)\s*\]\s*=\s*(.*)$", st, flags=re.S)
         if m and isinstance(self.env.get(m.group(1)), list):
             try:
-                self.env[m.group(1)][int(self.ev(m.group(2)))] = float(self.ev(m.group(3)))
+                val = self.ev(m.group(3))
+                self.env[m.group(1)][int(self.ev(m.group(2)))] = val if isinstance(val, V) else float(val)
             except Exception:
                 self.env.pop(m.group(1), None)
                 self.skipped += 1
+            return
+        # vector arrays: Vec_t name[N] = {Vec_t(...), ...};  Vec_t name[N];
+        m = re.match(r"^(?:const\s+)?Vec_t\s+(\w+)\s*\[\s*(\w*)\s*\]\s*(?:=\s*\{(.*)\})?$", st, flags=re.S)
+        if m:
+            try:
+                if m.group(3) is not None:
+                    self.env[m.group(1)] = [self.ev(a) for a in split_top(m.group(3)) if a]
+                else:
+                    self.env[m.group(1)] = [V() for _ in range(int(self.ev(m.group(2))))]
+            except Exception:
+                self.skipped += 1
+            return
+        # a logical volume of a shape, and its placement at the identity (same answers)
+        m = re.match(r"^(?:vecgeom::)?LogicalVolume\s+(\w+)\s*\(\s*\"[^\"]*\"\s*,\s*&\s*(\w+)\s*\)$", st)
+        if m:
+            if m.group(2) in self.shapes:
+                self.lvs[m.group(1)] = m.group(2)
+            return
+        m = re.match(r"^(?:auto\s+)?(\w+)\s*=\s*(\w+)\s*\.\s*Place\s*\(\s*\)$", st)
+        if m:
+            if m.group(2) in self.lvs:
+                self.shapes[m.group(1)] = self.shapes[self.lvs[m.group(2)]]
             return
         # vector declarations
         m = re.match(r"^(?:const\s+)?(?:Vec_t|Vector3D<[^>]*>|vecgeom::Vector3D<[^>]*>)\s+(.*)$", st, flags=re.S)

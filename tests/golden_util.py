@@ -9,7 +9,7 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-FILES = ["Box", "Tube", "Cons", "Polycone", "Torus2", "Trd", "Polyhedra"]
+FILES = ["Box", "Tube", "Cons", "Polycone", "Torus2", "Trd", "Polyhedra", "Trap"]
 QUERY_ID = {"Inside": 0, "Contains": 1, "DistanceToIn": 2, "DistanceToOut": 3, "SafetyToIn": 4, "SafetyToOut": 5}
 APPROX_TOL = 1e-6   # kApproxEqualTolerance of test/unit_tests/ApproxEqual.h
 RANGE_DELTA = 1e-4  # DELTA of OutRange in test/unit_tests/TestCons.cpp
@@ -46,6 +46,14 @@ def add_shape(geo, spec):
         if len(a) == 4:  # Trd1 constructor (x1, x2, y, z)
             return geo.add_trd(a[0], a[1], a[2], a[2], a[3])
         return geo.add_trd(*a[:5])
+    if t == "trap":
+        if len(a) == 1:  # eight corners
+            return geo.add_trap_corners(a[0])
+        if len(a) == 4:  # Trd1-like (dx1, dx2, dy, dz)
+            return geo.add_trap(a[3], 0.0, 0.0, a[2], a[0], a[0], 0.0, a[2], a[1], a[1], 0.0)
+        if len(a) == 5:  # Trd2-like (dx1, dx2, dy1, dy2, dz)
+            return geo.add_trap(a[4], 0.0, 0.0, a[2], a[0], a[0], 0.0, a[3], a[1], a[1], 0.0)
+        return geo.add_trap(*a[:11])
     if t == "polyhedron":
         sphi, dphi, nsides, nz, z, rmin, rmax = a[:7]
         nz = int(nz)

@@ -85,6 +85,36 @@ def test_small_barrel_variants_match_oracle():
         compare_builders(W.build_barrel, seed=seed, nlayers=4, n0=20, n1=300)
 
 
+def test_trap_ring_tables_match_oracle():
+    info, nbvh = compare_builders(W.build_trap_ring)
+    assert info["n_pv"] == 1 + 48 + 1 and nbvh >= 1
+
+
+def test_trap_records_match_oracle_and_reference_extents():
+    """Trapezoid extents from the host records equal the oracle's, and the published ones of
+    test/unit_tests/TestTrap.cpp (TestVECGEOM393: Trap(60, 20 deg, 5 deg, 40, 30, 40, 10 deg,
+    16, 10, 14, 10 deg); trap2 from corners)."""
+    deg = np.arctan(1.0) / 45.0
+    par = (60.0, 20 * deg, 5 * deg, 40.0, 30.0, 40.0, 10 * deg, 16.0, 10.0, 14.0, 10 * deg)
+    corners = [(-10.0, -20.0, -40.0), (10.0, -20.0, -40.0), (-10.0, 20.0, -40.0), (10.0, 20.0, -40.0),
+               (-30.0, -40.0, 40.0), (30.0, -40.0, 40.0), (-30.0, 40.0, 40.0), (30.0, 40.0, 40.0)]
+    p, o = vg.Geometry(), OracleGeometry()
+    for geo in (p, o):
+        geo.add_trap(*par)
+        geo.add_trap_corners(corners)
+        geo.add_trap(*W.TRAP_WEDGE)
+        geo.add_trap_corners(0.5 * W.trap_corners(*W.TRAP_WEDGE))
+    for s in range(4):
+        assert np.array_equal(np.array(p.shape_extent(s)), np.array(o.shape_extent(s))), s
+    lo, hi = p.shape_extent(0)
+    assert np.allclose(lo, (-58.80819229, -41.90332577, -60.0), rtol=0, atol=1e-8)
+    assert np.allclose(hi, (38.57634475, 38.09667423, 60.0), rtol=0, atol=1e-8)
+    lo, hi = p.shape_extent(1)
+    assert np.allclose(lo, (-30.0, -40.0, -40.0)) and np.allclose(hi, (30.0, 40.0, 40.0))
+    with pytest.raises(vg.VGError):
+        p.add_trap(0.0, 0.0, 0.0, 1.0, 1.0, 1.0, 0.0, 1.0, 1.0, 1.0, 0.0)
+
+
 def test_builder_rejects_bad_ids():
     g = vg.Geometry()
     with pytest.raises(vg.VGError):

@@ -20,6 +20,7 @@ SHAPES = {
     "tube_phi": ("tube", (10.0, 20.0, 30.0, 0.3, 1.8)),
     "cone": ("cone", (5.0, 10.0, 8.0, 15.0, 25.0, 0.0, 2 * np.pi)),
     "trd": ("trd", (30.0, 10.0, 40.0, 15.0, 60.0)),
+    "trap": ("trap", (60.0, 0.1, 0.4, 40.0, 20.0, 30.0, 0.15, 50.0, 25.0, 35.0, 0.15)),
 }
 
 

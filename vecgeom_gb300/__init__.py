@@ -37,6 +37,7 @@ NAVSTATE_DTYPE = np.dtype([("nav_ind", "<u4"), ("last_exited", "<u4"), ("on_boun
 assert NAVSTATE_DTYPE.itemsize == 12
 
 SHAPE_BOX, SHAPE_TUBE, SHAPE_CONE, SHAPE_POLYCONE, SHAPE_POLYHEDRON, SHAPE_TORUS2, SHAPE_TRD, SHAPE_BOOLMINUS = range(1, 9)
+SHAPE_TRAPEZOID = 9
 
 
 class VGError(RuntimeError):
@@ -62,6 +63,8 @@ _SIGS = {
                                                 ctypes.c_int32, _c_dp, _c_dp, _c_dp]),
     "vg_geom_add_torus2": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 5),
     "vg_geom_add_trd": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 5),
+    "vg_geom_add_trap": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 11),
+    "vg_geom_add_trap_corners": (ctypes.c_int32, [_c_vp, _c_dp]),
     "vg_geom_add_boolean_subtraction": (ctypes.c_int32, [_c_vp, ctypes.c_int32, ctypes.c_int32]),
     "vg_geom_add_logical_volume": (ctypes.c_int32, [_c_vp, ctypes.c_int32]),
     "vg_geom_place": (ctypes.c_int32, [_c_vp, ctypes.c_int32, _c_dp, _c_dp]),
@@ -227,6 +230,18 @@ class Geometry:
 
     def add_trd(self, dx1, dx2, dy1, dy2, dz):
         return _check(_lib.vg_geom_add_trd(self._h, dx1, dx2, dy1, dy2, dz), "add_trd")
+
+    def add_trap(self, dz, theta, phi, dy1, dx1, dx2, alpha1, dy2, dx3, dx4, alpha2):
+        """UnplacedTrapezoid(dz, theta, phi, dy1, dx1, dx2, alpha1, dy2, dx3, dx4, alpha2), angles
+        in radians."""
+        return _check(_lib.vg_geom_add_trap(self._h, dz, theta, phi, dy1, dx1, dx2, alpha1, dy2, dx3, dx4, alpha2),
+                      "add_trap")
+
+    def add_trap_corners(self, corners):
+        """UnplacedTrapezoid(TrapCorners): eight (x, y, z) corners, (---) (+--) (-+-) (++-) (--+)
+        (+-+) (-++) (+++)."""
+        c = np.ascontiguousarray(np.asarray(corners, dtype=np.float64).reshape(24))
+        return _check(_lib.vg_geom_add_trap_corners(self._h, c.ctypes.data_as(_c_dp)), "add_trap_corners")
 
     def add_boolean_subtraction(self, left_pv, right_pv):
         return _check(_lib.vg_geom_add_boolean_subtraction(self._h, left_pv, right_pv), "add_boolean_subtraction")

@@ -301,6 +301,17 @@ int32_t vg_geom_add_trd(vg_geom *g, double dx1, double dx2, double dy1, double d
   const double p[5] = {dx1, dx2, dy1, dy2, dz};
   return add_shape(g, vg::kShapeTrd, p, 5);
 }
+int32_t vg_geom_add_trap(vg_geom *g, double dz, double theta, double phi, double dy1, double dx1, double dx2,
+                         double alpha1, double dy2, double dx3, double dx4, double alpha2)
+{
+  const double p[11] = {dz, theta, phi, dy1, dx1, dx2, alpha1, dy2, dx3, dx4, alpha2};
+  return add_shape(g, vg::kShapeTrap, p, 11);
+}
+int32_t vg_geom_add_trap_corners(vg_geom *g, const double *corners)
+{
+  if (!corners) return fail(VG_EINVAL, "null corner array");
+  return add_shape(g, vg::kShapeTrap, corners, 24);
+}
 int32_t vg_geom_add_boolean_subtraction(vg_geom *g, int32_t left_pv, int32_t right_pv)
 {
   const double p[2] = {(double)left_pv, (double)right_pv};

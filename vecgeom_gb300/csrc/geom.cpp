@@ -284,6 +284,78 @@ void make_trd(const double *p, HostShape &s)
   s.hi[0] = mx, s.hi[1] = my, s.hi[2] = t.dz;
 }
 
+// Trapezoid: side planes from the eight corners, either given (UnplacedTrapezoid.cpp:496-524,
+// dz from the last corner) or made from the 11 parameters (UnplacedTrapezoid.h:56-64: tan of
+// alpha1/alpha2; TrapezoidStruct.h CalculateCached: tan(theta) cos(phi), tan(theta) sin(phi);
+// UnplacedTrapezoid.cpp:447-466 FromParametersToCorners). Planes: UnplacedTrapezoid.cpp:630-679
+// (faces 0154 -Y, 2673 +Y, 0462 -X, 1375 +X), each by MakeAPlane (:569-620): n = (p3 - p1) x
+// (p4 - p2) times 1/|n|, d = -n . ((p1 + p2 + p3 + p4) 0.25). Extent: UnplacedTrapezoid.cpp:
+// 298-337 on the corners re-derived from the planes (:468-494 fromPlanesToCorners).
+bool make_trap(const double *p, int np, HostShape &s, std::string &err)
+{
+  double pt[8][3];
+  TrapRec t{};
+  if (np == 24) {
+    for (int k = 0; k < 8; ++k)
+      for (int j = 0; j < 3; ++j) pt[k][j] = p[3 * k + j];
+    t.dz = pt[7][2];
+  } else if (np == 11) {
+    const double dz = p[0], dy1 = p[3], dx1 = p[4], dx2 = p[5], dy2 = p[7], dx3 = p[8], dx4 = p[9];
+    const double ta1 = std::tan(p[6]), ta2 = std::tan(p[10]);
+    const double tcp = std::tan(p[1]) * std::cos(p[2]), tsp = std::tan(p[1]) * std::sin(p[2]);
+    const double a1 = ta1 * dy1, a2 = ta2 * dy2, xz = tcp * dz, yz = tsp * dz;
+    const double c[8][3] = {{-xz - a1 - dx1, -yz - dy1, -dz}, {-xz - a1 + dx1, -yz - dy1, -dz},
+                            {-xz + a1 - dx2, -yz + dy1, -dz}, {-xz + a1 + dx2, -yz + dy1, -dz},
+                            {+xz - a2 - dx3, +yz - dy2, +dz}, {+xz - a2 + dx3, +yz - dy2, +dz},
+                            {+xz + a2 - dx4, +yz + dy2, +dz}, {+xz + a2 + dx4, +yz + dy2, +dz}};
+    std::memcpy(pt, c, sizeof(pt));
+    t.dz = dz;
+  } else {
+    err = "a trapezoid takes 11 parameters or 8 corners (24 values)";
+    return false;
+  }
+  static const int face[4][4] = {{0, 1, 5, 4}, {2, 6, 7, 3}, {0, 4, 6, 2}, {1, 3, 7, 5}};
+  for (int i = 0; i < 4; ++i) {
+    const double *p1 = pt[face[i][0]], *p2 = pt[face[i][1]], *p3 = pt[face[i][2]], *p4 = pt[face[i][3]];
+    const double u[3] = {p3[0] - p1[0], p3[1] - p1[1], p3[2] - p1[2]};
+    const double v[3] = {p4[0] - p2[0], p4[1] - p2[1], p4[2] - p2[2]};
+    double n[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]};
+    const double inv = 1. / std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    for (double &x : n) x = x * inv;
+    double c[3];
+    for (int j = 0; j < 3; ++j) c[j] = 0.25 * (((p1[j] + p2[j]) + p3[j]) + p4[j]);
+    t.a[i] = n[0], t.b[i] = n[1], t.c[i] = n[2];
+    t.d[i] = -(n[0] * c[0] + n[1] * c[1] + n[2] * c[2]);
+  }
+  if (!(t.dz > 0.) || !std::isfinite(t.dz)) {
+    err = "trapezoid half length must be positive";
+    return false;
+  }
+  t.dz_plus  = t.dz + kHalfTolerance;
+  t.dz_minus = t.dz - kHalfTolerance;
+  s.type     = kShapeTrap;
+  pack(s, t);
+  const double z = t.dz;
+  double x[8], y[8];
+  for (int k = 0; k < 8; ++k) {
+    const int yp = (k >> 1) & 1, xp = 2 + (k & 1);
+    const double sz = (k < 4) ? -z : z;
+    y[k] = -(t.d[yp] + sz * t.c[yp]) / t.b[yp];
+    x[k] = ((t.b[xp] / t.b[yp]) * (t.d[yp] + sz * t.c[yp]) - (t.d[xp] + sz * t.c[xp])) / t.a[xp];
+  }
+  auto mx = [](const double *v) {
+    auto M = [](double a, double b) { return a > b ? a : b; };
+    return M(M(M(v[0], v[1]), M(v[2], v[3])), M(M(v[4], v[5]), M(v[6], v[7])));
+  };
+  auto mn = [](const double *v) {
+    auto M = [](double a, double b) { return a < b ? a : b; };
+    return M(M(M(v[0], v[1]), M(v[2], v[3])), M(M(v[4], v[5]), M(v[6], v[7])));
+  };
+  s.lo[0] = mn(x), s.lo[1] = mn(y), s.lo[2] = -z;
+  s.hi[0] = mx(x), s.hi[1] = mx(y), s.hi[2] = z;
+  return true;
+}
+
 // PolyconeStruct.h:124-239 Init: one ConeStruct(prevRmin, prevRmax, rMin, rMax, dz, phiStart,
 // phiTotal) per z interval longer than kTolerance, shifted to the interval's middle.
 bool make_polycone(const double *p, int np, HostShape &s, std::string &err)
@@ -640,6 +712,9 @@ int32_t Geometry::add_shape(int32_t type, const double *p, int np, std::string &
   case kShapeTrd:
     if (!need(5)) return -1;
     make_trd(p, s);
+    break;
+  case kShapeTrap:
+    if (!make_trap(p, np, s, err)) return -1;
     break;
   case kShapePolyhedron:
     if (!need(4) || !make_polyhedron(p, np, s, err)) {

@@ -90,5 +90,6 @@ bool make_polycone(const double *p, int np, HostShape &s, std::string &err);
 bool make_polyhedron(const double *p, int np, HostShape &s, std::string &err);
 void make_torus2(const double *p, HostShape &s);
 void make_trd(const double *p, HostShape &s);
+bool make_trap(const double *p, int np, HostShape &s, std::string &err);
 
 } // namespace vg

@@ -37,6 +37,7 @@ VG_OPS(BoxRec, box)
 VG_OPS(TubeRec, tube)
 VG_OPS(ConeRec, cone)
 VG_OPS(TrdRec, trd)
+VG_OPS(TrapRec, trap)
 VG_OPS(TorusRec, torus)
 #undef VG_OPS
 
@@ -252,6 +253,7 @@ cudaError_t launch_shape_query_fp64(int type, const double *rec, const Xform &xf
   case kShapeTube: return launch_typed<TubeRec>(rec, xf, apply_xf, lbd, q, a, s);
   case kShapeCone: return launch_typed<ConeRec>(rec, xf, apply_xf, lbd, q, a, s);
   case kShapeTrd: return launch_typed<TrdRec>(rec, xf, apply_xf, lbd, q, a, s);
+  case kShapeTrap: return launch_typed<TrapRec>(rec, xf, apply_xf, lbd, q, a, s);
   case kShapeTorus2: return launch_typed<TorusRec>(rec, xf, apply_xf, lbd, q, a, s);
   default: return cudaErrorNotSupported;
   }

@@ -161,6 +161,116 @@ __device__ __forceinline__ double trd_safety(const TrdRec &t, V3 p, bool inside)
 __device__ __forceinline__ double trd_safety_in(const TrdRec &t, V3 p) { return trd_safety(t, p, false); }
 __device__ __forceinline__ double trd_safety_out(const TrdRec &t, V3 p) { return trd_safety(t, p, true); }
 
+// ================================================================ Trap
+// Two z planes at +-dz and four side planes (PlaneShell<4>, VecGeom/base/PlaneShell.h),
+// evaluated in the reference's order: plane value a x + b y + c z + d summed left to right.
+__device__ __forceinline__ double trap_plane(const TrapRec &t, int i, V3 p)
+{
+  return t.a[i] * p.x + t.b[i] * p.y + t.c[i] * p.z + t.d[i];
+}
+__device__ __forceinline__ double trap_proj(const TrapRec &t, int i, V3 v)
+{
+  return t.a[i] * v.x + t.b[i] * v.y + t.c[i] * v.z;
+}
+// TrapezoidImplementation.h:65-106 + PlaneShell.h GenericKernelForContainsAndInside: outside
+// beyond dz + tol or a plane value above tol; inside within dz - tol and every plane value
+// below -tol (inside is assigned last)
+__device__ __forceinline__ int trap_inside(const TrapRec &t, V3 p)
+{
+  bool out = dlt(t.dz_plus, fabs(p.z));
+  bool in  = dabs_lt(p.z, t.dz_minus);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const double s = trap_plane(t, i, p);
+    out            = out || dgt(s, kHalfTolerance);
+    in             = in && dlt(s, -kHalfTolerance);
+  }
+  return in ? kInside : (out ? kOutside : kSurface);
+}
+__device__ __forceinline__ bool trap_contains(const TrapRec &t, V3 p)
+{
+  bool out = dlt(t.dz, fabs(p.z));
+#pragma unroll
+  for (int i = 0; i < 4; ++i) out = out || dgt(trap_plane(t, i, p), 0.);
+  return !out;
+}
+// TrapezoidImplementation.h:107-126 + PlaneShell.h DistanceToIn. The z slab gives [smin, smax];
+// each side plane the ray crosses inward raises smin, outward lowers smax; kInfLength as soon
+// as the ray provably misses. The reference tests every plane for the first kind of miss
+// before clipping; any miss returns kInfLength, so one pass in plane order gives the same
+// value. Exit distances -pdist / proj are divided only for the planes that use them.
+static __device__ __noinline__ double trap_dist_in(const TrapRec &t, V3 p, V3 d)
+{
+  const double sdz = flipsign(t.dz, d.z); // Sign(d.z) * dz
+  const double max = sdz - p.z;
+  if (dlt(flipsign(max, d.z), kHalfTolerance)) return kInfLength;
+  const double invdir = 1.0 / nonzero(d.z);
+  double smax         = max * invdir;
+  double smin         = -(sdz + p.z) * invdir;
+  bool pos[4], dirp[4];
+  double pd[4], pj[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    pd[i]   = trap_plane(t, i, p);
+    pj[i]   = trap_proj(t, i, d);
+    pos[i]  = dgt(pd[i], -kHalfTolerance);
+    dirp[i] = dgt(pj[i], 0.);
+    if ((dgt(pd[i], kHalfTolerance) && dge(pj[i], 0.)) || (pos[i] && dirp[i])) return kInfLength;
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const bool fromIn = !pos[i] && dirp[i], fromOut = pos[i] && !dirp[i];
+    if (fromIn || fromOut) {
+      const double v = -pd[i] / nonzero(pj[i]);
+      if (fromIn) {
+        if (dlt(v, smin)) return kInfLength;
+        if (dlt(v, smax)) smax = v;
+      } else {
+        if (dgt(v, smax)) return kInfLength;
+        if (dgt(v, smin)) smin = v;
+      }
+    }
+  }
+  return dle(smin, smax) ? smin : kInfLength;
+}
+// TrapezoidImplementation.h:151-167 + PlaneShell.h DistanceToOut: -1 beyond dz + tol;
+// otherwise the z exit, lowered by the plane pass (-1 when outside a plane, then any smaller
+// exit distance, planes in order).
+static __device__ __noinline__ double trap_dist_out(const TrapRec &t, V3 p, V3 d)
+{
+  if (dlt(t.dz_plus, fabs(p.z))) return -1.;
+  double distance = kInfLength;
+  if (dne(d.z, 0.)) distance = (flipsign(t.dz, d.z) - p.z) / nonzero(d.z);
+  double out = kInfLength;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const double pd = trap_plane(t, i, p);
+    const double pj = trap_proj(t, i, d);
+    if (dgt(pd, kHalfTolerance)) out = -1.;
+    if (dgt(pj, 0.)) {
+      const double v = -pd / nonzero(pj);
+      if (dlt(v, out)) out = v;
+    }
+  }
+  return dlt(out, distance) ? out : distance;
+}
+// TrapezoidImplementation.h:183-218 + PlaneShell.h SafetyToIn / SafetyToOut (N = 4): the
+// z-plane value, then the largest (smallest, negated) plane value taken in plane order
+__device__ __forceinline__ double trap_safety_in(const TrapRec &t, V3 p)
+{
+  double safety = fabs(p.z) - t.dz;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) safety = dmax(trap_plane(t, i, p), safety);
+  return safety;
+}
+__device__ __forceinline__ double trap_safety_out(const TrapRec &t, V3 p)
+{
+  double safety = t.dz - fabs(p.z);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) safety = dmin(-trap_plane(t, i, p), safety);
+  return safety;
+}
+
 // ================================================================ Polycone
 struct PolyconeView {
   const double *r;

@@ -23,6 +23,7 @@ enum ShapeType : int32_t {
   kShapeTorus2     = 6,
   kShapeTrd        = 7,
   kShapeBoolMinus  = 8,
+  kShapeTrap       = 9,
 };
 
 // VecGeom/base/Math.h:27-52 (double precision)
@@ -77,6 +78,14 @@ struct ConeRec {
 struct TrdRec {
   double dx1, dx2, dy1, dy2, dz;
   double x2minusx1, y2minusy1, halfx1plusx2, halfy1plusy2, calfx, calfy, fx, fy, tolx, toly, pad;
+};
+
+// VecGeom/volumes/TrapezoidStruct.h:20-63 in the VECGEOM_PLANESHELL build (PlaneShell<4>,
+// VecGeom/base/PlaneShell.h:25-31): half length in z, dz -+ kHalfTolerance, and the four side
+// planes a x + b y + c z + d (outward unit normals) in the order -Y, +Y, -X, +X.
+struct TrapRec {
+  double dz, dz_plus, dz_minus, pad;
+  double a[4], b[4], c[4], d[4];
 };
 
 // Polycone record: header, section boundaries, then one (shift, cone) block per section

@@ -213,6 +213,43 @@ def build_detector(geo, seed=0xDE7EC7, nlayers=20, total_modules=150000, wedges_
     return world
 
 
+def trap_corners(dz, theta, phi, dy1, dx1, dx2, alpha1, dy2, dx3, dx4, alpha2):
+    """The eight corners of UnplacedTrapezoid(dz, theta, phi, ...) (UnplacedTrapezoid.cpp:447-466),
+    shape (8, 3), in the order (---) (+--) (-+-) (++-) (--+) (+-+) (-++) (+++)."""
+    t1, t2 = math.tan(alpha1) * dy1, math.tan(alpha2) * dy2
+    xz, yz = math.tan(theta) * math.cos(phi) * dz, math.tan(theta) * math.sin(phi) * dz
+    c = []
+    for z, xc, yc, dy, a, dxm, dxp in ((-dz, -xz, -yz, dy1, t1, dx1, dx2), (dz, xz, yz, dy2, t2, dx3, dx4)):
+        c += [(xc - a - dxm, yc - dy, z), (xc - a + dxm, yc - dy, z), (xc + a - dxp, yc + dy, z),
+              (xc + a + dxp, yc + dy, z)]
+    return np.array(c)
+
+
+TRAP_WEDGE = (60.0, 0.1, 0.4, 40.0, 20.0, 30.0, 0.15, 50.0, 25.0, 35.0, 0.15)
+
+
+def build_trap_ring(geo, n_phi=16, radius=300.0, z_rings=(-120.0, 0.0, 120.0), close=True):
+    """Rings of general trapezoids (tilted by theta/phi, sheared by alpha) pointing radially,
+    each holding a half-size trapezoid made from its corners, in a 1.2 m box: a calorimeter-like
+    test geometry for the trapezoid kernels inside the navigator."""
+    world_lv = geo.add_logical_volume(geo.add_box(600.0, 600.0, 400.0))
+    wedge_lv = geo.add_logical_volume(geo.add_trap(*TRAP_WEDGE))
+    inner_lv = geo.add_logical_volume(geo.add_trap_corners(0.5 * trap_corners(*TRAP_WEDGE)))
+    geo.place_daughter(wedge_lv, inner_lv)
+    for z in z_rings:
+        for j in range(n_phi):
+            ph = TWO_PI * j / n_phi
+            c, s = math.cos(ph), math.sin(ph)
+            # local x -> tangential, local y -> global z, local z -> radial
+            rot = (-s, 0.0, c, c, 0.0, s, 0.0, 1.0, 0.0)
+            geo.place_daughter(world_lv, wedge_lv, (radius * c, radius * s, z), rot)
+    world = geo.place(world_lv)
+    geo.set_world(world)
+    if close:
+        geo.close()
+    return world
+
+
 def tracks_in_cylinder(n, seed, rmax=30.0, halfz=500.0):
     """Config 3 track starts: uniform in the cylinder r < rmax, |z| < halfz, isotropic."""
     g = rng(seed, 5)
