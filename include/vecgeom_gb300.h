@@ -117,6 +117,11 @@ int32_t vg_geom_add_trap(vg_geom *g, double dz, double theta, double phi, double
 /* UnplacedTrapezoid(TrapCorners) (VecGeom/volumes/UnplacedTrapezoid.h:84-86): corners[24] = eight
  * (x, y, z) in the order (---) (+--) (-+-) (++-) (--+) (+-+) (-++) (+++); dz is the last z. */
 int32_t vg_geom_add_trap_corners(vg_geom *g, const double *corners);
+/* A trapezoid from its half length and side planes exactly as an existing UnplacedTrapezoid
+ * holds them (TrapezoidStruct.h:20-63: fDz and GetPlane(i) for i = 0..3, the planes -Y, +Y,
+ * -X, +X): planes[16] = (a, b, c, d) of each plane in that order. Mirrors any trapezoid
+ * bit-exactly, whichever constructor made it. */
+int32_t vg_geom_add_trap_planes(vg_geom *g, double dz, const double *planes);
 /* UnplacedBooleanVolume<kSubtraction>(left, right): operands are placed volumes created
  * with vg_geom_place (VecGeom/volumes/BooleanStruct.h:19-33) */
 int32_t vg_geom_add_boolean_subtraction(vg_geom *g, int32_t left_pv, int32_t right_pv);

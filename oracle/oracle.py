@@ -109,6 +109,9 @@ class OracleGeometry:
     def add_trap(self, dz, theta, phi, dy1, dx1, dx2, alpha1, dy2, dx3, dx4, alpha2):
         return self._shape(9, [dz, theta, phi, dy1, dx1, dx2, alpha1, dy2, dx3, dx4, alpha2])
 
+    def add_trap_planes(self, dz, planes):
+        return self._shape(9, [dz] + list(np.asarray(planes, dtype=np.float64).reshape(16)))
+
     def add_trap_corners(self, corners):
         c = np.asarray(corners, dtype=np.float64).reshape(24)
         return self._shape(9, list(c))

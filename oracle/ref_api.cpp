@@ -40,7 +40,7 @@ void *oracle_geom_create() { return new Geometry(); }
 void oracle_geom_destroy(void *g) { delete static_cast<Geometry *>(g); }
 
 // type: 1 Box, 2 Tube, 3 Cone, 4 Polycone, 5 Polyhedron, 6 Torus2, 7 Trd, 8 BooleanSubtraction,
-// 9 Trapezoid (11 parameters, or 24 = eight corners x, y, z)
+// 9 Trapezoid (11 parameters, 24 = eight corners x, y, z, or 17 = dz and four planes a, b, c, d)
 int oracle_add_shape(void *gp, int type, const double *p, int np)
 {
   Geometry *g = static_cast<Geometry *>(gp);
@@ -69,6 +69,8 @@ int oracle_add_shape(void *gp, int type, const double *p, int np)
       s = new Trap(c);
     } else if (np == 11) {
       s = new Trap(p);
+    } else if (np == 17) {
+      s = new Trap(p[0], p + 1);
     } else {
       return -1;
     }

@@ -276,6 +276,11 @@ Trap::Trap(const Vec3 *corners)
   fDz = corners[7].z();
   MakePlanes(corners);
 }
+Trap::Trap(double dz, const double *planes) : fDz(dz)
+{
+  for (int i = 0; i < 4; ++i)
+    fA[i] = planes[4 * i], fB[i] = planes[4 * i + 1], fC[i] = planes[4 * i + 2], fD[i] = planes[4 * i + 3];
+}
 // UnplacedTrapezoid.cpp:630-679 MakePlanes: faces (0,1,5,4) -Y, (2,6,7,3) +Y, (0,4,6,2) -X,
 // (1,3,7,5) +X.
 void Trap::MakePlanes(const Vec3 *pt)

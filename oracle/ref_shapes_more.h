@@ -39,6 +39,8 @@ struct Trap : UnplacedShape {
   explicit Trap(const double *par);
   // UnplacedTrapezoid(TrapCorners): corners p0(---) p1(+--) p2(-+-) p3(++-) p4(--+) p5(+-+) p6(-++) p7(+++)
   explicit Trap(const Vec3 *corners);
+  // dz and the planes as an UnplacedTrapezoid holds them (TrapezoidStruct GetPlane(0..3))
+  Trap(double dz, const double *planes);
   void MakePlanes(const Vec3 *pt);
   void MakeAPlane(Vec3 const &p1, Vec3 const &p2, Vec3 const &p3, Vec3 const &p4, int i);
   double PlaneDist(int i, Vec3 const &p) const { return fA[i] * p.x() + fB[i] * p.y() + fC[i] * p.z() + fD[i]; }

@@ -2,6 +2,7 @@
 host geometry builder reproduces the oracle's daughter boxes, BVHs and NavIndex table
 bit-for-bit (no GPU needed: vg_geom_build flattens on the host only)."""
 import ctypes
+import math
 import os
 import re
 
@@ -113,6 +114,35 @@ def test_trap_records_match_oracle_and_reference_extents():
     assert np.allclose(lo, (-30.0, -40.0, -40.0)) and np.allclose(hi, (30.0, 40.0, 40.0))
     with pytest.raises(vg.VGError):
         p.add_trap(0.0, 0.0, 0.0, 1.0, 1.0, 1.0, 0.0, 1.0, 1.0, 1.0, 0.0)
+
+
+def planes_from_corners(c):
+    """The four side planes (a, b, c, d) of a trapezoid from its corners, in plain float
+    arithmetic in the order of UnplacedTrapezoid.cpp:569-620 (so bit-equal to the C++)."""
+    out = []
+    for f in ((0, 1, 5, 4), (2, 6, 7, 3), (0, 4, 6, 2), (1, 3, 7, 5)):
+        p1, p2, p3, p4 = (tuple(float(v) for v in c[k]) for k in f)
+        u = [p3[j] - p1[j] for j in range(3)]
+        v = [p4[j] - p2[j] for j in range(3)]
+        n = [u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]]
+        inv = 1.0 / math.sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2])
+        n = [x * inv for x in n]
+        ctr = [0.25 * (((p1[j] + p2[j]) + p3[j]) + p4[j]) for j in range(3)]
+        out += [n[0], n[1], n[2], -(n[0] * ctr[0] + n[1] * ctr[1] + n[2] * ctr[2])]
+    return out
+
+
+def test_trap_from_planes_equals_trap_from_corners():
+    """vg_geom_add_trap_planes (the exact mirror of an existing trapezoid) gives the same
+    record as the corner constructor when fed that constructor's planes."""
+    corners = W.trap_corners(*W.TRAP_WEDGE)
+    p, o = vg.Geometry(), OracleGeometry()
+    for geo in (p, o):
+        geo.add_trap_corners(corners)
+        geo.add_trap_planes(float(corners[7][2]), planes_from_corners(corners))
+    for geo in (p, o):
+        assert np.array_equal(np.array(geo.shape_extent(0)), np.array(geo.shape_extent(1)))
+    assert np.array_equal(np.array(p.shape_extent(1)), np.array(o.shape_extent(1)))
 
 
 def test_builder_rejects_bad_ids():

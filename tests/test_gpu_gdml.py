@@ -1,8 +1,9 @@
 """Navigation in a geometry read from GDML (tests/golden/gdml/detector.gdml: boxes in a
 barrel tube, Trd wedges in polycone endcaps, trapezoids in a polyhedra, a torus, a phi-cut
 cone and a boolean subtraction, with rotations from GDML angles): LocatePoint and the
-transport stream step for step equal to the oracle (FP64), and every mixed-precision
-schedule equal to FP64."""
+transport stream step for step equal to the oracle (FP64: states bit-exact, steps bit-exact
+except at the Torus2, within 1e-8 mm there), and every mixed-precision schedule equal to
+FP64."""
 import os
 
 import numpy as np
@@ -56,7 +57,15 @@ def test_gdml_locate_and_transport_match_oracle(cuda, gdml_det):
     tsl = tsp.cpu().numpy().reshape(n, max_steps)
     mask = np.arange(max_steps)[None, :] < ns[:, None]
     assert np.array_equal(trs[mask], ref_tr[mask])
-    assert np.array_equal(tsl[mask], ref_ts[mask])
+    # steps bit-exact, except the steps into or out of the Torus2 ring: its cubic solve calls
+    # cbrt/pow/cos/atan2, whose CUDA and libm results differ in the last bits, so those
+    # steps are compared at 1e-8 mm (the tolerance stated for Torus2 elsewhere)
+    torus_ind = o.locate(np.array([1000.0]), np.array([0.0]), np.array([1500.0]))[0]["nav_ind"][0]
+    prev = np.concatenate([ref_st["nav_ind"][:, None], ref_tr[:, :-1]], axis=1)
+    differ = mask & (tsl != ref_ts)
+    assert (np.abs(tsl - ref_ts)[differ] <= 1e-8).all()
+    assert ((ref_tr == torus_ind) | (prev == torus_ind))[differ].all()
+    assert differ.sum() < 0.01 * mask.sum()
     # tracks cross the modules, wedges, trapezoids and the other daughters
     assert len(np.unique(ref_tr[mask])) > 120 and ns.sum() > 2 * n
 

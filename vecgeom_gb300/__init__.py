@@ -65,6 +65,7 @@ _SIGS = {
     "vg_geom_add_trd": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 5),
     "vg_geom_add_trap": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 11),
     "vg_geom_add_trap_corners": (ctypes.c_int32, [_c_vp, _c_dp]),
+    "vg_geom_add_trap_planes": (ctypes.c_int32, [_c_vp, ctypes.c_double, _c_dp]),
     "vg_geom_add_boolean_subtraction": (ctypes.c_int32, [_c_vp, ctypes.c_int32, ctypes.c_int32]),
     "vg_geom_add_logical_volume": (ctypes.c_int32, [_c_vp, ctypes.c_int32]),
     "vg_geom_place": (ctypes.c_int32, [_c_vp, ctypes.c_int32, _c_dp, _c_dp]),
@@ -242,6 +243,12 @@ class Geometry:
         (+-+) (-++) (+++)."""
         c = np.ascontiguousarray(np.asarray(corners, dtype=np.float64).reshape(24))
         return _check(_lib.vg_geom_add_trap_corners(self._h, c.ctypes.data_as(_c_dp)), "add_trap_corners")
+
+    def add_trap_planes(self, dz, planes):
+        """A trapezoid from dz and its four side planes (a, b, c, d), ordered -Y, +Y, -X, +X, as
+        an existing UnplacedTrapezoid holds them."""
+        c = np.ascontiguousarray(np.asarray(planes, dtype=np.float64).reshape(16))
+        return _check(_lib.vg_geom_add_trap_planes(self._h, dz, c.ctypes.data_as(_c_dp)), "add_trap_planes")
 
     def add_boolean_subtraction(self, left_pv, right_pv):
         return _check(_lib.vg_geom_add_boolean_subtraction(self._h, left_pv, right_pv), "add_boolean_subtraction")

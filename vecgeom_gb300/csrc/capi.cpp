@@ -312,6 +312,14 @@ int32_t vg_geom_add_trap_corners(vg_geom *g, const double *corners)
   if (!corners) return fail(VG_EINVAL, "null corner array");
   return add_shape(g, vg::kShapeTrap, corners, 24);
 }
+int32_t vg_geom_add_trap_planes(vg_geom *g, double dz, const double *planes)
+{
+  if (!planes) return fail(VG_EINVAL, "null plane array");
+  double p[17];
+  p[0] = dz;
+  for (int i = 0; i < 16; ++i) p[1 + i] = planes[i];
+  return add_shape(g, vg::kShapeTrap, p, 17);
+}
 int32_t vg_geom_add_boolean_subtraction(vg_geom *g, int32_t left_pv, int32_t right_pv)
 {
   const double p[2] = {(double)left_pv, (double)right_pv};

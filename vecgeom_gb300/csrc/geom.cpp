@@ -284,7 +284,8 @@ void make_trd(const double *p, HostShape &s)
   s.hi[0] = mx, s.hi[1] = my, s.hi[2] = t.dz;
 }
 
-// Trapezoid: side planes from the eight corners, either given (UnplacedTrapezoid.cpp:496-524,
+// Trapezoid: the side planes as given (dz + TrapezoidStruct::GetPlane(0..3)), or from the eight
+// corners, either given (UnplacedTrapezoid.cpp:496-524,
 // dz from the last corner) or made from the 11 parameters (UnplacedTrapezoid.h:56-64: tan of
 // alpha1/alpha2; TrapezoidStruct.h CalculateCached: tan(theta) cos(phi), tan(theta) sin(phi);
 // UnplacedTrapezoid.cpp:447-466 FromParametersToCorners). Planes: UnplacedTrapezoid.cpp:630-679
@@ -295,7 +296,10 @@ bool make_trap(const double *p, int np, HostShape &s, std::string &err)
 {
   double pt[8][3];
   TrapRec t{};
-  if (np == 24) {
+  if (np == 17) { // dz, then (a, b, c, d) of the planes -Y, +Y, -X, +X as the reference holds them
+    t.dz = p[0];
+    for (int i = 0; i < 4; ++i) t.a[i] = p[1 + 4 * i], t.b[i] = p[2 + 4 * i], t.c[i] = p[3 + 4 * i], t.d[i] = p[4 + 4 * i];
+  } else if (np == 24) {
     for (int k = 0; k < 8; ++k)
       for (int j = 0; j < 3; ++j) pt[k][j] = p[3 * k + j];
     t.dz = pt[7][2];
@@ -311,11 +315,11 @@ bool make_trap(const double *p, int np, HostShape &s, std::string &err)
     std::memcpy(pt, c, sizeof(pt));
     t.dz = dz;
   } else {
-    err = "a trapezoid takes 11 parameters or 8 corners (24 values)";
+    err = "a trapezoid takes 11 parameters, 8 corners (24 values) or dz and 4 planes (17 values)";
     return false;
   }
   static const int face[4][4] = {{0, 1, 5, 4}, {2, 6, 7, 3}, {0, 4, 6, 2}, {1, 3, 7, 5}};
-  for (int i = 0; i < 4; ++i) {
+  for (int i = 0; i < 4 && np != 17; ++i) {
     const double *p1 = pt[face[i][0]], *p2 = pt[face[i][1]], *p3 = pt[face[i][2]], *p4 = pt[face[i][3]];
     const double u[3] = {p3[0] - p1[0], p3[1] - p1[1], p3[2] - p1[2]};
     const double v[3] = {p4[0] - p2[0], p4[1] - p2[1], p4[2] - p2[2]};
