@@ -186,6 +186,18 @@ int vg_placed_safety_to_out(const vg_geom *g, int32_t pv, const double *x, const
 int vg_nav_locate_point(const vg_geom *g, const double *x, const double *y, const double *z, size_t n,
                         vg_navstate *out, void *stream);
 
+/* vg_nav_approach_next_daughter replaces BVH::ApproachNextDaughter(localpoint, localdir, step,
+ * last) (VecGeom/base/BVH.h:147-159, source/BVH.cpp:394-449), called per track in the frame of
+ * its state's volume (the state's global-to-local matrix) with `last` = the state's last-exited
+ * volume, as the step passes it to CheckDaughterIntersections. step[] is in/out: on entry the
+ * largest distance of interest, on exit lowered to the distance at which the ray first reaches
+ * a daughter's bounding box (VUnplacedVolume::ApproachSolid, UnplacedVolume.h:272-280).
+ * status[] (nullable) gets VG_TRACK_OK, or an error code with step[] left unchanged.
+ * Device pointers; plain FP64, results identical to the reference's FP64 arithmetic. */
+int vg_nav_approach_next_daughter(const vg_geom *g, const double *x, const double *y, const double *z,
+                                  const double *dx, const double *dy, const double *dz, const vg_navstate *in,
+                                  double *step, int32_t *status, size_t n, void *stream);
+
 /* vg_nav_compute_step_and_next_volume replaces the SoA navigator call
  * VNavigator::ComputeStepsAndPropagatedStates(SOA3D const&, SOA3D const&, Precision const*
  * step_limits, NavigationState const* const* in, NavigationState** out, Precision* steps)

@@ -43,6 +43,7 @@ def load():
             "oracle_nav_locate": (ctypes.c_double, [_vp, ctypes.c_size_t, _vp, _vp, _vp, _vp, ctypes.c_int]),
             "oracle_nav_step": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 11 + [ctypes.c_int]),
             "oracle_nav_step_safety": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 11 + [ctypes.c_int]),
+            "oracle_nav_approach": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 8 + [ctypes.c_int]),
             "oracle_nav_transport": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 7 +
                                      [ctypes.c_int, _vp, _vp, _vp, _vp, ctypes.c_int]),
         }
@@ -199,6 +200,14 @@ class OracleGeometry:
         t = _lib.oracle_nav_step_safety(self._h, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(step_limit),
                                         _p(states), _p(out), _p(step), _p(saf), nthreads)
         return out, step, saf, t
+
+    def approach_next_daughter(self, x, y, z, dx, dy, dz, states, step, nthreads=1):
+        """BVH::ApproachNextDaughter per track; returns the new step array (a copy of `step`
+        lowered to the first daughter bounding box the ray reaches)."""
+        out = np.array(step, dtype=np.float64, copy=True)
+        _lib.oracle_nav_approach(self._h, len(x), _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(states), _p(out),
+                                 nthreads)
+        return out
 
     def transport(self, x, y, z, dx, dy, dz, states, max_steps, trace=False, nthreads=1):
         n = len(x)

@@ -201,6 +201,19 @@ double oracle_nav_step(void *gp, size_t n, const double *x, const double *y, con
   });
 }
 
+// BVH::ApproachNextDaughter per track in the state's volume; step[] in/out (states outside
+// the world keep their step).
+double oracle_nav_approach(void *gp, size_t n, const double *x, const double *y, const double *z, const double *dx,
+                           const double *dy, const double *dz, const NavState *in, double *step, int nthreads)
+{
+  Geometry *g = static_cast<Geometry *>(gp);
+  return ParallelFor(n, nthreads, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i)
+      if (in[i].navInd != 0)
+        step[i] = g->ApproachNextDaughter(Vec3(x[i], y[i], z[i]), Vec3(dx[i], dy[i], dz[i]), step[i], in[i]);
+  });
+}
+
 // Step + safety (VNavigator.h:1014-1064).
 double oracle_nav_step_safety(void *gp, size_t n, const double *x, const double *y, const double *z,
                               const double *dx, const double *dy, const double *dz, const double *step_limit,

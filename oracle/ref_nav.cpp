@@ -170,6 +170,79 @@ void BVH::CheckDaughterIntersections(Vec3 const &lp, Vec3 const &ld, double &ste
   } while (ptr > stack);
 }
 
+// VUnplacedVolume::ApproachSolid (VecGeom/volumes/UnplacedVolume.h:272-280): the slab
+// distance of BoxImplementation::IntersectCachedKernel2 (BoxImplementation.h:324-368) to the
+// shape's bounding box (its Extent) within [0, kInfLength], kInfLength on a miss.
+static double ApproachSolid(UnplacedShape const &s, Vec3 const &p, Vec3 const &inv)
+{
+  Vec3 c[2];
+  s.Extent(c[0], c[1]);
+  const int sx = inv.x() < 0, sy = inv.y() < 0, sz = inv.z() < 0;
+  double tmin        = (c[sx].x() - p.x()) * inv.x();
+  const double tymax = (c[1 - sy].y() - p.y()) * inv.y();
+  if (tmin > tymax) return kInfLength;
+  double tmax        = (c[1 - sx].x() - p.x()) * inv.x();
+  const double tymin = (c[sy].y() - p.y()) * inv.y();
+  if (tymin > tmax) return kInfLength;
+  tmin               = Max(tmin, tymin);
+  tmax               = Min(tmax, tymax);
+  const double tzmin = (c[sz].z() - p.z()) * inv.z();
+  const double tzmax = (c[1 - sz].z() - p.z()) * inv.z();
+  if (tmin > tzmax || tzmin > tmax) return kInfLength;
+  tmin = Max(tmin, tzmin);
+  tmax = Min(tmax, tzmax);
+  if (!(tmin <= kInfLength + kTolerance && tmax > 0. - kTolerance)) return kInfLength;
+  return tmin;
+}
+
+// source/BVH.cpp:394-449 ApproachNextDaughter: CheckDaughterIntersections' traversal with the
+// daughters' bounding-box approach distance in place of their DistanceToIn
+void BVH::ApproachNextDaughter(Vec3 const &lp, Vec3 const &ld, double &step, PlacedVolume const *last) const
+{
+  unsigned stack[kMaxDepth] = {0}, *ptr = &stack[1];
+  const Vec3 invdir(1.0 / NonZero(ld[0]), 1.0 / NonZero(ld[1]), 1.0 / NonZero(ld[2]));
+  do {
+    const unsigned id = *--ptr;
+    if (nchild[id] >= 0) {
+      for (int i = 0; i < nchild[id]; ++i) {
+        const int prim = primId[offset[id] + i];
+        if (aabbs[prim].IntersectInvDir(lp, invdir, step)) {
+          PlacedVolume const *vol = lv.daughters[prim];
+          const Vec3 p            = vol->T.Transform(lp);
+          const Vec3 d            = vol->T.TransformDirection(ld);
+          const Vec3 inv(1.0 / NonZero(d[0]), 1.0 / NonZero(d[1]), 1.0 / NonZero(d[2]));
+          const double dist = ApproachSolid(*vol->Shape(), p, inv);
+          if (dist < step && !(dist <= 0.0 && vol == last)) step = dist;
+        }
+      }
+    } else {
+      const unsigned childL = 2 * id + 1;
+      const unsigned childR = 2 * id + 2;
+      double tminL = kInfLength, tmaxL = -kInfLength, tminR = kInfLength, tmaxR = -kInfLength;
+      nodes[childL].ComputeIntersectionInvDir(lp, invdir, tminL, tmaxL);
+      nodes[childR].ComputeIntersectionInvDir(lp, invdir, tminR, tmaxR);
+      const bool traverseL = tminL <= tmaxL && tmaxL >= 0.0 && tminL < step;
+      const bool traverseR = tminR <= tmaxR && tmaxR >= 0.0 && tminR < step;
+      if (tminR < tminL) {
+        if (traverseR) *ptr++ = childR;
+        if (traverseL) *ptr++ = childL;
+      } else {
+        if (traverseL) *ptr++ = childL;
+        if (traverseR) *ptr++ = childR;
+      }
+    }
+  } while (ptr > stack);
+}
+
+double Geometry::ApproachNextDaughter(Vec3 const &gp, Vec3 const &gd, double step, NavState const &in) const
+{
+  Transformation3D m;
+  TopMatrix(in.navInd, m);
+  LogicalVolume const *lv = Top(in.navInd)->lv;
+  if (!lv->daughters.empty()) lv->bvh->ApproachNextDaughter(m.Transform(gp), m.TransformDirection(gd), step, Top(in.lastExited));
+  return step;
+}
+
 // BVH.h:236-285 LevelLocate (excluded-volume variant)
 bool BVH::LevelLocate(PlacedVolume const *excl, Vec3 const &lp, PlacedVolume const *&pvol, Vec3 &dlp) const
 {

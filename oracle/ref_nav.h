@@ -95,6 +95,7 @@ struct BVH {
                                   PlacedVolume const *&hit, int *nvisited = nullptr) const;
   bool LevelLocate(PlacedVolume const *excl, Vec3 const &lp, PlacedVolume const *&pvol, Vec3 &dlp) const;
   double ComputeSafety(Vec3 const &lp, double safety) const;
+  void ApproachNextDaughter(Vec3 const &lp, Vec3 const &ld, double &step, PlacedVolume const *last) const;
 };
 
 // NavStateIndex (VecGeom/navigation/NavStateIndex.h:39-41)
@@ -145,6 +146,9 @@ struct Geometry {
   // VNavigatorHelper<BVHNavigator<false>>::ComputeStepAndPropagatedState (VNavigator.h:436-492)
   double ComputeStepAndPropagatedState(Vec3 const &gp, Vec3 const &gd, double stepLimit, NavState const &in,
                                        NavState &out, int *nvisited = nullptr) const;
+  // BVH::ApproachNextDaughter (source/BVH.cpp:394-449) in the frame of the state's volume,
+  // `last` = the state's last-exited volume, as CheckDaughterIntersections gets it
+  double ApproachNextDaughter(Vec3 const &gp, Vec3 const &gd, double step, NavState const &in) const;
   // VNavigatorHelper::ComputeStepAndSafetyAndPropagatedState (VNavigator.h:1014-1064)
   double ComputeStepAndSafetyAndPropagatedState(Vec3 const &gp, Vec3 const &gd, double stepLimit,
                                                 NavState const &in, NavState &out, double &safety) const;

@@ -92,6 +92,7 @@ _SIGS = {
     "vg_placed_safety_to_out": (ctypes.c_int, [_c_vp, ctypes.c_int32, _c_vp, _c_vp, _c_vp, ctypes.c_size_t,
                                                _c_vp, ctypes.c_uint32, _c_vp]),
     "vg_nav_locate_point": (ctypes.c_int, [_c_vp, _c_vp, _c_vp, _c_vp, ctypes.c_size_t, _c_vp, _c_vp]),
+    "vg_nav_approach_next_daughter": (ctypes.c_int, [_c_vp] + [_c_vp] * 9 + [ctypes.c_size_t, _c_vp]),
     "vg_nav_compute_step_and_next_volume": (ctypes.c_int, [_c_vp] + [_c_vp] * 11 +
                                             [ctypes.c_size_t, ctypes.c_uint32, _c_vp]),
     "vg_nav_compute_step_and_next_volume_host": (ctypes.c_int, [_c_vp] + [_c_vp] * 11 +
@@ -346,6 +347,14 @@ class Geometry:
         """GlobalLocator::LocateGlobalPoint(world, p, state, true); out_states: uint8 tensor (n*12)."""
         _check(_lib.vg_nav_locate_point(self._h, _ptr(x), _ptr(y), _ptr(z), x.numel(), _ptr(out_states),
                                         _stream()), "vg_nav_locate_point")
+
+    def approach_next_daughter(self, x, y, z, dx, dy, dz, in_states, step, status=None):
+        """BVH::ApproachNextDaughter per track in its state's volume (CUDA tensors): `step`
+        (float64, in/out) is lowered to the distance at which the ray first reaches a
+        daughter's bounding box."""
+        _check(_lib.vg_nav_approach_next_daughter(self._h, _ptr(x), _ptr(y), _ptr(z), _ptr(dx), _ptr(dy), _ptr(dz),
+                                                  _ptr(in_states), _ptr(step), _ptr(status), x.numel(), _stream()),
+               "vg_nav_approach_next_daughter")
 
     def compute_step_and_next_volume(self, x, y, z, dx, dy, dz, in_states, out_states, step, step_limit=None,
                                      status=None, flags=PREC_FP64, workspace=None, nodes_visited=None):

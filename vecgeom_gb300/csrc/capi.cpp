@@ -468,6 +468,19 @@ int vg_nav_locate_point(const vg_geom *g, const double *x, const double *y, cons
   return e == cudaSuccess ? VG_OK : cuda_fail(e, "locate launch");
 }
 
+int vg_nav_approach_next_daughter(const vg_geom *g, const double *x, const double *y, const double *z,
+                                  const double *dx, const double *dy, const double *dz, const vg_navstate *in,
+                                  double *step, int32_t *status, size_t n, void *stream)
+{
+  if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
+  if (n > 0 && (!x || !y || !z || !dx || !dy || !dz || !in || !step))
+    return fail(VG_EINVAL, "null input/output array");
+  const cudaError_t e =
+      vg::launch_approach_fp64(g->geo.dev, x, y, z, dx, dy, dz, reinterpret_cast<const vg::NavState *>(in), step,
+                               status, n, (cudaStream_t)stream);
+  return e == cudaSuccess ? VG_OK : cuda_fail(e, "approach launch");
+}
+
 int vg_nav_compute_step_and_next_volume(const vg_geom *g, const double *x, const double *y, const double *z,
                                         const double *dx, const double *dy, const double *dz,
                                         const double *step_limit, const vg_navstate *in, vg_navstate *out,

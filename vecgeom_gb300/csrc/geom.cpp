@@ -1149,6 +1149,11 @@ int Geometry::upload(std::string &err)
   const size_t o_bn0 = a.add(bvh_node0), o_bp0 = a.add(bvh_prim0), o_nnc = a.add(node_nchild);
   const size_t o_nof = a.add(node_offset), o_nbx = a.add(node_box), o_pid = a.add(prim_id);
   const size_t o_lvdp = a.add(lv_depth), o_ds3 = a.add(dau_slot3);
+  // VUnplacedVolume::fBBox (UnplacedVolume.h:45, ComputeBBox = Extent) of every shape
+  std::vector<double> shape_bbox(6 * shapes.size());
+  for (size_t i = 0; i < shapes.size(); ++i)
+    for (int k = 0; k < 3; ++k) shape_bbox[6 * i + k] = shapes[i].lo[k], shape_bbox[6 * i + 3 + k] = shapes[i].hi[k];
+  const size_t o_sbb = a.add(shape_bbox);
   // FP32 bounding descriptors of the shapes (mixed-precision navigator): kind 0 = box
   // (lo, hi; flag 1 when the box is the shape itself), kind 1 = cylindrical shell (rmin,
   // rmax, zlo, zhi; flag 1 when the shell is the shape itself). Radii and z are rounded
@@ -1265,6 +1270,7 @@ int Geometry::upload(std::string &err)
   dev.nav_words   = (uint32_t)nav_words;
   dev.lv_depth    = reinterpret_cast<const int32_t *>(P(o_lvdp));
   dev.dau_slot3   = reinterpret_cast<const int32_t *>(P(o_ds3));
+  dev.shape_bbox  = reinterpret_cast<const double *>(P(o_sbb));
   dev.shape_lbd   = reinterpret_cast<const float *>(P(o_lbd));
   dev.leaf_rec    = reinterpret_cast<const LeafRec *>(P(o_lrec));
   dev.pv_rec      = reinterpret_cast<const PvRec *>(P(o_pvr));

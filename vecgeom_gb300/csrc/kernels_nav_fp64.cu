@@ -52,7 +52,44 @@ __global__ void __launch_bounds__(256) k_step(const DevGeom g, const StepArgs a)
   }
 }
 
+// BVH::ApproachNextDaughter (source/BVH.cpp:394-449) in the frame of each track's volume,
+// with the state's last-exited volume as `last`, as the step passes it to
+// CheckDaughterIntersections.
+__global__ void __launch_bounds__(256) k_approach(const DevGeom g, const double *__restrict__ x,
+                                                  const double *__restrict__ y, const double *__restrict__ z,
+                                                  const double *__restrict__ dx, const double *__restrict__ dy,
+                                                  const double *__restrict__ dz, const NavState *__restrict__ in,
+                                                  double *__restrict__ step, int32_t *__restrict__ status, size_t n)
+{
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const NavState s = in[i];
+    int st           = kTrackErrState;
+    if (s.navInd != 0) {
+      const Xform m = f64::nav_top_matrix(g, s.navInd);
+      const int lv  = g.pv_lv[f64::nav_top(g, s.navInd)];
+      double t      = step[i];
+      st            = kTrackOk;
+      if (g.lv_nd[lv] > 0)
+        st = f64::bvh_approach_next_daughter(g, lv, f64::to_local(m, V3{__ldg(x + i), __ldg(y + i), __ldg(z + i)}),
+                                             f64::rotate(m, V3{__ldg(dx + i), __ldg(dy + i), __ldg(dz + i)}), t,
+                                             f64::nav_top(g, s.lastExited));
+      if (st == kTrackOk) step[i] = t;
+    }
+    if (status) status[i] = st;
+  }
+}
+
 } // namespace
+
+cudaError_t launch_approach_fp64(const DevGeom &g, const double *x, const double *y, const double *z,
+                                 const double *dx, const double *dy, const double *dz, const NavState *in,
+                                 double *step, int32_t *status, size_t n, cudaStream_t s)
+{
+  if (n == 0) return cudaSuccess;
+  k_approach<<<grid_for(n, 256), 256, 0, s>>>(g, x, y, z, dx, dy, dz, in, step, status, n);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_locate_fp64(const DevGeom &g, const double *x, const double *y, const double *z, size_t n,
                                NavState *out, cudaStream_t s)

@@ -42,6 +42,10 @@ cudaError_t launch_shape_query_dyn_fp64(const DevGeom &g, int shape, const Xform
 cudaError_t launch_locate_fp64(const DevGeom &g, const double *x, const double *y, const double *z, size_t n,
                                NavState *out, cudaStream_t s);
 cudaError_t launch_step_fp64(const DevGeom &g, const StepArgs &a, cudaStream_t s);
+// BVH::ApproachNextDaughter per track in its state's volume; step in/out, status nullable
+cudaError_t launch_approach_fp64(const DevGeom &g, const double *x, const double *y, const double *z,
+                                 const double *dx, const double *dy, const double *dz, const NavState *in,
+                                 double *step, int32_t *status, size_t n, cudaStream_t s);
 cudaError_t launch_step_mixed(const DevGeom &g, const StepArgs &a, cudaStream_t s);
 cudaError_t launch_step_mixed_queue(const DevGeom &g, const StepArgs &a, unsigned long long *counter,
                                     int blocks_per_sm, cudaStream_t s);

@@ -144,6 +144,81 @@ __device__ __forceinline__ int bvh_check_daughters(const DevGeom &g, int lv, V3 
   return kTrackOk;
 }
 
+// VUnplacedVolume::ApproachSolid (UnplacedVolume.h:272-280): BoxImplementation::
+// IntersectCachedKernel2 (BoxImplementation.h:324-368) on the shape's bounding box `bb`
+// (lo xyz, hi xyz) with t0 = 0, t1 = kInfLength; kInfLength on a miss.
+__device__ __forceinline__ double approach_solid(const double *bb, V3 p, V3 inv)
+{
+  const int sx = dlt(inv.x, 0.) ? 3 : 0, sy = dlt(inv.y, 0.) ? 3 : 0, sz = dlt(inv.z, 0.) ? 3 : 0;
+  double tmin        = (__ldg(bb + sx) - p.x) * inv.x;
+  const double tymax = (__ldg(bb + 4 - sy) - p.y) * inv.y;
+  if (dgt(tmin, tymax)) return kInfLength;
+  double tmax        = (__ldg(bb + 3 - sx) - p.x) * inv.x;
+  const double tymin = (__ldg(bb + 1 + sy) - p.y) * inv.y;
+  if (dgt(tymin, tmax)) return kInfLength;
+  tmin               = dmax(tmin, tymin);
+  tmax               = dmin(tmax, tymax);
+  const double tzmin = (__ldg(bb + 2 + sz) - p.z) * inv.z;
+  const double tzmax = (__ldg(bb + 5 - sz) - p.z) * inv.z;
+  if (dgt(tmin, tzmax) || dgt(tzmin, tmax)) return kInfLength;
+  tmin = dmax(tmin, tzmin);
+  tmax = dmin(tmax, tzmax);
+  if (!(dle(tmin, kInfLength + kTolerance) && dgt(tmax, 0. - kTolerance))) return kInfLength;
+  return tmin;
+}
+
+// BVH::ApproachNextDaughter (source/BVH.cpp:394-449): the traversal of
+// CheckDaughterIntersections with each candidate's bounding-box approach distance (in its own
+// frame) in place of its DistanceToIn; lowers `step` to the first box the ray reaches.
+__device__ __forceinline__ int bvh_approach_next_daughter(const DevGeom &g, int lv, V3 lp, V3 ld, double &step,
+                                                          int last_pv)
+{
+  const int b = g.lv_bvh[lv];
+  if (b < 0) return kTrackOk;
+  const int node0 = g.bvh_node0[b];
+  const int dbase = g.lv_dstart[lv];
+  const V3 inv{1.0 / nonzero(ld.x), 1.0 / nonzero(ld.y), 1.0 / nonzero(ld.z)};
+  unsigned stack[32];
+  int sp   = 1;
+  stack[0] = 0;
+  do {
+    const unsigned id = stack[--sp];
+    const int nc      = __ldg(&g.node_nchild[node0 + id]);
+    if (nc >= 0) {
+      const int off = __ldg(&g.node_offset[node0 + id]);
+      for (int i = 0; i < nc; ++i) {
+        const int prim = __ldg(&g.prim_id[off + i]);
+        double tmin, tmax;
+        aabb_slab(g.prim_box + 6 * (size_t)(dbase + prim), lp, inv, tmin, tmax);
+        if (dle(tmin, tmax) && dge(tmax, 0.0) && dlt(tmin, step)) {
+          const int vol  = __ldg(&g.daughters[dbase + prim]);
+          const Xform &m = g.pv_xf[vol];
+          const V3 d     = rotate(m, ld);
+          const V3 dinv{1.0 / nonzero(d.x), 1.0 / nonzero(d.y), 1.0 / nonzero(d.z)};
+          const double dist = approach_solid(g.shape_bbox + 6 * (size_t)pv_shape(g, vol), to_local(m, lp), dinv);
+          if (dlt(dist, step) && !(dle(dist, 0.0) && vol == last_pv)) step = dist;
+        }
+      }
+    } else {
+      const unsigned cl = 2 * id + 1, cr = 2 * id + 2;
+      double tminL, tmaxL, tminR, tmaxR;
+      aabb_slab(g.node_box + 6 * (size_t)(node0 + cl), lp, inv, tminL, tmaxL);
+      aabb_slab(g.node_box + 6 * (size_t)(node0 + cr), lp, inv, tminR, tmaxR);
+      const bool tl = dle(tminL, tmaxL) && dge(tmaxL, 0.0) && dlt(tminL, step);
+      const bool tr = dle(tminR, tmaxR) && dge(tmaxR, 0.0) && dlt(tminR, step);
+      if (sp + 2 > 32) return kTrackErrStack;
+      if (dlt(tminR, tminL)) {
+        if (tr) stack[sp++] = cr;
+        if (tl) stack[sp++] = cl;
+      } else {
+        if (tl) stack[sp++] = cl;
+        if (tr) stack[sp++] = cr;
+      }
+    }
+  } while (sp > 0);
+  return kTrackOk;
+}
+
 // BVH::LevelLocate, excluded-volume variant (BVH.h:236-285)
 __device__ __forceinline__ bool bvh_level_locate(const DevGeom &g, int lv, int excl_pv, V3 lp, int &pv, V3 &dlp,
                                                  int &status)

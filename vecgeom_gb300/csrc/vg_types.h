@@ -211,6 +211,7 @@ struct DevGeom {
   uint32_t nav_words;
   const int32_t *lv_depth;    // BVH depth per LV (-1: no BVH)
   const int32_t *dau_slot3;   // depth-3 subtree (0..7) of each daughter slot's leaf, or -1
+  const double *shape_bbox;   // 6 doubles per shape: its bounding box (Extent: lo xyz, hi xyz)
   int32_t world_pv;
   int32_t max_depth;
   int32_t n_pv;
