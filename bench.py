@@ -581,13 +581,22 @@ def main():
     for _ in range(2):
         geo.compute_step_and_next_volume_host(*hp, hst, hout, hstep, flags=head)
     barrier()
-    ke = max(3, args.steps // 4)
+    # each host-entry call returns with its results in host memory; the calls are timed one
+    # by one (the spread shows host and link noise of a shared machine) and the value is the
+    # whole run: all calls' steps over the total time
+    ke = max(5, args.steps // 2)
+    calls = []
     t0 = time.perf_counter()
     for _ in range(ke):
+        c0 = time.perf_counter()
         geo.compute_step_and_next_volume_host(*hp, hst, hout, hstep, flags=head)
+        calls.append(time.perf_counter() - c0)
     torch.cuda.synchronize()
     barrier()
     e2e_s = (time.perf_counter() - t0) / ke
+    calls.sort()
+    e2e_calls = {"calls": ke, "min": round(1e3 * calls[0], 3), "median": round(1e3 * calls[ke // 2], 3),
+                 "max": round(1e3 * calls[-1], 3)}
 
     peaks = {}
     try:
@@ -627,7 +636,7 @@ def main():
         "transport_stream": stream,
         "shape_queries": shapes,
         "e2e": {"value": ws * n / e2e_s, "unit": "nav steps/s", "h2d_bytes_per_step": n * (48 + 12),
-                "d2h_bytes_per_step": n * (12 + 8)},
+                "d2h_bytes_per_step": n * (12 + 8), "ms_per_call": e2e_calls},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": STEP_TRAFFIC_PER_STEP * n if head & 4 else None,
                      "traffic_note": "DRAM read + write of one step-kernel launch, ncu on 2^20 steps scaled to %d "
