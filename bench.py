@@ -356,18 +356,21 @@ def shape_rows(args, torch, dev, hbm_peak):
     return rows
 
 
-def cpu_time_steps(args, host_inputs, host_states, nthreads, reps=3):
-    """Oracle port timing on the host cores over the given sample."""
+def cpu_time_steps(args, host_inputs, host_states, nthreads, reps=5):
+    """Oracle port timing over the given sample: the median of `reps` repetitions after one
+    warm-up, on `nthreads` host threads and on one thread; returns (all-thread steps/s,
+    single-thread steps/s)."""
     from oracle.oracle import OracleGeometry
     o = OracleGeometry()
     builder(args.workload)(o)
     st = np.frombuffer(host_states.tobytes(), dtype=[("nav_ind", "<u4"), ("last_exited", "<u4"),
                                                     ("on_boundary", "u1"), ("pad", "u1", 3)]).copy()
-    best = None
-    for _ in range(reps):
-        _, _, _, t = o.step(*host_inputs, st, nthreads=nthreads)
-        best = t if best is None else min(best, t)
-    return len(host_inputs[0]) / best
+    rates = []
+    for threads in (nthreads, 1):
+        o.step(*host_inputs, st, nthreads=threads)
+        ts = sorted(o.step(*host_inputs, st, nthreads=threads)[3] for _ in range(reps))
+        rates.append(len(host_inputs[0]) / ts[reps // 2])
+    return rates[0], rates[1]
 
 
 def oracle_sample_steps(o, m, seed, nthreads, max_steps=400):
@@ -657,9 +660,10 @@ def main():
         hin = [a[:m].cpu().numpy() for a in t]
         hs = st[: m * 12].cpu().numpy()
         nthreads = os.cpu_count() or 1
-        cv = cpu_time_steps(args, hin, hs, nthreads)
+        cv, cv1 = cpu_time_steps(args, hin, hs, nthreads)
         line["cpu_baseline"] = {"value": cv, "unit": "nav steps/s", "cores": nthreads, "kind": "port",
-                                "sample": "%d of the %d step inputs, best of 3" % (m, n)}
+                                "single_thread_value": cv1,
+                                "sample": "%d of the %d step inputs, median of 5 after a warm-up" % (m, n)}
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
