@@ -179,6 +179,27 @@ int vg_placed_safety_to_in(const vg_geom *g, int32_t pv, const double *x, const 
 int vg_placed_safety_to_out(const vg_geom *g, int32_t pv, const double *x, const double *y, const double *z, size_t n,
                             double *out, uint32_t flags, void *stream);
 
+/* ---------------------------------------------------------------- unplaced SoA queries
+ * The same six queries on a shape by id, with points and directions in the shape's own frame
+ * (no transformation applied), for the VUnplacedVolume interface
+ * (VecGeom/volumes/UnplacedVolume.h): Contains (:89), Inside (:96), DistanceToIn (:192),
+ * DistanceToOut(SOA3D, SOA3D, step_max*, out*) (:144), SafetyToIn (:223),
+ * SafetyToOut(SOA3D, out*) (:179). Arguments and results as for the placed queries. */
+int vg_shape_inside(const vg_geom *g, int32_t shape, const double *x, const double *y, const double *z, size_t n,
+                    int32_t *out, uint32_t flags, void *stream);
+int vg_shape_contains(const vg_geom *g, int32_t shape, const double *x, const double *y, const double *z, size_t n,
+                      uint8_t *out, uint32_t flags, void *stream);
+int vg_shape_distance_to_in(const vg_geom *g, int32_t shape, const double *x, const double *y, const double *z,
+                            const double *dx, const double *dy, const double *dz, const double *step_max, size_t n,
+                            double *out, uint32_t flags, void *stream);
+int vg_shape_distance_to_out(const vg_geom *g, int32_t shape, const double *x, const double *y, const double *z,
+                             const double *dx, const double *dy, const double *dz, const double *step_max, size_t n,
+                             double *out, uint32_t flags, void *stream);
+int vg_shape_safety_to_in(const vg_geom *g, int32_t shape, const double *x, const double *y, const double *z,
+                          size_t n, double *out, uint32_t flags, void *stream);
+int vg_shape_safety_to_out(const vg_geom *g, int32_t shape, const double *x, const double *y, const double *z,
+                           size_t n, double *out, uint32_t flags, void *stream);
+
 /* ---------------------------------------------------------------- navigation
  * vg_nav_locate_point replaces GlobalLocator::LocateGlobalPoint(world, p, state, true)
  * (VecGeom/navigation/GlobalLocator.h:35-82) with BVHLevelLocator on every logical volume

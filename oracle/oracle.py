@@ -43,6 +43,8 @@ def load():
             "oracle_nav_locate": (ctypes.c_double, [_vp, ctypes.c_size_t, _vp, _vp, _vp, _vp, ctypes.c_int]),
             "oracle_nav_step": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 11 + [ctypes.c_int]),
             "oracle_nav_step_safety": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 11 + [ctypes.c_int]),
+            "oracle_shape_query": (ctypes.c_double, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_size_t] + [_vp] * 6 +
+                                   [ctypes.c_double, _vp, _vp, ctypes.c_int]),
             "oracle_nav_approach": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 8 + [ctypes.c_int]),
             "oracle_nav_transport": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 7 +
                                      [ctypes.c_int, _vp, _vp, _vp, _vp, ctypes.c_int]),
@@ -152,6 +154,16 @@ class OracleGeometry:
         t = _lib.oracle_placed_query(self._h, pv, q, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), step_max,
                                      _p(outd), _p(outi), nthreads)
         return (outi if q in (0, 1) else outd), t
+
+    def shape_query(self, shape, q, x, y, z, dx=None, dy=None, dz=None, step_max=np.finfo(np.float64).max,
+                    nthreads=1):
+        """The query q (as in query()) on an unplaced shape, points in its own frame."""
+        n = len(x)
+        outd = np.empty(n, np.float64)
+        outi = np.empty(n, np.int32)
+        _lib.oracle_shape_query(self._h, shape, q, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), step_max,
+                                _p(outd), _p(outi), nthreads)
+        return outi if q in (0, 1) else outd
 
     def nav_table(self):
         n = _lib.oracle_nav_table_words(self._h)

@@ -130,6 +130,28 @@ double oracle_placed_query(void *gp, int pv, int q, size_t n, const double *x, c
   });
 }
 
+// The same queries on an unplaced shape, points in its own frame (VUnplacedVolume).
+double oracle_shape_query(void *gp, int shape, int q, size_t n, const double *x, const double *y, const double *z,
+                          const double *dx, const double *dy, const double *dz, double step_max, double *outd,
+                          int *outi, int nthreads)
+{
+  Geometry *g            = static_cast<Geometry *>(gp);
+  UnplacedShape const *s = g->shapes.at(shape).get();
+  return ParallelFor(n, nthreads, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i) {
+      const Vec3 p(x[i], y[i], z[i]);
+      switch (q) {
+      case 0: outi[i] = s->Inside(p); break;
+      case 1: outi[i] = s->Contains(p) ? 1 : 0; break;
+      case 2: outd[i] = s->DistanceToIn(p, Vec3(dx[i], dy[i], dz[i]), step_max); break;
+      case 3: outd[i] = s->DistanceToOut(p, Vec3(dx[i], dy[i], dz[i]), step_max); break;
+      case 4: outd[i] = s->SafetyToIn(p); break;
+      case 5: outd[i] = s->SafetyToOut(p); break;
+      }
+    }
+  });
+}
+
 size_t oracle_nav_table_words(void *g) { return static_cast<Geometry *>(g)->tableWords; }
 void oracle_nav_table(void *gp, uint32_t *out)
 {

@@ -128,6 +128,9 @@ _SIGS = {
                                                [ctypes.c_size_t, ctypes.c_uint32, _c_vp, ctypes.c_size_t,
                                                 _c_vp]),
 }
+# the unplaced (shape-frame) queries take the same arguments, with a shape id for the placed id
+for _q in ("inside", "contains", "distance_to_in", "distance_to_out", "safety_to_in", "safety_to_out"):
+    _SIGS["vg_shape_" + _q] = _SIGS["vg_placed_" + _q]
 
 
 def load_library(path=None):
@@ -341,6 +344,19 @@ class Geometry:
     def safety_to_out(self, pv, x, y, z, out, flags=PREC_FP64):
         _check(_lib.vg_placed_safety_to_out(self._h, pv, _ptr(x), _ptr(y), _ptr(z), x.numel(), _ptr(out), flags,
                                             _stream()), "vg_placed_safety_to_out")
+
+    # ---------------------------------------------------------------- unplaced queries (shape frame)
+    def shape_query(self, q, shape, x, y, z, out, dx=None, dy=None, dz=None, flags=PREC_FP64):
+        """One of the six queries on shape `shape` with points (and directions) in its own
+        frame: q = "inside", "contains", "distance_to_in", "distance_to_out", "safety_to_in"
+        or "safety_to_out" (VUnplacedVolume)."""
+        fn = getattr(_lib, "vg_shape_" + q)
+        if q.startswith("distance"):
+            _check(fn(self._h, shape, _ptr(x), _ptr(y), _ptr(z), _ptr(dx), _ptr(dy), _ptr(dz), None, x.numel(),
+                      _ptr(out), flags, _stream()), "vg_shape_" + q)
+        else:
+            _check(fn(self._h, shape, _ptr(x), _ptr(y), _ptr(z), x.numel(), _ptr(out), flags, _stream()),
+                   "vg_shape_" + q)
 
     # ---------------------------------------------------------------- navigation (CUDA tensors)
     def locate_point(self, x, y, z, out_states):

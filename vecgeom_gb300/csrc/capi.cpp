@@ -216,6 +216,29 @@ int32_t add_shape(vg_geom *g, int type, const double *p, int np)
 
 enum Query { kQInside = 0, kQContains = 1, kQDistIn = 2, kQDistOut = 3, kQSafIn = 4, kQSafOut = 5 };
 
+// One SoA query of shape `shape`; the points go through `xf` first when apply_xf is set
+// (placed volumes), or are in the shape's own frame (unplaced queries).
+int shape_query(const vg_geom *g, int32_t shape, const vg::Xform &xf, int apply_xf, int q, const double *x,
+                const double *y, const double *z, const double *dx, const double *dy, const double *dz, size_t n,
+                void *out, uint32_t flags, void *stream)
+{
+  vg::Geometry const &geo = g->geo;
+  if (flags > VG_PREC_MIXED) return fail(VG_EINVAL, "invalid precision flags");
+  if (n > 0 && (!x || !y || !z || !out || ((q == kQDistIn || q == kQDistOut) && (!dx || !dy || !dz))))
+    return fail(VG_EINVAL, "null input/output array");
+  const int32_t type = geo.shapes[shape].type;
+  vg::QueryArgs a{x, y, z, dx, dy, dz, n, out};
+  const bool composite = type == vg::kShapePolycone || type == vg::kShapePolyhedron || type == vg::kShapeBoolMinus;
+  const bool mixed      = (flags & VG_PREC_MIXED) != 0;
+  const float *lbd      = mixed ? geo.shape_lbd_host.data() + 8 * (size_t)shape : nullptr;
+  const cudaError_t e   = composite ? vg::launch_shape_query_dyn_fp64(geo.dev, shape, xf, apply_xf, q, a,
+                                                                    (cudaStream_t)stream, mixed)
+                                  : vg::launch_shape_query_fp64(type, geo.shape_rec(shape), xf, apply_xf, q, a,
+                                                                (cudaStream_t)stream, lbd);
+  if (e == cudaErrorNotSupported) return fail(VG_EINVAL, "shape type not supported by this query path");
+  return e == cudaSuccess ? VG_OK : cuda_fail(e, "shape query launch");
+}
+
 int placed_query(const vg_geom *g, int32_t pv, int q, const double *x, const double *y, const double *z,
                  const double *dx, const double *dy, const double *dz, size_t n, void *out, uint32_t flags,
                  void *stream)
@@ -223,21 +246,17 @@ int placed_query(const vg_geom *g, int32_t pv, int q, const double *x, const dou
   if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
   vg::Geometry const &geo = g->geo;
   if (pv < 0 || pv >= (int32_t)geo.pvs.size()) return fail(VG_EINVAL, "invalid placed-volume id");
-  if (flags > VG_PREC_MIXED) return fail(VG_EINVAL, "invalid precision flags");
-  if (n > 0 && (!x || !y || !z || !out || ((q == kQDistIn || q == kQDistOut) && (!dx || !dy || !dz))))
-    return fail(VG_EINVAL, "null input/output array");
-  const int32_t shape = geo.lvs[geo.pvs[pv].lv].shape;
-  const int32_t type  = geo.shapes[shape].type;
-  vg::QueryArgs a{x, y, z, dx, dy, dz, n, out};
-  const bool composite = type == vg::kShapePolycone || type == vg::kShapePolyhedron || type == vg::kShapeBoolMinus;
-  const bool mixed      = (flags & VG_PREC_MIXED) != 0;
-  const float *lbd      = mixed ? geo.shape_lbd_host.data() + 8 * (size_t)shape : nullptr;
-  const cudaError_t e   = composite ? vg::launch_shape_query_dyn_fp64(geo.dev, shape, geo.pvs[pv].xf.m, q, a,
-                                                                    (cudaStream_t)stream, mixed)
-                                  : vg::launch_shape_query_fp64(type, geo.shape_rec(shape), geo.pvs[pv].xf.m, 1, q,
-                                                                a, (cudaStream_t)stream, lbd);
-  if (e == cudaErrorNotSupported) return fail(VG_EINVAL, "shape type not supported by this query path");
-  return e == cudaSuccess ? VG_OK : cuda_fail(e, "shape query launch");
+  return shape_query(g, geo.lvs[geo.pvs[pv].lv].shape, geo.pvs[pv].xf.m, 1, q, x, y, z, dx, dy, dz, n, out, flags,
+                     stream);
+}
+
+int unplaced_query(const vg_geom *g, int32_t shape, int q, const double *x, const double *y, const double *z,
+                   const double *dx, const double *dy, const double *dz, size_t n, void *out, uint32_t flags,
+                   void *stream)
+{
+  if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
+  if (shape < 0 || shape >= (int32_t)g->geo.shapes.size()) return fail(VG_EINVAL, "invalid shape id");
+  return shape_query(g, shape, vg::Xform{}, 0, q, x, y, z, dx, dy, dz, n, out, flags, stream);
 }
 } // namespace
 
@@ -455,6 +474,41 @@ int vg_placed_safety_to_out(const vg_geom *g, int32_t pv, const double *x, const
                             double *out, uint32_t flags, void *stream)
 {
   return placed_query(g, pv, kQSafOut, x, y, z, nullptr, nullptr, nullptr, n, out, flags, stream);
+}
+
+int vg_shape_inside(const vg_geom *g, int32_t shape, const double *x, const double *y, const double *z, size_t n,
+                    int32_t *out, uint32_t flags, void *stream)
+{
+  return unplaced_query(g, shape, kQInside, x, y, z, nullptr, nullptr, nullptr, n, out, flags, stream);
+}
+int vg_shape_contains(const vg_geom *g, int32_t shape, const double *x, const double *y, const double *z, size_t n,
+                      uint8_t *out, uint32_t flags, void *stream)
+{
+  return unplaced_query(g, shape, kQContains, x, y, z, nullptr, nullptr, nullptr, n, out, flags, stream);
+}
+int vg_shape_distance_to_in(const vg_geom *g, int32_t shape, const double *x, const double *y, const double *z,
+                            const double *dx, const double *dy, const double *dz, const double *step_max, size_t n,
+                            double *out, uint32_t flags, void *stream)
+{
+  (void)step_max;
+  return unplaced_query(g, shape, kQDistIn, x, y, z, dx, dy, dz, n, out, flags, stream);
+}
+int vg_shape_distance_to_out(const vg_geom *g, int32_t shape, const double *x, const double *y, const double *z,
+                             const double *dx, const double *dy, const double *dz, const double *step_max, size_t n,
+                             double *out, uint32_t flags, void *stream)
+{
+  (void)step_max;
+  return unplaced_query(g, shape, kQDistOut, x, y, z, dx, dy, dz, n, out, flags, stream);
+}
+int vg_shape_safety_to_in(const vg_geom *g, int32_t shape, const double *x, const double *y, const double *z,
+                          size_t n, double *out, uint32_t flags, void *stream)
+{
+  return unplaced_query(g, shape, kQSafIn, x, y, z, nullptr, nullptr, nullptr, n, out, flags, stream);
+}
+int vg_shape_safety_to_out(const vg_geom *g, int32_t shape, const double *x, const double *y, const double *z,
+                           size_t n, double *out, uint32_t flags, void *stream)
+{
+  return unplaced_query(g, shape, kQSafOut, x, y, z, nullptr, nullptr, nullptr, n, out, flags, stream);
 }
 
 int vg_nav_locate_point(const vg_geom *g, const double *x, const double *y, const double *z, size_t n,

@@ -213,7 +213,8 @@ cudaError_t launch_typed(const double *recp, const Xform &xf, int apply_xf, cons
 // the geometry arena and the query goes through the run-time dispatch.
 template <int Q, bool M>
 __global__ void __launch_bounds__(256) k_shape_query_dyn(const DevGeom g, const int shape, const Xform xf,
-                                                         const double *__restrict__ x, const double *__restrict__ y,
+                                                         const int apply_xf, const double *__restrict__ x,
+                                                         const double *__restrict__ y,
                                                          const double *__restrict__ z, const double *__restrict__ dx,
                                                          const double *__restrict__ dy, const double *__restrict__ dz,
                                                          size_t n, void *__restrict__ out)
@@ -222,7 +223,7 @@ __global__ void __launch_bounds__(256) k_shape_query_dyn(const DevGeom g, const 
   const size_t stride     = (size_t)gridDim.x * blockDim.x;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     V3 p{__ldg(x + i), __ldg(y + i), __ldg(z + i)};
-    const bool framed = (Q == 0 || Q == 1 || Q == 2 || Q == 4);
+    const bool framed = apply_xf && (Q == 0 || Q == 1 || Q == 2 || Q == 4);
     if (framed) p = f64::to_local(xf, p);
     if (Q == 0 || Q == 1) {
       const int c = M ? mixed::lb_classify(lb, p) : 0;
@@ -259,14 +260,16 @@ cudaError_t launch_shape_query_fp64(int type, const double *rec, const Xform &xf
   }
 }
 
-cudaError_t launch_shape_query_dyn_fp64(const DevGeom &g, int shape, const Xform &xf, int q, const QueryArgs &a,
-                                        cudaStream_t s, bool mixed)
+cudaError_t launch_shape_query_dyn_fp64(const DevGeom &g, int shape, const Xform &xf, int apply_xf, int q,
+                                        const QueryArgs &a, cudaStream_t s, bool mixed)
 {
   if (a.n == 0) return cudaSuccess;
   const unsigned grid = grid_for(a.n, 256);
-#define VG_DYN(Q)                                                                                                  \
-  (mixed ? k_shape_query_dyn<Q, true><<<grid, 256, 0, s>>>(g, shape, xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out) \
-         : k_shape_query_dyn<Q, false><<<grid, 256, 0, s>>>(g, shape, xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n, a.out))
+#define VG_DYN(Q)                                                                                                   \
+  (mixed ? k_shape_query_dyn<Q, true><<<grid, 256, 0, s>>>(g, shape, xf, apply_xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, \
+                                                           a.n, a.out)                                             \
+         : k_shape_query_dyn<Q, false><<<grid, 256, 0, s>>>(g, shape, xf, apply_xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, \
+                                                            a.n, a.out))
   switch (q) {
   case 0: mixed = false, VG_DYN(0); break; // FP64 is the faster classification (see launch_typed_q)
   case 1: mixed = false, VG_DYN(1); break;
