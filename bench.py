@@ -513,7 +513,7 @@ def main():
     tuning = None
     if args.tune and head & (vg.NAV_SORT | vg.NAV_QUEUE):
         from vecgeom_gb300.tune import autotune
-        cands = [(head, b, q) for b in (0, 7, 5) for q in ((1, 2, 3) if head & vg.NAV_QUEUE else (1,))]
+        cands = [(head, b, q) for b in (0, 7, 5) for q in ((1, 2, 3, 4) if head & vg.NAV_QUEUE else (1,))]
         tuning = autotune(geo, t, st, candidates=cands, cache=None)
     ms_fp64 = timed(vg.PREC_FP64)
     out64, step64 = out.clone(), step.clone()

@@ -305,8 +305,9 @@ int vg_nav_sort_key_params(const vg_geom *g, float lo[3], float scale[3], int32_
  * logical-volume id; fewer bits mean fewer radix passes and coarser cells), and
  * `queue_blocks_per_sm`, the configuration of the VG_NAV_QUEUE kernel (1: blocks of 256
  * threads, one per SM, full register budget; 2: two per SM, half the registers, twice the
- * resident warps; 3: blocks of 128 threads, three per SM, 168 registers; 0 = 1). Set before
- * sorted calls are in flight. */
+ * resident warps; 3: blocks of 128 threads, three per SM, 168 registers; 4: blocks of 128
+ * threads, five per SM, 20 resident warps at 102 registers; 0 = 1). Set before sorted calls
+ * are in flight. */
 int vg_nav_set_tuning(vg_geom *g, int32_t cell_bits, int32_t queue_blocks_per_sm);
 
 /* ---------------------------------------------------------------- learned proposal

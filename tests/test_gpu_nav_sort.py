@@ -97,6 +97,43 @@ def test_scheduling_variants_identical(cuda, geo, prec):
             assert np.array_equal(a, b), f
 
 
+def test_tuning_configurations_identical(cuda, geo):
+    """Every work-queue configuration (256 x 1, 256 x 2, 128 x 3, 128 x 5 threads x blocks per
+    SM) and sort-key resolution gives the plain FP64 results, in the step and in the transport
+    stream; out-of-range settings are rejected."""
+    import vecgeom_gb300 as vg
+    name, g, pts, dev, st = geo
+    n = dev[0].numel()
+
+    def run(flags):
+        out = cuda.empty(n * 12, dtype=cuda.uint8, device="cuda:0")
+        step = cuda.empty(n, dtype=cuda.float64, device="cuda:0")
+        g.compute_step_and_next_volume(*dev, st, out, step, flags=flags)
+        return out.cpu().numpy(), step.cpu().numpy()
+
+    base = run(vg.PREC_FP64)
+    m = 4096
+    sub = [d[:m].clone() for d in dev]
+    sst = st[: m * 12].clone()
+    ref_t = g.transport(*[d.clone() for d in sub], sst.clone(), max_steps=50, flags=vg.PREC_FP64)
+    try:
+        for qb in (1, 2, 3, 4):
+            for bits in (0, 5):
+                g.set_tuning(bits, qb)
+                got = run(vg.PREC_MIXED | vg.NAV_SORT | vg.NAV_QUEUE)
+                assert np.array_equal(got[0], base[0]) and np.array_equal(got[1], base[1]), (qb, bits)
+            tst = sst.clone()
+            got_t = g.transport(*[d.clone() for d in sub], tst, max_steps=50,
+                                flags=vg.PREC_MIXED | vg.NAV_SORT | vg.NAV_QUEUE)
+            assert cuda.equal(got_t[0], ref_t[0]), qb
+        with pytest.raises(vg.VGError):
+            g.set_tuning(0, 5)
+        with pytest.raises(vg.VGError):
+            g.set_tuning(11, 1)
+    finally:
+        g.set_tuning(0, 0)
+
+
 def test_host_entry_sorted_queue(cuda, geo):
     import vecgeom_gb300 as vg
     name, g, pts, dev, st = geo

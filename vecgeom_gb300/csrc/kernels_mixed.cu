@@ -255,6 +255,7 @@ cudaError_t launch_step_mixed_queue(const DevGeom &g, const StepArgs &a, unsigne
                                     int blocks_per_sm, cudaStream_t s)
 {
   if (a.n == 0) return cudaSuccess;
+  if (blocks_per_sm == 4) return launch_queue<128, 5>(g, a, counter, s);
   if (blocks_per_sm == 3) return launch_queue<128, 3>(g, a, counter, s);
   return blocks_per_sm == 2 ? launch_queue<256, 2>(g, a, counter, s) : launch_queue<256, 1>(g, a, counter, s);
 }
@@ -274,6 +275,7 @@ cudaError_t launch_transport_iter(const DevGeom &g, const TransportArgs &a, bool
 {
   if (a.n == 0) return cudaSuccess;
   if (!mixed) return launch_transport<false, 256, 1>(g, a, counter, s);
+  if (blocks_per_sm == 4) return launch_transport<true, 128, 5>(g, a, counter, s);
   if (blocks_per_sm == 3) return launch_transport<true, 128, 3>(g, a, counter, s);
   return blocks_per_sm == 2 ? launch_transport<true, 256, 2>(g, a, counter, s)
                             : launch_transport<true, 256, 1>(g, a, counter, s);
