@@ -126,6 +126,14 @@ int32_t vg_geom_add_trap_planes(vg_geom *g, double dz, const double *planes);
  * with vg_geom_place (VecGeom/volumes/BooleanStruct.h:19-33) */
 int32_t vg_geom_add_boolean_subtraction(vg_geom *g, int32_t left_pv, int32_t right_pv);
 
+/* Save / load a geometry description: the builder calls made on `g` (shapes, logical
+ * volumes, placements, world), in order, to a binary file; loading replays them on a new,
+ * empty handle, which gives the same ids, records and tables as the original (the caller
+ * then closes it). No reference counterpart: it replaces the rebuild of a closed VecGeom
+ * geometry (GeoManager::CloseGeometry, source/GeoManager.cpp:192) when the mirror is reused. */
+int vg_geom_save(const vg_geom *g, const char *path);
+int vg_geom_load(vg_geom *g, const char *path);
+
 /* LogicalVolume(shape); returns the logical-volume id. */
 int32_t vg_geom_add_logical_volume(vg_geom *g, int32_t shape_id);
 /* LogicalVolume::Place(transformation): a placed volume with no mother (world, boolean

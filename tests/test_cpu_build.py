@@ -176,3 +176,41 @@ def test_binding_arity_matches_header():
     for name, (res, args) in vg._SIGS.items():
         assert name in ar, name
         assert len(args) == ar[name], (name, len(args), ar[name])
+
+
+def test_geometry_save_and_load_replay(tmp_path):
+    """vg_geom_save / vg_geom_load: a detector-like geometry (GDML: every supported solid,
+    a boolean, rotations) and the barrel, saved and loaded into a new handle, give the same
+    NavIndex table, BVHs and shape extents; a missing or foreign file fails."""
+    from vecgeom_gb300 import gdml
+    det = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "gdml", "detector.gdml")
+    for build in (lambda g: gdml.load(det, g, close=False), lambda g: W.build_barrel(g, nlayers=4, close=False)):
+        a = vg.Geometry()
+        build(a)
+        path = str(tmp_path / "geom.vgg")
+        a.save(path)
+        b = vg.Geometry.load(path)
+        assert b.pv_lv == a.pv_lv
+        a.build()
+        b.build()
+        ia = a.info()
+        assert ia == b.info() and ia["n_pv"] > 100
+        assert np.array_equal(a.nav_table(), b.nav_table())
+        for lv in range(ia["n_lv"]):  # the logical volumes with daughters have a BVH
+            try:
+                pa = a.bvh(lv)
+            except vg.VGError:
+                with pytest.raises(vg.VGError):
+                    b.bvh(lv)
+                continue
+            pb = b.bvh(lv)
+            for k in ("prim", "offset", "nchild", "nodes", "boxes"):
+                assert np.array_equal(pa[k], pb[k]), (lv, k)
+        for s in range(ia["n_shapes"]):
+            assert np.array_equal(np.array(a.shape_extent(s)), np.array(b.shape_extent(s)))
+    with pytest.raises(vg.VGError):
+        vg.Geometry.load(str(tmp_path / "missing.vgg"))
+    bad = tmp_path / "bad.vgg"
+    bad.write_bytes(b"not a geometry file at all")
+    with pytest.raises(vg.VGError):
+        vg.Geometry.load(str(bad))

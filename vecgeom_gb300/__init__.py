@@ -66,6 +66,8 @@ _SIGS = {
     "vg_geom_add_trap": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 11),
     "vg_geom_add_trap_corners": (ctypes.c_int32, [_c_vp, _c_dp]),
     "vg_geom_add_trap_planes": (ctypes.c_int32, [_c_vp, ctypes.c_double, _c_dp]),
+    "vg_geom_save": (ctypes.c_int, [_c_vp, ctypes.c_char_p]),
+    "vg_geom_load": (ctypes.c_int, [_c_vp, ctypes.c_char_p]),
     "vg_geom_add_boolean_subtraction": (ctypes.c_int32, [_c_vp, ctypes.c_int32, ctypes.c_int32]),
     "vg_geom_add_logical_volume": (ctypes.c_int32, [_c_vp, ctypes.c_int32]),
     "vg_geom_place": (ctypes.c_int32, [_c_vp, ctypes.c_int32, _c_dp, _c_dp]),
@@ -256,6 +258,29 @@ class Geometry:
 
     def add_boolean_subtraction(self, left_pv, right_pv):
         return _check(_lib.vg_geom_add_boolean_subtraction(self._h, left_pv, right_pv), "add_boolean_subtraction")
+
+    def save(self, path):
+        """Write the builder calls made so far (shapes, volumes, placements, world) to `path`."""
+        _check(_lib.vg_geom_save(self._h, os.fsencode(path)), "vg_geom_save")
+
+    @classmethod
+    def load(cls, path):
+        """A new, open geometry replaying the builder calls saved in `path` (close it to use it)."""
+        g = cls()
+        _check(_lib.vg_geom_load(g._h, os.fsencode(path)), "vg_geom_load")
+        # the placed volumes' logical volumes, from the placements in the log
+        log = np.fromfile(path, dtype=np.float64, offset=20)
+        i = 0
+        while i < len(log):
+            op = int(log[i])
+            if op == 1:
+                i += 3 + int(log[i + 2])
+            elif op == 3:
+                g.pv_lv.append(int(log[i + 1]))
+                i += 15
+            else:
+                i += 2
+        return g
 
     def add_logical_volume(self, shape):
         return _check(_lib.vg_geom_add_logical_volume(self._h, shape), "add_logical_volume")

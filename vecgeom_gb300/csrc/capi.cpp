@@ -5,6 +5,7 @@
 #include "learn.h"
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <random>
@@ -21,6 +22,9 @@ struct vg_geom {
   vg::SortKeyParams sort{}; // set when the geometry is closed
   int queue_blocks = 1;     // work-queue kernel configuration: 1 = 256 x 1, 2 = 256 x 2, 3 = 128 x 3, 4 = 128 x 5
                             // threads x resident blocks per SM
+  // builder log for vg_geom_save / vg_geom_load: every successful builder call as
+  // (op, arguments...) in call order, so a replay reproduces every id
+  std::vector<double> oplog;
   const vg_mlp *proposer = nullptr; // learned proposal used by VG_NAV_LEARNED
   int propose_tensor      = 1;       // proposal kernel of VG_NAV_LEARNED: 1 tcgen05, 0 SIMT
   // host-pointer step: a copy stream and per-chunk events for overlapping the inputs'
@@ -206,12 +210,17 @@ int step_launch(const vg_geom *g, vg::StepArgs a, uint32_t flags, void *ws, size
   return e == cudaSuccess ? VG_OK : cuda_fail(e, "navigation step launch");
 }
 
+enum GeomOp { kOpShape = 1, kOpLv = 2, kOpPlace = 3, kOpWorld = 4 };
+
 int32_t add_shape(vg_geom *g, int type, const double *p, int np)
 {
   if (!g) return fail(VG_EINVAL, "null geometry handle");
   std::string err;
   const int32_t id = g->geo.add_shape(type, p, np, err);
-  return id < 0 ? fail(g->geo.closed ? VG_ESTATE : VG_EINVAL, err) : id;
+  if (id < 0) return fail(g->geo.closed ? VG_ESTATE : VG_EINVAL, err);
+  g->oplog.insert(g->oplog.end(), {(double)kOpShape, (double)type, (double)np});
+  g->oplog.insert(g->oplog.end(), p, p + np);
+  return id;
 }
 
 enum Query { kQInside = 0, kQContains = 1, kQDistIn = 2, kQDistOut = 3, kQSafIn = 4, kQSafOut = 5 };
@@ -350,14 +359,24 @@ int32_t vg_geom_add_logical_volume(vg_geom *g, int32_t shape_id)
   if (!g) return fail(VG_EINVAL, "null geometry handle");
   std::string err;
   const int32_t id = g->geo.add_lv(shape_id, err);
-  return id < 0 ? fail(g->geo.closed ? VG_ESTATE : VG_EINVAL, err) : id;
+  if (id < 0) return fail(g->geo.closed ? VG_ESTATE : VG_EINVAL, err);
+  g->oplog.insert(g->oplog.end(), {(double)kOpLv, (double)shape_id});
+  return id;
+}
+static void log_place(vg_geom *g, int32_t lv, int32_t mother, const double *trans, const double *rot)
+{
+  g->oplog.insert(g->oplog.end(), {(double)kOpPlace, (double)lv, (double)mother});
+  g->oplog.insert(g->oplog.end(), trans, trans + 3);
+  g->oplog.insert(g->oplog.end(), rot, rot + 9);
 }
 int32_t vg_geom_place(vg_geom *g, int32_t lv, const double trans[3], const double rot[9])
 {
   if (!g || !trans || !rot) return fail(VG_EINVAL, "null argument");
   std::string err;
   const int32_t id = g->geo.place(lv, trans, rot, -1, err);
-  return id < 0 ? fail(g->geo.closed ? VG_ESTATE : VG_EINVAL, err) : id;
+  if (id < 0) return fail(g->geo.closed ? VG_ESTATE : VG_EINVAL, err);
+  log_place(g, lv, -1, trans, rot);
+  return id;
 }
 int32_t vg_geom_place_daughter(vg_geom *g, int32_t mother_lv, int32_t lv, const double trans[3], const double rot[9])
 {
@@ -365,7 +384,9 @@ int32_t vg_geom_place_daughter(vg_geom *g, int32_t mother_lv, int32_t lv, const 
   if (mother_lv < 0) return fail(VG_EINVAL, "invalid mother logical volume id");
   std::string err;
   const int32_t id = g->geo.place(lv, trans, rot, mother_lv, err);
-  return id < 0 ? fail(g->geo.closed ? VG_ESTATE : VG_EINVAL, err) : id;
+  if (id < 0) return fail(g->geo.closed ? VG_ESTATE : VG_EINVAL, err);
+  log_place(g, lv, mother_lv, trans, rot);
+  return id;
 }
 int vg_geom_set_world(vg_geom *g, int32_t world_pv)
 {
@@ -373,6 +394,70 @@ int vg_geom_set_world(vg_geom *g, int32_t world_pv)
   if (g->geo.closed) return fail(VG_ESTATE, "geometry is closed");
   if (world_pv < 0 || world_pv >= (int32_t)g->geo.pvs.size()) return fail(VG_EINVAL, "invalid placed-volume id");
   g->geo.world = world_pv;
+  g->oplog.insert(g->oplog.end(), {(double)kOpWorld, (double)world_pv});
+  return VG_OK;
+}
+
+static const char kGeomMagic[8] = {'V', 'G', 'G', 'B', '3', '0', '0', 'G'};
+constexpr uint32_t kGeomVersion  = 1;
+
+int vg_geom_save(const vg_geom *g, const char *path)
+{
+  if (!g || !path) return fail(VG_EINVAL, "null argument");
+  FILE *f = std::fopen(path, "wb");
+  if (!f) return fail(VG_EINVAL, std::string("cannot open ") + path + " for writing");
+  const uint64_t n = g->oplog.size();
+  bool ok = std::fwrite(kGeomMagic, 1, 8, f) == 8 && std::fwrite(&kGeomVersion, 4, 1, f) == 1 &&
+            std::fwrite(&n, 8, 1, f) == 1 && (n == 0 || std::fwrite(g->oplog.data(), 8, n, f) == n);
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? VG_OK : fail(VG_EINVAL, std::string("write error on ") + path);
+}
+
+int vg_geom_load(vg_geom *g, const char *path)
+{
+  if (!g || !path) return fail(VG_EINVAL, "null argument");
+  if (!g->oplog.empty() || !g->geo.shapes.empty() || g->geo.closed)
+    return fail(VG_ESTATE, "vg_geom_load needs a new, empty geometry");
+  FILE *f = std::fopen(path, "rb");
+  if (!f) return fail(VG_EINVAL, std::string("cannot open ") + path);
+  char magic[8];
+  uint32_t version = 0;
+  uint64_t n       = 0;
+  bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kGeomMagic, 8) == 0 &&
+            std::fread(&version, 4, 1, f) == 1 && version == kGeomVersion && std::fread(&n, 8, 1, f) == 1 &&
+            n < (uint64_t(1) << 34);
+  std::vector<double> log;
+  if (ok) {
+    log.resize(n);
+    ok = n == 0 || std::fread(log.data(), 8, n, f) == n;
+  }
+  std::fclose(f);
+  if (!ok) return fail(VG_EINVAL, std::string("not a saved geometry (or truncated): ") + path);
+  size_t i = 0;
+  auto take = [&](size_t k) { return i + k <= log.size(); };
+  while (i < log.size()) {
+    const int op = (int)log[i];
+    int32_t r    = -1;
+    if (op == kOpShape && take(3) && take(3 + (size_t)log[i + 2])) {
+      const int np = (int)log[i + 2];
+      r            = add_shape(g, (int)log[i + 1], log.data() + i + 3, np);
+      i += 3 + np;
+    } else if (op == kOpLv && take(2)) {
+      r = vg_geom_add_logical_volume(g, (int32_t)log[i + 1]);
+      i += 2;
+    } else if (op == kOpPlace && take(15)) {
+      const int32_t lv = (int32_t)log[i + 1], mother = (int32_t)log[i + 2];
+      r = mother < 0 ? vg_geom_place(g, lv, log.data() + i + 3, log.data() + i + 6)
+                     : vg_geom_place_daughter(g, mother, lv, log.data() + i + 3, log.data() + i + 6);
+      i += 15;
+    } else if (op == kOpWorld && take(2)) {
+      r = vg_geom_set_world(g, (int32_t)log[i + 1]);
+      i += 2;
+    } else {
+      return fail(VG_EINVAL, std::string("corrupt saved geometry: ") + path);
+    }
+    if (r < 0) return r;
+  }
   return VG_OK;
 }
 int vg_geom_close(vg_geom *g)
