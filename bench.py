@@ -71,6 +71,9 @@ def parse():
                     help="time the headline step as replays of a captured CUDA graph (1/0)")
     ap.add_argument("--tune", type=int, default=1,
                     help="autotune sort-key bits / queue occupancy before timing (untimed; 1/0)")
+    ap.add_argument("--cell-bits", type=int, default=0, help="sort-key Morton bits per axis without --tune (0: default)")
+    ap.add_argument("--queue-blocks", type=int, default=0,
+                    help="work-queue configuration without --tune (1: 256x1, 2: 256x2, 3: 128x3, 4: 128x5; 0: default)")
     return ap.parse_args()
 
 
@@ -515,6 +518,8 @@ def main():
         from vecgeom_gb300.tune import autotune
         cands = [(head, b, q) for b in (0, 7, 5) for q in ((1, 2, 3, 4) if head & vg.NAV_QUEUE else (1,))]
         tuning = autotune(geo, t, st, candidates=cands, cache=None)
+    elif args.cell_bits or args.queue_blocks:
+        geo.set_tuning(args.cell_bits, args.queue_blocks)
     ms_fp64 = timed(vg.PREC_FP64)
     out64, step64 = out.clone(), step.clone()
     variants = {"fp64": ms_fp64}
