@@ -35,9 +35,10 @@ STEP_BYTES = 24 + 24 + 12 + 12 + 8  # p, d, state in, state out, step (FP64 SoA 
 # launch of one scheduled step on 2^20 detector step inputs; the summary is under profiles/).
 # Per-thread counts do not depend on how lanes group into warps, so they hold at 2^22.
 FP64_OPS_PER_STEP = 302.6
-# DRAM bytes per launch of the step kernel, from the same capture (read 499.5 MB + write
-# 66.3 MB per 2^20 steps), scaled to the 2^22-step launch by the steps it processes.
-STEP_TRAFFIC_PER_STEP = (499.5e6 + 66.3e6) / (1 << 20)
+# DRAM bytes per launch of the step kernel in the tuned 128 x 5 configuration, from one ncu
+# capture (read 727.3 MB + write 297.5 MB per 2^20 steps, spills included), scaled to the
+# 2^22-step launch by the steps it processes.
+STEP_TRAFFIC_PER_STEP = (727.3e6 + 297.5e6) / (1 << 20)
 # name -> (precision | scheduling flags): 1 = VG_PREC_MIXED, 2 = VG_NAV_SORT, 4 = VG_NAV_QUEUE
 # 8 = VG_NAV_LEARNED (explore the BVH subtree proposed by the trained model first)
 SCHEDULES = {"fp64": 0, "fp64_sort": 2, "mixed": 1, "mixed_sort": 3, "mixed_queue": 5, "mixed_sort_queue": 7,
@@ -648,8 +649,8 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": STEP_TRAFFIC_PER_STEP * n if head & 4 else None,
                      "traffic_note": "DRAM read + write of one step-kernel launch, ncu on 2^20 steps scaled to %d "
-                                     "(geometry L2 misses and the sorted-order gathers: 540 B/step vs 80 "
-                                     "algorithmic)" % n,
+                                     "(128 x 5 queue kernel: geometry L2 misses, sorted-order gathers and register "
+                                     "spills: 977 B/step vs 80 algorithmic)" % n,
                      "kernel": "k_step_mixed_queue" if head & 4 else ("k_step_mixed" if head & 1 else "k_step"),
                      "step_kernel_time_note": "sort and proposal kernels excluded" if head & 8 else "sort excluded",
                      "note": "algorithmic bytes %d B/step over the step kernel's time (sort excluded); the "
