@@ -280,7 +280,11 @@ class _Reader:
 def load(source, geo, close=True):
     """Build the GDML geometry `source` (a path, or the document text when it starts with
     '<') on `geo`; returns a GDMLGeometry. `close=False` leaves the geometry open."""
-    text = source if source.lstrip().startswith("<") else open(source, encoding="utf-8").read()
+    if source.lstrip().startswith("<"):
+        text = source
+    else:
+        with open(source, encoding="utf-8") as f:
+            text = f.read()
     root = ET.fromstring(text)
     r = _Reader(geo, close)
     r.node(root)
