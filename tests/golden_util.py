@@ -3,7 +3,6 @@ made by tests/golden/extract_unit_vectors.py): loading, shape construction throu
 geometry API (the oracle's or the product's, which share method names), and the tests'
 own comparison rules."""
 import json
-import math
 import os
 
 import numpy as np

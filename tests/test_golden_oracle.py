@@ -4,7 +4,6 @@ tests/golden/unit_*.json): every extracted assert passes with the tests' own com
 Soft checks (TestCons prints a mismatch instead of asserting) must pass too, except the
 ones listed in golden_util.SOFT_EXCEPTIONS, where the reference's own code path gives a
 different answer (each entry says why)."""
-import numpy as np
 import pytest
 
 import golden_util as G

@@ -2,7 +2,6 @@
 (sort, tensor-core proposals, persistent step kernel) captured into a graph and replayed
 gives the eager call's states and steps, also after the inputs change in place; the plain
 FP64 step likewise."""
-import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
