@@ -41,6 +41,8 @@ FILES = {
 # unplaced shapes constructed without a label argument
 NO_LABEL = {"vecgeom::UnplacedTrapezoid"}
 QUERIES = {"Inside", "Contains", "DistanceToIn", "DistanceToOut", "SafetyToIn", "SafetyToOut"}
+# Extent(lo, hi) results are recorded as the queries "ExtentMin" / "ExtentMax" (no point;
+# the expected value is a vector compared component-wise with ApproxEqual)
 
 
 class V:
@@ -249,6 +251,7 @@ class Extractor:
         self.env = dict(BASE_ENV)
         self.shapes = {}   # var -> {"type", "args"}
         self.lvs = {}      # logical-volume var -> shape var
+        self.uninit = set()  # vectors declared without a value and not assigned since
         self.results = {}  # var -> pending query descriptor
         self.cases = []
         self.skipped = 0
@@ -322,6 +325,13 @@ class Extractor:
                 except Exception:
                     continue
                 if isinstance(val, V):
+                    # an expected vector must be a value the test states, not another
+                    # output (e.g. GetBBox into a vector declared without a value)
+                    if qd["query"].startswith("Extent") and a[1].strip() not in self.uninit:
+                        self.emit(qd, "approx_vec", list(val.v), line)
+                        ok = True
+                    continue
+                if qd["query"].startswith("Extent"):
                     continue
                 self.emit(qd, "approx", float(val), line)
                 ok = True
@@ -472,6 +482,7 @@ class Extractor:
                             self.env[mm.group(1)] = self.ev(mm.group(2))
                         else:
                             self.env[decl] = V()
+                            self.uninit.add(decl)  # declared without a value
                 except Exception:
                     self.skipped += 1
             return
@@ -515,6 +526,7 @@ class Extractor:
         m = re.match(r"^(\w+)\s*=\s*(.*)$", st, flags=re.S)
         if m:
             var, rhs = m.group(1), m.group(2)
+            self.uninit.discard(var)
             qd = None
             try:
                 qd = self.query_call(rhs)
@@ -528,6 +540,16 @@ class Extractor:
                 self.env[var] = self.ev(rhs)
             except Exception:
                 self.env.pop(var, None)
+            return
+        # shape.Extent(lo, hi): the two vectors become pending results (known answers follow)
+        m = re.match(r"^(\w+)\s*(?:\.|->)\s*Extent\s*\(\s*(\w+)\s*,\s*(\w+)\s*\)$", st)
+        if m:
+            if m.group(1) in self.shapes:
+                for var, q in ((m.group(2), "ExtentMin"), (m.group(3), "ExtentMax")):
+                    self.results[var] = {"shape": m.group(1), "query": q, "p": None, "d": None}
+                    self.env.pop(var, None)
+            else:
+                self.skipped += 1
             return
         # in-place vector mutators
         m = re.match(r"^(\w+)\s*\.\s*(Normalize|Set)\s*\((.*)\)$", st, flags=re.S)

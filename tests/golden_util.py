@@ -93,10 +93,23 @@ def passes(kind, actual, expected, tol=None):
     return {"==": a == e, "!=": a != e, "<": a < e, "<=": a <= e, ">": a > e, ">=": a >= e}[kind]
 
 
+def approx_equal_vec(v, w):
+    """ApproxEqual of two 3-vectors (component-wise, test/unit_tests/ApproxEqual.h:21-28)."""
+    return all(approx_equal(float(a), float(b)) for a, b in zip(v, w))
+
+
+def extent_cases(doc):
+    """The Extent(lo, hi) known answers: (shape name, "ExtentMin" / "ExtentMax", expected)."""
+    return [(c["shape"], c["query"], c["expected"]) for c in doc["cases"] if c["query"].startswith("Extent")]
+
+
 def grouped(doc):
-    """Cases grouped by (shape, query): arrays of points/directions and the case list."""
+    """Cases grouped by (shape, query): arrays of points/directions and the case list
+    (the point queries only; Extent cases are in extent_cases)."""
     groups = {}
     for c in doc["cases"]:
+        if c["query"] not in QUERY_ID:
+            continue
         groups.setdefault((c["shape"], c["query"]), []).append(c)
     for (shape, q), cs in groups.items():
         p = np.array([c["p"] for c in cs], dtype=np.float64)

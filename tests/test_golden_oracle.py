@@ -4,6 +4,7 @@ tests/golden/unit_*.json): every extracted assert passes with the tests' own com
 Soft checks (TestCons prints a mismatch instead of asserting) must pass too, except the
 ones listed in golden_util.SOFT_EXCEPTIONS, where the reference's own code path gives a
 different answer (each entry says why)."""
+import numpy as np
 import pytest
 
 import golden_util as G
@@ -28,6 +29,27 @@ def test_oracle_matches_reference_unit_tests(name):
             if not G.passes(c["kind"], v, c["expected"], c.get("tol")) and not G.excepted(name, c):
                 fails.append((c["line"], shape, q, c["p"], c["d"], c["kind"], c["expected"], float(v)))
     assert not fails, "%d of %d fail, first: %s" % (len(fails), len(doc["cases"]), fails[:5])
+
+
+@pytest.mark.parametrize("name", G.FILES)
+def test_extents_match_reference_unit_tests(name):
+    """The Extent known answers of the same tests, for the oracle and for the product's host
+    geometry builder (whose extents make the BVH boxes); the two also agree exactly."""
+    import vecgeom_gb300 as vg
+    from oracle.oracle import OracleGeometry
+    doc = G.load(name)
+    cases = G.extent_cases(doc)
+    if not cases:
+        pytest.skip("the test file checks no extents")
+    for shape, q, expected in cases:
+        spec = doc["shapes"][shape]
+        got = []
+        for geo in (OracleGeometry(), vg.Geometry()):
+            s = G.add_shape(geo, spec)
+            lo, hi = geo.shape_extent(s)
+            got.append(np.array(lo if q == "ExtentMin" else hi))
+        assert G.approx_equal_vec(got[0], expected), (name, shape, q, got[0], expected)
+        assert np.array_equal(got[0], got[1]), (name, shape, q)
 
 
 def test_pin_detects_a_planted_error():
