@@ -29,6 +29,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+METRIC = "nav steps/s on 1 GB300, plain FP64 vs mixed-prec+learned order, ids identical"
+UNIT = "nav steps/s"
 STEP_BYTES = 24 + 24 + 12 + 12 + 8  # p, d, state in, state out, step (FP64 SoA + 12 B states)
 # FP64-pipe thread instructions per scheduled detector step (sort keys 3.0 + proposal 10.2 +
 # step kernel 289.4), counted by ncu (sm__thread_inst_executed_pipe_fp64_pred_on over every
@@ -301,13 +303,42 @@ QUERY_BYTES = {"inside": 28, "contains": 25, "distance_to_in": 56, "distance_to_
                "safety_to_out": 32}  # FP64 SoA inputs + output per query (step_max not passed)
 
 
-def shape_rows(args, torch, dev, hbm_peak):
+# Parity bar of distances and safeties against the FP64 oracle (the tests' bar)
+ABS_TOL, REL_TOL = 1e-9, 1e-12
+INF = np.finfo(np.float64).max
+
+
+def compare_to_oracle(gpu, ref):
+    """Parity figures of one GPU output array against the oracle's on the same inputs:
+    integer outputs must be equal; distances and safeties within 1e-9 mm + 1e-12 relative,
+    with the kInfLength sentinel matching exactly."""
+    gpu, ref = np.asarray(gpu), np.asarray(ref)
+    if gpu.dtype != np.float64:
+        return {"mismatch_vs_oracle": int((gpu.astype(np.int64) != ref.astype(np.int64)).sum())}
+    inf_g, inf_r = gpu == INF, ref == INF
+    fin = ~inf_g & ~inf_r
+    d = np.abs(gpu - ref)[fin]
+    tol = ABS_TOL + REL_TOL * np.abs(ref[fin])
+    return {"max_abs_err_vs_oracle": float(d.max()) if d.size else 0.0,
+            "beyond_tol_vs_oracle": int((d > tol).sum()) + int((inf_g != inf_r).sum()),
+            "bit_identical_to_oracle": int((gpu.view(np.int64) == ref.view(np.int64)).sum())}
+
+
+QUERY_INDEX = {"inside": 0, "contains": 1, "distance_to_in": 2, "distance_to_out": 3, "safety_to_in": 4,
+               "safety_to_out": 5}
+
+
+def shape_rows(args, torch, dev, hbm_peak, oracle=True):
     """Config 1 (Box, Tube, Cone; 2^20 points uniform in the 1.2x extent box) and config 2
     (2^22 points: thirds inside, outside, within 1e-6 mm of the surface) shape queries per
-    precision: queries/s, algorithmic GB/s and its fraction of the HBM peak, and for the
-    mixed path the largest difference to FP64 per query."""
+    precision: queries/s, algorithmic GB/s and its fraction of the HBM peak; every output of
+    both precisions is compared with the FP64 oracle run over the same points on the host
+    cores (untimed), and the mixed path also with the FP64 kernel."""
     import vecgeom_gb300 as vg
     from vecgeom_gb300 import workloads as W
+    if oracle:
+        from oracle.oracle import OracleGeometry
+    nthreads = os.cpu_count() or 1
     rows = []
     cases = [(k, v, 1 << 20, "cfg1") for k, v in W.SHAPES_CFG1.items()] + \
             [(k, v, 1 << 22, "cfg2") for k, v in W.SHAPES_CFG2.items()]
@@ -328,6 +359,11 @@ def shape_rows(args, torch, dev, hbm_peak):
             pts, dirs = W.shape_points_mixed(lo, hi, n, args.seed, lambda *c: q_gpu(g.inside, torch.int32, *c),
                                              lambda *c: q_gpu(g.distance_to_out, torch.float64, *c))
         t = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (*pts, *dirs)]
+        o_geo = o_pv = None
+        if oracle:
+            o_geo = OracleGeometry()
+            _, o_pv = W.build_single_shape(o_geo, kind, params)
+            host_cols = [np.ascontiguousarray(a) for a in (*pts, *dirs)]
         outs = {"inside": torch.empty(n, dtype=torch.int32, device=dev),
                 "contains": torch.empty(n, dtype=torch.uint8, device=dev)}
         for prec_name, prec in (("fp64", vg.PREC_FP64), ("mixed", vg.PREC_MIXED)):
@@ -346,6 +382,12 @@ def shape_rows(args, torch, dev, hbm_peak):
                 row = {"config": cfg, "shape": name, "query": q, "precision": prec_name, "n": n,
                        "input_bytes": QUERY_BYTES[q] * n, "l2_resident_inputs": QUERY_BYTES[q] * n < 129e6,
                        "queries_per_s": n / (ms * 1e-3), "GB_per_s": gbs, "hbm_frac": gbs / hbm_peak}
+                if oracle:
+                    if (q, "oracle") not in outs:
+                        outs[(q, "oracle")] = o_geo.query(o_pv, QUERY_INDEX[q], *host_cols, nthreads=nthreads)[0]
+                    got = o.cpu().numpy()
+                    row.update(compare_to_oracle(got.astype(np.int32) if q == "contains" else got,
+                                                 outs[(q, "oracle")]))
                 if prec_name == "fp64":
                     outs[(q, "ref")] = o.clone()
                 else:
@@ -377,47 +419,29 @@ def cpu_time_steps(args, host_inputs, host_states, nthreads, reps=5):
     return rates[0], rates[1]
 
 
-def oracle_sample_steps(o, m, seed, nthreads, max_steps=400):
-    """The detector workload's step inputs generated on the CPU: m primaries transported by
-    the oracle, every pre-step (point, direction, state) pooled, m of them drawn uniformly."""
-    from vecgeom_gb300 import workloads as W
-    (x, y, z), (dx, dy, dz) = W.primaries_eta_phi(m, seed)
-    st, _ = o.locate(x, y, z, nthreads=nthreads)
-    pool = [[] for _ in range(7)]
-    for _ in range(max_steps):
-        alive = st["nav_ind"] != 0
-        if not alive.any():
-            break
-        for k, a in enumerate((x, y, z, dx, dy, dz, st)):
-            pool[k].append(a[alive])
-        out, step, _, _ = o.step(x, y, z, dx, dy, dz, st, nthreads=nthreads)
-        x = np.where(alive, x + step * dx, x)
-        y = np.where(alive, y + step * dy, y)
-        z = np.where(alive, z + step * dz, z)
-        st = np.where(alive, out, st)
-    cat = [np.concatenate(p) for p in pool]
-    pick = W.rng(seed, 21).permutation(len(cat[0]))[:m]
-    return [np.ascontiguousarray(c[pick]) for c in cat[:6]], np.ascontiguousarray(cat[6][pick])
-
-
 def run_reference(args, ws, rank):
     """CPU implementation of the path (the oracle port; the reference itself needs VecCore,
-    which is not available) on all host cores, same metric and config, each step a bounded
-    sample of the batch."""
+    which is not available) on all host cores, same metric and config. Each step is a
+    bounded sample of the batch: the first --cpu-sample of the GPU arm's own step inputs,
+    reproduced on the CPU (the same primaries transported by the oracle, the same seeded
+    draw), so both arms' CPU figures step the very same tracks."""
     if rank != 0:
         return
     nthreads = os.cpu_count() or 1
-    from oracle.oracle import OracleGeometry
+    from oracle.oracle import OracleGeometry, transport_step_sample
     from vecgeom_gb300 import workloads as W
     o = OracleGeometry()
     builder(args.workload)(o)
     m = min(args.cpu_sample, args.tracks)
     if args.workload == "detector":
-        sub, st = oracle_sample_steps(o, m, args.seed, nthreads)
+        sub, st, _ = transport_step_sample(o, args.tracks, args.seed, args.primaries, nthreads=nthreads, first=m)
+        sample = ("the first %d of the %d step inputs of the GPU arm (its transport-history draw, reproduced "
+                  "on the host by the oracle)" % (m, args.tracks))
     else:
-        pts, dirs = W.tracks_in_cylinder(m, seed=args.seed)
-        sub = [np.ascontiguousarray(a) for a in (*pts, *dirs)]
+        pts, dirs = W.tracks_in_cylinder(args.tracks, seed=args.seed)
+        sub = [np.ascontiguousarray(a[:m]) for a in (*pts, *dirs)]
         st, _ = o.locate(*sub[:3], nthreads=nthreads)
+        sample = "the first %d of the %d tracks of the GPU arm" % (m, args.tracks)
     for _ in range(args.warmup):
         o.step(*sub, st, nthreads=nthreads)
     times = []
@@ -426,15 +450,13 @@ def run_reference(args, ws, rank):
         times.append(t)
     tot = sum(times)
     value = m * args.steps / tot
-    line = {"metric": "nav steps/s", "value": value, "unit": "nav steps/s", "n_gpus": args.gpus, "steps": args.steps,
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": config_of(args), "impl": "reference",
-            "cpu_baseline": {"value": value, "unit": "nav steps/s", "cores": nthreads, "kind": "port",
-                             "sample": "%d step inputs per step (drawn from the oracle's own transport "
-                                       "histories when the workload is the detector) of the %d-track batch"
-                                       % (m, args.tracks)},
-            "e2e": {"value": value, "unit": "nav steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                             "sample": sample + ", every step"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -538,6 +560,7 @@ def main():
     n_err = int((status != 0).sum().item())
     ids_equal = bool(torch.equal(out64, out))
     step_err = float((step64 - step).abs().max().item())
+    head_out, head_step = out.cpu().numpy(), step.cpu().numpy()
 
     # the track sort alone (part of every sorted step), to separate the step kernel's time
     ms_sort = 0.0
@@ -575,12 +598,13 @@ def main():
     ms_kernel = ms_head - ms_sort - ms_propose
 
     stream = run_stream(args, geo, torch, dev, head, ClockSampler, local) if (args.stream and rank == 0) else None
-    peaks_early = {}
+    peaks = {}
     try:
-        peaks_early = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except (OSError, ValueError):
         pass
-    shapes = shape_rows(args, torch, dev, peaks_early.get("hbm_gbs", 6800.0)) if (args.shapes and rank == 0) else None
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    shapes = shape_rows(args, torch, dev, hbm_peak) if (args.shapes and rank == 0) else None
 
     # e2e: host arrays through the host-pointer C-ABI entry point, copies inside the timed region
     hp = [a.cpu().pin_memory() for a in t]
@@ -606,14 +630,8 @@ def main():
     in_order = [round(1e3 * c, 3) for c in calls]
     calls.sort()
     e2e_calls = {"calls": ke, "min": round(1e3 * calls[0], 3), "median": round(1e3 * calls[ke // 2], 3),
-                 "max": round(1e3 * calls[-1], 3), "in_order": in_order}
+                 "max": round(1e3 * calls[-1], 3)}
 
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except (OSError, ValueError):
-        pass
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
     value = ws * n / (ms_head * 1e-3)
     achieved = STEP_BYTES * n / (ms_kernel * 1e-3) / 1e9
     # FP64 roofline of the scheduled step (the bound of the navigation rows): FP64 pipe
@@ -624,57 +642,141 @@ def main():
         roofline_fp64 = {"bound": "fp64", "achieved": FP64_OPS_PER_STEP * n / (ms_head * 1e-3), "peak": fp64_peak,
                          "unit": "FP64 thread-ops/s", "frac": FP64_OPS_PER_STEP * n / (ms_head * 1e-3) / fp64_peak,
                          "ops_per_step": FP64_OPS_PER_STEP,
-                         "note": "ops per step counted by ncu (summary under profiles/); peak = DFMA "
-                                 "rate of a probe kernel timed in this run"}
-    line = {
-        "metric": "nav steps/s", "value": value, "unit": "nav steps/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_head, "higher_is_better": True, "scaling": "weak",
-        "ms_per_step_min_max": [round(v, 4) for v in spread.get(head, (ms_head, ms_head))],
-        "cuda_graph": bool(args.graph), "ms_per_step_eager": ms_head_eager,
-        "vs_baseline": None, "dtype": "f64 (mixed: FP32 pruning, FP64 decisions)",
-        "data": "synthetic (seeded; geometry built in code, tracks generated on the GPU)",
-        "config": dict(config_of(args, pool), schedule=args.schedule,
-                       l2="inputs %.0f MB > L2 (129 MB); geometry L2/HBM-resident by design" % (n * 60 / 1e6),
-                       parallelism="replicas" if ws > 1 else "single GPU"),
-        "plain_fp64": {"value": ws * n / (ms_fp64 * 1e-3), "ms_per_step": ms_fp64},
-        "speedup_vs_plain_fp64": ms_fp64 / ms_head,
-        "ids_identical_to_fp64": ids_equal, "max_step_diff_vs_fp64_mm": step_err,
-        "schedules_ms_per_step": variants, "all_schedules_identical_to_fp64": identical and ids_equal,
-        "sort_ms_per_step": ms_sort, "propose_ms_per_step": ms_propose, "step_kernel_ms_per_step": ms_kernel,
-        "tuning": None if tuning is None else {k: tuning[k] for k in ("cell_bits", "queue_blocks", "timings")},
-        "learned": learned_info,
-        "transport_stream": stream,
-        "shape_queries": shapes,
-        "e2e": {"value": ws * n / e2e_s, "unit": "nav steps/s", "h2d_bytes_per_step": n * (48 + 12),
-                "d2h_bytes_per_step": n * (12 + 8), "ms_per_call": e2e_calls},
+                         "note": "ncu-counted ops per step; peak = DFMA probe timed in this run"}
+    m = {
+        "value": value, "ms_per_step": ms_head, "n": n, "ws": ws, "args": args, "pool": pool,
+        "ms_fp64": ms_fp64, "ms_fp64_sort": variants.get("fp64_sort"), "ids_equal": ids_equal, "step_err": step_err,
+        "e2e_value": ws * n / e2e_s, "e2e_calls": e2e_calls, "head": head, "passes": passes,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": STEP_TRAFFIC_PER_STEP * n if head & 4 else None,
-                     "traffic_note": "DRAM read + write of one step-kernel launch, ncu on 2^20 steps scaled to %d "
-                                     "(128 x 5 queue kernel: geometry L2 misses, sorted-order gathers and register "
-                                     "spills: 977 B/step vs 80 algorithmic)" % n,
                      "kernel": "k_step_mixed_queue" if head & 4 else ("k_step_mixed" if head & 1 else "k_step"),
-                     "step_kernel_time_note": "sort and proposal kernels excluded" if head & 8 else "sort excluded",
-                     "note": "algorithmic bytes %d B/step over the step kernel's time (sort excluded); the "
-                             "kernel is issue/latency bound, not HBM-bound, see profiles/; peak %s"
-                             % (STEP_BYTES, "of measured" if peaks else "of fallback")},
-        "roofline_fp64": roofline_fp64,
-        "gpu_launches": args.steps * (1 + ((1 + 3 * passes) if head & 2 else 0) + (1 if head & 8 else 0)),
-        "track_errors": n_err,
-        "clocks": clocks.summary(),
+                     "note": "80 algorithmic B/step over the step kernel's own time; traffic = ncu DRAM bytes "
+                             "of one launch (2^20-step capture scaled by steps); peak %s"
+                             % ("of measured" if peaks else "of fallback")},
+        "roofline_fp64": roofline_fp64, "n_err": n_err, "clocks": clocks.summary(),
     }
     if rank == 0:
-        m = min(args.cpu_sample, n)
-        hin = [a[:m].cpu().numpy() for a in t]
-        hs = st[: m * 12].cpu().numpy()
+        emit({"section": "schedules", "ms_per_step": variants, "all_identical_to_fp64": identical and ids_equal,
+              "ms_per_step_min_max": [round(v, 4) for v in spread.get(head, (ms_head, ms_head))],
+              "ms_per_step_eager": ms_head_eager, "cuda_graph": bool(args.graph),
+              "sort_ms_per_step": ms_sort, "propose_ms_per_step": ms_propose, "step_kernel_ms_per_step": ms_kernel,
+              "tuning": None if tuning is None else {k: tuning[k] for k in ("cell_bits", "queue_blocks", "timings")},
+              "e2e_ms_per_call_in_order": in_order})
+        if learned_info is not None:
+            emit({"section": "learned", **learned_info})
+        if stream is not None:
+            emit({"section": "transport_stream", **stream})
+        if shapes is not None:
+            emit({"section": "shape_queries", "rows": shapes})
+        # parity against the FP64 oracle over every one of the n step inputs (host cores,
+        # untimed), for the headline schedule and for plain FP64
         nthreads = os.cpu_count() or 1
-        cv, cv1 = cpu_time_steps(args, hin, hs, nthreads)
-        line["cpu_baseline"] = {"value": cv, "unit": "nav steps/s", "cores": nthreads, "kind": "port",
-                                "single_thread_value": cv1,
-                                "sample": "%d of the %d step inputs, median of 5 after a warm-up" % (m, n)}
-        print(json.dumps(line), flush=True)
+        from oracle.oracle import OracleGeometry
+        og = OracleGeometry()
+        builder(args.workload)(og)
+        hin = [np.ascontiguousarray(a.cpu().numpy()) for a in t]
+        hst_np = np.frombuffer(st.cpu().numpy().tobytes(), dtype=NAVSTATE_NP).copy()
+        o_out, o_step, _, o_sec = og.step(*hin, hst_np, nthreads=nthreads)
+        parity = {"section": "parity_vs_oracle", "tracks": n, "oracle_seconds": round(o_sec, 3),
+                  "oracle_threads": nthreads,
+                  "headline": nav_parity(head_out, head_step, o_out, o_step),
+                  "plain_fp64": nav_parity(out64.cpu().numpy(), step64.cpu().numpy(), o_out, o_step)}
+        if shapes is not None:
+            parity["shapes"] = shape_parity_summary(shapes)
+        emit(parity)
+        m["parity"] = parity
+        # CPU baseline: the oracle on the first cpu_sample step inputs (the same inputs the
+        # reference arm reproduces and steps)
+        k = min(args.cpu_sample, n)
+        cv, cv1 = cpu_time_steps(args, [a[:k] for a in hin], hst_np[:k], nthreads)
+        m["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": nthreads, "kind": "port",
+                             "single_thread_value": cv1,
+                             "sample": "the first %d of the %d step inputs, median of 5 after a warm-up" % (k, n)}
+        emit(headline_line(m))
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+NAVSTATE_NP = np.dtype([("nav_ind", "<u4"), ("last_exited", "<u4"), ("on_boundary", "u1"), ("pad", "u1", 3)])
+
+
+def emit(obj):
+    print(json.dumps(obj), flush=True)
+
+
+def nav_parity(gpu_out, gpu_step, o_out, o_step):
+    """Out-states (all three fields) must be bit-identical to the oracle's; steps within
+    1e-9 mm + 1e-12 relative (reported: bit-identical count and largest difference)."""
+    g = np.frombuffer(np.ascontiguousarray(gpu_out).tobytes(), dtype=NAVSTATE_NP)
+    diff = ((g["nav_ind"] != o_out["nav_ind"]) | (g["last_exited"] != o_out["last_exited"])
+            | (g["on_boundary"] != o_out["on_boundary"]))
+    r = {"state_mismatch": int(diff.sum()), "next_volume_mismatch": int((g["nav_ind"] != o_out["nav_ind"]).sum())}
+    r.update(compare_to_oracle(np.asarray(gpu_step, dtype=np.float64), o_step))
+    return r
+
+
+def shape_parity_summary(rows):
+    """Totals of the shape rows' oracle comparison, per precision, with the largest error
+    per shape; mixed Box safeties are lowered by their proven bound on purpose and are
+    listed apart."""
+    out = {}
+    for prec in ("fp64", "mixed"):
+        sel = [r for r in rows if r["precision"] == prec]
+        bounded = [r for r in sel if prec == "mixed" and r["shape"] == "box" and r["query"].startswith("safety")]
+        strict = [r for r in sel if r not in bounded]
+        per_shape = {}
+        for r in strict:
+            e = r.get("max_abs_err_vs_oracle")
+            if e is not None:
+                per_shape[r["shape"]] = max(per_shape.get(r["shape"], 0.0), e)
+        out[prec] = {"queries": sum(r["n"] for r in sel),
+                     "int_mismatch": sum(r.get("mismatch_vs_oracle", 0) for r in strict),
+                     "beyond_tol": sum(r.get("beyond_tol_vs_oracle", 0) for r in strict),
+                     "max_abs_err_per_shape": per_shape}
+        if bounded:
+            out[prec]["box_safety_bounded_max_err"] = max(r["max_abs_err_vs_oracle"] for r in bounded)
+    return out
+
+
+def headline_line(m):
+    """The result line the driver parses (the last line of stdout, kept to a few KB): the
+    contract keys, e2e, rooflines, CPU baseline, clocks and the identity/parity summary."""
+    args, n, ws = m["args"], m["n"], m["ws"]
+    cfg = {"workload": "config-4 detector nav step (150,213 placed volumes: 150k barrel box modules, 2x12 "
+                       "Polycone holders, 2x2000 Trd wedges; depth 4)" if args.workload == "detector"
+           else "config-3 barrel nav step (1e4 placed volumes, depth 4)",
+           "tracks": args.tracks, "seed": args.seed, "schedule": args.schedule,
+           "l2": "inputs %.0f MB > L2 (129 MB)" % (n * 60 / 1e6),
+           "parallelism": "replicas" if ws > 1 else "single GPU"}
+    line = {
+        "metric": METRIC, "value": m["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": m["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 (mixed: FP32 pruning, FP64 decisions)",
+        "data": "synthetic (seeded; geometry built in code, tracks from GPU transport histories)", "config": cfg,
+        "plain_fp64_value": ws * n / (m["ms_fp64"] * 1e-3),
+        "speedup_vs_plain_fp64": m["ms_fp64"] / m["ms_per_step"],
+        "speedup_vs_fp64_sort": (m["ms_fp64_sort"] / m["ms_per_step"]) if m.get("ms_fp64_sort") else None,
+        "ids_identical_to_fp64": m["ids_equal"], "max_step_diff_vs_fp64_mm": m["step_err"],
+        "e2e": {"value": m["e2e_value"], "unit": UNIT, "h2d_bytes_per_step": n * (48 + 12),
+                "d2h_bytes_per_step": n * (12 + 8), "ms_per_call": m["e2e_calls"]},
+        "roofline": m["roofline"], "roofline_fp64": m["roofline_fp64"],
+        "gpu_launches": args.steps * (1 + ((1 + 3 * m["passes"]) if m["head"] & 2 else 0) + (1 if m["head"] & 8 else 0)),
+        "track_errors": m["n_err"], "clocks": m["clocks"],
+    }
+    par = m.get("parity")
+    if par:
+        h, f = par["headline"], par["plain_fp64"]
+        line["vs_oracle"] = {"tracks": par["tracks"], "state_mismatch": h["state_mismatch"],
+                             "step_beyond_tol": h["beyond_tol_vs_oracle"],
+                             "step_max_abs_err": h["max_abs_err_vs_oracle"],
+                             "plain_fp64_state_mismatch": f["state_mismatch"]}
+        if "shapes" in par:
+            line["vs_oracle"]["shape_queries"] = {p: {k: v for k, v in d.items() if k != "max_abs_err_per_shape"}
+                                                  for p, d in par["shapes"].items()}
+    if "cpu_baseline" in m:
+        line["cpu_baseline"] = m["cpu_baseline"]
+    return line
 
 
 if __name__ == "__main__":

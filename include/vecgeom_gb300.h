@@ -266,12 +266,15 @@ int vg_nav_compute_step_and_next_volume_ws(const vg_geom *g, const double *x, co
                                            uint32_t flags, void *workspace, size_t workspace_bytes, void *stream);
 
 /* The scheduled step without any allocation and without a caller workspace: scratch is a
- * fixed device array inside the library (capacity 2^20 tracks per call; larger n is
- * rejected with VG_EINVAL). No reference counterpart: it exists for callers that may not
- * allocate device memory on the step path. Calls that overlap in time share the scratch
- * and race, so callers serialise them; the first call on a device looks the scratch up
- * and belongs in setup, before any stream capture. Same flags and results as
- * vg_nav_compute_step_and_next_volume_ws. */
+ * fixed 17.3 MiB device array inside the library (capacity 2^20 tracks per call with any
+ * flags, VG_NAV_LEARNED's proposal slots included; larger n is rejected with VG_EINVAL).
+ * No reference counterpart: it exists for callers that may not allocate device memory on
+ * the step path. Calls that overlap in time share the scratch and race, so callers
+ * serialise them; the first call on a device looks the scratch up and belongs in setup,
+ * before any stream capture. The looked-up address is kept for the life of the process:
+ * after cudaDeviceReset (or a reset of the primary context) it is stale, so a process
+ * that resets a device must not call this entry point on it again. Same flags and results
+ * as vg_nav_compute_step_and_next_volume_ws. */
 int vg_nav_compute_step_and_next_volume_noalloc(const vg_geom *g, const double *x, const double *y, const double *z,
                                                 const double *dx, const double *dy, const double *dz,
                                                 const double *step_limit, const vg_navstate *in, vg_navstate *out,

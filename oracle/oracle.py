@@ -230,3 +230,59 @@ class OracleGeometry:
         t = _lib.oracle_nav_transport(self._h, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(states),
                                       max_steps, _p(nsteps), _p(final), _p(tr), _p(trs), nthreads)
         return nsteps, final, tr, trs, t
+
+
+def transport_step_sample(o, n_samples, seed, n_primaries, max_steps=200, nthreads=1, first=None):
+    """The step inputs of vecgeom_gb300.workloads.sample_transport_steps reproduced on the
+    CPU: the same primaries transported by the oracle's FP64 navigator (positions advanced as
+    p + step * d), every pre-step (point, direction, state) of the alive tracks pooled in the
+    same order, and the same seeded uniform draw (torch.randperm on a CPU generator) of
+    `n_samples` of them. The GPU's FP64 step equals the oracle's bit for bit, so the result
+    is the GPU sample itself; `first` keeps only that many leading samples. Two transport
+    passes: the first counts the pool, the second gathers the drawn entries. Returns
+    ([x, y, z, dx, dy, dz], states, pool size)."""
+    import torch
+
+    from vecgeom_gb300 import workloads as W
+    (x0, y0, z0), (dx, dy, dz) = W.primaries_eta_phi(n_primaries, seed)
+
+    def transport(visit):
+        x, y, z = x0.copy(), y0.copy(), z0.copy()
+        st, _ = o.locate(x, y, z, nthreads=nthreads)
+        for it in range(max_steps):
+            idx = np.flatnonzero(st["nav_ind"] != 0)
+            if idx.size == 0:
+                break
+            a = [np.ascontiguousarray(v[idx]) for v in (x, y, z, dx, dy, dz)]
+            sa = np.ascontiguousarray(st[idx])
+            visit(it, a, sa)
+            out, step, _, _ = o.step(*a, sa, nthreads=nthreads)
+            x[idx] = a[0] + step * a[3]
+            y[idx] = a[1] + step * a[4]
+            z[idx] = a[2] + step * a[5]
+            st[idx] = out
+
+    counts = []
+    transport(lambda it, a, sa: counts.append(len(sa)))
+    total = int(sum(counts))
+    gen = torch.Generator(device="cpu").manual_seed(seed & 0x7FFFFFFF)
+    pick = torch.randperm(total, generator=gen)[:n_samples].numpy()
+    if first is not None:
+        pick = pick[:first]
+    starts = np.concatenate([[0], np.cumsum(counts)])
+    cols = [np.empty(len(pick)) for _ in range(6)]
+    states = np.zeros(len(pick), NAVSTATE_DTYPE)
+    order = np.argsort(pick, kind="stable")
+    sorted_pick = pick[order]
+
+    def gather(it, a, sa):
+        lo, hi = np.searchsorted(sorted_pick, [starts[it], starts[it + 1]])
+        if hi > lo:
+            rows = order[lo:hi]
+            local = sorted_pick[lo:hi] - starts[it]
+            for k in range(6):
+                cols[k][rows] = a[k][local]
+            states[rows] = sa[local]
+
+    transport(gather)
+    return cols, states, total

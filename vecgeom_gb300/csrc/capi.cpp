@@ -811,9 +811,13 @@ int vg_nav_compute_step_and_next_volume_noalloc(const vg_geom *g, const double *
     return fail(VG_EINVAL, "null input/output array");
   void *ws     = nullptr;
   size_t bytes = 0;
-  if (flags & (VG_NAV_SORT | VG_NAV_QUEUE)) {
+  if (step_workspace_bytes(n, flags & kNavFlags) > 0) {
     const cudaError_t e = vg::noalloc_scratch(&ws, &bytes);
     if (e != cudaSuccess) return cuda_fail(e, "no-allocation scratch lookup");
+    // the fixed array must hold the workspace of the largest call with every flag
+    if (bytes < step_workspace_bytes(vg::noalloc_max_tracks(), kNavFlags))
+      return fail(VG_ESTATE, "no-allocation scratch smaller than the workspace of " +
+                                 std::to_string(vg::noalloc_max_tracks()) + " tracks");
   }
   vg::StepArgs a{x,   y,   z,   dx,  dy,  dz, step_limit, reinterpret_cast<const vg::NavState *>(in),
                  reinterpret_cast<vg::NavState *>(out), step, status, nullptr, n};
