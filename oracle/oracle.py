@@ -48,6 +48,11 @@ def load():
             "oracle_nav_approach": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 8 + [ctypes.c_int]),
             "oracle_nav_transport": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 7 +
                                      [ctypes.c_int, _vp, _vp, _vp, _vp, ctypes.c_int]),
+            "oracle_nav_step_simple": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 10 + [ctypes.c_int]),
+            "oracle_nav_locate_simple": (ctypes.c_double, [_vp, ctypes.c_size_t, _vp, _vp, _vp, _vp, ctypes.c_int]),
+            "oracle_nav_crosscheck": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 6 +
+                                      [ctypes.c_int, _vp, ctypes.c_int]),
+            "oracle_check_nav_index": (ctypes.c_int, [_vp, _vp, ctypes.c_size_t, _vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -109,6 +114,10 @@ class OracleGeometry:
     def add_boolean_subtraction(self, left_pv, right_pv):
         return self._shape(8, [left_pv, right_pv])
 
+    def add_boolean_union(self, left_pv, right_pv):
+        """Union of two placed volumes (oracle only: the product has no union)."""
+        return self._shape(10, [left_pv, right_pv])
+
     def add_trap(self, dz, theta, phi, dy1, dx1, dx2, alpha1, dy2, dx3, dx4, alpha2):
         return self._shape(9, [dz, theta, phi, dy1, dx1, dx2, alpha1, dy2, dx3, dx4, alpha2])
 
@@ -147,7 +156,8 @@ class OracleGeometry:
 
     # ------------------------------------------------------------ queries (numpy, CPU)
     def query(self, pv, q, x, y, z, dx=None, dy=None, dz=None, step_max=np.finfo(np.float64).max, nthreads=1):
-        """q: 0 Inside, 1 Contains, 2 DistanceToIn, 3 DistanceToOut, 4 SafetyToIn, 5 SafetyToOut."""
+        """q: 0 Inside, 1 Contains, 2 DistanceToIn, 3 DistanceToOut, 4 SafetyToIn, 5 SafetyToOut,
+        6 PlacedDistanceToOut (DistanceToOut of a point and direction in the mother's frame)."""
         n = len(x)
         outd = np.empty(n, np.float64)
         outi = np.empty(n, np.int32)
@@ -186,21 +196,52 @@ class OracleGeometry:
         _lib.oracle_bvh_arrays(self._h, lv, _p(prim), _p(off), _p(nch), _p(nodes), _p(boxes))
         return dict(depth=dep.value, prim=prim, offset=off, nchild=nch, nodes=nodes, boxes=boxes)
 
-    def locate(self, x, y, z, nthreads=1):
+    def locate(self, x, y, z, nthreads=1, navigator="bvh"):
+        """GlobalLocator::LocateGlobalPoint from the world with BVHLevelLocator, or with
+        navigator="simple" the brute-force SimpleLevelLocator."""
         out = np.zeros(len(x), NAVSTATE_DTYPE)
-        t = _lib.oracle_nav_locate(self._h, len(x), _p(x), _p(y), _p(z), _p(out), nthreads)
+        fn = _lib.oracle_nav_locate_simple if navigator == "simple" else _lib.oracle_nav_locate
+        t = fn(self._h, len(x), _p(x), _p(y), _p(z), _p(out), nthreads)
         return out, t
 
-    def step(self, x, y, z, dx, dy, dz, states, step_limit=None, nthreads=1, count_nodes=False):
+    def step(self, x, y, z, dx, dy, dz, states, step_limit=None, nthreads=1, count_nodes=False, navigator="bvh"):
+        """One ComputeStepAndPropagatedState per track with BVHNavigator, or with
+        navigator="simple" the brute-force NewSimpleNavigator (+ SimpleLevelLocator)."""
         n = len(x)
         if step_limit is None:
             step_limit = np.full(n, np.finfo(np.float64).max)
         out = np.zeros(n, NAVSTATE_DTYPE)
         step = np.zeros(n)
+        if navigator == "simple":
+            t = _lib.oracle_nav_step_simple(self._h, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(step_limit),
+                                            _p(states), _p(out), _p(step), nthreads)
+            return out, step, None, t
         nv = np.zeros(n, np.int32) if count_nodes else None
         t = _lib.oracle_nav_step(self._h, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(step_limit),
                                  _p(states), _p(out), _p(step), _p(nv), nthreads)
         return out, step, nv, t
+
+    def crosscheck(self, x, y, z, dx, dy, dz, max_steps=1000, nthreads=1):
+        """The reference's TestVGDMLNavigation loop: every track stepped to the world's edge by
+        the BVH navigator, each step compared with the brute-force navigator's from the same
+        state. Returns counts: steps, not_nearly_equal, bit_different, state_different,
+        start_state_different."""
+        c = np.zeros(5, np.int64)
+        _lib.oracle_nav_crosscheck(self._h, len(x), _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), max_steps, _p(c),
+                                   nthreads)
+        return dict(zip(("steps", "not_nearly_equal", "bit_different", "state_different",
+                         "start_state_different"), (int(v) for v in c)))
+
+    def check_nav_index(self, table=None):
+        """test/benchmark/TestNavIndex.cpp's checks of a NavIndex table (this geometry's own
+        when `table` is None) over every placed-volume path: (error code, paths visited)."""
+        paths = np.zeros(1, np.int64)
+        if table is None:
+            err = _lib.oracle_check_nav_index(self._h, None, 0, _p(paths))
+        else:
+            tab = np.ascontiguousarray(table, dtype=np.uint32)
+            err = _lib.oracle_check_nav_index(self._h, _p(tab), tab.size, _p(paths))
+        return int(err), int(paths[0])
 
     def step_safety(self, x, y, z, dx, dy, dz, states, step_limit=None, nthreads=1):
         n = len(x)

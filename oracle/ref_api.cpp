@@ -6,7 +6,10 @@
 // track range into contiguous chunks over std::thread workers.
 #include "ref_nav.h"
 #include "ref_shapes_more.h"
+#include <atomic>
+#include <cfloat>
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <thread>
 #include <vector>
@@ -40,7 +43,7 @@ void *oracle_geom_create() { return new Geometry(); }
 void oracle_geom_destroy(void *g) { delete static_cast<Geometry *>(g); }
 
 // type: 1 Box, 2 Tube, 3 Cone, 4 Polycone, 5 Polyhedron, 6 Torus2, 7 Trd, 8 BooleanSubtraction,
-// 9 Trapezoid (11 parameters, 24 = eight corners x, y, z, or 17 = dz and four planes a, b, c, d)
+// 10 BooleanUnion (oracle only), 9 Trapezoid (11 parameters, 24 = eight corners x, y, z, or 17 = dz and four planes a, b, c, d)
 int oracle_add_shape(void *gp, int type, const double *p, int np)
 {
   Geometry *g = static_cast<Geometry *>(gp);
@@ -62,6 +65,7 @@ int oracle_add_shape(void *gp, int type, const double *p, int np)
   case 6: s = new Torus2(p[0], p[1], p[2], p[3], p[4]); break;
   case 7: s = new Trd(p[0], p[1], p[2], p[3], p[4]); break;
   case 8: s = new BooleanMinus(g->pvs.at((int)p[0]).get(), g->pvs.at((int)p[1]).get()); break;
+  case 10: s = new BooleanUnion(g->pvs.at((int)p[0]).get(), g->pvs.at((int)p[1]).get()); break;
   case 9:
     if (np == 24) {
       Vec3 c[8];
@@ -125,6 +129,7 @@ double oracle_placed_query(void *gp, int pv, int q, size_t n, const double *x, c
       case 3: outd[i] = v->DistanceToOut(p, Vec3(dx[i], dy[i], dz[i]), step_max); break;
       case 4: outd[i] = v->SafetyToIn(p); break;
       case 5: outd[i] = v->SafetyToOut(p); break;
+      case 6: outd[i] = v->PlacedDistanceToOut(p, Vec3(dx[i], dy[i], dz[i]), step_max); break;
       }
     }
   });
@@ -276,6 +281,98 @@ double oracle_nav_transport(void *gp, size_t n, const double *x, const double *y
       final_state[i] = s;
     }
   });
+}
+
+// The brute-force second navigator (NewSimpleNavigator + SimpleLevelLocator): one step per
+// track, as oracle_nav_step, and LocateGlobalPoint from the world.
+double oracle_nav_step_simple(void *gp, size_t n, const double *x, const double *y, const double *z,
+                              const double *dx, const double *dy, const double *dz, const double *step_limit,
+                              const NavState *in, NavState *out, double *step, int nthreads)
+{
+  Geometry *g = static_cast<Geometry *>(gp);
+  return ParallelFor(n, nthreads, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i) {
+      if (in[i].navInd == 0) {
+        out[i]  = in[i];
+        step[i] = 0.;
+        continue;
+      }
+      step[i] = g->ComputeStepAndPropagatedState(Vec3(x[i], y[i], z[i]), Vec3(dx[i], dy[i], dz[i]), step_limit[i],
+                                                 in[i], out[i], nullptr, true);
+    }
+  });
+}
+
+double oracle_nav_locate_simple(void *gp, size_t n, const double *x, const double *y, const double *z, NavState *out,
+                                int nthreads)
+{
+  Geometry *g = static_cast<Geometry *>(gp);
+  return ParallelFor(n, nthreads, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i) {
+      NavState s;
+      g->LocateGlobalPoint(g->world, Vec3(x[i], y[i], z[i]), s, true, true);
+      out[i] = s;
+    }
+  });
+}
+
+// persistency/gdml/test/TestVGDMLNavigation/TestVGDMLNavigation.cpp:38-49 nearly_equal
+static bool NearlyEqual(double x, double y)
+{
+  if (x == y) return true;
+  if (x * y == 0.0) return std::abs(x - y) < DBL_EPSILON * DBL_EPSILON;
+  return std::abs(x - y) < (std::abs(x) + std::abs(y)) * DBL_EPSILON;
+}
+
+// TestVGDMLNavigation.cpp:54-91 navigate(): each track is located from its start point, then
+// stepped until it leaves the world (or max_steps) with the BVH navigator, and at every step
+// the brute-force navigator (NewSimpleNavigator, the reference's own reference) steps the
+// same state; the point moves by max(step, kTolerance) along the direction. counts[0] steps
+// compared, [1] steps not nearly equal (the reference test's criterion), [2] steps that
+// differ in any bit, [3] out-states that differ in any field, [4] start states that the
+// two locators place differently.
+double oracle_nav_crosscheck(void *gp, size_t n, const double *x, const double *y, const double *z,
+                             const double *dx, const double *dy, const double *dz, int max_steps, long *counts,
+                             int nthreads)
+{
+  Geometry *g = static_cast<Geometry *>(gp);
+  std::vector<long> part((size_t)std::max(1, nthreads) * 5, 0);
+  std::atomic<int> slot{0};
+  const double t = ParallelFor(n, nthreads, [&](size_t b, size_t e) {
+    long *c = &part[(size_t)(slot++) * 5];
+    for (size_t i = b; i < e; ++i) {
+      Vec3 p(x[i], y[i], z[i]);
+      const Vec3 d(dx[i], dy[i], dz[i]);
+      NavState cur, cs;
+      g->LocateGlobalPoint(g->world, p, cur, true);
+      g->LocateGlobalPoint(g->world, p, cs, true, true);
+      if (cur.navInd != cs.navInd) ++c[4];
+      for (int k = 0; k < max_steps && cur.navInd != 0; ++k) {
+        NavState nb, ns;
+        const double ref  = g->ComputeStepAndPropagatedState(p, d, kInfLength, cur, ns, nullptr, true);
+        const double step = g->ComputeStepAndPropagatedState(p, d, kInfLength, cur, nb);
+        ++c[0];
+        if (!NearlyEqual(step, ref)) ++c[1];
+        if (std::memcmp(&step, &ref, sizeof(double)) != 0) ++c[2];
+        if (nb.navInd != ns.navInd || nb.lastExited != ns.lastExited || nb.onBoundary != ns.onBoundary) ++c[3];
+        p   = p + std::max(step, kTolerance) * d;
+        cur = nb;
+      }
+    }
+  });
+  for (int k = 0; k < 5; ++k) {
+    counts[k] = 0;
+    for (size_t s2 = 0; s2 < part.size() / 5; ++s2) counts[k] += part[s2 * 5 + k];
+  }
+  return t;
+}
+
+// test/benchmark/TestNavIndex.cpp on a NavIndex table (this geometry's own when tab is null)
+int oracle_check_nav_index(void *gp, const uint32_t *tab, size_t words, long *paths)
+{
+  Geometry *g = static_cast<Geometry *>(gp);
+  if (!tab) return g->CheckNavIndexTable(g->table, g->tableWords, paths);
+  return g->CheckNavIndexTable(tab, words, paths);
 }
 
 } // extern "C"

@@ -154,6 +154,20 @@ struct Transformation3D {
     m[2] += l[2] * r[8];
     return m;
   }
+  Vec3 InverseTransformDirection(Vec3 const &l) const
+  {
+    Vec3 m;
+    m[0] = l[0] * r[0];
+    m[0] += l[1] * r[1];
+    m[0] += l[2] * r[2];
+    m[1] = l[0] * r[3];
+    m[1] += l[1] * r[4];
+    m[1] += l[2] * r[5];
+    m[2] = l[0] * r[6];
+    m[2] += l[1] * r[7];
+    m[2] += l[2] * r[8];
+    return m;
+  }
   void MultiplyFromRight(Transformation3D const &rhs)
   {
     if (rhs.identity) return;

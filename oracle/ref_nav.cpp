@@ -487,9 +487,24 @@ void Geometry::Close()
 }
 
 // ---------------------------------------------------------------- GlobalLocator
+bool Geometry::LevelLocate(LogicalVolume const *lv, PlacedVolume const *excl, Vec3 const &lp,
+                           PlacedVolume const *&pvol, Vec3 &dlp, bool simple) const
+{
+  if (!simple) return lv->bvh->LevelLocate(excl, lp, pvol, dlp);
+  // SimpleLevelLocator.h:122-140 LevelLocateKernel<ExclV, false> with CheckCandidateVol (:20-45)
+  for (PlacedVolume const *d : lv->daughters) {
+    if (d == excl) continue;
+    if (d->Contains(lp, dlp)) {
+      pvol = d;
+      return true;
+    }
+  }
+  return false;
+}
+
 // GlobalLocator.h:35-82 LocateGlobalPoint (BVHLevelLocator::LevelLocate -> BVH::LevelLocate)
-PlacedVolume const *Geometry::LocateGlobalPoint(PlacedVolume const *vol, Vec3 const &point, NavState &s,
-                                                bool top) const
+PlacedVolume const *Geometry::LocateGlobalPoint(PlacedVolume const *vol, Vec3 const &point, NavState &s, bool top,
+                                                bool simple) const
 {
   PlacedVolume const *cand = vol;
   Vec3 cur                 = point;
@@ -501,7 +516,7 @@ PlacedVolume const *Geometry::LocateGlobalPoint(PlacedVolume const *vol, Vec3 co
     while (!lv->daughters.empty() && godeeper) {
       Vec3 tp;
       PlacedVolume const *pv = nullptr;
-      godeeper               = lv->bvh->LevelLocate(nullptr, cur, pv, tp);
+      godeeper               = LevelLocate(lv, nullptr, cur, pv, tp, simple);
       if (godeeper) {
         s.navInd = Push(s.navInd, pv);
         cand     = Top(s.navInd);
@@ -515,7 +530,7 @@ PlacedVolume const *Geometry::LocateGlobalPoint(PlacedVolume const *vol, Vec3 co
 
 // GlobalLocator.h:88-135 LocateGlobalPointExclVolume (top = false)
 PlacedVolume const *Geometry::LocateGlobalPointExclVolume(PlacedVolume const *vol, PlacedVolume const *excl,
-                                                          Vec3 const &point, NavState &s) const
+                                                          Vec3 const &point, NavState &s, bool simple) const
 {
   PlacedVolume const *cand = vol;
   Vec3 cur                 = point;
@@ -526,7 +541,7 @@ PlacedVolume const *Geometry::LocateGlobalPointExclVolume(PlacedVolume const *vo
     while (!lv->daughters.empty() && godeeper) {
       godeeper = false;
       Vec3 tp;
-      godeeper = lv->bvh->LevelLocate(excl, cur, cand, tp);
+      godeeper = LevelLocate(lv, excl, cur, cand, tp, simple);
       if (godeeper) {
         lv       = cand->lv;
         cur      = tp;
@@ -538,7 +553,7 @@ PlacedVolume const *Geometry::LocateGlobalPointExclVolume(PlacedVolume const *vo
 }
 
 // GlobalLocator.h:171-200 RelocatePointFromPathForceDifferent
-PlacedVolume const *Geometry::RelocatePointFromPathForceDifferent(Vec3 const &lp, NavState &s) const
+PlacedVolume const *Geometry::RelocatePointFromPathForceDifferent(Vec3 const &lp, NavState &s, bool simple) const
 {
   PlacedVolume const *currentmother = Top(s.navInd);
   PlacedVolume const *entryvol      = currentmother;
@@ -555,7 +570,7 @@ PlacedVolume const *Geometry::RelocatePointFromPathForceDifferent(Vec3 const &lp
     }
     if (currentmother) {
       s.navInd = Pop(s.navInd);
-      return LocateGlobalPointExclVolume(currentmother, entryvol, tmp, s);
+      return LocateGlobalPointExclVolume(currentmother, entryvol, tmp, s, simple);
     }
   }
   return currentmother;
@@ -563,7 +578,7 @@ PlacedVolume const *Geometry::RelocatePointFromPathForceDifferent(Vec3 const &lp
 
 // ---------------------------------------------------------------- navigation step
 double Geometry::ComputeStepAndPropagatedState(Vec3 const &gp, Vec3 const &gd, double stepLimit, NavState const &in,
-                                               NavState &out, int *nvisited) const
+                                               NavState &out, int *nvisited, bool simple) const
 {
   // DoGlobalToLocalTransformation (VNavigator.h:258-270)
   Transformation3D m;
@@ -581,7 +596,18 @@ double Geometry::ComputeStepAndPropagatedState(Vec3 const &gp, Vec3 const &gd, d
   // daughters have no BVH and no daughter to hit.
   if (!lv->daughters.empty()) {
     PlacedVolume const *last = Top(in.lastExited);
-    lv->bvh->CheckDaughterIntersections(lp, ld, step, last, hit, nvisited);
+    if (!simple) {
+      lv->bvh->CheckDaughterIntersections(lp, ld, step, last, hit, nvisited);
+    } else {
+      // NewSimpleNavigator::CheckDaughterIntersections (NewSimpleNavigator.h:33-63, without
+      // CHECKCONTAINS): DistanceToIn of every daughter in order with the running step
+      for (PlacedVolume const *d : lv->daughters) {
+        const double dd  = d->DistanceToIn(lp, ld, step);
+        const bool valid = (dd < step && !std::isinf(dd)) && !((dd <= 0.) && last == d);
+        hit              = valid ? d : hit;
+        step             = valid ? dd : step;
+      }
+    }
   }
   // PrepareOutState (VNavigator.h:192-235)
   out = in;
@@ -605,11 +631,11 @@ double Geometry::ComputeStepAndPropagatedState(Vec3 const &gp, Vec3 const &gd, d
   const double extra = 1E-6;
   const Vec3 after   = lp + (step + extra) * ld;
   if (Top(out.navInd) == Top(in.navInd)) {
-    RelocatePointFromPathForceDifferent(after, out);
+    RelocatePointFromPathForceDifferent(after, out, simple);
   } else {
     PlacedVolume const *next = Top(out.navInd);
     out.navInd               = Pop(out.navInd);
-    LocateGlobalPoint(next, next->T.Transform(after), out, false);
+    LocateGlobalPoint(next, next->T.Transform(after), out, false, simple);
   }
   while (Top(out.navInd) != nullptr && Top(out.navInd)->IsAssembly()) out.navInd = Pop(out.navInd);
   return step;
@@ -626,6 +652,61 @@ double Geometry::ComputeStepAndSafetyAndPropagatedState(Vec3 const &gp, Vec3 con
   safety                   = pvol->SafetyToOut(lp);
   if (safety > 0.0 && !pvol->lv->daughters.empty()) safety = pvol->lv->bvh->ComputeSafety(lp, safety);
   return ComputeStepAndPropagatedState(gp, gd, stepLimit, in, out);
+}
+
+// test/benchmark/TestNavIndex.cpp:30-127: walk every placed-volume path from the world,
+// passing the index made by PushImpl from the mother's index, and check at each node the
+// index recomputed from the path, the top volume, the level, Pop/Push consistency, the
+// daughter count and the cached global matrix (NavStateIndex::TopMatrixImpl) against the
+// product of the path's transformations (NavStatePath::TopMatrix, NavStatePath.h:616-628).
+// The accessors read `tab` through this geometry's own helpers, so the table pointer is
+// swapped in for the duration of the walk (single-threaded test use only).
+int Geometry::CheckNavIndexTable(const uint32_t *tab, size_t words, long *paths) const
+{
+  Geometry *self       = const_cast<Geometry *>(this);
+  uint32_t *saved      = self->table;
+  const size_t savedWr = self->tableWords;
+  self->table          = const_cast<uint32_t *>(tab);
+  self->tableWords     = words;
+  std::vector<PlacedVolume const *> path;
+  long visited = 0;
+  std::function<int(PlacedVolume const *, uint32_t)> visit = [&](PlacedVolume const *pv, uint32_t nav) -> int {
+    if (nav == 0 || nav >= words) return 2;
+    path.push_back(pv);
+    ++visited;
+    // GlobalToLocalVisitor::apply (TestNavIndex.cpp:36-96)
+    const int level  = (int)path.size() - 1;
+    uint32_t ind     = 1;
+    PlacedVolume const *pd = nullptr;
+    for (int i = 1; i < level + 1; ++i) {
+      pd = path[i];
+      if (pd->childId < 0) return 1;
+      ind = Push(ind, pd);
+    }
+    if (ind != nav) return 2;
+    if (Top(ind) != pv) return 3;
+    if (level != (int)Level(ind)) return 4;
+    if (level > 0 && ind != Push(Pop(ind), pd)) return 5;
+    if (NDaughters(ind) != pv->lv->daughters.size()) return 6;
+    Transformation3D byPath, byIndex;
+    for (int i = 1; i < level + 1; ++i) byPath.MultiplyFromRight(path[i]->T);
+    TopMatrix(ind, byIndex);
+    for (int k = 0; k < 3; ++k)
+      if (!(byPath.t[k] == byIndex.t[k])) return 7;
+    for (int k = 0; k < 9; ++k)
+      if (!(byPath.r[k] == byIndex.r[k])) return 7;
+    for (PlacedVolume const *d : pv->lv->daughters) {
+      const int e = visit(d, Push(nav, d));
+      if (e) return e;
+    }
+    path.pop_back();
+    return 0;
+  };
+  const int err    = world ? visit(world, 1) : 0;
+  self->table      = saved;
+  self->tableWords = savedWr;
+  if (paths) *paths = visited;
+  return err;
 }
 
 } // namespace oracle

@@ -136,16 +136,34 @@ struct Geometry {
   unsigned short NDaughters(uint32_t n) const;
   void TopMatrix(uint32_t n, Transformation3D &trans) const;
 
-  // GlobalLocator (VecGeom/navigation/GlobalLocator.h:35-200) with BVHLevelLocator on every
-  // logical volume that has daughters.
-  PlacedVolume const *LocateGlobalPoint(PlacedVolume const *vol, Vec3 const &p, NavState &s, bool top) const;
-  PlacedVolume const *LocateGlobalPointExclVolume(PlacedVolume const *vol, PlacedVolume const *excl, Vec3 const &p,
-                                                  NavState &s) const;
-  PlacedVolume const *RelocatePointFromPathForceDifferent(Vec3 const &lp, NavState &s) const;
+  // Level locators. BVHLevelLocator (VecGeom/navigation/BVHLevelLocator.h:44-96 ->
+  // BVH::LevelLocate) normally; with `simple`, SimpleLevelLocator
+  // (VecGeom/navigation/SimpleLevelLocator.h:122-140): every daughter in order, the first
+  // one that contains the point. The simple forms are the brute-force second navigator the
+  // reference validates its BVH navigator against.
+  bool LevelLocate(LogicalVolume const *lv, PlacedVolume const *excl, Vec3 const &lp, PlacedVolume const *&pvol,
+                   Vec3 &dlp, bool simple) const;
 
-  // VNavigatorHelper<BVHNavigator<false>>::ComputeStepAndPropagatedState (VNavigator.h:436-492)
+  // GlobalLocator (VecGeom/navigation/GlobalLocator.h:35-200) with BVHLevelLocator (or, with
+  // `simple`, SimpleLevelLocator) on every logical volume that has daughters.
+  PlacedVolume const *LocateGlobalPoint(PlacedVolume const *vol, Vec3 const &p, NavState &s, bool top,
+                                        bool simple = false) const;
+  PlacedVolume const *LocateGlobalPointExclVolume(PlacedVolume const *vol, PlacedVolume const *excl, Vec3 const &p,
+                                                  NavState &s, bool simple = false) const;
+  PlacedVolume const *RelocatePointFromPathForceDifferent(Vec3 const &lp, NavState &s, bool simple = false) const;
+
+  // VNavigatorHelper<BVHNavigator<false>>::ComputeStepAndPropagatedState (VNavigator.h:436-492);
+  // with `simple`, VNavigatorHelper<NewSimpleNavigator<false>> (NewSimpleNavigator.h:33-63:
+  // DistanceToIn of every daughter in order) relocating with SimpleLevelLocator.
   double ComputeStepAndPropagatedState(Vec3 const &gp, Vec3 const &gd, double stepLimit, NavState const &in,
-                                       NavState &out, int *nvisited = nullptr) const;
+                                       NavState &out, int *nvisited = nullptr, bool simple = false) const;
+
+  // test/benchmark/TestNavIndex.cpp:30-96 GlobalToLocalVisitor over every placed-volume path
+  // (visitAllPlacedVolumesPassNavIndex, :101-127), applied to `tab` (this geometry's own
+  // NavIndex table, or a table built elsewhere for the same geometry). Returns the
+  // reference's error code: 0 pass, 1 bad child id, 2 index mismatch, 3 top volume, 4 level,
+  // 5 push/pop, 6 daughter count, 7 cached global matrix; *paths receives the paths visited.
+  int CheckNavIndexTable(const uint32_t *tab, size_t words, long *paths) const;
   // BVH::ApproachNextDaughter (source/BVH.cpp:394-449) in the frame of the state's volume,
   // `last` = the state's last-exited volume, as CheckDaughterIntersections gets it
   double ApproachNextDaughter(Vec3 const &gp, Vec3 const &gd, double step, NavState const &in) const;

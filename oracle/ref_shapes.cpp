@@ -1,6 +1,8 @@
 // ORACLE — TEST INFRASTRUCTURE ONLY (see ref_base.h).
 // Scalar restatement of Wedge, Box, Tube and Cone. Citations are to the reference's files.
 #include "ref_shapes.h"
+#include <cstdio>
+#include <cstdlib>
 #include <cmath>
 
 namespace oracle {
@@ -64,6 +66,29 @@ int Box::Inside(Vec3 const &p) const
   return in;
 }
 bool Box::Contains(Vec3 const &p) const { return (p.Abs() - dim).Max() < 0.; }
+
+Vec3 UnplacedShape::Normal(Vec3 const &, bool &) const
+{
+  std::fprintf(stderr, "oracle: Normal() is not restated for this shape\n");
+  std::abort();
+}
+
+// BoxImplementation.h:172-192 NormalKernel: the faces within kHalfTolerance of the nearest
+// one contribute their axis, averaged on edges and corners
+Vec3 Box::Normal(Vec3 const &p, bool &valid) const
+{
+  const Vec3 safety = (p.Abs() - dim).Abs();
+  const double safmin = safety.Min();
+  valid               = safmin < kHalfTolerance;
+  Vec3 normal(0., 0., 0.);
+  for (int k = 0; k < 3; ++k)
+    if (safety[k] - safmin < kHalfTolerance) normal[k] = Sign(p[k]);
+  if (normal.Mag2() > 1.0) {
+    const double m = normal.Mag();
+    normal         = Vec3(normal[0] / m, normal[1] / m, normal[2] / m);
+  }
+  return normal;
+}
 
 // BoxImplementation.h:109-131
 double Box::DistanceToIn(Vec3 const &p, Vec3 const &d, double) const

@@ -20,6 +20,9 @@ struct UnplacedShape {
   virtual double SafetyToOut(Vec3 const &p) const                             = 0;
   virtual void Extent(Vec3 &lo, Vec3 &hi) const                               = 0;
   virtual bool IsAssembly() const { return false; }
+  // Surface normal (VUnplacedVolume::Normal). Restated only where an oracle query needs it
+  // (the Box, for the boolean union's Inside); reaching the default is a test-setup error.
+  virtual Vec3 Normal(Vec3 const &p, bool &valid) const;
 };
 
 // ---------------------------------------------------------------- Wedge
@@ -47,6 +50,7 @@ struct Wedge {
 struct Box : UnplacedShape {
   Vec3 dim;
   Box(double dx, double dy, double dz) : dim(dx, dy, dz) {}
+  Vec3 Normal(Vec3 const &p, bool &valid) const override;
   int Inside(Vec3 const &p) const override;
   bool Contains(Vec3 const &p) const override;
   double DistanceToIn(Vec3 const &p, Vec3 const &d, double) const override;

@@ -783,7 +783,127 @@ double BooleanMinus::SafetyToOut(Vec3 const &p) const
   return Min(sl, sr);
 }
 
-// source/UnplacedBooleanVolume.cpp:403-458 TransformedExtent of the left operand
+// source/UnplacedBooleanVolume.cpp:403-441 TransformedExtent: the operand's extent box
+// corners brought into the boolean's frame
+static void TransformedExtent(PlacedVolume const *pv, Vec3 &aMin, Vec3 &aMax)
+{
+  Vec3 lower, upper;
+  pv->Shape()->Extent(lower, upper);
+  const Vec3 delta = upper - lower;
+  double mn[3] = {kInfLength, kInfLength, kInfLength}, mx[3] = {-kInfLength, -kInfLength, -kInfLength};
+  for (int x = 0; x <= 1; ++x)
+    for (int y = 0; y <= 1; ++y)
+      for (int z = 0; z <= 1; ++z) {
+        Vec3 c(lower.x() + x * delta.x(), lower.y() + y * delta.y(), lower.z() + z * delta.z());
+        const Vec3 t = pv->T.InverseTransform(c);
+        for (int k = 0; k < 3; ++k) {
+          mn[k] = std::min(mn[k], t[k]);
+          mx[k] = std::max(mx[k], t[k]);
+        }
+      }
+  aMin = Vec3(mn[0], mn[1], mn[2]);
+  aMax = Vec3(mx[0], mx[1], mx[2]);
+}
+
+// ====================================================================== Boolean union
+// BooleanUnionImplementation.h:62-69 Contains
+bool BooleanUnion::Contains(Vec3 const &p) const
+{
+  if (fLeft->Contains(p)) return true;
+  return fRight->Contains(p);
+}
+
+// BooleanUnionImplementation.h:71-118 Inside (touching solids on both surfaces count as
+// inside when their outward normals oppose)
+int BooleanUnion::Inside(Vec3 const &p) const
+{
+  const int a = fLeft->Inside(p);
+  if (a == kInside) return kInside;
+  const int b = fRight->Inside(p);
+  if (b == kInside) return kInside;
+  if (a == kSurface && b == kSurface) {
+    bool va = false, vb = false;
+    const Vec3 na = fLeft->T.InverseTransformDirection(fLeft->Shape()->Normal(fLeft->T.Transform(p), va));
+    const Vec3 nb = fRight->T.InverseTransformDirection(fRight->Shape()->Normal(fRight->T.Transform(p), vb));
+    return na.Dot(nb) < 0 ? kInside : kSurface;
+  }
+  return (a == kSurface || b == kSurface) ? kSurface : kOutside;
+}
+
+// BooleanUnionImplementation.h:120-128 DistanceToIn
+double BooleanUnion::DistanceToIn(Vec3 const &p, Vec3 const &d, double stepMax) const
+{
+  const double d1 = fLeft->DistanceToIn(p, d, stepMax);
+  const double d2 = fRight->DistanceToIn(p, d, stepMax);
+  return Min(d1, d2);
+}
+
+// BooleanUnionImplementation.h:130-178 DistanceToOut: leave the operand the point is in,
+// push by kPushTolerance, continue through the other operand while it connects
+double BooleanUnion::DistanceToOut(Vec3 const &point, Vec3 const &dir, double) const
+{
+  double dist           = 0.;
+  const double pushdist = kPushTolerance;
+  const int positionA   = fLeft->Inside(point);
+  Vec3 nextp            = point;
+  bool connecting       = false;
+  auto kernel = [&](PlacedVolume const *A, PlacedVolume const *B) {
+    do {
+      connecting       = false;
+      const double d1  = A->PlacedDistanceToOut(nextp, dir, kInfLength);
+      dist += (d1 >= 0. && d1 < kInfLength) ? d1 : 0;
+      dist += pushdist;
+      nextp = point + dist * dir;
+      if (B->Inside(nextp) != kOutside) {
+        const double d2 = B->PlacedDistanceToOut(nextp, dir, kInfLength);
+        dist += (d2 >= 0. && d2 < kInfLength) ? d2 : 0;
+        dist += pushdist;
+        nextp      = point + dist * dir;
+        connecting = true;
+      }
+    } while (connecting && (A->Inside(nextp) != kOutside));
+  };
+  if (positionA != kOutside)
+    kernel(fLeft, fRight);
+  else
+    kernel(fRight, fLeft);
+  double distance = dist - pushdist;
+  if (distance < kTolerance && positionA == kOutside && fRight->Inside(point) == kOutside) distance = -kTolerance;
+  return distance;
+}
+
+// BooleanUnionImplementation.h:180-191 SafetyToIn
+double BooleanUnion::SafetyToIn(Vec3 const &p) const
+{
+  const double a = fLeft->SafetyToIn(p);
+  const double b = fRight->SafetyToIn(p);
+  return Min(a, b);
+}
+
+// BooleanUnionImplementation.h:193-218 SafetyToOut
+double BooleanUnion::SafetyToOut(Vec3 const &p) const
+{
+  const int ia = fLeft->Inside(p);
+  const int ib = fRight->Inside(p);
+  if (ia == kOutside && ib == kOutside) return -kTolerance;
+  if (ia != kOutside && ib != kOutside)
+    return Max(fLeft->SafetyToOut(p), fRight->SafetyToOut(fRight->T.Transform(p)));
+  if (ia == kSurface || ib == kSurface) return -kTolerance;
+  if (ia == kOutside) return fRight->SafetyToOut(fRight->T.Transform(p));
+  return fLeft->SafetyToOut(p);
+}
+
+// source/UnplacedBooleanVolume.cpp:461-476 Extent of the union: both operands' boxes
+void BooleanUnion::Extent(Vec3 &aMin, Vec3 &aMax) const
+{
+  Vec3 l0, l1, r0, r1;
+  TransformedExtent(fLeft, l0, l1);
+  TransformedExtent(fRight, r0, r1);
+  aMin = Vec3(Min(l0.x(), r0.x()), Min(l0.y(), r0.y()), Min(l0.z(), r0.z()));
+  aMax = Vec3(Max(l1.x(), r1.x()), Max(l1.y(), r1.y()), Max(l1.z(), r1.z()));
+}
+
+// source/UnplacedBooleanVolume.cpp:443-458 TransformedExtent of the left operand
 void BooleanMinus::Extent(Vec3 &aMin, Vec3 &aMax) const
 {
   Vec3 lower, upper;

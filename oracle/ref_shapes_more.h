@@ -89,6 +89,21 @@ struct BooleanMinus : UnplacedShape {
   void Extent(Vec3 &lo, Vec3 &hi) const override;
 };
 
+// VecGeom/volumes/kernel/BooleanUnionImplementation.h (kUnion); operands are placed volumes.
+// Test infrastructure beyond the product's shapes: the reference's boolean unit test
+// subtracts a union, so the oracle restates the union to check its subtraction there.
+struct BooleanUnion : UnplacedShape {
+  PlacedVolume const *fLeft, *fRight;
+  BooleanUnion(PlacedVolume const *l, PlacedVolume const *r) : fLeft(l), fRight(r) {}
+  int Inside(Vec3 const &p) const override;
+  bool Contains(Vec3 const &p) const override;
+  double DistanceToIn(Vec3 const &p, Vec3 const &d, double smax) const override;
+  double DistanceToOut(Vec3 const &p, Vec3 const &d, double smax) const override;
+  double SafetyToIn(Vec3 const &p) const override;
+  double SafetyToOut(Vec3 const &p) const override;
+  void Extent(Vec3 &lo, Vec3 &hi) const override;
+};
+
 } // namespace oracle
 
 namespace oracle {

@@ -623,7 +623,10 @@ class Extractor:
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("VECGEOM_SOURCE_DIR")
+    if not root:
+        sys.exit("usage: extract_unit_vectors.py <VecGeom source tree> [output dir] "
+                 "(or set VECGEOM_SOURCE_DIR)")
     out = sys.argv[2] if len(sys.argv) > 2 else os.path.dirname(os.path.abspath(__file__))
     for shape, (fname, types) in FILES.items():
         path = os.path.join(root, "test", "unit_tests", fname)

@@ -16,7 +16,9 @@ from vecgeom_gb300 import gdml
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 DETECTOR = os.path.join(HERE, "golden", "gdml", "detector.gdml")
-REF_GDMLS = "/root/reference/persistency/gdml/gdmls"
+# the reference's own example GDML files, where a VecGeom source tree is named by
+# VECGEOM_SOURCE_DIR (the tests that read them are skipped otherwise)
+REF_GDMLS = os.path.join(os.environ.get("VECGEOM_SOURCE_DIR", "/nonexistent"), "persistency", "gdml", "gdmls")
 
 
 def compare(path):

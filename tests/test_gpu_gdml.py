@@ -2,7 +2,7 @@
 barrel tube, Trd wedges in polycone endcaps, trapezoids in a polyhedra, a torus, a phi-cut
 cone and a boolean subtraction, with rotations from GDML angles): LocatePoint and the
 transport stream step for step equal to the oracle (FP64: states bit-exact, steps bit-exact
-except at the Torus2, within 1e-8 mm there), and every mixed-precision schedule equal to
+except at the Torus2, within 1e-9 mm + 1e-12 relative there), and every mixed-precision schedule equal to
 FP64."""
 import os
 
@@ -59,11 +59,11 @@ def test_gdml_locate_and_transport_match_oracle(cuda, gdml_det):
     assert np.array_equal(trs[mask], ref_tr[mask])
     # steps bit-exact, except the steps into or out of the Torus2 ring: its cubic solve calls
     # cbrt/pow/cos/atan2, whose CUDA and libm results differ in the last bits, so those
-    # steps are compared at 1e-8 mm (the tolerance stated for Torus2 elsewhere)
+    # steps are compared at 1e-9 mm + 1e-12 relative (the bar of every shape)
     torus_ind = o.locate(np.array([1000.0]), np.array([0.0]), np.array([1500.0]))[0]["nav_ind"][0]
     prev = np.concatenate([ref_st["nav_ind"][:, None], ref_tr[:, :-1]], axis=1)
     differ = mask & (tsl != ref_ts)
-    assert (np.abs(tsl - ref_ts)[differ] <= 1e-8).all()
+    assert (np.abs(tsl - ref_ts)[differ] <= 1e-9 + 1e-12 * np.abs(ref_ts[differ])).all()
     assert ((ref_tr == torus_ind) | (prev == torus_ind))[differ].all()
     assert differ.sum() < 0.01 * mask.sum()
     # tracks cross the modules, wedges, trapezoids and the other daughters

@@ -1,8 +1,8 @@
 """The CUDA shape kernels against the known answers of the reference's own unit tests
 (tests/golden/unit_*.json) and against the oracle on the same points: every hard assert
 passes, soft checks pass except the documented exceptions, and results equal the oracle's
-(Inside exactly; distances and safeties within 1e-9 mm + 1e-12 relative, Torus2 within
-1e-8 mm)."""
+(Inside exactly; distances and safeties within 1e-9 mm + 1e-12 relative, every shape
+including Torus2)."""
 import numpy as np
 import pytest
 
@@ -51,8 +51,6 @@ def test_kernels_match_reference_unit_tests(cuda, name):
                 fails.append((c["line"], shape, q, c["expected"], float(v)))
         if qi in (0, 1):
             bad = got.astype(np.int64) != ref.astype(np.int64)
-        elif spec["type"] == "torus2":
-            bad = ~((got == ref) | (np.abs(got - ref) <= 1e-8))
         else:
             bad = dist_mismatch(got, ref)
         diff += [(shape, q, float(a), float(b)) for a, b in zip(got[bad], ref[bad])]

@@ -127,11 +127,12 @@ def test_placed_transform_parity(cuda):
         assert not dist_mismatch(got[q], ref[q]).any(), q
 
 
-# Stated per-shape tolerance of the FP64 path against the FP64 oracle. Torus2's cubic
-# resolvent calls cbrt/pow/cos/atan2, whose CUDA and libm results differ in the last ulps;
-# the Newton polish then stops within kTolerance (1e-9 mm) of the root, so its distances are
-# compared at 1e-8 mm. Every other shape uses only +,-,*,/ and sqrt and meets 1e-9 + 1e-12 rel.
-CFG2_TOL = {"torus2": 1e-8}
+# Every shape meets 1e-9 mm + 1e-12 relative against the FP64 oracle. Torus2 is the one
+# shape whose results are not all bit-identical: its cubic resolvent calls cbrt/pow/cos/atan2,
+# whose CUDA and libm results differ in the last ulps, and the Newton polish then stops
+# within kTolerance of the root (measured on 2^22 config-2 points: at most 9.6e-10 mm for
+# DistanceToIn and 5.5e-10 mm for DistanceToOut; Inside and the safeties bit-identical).
+CFG2_TOL = {}
 
 
 @pytest.mark.parametrize("name", ["tube_phi", "polycone", "polyhedron", "torus2", "trd", "box_minus_tube"])

@@ -1,6 +1,7 @@
 """The unplaced (shape-frame) SoA queries, vg_shape_*: points and directions go to the shape
 kernels untransformed (VUnplacedVolume), so signed zeros reach the kernels as given. Against
-the oracle's unplaced queries: bit-exact in FP64 (Torus2 distances within 1e-8 mm), and the
+the oracle's unplaced queries: bit-exact in FP64 (Torus2 distances within 1e-9 mm + 1e-12
+relative), and the
 mixed-precision results equal to FP64 (Box safeties excepted: their FP32 form has a stated
 bound)."""
 import numpy as np
@@ -64,7 +65,7 @@ def test_unplaced_queries_match_oracle(cuda, name):
         ref = o.shape_query(so, qi, *pts, *(dirs if qi in (2, 3) else ()))
         got = res[vg.PREC_FP64, qi]
         if kind == "torus2" and qi in (2, 3):
-            bad = ~((got == ref) | (np.abs(got - ref) <= 1e-8))
+            bad = ~((got == ref) | (np.abs(got - ref) <= 1e-9 + 1e-12 * np.abs(ref)))
         else:
             bad = ~((got == ref) | (np.isnan(got) & np.isnan(ref)))
         assert not bad.any(), (name, QUERIES[qi], int(bad.sum()), got[bad][:3], ref[bad][:3])
