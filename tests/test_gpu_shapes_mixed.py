@@ -75,3 +75,52 @@ def test_mixed_placed_transform(cuda):
     b = _run(cuda, g, pv, (x, y, z), dirs, vg.PREC_MIXED)
     for q in QUERIES:
         assert np.array_equal(a[q], b[q]), q
+
+
+# Polyhedra for the FP32-screened distances: the config-2 one, phi cut-outs below and above
+# pi, inner radii on some segments, and a z plane shared by two segments (the same-z case of
+# Quadrilaterals::DistanceToOut).
+POLYHEDRA = [
+    (0.3, 1.8, 5, (-100.0, 0.0, 0.0, 50.0), (0.0, 10.0, 20.0, 5.0), (40.0, 60.0, 50.0, 30.0)),
+    (0.0, 4.5, 3, (-10.0, 10.0), (0.0, 0.0), (20.0, 30.0)),
+    (0.5, 2 * np.pi, 6, (-50.0, -20.0, 30.0, 60.0), (10.0, 0.0, 0.0, 15.0), (40.0, 45.0, 45.0, 20.0)),
+    (0.0, 2 * np.pi, 8, (-300.0, -100.0, -100.0, 200.0, 400.0), (50.0, 60.0, 80.0, 80.0, 0.0),
+     (150.0, 200.0, 250.0, 300.0, 100.0)),
+]
+
+
+@pytest.mark.parametrize("k", range(len(POLYHEDRA)))
+def test_mixed_polyhedron_distances_equal_fp64(cuda, k):
+    """Near-surface, inside and outside points; a third of the rays along the axes or in the
+    xy plane (grazing the side faces, parallel to the z planes), where the FP32 screen must
+    leave every quadrilateral to FP64."""
+    import vecgeom_gb300 as vg
+    from vecgeom_gb300 import workloads as W
+    g = vg.Geometry()
+    s, pv = W.build_single_shape(g, "polyhedron", POLYHEDRA[k])
+    lo, hi = g.shape_extent(s)
+    inside = lambda x, y, z: _run(cuda, g, pv, (x, y, z), (x, y, z), vg.PREC_FP64)["inside"]
+
+    def dout(x, y, z, dx, dy, dz):
+        return _run(cuda, g, pv, (x, y, z), (dx, dy, dz), vg.PREC_FP64)["distance_to_out"]
+
+    pts, dirs = W.shape_points_mixed(lo, hi, 3 * 16384, 321 + k, inside, dout)
+    n = len(pts[0])
+    dirs = [np.array(c) for c in dirs]
+    rng = np.random.default_rng(k)
+    sel = rng.random(n) < 1 / 3
+    axis = rng.integers(0, 8, n)
+    for i in np.flatnonzero(sel):
+        a = axis[i]
+        if a < 6:
+            v = [0.0, 0.0, 0.0]
+            v[a // 2] = 1.0 if a % 2 == 0 else -1.0
+        else:
+            ph = rng.random() * 2 * np.pi
+            v = [np.cos(ph), np.sin(ph), 0.0]
+        for c in range(3):
+            dirs[c][i] = v[c]
+    a = _run(cuda, g, pv, pts, dirs, vg.PREC_FP64)
+    b = _run(cuda, g, pv, pts, dirs, vg.PREC_MIXED)
+    for q in ("distance_to_in", "distance_to_out"):
+        assert np.array_equal(a[q].view(np.int64), b[q].view(np.int64)), (q, int((a[q] != b[q]).sum()))

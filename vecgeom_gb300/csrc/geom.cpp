@@ -574,7 +574,13 @@ bool make_polyhedron(const double *p, int np, HostShape &s, std::string &err)
   const int oZ = take(nz), oRmin = take(nz), oRmax = take(nz), oSameZ = take(nz), oPhiSec = take(3 * (S + 1));
   const int oSeg = take(4 * nseg);
   std::vector<int> qbase(nseg);
-  for (int i = 0; i < nseg; ++i) qbase[i] = take(kPolyQuadDoubles * (nout[i] + nphi[i] + nin[i]));
+  int nquads = 0;
+  for (int i = 0; i < nseg; ++i) {
+    qbase[i] = take(kPolyQuadDoubles * (nout[i] + nphi[i] + nin[i]));
+    nquads += nout[i] + nphi[i] + nin[i];
+  }
+  const int oQ0 = nseg > 0 ? qbase[0] : off; // quadrilaterals are contiguous (a multiple of 4 doubles each)
+  const int oQF = take((nquads * kPolyQuadFloats + 1) / 2);
   std::vector<double> rec(off, 0.);
   PolyhedronRec h{};
   h.nsides = S, h.nseg = nseg, h.nz = nz;
@@ -582,6 +588,7 @@ bool make_polyhedron(const double *p, int np, HostShape &s, std::string &err)
             (largePhiCutout ? kPolyFlagLargePhi : 0);
   h.phiStart = fPhiStart, h.phiDelta = fPhiDelta;
   h.offZ = oZ, h.offRMin = oRmin, h.offRMax = oRmax, h.offSameZ = oSameZ, h.offPhiSec = oPhiSec, h.offSeg = oSeg;
+  h.offQuad0 = oQ0, h.offQuadF = oQF;
   h.w = make_wedge(fPhiDelta, fPhiStart);
   for (int i = 0; i < nz; ++i) {
     rec[oZ + i] = zp[i], rec[oRmin + i] = rmin[i], rec[oRmax + i] = rmax[i];
@@ -655,6 +662,10 @@ bool make_polyhedron(const double *p, int np, HostShape &s, std::string &err)
       if (hdot(hv(q1[0], q1[1], q1[2]), phiSec[S]) < 0) flip_quad(q1);
     }
   }
+  // FP32 copies of the planes of every quadrilateral, in record order
+  float *qf = reinterpret_cast<float *>(rec.data() + oQF);
+  for (int k = 0; k < nquads; ++k)
+    for (int i = 0; i < kPolyQuadFloats; ++i) qf[kPolyQuadFloats * k + i] = (float)rec[oQ0 + kPolyQuadDoubles * k + i];
   std::memcpy(rec.data(), &h, sizeof(h));
   s.type = kShapePolyhedron;
   s.rec  = std::move(rec);

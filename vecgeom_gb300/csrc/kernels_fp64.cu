@@ -5,6 +5,7 @@
 #include "launch.h"
 #include "nav_fp64.cuh"
 #include "shapes_mixed.cuh"
+#include "shapes_polyhedron_mixed.cuh"
 #include <type_traits>
 
 namespace vg {
@@ -220,6 +221,8 @@ __global__ void __launch_bounds__(256) k_shape_query_dyn(const DevGeom g, const 
                                                          size_t n, void *__restrict__ out)
 {
   const mixed::ShapeLB lb = M ? reinterpret_cast<const mixed::ShapeLB *>(g.shape_lbd)[shape] : mixed::ShapeLB{};
+  const bool poly         = g.shape_type[shape] == kShapePolyhedron;
+  const int off           = g.shape_off[shape];
   const size_t stride     = (size_t)gridDim.x * blockDim.x;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     V3 p{__ldg(x + i), __ldg(y + i), __ldg(z + i)};
@@ -234,9 +237,16 @@ __global__ void __launch_bounds__(256) k_shape_query_dyn(const DevGeom g, const 
     if (Q == 2 || Q == 3) {
       V3 d{__ldg(dx + i), __ldg(dy + i), __ldg(dz + i)};
       if (framed) d = f64::rotate(xf, d);
-      static_cast<double *>(out)[i] =
-          (Q == 2) ? ((M && mixed::lb_certain_miss(lb, p, d)) ? kInfLength : f64::shape_dist_in(g, shape, p, d))
-                   : f64::shape_dist_out(g, shape, p, d);
+      double r;
+      if (M && poly) { // FP32-screened quadrilaterals, same FP64 results
+        const PolyhedronRec &rec = f64::rec_at<PolyhedronRec>(g, off);
+        r = (Q == 2) ? (mixed::lb_certain_miss(lb, p, d) ? kInfLength : mixed::polyhedron_dist_in_mixed(rec, p, d))
+                     : mixed::polyhedron_dist_out_mixed(rec, p, d);
+      } else {
+        r = (Q == 2) ? ((M && mixed::lb_certain_miss(lb, p, d)) ? kInfLength : f64::shape_dist_in(g, shape, p, d))
+                     : f64::shape_dist_out(g, shape, p, d);
+      }
+      static_cast<double *>(out)[i] = r;
     }
     if (Q == 4) static_cast<double *>(out)[i] = f64::shape_safety_in(g, shape, p);
     if (Q == 5) static_cast<double *>(out)[i] = f64::shape_safety_out(g, shape, p);

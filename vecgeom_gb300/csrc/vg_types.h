@@ -111,16 +111,20 @@ struct TorusRec {
 // n_inner, first quadrilateral) and the quadrilaterals of all segments (outer, phi, inner
 // in that order), kPolyQuadDoubles each: plane normal + distance, four side planes
 // (normal + distance) and four corners (Quadrilaterals.h:28-37). Offsets in doubles from
-// the record start.
+// the record start. After the quadrilaterals, an FP32 copy of each one's planes (normal +
+// distance, then the four side planes: kPolyQuadFloats floats, rounded to nearest) in the
+// same order, for the mixed-precision screens: quadrilateral k (counted from offQuad0) has
+// its copy at float offset 2 * offQuadF + kPolyQuadFloats * k.
 struct PolyhedronRec {
   double nsides, nseg, nz, flags; // flags: 1 inner radii, 2 phi cutout, 4 phi cutout > pi
   double phiStart, phiDelta, tubeOffset, pad0;
-  double offZ, offRMin, offRMax, offSameZ, offPhiSec, offSeg, pad1, pad2;
+  double offZ, offRMin, offRMax, offSameZ, offPhiSec, offSeg, offQuad0, offQuadF;
   WedgeRec w;
   double pad3[3];
   TubeRec bt;
 };
 constexpr int kPolyQuadDoubles = 32; // n[3] d | (sideN[3] sideD) x 4 | corner[3] x 4
+constexpr int kPolyQuadFloats  = 20; // n[3] d | (sideN[3] sideD) x 4
 constexpr int kPolyFlagInner = 1, kPolyFlagPhi = 2, kPolyFlagLargePhi = 4;
 
 // Boolean subtraction record (VecGeom/volumes/BooleanStruct.h:19-33): operand placed-volume ids.
