@@ -124,3 +124,39 @@ def test_mixed_polyhedron_distances_equal_fp64(cuda, k):
     b = _run(cuda, g, pv, pts, dirs, vg.PREC_MIXED)
     for q in ("distance_to_in", "distance_to_out"):
         assert np.array_equal(a[q].view(np.int64), b[q].view(np.int64)), (q, int((a[q] != b[q]).sum()))
+
+
+POLYCONES = [
+    (0.0, 2 * np.pi, (-500.0, -300.0, -100.0, 0.0, 250.0, 500.0), (50.0, 60.0, 0.0, 0.0, 80.0, 120.0),
+     (150.0, 300.0, 200.0, 400.0, 380.0, 390.0)),
+    (0.4, 2.5, (-40.0, -10.0, 10.0, 40.0), (5.0, 10.0, 10.0, 2.0), (20.0, 30.0, 25.0, 50.0)),
+    (0.0, 2 * np.pi, (-1.0, 0.0, 1.0, 300.0), (0.0, 0.0, 0.0, 0.0), (100.0, 10.0, 300.0, 5.0)),
+]
+
+
+@pytest.mark.parametrize("k", range(len(POLYCONES)))
+def test_mixed_polycone_distances_equal_fp64(cuda, k):
+    """Polycones with hollow, solid, steep and phi-cut sections: the FP32 section screen of
+    DistanceToIn gives the FP64 results bit for bit, also for rays along the axes."""
+    import vecgeom_gb300 as vg
+    from vecgeom_gb300 import workloads as W
+    g = vg.Geometry()
+    s, pv = W.build_single_shape(g, "polycone", POLYCONES[k])
+    lo, hi = g.shape_extent(s)
+    inside = lambda x, y, z: _run(cuda, g, pv, (x, y, z), (x, y, z), vg.PREC_FP64)["inside"]
+
+    def dout(x, y, z, dx, dy, dz):
+        return _run(cuda, g, pv, (x, y, z), (dx, dy, dz), vg.PREC_FP64)["distance_to_out"]
+
+    pts, dirs = W.shape_points_mixed(lo, hi, 3 * 16384, 555 + k, inside, dout)
+    dirs = [np.array(c) for c in dirs]
+    rng = np.random.default_rng(50 + k)
+    sel = np.flatnonzero(rng.random(len(pts[0])) < 0.25)
+    for i in sel:
+        a = rng.integers(0, 6)
+        for c in range(3):
+            dirs[c][i] = (1.0 if a % 2 == 0 else -1.0) if c == a // 2 else 0.0
+    a = _run(cuda, g, pv, pts, dirs, vg.PREC_FP64)
+    b = _run(cuda, g, pv, pts, dirs, vg.PREC_MIXED)
+    for q in ("distance_to_in", "distance_to_out"):
+        assert np.array_equal(a[q].view(np.int64), b[q].view(np.int64)), (q, int((a[q] != b[q]).sum()))

@@ -420,6 +420,18 @@ bool make_polycone(const double *p, int np, HostShape &s, std::string &err)
     double *sec = r.data() + base + i * kPolyconeSectionDoubles;
     sec[0]      = shifts[i];
     std::memcpy(sec + 4, cones[i].rec.data(), sizeof(ConeRec));
+    // the section's cylindrical shell (every radius the cone record holds), padded by
+    // 4e-3 mm and rounded outward to FP32, for the mixed-precision screen
+    const ConeRec &c  = *reinterpret_cast<const ConeRec *>(cones[i].rec.data());
+    const double rlo  = std::min(std::min(c.rmin1, c.rmin2), std::min(c.frmin1, c.frmin2));
+    const double rhi  = std::max(std::max(std::max(c.rmax1, c.rmax2), std::max(c.frmax1, c.frmax2)),
+                                 std::max(c.origRmax1, c.origRmax2));
+    const double pad  = 4e-3;
+    auto down = [](double v) { const float f = (float)v; return (double)f > v ? std::nextafter(f, -INFINITY) : f; };
+    auto up   = [](double v) { const float f = (float)v; return (double)f < v ? std::nextafter(f, INFINITY) : f; };
+    const float shell[4] = {std::max(0.f, down(rlo - pad)), up(rhi + pad), down(shifts[i] - c.dz - pad),
+                            up(shifts[i] + c.dz + pad)};
+    std::memcpy(sec + 1, shell, sizeof(shell));
   }
   s.type = kShapePolycone;
   s.rec  = std::move(r);

@@ -5,7 +5,7 @@
 #include "launch.h"
 #include "nav_fp64.cuh"
 #include "shapes_mixed.cuh"
-#include "shapes_polyhedron_mixed.cuh"
+#include "shapes_poly_mixed.cuh"
 #include <type_traits>
 
 namespace vg {
@@ -222,6 +222,7 @@ __global__ void __launch_bounds__(256) k_shape_query_dyn(const DevGeom g, const 
 {
   const mixed::ShapeLB lb = M ? reinterpret_cast<const mixed::ShapeLB *>(g.shape_lbd)[shape] : mixed::ShapeLB{};
   const bool poly         = g.shape_type[shape] == kShapePolyhedron;
+  const bool pcone        = g.shape_type[shape] == kShapePolycone;
   const int off           = g.shape_off[shape];
   const size_t stride     = (size_t)gridDim.x * blockDim.x;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
@@ -242,6 +243,9 @@ __global__ void __launch_bounds__(256) k_shape_query_dyn(const DevGeom g, const 
         const PolyhedronRec &rec = f64::rec_at<PolyhedronRec>(g, off);
         r = (Q == 2) ? (mixed::lb_certain_miss(lb, p, d) ? kInfLength : mixed::polyhedron_dist_in_mixed(rec, p, d))
                      : mixed::polyhedron_dist_out_mixed(rec, p, d);
+      } else if (M && pcone && Q == 2) { // FP32-screened sections, same FP64 results
+        r = mixed::lb_certain_miss(lb, p, d) ? kInfLength
+                                             : mixed::polycone_dist_in_mixed(f64::rec_at<PolyconeRec>(g, off), p, d);
       } else {
         r = (Q == 2) ? ((M && mixed::lb_certain_miss(lb, p, d)) ? kInfLength : f64::shape_dist_in(g, shape, p, d))
                      : f64::shape_dist_out(g, shape, p, d);

@@ -1,4 +1,6 @@
-// Mixed-precision Polyhedron distances (VG_PREC_MIXED): the FP64 kernels of
+// Mixed-precision Polyhedron and Polycone distances (VG_PREC_MIXED).
+//
+// Polyhedron: the FP64 kernels of
 // shapes_polyhedron_fp64.cuh with one change. Before a quadrilateral is evaluated in FP64
 // inside Quadrilaterals::DistanceToIn / DistanceToOut (VecGeom/volumes/Quadrilaterals.h:
 // 326-376, 447-496), an FP32 test on the record's FP32 copy of its planes tries to prove
@@ -22,6 +24,7 @@
 // than the bound; grazing rays (|proj| < 2^-6) and far crossings get no side/z screen.
 #pragma once
 #include "nav_mixed.cuh"
+#include "shapes_more_fp64.cuh"
 #include "shapes_polyhedron_fp64.cuh"
 
 namespace vg {
@@ -121,13 +124,24 @@ __device__ __forceinline__ bool rejects_out(const PolyF32 &m, const float *f, bo
   return x.z < zMin - kTolF - ez || x.z >= zMax + kTolF + ez; // zMin - kTol <= zp < zMax + kTol fails
 }
 
-// qs_dist_in (shapes_polyhedron_fp64.cuh) with the FP32 screen in front of each quadrilateral.
+// qs_dist_in (shapes_polyhedron_fp64.cuh) with the FP32 screen in front of each
+// quadrilateral, in rounds: every lane skips, in FP32, the quadrilaterals proven rejected,
+// then the lanes that reached a candidate test it in FP64 together (same order and tests
+// as the FP64 loop for each lane; the first valid quadrilateral wins).
 static __device__ __noinline__ double qs_dist_in_m(const PolyF32 &m, f64::QuadSet s, V3 p, V3 d, bool behind)
 {
+  const unsigned mask = __activemask();
   double best = kInfLength;
-  for (int i = 0; i < s.n; ++i) {
-    const double *q = s.at(i);
-    if (rejects_in(m, m.of(q), behind)) continue;
+  int i       = 0;
+  bool active = true;
+  while (true) {
+    if (active) {
+      while (i < s.n && rejects_in(m, m.of(s.at(i)), behind)) ++i;
+      if (i >= s.n) active = false;
+    }
+    if (!__any_sync(mask, active)) break;
+    if (!active) continue;
+    const double *q = s.at(i++);
     const V3 n      = f64::qnormal(q);
     double distance = dot(p, n) + __ldg(q + 3);
     if (!((behind ? -distance : distance) > -kTolerance)) continue;
@@ -141,23 +155,32 @@ static __device__ __noinline__ double qs_dist_in_m(const PolyF32 &m, f64::QuadSe
       if (!valid) break;
     }
     if (valid) best = distance;
-    if (best < kInfLength) break;
+    if (best < kInfLength) active = false;
   }
   return f64::dmax(0., best);
 }
 
-// qs_dist_out with the FP32 screen (zMin, zMax: the segment's z range, FP64 and FP32).
+// qs_dist_out with the FP32 screen (zMin, zMax: the segment's z range), in rounds as above;
+// every quadrilateral not proven rejected is tested in FP64 in order (minimum of the valid).
 static __device__ __noinline__ double qs_dist_out_m(const PolyF32 &m, f64::QuadSet s, V3 p, V3 d, double zMin,
                                                     double zMax)
 {
-  const bool sameZ = zMin == zMax;
+  const unsigned mask = __activemask();
+  const bool sameZ    = zMin == zMax;
   const float zMinF = (float)zMin, zMaxF = (float)zMax;
   double best = kInfLength;
-  for (int i = 0; i < s.n; ++i) {
-    const double *q = s.at(i);
-    if (rejects_out(m, m.of(q), sameZ, zMinF, zMaxF)) continue;
-    const V3 n = f64::qnormal(q);
-    double t   = dot(p, n) + __ldg(q + 3);
+  int i       = 0;
+  bool active = true;
+  while (true) {
+    if (active) {
+      while (i < s.n && rejects_out(m, m.of(s.at(i)), sameZ, zMinF, zMaxF)) ++i;
+      if (i >= s.n) active = false;
+    }
+    if (!__any_sync(mask, active)) break;
+    if (!active) continue;
+    const double *q = s.at(i++);
+    const V3 n      = f64::qnormal(q);
+    double t        = dot(p, n) + __ldg(q + 3);
     if (!(t < kTolerance)) continue;
     const double proj = dot(d, n);
     if (!(proj > 0)) continue;
@@ -273,6 +296,70 @@ static __device__ __noinline__ double polyhedron_dist_out_mixed(const Polyhedron
   }
   f64::ph_endcaps(v, true, p, d, distance);
   if (distance >= kInfLength) distance = 0.;
+  return distance;
+}
+
+// ---------------------------------------------------------------- Polycone
+// PolyconeImplementation.h:148-180 DistanceToIn walks the sections from the point's one in
+// the direction of the ray and stops at the first whose Cone DistanceToIn is below
+// kInfLength. A section is not evaluated in FP64 when FP32 proves that the point lies
+// outside its padded cylindrical shell (4e-3 mm beyond every radius and z face the cone
+// has, rounded outward; the FP32 point is within 1e-3 mm of the FP64 one up to 4 m) and
+// that the ray misses that shell: the cone's FP64 DistanceToIn is then kInfLength, its
+// miss value, which is what the loop is given. Other sections run the FP64 Cone kernel,
+// so the result is the FP64 kernel's.
+__device__ __forceinline__ bool pc_section_certain_miss(const f64::PolyconeView &v, int i, F3 pf, F3 df)
+{
+  const float *sh = reinterpret_cast<const float *>(v.sec(i) + 1);
+  const float rmin = __ldg(sh), rmax = __ldg(sh + 1), zlo = __ldg(sh + 2), zhi = __ldg(sh + 3);
+  const float r2 = fmaf(pf.x, pf.x, pf.y * pf.y);
+  const bool outside = pf.z < zlo || pf.z > zhi || r2 > rmax * rmax || (rmin > 0.f && r2 < rmin * rmin);
+  return outside && shell_lb(rmin, rmax, zlo, zhi, pf, df) == INFINITY;
+}
+
+// The section loop in rounds: each lane first walks, in FP32, past the sections it can prove
+// missed (their FP64 value would be kInfLength), then the lanes that reached a candidate
+// evaluate it in FP64 together (one Cone kernel per round for the whole warp, instead of
+// one per lane and iteration). Each lane sees the reference's sequence of values.
+static __device__ __noinline__ double polycone_dist_in_mixed(const PolyconeRec &rec, V3 p, V3 d)
+{
+  const unsigned mask = __activemask();
+  const f64::PolyconeView v(rec);
+  const F3 pf = f3(p), df = f3(d);
+  const bool screen = fabsf(pf.x) <= 4000.f && fabsf(pf.y) <= 4000.f && fabsf(pf.z) <= 4000.f;
+  double distance = kInfLength;
+  int increment   = f64::dgt(d.z, 0.) ? 1 : -1;
+  if (f64::dabs_lt(d.z, kTolerance)) increment = 0;
+  int index = v.index(p.z);
+  if (index == -1) index = 0;
+  if (index == -2) index = v.nsec - 1;
+  bool active = true;
+  while (true) {
+    if (active && screen) { // FP32 walk: a proven miss is the FP64 loop's kInfLength iteration
+      while (pc_section_certain_miss(v, index, pf, df)) {
+        distance = kInfLength;
+        if (!increment) {
+          active = false;
+          break;
+        }
+        index += increment;
+        if (index < 0 || index >= v.nsec) {
+          active = false;
+          break;
+        }
+      }
+    }
+    if (!__any_sync(mask, active)) break;
+    if (active) {
+      distance = f64::cone_dist_in(v.cone(index), v.local(p, index), d);
+      if (f64::dlt(distance, kInfLength) || !increment) {
+        active = false;
+      } else {
+        index += increment;
+        if (index < 0 || index >= v.nsec) active = false;
+      }
+    }
+  }
   return distance;
 }
 

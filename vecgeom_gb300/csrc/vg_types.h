@@ -91,9 +91,12 @@ struct TrapRec {
 // Polycone record: header, section boundaries, then one (shift, cone) block per section
 // (VecGeom/volumes/PolyconeStruct.h:26-36, PolyconeSection.h). Variable length; the views
 // below address it in place.
+// Each section block: z shift, then four FP32 values in the next two doubles (the section's
+// conservative cylindrical shell in the polycone frame, padded by 4e-3 mm and rounded
+// outward: rmin, rmax, zlo, zhi; for the mixed-precision screen), one pad double, ConeRec.
 struct PolyconeRec {
   double nsec, sphi, dphi, reserved;
-  double data[1]; // zs[nsec+1], pad to a multiple of 4, then nsec x (shift, 3 pad, ConeRec, pad)
+  double data[1]; // zs[nsec+1], pad to a multiple of 4, then nsec x (shift, shell, pad, ConeRec, pad)
 };
 constexpr int kPolyconeSectionDoubles = 4 + ((int)(sizeof(ConeRec) / sizeof(double)) + 3) / 4 * 4;
 VG_HD inline int polycone_section_base(int nsec) { return ((4 + nsec + 1) + 3) / 4 * 4; }
