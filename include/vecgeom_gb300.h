@@ -49,6 +49,7 @@ extern "C" {
 #define VG_SHAPE_TRD 7
 #define VG_SHAPE_BOOLEAN_SUBTRACTION 8
 #define VG_SHAPE_TRAPEZOID 9
+#define VG_SHAPE_CUT_TUBE 10
 
 /* Precision flags for queries and navigation */
 #define VG_PREC_FP64 0u  /* plain FP64: results identical to the reference's FP64 path          */
@@ -122,6 +123,12 @@ int32_t vg_geom_add_trap_corners(vg_geom *g, const double *corners);
  * -X, +X): planes[16] = (a, b, c, d) of each plane in that order. Mirrors any trapezoid
  * bit-exactly, whichever constructor made it. */
 int32_t vg_geom_add_trap_planes(vg_geom *g, double dz, const double *planes);
+/* UnplacedCutTube(rmin, rmax, dz, sphi, dphi, bx, by, bz, tx, ty, tz)
+ * (VecGeom/volumes/UnplacedCutTube.h:54-70): a tube section between two cut planes through
+ * (0, 0, -dz) and (0, 0, +dz) with outward normals (bx, by, bz), bz < 0, and (tx, ty, tz),
+ * tz > 0 (other normals are rejected with VG_EINVAL, as the reference throws). */
+int32_t vg_geom_add_cut_tube(vg_geom *g, double rmin, double rmax, double dz, double sphi, double dphi, double bx,
+                             double by, double bz, double tx, double ty, double tz);
 /* UnplacedBooleanVolume<kSubtraction>(left, right): operands are placed volumes created
  * with vg_geom_place (VecGeom/volumes/BooleanStruct.h:19-33) */
 int32_t vg_geom_add_boolean_subtraction(vg_geom *g, int32_t left_pv, int32_t right_pv);

@@ -114,6 +114,9 @@ class OracleGeometry:
     def add_boolean_subtraction(self, left_pv, right_pv):
         return self._shape(8, [left_pv, right_pv])
 
+    def add_cut_tube(self, rmin, rmax, dz, sphi, dphi, bottom_normal, top_normal):
+        return self._shape(11, [rmin, rmax, dz, sphi, dphi, *bottom_normal, *top_normal])
+
     def add_boolean_union(self, left_pv, right_pv):
         """Union of two placed volumes (oracle only: the product has no union)."""
         return self._shape(10, [left_pv, right_pv])

@@ -924,4 +924,214 @@ void BooleanMinus::Extent(Vec3 &aMin, Vec3 &aMax) const
   aMax = Vec3(mx[0], mx[1], mx[2]);
 }
 
+// ====================================================================== Cut tube
+// Plane.h:40-49 Set(normal, origin): zero components below kTolerance, then normalise
+void CutPlane::Set(Vec3 normal, Vec3 const &origin)
+{
+  for (int i = 0; i < 3; ++i)
+    if (Abs(normal[i]) < kTolerance) normal[i] = 0.0;
+  const double inv = 1. / normal.Mag();
+  n                = inv * normal;
+  d                = inv * -normal.Dot(origin);
+}
+
+// CutTubeStruct.h:38-49
+CutTube::CutTube(double rmin, double rmax, double z, double sphi, double dphi, Vec3 bottom, Vec3 top)
+    : fDz(z), fTube(rmin, rmax, kInfLength, sphi, dphi)
+{
+  fCut[0].Set(bottom.Unit(), Vec3(0., 0., -z));
+  fCut[1].Set(top.Unit(), Vec3(0., 0., z));
+  fCosPhi1 = std::cos(sphi);
+  fSinPhi1 = std::sin(sphi);
+  fCosPhi2 = std::cos(sphi + dphi);
+  fSinPhi2 = std::sin(sphi + dphi);
+  fMaxVal  = Max(rmax, z);
+}
+
+// CutPlanes.h Inside (:130-142): inside both, surface within kTolerance of either
+int CutTube::CutInside(Vec3 const &p) const
+{
+  const double d0 = fCut[0].Dist(p), d1 = fCut[1].Dist(p);
+  int inside      = (d0 < 0.0 && d1 < 0.0) ? kInside : kOutside;
+  if (Abs(d0) < kTolerance || Abs(d1) < kTolerance) inside = kSurface;
+  return inside;
+}
+
+// CutPlanes.h DistanceToIn (:144-156) with Plane::DistanceToIn (Plane.h:128-147): per plane
+// -saf/ndd when approaching from outside the tolerance band, -kInfLength when the
+// direction is along the normal; the larger of the two
+double CutTube::CutDistanceToIn(Vec3 const &p, Vec3 const &dir) const
+{
+  double dd[2];
+  for (int i = 0; i < 2; ++i) {
+    double distance  = -kInfLength;
+    const double ndd = NonZero(dir.Dot(fCut[i].n));
+    const double saf = fCut[i].Dist(p);
+    const bool valid = ndd < 0. && saf > -kTolerance;
+    if (valid) distance = -saf / ndd;
+    if (dir.Dot(fCut[i].n) > 0.) distance = -kInfLength;
+    dd[i] = distance;
+  }
+  return Max(dd[0], dd[1]);
+}
+
+// CutPlanes.h DistanceToOut (:158-166) with Plane::DistanceToOut (Plane.h:149-170)
+double CutTube::CutDistanceToOut(Vec3 const &p, Vec3 const &dir) const
+{
+  double dd[2];
+  for (int i = 0; i < 2; ++i) {
+    double distance  = kInfLength;
+    const double ndd = NonZero(dir.Dot(fCut[i].n));
+    const double saf = fCut[i].Dist(p);
+    const bool valid = ndd > 0. && saf < kTolerance;
+    if (saf > kTolerance) distance = -kInfLength;
+    if (valid) distance = -saf / ndd;
+    dd[i] = distance;
+  }
+  return Min(dd[0], dd[1]);
+}
+
+double CutTube::CutSafetyToIn(Vec3 const &p) const { return Max(fCut[0].Dist(p), fCut[1].Dist(p)); }
+double CutTube::CutSafetyToOut(Vec3 const &p) const { return Min(-fCut[0].Dist(p), -fCut[1].Dist(p)); }
+
+// CutTubeImplementation.h:114-126 Contains
+bool CutTube::Contains(Vec3 const &p) const
+{
+  const bool inCut = fCut[0].Dist(p) < 0. && fCut[1].Dist(p) < 0.;
+  if (!inCut) return false;
+  return fTube.Contains(p) && inCut;
+}
+
+// CutTubeImplementation.h:128-142 Inside
+int CutTube::Inside(Vec3 const &p) const
+{
+  const int ic = CutInside(p);
+  if (ic == kOutside) return kOutside;
+  int inside = fTube.Inside(p);
+  if (ic == kOutside || (ic == kSurface && inside != kOutside)) inside = ic;
+  return inside;
+}
+
+// CutTubeImplementation.h:144-169 DistanceToIn: far points are first moved to 100 x the
+// largest dimension from the origin along the ray
+double CutTube::DistanceToIn(Vec3 const &pointT, Vec3 const &dir, double stepMax) const
+{
+  Vec3 point          = pointT;
+  const double ptDist = point.Mag();
+  double distToMove   = 0.;
+  const double order  = 100.;
+  if (ptDist > order * fMaxVal) {
+    distToMove = ptDist - order * fMaxVal;
+    point      = point + distToMove * dir;
+  }
+  double distance = DistanceToInKernel(point, dir, stepMax);
+  distance += distToMove;
+  return distance;
+}
+
+// CutTubeImplementation.h:171-258 DistanceToInKernel (USE_CONV_WRONG_SIDE): points inside
+// give -1; the ray is first moved to the cut planes when it hits them within stepMax, then
+// the tube distance from there, limited by the exit from the cut planes
+double CutTube::DistanceToInKernel(Vec3 const &point, Vec3 const &direction, double stepMax) const
+{
+  double distance = kInfLength;
+  int insideCut   = CutInside(point);
+  int instart     = fTube.Inside(point);
+  if (insideCut == kOutside || (insideCut == kSurface && instart != kOutside)) instart = insideCut;
+  if (instart == kInside) distance = -1.;
+  double dplanes         = CutDistanceToIn(point, direction);
+  const double safplanes = CutSafetyToIn(point);
+  const bool hitplanes   = Abs(dplanes) < stepMax && safplanes > -kTolerance;
+  if (insideCut != kInside && !hitplanes) return distance;
+  Vec3 propagated = point;
+  if (!hitplanes) dplanes = 0.;
+  if (hitplanes) {
+    propagated = propagated + dplanes * direction;
+    insideCut  = CutInside(propagated);
+  }
+  bool done = insideCut == kOutside;
+  done      = done || instart == kInside;
+  if (done) return distance;
+  instart           = fTube.Inside(propagated);
+  const bool inside = hitplanes && (instart != kOutside);
+  if (inside && !done) distance = dplanes;
+  done = done || inside;
+  if (done) {
+    if (Abs(distance) < kTolerance) distance = 0.;
+    return distance;
+  }
+  const double dexit = CutDistanceToOut(propagated, direction);
+  double dtube       = fTube.DistanceToInKernel(propagated, direction);
+  if (dtube < 0.) dtube = 0.;
+  if (dexit < dtube) dtube = kInfLength;
+  if (!done && (dtube + dplanes) < stepMax) distance = dtube + dplanes;
+  return distance;
+}
+
+// CutTubeImplementation.h:262-280 DistanceToOut
+double CutTube::DistanceToOut(Vec3 const &point, Vec3 const &direction, double stepMax) const
+{
+  double distance    = CutDistanceToOut(point, direction);
+  const double dtube = fTube.DistanceToOut(point, direction, stepMax);
+  if (dtube < distance) distance = dtube;
+  return distance;
+}
+
+// CutTubeImplementation.h:283-298 SafetyToIn
+double CutTube::SafetyToIn(Vec3 const &point) const
+{
+  double safety        = CutSafetyToIn(point);
+  const double saftube = fTube.SafetyToIn(point);
+  if (saftube > safety) safety = saftube;
+  return safety;
+}
+
+// CutTubeImplementation.h:301-315 SafetyToOut
+double CutTube::SafetyToOut(Vec3 const &point) const
+{
+  double safety        = CutSafetyToOut(point);
+  const double saftube = fTube.SafetyToOut(point);
+  if (saftube < safety) safety = saftube;
+  return safety;
+}
+
+// source/UnplacedCutTube.cpp:128-172 Extent (ZlimitTop / ZlimitBottom, UnplacedCutTube.h:135-147)
+void CutTube::Extent(Vec3 &aMin, Vec3 &aMax) const
+{
+  const Vec3 tn = fCut[1].n, bn = fCut[0].n;
+  const double rmax = fTube.fRmax, rmin = fTube.fRmin, sphi = fTube.fSphi, dphi = fTube.fDphi, z = fDz;
+  auto zTop = [&](double r, double ph) { return z - (r / tn.z()) * (tn.x() * std::cos(ph) + tn.y() * std::sin(ph)); };
+  auto zBot = [&](double r, double ph) { return -z - (r / bn.z()) * (bn.x() * std::cos(ph) + bn.y() * std::sin(ph)); };
+  const double dztop    = rmax * Sqrt(1. - tn.z() * tn.z()) / tn.z();
+  const double dzbottom = -rmax * Sqrt(1. - bn.z() * bn.z()) / bn.z();
+  aMin = Vec3(-rmax, -rmax, -z - dzbottom);
+  aMax = Vec3(rmax, rmax, z + dztop);
+  if (dphi == kTwoPi) return;
+  Wedge const &w = fTube.fPhiWedge;
+  if (!w.Contains(Vec3(-tn.x(), -tn.y(), 0.))) {
+    aMax[2] = Max(zTop(rmax, sphi), zTop(rmax, sphi + dphi));
+    aMax[2] = Max(aMax[2], Max(zTop(rmin, sphi), zTop(rmin, sphi + dphi)));
+  }
+  if (!w.Contains(Vec3(-bn.x(), -bn.y(), 0.))) {
+    aMin[2] = Min(zBot(rmax, sphi), zBot(rmax, sphi + dphi));
+    aMin[2] = Min(aMin[2], Min(zBot(rmin, sphi), zBot(rmin, sphi + dphi)));
+  }
+  if (!w.Contains(Vec3(1., 0., 0.))) {
+    aMax[0] = Max(rmax * fCosPhi1, rmax * fCosPhi2);
+    aMax[0] = Max(aMax[0], Max(rmin * fCosPhi1, rmin * fCosPhi2));
+  }
+  if (!w.Contains(Vec3(-1., 0., 0.))) {
+    aMin[0] = Min(rmax * fCosPhi1, rmax * fCosPhi2);
+    aMin[0] = Min(aMin[0], Min(rmin * fCosPhi1, rmin * fCosPhi2));
+  }
+  if (!w.Contains(Vec3(0., 1., 0.))) {
+    aMax[1] = Max(rmax * fSinPhi1, rmax * fSinPhi2);
+    aMax[1] = Max(aMax[1], Max(rmin * fSinPhi1, rmin * fSinPhi2));
+  }
+  if (!w.Contains(Vec3(0., -1., 0.))) {
+    aMin[1] = Min(rmax * fSinPhi1, rmax * fSinPhi2);
+    aMin[1] = Min(aMin[1], Min(rmin * fSinPhi1, rmin * fSinPhi2));
+  }
+}
+
 } // namespace oracle

@@ -89,6 +89,38 @@ struct BooleanMinus : UnplacedShape {
   void Extent(Vec3 &lo, Vec3 &hi) const override;
 };
 
+// VecGeom/volumes/Plane.h: a plane n.p + d (n unit), positive on the outside.
+struct CutPlane {
+  Vec3 n;
+  double d = 0.;
+  void Set(Vec3 normal, Vec3 const &origin); // Plane.h:40-49
+  double Dist(Vec3 const &p) const { return p.Dot(n) + d; } // Plane.h:98-107 DistPlane
+};
+
+// VecGeom/volumes/CutTubeStruct.h, VecGeom/volumes/CutPlanes.h,
+// VecGeom/volumes/kernel/CutTubeImplementation.h: a tube (UniversalTube of infinite
+// half-length) between two cut planes through (0, 0, -dz) and (0, 0, +dz).
+struct CutTube : UnplacedShape {
+  double fDz;
+  Tube fTube;
+  CutPlane fCut[2];
+  double fCosPhi1, fSinPhi1, fCosPhi2, fSinPhi2, fMaxVal;
+  CutTube(double rmin, double rmax, double z, double sphi, double dphi, Vec3 bottom, Vec3 top);
+  int CutInside(Vec3 const &p) const;             // CutPlanes.h Inside
+  double CutDistanceToIn(Vec3 const &p, Vec3 const &d) const;
+  double CutDistanceToOut(Vec3 const &p, Vec3 const &d) const;
+  double CutSafetyToIn(Vec3 const &p) const;
+  double CutSafetyToOut(Vec3 const &p) const;
+  double DistanceToInKernel(Vec3 const &p, Vec3 const &d, double stepMax) const;
+  int Inside(Vec3 const &p) const override;
+  bool Contains(Vec3 const &p) const override;
+  double DistanceToIn(Vec3 const &p, Vec3 const &d, double smax) const override;
+  double DistanceToOut(Vec3 const &p, Vec3 const &d, double smax) const override;
+  double SafetyToIn(Vec3 const &p) const override;
+  double SafetyToOut(Vec3 const &p) const override;
+  void Extent(Vec3 &lo, Vec3 &hi) const override;
+};
+
 // VecGeom/volumes/kernel/BooleanUnionImplementation.h (kUnion); operands are placed volumes.
 // Test infrastructure beyond the product's shapes: the reference's boolean unit test
 // subtracts a union, so the oracle restates the union to check its subtraction there.

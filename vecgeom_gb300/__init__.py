@@ -38,6 +38,7 @@ assert NAVSTATE_DTYPE.itemsize == 12
 
 SHAPE_BOX, SHAPE_TUBE, SHAPE_CONE, SHAPE_POLYCONE, SHAPE_POLYHEDRON, SHAPE_TORUS2, SHAPE_TRD, SHAPE_BOOLMINUS = range(1, 9)
 SHAPE_TRAPEZOID = 9
+SHAPE_CUT_TUBE = 10
 
 
 class VGError(RuntimeError):
@@ -65,6 +66,7 @@ _SIGS = {
     "vg_geom_add_trd": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 5),
     "vg_geom_add_trap": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 11),
     "vg_geom_add_trap_corners": (ctypes.c_int32, [_c_vp, _c_dp]),
+    "vg_geom_add_cut_tube": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 11),
     "vg_geom_add_trap_planes": (ctypes.c_int32, [_c_vp, ctypes.c_double, _c_dp]),
     "vg_geom_save": (ctypes.c_int, [_c_vp, ctypes.c_char_p]),
     "vg_geom_load": (ctypes.c_int, [_c_vp, ctypes.c_char_p]),
@@ -249,6 +251,12 @@ class Geometry:
         (+-+) (-++) (+++)."""
         c = np.ascontiguousarray(np.asarray(corners, dtype=np.float64).reshape(24))
         return _check(_lib.vg_geom_add_trap_corners(self._h, c.ctypes.data_as(_c_dp)), "add_trap_corners")
+
+    def add_cut_tube(self, rmin, rmax, dz, sphi, dphi, bottom_normal, top_normal):
+        """UnplacedCutTube: a tube section between two cut planes through (0, 0, -dz) and
+        (0, 0, dz) with the given outward normals (bottom z < 0, top z > 0)."""
+        b, t = [float(v) for v in bottom_normal], [float(v) for v in top_normal]
+        return _check(_lib.vg_geom_add_cut_tube(self._h, rmin, rmax, dz, sphi, dphi, *b, *t), "add_cut_tube")
 
     def add_trap_planes(self, dz, planes):
         """A trapezoid from dz and its four side planes (a, b, c, d), ordered -Y, +Y, -X, +X, as

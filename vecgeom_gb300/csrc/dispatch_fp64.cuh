@@ -30,6 +30,7 @@ __device__ __forceinline__ const R &rec_at(const DevGeom &g, int off)
   case kShapeCone: return cone_##FN(rec_at<ConeRec>(g, off), __VA_ARGS__);                      \
   case kShapeTrd: return trd_##FN(rec_at<TrdRec>(g, off), __VA_ARGS__);                         \
   case kShapeTrap: return trap_##FN(rec_at<TrapRec>(g, off), __VA_ARGS__);                      \
+  case kShapeCutTube: return cuttube_##FN(rec_at<CutTubeRec>(g, off), __VA_ARGS__);             \
   case kShapePolycone: return polycone_##FN(rec_at<PolyconeRec>(g, off), __VA_ARGS__);          \
   case kShapePolyhedron: return polyhedron_##FN(rec_at<PolyhedronRec>(g, off), __VA_ARGS__);    \
   case kShapeTorus2: return torus_##FN(rec_at<TorusRec>(g, off), __VA_ARGS__);                  \

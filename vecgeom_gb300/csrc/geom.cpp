@@ -183,6 +183,64 @@ void make_tube(const double *p, HostShape &s)
   phi_section_extent(t.w, t.sphi, t.dphi, t.rmin, t.rmax, t.z, s.lo, s.hi);
 }
 
+// CutTubeStruct constructor (CutTubeStruct.h:38-49) with CutPlanes::Set / Plane::Set
+// (Plane.h:40-49), UnplacedCutTube's normal check (UnplacedCutTube.h:36-50) and Extent
+// (source/UnplacedCutTube.cpp:128-172).
+bool make_cut_tube(const double *p, HostShape &s, std::string &err)
+{
+  const double rmin = p[0], rmax = p[1], z = p[2], sphi = p[3], dphi = p[4];
+  if (!(p[7] < 0) || !(p[10] > 0)) {
+    err = "illegal normal direction for cut planes (bottom z must be < 0, top z > 0)";
+    return false;
+  }
+  CutTubeRec c{};
+  const double tp[5] = {rmin, rmax, kInfLength, sphi, dphi};
+  HostShape ts;
+  make_tube(tp, ts);
+  std::memcpy(&c.t, ts.rec.data(), sizeof(TubeRec));
+  auto set_plane = [](const double *nin, double oz, double *n, double &d) {
+    // Vector3D::Unit (Vector3D.h:284-290), then Plane::Set: zero components below
+    // kTolerance and normalise again
+    const double m2 = nin[0] * nin[0] + nin[1] * nin[1] + nin[2] * nin[2];
+    const double s  = std::sqrt(m2 + kMinimum);
+    double v[3]     = {nin[0] / s, nin[1] / s, nin[2] / s};
+    for (double &x : v)
+      if (std::fabs(x) < kTolerance) x = 0.0;
+    const double inv = 1. / std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    for (int k = 0; k < 3; ++k) n[k] = inv * v[k];
+    d = inv * -(v[0] * 0. + v[1] * 0. + v[2] * oz);
+  };
+  double n0[3], n1[3];
+  set_plane(p + 5, -z, n0, c.d0);
+  set_plane(p + 8, z, n1, c.d1);
+  c.n0x = n0[0], c.n0y = n0[1], c.n0z = n0[2], c.n1x = n1[0], c.n1y = n1[1], c.n1z = n1[2];
+  c.dz     = z;
+  c.maxVal = rmax > z ? rmax : z;
+  s.type   = kShapeCutTube;
+  pack(s, c);
+  // Extent
+  const double cp1 = std::cos(sphi), sp1 = std::sin(sphi), cp2 = std::cos(sphi + dphi), sp2 = std::sin(sphi + dphi);
+  auto zTop = [&](double r, double ph) { return z - (r / n1[2]) * (n1[0] * std::cos(ph) + n1[1] * std::sin(ph)); };
+  auto zBot = [&](double r, double ph) { return -z - (r / n0[2]) * (n0[0] * std::cos(ph) + n0[1] * std::sin(ph)); };
+  const double dztop    = rmax * std::sqrt(1. - n1[2] * n1[2]) / n1[2];
+  const double dzbottom = -rmax * std::sqrt(1. - n0[2] * n0[2]) / n0[2];
+  s.lo[0] = -rmax, s.lo[1] = -rmax, s.lo[2] = -z - dzbottom;
+  s.hi[0] = rmax, s.hi[1] = rmax, s.hi[2] = z + dztop;
+  if (dphi == kTwoPi) return true;
+  auto mx = [](double a, double b) { return a > b ? a : b; };
+  auto mn = [](double a, double b) { return a < b ? a : b; };
+  auto contains = [&](double x, double y) { return wedge_contains(c.t.w, x, y); };
+  if (!contains(-n1[0], -n1[1]))
+    s.hi[2] = mx(mx(zTop(rmax, sphi), zTop(rmax, sphi + dphi)), mx(zTop(rmin, sphi), zTop(rmin, sphi + dphi)));
+  if (!contains(-n0[0], -n0[1]))
+    s.lo[2] = mn(mn(zBot(rmax, sphi), zBot(rmax, sphi + dphi)), mn(zBot(rmin, sphi), zBot(rmin, sphi + dphi)));
+  if (!contains(1., 0.)) s.hi[0] = mx(mx(rmax * cp1, rmax * cp2), mx(rmin * cp1, rmin * cp2));
+  if (!contains(-1., 0.)) s.lo[0] = mn(mn(rmax * cp1, rmax * cp2), mn(rmin * cp1, rmin * cp2));
+  if (!contains(0., 1.)) s.hi[1] = mx(mx(rmax * sp1, rmax * sp2), mx(rmin * sp1, rmin * sp2));
+  if (!contains(0., -1.)) s.lo[1] = mn(mn(rmax * sp1, rmax * sp2), mn(rmin * sp1, rmin * sp2));
+  return true;
+}
+
 // ConeStruct constructor, SetAndCheck{D,S}PhiAngle and CalculateCached (ConeStruct.h:85-336)
 void make_cone(const double *p, HostShape &s)
 {
@@ -752,6 +810,9 @@ int32_t Geometry::add_shape(int32_t type, const double *p, int np, std::string &
   case kShapeTorus2:
     if (!need(5)) return -1;
     make_torus2(p, s);
+    break;
+  case kShapeCutTube:
+    if (!need(11) || !make_cut_tube(p, s, err)) return -1;
     break;
   case kShapePolycone:
     if (!need(3) || !make_polycone(p, np, s, err)) return -1;

@@ -475,6 +475,135 @@ __device__ __forceinline__ double tube_safety_out(const TubeRec &t, V3 p)
   return safety;
 }
 
+// ================================================================ Cut tube
+// CutPlanes.h / Plane.h on the record's two planes: DistPlane = p.n + d (Plane.h:98-107)
+__device__ __forceinline__ double cut_dist0(const CutTubeRec &c, V3 p) { return p.x * c.n0x + p.y * c.n0y + p.z * c.n0z + c.d0; }
+__device__ __forceinline__ double cut_dist1(const CutTubeRec &c, V3 p) { return p.x * c.n1x + p.y * c.n1y + p.z * c.n1z + c.d1; }
+// CutPlanes::Inside (CutPlanes.h:130-142)
+__device__ __forceinline__ int cut_inside(const CutTubeRec &c, V3 p)
+{
+  const double d0 = cut_dist0(c, p), d1 = cut_dist1(c, p);
+  int inside      = (dlt(d0, 0.0) && dlt(d1, 0.0)) ? kInside : kOutside;
+  if (dabs_lt(d0, kTolerance) || dabs_lt(d1, kTolerance)) inside = kSurface;
+  return inside;
+}
+// Plane::DistanceToIn (Plane.h:128-147) masked to -kInfLength when moving along the normal
+// (CutPlanes.h:144-156)
+__device__ __forceinline__ double cut_plane_dist_in(double nx, double ny, double nz, double dd, V3 p, V3 dir)
+{
+  double distance  = -kInfLength;
+  const double dt  = dir.x * nx + dir.y * ny + dir.z * nz;
+  const double ndd = nonzero(dt);
+  const double saf = p.x * nx + p.y * ny + p.z * nz + dd;
+  if (dlt(ndd, 0.) && dgt(saf, -kTolerance)) distance = -saf / ndd;
+  if (dgt(dt, 0.)) distance = -kInfLength;
+  return distance;
+}
+// Plane::DistanceToOut (Plane.h:149-170)
+__device__ __forceinline__ double cut_plane_dist_out(double nx, double ny, double nz, double dd, V3 p, V3 dir)
+{
+  double distance  = kInfLength;
+  const double ndd = nonzero(dir.x * nx + dir.y * ny + dir.z * nz);
+  const double saf = p.x * nx + p.y * ny + p.z * nz + dd;
+  if (dgt(saf, kTolerance)) distance = -kInfLength;
+  if (dgt(ndd, 0.) && dlt(saf, kTolerance)) distance = -saf / ndd;
+  return distance;
+}
+__device__ __forceinline__ double cut_dist_in(const CutTubeRec &c, V3 p, V3 d)
+{
+  return dmax(cut_plane_dist_in(c.n0x, c.n0y, c.n0z, c.d0, p, d), cut_plane_dist_in(c.n1x, c.n1y, c.n1z, c.d1, p, d));
+}
+__device__ __forceinline__ double cut_dist_out(const CutTubeRec &c, V3 p, V3 d)
+{
+  return dmin(cut_plane_dist_out(c.n0x, c.n0y, c.n0z, c.d0, p, d), cut_plane_dist_out(c.n1x, c.n1y, c.n1z, c.d1, p, d));
+}
+
+// CutTubeImplementation.h:114-126 Contains
+__device__ __forceinline__ bool cuttube_contains(const CutTubeRec &c, V3 p)
+{
+  const bool inCut = dlt(cut_dist0(c, p), 0.) && dlt(cut_dist1(c, p), 0.);
+  if (!inCut) return false;
+  return tube_contains(c.t, p);
+}
+// CutTubeImplementation.h:128-142 Inside
+__device__ __forceinline__ int cuttube_inside(const CutTubeRec &c, V3 p)
+{
+  const int ic = cut_inside(c, p);
+  if (ic == kOutside) return kOutside;
+  const int it = tube_inside(c.t, p);
+  return (ic == kSurface && it != kOutside) ? ic : it;
+}
+// CutTubeImplementation.h:171-258 DistanceToInKernel with stepMax = kInfLength: a value the
+// reference gives below its stepMax does not depend on it (the cut-plane hit needs |d| <
+// stepMax, the tube hit d < stepMax), so a navigator that accepts only distances below its
+// current step makes the same choices as the reference's, which passes that step.
+static __device__ __noinline__ double cuttube_dist_in_kernel(const CutTubeRec &c, V3 point, V3 dir)
+{
+  const double stepMax = kInfLength;
+  double distance      = kInfLength;
+  int insideCut        = cut_inside(c, point);
+  int instart          = tube_inside(c.t, point);
+  if (insideCut == kOutside || (insideCut == kSurface && instart != kOutside)) instart = insideCut;
+  if (instart == kInside) distance = -1.;
+  double dplanes         = cut_dist_in(c, point, dir);
+  const double safplanes = dmax(cut_dist0(c, point), cut_dist1(c, point));
+  const bool hitplanes   = dlt(fabs(dplanes), stepMax) && dgt(safplanes, -kTolerance);
+  if (insideCut != kInside && !hitplanes) return distance;
+  V3 propagated = point;
+  if (!hitplanes) dplanes = 0.;
+  if (hitplanes) {
+    propagated = V3{propagated.x + dplanes * dir.x, propagated.y + dplanes * dir.y, propagated.z + dplanes * dir.z};
+    insideCut  = cut_inside(c, propagated);
+  }
+  if (insideCut == kOutside || instart == kInside) return distance;
+  const bool inside = hitplanes && (tube_inside(c.t, propagated) != kOutside);
+  if (inside) {
+    distance = dplanes;
+    if (dabs_lt(distance, kTolerance)) distance = 0.;
+    return distance;
+  }
+  const double dexit = cut_dist_out(c, propagated, dir);
+  double dtube       = tube_dist_in_kernel(c.t, propagated, dir);
+  if (dlt(dtube, 0.)) dtube = 0.;
+  if (dlt(dexit, dtube)) dtube = kInfLength;
+  if (dlt(dtube + dplanes, stepMax)) distance = dtube + dplanes;
+  return distance;
+}
+// CutTubeImplementation.h:144-169 DistanceToIn (far points moved to 100 x max(rmax, dz))
+__device__ __forceinline__ double cuttube_dist_in(const CutTubeRec &c, V3 p, V3 d)
+{
+  const double ptDist = sqrt(p.x * p.x + p.y * p.y + p.z * p.z);
+  double distToMove   = 0.;
+  if (dgt(ptDist, 100. * c.maxVal)) {
+    distToMove = ptDist - 100. * c.maxVal;
+    p          = V3{p.x + distToMove * d.x, p.y + distToMove * d.y, p.z + distToMove * d.z};
+  }
+  return cuttube_dist_in_kernel(c, p, d) + distToMove;
+}
+// CutTubeImplementation.h:262-280 DistanceToOut
+__device__ __forceinline__ double cuttube_dist_out(const CutTubeRec &c, V3 p, V3 d)
+{
+  double distance    = cut_dist_out(c, p, d);
+  const double dtube = tube_dist_out(c.t, p, d);
+  if (dlt(dtube, distance)) distance = dtube;
+  return distance;
+}
+// CutTubeImplementation.h:283-315 SafetyToIn / SafetyToOut
+__device__ __forceinline__ double cuttube_safety_in(const CutTubeRec &c, V3 p)
+{
+  double safety        = dmax(cut_dist0(c, p), cut_dist1(c, p));
+  const double saftube = tube_safety_in(c.t, p);
+  if (dgt(saftube, safety)) safety = saftube;
+  return safety;
+}
+__device__ __forceinline__ double cuttube_safety_out(const CutTubeRec &c, V3 p)
+{
+  double safety        = dmin(-cut_dist0(c, p), -cut_dist1(c, p));
+  const double saftube = tube_safety_out(c.t, p);
+  if (dlt(saftube, safety)) safety = saftube;
+  return safety;
+}
+
 // ================================================================ Cone
 __device__ __forceinline__ bool cone_phi(const ConeRec &c) { return dlt(c.dphi, kTwoPi); }
 __device__ __forceinline__ bool cone_rmin(const ConeRec &c) { return dgt(c.rmin1, 0.) || dgt(c.rmin2, 0.); }

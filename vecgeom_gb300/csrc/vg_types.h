@@ -24,6 +24,7 @@ enum ShapeType : int32_t {
   kShapeTrd        = 7,
   kShapeBoolMinus  = 8,
   kShapeTrap       = 9,
+  kShapeCutTube    = 10,
 };
 
 // VecGeom/base/Math.h:27-52 (double precision)
@@ -129,6 +130,15 @@ struct PolyhedronRec {
 constexpr int kPolyQuadDoubles = 32; // n[3] d | (sideN[3] sideD) x 4 | corner[3] x 4
 constexpr int kPolyQuadFloats  = 20; // n[3] d | (sideN[3] sideD) x 4
 constexpr int kPolyFlagInner = 1, kPolyFlagPhi = 2, kPolyFlagLargePhi = 4;
+
+// Cut tube (VecGeom/volumes/CutTubeStruct.h:22-49): the tube record of UniversalTube with
+// infinite half-length, the two cut planes (unit normal and distance, Plane.h:40-49: bottom
+// through (0, 0, -dz), top through (0, 0, +dz)), dz and the far-point scale max(rmax, dz).
+struct CutTubeRec {
+  TubeRec t;
+  double n0x, n0y, n0z, d0, n1x, n1y, n1z, d1;
+  double dz, maxVal, pad0, pad1;
+};
 
 // Boolean subtraction record (VecGeom/volumes/BooleanStruct.h:19-33): operand placed-volume ids.
 struct BoolRec {

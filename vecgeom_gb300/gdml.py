@@ -173,6 +173,10 @@ class _Reader:
                 s = g.add_polycone(sphi, dphi, z, rmin, rmax)
             else:
                 s = g.add_polyhedron(sphi, dphi, self._int(n, "numsides"), z, rmin, rmax)
+        elif tag == "cutTube":
+            # Middleware::processCutTube: the normals' components are read as lengths
+            s = g.add_cut_tube(ln("rmin"), ln("rmax"), ln("z") / 2.0, an("startphi"), an("deltaphi"),
+                               (ln("lowX"), ln("lowY"), ln("lowZ")), (ln("highX"), ln("highY"), ln("highZ")))
         elif tag == "torus":
             s = g.add_torus2(ln("rmin"), ln("rmax"), ln("rtor"), an("startphi"), an("deltaphi"))
         elif tag == "trd":

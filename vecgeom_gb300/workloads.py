@@ -250,6 +250,28 @@ def build_trap_ring(geo, n_phi=16, radius=300.0, z_rings=(-120.0, 0.0, 120.0), c
     return world
 
 
+def build_cut_tube_ring(geo, n_phi=12, radius=300.0, close=True):
+    """Cut tubes in a 1.2 m box: a ring of hollow pipes along z with tilted end cuts, each
+    holding a box in its wall, rotated about z to face the centre; a phi-section cut tube
+    in the middle. Tests the cut tube kernels inside the navigator."""
+    world_lv = geo.add_logical_volume(geo.add_box(600.0, 600.0, 400.0))
+    pipe_lv = geo.add_logical_volume(geo.add_cut_tube(20.0, 40.0, 150.0, 0.0, TWO_PI, (0.0, -0.3, -1.0),
+                                                      (0.2, 0.0, 1.0)))
+    bar_lv = geo.add_logical_volume(geo.add_box(5.0, 5.0, 40.0))
+    geo.place_daughter(pipe_lv, bar_lv, (30.0, 0.0, 0.0))
+    for j in range(n_phi):
+        ph = TWO_PI * j / n_phi
+        geo.place_daughter(world_lv, pipe_lv, (radius * math.cos(ph), radius * math.sin(ph), 0.0), rot_z(ph))
+    mid_lv = geo.add_logical_volume(geo.add_cut_tube(50.0, 100.0, 80.0, 0.3, 2.0, (0.1, 0.1, -1.0),
+                                                     (-0.2, 0.05, 1.0)))
+    geo.place_daughter(world_lv, mid_lv)
+    world = geo.place(world_lv)
+    geo.set_world(world)
+    if close:
+        geo.close()
+    return world
+
+
 def tracks_in_cylinder(n, seed, rmax=30.0, halfz=500.0):
     """Config 3 track starts: uniform in the cylinder r < rmax, |z| < halfz, isotropic."""
     g = rng(seed, 5)
