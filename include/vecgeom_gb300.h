@@ -50,6 +50,7 @@ extern "C" {
 #define VG_SHAPE_BOOLEAN_SUBTRACTION 8
 #define VG_SHAPE_TRAPEZOID 9
 #define VG_SHAPE_CUT_TUBE 10
+#define VG_SHAPE_SPHERE 11
 
 /* Precision flags for queries and navigation */
 #define VG_PREC_FP64 0u  /* plain FP64: results identical to the reference's FP64 path          */
@@ -123,6 +124,11 @@ int32_t vg_geom_add_trap_corners(vg_geom *g, const double *corners);
  * -X, +X): planes[16] = (a, b, c, d) of each plane in that order. Mirrors any trapezoid
  * bit-exactly, whichever constructor made it. */
 int32_t vg_geom_add_trap_planes(vg_geom *g, double dz, const double *planes);
+/* UnplacedSphere(rmin, rmax, sphi, dphi, stheta, dtheta), angles in radians
+ * (VecGeom/volumes/UnplacedSphere.h:40-45, source/UnplacedSphere.cpp:31-37): a spherical
+ * shell section; the angles are checked and wrapped as SphereStruct.h:96-170 does. */
+int32_t vg_geom_add_sphere(vg_geom *g, double rmin, double rmax, double sphi, double dphi, double stheta,
+                           double dtheta);
 /* UnplacedCutTube(rmin, rmax, dz, sphi, dphi, bx, by, bz, tx, ty, tz)
  * (VecGeom/volumes/UnplacedCutTube.h:54-70): a tube section between two cut planes through
  * (0, 0, -dz) and (0, 0, +dz) with outward normals (bx, by, bz), bz < 0, and (tx, ty, tz),

@@ -114,6 +114,9 @@ class OracleGeometry:
     def add_boolean_subtraction(self, left_pv, right_pv):
         return self._shape(8, [left_pv, right_pv])
 
+    def add_sphere(self, rmin, rmax, sphi=0.0, dphi=2 * np.pi, stheta=0.0, dtheta=np.pi):
+        return self._shape(12, [rmin, rmax, sphi, dphi, stheta, dtheta])
+
     def add_cut_tube(self, rmin, rmax, dz, sphi, dphi, bottom_normal, top_normal):
         return self._shape(11, [rmin, rmax, dz, sphi, dphi, *bottom_normal, *top_normal])
 

@@ -89,6 +89,52 @@ struct BooleanMinus : UnplacedShape {
   void Extent(Vec3 &lo, Vec3 &hi) const override;
 };
 
+// VecGeom/volumes/ThetaCone_Evolution.h: the theta range [sTheta, sTheta + dTheta] of a
+// sphere as two cones about the z axis.
+struct ThetaCone {
+  double fSTheta, fDTheta, kAngTol, halfAngTol, fETheta, tanSTheta, tanETheta, tanBisector, slope1, slope2,
+      tanSTheta2, tanETheta2;
+  ThetaCone() {}
+  ThetaCone(double sTheta, double dTheta);
+  bool IsOnSurfaceGeneric(Vec3 const &p, bool start) const;
+  Vec3 GetNormal(Vec3 const &p, bool start) const;
+  bool IsPointOnSurfaceAndMovingOut(Vec3 const &p, Vec3 const &d, bool start, bool movingOut) const;
+  bool IsCompletelyInside(Vec3 const &p) const;
+  bool IsCompletelyOutside(Vec3 const &p) const;
+  bool Contains(Vec3 const &p) const { return !IsCompletelyOutside(p); }
+  double DistanceToLine(double slope, double x, double y) const;
+  double SafetyToIn(Vec3 const &p) const;
+  double SafetyToOut(Vec3 const &p) const;
+  void DistanceToIn(Vec3 const &p, Vec3 const &d, double &d1, double &d2, bool &i1, bool &i2) const;
+  void DistanceToOut(Vec3 const &p, Vec3 const &d, double &d1, double &d2, bool &i1, bool &i2) const;
+};
+
+// VecGeom/volumes/SphereStruct.h, VecGeom/volumes/SphereUtilities.h,
+// VecGeom/volumes/kernel/SphereImplementation.h, source/UnplacedSphere.cpp.
+struct Sphere : UnplacedShape {
+  double fRmin, fRmax, fSPhi, fDPhi, fSTheta, fDTheta, eTheta;
+  bool fFullPhiSphere = true, fFullThetaSphere = true, fFullSphere = true;
+  Wedge fPhiWedge;
+  ThetaCone fThetaCone;
+  Sphere(double rmin, double rmax, double sphi, double dphi, double stheta, double dtheta);
+  // Wedge_Evolution.h:236-245 IsPointOnSurfaceAndMovingOut, :391-432 DistanceToIn / DistanceToOut
+  bool WedgeOnSurfaceMoving(Vec3 const &p, Vec3 const &d, bool start, bool movingOut) const;
+  void WedgeDistanceToIn(Vec3 const &p, Vec3 const &d, double &d1, double &d2) const;
+  void WedgeDistanceToOut(Vec3 const &p, Vec3 const &d, double &d1, double &d2) const;
+  void ContainsAndInside(Vec3 const &p, bool forInside, bool &cin, bool &cout) const;
+  bool IsCompletelyInside(Vec3 const &p) const;
+  bool IsCompletelyOutside(Vec3 const &p) const;
+  bool IsPointOnSurfaceAndMovingOut(Vec3 const &p, Vec3 const &d, bool movingOut) const;
+  void GetMinDistFromPhi(Vec3 const &p, Vec3 const &d, bool toIn, bool done, double &distance) const;
+  int Inside(Vec3 const &p) const override;
+  bool Contains(Vec3 const &p) const override;
+  double DistanceToIn(Vec3 const &p, Vec3 const &d, double smax) const override;
+  double DistanceToOut(Vec3 const &p, Vec3 const &d, double smax) const override;
+  double SafetyToIn(Vec3 const &p) const override;
+  double SafetyToOut(Vec3 const &p) const override;
+  void Extent(Vec3 &lo, Vec3 &hi) const override;
+};
+
 // VecGeom/volumes/Plane.h: a plane n.p + d (n unit), positive on the outside.
 struct CutPlane {
   Vec3 n;

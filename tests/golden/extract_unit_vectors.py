@@ -1,7 +1,7 @@
 """Extract known-answer vectors from VecGeom's shape unit tests into JSON fixtures.
 
-Reads test/unit_tests/Test{Box,Tube,Cons,Polycone,Torus2,Trd,Polyhedra,Trap}.cpp of a VecGeom source
-tree AS TEXT (nothing of it is compiled or run) and records, for every assert that checks
+Reads test/unit_tests/Test{Box,Tube,Cons,Polycone,Torus2,Trd,Polyhedra,Trap,Sphere}.cpp of a VecGeom
+source tree AS TEXT (nothing of it is compiled or run) and records, for every assert that checks
 a query result of a shape constructed in the test:
 
     shape constructor arguments, query name, point, direction, expected value, comparison
@@ -37,6 +37,12 @@ FILES = {
     "Trd": ("TestTrd.cpp", {"Trd_t": "trd"}),
     "Polyhedra": ("TestPolyhedra.cpp", {"Polyhedra_t": "polyhedron"}),
     "Trap": ("TestTrap.cpp", {"Trap_t": "trap", "vecgeom::UnplacedTrapezoid": "trap"}),
+    "Sphere": ("TestSphere.cpp", {"Sphere_t": "sphere"}),
+}
+# object-like macros of a test file, expanded textually (unparenthesised, as the
+# preprocessor does) before the file is evaluated
+MACROS = {
+    "TestSphere.cpp": [("deg", "PI / 180."), ("PI", "3.14159265358979323846")],
 }
 # unplaced shapes constructed without a label argument
 NO_LABEL = {"vecgeom::UnplacedTrapezoid"}
@@ -632,6 +638,9 @@ def main():
         path = os.path.join(root, "test", "unit_tests", fname)
         with open(path) as f:
             src = f.read()
+        for name, body in MACROS.get(fname, []):
+            src = re.sub(r"^\s*#define\s+%s\b[^\n]*$" % name, "", src, flags=re.M)
+            src = re.sub(r"\b%s\b" % name, body, src)
         ex = Extractor(types)
         ex.run(src)
         doc = {"source": "test/unit_tests/" + fname, "shapes": ex.used_shapes, "cases": ex.cases,

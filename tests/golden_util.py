@@ -8,7 +8,7 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-FILES = ["Box", "Tube", "Cons", "Polycone", "Torus2", "Trd", "Polyhedra", "Trap"]
+FILES = ["Box", "Tube", "Cons", "Polycone", "Torus2", "Trd", "Polyhedra", "Trap", "Sphere"]
 QUERY_ID = {"Inside": 0, "Contains": 1, "DistanceToIn": 2, "DistanceToOut": 3, "SafetyToIn": 4, "SafetyToOut": 5}
 APPROX_TOL = 1e-6   # kApproxEqualTolerance of test/unit_tests/ApproxEqual.h
 RANGE_DELTA = 1e-4  # DELTA of OutRange in test/unit_tests/TestCons.cpp
@@ -41,6 +41,8 @@ def add_shape(geo, spec):
         return geo.add_cone(*a[:7])
     if t == "torus2":
         return geo.add_torus2(*a[:5])
+    if t == "sphere":
+        return geo.add_sphere(*a[:6])
     if t == "trd":
         if len(a) == 4:  # Trd1 constructor (x1, x2, y, z)
             return geo.add_trd(a[0], a[1], a[2], a[2], a[3])

@@ -96,8 +96,9 @@ def test_errors_are_named(doc, msg):
 
 
 SUPPORTED_REF = ["oneBox", "oneTube", "oneConeSegment", "onePolycone", "onePolyhedron", "oneTorus", "oneTrapezoid",
-                 "oneGeneralTrapezoid", "twoBoxes", "aPosition", "aRotation", "solidSubtraction", "oneCutTube"]
-UNSUPPORTED_REF = ["oneOrb", "oneSphere", "oneParallelepiped", "solidUnion", "solidIntersection",
+                 "oneGeneralTrapezoid", "twoBoxes", "aPosition", "aRotation", "solidSubtraction", "oneCutTube",
+                 "oneSphere"]
+UNSUPPORTED_REF = ["oneOrb", "oneParallelepiped", "solidUnion", "solidIntersection",
                    "aConstant", "scaledPhysvol"]
 
 

@@ -1,5 +1,5 @@
 """The oracle against the known answers of the reference's own shape unit tests
-(test/unit_tests/Test{Box,Tube,Cons,Polycone,Torus2,Trd,Polyhedra,Trap}.cpp, extracted as text into
+(test/unit_tests/Test{Box,Tube,Cons,Polycone,Torus2,Trd,Polyhedra,Trap,Sphere}.cpp, extracted as text into
 tests/golden/unit_*.json): every extracted assert passes with the tests' own comparison.
 Soft checks (TestCons prints a mismatch instead of asserting) must pass too, except the
 ones listed in golden_util.SOFT_EXCEPTIONS, where the reference's own code path gives a

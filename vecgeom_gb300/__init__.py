@@ -39,6 +39,7 @@ assert NAVSTATE_DTYPE.itemsize == 12
 SHAPE_BOX, SHAPE_TUBE, SHAPE_CONE, SHAPE_POLYCONE, SHAPE_POLYHEDRON, SHAPE_TORUS2, SHAPE_TRD, SHAPE_BOOLMINUS = range(1, 9)
 SHAPE_TRAPEZOID = 9
 SHAPE_CUT_TUBE = 10
+SHAPE_SPHERE = 11
 
 
 class VGError(RuntimeError):
@@ -67,6 +68,7 @@ _SIGS = {
     "vg_geom_add_trap": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 11),
     "vg_geom_add_trap_corners": (ctypes.c_int32, [_c_vp, _c_dp]),
     "vg_geom_add_cut_tube": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 11),
+    "vg_geom_add_sphere": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 6),
     "vg_geom_add_trap_planes": (ctypes.c_int32, [_c_vp, ctypes.c_double, _c_dp]),
     "vg_geom_save": (ctypes.c_int, [_c_vp, ctypes.c_char_p]),
     "vg_geom_load": (ctypes.c_int, [_c_vp, ctypes.c_char_p]),
@@ -251,6 +253,10 @@ class Geometry:
         (+-+) (-++) (+++)."""
         c = np.ascontiguousarray(np.asarray(corners, dtype=np.float64).reshape(24))
         return _check(_lib.vg_geom_add_trap_corners(self._h, c.ctypes.data_as(_c_dp)), "add_trap_corners")
+
+    def add_sphere(self, rmin, rmax, sphi=0.0, dphi=2 * np.pi, stheta=0.0, dtheta=np.pi):
+        """UnplacedSphere: a spherical shell section (angles in radians)."""
+        return _check(_lib.vg_geom_add_sphere(self._h, rmin, rmax, sphi, dphi, stheta, dtheta), "add_sphere")
 
     def add_cut_tube(self, rmin, rmax, dz, sphi, dphi, bottom_normal, top_normal):
         """UnplacedCutTube: a tube section between two cut planes through (0, 0, -dz) and

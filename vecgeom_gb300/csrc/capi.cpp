@@ -335,6 +335,12 @@ int32_t vg_geom_add_trap(vg_geom *g, double dz, double theta, double phi, double
   const double p[11] = {dz, theta, phi, dy1, dx1, dx2, alpha1, dy2, dx3, dx4, alpha2};
   return add_shape(g, vg::kShapeTrap, p, 11);
 }
+int32_t vg_geom_add_sphere(vg_geom *g, double rmin, double rmax, double sphi, double dphi, double stheta,
+                           double dtheta)
+{
+  const double p[6] = {rmin, rmax, sphi, dphi, stheta, dtheta};
+  return add_shape(g, vg::kShapeSphere, p, 6);
+}
 int32_t vg_geom_add_cut_tube(vg_geom *g, double rmin, double rmax, double dz, double sphi, double dphi, double bx,
                              double by, double bz, double tx, double ty, double tz)
 {

@@ -241,6 +241,95 @@ bool make_cut_tube(const double *p, HostShape &s, std::string &err)
   return true;
 }
 
+// SphereStruct constructor (SphereStruct.h:256-276: CheckPhiAngles :160-170 / :126-158,
+// CheckThetaAngles :96-124), ThetaCone constructor (ThetaCone_Evolution.h:44-69) and
+// UnplacedSphere::Extent (source/UnplacedSphere.cpp:74-160).
+void make_sphere(const double *p, HostShape &s)
+{
+  const double pRmin = p[0], pRmax = p[1], pSPhi = p[2], pDPhi = p[3], pSTheta = p[4], pDTheta = p[5];
+  SphereRec r{};
+  r.rmin = pRmin, r.rmax = pRmax, r.sphi = pSPhi, r.dphi = pDPhi, r.stheta = pSTheta, r.dtheta = pDTheta;
+  bool fullPhi               = true;
+  const double kAngTolerance = 1e-9;
+  if (pDPhi >= 2 * kPi - kAngTolerance * 0.5) {
+    r.dphi = 2 * kPi, r.sphi = 0, fullPhi = true;
+  } else {
+    fullPhi = false;
+    if (pDPhi > 0) r.dphi = pDPhi;
+  }
+  if (!fullPhi) {
+    r.sphi = (pSPhi < 0) ? 2 * kPi - std::fmod(std::fabs(pSPhi), 2 * kPi) : std::fmod(pSPhi, 2 * kPi);
+    if (r.sphi + r.dphi > 2 * kPi) r.sphi -= 2 * kPi;
+  }
+  if (!((pSTheta < 0) || (pSTheta > kPi))) r.stheta = pSTheta;
+  if (pDTheta + pSTheta >= kPi)
+    r.dtheta = kPi - pSTheta;
+  else if (pDTheta > 0)
+    r.dtheta = pDTheta;
+  const bool fullTheta = !(r.dtheta - r.stheta < kPi);
+  r.fullPhi = fullPhi ? 1. : 0., r.fullTheta = fullTheta ? 1. : 0., r.fullSphere = (fullPhi && fullTheta) ? 1. : 0.;
+  r.eTheta = r.stheta + r.dtheta;
+  r.w      = make_wedge(pDPhi, pSPhi);
+  // the theta cone from the raw angles
+  r.tcS = pSTheta, r.tcE = pSTheta + pDTheta;
+  double ts = r.tcS, te = r.tcE;
+  if (r.tcS > kPi / 2) ts = kPi - r.tcS;
+  if (r.tcE > kPi / 2) te = kPi - r.tcE;
+  r.tanS   = std::tan(ts);
+  r.tanS2  = r.tanS * r.tanS;
+  r.tanE   = std::tan(te);
+  r.tanE2  = r.tanE * r.tanE;
+  r.tanBis = std::tan(ts + (pDTheta / 2));
+  if (r.tcS > kPi / 2 && r.tcE > kPi / 2) r.tanBis = std::tan(ts - (pDTheta / 2));
+  r.slope1 = std::tan(kPi / 2 - r.tcS);
+  r.slope2 = std::tan(kPi / 2 - r.tcE);
+  s.type   = kShapeSphere;
+  pack(s, r);
+  // Extent
+  const double rmax = r.rmax, rmin = r.rmin;
+  for (int k = 0; k < 3; ++k) s.lo[k] = -rmax, s.hi[k] = rmax;
+  const double eTheta = r.stheta + r.dtheta;
+  if (fullPhi && fullTheta) return;
+  double st1 = 0., st2 = 0.;
+  auto mx = [](double a, double b) { return a > b ? a : b; };
+  auto mn = [](double a, double b) { return a < b ? a : b; };
+  if (!fullTheta) {
+    s.hi[2] = ((r.stheta <= kPi / 2.) ? rmax : rmin) * std::cos(r.stheta);
+    s.lo[2] = ((eTheta <= kPi / 2.) ? rmin : rmax) * std::cos(eTheta);
+    st1     = std::sin(r.stheta);
+    st2     = std::sin(r.eTheta);
+    if (r.stheta <= kPi / 2.) {
+      if (eTheta < kPi / 2.) s.hi[0] = rmax * st2, s.lo[0] = -rmax * st2, s.hi[1] = rmax * st2, s.lo[1] = -rmax * st2;
+    } else {
+      s.hi[0] = rmax * st1, s.lo[0] = -rmax * st1, s.hi[1] = rmax * st1, s.lo[1] = -rmax * st1;
+    }
+  }
+  if (!fullPhi) {
+    double Rmax = rmax;
+    if (r.stheta > kPi / 2.) Rmax *= st1;
+    if (eTheta < kPi / 2.) Rmax *= st2;
+    const double Rmin    = rmin * mn(st1, st2);
+    const double Rin     = 0.5 * (Rmax + Rmin);
+    const bool phi0out   = !wedge_contains(r.w, Rin, 0), phi90out = !wedge_contains(r.w, 0, Rin);
+    const bool phi180out = !wedge_contains(r.w, -Rin, 0), phi270out = !wedge_contains(r.w, 0, -Rin);
+    if (!(phi0out || phi90out || phi180out || phi270out)) return;
+    const double Cx = Rmax * std::cos(r.sphi), Dx = Rmax * std::cos(r.sphi + r.dphi);
+    const double Cy = Rmax * std::sin(r.sphi), Dy = Rmax * std::sin(r.sphi + r.dphi);
+    if (phi0out) s.hi[0] = mx(Cx, Dx);
+    if (phi90out) s.hi[1] = mx(Cy, Dy);
+    if (phi180out) s.lo[0] = mn(Cx, Dx);
+    if (phi270out) s.lo[1] = mn(Cy, Dy);
+    if (r.dphi >= kPi) return;
+    const double Ax = Rmin * std::cos(r.sphi), Bx = Rmin * std::cos(r.sphi + r.dphi);
+    const double Ay = Rmin * std::sin(r.sphi), By = Rmin * std::sin(r.sphi + r.dphi);
+    double t;
+    t = mx(Ax, Bx), s.hi[0] = t > s.hi[0] ? t : s.hi[0];
+    t = mx(Ay, By), s.hi[1] = t > s.hi[1] ? t : s.hi[1];
+    t = mn(Ax, Bx), s.lo[0] = t < s.lo[0] ? t : s.lo[0];
+    t = mn(Ay, By), s.lo[1] = t < s.lo[1] ? t : s.lo[1];
+  }
+}
+
 // ConeStruct constructor, SetAndCheck{D,S}PhiAngle and CalculateCached (ConeStruct.h:85-336)
 void make_cone(const double *p, HostShape &s)
 {
@@ -813,6 +902,10 @@ int32_t Geometry::add_shape(int32_t type, const double *p, int np, std::string &
     break;
   case kShapeCutTube:
     if (!need(11) || !make_cut_tube(p, s, err)) return -1;
+    break;
+  case kShapeSphere:
+    if (!need(6)) return -1;
+    make_sphere(p, s);
     break;
   case kShapePolycone:
     if (!need(3) || !make_polycone(p, np, s, err)) return -1;

@@ -41,6 +41,7 @@ VG_OPS(TrdRec, trd)
 VG_OPS(TrapRec, trap)
 VG_OPS(TorusRec, torus)
 VG_OPS(CutTubeRec, cuttube)
+VG_OPS(SphereRec, sphere)
 #undef VG_OPS
 
 // Q: 0 Inside, 1 Contains, 2 DistanceToIn, 3 DistanceToOut, 4 SafetyToIn, 5 SafetyToOut.
@@ -272,6 +273,7 @@ cudaError_t launch_shape_query_fp64(int type, const double *rec, const Xform &xf
   case kShapeTrap: return launch_typed<TrapRec>(rec, xf, apply_xf, lbd, q, a, s);
   case kShapeTorus2: return launch_typed<TorusRec>(rec, xf, apply_xf, lbd, q, a, s);
   case kShapeCutTube: return launch_typed<CutTubeRec>(rec, xf, apply_xf, lbd, q, a, s);
+  case kShapeSphere: return launch_typed<SphereRec>(rec, xf, apply_xf, lbd, q, a, s);
   default: return cudaErrorNotSupported;
   }
 }

@@ -25,6 +25,7 @@ enum ShapeType : int32_t {
   kShapeBoolMinus  = 8,
   kShapeTrap       = 9,
   kShapeCutTube    = 10,
+  kShapeSphere     = 11,
 };
 
 // VecGeom/base/Math.h:27-52 (double precision)
@@ -138,6 +139,16 @@ struct CutTubeRec {
   TubeRec t;
   double n0x, n0y, n0z, d0, n1x, n1y, n1z, d1;
   double dz, maxVal, pad0, pad1;
+};
+
+// Sphere (VecGeom/volumes/SphereStruct.h:20-276): radii and the checked angles, the full-
+// phi / full-theta flags, the phi wedge and the theta cone (ThetaCone_Evolution.h:21-69)
+// made from the constructor's raw angles, as the reference makes them.
+struct SphereRec {
+  double rmin, rmax, sphi, dphi, stheta, dtheta, eTheta;
+  double fullPhi, fullTheta, fullSphere; // 0 or 1
+  WedgeRec w;
+  double tcS, tcE, tanS, tanE, tanS2, tanE2, tanBis, slope1, slope2, pad0;
 };
 
 // Boolean subtraction record (VecGeom/volumes/BooleanStruct.h:19-33): operand placed-volume ids.

@@ -173,6 +173,9 @@ class _Reader:
                 s = g.add_polycone(sphi, dphi, z, rmin, rmax)
             else:
                 s = g.add_polyhedron(sphi, dphi, self._int(n, "numsides"), z, rmin, rmax)
+        elif tag == "sphere":
+            s = g.add_sphere(ln("rmin"), ln("rmax"), an("startphi"), an("deltaphi"), an("starttheta"),
+                             an("deltatheta"))
         elif tag == "cutTube":
             # Middleware::processCutTube: the normals' components are read as lengths
             s = g.add_cut_tube(ln("rmin"), ln("rmax"), ln("z") / 2.0, an("startphi"), an("deltaphi"),

@@ -250,6 +250,35 @@ def build_trap_ring(geo, n_phi=16, radius=300.0, z_rings=(-120.0, 0.0, 120.0), c
     return world
 
 
+def build_sphere_shells(geo, close=True):
+    """Spherical shells in a 1.2 m box: a hollow shell cut to a band of polar angles around
+    the equator holding a ring of boxes, a polar cap (theta 0 to 0.5 rad) and its opposite
+    cap (theta beyond pi - 0.6 rad) each holding a smaller full sphere, and a phi sector of
+    a hemisphere (theta up to pi / 2, phi 0.2 to 2.4 rad). Tests the sphere kernels (phi
+    wedge and theta cone in every regime) inside the navigator."""
+    world_lv = geo.add_logical_volume(geo.add_box(600.0, 600.0, 600.0))
+    band_lv = geo.add_logical_volume(geo.add_sphere(300.0, 380.0, 0.0, TWO_PI, 1.2, 0.74))
+    tile_lv = geo.add_logical_volume(geo.add_box(10.0, 10.0, 10.0))
+    for j in range(16):
+        ph = TWO_PI * (j + 0.5) / 16
+        geo.place_daughter(band_lv, tile_lv, (340.0 * math.cos(ph), 340.0 * math.sin(ph), 0.0), rot_z(ph))
+    geo.place_daughter(world_lv, band_lv)
+    cap_lv = geo.add_logical_volume(geo.add_sphere(150.0, 280.0, 0.0, TWO_PI, 0.0, 0.5))
+    ball_lv = geo.add_logical_volume(geo.add_sphere(0.0, 25.0))
+    geo.place_daughter(cap_lv, ball_lv, (0.0, 0.0, 220.0))
+    geo.place_daughter(world_lv, cap_lv)
+    low_lv = geo.add_logical_volume(geo.add_sphere(0.0, 280.0, 0.0, TWO_PI, math.pi - 0.6, 0.6))
+    geo.place_daughter(low_lv, ball_lv, (0.0, 0.0, -200.0))
+    geo.place_daughter(world_lv, low_lv)
+    sector_lv = geo.add_logical_volume(geo.add_sphere(30.0, 120.0, 0.2, 2.2, 0.0, 0.5 * math.pi))
+    geo.place_daughter(world_lv, sector_lv, (0.0, 0.0, 10.0))
+    world = geo.place(world_lv)
+    geo.set_world(world)
+    if close:
+        geo.close()
+    return world
+
+
 def build_cut_tube_ring(geo, n_phi=12, radius=300.0, close=True):
     """Cut tubes in a 1.2 m box: a ring of hollow pipes along z with tilted end cuts, each
     holding a box in its wall, rotated about z to face the centre; a phi-section cut tube
