@@ -51,6 +51,7 @@ extern "C" {
 #define VG_SHAPE_TRAPEZOID 9
 #define VG_SHAPE_CUT_TUBE 10
 #define VG_SHAPE_SPHERE 11
+#define VG_SHAPE_GENTRAP 12
 
 /* Precision flags for queries and navigation */
 #define VG_PREC_FP64 0u  /* plain FP64: results identical to the reference's FP64 path          */
@@ -129,6 +130,13 @@ int32_t vg_geom_add_trap_planes(vg_geom *g, double dz, const double *planes);
  * shell section; the angles are checked and wrapped as SphereStruct.h:96-170 does. */
 int32_t vg_geom_add_sphere(vg_geom *g, double rmin, double rmax, double sphi, double dphi, double stheta,
                            double dtheta);
+/* UnplacedGenTrap(verticesx[8], verticesy[8], dz) (VecGeom/volumes/UnplacedGenTrap.h:38-45,
+ * GenTrapStruct.h Initialize): a generic trapezoid (Arb8) between z = -dz (vertices 0-3)
+ * and z = +dz (vertices 4-7), lateral faces planar or twisted. Anticlockwise vertices are
+ * reordered clockwise as the reference does; shapes the reference's Initialize reports as
+ * errors (opposite orientations, crossing opposite segments, non-convex bases, dz <= 0)
+ * are rejected with VG_EINVAL. */
+int32_t vg_geom_add_gentrap(vg_geom *g, const double *vertices_x, const double *vertices_y, double dz);
 /* UnplacedCutTube(rmin, rmax, dz, sphi, dphi, bx, by, bz, tx, ty, tz)
  * (VecGeom/volumes/UnplacedCutTube.h:54-70): a tube section between two cut planes through
  * (0, 0, -dz) and (0, 0, +dz) with outward normals (bx, by, bz), bz < 0, and (tx, ty, tz),

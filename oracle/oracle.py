@@ -33,6 +33,8 @@ def load():
             "oracle_set_world": (None, [_vp, ctypes.c_int]),
             "oracle_close": (ctypes.c_int, [_vp]),
             "oracle_shape_extent": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp]),
+            "oracle_shape_normal": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp]),
+            "oracle_gentrap_valid": (ctypes.c_int, [_dp, _dp, ctypes.c_double]),
             "oracle_placed_query": (ctypes.c_double, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_size_t] + [_vp] * 6 +
                                     [ctypes.c_double, _vp, _vp, ctypes.c_int]),
             "oracle_nav_table_words": (ctypes.c_size_t, [_vp]),
@@ -116,6 +118,25 @@ class OracleGeometry:
 
     def add_sphere(self, rmin, rmax, sphi=0.0, dphi=2 * np.pi, stheta=0.0, dtheta=np.pi):
         return self._shape(12, [rmin, rmax, sphi, dphi, stheta, dtheta])
+
+    def add_gentrap(self, vertices_x, vertices_y, dz):
+        """GenTrap (UnplacedGenTrap): x and y of the eight vertices (four at -dz, then four
+        at +dz) and the half-length dz."""
+        return self._shape(13, [*vertices_x, *vertices_y, dz])
+
+    @staticmethod
+    def gentrap_valid(vertices_x, vertices_y, dz):
+        """Whether the reference's GenTrapStruct::Initialize accepts these vertices."""
+        ax, px = _d(vertices_x)
+        ay, py = _d(vertices_y)
+        return bool(load().oracle_gentrap_valid(px, py, dz))
+
+    def shape_normal(self, shape, p):
+        """VUnplacedVolume::Normal at p (shape frame): (normal, valid)."""
+        n = np.zeros(3)
+        a, pp = _d(p)
+        ok = _lib.oracle_shape_normal(self._h, shape, pp, n.ctypes.data_as(_dp))
+        return n, bool(ok)
 
     def add_cut_tube(self, rmin, rmax, dz, sphi, dphi, bottom_normal, top_normal):
         return self._shape(11, [rmin, rmax, dz, sphi, dphi, *bottom_normal, *top_normal])

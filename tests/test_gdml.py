@@ -81,6 +81,19 @@ def test_attribute_values_follow_stod_and_constants():
     assert hi[2] == 5.0
 
 
+def test_arb8_reads_vertices_without_the_length_unit():
+    """Middleware::processGenTrap reads v1x..v8y as plain numbers and dz with the length unit."""
+    doc = """<gdml><solids>
+      <arb8 name="g" v1x="-3" v1y="-3" v2x="-3" v2y="3" v3x="3" v3y="3" v4x="3" v4y="-3"
+            v5x="-2" v5y="-2" v6x="-2" v6y="2" v7x="2" v7y="2" v8x="2" v8y="-2" dz="5" lunit="cm"/>
+      </solids><structure><volume name="w"><solidref ref="g"/></volume></structure>
+      <setup><world ref="w"/></setup></gdml>"""
+    for geo in (OracleGeometry(), HostOnly(vg.Geometry())):
+        r = gdml.load(doc, geo)
+        lo, hi = geo.shape_extent(r.solids["g"])
+        assert np.array_equal(lo, (-3.0, -3.0, -50.0)) and np.array_equal(hi, (3.0, 3.0, 50.0))
+
+
 @pytest.mark.parametrize("doc, msg", [
     ("<gdml><solids><orb name='o' r='1'/></solids></gdml>", "unsupported solid <orb>"),
     ("<gdml><solids><box name='b' x='1' y='1' z='1'/><box name='b' x='2' y='1' z='1'/></solids></gdml>",
@@ -100,6 +113,15 @@ SUPPORTED_REF = ["oneBox", "oneTube", "oneConeSegment", "onePolycone", "onePolyh
                  "oneSphere"]
 UNSUPPORTED_REF = ["oneOrb", "oneParallelepiped", "solidUnion", "solidIntersection",
                    "aConstant", "scaledPhysvol"]
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_GDMLS), reason="no VecGeom source tree")
+def test_reference_arb8_file_with_duplicate_solid_name():
+    """oneArbitraryTrapezoid.gdml names two solids "world" (a trd and the arb8): the reference's
+    middleware fails the second insertion and its Load returns false
+    (persistency/gdml/source/src/Middleware.cpp:643-647, :206-211); the reader raises."""
+    with pytest.raises(gdml.GDMLError, match="defined twice"):
+        gdml.load(os.path.join(REF_GDMLS, "oneArbitraryTrapezoid.gdml"), OracleGeometry())
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_GDMLS), reason="no VecGeom source tree")

@@ -47,7 +47,7 @@ def test_kernels_match_reference_unit_tests(cuda, name):
         cols = [p[:, k].copy() for k in range(3)] + ([d[:, k].copy() for k in range(3)] if qi in (2, 3) else [])
         ref, _ = o.query(opv, qi, *cols)
         for c, v in zip(cs, got):
-            if not G.passes(c["kind"], v, c["expected"], c.get("tol")) and not G.excepted(name, c):
+            if not G.case_passes(name, c, v):
                 fails.append((c["line"], shape, q, c["expected"], float(v)))
         if qi in (0, 1):
             bad = got.astype(np.int64) != ref.astype(np.int64)

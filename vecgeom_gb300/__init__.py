@@ -40,6 +40,7 @@ SHAPE_BOX, SHAPE_TUBE, SHAPE_CONE, SHAPE_POLYCONE, SHAPE_POLYHEDRON, SHAPE_TORUS
 SHAPE_TRAPEZOID = 9
 SHAPE_CUT_TUBE = 10
 SHAPE_SPHERE = 11
+SHAPE_GENTRAP = 12
 
 
 class VGError(RuntimeError):
@@ -69,6 +70,7 @@ _SIGS = {
     "vg_geom_add_trap_corners": (ctypes.c_int32, [_c_vp, _c_dp]),
     "vg_geom_add_cut_tube": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 11),
     "vg_geom_add_sphere": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 6),
+    "vg_geom_add_gentrap": (ctypes.c_int32, [_c_vp, _c_dp, _c_dp, ctypes.c_double]),
     "vg_geom_add_trap_planes": (ctypes.c_int32, [_c_vp, ctypes.c_double, _c_dp]),
     "vg_geom_save": (ctypes.c_int, [_c_vp, ctypes.c_char_p]),
     "vg_geom_load": (ctypes.c_int, [_c_vp, ctypes.c_char_p]),
@@ -257,6 +259,14 @@ class Geometry:
     def add_sphere(self, rmin, rmax, sphi=0.0, dphi=2 * np.pi, stheta=0.0, dtheta=np.pi):
         """UnplacedSphere: a spherical shell section (angles in radians)."""
         return _check(_lib.vg_geom_add_sphere(self._h, rmin, rmax, sphi, dphi, stheta, dtheta), "add_sphere")
+
+    def add_gentrap(self, vertices_x, vertices_y, dz):
+        """UnplacedGenTrap: x and y of the eight vertices (four at -dz, then four at +dz) and
+        the half-length dz; faces planar or twisted."""
+        vx = np.ascontiguousarray(np.asarray(vertices_x, dtype=np.float64).reshape(8))
+        vy = np.ascontiguousarray(np.asarray(vertices_y, dtype=np.float64).reshape(8))
+        return _check(_lib.vg_geom_add_gentrap(self._h, vx.ctypes.data_as(_c_dp), vy.ctypes.data_as(_c_dp), dz),
+                      "add_gentrap")
 
     def add_cut_tube(self, rmin, rmax, dz, sphi, dphi, bottom_normal, top_normal):
         """UnplacedCutTube: a tube section between two cut planes through (0, 0, -dz) and

@@ -341,6 +341,14 @@ int32_t vg_geom_add_sphere(vg_geom *g, double rmin, double rmax, double sphi, do
   const double p[6] = {rmin, rmax, sphi, dphi, stheta, dtheta};
   return add_shape(g, vg::kShapeSphere, p, 6);
 }
+int32_t vg_geom_add_gentrap(vg_geom *g, const double *vertices_x, const double *vertices_y, double dz)
+{
+  if (!vertices_x || !vertices_y) return fail(VG_EINVAL, "null vertex array");
+  double p[17];
+  for (int i = 0; i < 8; ++i) p[i] = vertices_x[i], p[8 + i] = vertices_y[i];
+  p[16] = dz;
+  return add_shape(g, vg::kShapeGenTrap, p, 17);
+}
 int32_t vg_geom_add_cut_tube(vg_geom *g, double rmin, double rmax, double dz, double sphi, double dphi, double bx,
                              double by, double bz, double tx, double ty, double tz)
 {

@@ -241,6 +241,130 @@ bool make_cut_tube(const double *p, HostShape &s, std::string &err)
   return true;
 }
 
+// GenTrapStruct::Initialize (GenTrapStruct.h) and SecondOrderSurfaceShell<4>::Initialize
+// (SecondOrderSurfaceShell.h). The record is the object the reference's device holds:
+// UnplacedGenTrap::CopyToGpu (source/UnplacedGenTrap.cpp:343-357) builds it again from the
+// host's vertices, which Initialize has already put in clockwise order. The shapes the
+// reference's Initialize reports as errors (and keeps half-built) are rejected here.
+bool make_gentrap(const double *p, HostShape &s, std::string &err)
+{
+  double vx[8], vy[8];
+  for (int i = 0; i < 8; ++i) vx[i] = p[i], vy[i] = p[8 + i];
+  const double dz = p[16];
+  if (!(dz > 0.)) {
+    err = "Half-length of generic trapezoid must be positive";
+    return false;
+  }
+  // orientation: signed doubled areas of both bases, accumulated edge by edge
+  double sum1 = 0., sum2 = 0.;
+  for (int i = 0; i < 4; ++i) {
+    const int j = (i + 1) % 4;
+    sum1 += vx[i] * vy[j] - vx[j] * vy[i];
+    sum2 += vx[i + 4] * vy[j + 4] - vx[j + 4] * vy[i + 4];
+  }
+  if (sum1 * sum2 < -kTolerance) {
+    err = "generic trap defined with opposite clockwise";
+    return false;
+  }
+  if (sum1 > kTolerance) { // anticlockwise: swap vertices 1 <-> 3 and 5 <-> 7
+    std::swap(vx[1], vx[3]), std::swap(vy[1], vy[3]);
+    std::swap(vx[5], vx[7]), std::swap(vy[5], vy[7]);
+  }
+  GenTrapRec r{};
+  for (int i = 0; i < 8; ++i) r.vx[i] = vx[i], r.vy[i] = vy[i];
+  for (int i = 0; i < 4; ++i) {
+    const int j     = (i + 1) % 4;
+    r.deltax[i]     = vx[j] - vx[i];
+    r.deltax[i + 4] = vx[j + 4] - vx[i + 4];
+    r.deltay[i]     = vy[j] - vy[i];
+    r.deltay[i + 4] = vy[j + 4] - vy[i + 4];
+  }
+  // SegmentsCrossing on the z = -dz / +dz vertices: both parameters strictly inside (0, 1)
+  auto crossing = [&](int a, int a1, int b, int b1) {
+    const double za = a < 4 ? -dz : dz, zb = b < 4 ? -dz : dz;
+    const double r0 = vx[a1] - vx[a], r1 = vy[a1] - vy[a], r2 = (a1 < 4 ? -dz : dz) - za;
+    const double s0 = vx[b1] - vx[b], s1 = vy[b1] - vy[b], s2 = (b1 < 4 ? -dz : dz) - zb;
+    const double c0 = r1 * s2 - r2 * s1, c1 = r2 * s0 - r0 * s2, c2 = r0 * s1 - r1 * s0;
+    if (c0 * c0 + c1 * c1 + c2 * c2 < kTolerance) return false;
+    const double q0 = vx[b] - vx[a], q1 = vy[b] - vy[a];
+    const double t  = (q0 * s1 - q1 * s0) / c2;
+    if (t < kTolerance || t > 1. - kTolerance) return false;
+    const double u = (q0 * r1 - q1 * r0) / c2;
+    if (u < kTolerance || u > 1. - kTolerance) return false;
+    return true;
+  };
+  if (crossing(0, 1, 3, 2) || crossing(1, 2, 0, 3) || crossing(4, 5, 7, 6) || crossing(5, 6, 4, 7)) {
+    err = "generic trap defined with crossing opposite segments";
+    return false;
+  }
+  for (int i = 0; i < 4; ++i) { // ComputeIsConvexQuadrilaterals
+    const int j = (i + 1) % 4;
+    if (r.deltax[i] * r.deltay[j] - r.deltay[i] * r.deltax[j] > kTolerance ||
+        r.deltax[i + 4] * r.deltay[j + 4] - r.deltay[i + 4] * r.deltax[j + 4] > kTolerance) {
+      err = "generic trap defined with top/bottom quadrilaterals not convex";
+      return false;
+    }
+  }
+  r.dz = dz, r.invDz = 1. / dz, r.halfInvDz = 0.5 / dz, r.dz2 = 0.5 / dz;
+  auto cross3 = [](const double *a, const double *b, double *c) {
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+  };
+  for (int i = 0; i < 4; ++i) {
+    const int j   = (i + 1) % 4;
+    r.connx[i]    = vx[i] - vx[i + 4];
+    r.conny[i]    = vy[i] - vy[i + 4];
+    const bool dg = std::fabs(vx[i] - vx[j]) < kTolerance && std::fabs(vy[i] - vy[j]) < kTolerance &&
+                    std::fabs(vx[i + 4] - vx[j + 4]) < kTolerance && std::fabs(vy[i + 4] - vy[j + 4]) < kTolerance;
+    if (dg) r.degenerated |= 1LL << i;
+    const double xa = vx[i], ya = vy[i], xb = vx[i + 4], yb = vy[i + 4];
+    const double xc = vx[j], yc = vy[j], xd = vx[j + 4], yd = vy[j + 4];
+    r.tx1[i]       = r.dz2 * (xb - xa);
+    r.ty1[i]       = r.dz2 * (yb - ya);
+    r.tx2[i]       = r.dz2 * (xd - xc);
+    r.ty2[i]       = r.dz2 * (yd - yc);
+    r.t1crosst2[i] = r.tx1[i] * r.ty2[i] - r.tx2[i] * r.ty1[i];
+    r.deltatx[i]   = r.tx2[i] - r.tx1[i];
+    r.deltaty[i]   = r.ty2[i] - r.ty1[i];
+    // vi = b - a, hi0 = c - a, vj = d - c, hi1 = d - b (z components from +-dz)
+    const double vi[3] = {xb - xa, yb - ya, dz - (-dz)}, hi0[3] = {xc - xa, yc - ya, -dz - (-dz)};
+    const double vj[3] = {xd - xc, yd - yc, dz - (-dz)}, hi1[3] = {xd - xb, yd - yb, dz - dz};
+    double n[3];
+    cross3(vi, hi0, n);
+    if (n[0] * n[0] + n[1] * n[1] + n[2] * n[2] < kTolerance) {
+      cross3(vi, hi1, n);
+      if (n[0] * n[0] + n[1] * n[1] + n[2] * n[2] < kTolerance) n[0] = 0., n[1] = 0., n[2] = 1.;
+    }
+    const double inv = 1. / std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    for (int k = 0; k < 3; ++k) r.normal[i][k] = n[k] * inv;
+    cross3(vi, hi0, r.viCrossHi0[i]);
+    cross3(vi, vj, r.viCrossVj[i]);
+    cross3(hi1, hi0, r.hi1CrossHi0[i]);
+    const bool flat = (std::fabs(xc - xa) < kTolerance && std::fabs(yc - ya) < kTolerance) ||
+                      (std::fabs(xd - xb) < kTolerance && std::fabs(yd - yb) < kTolerance) ||
+                      std::fabs((xc - xa) * (yd - yb) - (xd - xb) * (yc - ya)) < kTolerance;
+    if (!flat) r.curved |= 1LL << i;
+  }
+  r.planar = r.curved == 0;
+  // GenTrapStruct::Extent over the eight vertices, then ComputeBoundingBox
+  double lo[3] = {vx[0], vy[0], -dz}, hi[3] = {vx[0], vy[0], dz};
+  for (int i = 0; i < 8; ++i) {
+    if (lo[0] > vx[i]) lo[0] = vx[i];
+    if (hi[0] < vx[i]) hi[0] = vx[i];
+    if (lo[1] > vy[i]) lo[1] = vy[i];
+    if (hi[1] < vy[i]) hi[1] = vy[i];
+  }
+  for (int k = 0; k < 3; ++k) {
+    r.bborig[k] = 0.5 * (lo[k] + hi[k]);
+    r.bbdim[k]  = 0.5 * (hi[k] - lo[k]);
+    s.lo[k] = lo[k], s.hi[k] = hi[k];
+  }
+  s.type = kShapeGenTrap;
+  pack(s, r);
+  return true;
+}
+
 // SphereStruct constructor (SphereStruct.h:256-276: CheckPhiAngles :160-170 / :126-158,
 // CheckThetaAngles :96-124), ThetaCone constructor (ThetaCone_Evolution.h:44-69) and
 // UnplacedSphere::Extent (source/UnplacedSphere.cpp:74-160).
@@ -906,6 +1030,9 @@ int32_t Geometry::add_shape(int32_t type, const double *p, int np, std::string &
   case kShapeSphere:
     if (!need(6)) return -1;
     make_sphere(p, s);
+    break;
+  case kShapeGenTrap:
+    if (!need(17) || !make_gentrap(p, s, err)) return -1;
     break;
   case kShapePolycone:
     if (!need(3) || !make_polycone(p, np, s, err)) return -1;

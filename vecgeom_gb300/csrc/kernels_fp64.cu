@@ -42,6 +42,7 @@ VG_OPS(TrapRec, trap)
 VG_OPS(TorusRec, torus)
 VG_OPS(CutTubeRec, cuttube)
 VG_OPS(SphereRec, sphere)
+VG_OPS(GenTrapRec, gentrap)
 #undef VG_OPS
 
 // Q: 0 Inside, 1 Contains, 2 DistanceToIn, 3 DistanceToOut, 4 SafetyToIn, 5 SafetyToOut.
@@ -274,6 +275,7 @@ cudaError_t launch_shape_query_fp64(int type, const double *rec, const Xform &xf
   case kShapeTorus2: return launch_typed<TorusRec>(rec, xf, apply_xf, lbd, q, a, s);
   case kShapeCutTube: return launch_typed<CutTubeRec>(rec, xf, apply_xf, lbd, q, a, s);
   case kShapeSphere: return launch_typed<SphereRec>(rec, xf, apply_xf, lbd, q, a, s);
+  case kShapeGenTrap: return launch_typed<GenTrapRec>(rec, xf, apply_xf, lbd, q, a, s);
   default: return cudaErrorNotSupported;
   }
 }

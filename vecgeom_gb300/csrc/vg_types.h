@@ -26,6 +26,7 @@ enum ShapeType : int32_t {
   kShapeTrap       = 9,
   kShapeCutTube    = 10,
   kShapeSphere     = 11,
+  kShapeGenTrap    = 12,
 };
 
 // VecGeom/base/Math.h:27-52 (double precision)
@@ -149,6 +150,25 @@ struct SphereRec {
   double fullPhi, fullTheta, fullSphere; // 0 or 1
   WedgeRec w;
   double tcS, tcE, tanS, tanE, tanS2, tanE2, tanBis, slope1, slope2, pad0;
+};
+
+// Generic trapezoid (VecGeom/volumes/GenTrapStruct.h with its SecondOrderSurfaceShell<4>,
+// SecondOrderSurfaceShell.h): the eight vertices in the clockwise order the reference keeps
+// (bottom 0-3 at -dz, top 4-7 at +dz), the bounding box, the section terms of the struct
+// and the shell's per-surface terms. Surface i runs from vertex i to vertex (i+1)%4 (and
+// their tops): fxa = vx[i], fxb = vx[i+4], fxc = vx[j], fxd = vx[j+4].
+struct GenTrapRec {
+  double bbdim[3], bborig[3];
+  double vx[8], vy[8];
+  double dz, invDz, halfInvDz, dz2; // dz2 = 0.5 / dz (the shell's fDz2)
+  double connx[4], conny[4];        // vx[i] - vx[i+4]
+  double deltax[8], deltay[8];      // edge vectors of the bottom (0-3) and top (4-7) polygons
+  double tx1[4], ty1[4], tx2[4], ty2[4], t1crosst2[4], deltatx[4], deltaty[4];
+  double normal[4][3], viCrossHi0[4][3], viCrossVj[4][3], hi1CrossHi0[4][3];
+  long long degenerated; // bit i: edge i collapsed on both bases (struct and shell agree)
+  long long curved;      // bit i: surface i is twisted (SecondOrderSurfaceShell fiscurved)
+  long long planar;      // no surface twisted (the shell's fisplanar)
+  long long pad;
 };
 
 // Boolean subtraction record (VecGeom/volumes/BooleanStruct.h:19-33): operand placed-volume ids.

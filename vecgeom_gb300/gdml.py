@@ -180,6 +180,12 @@ class _Reader:
             # Middleware::processCutTube: the normals' components are read as lengths
             s = g.add_cut_tube(ln("rmin"), ln("rmax"), ln("z") / 2.0, an("startphi"), an("deltaphi"),
                                (ln("lowX"), ln("lowY"), ln("lowZ")), (ln("highX"), ln("highY"), ln("highZ")))
+        elif tag == "arb8":
+            # Middleware::processGenTrap: the vertex coordinates are read without the length
+            # unit (DECLAREANDGETPLAINVAR), dz with it; dz is the half-length
+            vx = [self._double(n, "v%dx" % k) for k in range(1, 9)]
+            vy = [self._double(n, "v%dy" % k) for k in range(1, 9)]
+            s = g.add_gentrap(vx, vy, ln("dz"))
         elif tag == "torus":
             s = g.add_torus2(ln("rmin"), ln("rmax"), ln("rtor"), an("startphi"), an("deltaphi"))
         elif tag == "trd":

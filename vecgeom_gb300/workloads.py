@@ -301,6 +301,57 @@ def build_cut_tube_ring(geo, n_phi=12, radius=300.0, close=True):
     return world
 
 
+# GenTrap vertex sets (x of the eight vertices, y of the eight, half-length): four at -dz,
+# then four at +dz.
+GENTRAPS = {
+    # planar faces (a trapezoid-like box tapering in x and y), clockwise
+    "planar": ([-40.0, -40.0, 40.0, 40.0, -30.0, -30.0, 30.0, 30.0],
+               [-20.0, 20.0, 20.0, -20.0, -15.0, 15.0, 15.0, -15.0], 100.0),
+    # the top square turned against the bottom one: all four faces twisted
+    "twisted": ([-30.0, -30.0, 30.0, 30.0, -25.0, -35.0, 25.0, 35.0],
+                [-30.0, 30.0, 30.0, -30.0, -35.0, 25.0, 35.0, -25.0], 80.0),
+    # one twisted face and three planar ones (the unit test's trap2 shape scaled by 10)
+    "one_twisted": ([-30.0, -30.0, 30.0, 30.0, -20.0, -20.0, 20.0, 20.0],
+                    [-30.0, 30.0, 30.0, -30.0, -19.0, 20.0, 20.0, -20.0], 50.0),
+    # triangular bases: edge 1 collapsed on both (a degenerated face)
+    "triangle": ([-20.0, 0.0, 0.0, 20.0, -10.0, 0.0, 0.0, 10.0],
+                 [-20.0, 25.0, 25.0, -20.0, -10.0, 12.0, 12.0, -10.0], 50.0),
+    # the top collapsed to a point (a pyramid)
+    "pyramid": ([-25.0, -25.0, 25.0, 25.0, 0.0, 0.0, 0.0, 0.0],
+                [-25.0, 25.0, 25.0, -25.0, 0.0, 0.0, 0.0, 0.0], 40.0),
+    # given anticlockwise: the constructor reorders it
+    "anticlockwise": ([-35.0, 35.0, 35.0, -35.0, -30.0, 30.0, 30.0, -30.0],
+                      [-35.0, -35.0, 35.0, 35.0, -25.0, -25.0, 25.0, 25.0], 30.0),
+}
+
+
+def build_gentrap_ring(geo, close=True):
+    """Generic trapezoids in a 1.2 m box: a ring of eight twisted cells (r = 300 mm), six
+    planar cells (r = 150 mm) each holding a box, a triangular-base cell above the centre, a
+    pyramid below it, a one-twisted-face cell and an anticlockwise-given cell at the centre.
+    Tests the GenTrap kernels (planar and twisted faces, degenerated edges) inside the
+    navigator."""
+    world_lv = geo.add_logical_volume(geo.add_box(600.0, 600.0, 400.0))
+    lv = {k: geo.add_logical_volume(geo.add_gentrap(*v)) for k, v in GENTRAPS.items()}
+    bar_lv = geo.add_logical_volume(geo.add_box(10.0, 5.0, 40.0))
+    geo.place_daughter(lv["planar"], bar_lv)
+    for j in range(8):
+        ph = TWO_PI * (j + 0.5) / 8
+        geo.place_daughter(world_lv, lv["twisted"], (300.0 * math.cos(ph), 300.0 * math.sin(ph), 0.0), rot_z(ph))
+    for j in range(6):
+        ph = TWO_PI * j / 6
+        geo.place_daughter(world_lv, lv["planar"], (150.0 * math.cos(ph), 150.0 * math.sin(ph), 0.0), rot_z(ph))
+    geo.place_daughter(world_lv, lv["triangle"], (0.0, 0.0, 200.0))
+    geo.place_daughter(world_lv, lv["pyramid"], (0.0, 0.0, -200.0))
+    geo.place_daughter(world_lv, lv["one_twisted"], (0.0, 0.0, 90.0))
+    geo.place_daughter(world_lv, lv["anticlockwise"], (0.0, 0.0, -40.0))
+    world = geo.place(world_lv)
+    geo.set_world(world)
+    if close:
+        geo.close()
+    return world
+
+
 def tracks_in_cylinder(n, seed, rmax=30.0, halfz=500.0):
     """Config 3 track starts: uniform in the cylinder r < rmax, |z| < halfz, isotropic."""
     g = rng(seed, 5)
