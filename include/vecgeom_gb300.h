@@ -52,6 +52,7 @@ extern "C" {
 #define VG_SHAPE_CUT_TUBE 10
 #define VG_SHAPE_SPHERE 11
 #define VG_SHAPE_GENTRAP 12
+#define VG_SHAPE_HYPE 13
 
 /* Precision flags for queries and navigation */
 #define VG_PREC_FP64 0u  /* plain FP64: results identical to the reference's FP64 path          */
@@ -130,6 +131,11 @@ int32_t vg_geom_add_trap_planes(vg_geom *g, double dz, const double *planes);
  * shell section; the angles are checked and wrapped as SphereStruct.h:96-170 does. */
 int32_t vg_geom_add_sphere(vg_geom *g, double rmin, double rmax, double sphi, double dphi, double stheta,
                            double dtheta);
+/* UnplacedHype(rmin, rmax, stIn, stOut, dz) (VecGeom/volumes/UnplacedHype.h:55-61): a tube whose
+ * inner and outer surfaces are hyperboloids r^2 = rmin^2 + tan^2(stIn) z^2 and
+ * r^2 = rmax^2 + tan^2(stOut) z^2, |z| <= dz; stereo angles in radians. Like the reference,
+ * the parameters are not checked. */
+int32_t vg_geom_add_hype(vg_geom *g, double rmin, double rmax, double stereo_in, double stereo_out, double dz);
 /* UnplacedGenTrap(verticesx[8], verticesy[8], dz) (VecGeom/volumes/UnplacedGenTrap.h:38-45,
  * GenTrapStruct.h Initialize): a generic trapezoid (Arb8) between z = -dz (vertices 0-3)
  * and z = +dz (vertices 4-7), lateral faces planar or twisted. Anticlockwise vertices are

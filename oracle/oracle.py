@@ -119,6 +119,11 @@ class OracleGeometry:
     def add_sphere(self, rmin, rmax, sphi=0.0, dphi=2 * np.pi, stheta=0.0, dtheta=np.pi):
         return self._shape(12, [rmin, rmax, sphi, dphi, stheta, dtheta])
 
+    def add_hype(self, rmin, rmax, stereo_in, stereo_out, dz):
+        """Hype (UnplacedHype): inner and outer radius at z = 0, inner and outer stereo angles
+        (radians) and the half-length dz."""
+        return self._shape(14, [rmin, rmax, stereo_in, stereo_out, dz])
+
     def add_gentrap(self, vertices_x, vertices_y, dz):
         """GenTrap (UnplacedGenTrap): x and y of the eight vertices (four at -dz, then four
         at +dz) and the half-length dz."""

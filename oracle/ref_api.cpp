@@ -45,7 +45,8 @@ void oracle_geom_destroy(void *g) { delete static_cast<Geometry *>(g); }
 // type: 1 Box, 2 Tube, 3 Cone, 4 Polycone, 5 Polyhedron, 6 Torus2, 7 Trd, 8 BooleanSubtraction,
 // 10 BooleanUnion (oracle only), 11 CutTube (rmin, rmax, dz, sphi, dphi, bottom normal, top
 // normal), 12 Sphere (rmin, rmax, sphi, dphi, stheta, dtheta), 13 GenTrap (x of the eight
-// vertices, their y, dz), 9 Trapezoid (11 parameters, 24 = eight corners x, y, z, or 17 = dz and four planes a, b, c, d)
+// vertices, their y, dz), 14 Hype (rmin, rmax, inner stereo angle, outer stereo angle, dz),
+// 9 Trapezoid (11 parameters, 24 = eight corners x, y, z, or 17 = dz and four planes a, b, c, d)
 int oracle_add_shape(void *gp, int type, const double *p, int np)
 {
   Geometry *g = static_cast<Geometry *>(gp);
@@ -73,6 +74,7 @@ int oracle_add_shape(void *gp, int type, const double *p, int np)
     if (np != 17) return -1;
     s = new GenTrap(p, p + 8, p[16]);
     break;
+  case 14: s = new Hype(p[0], p[1], p[2], p[3], p[4]); break;
   case 11: s = new CutTube(p[0], p[1], p[2], p[3], p[4], Vec3(p[5], p[6], p[7]), Vec3(p[8], p[9], p[10])); break;
   case 9:
     if (np == 24) {

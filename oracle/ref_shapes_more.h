@@ -191,6 +191,35 @@ struct GenTrap : UnplacedShape {
   void Extent(Vec3 &lo, Vec3 &hi) const override;
 };
 
+// VecGeom/volumes/HypeStruct.h (CalculateCached), VecGeom/volumes/HypeUtilities.h,
+// VecGeom/volumes/kernel/HypeImplementation.h with the UniversalHype treatment
+// (shapetypes/HypeTypes.h: the inner surface is treated when rmin > 0 or the inner stereo
+// angle is not 0) and the scalar HypeHelpers specialisation (the one the CUDA build runs).
+struct Hype : UnplacedShape {
+  double fRmin, fRmax, fStIn, fStOut, fDz;
+  double fTIn, fTOut, fTIn2, fTOut2, fRmin2, fRmax2, fDz2;
+  double fEndInnerRadius2, fEndOuterRadius2, fEndInnerRadius, fEndOuterRadius;
+  double zToleranceLevel, innerRadToleranceLevel, outerRadToleranceLevel;
+  bool fInner;
+  Hype(double rmin, double rmax, double stIn, double stOut, double dz);
+  void ContainsAndInside(Vec3 const &p, bool forInside, bool &cin, bool &cout) const;
+  bool IsCompletelyInside(Vec3 const &p) const;
+  bool IsCompletelyOutside(Vec3 const &p) const;
+  bool OnSurfaceMovingInside(Vec3 const &p, Vec3 const &d) const;
+  bool OnSurfaceMovingOutside(Vec3 const &p, Vec3 const &d) const;
+  bool OnOuterSurfaceMovingOutside(Vec3 const &p, Vec3 const &d) const;
+  bool OnInnerSurfaceMovingOutside(Vec3 const &p, Vec3 const &d) const;
+  bool ZPlaneIntersection(Vec3 const &p, Vec3 const &d, bool forDistToIn, double &zDist) const;
+  bool HyperbolicIntersection(Vec3 const &p, Vec3 const &d, bool forDistToIn, bool inner, double &dist) const;
+  int Inside(Vec3 const &p) const override;
+  bool Contains(Vec3 const &p) const override;
+  double DistanceToIn(Vec3 const &p, Vec3 const &d, double smax) const override;
+  double DistanceToOut(Vec3 const &p, Vec3 const &d, double smax) const override;
+  double SafetyToIn(Vec3 const &p) const override;
+  double SafetyToOut(Vec3 const &p) const override;
+  void Extent(Vec3 &lo, Vec3 &hi) const override;
+};
+
 // VecGeom/volumes/Plane.h: a plane n.p + d (n unit), positive on the outside.
 struct CutPlane {
   Vec3 n;

@@ -8,7 +8,7 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-FILES = ["Box", "Tube", "Cons", "Polycone", "Torus2", "Trd", "Polyhedra", "Trap", "Sphere", "GenTrap"]
+FILES = ["Box", "Tube", "Cons", "Polycone", "Torus2", "Trd", "Polyhedra", "Trap", "Sphere", "GenTrap", "Hype"]
 QUERY_ID = {"Inside": 0, "Contains": 1, "DistanceToIn": 2, "DistanceToOut": 3, "SafetyToIn": 4, "SafetyToOut": 5}
 APPROX_TOL = 1e-6   # kApproxEqualTolerance of test/unit_tests/ApproxEqual.h
 RANGE_DELTA = 1e-4  # DELTA of OutRange in test/unit_tests/TestCons.cpp
@@ -93,6 +93,8 @@ def add_shape(geo, spec):
         return geo.add_sphere(*a[:6])
     if t == "gentrap":
         return geo.add_gentrap(a[0], a[1], a[2])
+    if t == "hype":
+        return geo.add_hype(*a[:5])
     if t == "trd":
         if len(a) == 4:  # Trd1 constructor (x1, x2, y, z)
             return geo.add_trd(a[0], a[1], a[2], a[2], a[3])
@@ -136,6 +138,8 @@ def approx_equal(x, y):
 
 def passes(kind, actual, expected, tol=None):
     a, e = float(actual), float(expected)
+    if kind == "any":  # one side of a comparison between two query results (doc["pairs"])
+        return True
     if kind == "absdiff":  # std::fabs(actual - expected) < tol
         return abs(a - e) < tol
     if kind == "approx":

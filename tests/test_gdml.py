@@ -94,6 +94,20 @@ def test_arb8_reads_vertices_without_the_length_unit():
         assert np.array_equal(lo, (-3.0, -3.0, -50.0)) and np.array_equal(hi, (3.0, 3.0, 50.0))
 
 
+def test_hype_reads_stereo_angles_without_the_angle_unit():
+    """Middleware::processHype reads inst and outst as plain numbers (radians whatever aunit
+    says), the radii and z with the length unit; z is the full length."""
+    doc = """<gdml><solids>
+      <hype name="h" rmin="1" rmax="2" inst="0.5" outst="0.25" z="10" lunit="cm" aunit="deg"/>
+      </solids><structure><volume name="w"><solidref ref="h"/></volume></structure>
+      <setup><world ref="w"/></setup></gdml>"""
+    for geo in (OracleGeometry(), HostOnly(vg.Geometry())):
+        r = gdml.load(doc, geo)
+        lo, hi = geo.shape_extent(r.solids["h"])
+        rmax = math.sqrt(20.0 ** 2 + math.tan(0.25) ** 2 * 50.0 ** 2)
+        assert np.allclose(hi, (rmax, rmax, 50.0), rtol=1e-15)
+
+
 @pytest.mark.parametrize("doc, msg", [
     ("<gdml><solids><orb name='o' r='1'/></solids></gdml>", "unsupported solid <orb>"),
     ("<gdml><solids><box name='b' x='1' y='1' z='1'/><box name='b' x='2' y='1' z='1'/></solids></gdml>",
@@ -110,7 +124,7 @@ def test_errors_are_named(doc, msg):
 
 SUPPORTED_REF = ["oneBox", "oneTube", "oneConeSegment", "onePolycone", "onePolyhedron", "oneTorus", "oneTrapezoid",
                  "oneGeneralTrapezoid", "twoBoxes", "aPosition", "aRotation", "solidSubtraction", "oneCutTube",
-                 "oneSphere"]
+                 "oneSphere", "oneHyperbolicTube"]
 UNSUPPORTED_REF = ["oneOrb", "oneParallelepiped", "solidUnion", "solidIntersection",
                    "aConstant", "scaledPhysvol"]
 

@@ -1,5 +1,5 @@
 """The oracle against the known answers of the reference's own shape unit tests
-(test/unit_tests/Test{Box,Tube,Cons,Polycone,Torus2,Trd,Polyhedra,Trap,Sphere,GenTrap}.cpp, extracted as
+(test/unit_tests/Test{Box,Tube,Cons,Polycone,Torus2,Trd,Polyhedra,Trap,Sphere,GenTrap,Hype}.cpp, extracted as
 text into tests/golden/unit_*.json): every extracted assert passes with the tests' own
 comparison, except the few golden_util lists with the reason (rounding-only misses of the
 reference's generic kernels, print-only checks its own code fails).
@@ -66,6 +66,23 @@ def test_normals_match_reference_unit_tests(name):
         o = OracleGeometry()
         n, valid = o.shape_normal(G.add_shape(o, doc["shapes"][c["shape"]]), c["p"])
         assert valid and G.approx_equal_vec(n, c["expected"]), (c["line"], n, c["expected"])
+
+
+@pytest.mark.parametrize("name", [n for n in G.FILES if G.load(n).get("pairs")])
+def test_paired_results_match_reference_unit_tests(name):
+    """Asserts comparing two query results with each other (TestHype: ApproxEqual(Dist3, Dist4))."""
+    from oracle.oracle import OracleGeometry
+    doc = G.load(name)
+    for pair in doc["pairs"]:
+        vals = []
+        for k in (pair["a"], pair["b"]):
+            c = doc["cases"][k]
+            o = OracleGeometry()
+            pv = G.build(o, doc["shapes"][c["shape"]])
+            qi = G.QUERY_ID[c["query"]]
+            cols = [np.array([v]) for v in c["p"]] + ([np.array([v]) for v in c["d"]] if qi in (2, 3) else [])
+            vals.append(float(o.query(pv, qi, *cols)[0][0]))
+        assert G.approx_equal(*vals), (pair["line"], vals)
 
 
 def test_pin_detects_a_planted_error():

@@ -35,17 +35,19 @@ def _gdml(geo):
 
 GEOMETRIES = {"barrel": W.build_barrel, "detector": W.build_detector, "trap_ring": W.build_trap_ring,
               "gdml_detector": _gdml, "cut_tube_ring": W.build_cut_tube_ring,
-              "sphere_shells": W.build_sphere_shells, "gentrap_ring": W.build_gentrap_ring}
+              "sphere_shells": W.build_sphere_shells, "gentrap_ring": W.build_gentrap_ring,
+              "hype_ring": W.build_hype_ring}
 # full-track cross-checks per geometry (the config-4 detector's brute force is the slowest),
 # and the half-lengths of the box in which restarting tracks start (about the world's)
 TRACKS = {"barrel": 1 << 16, "detector": 1 << 13, "trap_ring": 1 << 16, "gdml_detector": 1 << 16,
-          "cut_tube_ring": 1 << 16, "sphere_shells": 1 << 16, "gentrap_ring": 1 << 16}
+          "cut_tube_ring": 1 << 16, "sphere_shells": 1 << 16, "gentrap_ring": 1 << 16, "hype_ring": 1 << 16}
 # primaries whose transport histories give at least 2^16 pre-step states
 PRIMARIES = {"barrel": 16384, "detector": 2048, "trap_ring": 1 << 16, "gdml_detector": 32768,
-             "cut_tube_ring": 1 << 16, "sphere_shells": 1 << 15, "gentrap_ring": 1 << 16}
+             "cut_tube_ring": 1 << 16, "sphere_shells": 1 << 15, "gentrap_ring": 1 << 16, "hype_ring": 1 << 16}
 HALF = {"barrel": (2000.0, 2000.0, 3000.0), "detector": (2000.0, 2000.0, 3000.0), "trap_ring": (600.0, 600.0, 400.0),
         "gdml_detector": (1500.0, 1500.0, 2000.0), "cut_tube_ring": (600.0, 600.0, 400.0),
-        "sphere_shells": (600.0, 600.0, 600.0), "gentrap_ring": (600.0, 600.0, 400.0)}
+        "sphere_shells": (600.0, 600.0, 600.0), "gentrap_ring": (600.0, 600.0, 400.0),
+        "hype_ring": (600.0, 600.0, 400.0)}
 
 
 @pytest.fixture(scope="module", params=sorted(GEOMETRIES))

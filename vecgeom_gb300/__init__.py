@@ -41,6 +41,7 @@ SHAPE_TRAPEZOID = 9
 SHAPE_CUT_TUBE = 10
 SHAPE_SPHERE = 11
 SHAPE_GENTRAP = 12
+SHAPE_HYPE = 13
 
 
 class VGError(RuntimeError):
@@ -71,6 +72,7 @@ _SIGS = {
     "vg_geom_add_cut_tube": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 11),
     "vg_geom_add_sphere": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 6),
     "vg_geom_add_gentrap": (ctypes.c_int32, [_c_vp, _c_dp, _c_dp, ctypes.c_double]),
+    "vg_geom_add_hype": (ctypes.c_int32, [_c_vp] + [ctypes.c_double] * 5),
     "vg_geom_add_trap_planes": (ctypes.c_int32, [_c_vp, ctypes.c_double, _c_dp]),
     "vg_geom_save": (ctypes.c_int, [_c_vp, ctypes.c_char_p]),
     "vg_geom_load": (ctypes.c_int, [_c_vp, ctypes.c_char_p]),
@@ -259,6 +261,11 @@ class Geometry:
     def add_sphere(self, rmin, rmax, sphi=0.0, dphi=2 * np.pi, stheta=0.0, dtheta=np.pi):
         """UnplacedSphere: a spherical shell section (angles in radians)."""
         return _check(_lib.vg_geom_add_sphere(self._h, rmin, rmax, sphi, dphi, stheta, dtheta), "add_sphere")
+
+    def add_hype(self, rmin, rmax, stereo_in, stereo_out, dz):
+        """UnplacedHype: radii at z = 0 of the inner and outer hyperboloids, their stereo
+        angles (radians) and the half-length dz."""
+        return _check(_lib.vg_geom_add_hype(self._h, rmin, rmax, stereo_in, stereo_out, dz), "add_hype")
 
     def add_gentrap(self, vertices_x, vertices_y, dz):
         """UnplacedGenTrap: x and y of the eight vertices (four at -dz, then four at +dz) and

@@ -341,6 +341,11 @@ int32_t vg_geom_add_sphere(vg_geom *g, double rmin, double rmax, double sphi, do
   const double p[6] = {rmin, rmax, sphi, dphi, stheta, dtheta};
   return add_shape(g, vg::kShapeSphere, p, 6);
 }
+int32_t vg_geom_add_hype(vg_geom *g, double rmin, double rmax, double stereo_in, double stereo_out, double dz)
+{
+  const double p[5] = {rmin, rmax, stereo_in, stereo_out, dz};
+  return add_shape(g, vg::kShapeHype, p, 5);
+}
 int32_t vg_geom_add_gentrap(vg_geom *g, const double *vertices_x, const double *vertices_y, double dz)
 {
   if (!vertices_x || !vertices_y) return fail(VG_EINVAL, "null vertex array");

@@ -8,6 +8,7 @@
 #include "shapes_polyhedron_fp64.cuh"
 #include "shapes_sphere_fp64.cuh"
 #include "shapes_gentrap_fp64.cuh"
+#include "shapes_hype_fp64.cuh"
 
 namespace vg {
 
@@ -35,6 +36,7 @@ __device__ __forceinline__ const R &rec_at(const DevGeom &g, int off)
   case kShapeCutTube: return cuttube_##FN(rec_at<CutTubeRec>(g, off), __VA_ARGS__);             \
   case kShapeSphere: return sphere_##FN(rec_at<SphereRec>(g, off), __VA_ARGS__);                \
   case kShapeGenTrap: return gentrap_##FN(rec_at<GenTrapRec>(g, off), __VA_ARGS__);             \
+  case kShapeHype: return hype_##FN(rec_at<HypeRec>(g, off), __VA_ARGS__);                      \
   case kShapePolycone: return polycone_##FN(rec_at<PolyconeRec>(g, off), __VA_ARGS__);          \
   case kShapePolyhedron: return polyhedron_##FN(rec_at<PolyhedronRec>(g, off), __VA_ARGS__);    \
   case kShapeTorus2: return torus_##FN(rec_at<TorusRec>(g, off), __VA_ARGS__);                  \

@@ -365,6 +365,34 @@ bool make_gentrap(const double *p, HostShape &s, std::string &err)
   return true;
 }
 
+// HypeStruct::CalculateCached (VecGeom/volumes/HypeStruct.h:49-75) and UnplacedHype::Extent
+// (source/UnplacedHype.cpp:94-100).
+void make_hype(const double *p, HostShape &s)
+{
+  HypeRec h{};
+  h.rmin = p[0], h.rmax = p[1], h.stIn = p[2], h.stOut = p[3], h.dz = p[4];
+  h.tIn             = std::tan(h.stIn);
+  h.tOut            = std::tan(h.stOut);
+  h.tIn2            = h.tIn * h.tIn;
+  h.tOut2           = h.tOut * h.tOut;
+  h.rmin2           = h.rmin * h.rmin;
+  h.rmax2           = h.rmax * h.rmax;
+  h.dz2             = h.dz * h.dz;
+  h.endInnerRadius2 = h.tIn2 * h.dz2 + h.rmin2;
+  h.endOuterRadius2 = h.tOut2 * h.dz2 + h.rmax2;
+  h.endInnerRadius  = std::sqrt(h.endInnerRadius2);
+  h.endOuterRadius  = std::sqrt(h.endOuterRadius2);
+  h.zTol            = kTolerance * h.dz;
+  h.innerTol        = kTolerance * h.endInnerRadius;
+  h.outerTol        = kTolerance * h.endOuterRadius;
+  h.inner           = (h.rmin > 0. || h.stIn != 0.) ? 1. : 0.;
+  s.type            = kShapeHype;
+  pack(s, h);
+  const double r = h.endOuterRadius;
+  s.lo[0] = -r, s.lo[1] = -r, s.lo[2] = -h.dz;
+  s.hi[0] = r, s.hi[1] = r, s.hi[2] = h.dz;
+}
+
 // SphereStruct constructor (SphereStruct.h:256-276: CheckPhiAngles :160-170 / :126-158,
 // CheckThetaAngles :96-124), ThetaCone constructor (ThetaCone_Evolution.h:44-69) and
 // UnplacedSphere::Extent (source/UnplacedSphere.cpp:74-160).
@@ -1033,6 +1061,10 @@ int32_t Geometry::add_shape(int32_t type, const double *p, int np, std::string &
     break;
   case kShapeGenTrap:
     if (!need(17) || !make_gentrap(p, s, err)) return -1;
+    break;
+  case kShapeHype:
+    if (!need(5)) return -1;
+    make_hype(p, s);
     break;
   case kShapePolycone:
     if (!need(3) || !make_polycone(p, np, s, err)) return -1;

@@ -43,6 +43,7 @@ VG_OPS(TorusRec, torus)
 VG_OPS(CutTubeRec, cuttube)
 VG_OPS(SphereRec, sphere)
 VG_OPS(GenTrapRec, gentrap)
+VG_OPS(HypeRec, hype)
 #undef VG_OPS
 
 // Q: 0 Inside, 1 Contains, 2 DistanceToIn, 3 DistanceToOut, 4 SafetyToIn, 5 SafetyToOut.
@@ -276,6 +277,7 @@ cudaError_t launch_shape_query_fp64(int type, const double *rec, const Xform &xf
   case kShapeCutTube: return launch_typed<CutTubeRec>(rec, xf, apply_xf, lbd, q, a, s);
   case kShapeSphere: return launch_typed<SphereRec>(rec, xf, apply_xf, lbd, q, a, s);
   case kShapeGenTrap: return launch_typed<GenTrapRec>(rec, xf, apply_xf, lbd, q, a, s);
+  case kShapeHype: return launch_typed<HypeRec>(rec, xf, apply_xf, lbd, q, a, s);
   default: return cudaErrorNotSupported;
   }
 }

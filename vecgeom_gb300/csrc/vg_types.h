@@ -27,6 +27,7 @@ enum ShapeType : int32_t {
   kShapeCutTube    = 10,
   kShapeSphere     = 11,
   kShapeGenTrap    = 12,
+  kShapeHype       = 13,
 };
 
 // VecGeom/base/Math.h:27-52 (double precision)
@@ -169,6 +170,16 @@ struct GenTrapRec {
   long long curved;      // bit i: surface i is twisted (SecondOrderSurfaceShell fiscurved)
   long long planar;      // no surface twisted (the shell's fisplanar)
   long long pad;
+};
+
+// Hyperboloid (VecGeom/volumes/HypeStruct.h:19-80, CalculateCached): radii at z = 0, stereo
+// angles, the half-length and the cached squares, end-cap radii and tolerance levels;
+// `inner` is InnerSurfaceExists (rmin > 0 or a non-zero inner stereo angle).
+struct HypeRec {
+  double rmin, rmax, stIn, stOut, dz;
+  double tIn, tOut, tIn2, tOut2, rmin2, rmax2, dz2;
+  double endInnerRadius2, endOuterRadius2, endInnerRadius, endOuterRadius;
+  double zTol, innerTol, outerTol, inner;
 };
 
 // Boolean subtraction record (VecGeom/volumes/BooleanStruct.h:19-33): operand placed-volume ids.

@@ -180,6 +180,10 @@ class _Reader:
             # Middleware::processCutTube: the normals' components are read as lengths
             s = g.add_cut_tube(ln("rmin"), ln("rmax"), ln("z") / 2.0, an("startphi"), an("deltaphi"),
                                (ln("lowX"), ln("lowY"), ln("lowZ")), (ln("highX"), ln("highY"), ln("highZ")))
+        elif tag == "hype":
+            # Middleware::processHype: the stereo angles are read without the angle unit
+            # (DECLAREANDGETPLAINVAR), z is the full length
+            s = g.add_hype(ln("rmin"), ln("rmax"), self._double(n, "inst"), self._double(n, "outst"), ln("z") / 2.0)
         elif tag == "arb8":
             # Middleware::processGenTrap: the vertex coordinates are read without the length
             # unit (DECLAREANDGETPLAINVAR), dz with it; dz is the half-length

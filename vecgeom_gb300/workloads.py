@@ -352,6 +352,37 @@ def build_gentrap_ring(geo, close=True):
     return world
 
 
+# Hyperboloids (rmin, rmax, inner stereo angle, outer stereo angle, dz)
+HYPES = {
+    "hollow": (20.0, 40.0, 0.3, 0.5, 100.0),   # both surfaces hyperbolic
+    "solid": (0.0, 30.0, 0.0, 0.7, 60.0),      # no inner surface
+    "cylinder_in": (15.0, 35.0, 0.0, 0.4, 50.0),  # inner surface a cylinder
+    "cone_in": (0.0, 40.0, 0.5, 0.6, 50.0),    # inner surface a double cone (rmin 0)
+}
+
+
+def build_hype_ring(geo, close=True):
+    """Hyperboloids in a 1.2 m box: a ring of six hollow hyperboloids (r = 250 mm) each
+    holding a box in its wall, and along the axis a solid one, one with a cylindrical inner
+    surface and one whose inner surface is a double cone. Tests the Hype kernels inside the
+    navigator."""
+    world_lv = geo.add_logical_volume(geo.add_box(600.0, 600.0, 400.0))
+    lv = {k: geo.add_logical_volume(geo.add_hype(*v)) for k, v in HYPES.items()}
+    bar_lv = geo.add_logical_volume(geo.add_box(4.0, 4.0, 20.0))
+    geo.place_daughter(lv["hollow"], bar_lv, (30.0, 0.0, 0.0))
+    for j in range(6):
+        ph = TWO_PI * (j + 0.5) / 6
+        geo.place_daughter(world_lv, lv["hollow"], (250.0 * math.cos(ph), 250.0 * math.sin(ph), 0.0), rot_z(ph))
+    geo.place_daughter(world_lv, lv["solid"], (0.0, 0.0, -150.0))
+    geo.place_daughter(world_lv, lv["cylinder_in"])
+    geo.place_daughter(world_lv, lv["cone_in"], (0.0, 0.0, 150.0))
+    world = geo.place(world_lv)
+    geo.set_world(world)
+    if close:
+        geo.close()
+    return world
+
+
 def tracks_in_cylinder(n, seed, rmax=30.0, halfz=500.0):
     """Config 3 track starts: uniform in the cylinder r < rmax, |z| < halfz, isotropic."""
     g = rng(seed, 5)
