@@ -165,3 +165,38 @@ def test_scheduling_flag_errors(cuda, geo):
     small = cuda.empty(256, dtype=cuda.uint8, device="cuda:0")
     with pytest.raises(vg.VGError):  # workspace too small
         g.compute_step_and_next_volume(*dev, st, out, step, flags=vg.NAV_SORT, workspace=small)
+
+
+@pytest.mark.parametrize("flags_name", ["fp64", "mixed_sort_queue", "mixed_sort_queue_learned"])
+def test_host_entry_pipelined_chunks(cuda, flags_name):
+    """From 2^18 tracks with a sorted schedule the host-array entry point copies its inputs
+    in four chunks and computes each chunk's sort keys and proposals as it arrives; every
+    out-state, step and status equals the device entry point's (a ragged size, so the chunks
+    differ in length), and so does the unsorted plain FP64 path."""
+    import vecgeom_gb300 as vg
+    from vecgeom_gb300 import learned as L
+    from vecgeom_gb300 import workloads as W
+    flags = {"fp64": vg.PREC_FP64, "mixed_sort_queue": vg.PREC_MIXED | vg.NAV_SORT | vg.NAV_QUEUE,
+             "mixed_sort_queue_learned": vg.PREC_MIXED | vg.NAV_SORT | vg.NAV_QUEUE | vg.NAV_LEARNED}[flags_name]
+    g = vg.Geometry()
+    W.build_barrel(g)
+    model = L.Proposer(g, seed=3)  # untrained: the learned order never changes results
+    model.attach(g)
+    n = 3 * (1 << 17) + 777
+    pts, dirs = W.tracks_in_cylinder(n, seed=99)
+    dev = [cuda.from_numpy(np.ascontiguousarray(a)).to("cuda:0") for a in (*pts, *dirs)]
+    st = cuda.empty(n * 12, dtype=cuda.uint8, device="cuda:0")
+    g.locate_point(*dev[:3], st)
+    out_d = cuda.empty(n * 12, dtype=cuda.uint8, device="cuda:0")
+    step_d = cuda.empty(n, dtype=cuda.float64, device="cuda:0")
+    status_d = cuda.empty(n, dtype=cuda.int32, device="cuda:0")
+    g.compute_step_and_next_volume(*dev, st, out_d, step_d, status=status_d, flags=flags)
+    h = [np.ascontiguousarray(a) for a in (*pts, *dirs)]
+    out_h = np.empty(n * 12, dtype=np.uint8)
+    step_h = np.empty(n, dtype=np.float64)
+    status_h = np.full(n, -7, dtype=np.int32)
+    for _ in range(2):  # the second call reuses the handle's staging and streams
+        g.compute_step_and_next_volume_host(*h, st.cpu().numpy(), out_h, step_h, status=status_h, flags=flags)
+        assert np.array_equal(out_h, out_d.cpu().numpy())
+        assert np.array_equal(step_h.view(np.int64), step_d.cpu().numpy().view(np.int64))
+        assert np.array_equal(status_h, status_d.cpu().numpy())
