@@ -13,6 +13,14 @@
 namespace vg {
 
 
+// Shape types compiled into this translation unit's dispatch (bit t set: shape type t). A
+// unit built for a subset serves only geometries whose shape types all lie in it; the
+// host selects it from the geometry's type mask (DevGeom::type_mask).
+#ifndef VG_SHAPE_MASK
+#define VG_SHAPE_MASK 0xffffffffu
+#endif
+#define VG_HAS_SHAPE(t) (((VG_SHAPE_MASK) >> (t)) & 1u)
+
 #ifndef VG_INLINE_CONTAINS
 #define VG_INLINE_CONTAINS 0
 #endif
@@ -28,18 +36,18 @@ __device__ __forceinline__ const R &rec_at(const DevGeom &g, int off)
 }
 #define VG_PRIM_CASES(FN, ...)                                                                  \
   switch (type) {                                                                               \
-  case kShapeBox: return box_##FN(rec_at<BoxRec>(g, off), __VA_ARGS__);                         \
-  case kShapeTube: return tube_##FN(rec_at<TubeRec>(g, off), __VA_ARGS__);                      \
-  case kShapeCone: return cone_##FN(rec_at<ConeRec>(g, off), __VA_ARGS__);                      \
-  case kShapeTrd: return trd_##FN(rec_at<TrdRec>(g, off), __VA_ARGS__);                         \
-  case kShapeTrap: return trap_##FN(rec_at<TrapRec>(g, off), __VA_ARGS__);                      \
-  case kShapeCutTube: return cuttube_##FN(rec_at<CutTubeRec>(g, off), __VA_ARGS__);             \
-  case kShapeSphere: return sphere_##FN(rec_at<SphereRec>(g, off), __VA_ARGS__);                \
-  case kShapeGenTrap: return gentrap_##FN(rec_at<GenTrapRec>(g, off), __VA_ARGS__);             \
-  case kShapeHype: return hype_##FN(rec_at<HypeRec>(g, off), __VA_ARGS__);                      \
-  case kShapePolycone: return polycone_##FN(rec_at<PolyconeRec>(g, off), __VA_ARGS__);          \
-  case kShapePolyhedron: return polyhedron_##FN(rec_at<PolyhedronRec>(g, off), __VA_ARGS__);    \
-  case kShapeTorus2: return torus_##FN(rec_at<TorusRec>(g, off), __VA_ARGS__);                  \
+  case kShapeBox: if (VG_HAS_SHAPE(kShapeBox)) return box_##FN(rec_at<BoxRec>(g, off), __VA_ARGS__); break; \
+  case kShapeTube: if (VG_HAS_SHAPE(kShapeTube)) return tube_##FN(rec_at<TubeRec>(g, off), __VA_ARGS__); break; \
+  case kShapeCone: if (VG_HAS_SHAPE(kShapeCone)) return cone_##FN(rec_at<ConeRec>(g, off), __VA_ARGS__); break; \
+  case kShapeTrd: if (VG_HAS_SHAPE(kShapeTrd)) return trd_##FN(rec_at<TrdRec>(g, off), __VA_ARGS__); break; \
+  case kShapeTrap: if (VG_HAS_SHAPE(kShapeTrap)) return trap_##FN(rec_at<TrapRec>(g, off), __VA_ARGS__); break; \
+  case kShapeCutTube: if (VG_HAS_SHAPE(kShapeCutTube)) return cuttube_##FN(rec_at<CutTubeRec>(g, off), __VA_ARGS__); break; \
+  case kShapeSphere: if (VG_HAS_SHAPE(kShapeSphere)) return sphere_##FN(rec_at<SphereRec>(g, off), __VA_ARGS__); break; \
+  case kShapeGenTrap: if (VG_HAS_SHAPE(kShapeGenTrap)) return gentrap_##FN(rec_at<GenTrapRec>(g, off), __VA_ARGS__); break; \
+  case kShapeHype: if (VG_HAS_SHAPE(kShapeHype)) return hype_##FN(rec_at<HypeRec>(g, off), __VA_ARGS__); break; \
+  case kShapePolycone: if (VG_HAS_SHAPE(kShapePolycone)) return polycone_##FN(rec_at<PolyconeRec>(g, off), __VA_ARGS__); break; \
+  case kShapePolyhedron: if (VG_HAS_SHAPE(kShapePolyhedron)) return polyhedron_##FN(rec_at<PolyhedronRec>(g, off), __VA_ARGS__); break; \
+  case kShapeTorus2: if (VG_HAS_SHAPE(kShapeTorus2)) return torus_##FN(rec_at<TorusRec>(g, off), __VA_ARGS__); break; \
   default: break;                                                                               \
   }
 
@@ -196,7 +204,7 @@ __device__ inline bool shape_contains_to(const DevGeom &g, int type, int off, V3
 static __device__ __noinline__ bool shape_contains_to(const DevGeom &g, int type, int off, V3 p)
 #endif
 {
-  if (type == kShapeBoolMinus) return boolminus_contains(g, rec_at<BoolRec>(g, off), p);
+  if (VG_HAS_SHAPE(kShapeBoolMinus) && type == kShapeBoolMinus) return boolminus_contains(g, rec_at<BoolRec>(g, off), p);
   return prim_contains_to(g, type, off, p);
 }
 __device__ inline bool shape_contains(const DevGeom &g, int shape, V3 p)
@@ -205,7 +213,7 @@ __device__ inline bool shape_contains(const DevGeom &g, int shape, V3 p)
 }
 __device__ inline int shape_inside_to(const DevGeom &g, int type, int off, V3 p)
 {
-  if (type == kShapeBoolMinus) return boolminus_inside(g, rec_at<BoolRec>(g, off), p);
+  if (VG_HAS_SHAPE(kShapeBoolMinus) && type == kShapeBoolMinus) return boolminus_inside(g, rec_at<BoolRec>(g, off), p);
   return prim_inside_to(g, type, off, p);
 }
 __device__ inline int shape_inside(const DevGeom &g, int shape, V3 p)
@@ -214,7 +222,7 @@ __device__ inline int shape_inside(const DevGeom &g, int shape, V3 p)
 }
 __device__ inline double shape_dist_in_to(const DevGeom &g, int type, int off, V3 p, V3 d)
 {
-  if (type == kShapeBoolMinus) return boolminus_dist_in(g, rec_at<BoolRec>(g, off), p, d);
+  if (VG_HAS_SHAPE(kShapeBoolMinus) && type == kShapeBoolMinus) return boolminus_dist_in(g, rec_at<BoolRec>(g, off), p, d);
   return prim_dist_in_to(g, type, off, p, d);
 }
 __device__ inline double shape_dist_in(const DevGeom &g, int shape, V3 p, V3 d)
@@ -223,7 +231,7 @@ __device__ inline double shape_dist_in(const DevGeom &g, int shape, V3 p, V3 d)
 }
 __device__ inline double shape_dist_out_to(const DevGeom &g, int type, int off, V3 p, V3 d)
 {
-  if (type == kShapeBoolMinus) return boolminus_dist_out(g, rec_at<BoolRec>(g, off), p, d);
+  if (VG_HAS_SHAPE(kShapeBoolMinus) && type == kShapeBoolMinus) return boolminus_dist_out(g, rec_at<BoolRec>(g, off), p, d);
   return prim_dist_out_to(g, type, off, p, d);
 }
 __device__ inline double shape_dist_out(const DevGeom &g, int shape, V3 p, V3 d)
@@ -232,7 +240,7 @@ __device__ inline double shape_dist_out(const DevGeom &g, int shape, V3 p, V3 d)
 }
 __device__ inline double shape_safety_in_to(const DevGeom &g, int type, int off, V3 p)
 {
-  if (type == kShapeBoolMinus) return boolminus_safety_in(g, rec_at<BoolRec>(g, off), p);
+  if (VG_HAS_SHAPE(kShapeBoolMinus) && type == kShapeBoolMinus) return boolminus_safety_in(g, rec_at<BoolRec>(g, off), p);
   return prim_safety_in_to(g, type, off, p);
 }
 __device__ inline double shape_safety_in(const DevGeom &g, int shape, V3 p)
@@ -241,7 +249,7 @@ __device__ inline double shape_safety_in(const DevGeom &g, int shape, V3 p)
 }
 __device__ inline double shape_safety_out_to(const DevGeom &g, int type, int off, V3 p)
 {
-  if (type == kShapeBoolMinus) return boolminus_safety_out(g, rec_at<BoolRec>(g, off), p);
+  if (VG_HAS_SHAPE(kShapeBoolMinus) && type == kShapeBoolMinus) return boolminus_safety_out(g, rec_at<BoolRec>(g, off), p);
   return prim_safety_out_to(g, type, off, p);
 }
 __device__ inline double shape_safety_out(const DevGeom &g, int shape, V3 p)

@@ -1610,6 +1610,8 @@ int Geometry::upload(std::string &err)
   dev.shape_lbd   = reinterpret_cast<const float *>(P(o_lbd));
   dev.leaf_rec    = reinterpret_cast<const LeafRec *>(P(o_lrec));
   dev.pv_rec      = reinterpret_cast<const PvRec *>(P(o_pvr));
+  dev.type_mask   = 0;
+  for (const int32_t t : stype) dev.type_mask |= 1u << t;
   dev.world_pv    = world;
   dev.max_depth   = max_depth;
   dev.n_pv        = (int32_t)pvs.size();

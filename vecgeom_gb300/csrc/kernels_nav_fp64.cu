@@ -1,5 +1,5 @@
-// Plain-FP64 navigation kernels: one thread per track, LocatePoint and
-// ComputeStepAndPropagatedState. Compiled with --fmad=false. These divergent kernels are
+// Plain-FP64 navigation kernels: one thread per track, LocatePoint, ApproachNextDaughter and
+// the launcher of ComputeStepAndPropagatedState (nav_fp64_step_impl.cuh, one build per shape set). Compiled with --fmad=false. These divergent kernels are
 // latency-bound, so FP64 compares stay on the FP64 pipe and the exact shortcuts are off
 // (VG_FP64_INT_COMPARE 0, VG_FP64_SHORTCUTS 0, see fp64_int.cuh).
 #define VG_FP64_INT_COMPARE 0
@@ -7,6 +7,8 @@
 #define VG_INLINE_CONTAINS 1
 #include "launch.h"
 #include "nav_fp64.cuh"
+#define VG_NAV_SET set_all
+#include "nav_fp64_step_impl.cuh"
 
 namespace vg {
 namespace {
@@ -31,24 +33,6 @@ __global__ void __launch_bounds__(256) k_locate(const DevGeom g, const double *_
     int status = 0;
     f64::locate_global_point(g, g.world_pv, V3{__ldg(x + i), __ldg(y + i), __ldg(z + i)}, s.navInd, true, status);
     out[i] = s;
-  }
-}
-
-__global__ void __launch_bounds__(256) k_step(const DevGeom g, const StepArgs a)
-{
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
-    const size_t t   = a.order ? (size_t)__ldg(a.order + i) : i;
-    const NavState s = a.in[t];
-    NavState o;
-    int st = 0, nv = 0;
-    const double lim = a.limit ? __ldg(a.limit + t) : kInfLength;
-    a.step[t] = f64::compute_step(g, V3{__ldg(a.x + t), __ldg(a.y + t), __ldg(a.z + t)},
-                                  V3{__ldg(a.dx + t), __ldg(a.dy + t), __ldg(a.dz + t)}, lim, s, o, st,
-                                  a.nvisited ? &nv : nullptr);
-    a.out[t] = o;
-    if (a.status) a.status[t] = st;
-    if (a.nvisited) a.nvisited[t] = nv;
   }
 }
 
@@ -102,8 +86,7 @@ cudaError_t launch_locate_fp64(const DevGeom &g, const double *x, const double *
 cudaError_t launch_step_fp64(const DevGeom &g, const StepArgs &a, cudaStream_t s)
 {
   if (a.n == 0) return cudaSuccess;
-  k_step<<<grid_for(a.n, 256), 256, 0, s>>>(g, a);
-  return cudaGetLastError();
+  return core_shapes_only(g) ? set_core::launch_step_fp64(g, a, s) : set_all::launch_step_fp64(g, a, s);
 }
 
 } // namespace vg

@@ -91,6 +91,25 @@ cudaError_t launch_transport_drain(const DevGeom &g, const TransportArgs &a, boo
                                    cudaStream_t s);
 cudaError_t launch_transport_init(const NavState *st, size_t n, int32_t *nsteps, int32_t *status, uint32_t *list,
                                   unsigned int *count, cudaStream_t s);
+// Builds of the navigation kernels per shape set: set_all dispatches every shape type,
+// set_core only kCoreShapeMask (smaller step kernels). The launchers above pick the build
+// for the geometry's shape set.
+inline bool core_shapes_only(const DevGeom &g) { return (g.type_mask & ~kCoreShapeMask) == 0u; }
+#define VG_NAV_SET_DECLS                                                                                           \
+  cudaError_t launch_step_fp64(const DevGeom &g, const StepArgs &a, cudaStream_t s);                               \
+  cudaError_t launch_step_mixed_queue(const DevGeom &g, const StepArgs &a, unsigned long long *counter,             \
+                                      int blocks_per_sm, cudaStream_t s);                                          \
+  cudaError_t launch_transport_iter(const DevGeom &g, const TransportArgs &a, bool mixed,                          \
+                                    unsigned long long *counter, int blocks_per_sm, cudaStream_t s);               \
+  cudaError_t launch_transport_drain(const DevGeom &g, const TransportArgs &a, bool mixed,                         \
+                                     unsigned long long *counter, cudaStream_t s);
+namespace set_all {
+VG_NAV_SET_DECLS
+}
+namespace set_core {
+VG_NAV_SET_DECLS
+}
+#undef VG_NAV_SET_DECLS
 // Fixed scratch of the no-allocation step entry point (noalloc.cu).
 size_t noalloc_max_tracks();
 cudaError_t noalloc_scratch(void **ptr, size_t *bytes);

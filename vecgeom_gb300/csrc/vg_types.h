@@ -30,6 +30,12 @@ enum ShapeType : int32_t {
   kShapeHype       = 13,
 };
 
+// The navigator's core shape set. Navigation kernels are also compiled with the dispatch of
+// these types only (smaller code: fewer instruction-cache misses in the step kernels); the
+// host runs that build for a geometry whose shapes all lie in the set (DevGeom::type_mask).
+constexpr uint32_t kCoreShapeMask = (1u << kShapeBox) | (1u << kShapeTube) | (1u << kShapeCone) |
+                                    (1u << kShapePolycone) | (1u << kShapeTrd);
+
 // VecGeom/base/Math.h:27-52 (double precision)
 constexpr double kTolerance     = 1e-9;
 constexpr double kHalfTolerance = 0.5 * kTolerance;
@@ -271,6 +277,7 @@ struct DevGeom {
   const int32_t *lv_depth;    // BVH depth per LV (-1: no BVH)
   const int32_t *dau_slot3;   // depth-3 subtree (0..7) of each daughter slot's leaf, or -1
   const double *shape_bbox;   // 6 doubles per shape: its bounding box (Extent: lo xyz, hi xyz)
+  uint32_t type_mask;         // bit t set: the geometry holds a shape of type t
   int32_t world_pv;
   int32_t max_depth;
   int32_t n_pv;
