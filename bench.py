@@ -76,7 +76,8 @@ def parse():
                     help="autotune sort-key bits / queue occupancy before timing (untimed; 1/0)")
     ap.add_argument("--cell-bits", type=int, default=0, help="sort-key Morton bits per axis without --tune (0: default)")
     ap.add_argument("--queue-blocks", type=int, default=0,
-                    help="work-queue configuration without --tune (1: 256x1, 2: 256x2, 3: 128x3, 4: 128x5; 0: default)")
+                    help="work-queue configuration without --tune (1: 256x1, 2: 256x2, 3: 128x3, 4: 128x5; "
+                         "5-8: the same with the step split into step and relocation kernels; 0: default)")
     return ap.parse_args()
 
 
@@ -539,7 +540,7 @@ def main():
     tuning = None
     if args.tune and head & (vg.NAV_SORT | vg.NAV_QUEUE):
         from vecgeom_gb300.tune import autotune
-        cands = [(head, b, q) for b in (0, 7, 5) for q in ((1, 2, 3, 4) if head & vg.NAV_QUEUE else (1,))]
+        cands = [(head, b, q) for b in (0, 7, 5) for q in (tuple(range(1, 9)) if head & vg.NAV_QUEUE else (1,))]
         tuning = autotune(geo, t, st, candidates=cands, cache=None)
     elif args.cell_bits or args.queue_blocks:
         geo.set_tuning(args.cell_bits, args.queue_blocks)

@@ -344,8 +344,9 @@ int vg_nav_sort_key_params(const vg_geom *g, float lo[3], float scale[3], int32_
  * `queue_blocks_per_sm`, the configuration of the VG_NAV_QUEUE kernel (1: blocks of 256
  * threads, one per SM, full register budget; 2: two per SM, half the registers, twice the
  * resident warps; 3: blocks of 128 threads, three per SM, 168 registers; 4: blocks of 128
- * threads, five per SM, 20 resident warps at 102 registers; 0 = 1). Set before sorted calls
- * are in flight. */
+ * threads, five per SM, 20 resident warps at 102 registers; 5-8: the budgets of 1-4 with the
+ * step split into two kernels, the step up to the boundary and then the relocation, over
+ * the same visiting order; 0 = 1). Set before sorted calls are in flight. */
 int vg_nav_set_tuning(vg_geom *g, int32_t cell_bits, int32_t queue_blocks_per_sm);
 
 /* ---------------------------------------------------------------- learned proposal

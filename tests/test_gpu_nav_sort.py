@@ -99,8 +99,9 @@ def test_scheduling_variants_identical(cuda, geo, prec):
 
 def test_tuning_configurations_identical(cuda, geo):
     """Every work-queue configuration (256 x 1, 256 x 2, 128 x 3, 128 x 5 threads x blocks per
-    SM) and sort-key resolution gives the plain FP64 results, in the step and in the transport
-    stream; out-of-range settings are rejected."""
+    SM, fused or with the step split into a step and a relocation kernel) and sort-key
+    resolution gives the plain FP64 results, in the step and in the transport stream;
+    out-of-range settings are rejected."""
     import vecgeom_gb300 as vg
     name, g, pts, dev, st = geo
     n = dev[0].numel()
@@ -117,7 +118,7 @@ def test_tuning_configurations_identical(cuda, geo):
     sst = st[: m * 12].clone()
     ref_t = g.transport(*[d.clone() for d in sub], sst.clone(), max_steps=50, flags=vg.PREC_FP64)
     try:
-        for qb in (1, 2, 3, 4):
+        for qb in range(1, 9):
             for bits in (0, 5):
                 g.set_tuning(bits, qb)
                 got = run(vg.PREC_MIXED | vg.NAV_SORT | vg.NAV_QUEUE)
@@ -127,7 +128,7 @@ def test_tuning_configurations_identical(cuda, geo):
                                 flags=vg.PREC_MIXED | vg.NAV_SORT | vg.NAV_QUEUE)
             assert cuda.equal(got_t[0], ref_t[0]), qb
         with pytest.raises(vg.VGError):
-            g.set_tuning(0, 5)
+            g.set_tuning(0, 9)
         with pytest.raises(vg.VGError):
             g.set_tuning(11, 1)
     finally:

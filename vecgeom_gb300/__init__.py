@@ -513,7 +513,8 @@ class Geometry:
 
     def set_tuning(self, cell_bits=0, queue_blocks_per_sm=0):
         """Sort-key Morton bits per axis and the work-queue kernel configuration (1: 256 x 1,
-        2: 256 x 2, 3: 128 x 3, 4: 128 x 5 threads x blocks per SM; 0: defaults). Results do not depend
+        2: 256 x 2, 3: 128 x 3, 4: 128 x 5 threads x blocks per SM; 5-8: the same budgets with the
+        step split into a step kernel and a relocation kernel; 0: defaults). Results do not depend
         on them."""
         _check(_lib.vg_nav_set_tuning(self._h, cell_bits, queue_blocks_per_sm), "vg_nav_set_tuning")
 

@@ -20,7 +20,8 @@ struct vg_geom {
   void *staging       = nullptr;
   size_t staging_size = 0;
   vg::SortKeyParams sort{}; // set when the geometry is closed
-  int queue_blocks = 1;     // work-queue kernel configuration: 1 = 256 x 1, 2 = 256 x 2, 3 = 128 x 3, 4 = 128 x 5
+  int queue_blocks = 1;     // work-queue kernel configuration: 1 = 256 x 1, 2 = 256 x 2, 3 = 128 x 3, 4 = 128 x 5;
+                            // 5-8: the same budgets with the step split in two kernels (step, relocation)
                             // threads x resident blocks per SM
   // builder log for vg_geom_save / vg_geom_load: every successful builder call as
   // (op, arguments...) in call order, so a replay reproduces every id
@@ -802,7 +803,7 @@ int vg_nav_set_tuning(vg_geom *g, int32_t cell_bits, int32_t queue_blocks_per_sm
   if (!closed_ok(g)) return g ? VG_ESTATE : VG_EINVAL;
   if (g->geo.world < 0) return fail(VG_ESTATE, "geometry has no world volume");
   if (cell_bits < 0 || cell_bits > 10) return fail(VG_EINVAL, "cell_bits must be in [0, 10]");
-  if (queue_blocks_per_sm < 0 || queue_blocks_per_sm > 4) return fail(VG_EINVAL, "queue_blocks_per_sm must be in [0, 4]");
+  if (queue_blocks_per_sm < 0 || queue_blocks_per_sm > 8) return fail(VG_EINVAL, "queue_blocks_per_sm must be in [0, 8]");
   g->sort         = sort_params(g->geo, cell_bits);
   g->queue_blocks = queue_blocks_per_sm ? queue_blocks_per_sm : 1;
   return VG_OK;

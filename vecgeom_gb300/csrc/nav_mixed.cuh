@@ -479,20 +479,19 @@ __device__ __forceinline__ void relocate_force_different_mixed(const DevGeom &g,
   }
 }
 
-// ComputeStepAndPropagatedState with FP32 pruning (same control flow as f64::compute_step).
-__device__ __forceinline__ double compute_step_mixed(const DevGeom &g, const ShapeLB *lbs, V3 gp, V3 gd, double limit,
-                                                     NavState const &in, NavState &out, int &status, int *nvisited,
-                                                     int proposal = -1)
+// What a step leaves to its relocation (ComputeStepAndPropagatedState's last part): nothing,
+// the exit through the mother (RelocatePoint), or the entry into the daughter pushed on the
+// state (LocateGlobalPoint from it).
+enum { kRelocNone = 0, kRelocExit = 1, kRelocEnter = 2 };
+
+// ComputeStepAndPropagatedState with FP32 pruning (same control flow as f64::compute_step),
+// up to the relocation: the returned step and `out` are final unless `reloc` is set, in
+// which case relocate_after_step_mixed completes `out` (and may set `status`).
+__device__ __forceinline__ double step_before_relocation_mixed(const DevGeom &g, V3 lp, V3 ld, double limit,
+                                                               NavState const &in, NavState &out, int &status,
+                                                               int *nvisited, int proposal, int &reloc)
 {
-  out    = in;
-  status = kTrackOk;
-  if (in.navInd == 0) {
-    status = kTrackErrState;
-    return 0.;
-  }
-  const Xform m   = f64::nav_top_matrix(g, in.navInd);
-  const V3 lp     = f64::to_local(m, gp);
-  const V3 ld     = f64::rotate(m, gd);
+  reloc           = kRelocNone;
   const int pv    = f64::nav_top(g, in.navInd);
   const PvRec rec = pv_rec(g, pv);
   double step     = f64::shape_dist_out_to(g, rec.type, rec.off, lp, ld);
@@ -526,14 +525,42 @@ __device__ __forceinline__ double compute_step_mixed(const DevGeom &g, const Sha
   out.lastExited = out.navInd;
   if (hit >= 0) out.navInd = f64::nav_push(g, out.navInd, hit);
   if (dlt(step, 0.)) step = 0.;
+  reloc = hit < 0 ? kRelocExit : kRelocEnter;
+  return step;
+}
+
+// The relocation of a step: lp, ld and step as step_before_relocation_mixed saw and returned
+// them, `out` as it left it.
+__device__ __forceinline__ void relocate_after_step_mixed(const DevGeom &g, const ShapeLB *lbs, V3 lp, V3 ld,
+                                                          double step, int reloc, NavState &out, int &status)
+{
   const double s = step + 1E-6;
   const V3 after{lp.x + s * ld.x, lp.y + s * ld.y, lp.z + s * ld.z};
-  if (hit < 0) {
+  if (reloc == kRelocExit) {
     relocate_force_different_mixed(g, lbs, after, out.navInd, status);
   } else {
-    out.navInd = f64::nav_pop(g, out.navInd);
+    const int hit = f64::nav_top(g, out.navInd);
+    out.navInd    = f64::nav_pop(g, out.navInd);
     locate_global_point_mixed(g, lbs, hit, f64::to_local(g.pv_xf[hit], after), out.navInd, false, status);
   }
+}
+
+__device__ __forceinline__ double compute_step_mixed(const DevGeom &g, const ShapeLB *lbs, V3 gp, V3 gd, double limit,
+                                                     NavState const &in, NavState &out, int &status, int *nvisited,
+                                                     int proposal = -1)
+{
+  out    = in;
+  status = kTrackOk;
+  if (in.navInd == 0) {
+    status = kTrackErrState;
+    return 0.;
+  }
+  const Xform m = f64::nav_top_matrix(g, in.navInd);
+  const V3 lp   = f64::to_local(m, gp);
+  const V3 ld   = f64::rotate(m, gd);
+  int reloc;
+  const double step = step_before_relocation_mixed(g, lp, ld, limit, in, out, status, nvisited, proposal, reloc);
+  if (reloc != kRelocNone) relocate_after_step_mixed(g, lbs, lp, ld, step, reloc, out, status);
   return step;
 }
 

@@ -71,6 +71,73 @@ __global__ void __launch_bounds__(Threads, MinBlocks) k_step_mixed_queue(const D
   }
 }
 
+// Split step (queue configurations 5-8): the first kernel computes each step up to its
+// relocation and leaves the relocation code in the out-state's first pad byte; the second
+// kernel relocates those tracks over the same visiting order, recomputing the local point
+// and direction from the input state, and clears the byte. Each kernel's body is about half
+// of the fused one (fewer instruction-cache misses, its own register budget). Results are
+// those of the fused kernel: the same operations on the same values.
+__device__ __forceinline__ void step_one_mixed_split(const DevGeom &g, const StepArgs &a, size_t t)
+{
+  const NavState s = a.in[t];
+  NavState o       = s;
+  int st = kTrackOk, nv = 0, reloc = mixed::kRelocNone;
+  double step = 0.;
+  if (s.navInd == 0) {
+    st = kTrackErrState;
+  } else {
+    const double lim = a.limit ? __ldg(a.limit + t) : kInfLength;
+    const Xform m    = f64::nav_top_matrix(g, s.navInd);
+    const f64::V3 lp = f64::to_local(m, f64::V3{__ldg(a.x + t), __ldg(a.y + t), __ldg(a.z + t)});
+    const f64::V3 ld = f64::rotate(m, f64::V3{__ldg(a.dx + t), __ldg(a.dy + t), __ldg(a.dz + t)});
+    step = mixed::step_before_relocation_mixed(g, lp, ld, lim, s, o, st, a.nvisited ? &nv : nullptr,
+                                               a.proposal ? (int)__ldg(a.proposal + t) : -1, reloc);
+  }
+  o.pad[0]  = (uint8_t)reloc;
+  a.step[t] = step;
+  a.out[t]  = o;
+  if (a.status) a.status[t] = st;
+  if (a.nvisited) a.nvisited[t] = nv;
+}
+
+__device__ __forceinline__ void relocate_one_mixed(const DevGeom &g, const mixed::ShapeLB *lbs, const StepArgs &a,
+                                                   size_t t)
+{
+  NavState o = a.out[t];
+  if (o.pad[0] == mixed::kRelocNone) return;
+  const int reloc  = o.pad[0];
+  o.pad[0]         = 0;
+  const NavState s = a.in[t];
+  const Xform m    = f64::nav_top_matrix(g, s.navInd);
+  const f64::V3 lp = f64::to_local(m, f64::V3{__ldg(a.x + t), __ldg(a.y + t), __ldg(a.z + t)});
+  const f64::V3 ld = f64::rotate(m, f64::V3{__ldg(a.dx + t), __ldg(a.dy + t), __ldg(a.dz + t)});
+  int st           = kTrackOk;
+  mixed::relocate_after_step_mixed(g, lbs, lp, ld, a.step[t], reloc, o, st);
+  a.out[t] = o;
+  if (a.status) a.status[t] = st;
+}
+
+template <int Threads, int MinBlocks, bool Relocate>
+__global__ void __launch_bounds__(Threads, MinBlocks) k_step_mixed_split(const DevGeom g, const StepArgs a,
+                                                                         unsigned long long *__restrict__ counter)
+{
+  const mixed::ShapeLB *lbs = reinterpret_cast<const mixed::ShapeLB *>(g.shape_lbd);
+  const int lane            = threadIdx.x & 31;
+  for (;;) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(counter, 32ull);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= a.n) break;
+    const size_t i = (size_t)base + lane;
+    if (i >= a.n) continue;
+    const size_t t = a.order ? (size_t)__ldg(a.order + i) : i;
+    if (Relocate)
+      relocate_one_mixed(g, lbs, a, t);
+    else
+      step_one_mixed_split(g, a, t);
+  }
+}
+
 #ifdef VG_NAV_UNSCHEDULED_KERNELS
 __global__ void __launch_bounds__(256) k_locate_mixed(const DevGeom g, const double *__restrict__ x,
                                                       const double *__restrict__ y, const double *__restrict__ z,
@@ -257,6 +324,37 @@ cudaError_t launch_queue(const DevGeom &g, const StepArgs &a, unsigned long long
   return cudaGetLastError();
 }
 
+
+template <int Threads, int MinBlocks, bool Relocate>
+cudaError_t launch_split(const DevGeom &g, const StepArgs &a, unsigned long long *counter, cudaStream_t s)
+{
+  static int resident = 0;
+  if (resident == 0) {
+    int r = 0;
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &r, k_step_mixed_split<Threads, MinBlocks, Relocate>, Threads, 0);
+    if (e != cudaSuccess) return e;
+    resident = r > 0 ? r : 1;
+  }
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  size_t blocks = (size_t)sms * resident, need = (a.n + Threads - 1) / Threads;
+  if (blocks > need) blocks = need;
+  k_step_mixed_split<Threads, MinBlocks, Relocate><<<(unsigned)blocks, Threads, 0, s>>>(g, a, counter);
+  return cudaGetLastError();
+}
+
+template <int Threads, int MinBlocks>
+cudaError_t launch_queue_split(const DevGeom &g, const StepArgs &a, unsigned long long *counter, cudaStream_t s)
+{
+  cudaError_t e = launch_split<Threads, MinBlocks, false>(g, a, counter, s);
+  if (e == cudaSuccess) e = launch_split<Threads, MinBlocks, true>(g, a, counter, s);
+  return e;
+}
 
 } // namespace
 } // namespace VG_NAV_SET

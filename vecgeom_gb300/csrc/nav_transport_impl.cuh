@@ -11,6 +11,7 @@ cudaError_t launch_transport_iter(const DevGeom &g, const TransportArgs &a, bool
 {
   if (a.n == 0) return cudaSuccess;
   if (!mixed) return launch_transport<false, 256, 1>(g, a, counter, s);
+  blocks_per_sm = (blocks_per_sm - 1) % 4 + 1; // split configurations: the fused kernel of the same budget
   if (blocks_per_sm == 4) return launch_transport<true, 128, 5>(g, a, counter, s);
   if (blocks_per_sm == 3) return launch_transport<true, 128, 3>(g, a, counter, s);
   return blocks_per_sm == 2 ? launch_transport<true, 256, 2>(g, a, counter, s)
