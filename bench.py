@@ -32,15 +32,19 @@ sys.path.insert(0, ROOT)
 METRIC = "nav steps/s on 1 GB300, plain FP64 vs mixed-prec+learned order, ids identical"
 UNIT = "nav steps/s"
 STEP_BYTES = 24 + 24 + 12 + 12 + 8  # p, d, state in, state out, step (FP64 SoA + 12 B states)
-# FP64-pipe thread instructions per scheduled detector step (sort keys 3.0 + proposal 10.2 +
-# step kernel 289.4), counted by ncu (sm__thread_inst_executed_pipe_fp64_pred_on over every
-# launch of one scheduled step on 2^20 detector step inputs; the summary is under profiles/).
+# FP64-pipe thread instructions per scheduled detector step, counted by ncu
+# (sm__thread_inst_executed_pipe_fp64_pred_on over the launches of one scheduled step on 2^20
+# detector step inputs; the summaries are under profiles/): sort keys 3.0 + proposal 10.2 +
+# the step kernel(s): 289.4 fused (work-queue configurations 1-4), 279.6 + 34.5 split into
+# the step and relocation kernels (configurations 5-8, which recompute the local frame).
 # Per-thread counts do not depend on how lanes group into warps, so they hold at 2^22.
-FP64_OPS_PER_STEP = 302.6
-# DRAM bytes per launch of the step kernel in the tuned 128 x 5 configuration, from one ncu
-# capture (read 727.3 MB + write 297.5 MB per 2^20 steps, spills included), scaled to the
-# 2^22-step launch by the steps it processes.
-STEP_TRAFFIC_PER_STEP = (727.3e6 + 297.5e6) / (1 << 20)
+FP64_OPS_PER_STEP = {"fused": 3.0 + 10.2 + 289.4, "split": 3.0 + 10.2 + 279.6 + 34.5}
+# DRAM bytes per step of the step kernel launch(es) by work-queue configuration, from one ncu
+# capture each on 2^20 steps (spills included), scaled to the bench launch by its steps:
+# fused 128 x 5: read 727.3 MB + write 297.5 MB; split 256 x 2: step kernel 438.8 + 104.3 MB,
+# relocation kernel 519.7 + 42.2 MB. Configurations not captured report null.
+STEP_TRAFFIC_PER_STEP = {4: (727.3e6 + 297.5e6) / (1 << 20),
+                         6: (438.8e6 + 104.3e6 + 519.7e6 + 42.2e6) / (1 << 20)}
 # name -> (precision | scheduling flags): 1 = VG_PREC_MIXED, 2 = VG_NAV_SORT, 4 = VG_NAV_QUEUE
 # 8 = VG_NAV_LEARNED (explore the BVH subtree proposed by the trained model first)
 SCHEDULES = {"fp64": 0, "fp64_sort": 2, "mixed": 1, "mixed_sort": 3, "mixed_queue": 5, "mixed_sort_queue": 7,
@@ -544,6 +548,8 @@ def main():
         tuning = autotune(geo, t, st, candidates=cands, cache=None)
     elif args.cell_bits or args.queue_blocks:
         geo.set_tuning(args.cell_bits, args.queue_blocks)
+    queue_cfg = (tuning["queue_blocks"] if tuning else args.queue_blocks) or 1
+    split = queue_cfg >= 5
     ms_fp64 = timed(vg.PREC_FP64)
     out64, step64 = out.clone(), step.clone()
     variants = {"fp64": ms_fp64}
@@ -640,19 +646,24 @@ def main():
     roofline_fp64 = None
     if head == SCHEDULES["mixed_sort_queue_learned"]:
         fp64_peak = vg.device_fp64_rate()
-        roofline_fp64 = {"bound": "fp64", "achieved": FP64_OPS_PER_STEP * n / (ms_head * 1e-3), "peak": fp64_peak,
-                         "unit": "FP64 thread-ops/s", "frac": FP64_OPS_PER_STEP * n / (ms_head * 1e-3) / fp64_peak,
-                         "ops_per_step": FP64_OPS_PER_STEP,
+        ops = FP64_OPS_PER_STEP["split" if split else "fused"]
+        roofline_fp64 = {"bound": "fp64", "achieved": ops * n / (ms_head * 1e-3), "peak": fp64_peak,
+                         "unit": "FP64 thread-ops/s", "frac": ops * n / (ms_head * 1e-3) / fp64_peak,
+                         "ops_per_step": ops,
                          "note": "ncu-counted ops per step; peak = DFMA probe timed in this run"}
     m = {
         "value": value, "ms_per_step": ms_head, "n": n, "ws": ws, "args": args, "pool": pool,
         "ms_fp64": ms_fp64, "ms_fp64_sort": variants.get("fp64_sort"), "ids_equal": ids_equal, "step_err": step_err,
         "e2e_value": ws * n / e2e_s, "e2e_calls": e2e_calls, "head": head, "passes": passes,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": STEP_TRAFFIC_PER_STEP * n if head & 4 else None,
-                     "kernel": "k_step_mixed_queue" if head & 4 else ("k_step_mixed" if head & 1 else "k_step"),
-                     "note": "80 algorithmic B/step over the step kernel's own time; traffic = ncu DRAM bytes "
-                             "of one launch (2^20-step capture scaled by steps); peak %s"
+                     "frac": achieved / hbm_peak,
+                     "traffic": STEP_TRAFFIC_PER_STEP[queue_cfg] * n
+                     if head & 4 and queue_cfg in STEP_TRAFFIC_PER_STEP else None,
+                     "kernel": ("k_step_mixed_split (step + relocation launches)" if split else "k_step_mixed_queue")
+                     if head & 4 else ("k_step_mixed" if head & 1 else "k_step"),
+                     "queue_configuration": queue_cfg,
+                     "note": "80 algorithmic B/step over the step kernel(s)' own time; traffic = ncu DRAM bytes "
+                             "of the launch(es) (2^20-step capture scaled by steps); peak %s"
                              % ("of measured" if peaks else "of fallback")},
         "roofline_fp64": roofline_fp64, "n_err": n_err, "clocks": clocks.summary(),
     }
