@@ -316,11 +316,14 @@ int vg_nav_compute_step_and_next_volume_noalloc(const vg_geom *g, const double *
  * trace_tracks record each step's out-state and length at [i * max_steps + k] of
  * trace_states / trace_steps. Each iteration steps all live tracks with one persistent
  * kernel (refilled from a compacted list of survivors), after sorting them (VG_NAV_SORT)
- * and computing proposals (VG_NAV_LEARNED) if asked. With VG_NAV_QUEUE, once fewer tracks
- * are alive than 512 per SM, the rest runs as one pass in which every thread steps a track
- * to its end and then takes the next (same results, no per-iteration sort or host round
- * trip). *iterations (nullable) receives the number of passes (iterations, plus one for
- * such a tail pass). Synchronises the stream. No single reference counterpart. */
+ * and computing proposals (VG_NAV_LEARNED) if asked. The iterations run in a device-side
+ * loop (a CUDA graph whose while-node repeats them until the stream ends; the live count
+ * never returns to the host in between). With VG_NAV_QUEUE, once fewer tracks are alive
+ * than 512 per SM, the rest runs as one pass in which every thread steps a track to its
+ * end and then takes the next (same results, no per-iteration sort). *iterations
+ * (nullable) receives the number of passes (iterations, plus one for such a tail pass).
+ * Synchronises the stream; builds and frees its graph on every call. No single reference
+ * counterpart. */
 size_t vg_nav_transport_workspace_bytes(size_t n, uint32_t flags);
 int vg_nav_transport(const vg_geom *g, double *x, double *y, double *z, const double *dx, const double *dy,
                      const double *dz, vg_navstate *states, size_t n, int32_t max_steps, uint32_t flags,

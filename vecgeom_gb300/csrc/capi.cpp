@@ -679,7 +679,7 @@ int vg_nav_compute_step_and_next_volume_ws(const vg_geom *g, const double *x, co
 size_t transport_ws_bytes(size_t n, uint32_t flags)
 {
   const size_t a = (n * sizeof(uint32_t) + 255) & ~size_t(255);
-  size_t b       = 2 * a + 3 * 256; // two track lists, survivor count, live count, queue counter
+  size_t b       = 2 * a + 4 * 256; // two track lists, two counts, queue counter, loop control
   if (flags & VG_NAV_LEARNED) b += (n + 255) & ~size_t(255);
   if (flags & VG_NAV_SORT) b += vg::nav_sort_workspace_bytes(n);
   return b;
@@ -714,7 +714,7 @@ int vg_nav_transport(const vg_geom *g, double *x, double *y, double *z, const do
   uint32_t *list[2] = {reinterpret_cast<uint32_t *>(w), reinterpret_cast<uint32_t *>(w + al)};
   unsigned int *cnt[2] = {reinterpret_cast<unsigned int *>(w + 2 * al), reinterpret_cast<unsigned int *>(w + 2 * al + 256)};
   unsigned long long *counter = reinterpret_cast<unsigned long long *>(w + 2 * al + 512);
-  unsigned char *rest         = w + 2 * al + 768;
+  unsigned char *rest         = w + 2 * al + 1024;
   int8_t *slots               = nullptr;
   if (flags & VG_NAV_LEARNED) {
     slots = reinterpret_cast<int8_t *>(rest);
@@ -730,41 +730,38 @@ int vg_nav_transport(const vg_geom *g, double *x, double *y, double *z, const do
     if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
       drain_below = (unsigned int)sms * 512u;
   }
-  int cur = 0, it = 0;
-  while (e == cudaSuccess && it < max_steps) {
-    unsigned int live = 0;
-    e = cudaMemcpyAsync(&live, cnt[cur], sizeof(live), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess || live == 0) break;
-    if (live < drain_below) {
-      vg::TransportArgs ta{x,       y,           z,       dx,          dy,         dz,    st,
+  // The iterations run in a device-side loop (a CUDA graph with a while-node, no host round
+  // trip per iteration); the host reads the loop's end state once and runs the tail pass.
+  vg::TransportCtl *ctl = reinterpret_cast<vg::TransportCtl *>(w + 2 * al + 768);
+  vg::TransportLoop L{};
+  L.g     = &g->geo.dev;
+  L.ta    = vg::TransportArgs{x,       y,           z,       dx,          dy,         dz,    st,
                            nsteps,  status,      (int)max_steps, reinterpret_cast<vg::NavState *>(trace_states),
-                           trace_steps, trace_tracks, list[cur], live, nullptr, nullptr, nullptr};
-      e = vg::launch_transport_drain(g->geo.dev, ta, (flags & VG_PREC_MIXED) != 0, counter, s);
-      ++it;
-      break;
-    }
-    const uint32_t *order = list[cur];
-    if (flags & VG_NAV_SORT) {
-      const uint32_t *sorted = nullptr;
-      e = vg::launch_nav_sort(g->geo.dev, g->sort, x, y, z, st, live, rest, &sorted, s, list[cur]);
-      if (e != cudaSuccess) break;
-      order = sorted;
-    }
-    if (flags & VG_NAV_LEARNED) {
-      vg::StepArgs pa{x, y, z, dx, dy, dz, nullptr, st, nullptr, nullptr, nullptr, nullptr, live};
-      pa.order = list[cur]; // live tracks in (near) track order, see step_launch
-      e = g->propose_tensor ? vg::launch_mlp_propose_tc(g->geo.dev, pa, g->proposer->wbf, slots, g->proposer->err, s)
-                            : vg::launch_mlp_propose(g->geo.dev, pa, g->proposer->wbf, slots, s);
-      if (e != cudaSuccess) break;
-    }
-    e = cudaMemsetAsync(cnt[cur ^ 1], 0, sizeof(unsigned int), s);
-    if (e != cudaSuccess) break;
+                           trace_steps, trace_tracks, nullptr, 0, nullptr, nullptr, nullptr};
+  L.n     = n;
+  L.list[0] = list[0], L.list[1] = list[1];
+  L.cnt[0] = cnt[0], L.cnt[1] = cnt[1];
+  L.counter        = counter;
+  L.ctl            = ctl;
+  L.mixed          = (flags & VG_PREC_MIXED) != 0;
+  L.queue_blocks   = g->queue_blocks;
+  L.sort_on        = (flags & VG_NAV_SORT) != 0;
+  L.sort           = g->sort;
+  L.sort_ws        = rest;
+  L.slots          = slots;
+  L.propose_tensor = g->propose_tensor;
+  L.wbf            = (flags & VG_NAV_LEARNED) ? g->proposer->wbf : nullptr;
+  L.mlp_err        = (flags & VG_NAV_LEARNED) ? g->proposer->err : nullptr;
+  L.max_steps      = (int)max_steps;
+  L.drain_below    = drain_below;
+  vg::TransportCtl end{};
+  if (e == cudaSuccess) e = vg::run_transport_loop(L, s, &end);
+  int it = end.it;
+  if (e == cudaSuccess && end.live > 0 && end.live < drain_below && it < max_steps) {
     vg::TransportArgs ta{x,       y,           z,       dx,          dy,         dz,    st,
                          nsteps,  status,      (int)max_steps, reinterpret_cast<vg::NavState *>(trace_states),
-                         trace_steps, trace_tracks, order, live, list[cur ^ 1], cnt[cur ^ 1], slots};
-    e = vg::launch_transport_iter(g->geo.dev, ta, (flags & VG_PREC_MIXED) != 0, counter, g->queue_blocks, s);
-    cur ^= 1;
+                         trace_steps, trace_tracks, list[end.cur], end.live, nullptr, nullptr, nullptr};
+    e = vg::launch_transport_drain(g->geo.dev, ta, (flags & VG_PREC_MIXED) != 0, counter, s);
     ++it;
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);

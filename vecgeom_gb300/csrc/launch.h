@@ -22,6 +22,7 @@ struct StepArgs {
   size_t n;
   const uint32_t *order = nullptr; // optional visiting order (track indices); null: 0..n-1
   const int8_t *proposal = nullptr; // optional learned first subtree per track (-1: none)
+  const unsigned int *n_dev = nullptr; // optional device count: only the first min(n, *n_dev) entries
 };
 
 // Sort key of a track: logical volume of its state above 3*cell_bits Morton bits of its
@@ -57,10 +58,12 @@ const uint32_t *nav_sort_keys_of(const uint32_t *order, const void *ws, size_t n
 // Keys + stable radix sort of the n tracks (or of the n track ids in `list`); *order
 // receives the sorted track indices (inside the workspace). keys_done: the keys of all n
 // tracks were already written by launch_nav_sort_keys (ranges of tracks, e.g. as their
-// inputs arrive), only the radix passes run.
+// inputs arrive), only the radix passes run. n_dev (optional, device memory): sort only the
+// first min(n, *n_dev) entries; n then only sizes the grids (a count the host does not know).
 cudaError_t launch_nav_sort(const DevGeom &g, const SortKeyParams &p, const double *x, const double *y,
                             const double *z, const NavState *in, size_t n, void *ws, const uint32_t **order,
-                            cudaStream_t s, const uint32_t *list = nullptr, bool keys_done = false);
+                            cudaStream_t s, const uint32_t *list = nullptr, bool keys_done = false,
+                            const unsigned int *n_dev = nullptr);
 cudaError_t launch_nav_sort_keys(const DevGeom &g, const SortKeyParams &p, const double *x, const double *y,
                                  const double *z, const NavState *in, size_t begin, size_t end, void *ws,
                                  cudaStream_t s);
@@ -83,9 +86,48 @@ struct TransportArgs {
   uint32_t *next;
   unsigned int *next_count;
   const int8_t *proposal;
+  const unsigned int *n_dev = nullptr; // optional device count: only the first min(n, *n_dev) entries
 };
 cudaError_t launch_transport_iter(const DevGeom &g, const TransportArgs &a, bool mixed, unsigned long long *counter,
                                   int blocks_per_sm, cudaStream_t s);
+// Device-side loop of the transport stream (transport_loop.cu): control block in device
+// memory; n[c] is the count the iteration from list c runs on (0 once stopped), `it` the
+// iterations made, `live` and `cur` the survivors and their list when the loop stopped.
+struct TransportCtl {
+  unsigned int n[2];
+  int it;
+  int stop;
+  unsigned int live;
+  int cur;
+  int pad[2];
+};
+// What the loop needs; the lists, counts, counter, slots and sort workspace are device
+// memory of n entries each (slots, sort_ws: null when VG_NAV_LEARNED / VG_NAV_SORT are off).
+struct TransportLoop {
+  const DevGeom *g;
+  TransportArgs ta; // the track arrays, max_steps and traces; list/n/next fields are set per iteration
+  size_t n;
+  uint32_t *list[2];
+  unsigned int *cnt[2];
+  unsigned long long *counter;
+  TransportCtl *ctl;
+  bool mixed;
+  int queue_blocks;
+  bool sort_on;
+  SortKeyParams sort;
+  void *sort_ws;
+  int8_t *slots;
+  int propose_tensor;
+  const uint16_t *wbf;
+  int *mlp_err;
+  int max_steps;
+  unsigned int drain_below;
+};
+// Runs the iterations until the loop's rule stops them, synchronises `s` and copies the
+// control block to *out.
+cudaError_t run_transport_loop(const TransportLoop &loop, cudaStream_t s, TransportCtl *out);
+cudaError_t launch_mlp_propose_tc(const DevGeom &g, const StepArgs &a, const uint16_t *wbf, int8_t *slot, int *err,
+                                  cudaStream_t s);
 // Transport tail: steps every track of `list` to its end in one launch (refill per lane).
 cudaError_t launch_transport_drain(const DevGeom &g, const TransportArgs &a, bool mixed, unsigned long long *counter,
                                    cudaStream_t s);

@@ -247,7 +247,8 @@ __global__ void __launch_bounds__(128) k_mlp_propose(const DevGeom g, const Step
   for (int e = threadIdx.x; e < kMlpE; e += blockDim.x) W[e] = bf(wbf[e]);
   __syncthreads();
   const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+  const size_t n      = a.n_dev && *a.n_dev < a.n ? (size_t)*a.n_dev : a.n;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     const size_t t = a.order ? (size_t)__ldg(a.order + i) : i;
     float f[kMlpIn];
     int lv = -1;

@@ -157,6 +157,7 @@ __global__ void __launch_bounds__(kTile, 5) k_mlp_propose_tc(const DevGeom g, co
 
   const uint32_t aW1 = smem_u32(sm + kOffW1), aW2 = smem_u32(sm + kOffW2), aW3 = smem_u32(sm + kOffW3);
   const uint32_t aA = smem_u32(sm + kOffA);
+  if (Step && a.n_dev && *a.n_dev < n) n = *a.n_dev; // a count known on the device only
   const size_t ntiles = (n + kTile - 1) / kTile;
   for (size_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     const size_t i = tile * kTile + t;

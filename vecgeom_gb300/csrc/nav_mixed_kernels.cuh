@@ -185,13 +185,14 @@ __global__ void __launch_bounds__(Threads, MinBlocks) k_transport_iter(const Dev
 {
   const mixed::ShapeLB *lbs = reinterpret_cast<const mixed::ShapeLB *>(g.shape_lbd);
   const int lane            = threadIdx.x & 31;
+  const size_t n            = a.n_dev && *a.n_dev < a.n ? (size_t)*a.n_dev : a.n;
   for (;;) {
     unsigned long long base = 0;
     if (lane == 0) base = atomicAdd(counter, 32ull);
     base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= a.n) break;
+    if (base >= n) break;
     const size_t i = (size_t)base + lane;
-    if (i >= a.n) continue;
+    if (i >= n) continue;
     const size_t t = __ldg(a.list + i);
     const NavState s = a.st[t];
     NavState o;

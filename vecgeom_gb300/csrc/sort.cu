@@ -36,8 +36,10 @@ __device__ __forceinline__ uint32_t cell(double c, float lo, float scale, uint32
 __global__ void __launch_bounds__(256) k_sort_keys(const DevGeom g, const SortKeyParams p, const double *__restrict__ x,
                                                    const double *__restrict__ y, const double *__restrict__ z,
                                                    const NavState *__restrict__ in, const uint32_t *__restrict__ list,
-                                                   size_t begin, size_t end, uint32_t *__restrict__ keys)
+                                                   size_t begin, size_t end, uint32_t *__restrict__ keys,
+                                                   const unsigned int *__restrict__ n_dev)
 {
+  if (n_dev && begin + *n_dev < end) end = begin + *n_dev;
   const uint32_t maxc = (1u << p.cell_bits) - 1u;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t j = begin + (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < end; j += stride) {
@@ -60,8 +62,10 @@ __global__ void __launch_bounds__(256) k_sort_keys(const DevGeom g, const SortKe
 
 // Per-tile digit counts, digit-major: hist[d * ntiles + tile].
 __global__ void __launch_bounds__(kSortBlock) k_radix_hist(const uint32_t *__restrict__ keys, size_t n, int shift,
-                                                           uint32_t *__restrict__ hist, unsigned ntiles)
+                                                           uint32_t *__restrict__ hist, unsigned ntiles,
+                                                           const unsigned int *__restrict__ n_dev)
 {
+  if (n_dev && *n_dev < n) n = *n_dev;
   __shared__ uint32_t h[256];
   h[threadIdx.x] = 0u;
   __syncthreads();
@@ -131,8 +135,10 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_scatter(const uint32_t *__
                                                               uint32_t *__restrict__ kout, uint32_t *__restrict__ vout,
                                                               size_t n, int shift, const uint32_t *__restrict__ hist,
                                                               const uint32_t *__restrict__ totals, unsigned ntiles,
-                                                              const uint32_t *__restrict__ list)
+                                                              const uint32_t *__restrict__ list,
+                                                              const unsigned int *__restrict__ n_dev)
 {
+  if (n_dev && *n_dev < n) n = *n_dev;
   __shared__ uint32_t cnt[kSortWarps][256];
   __shared__ uint32_t wsum[33];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -210,13 +216,13 @@ cudaError_t launch_nav_sort_keys(const DevGeom &g, const SortKeyParams &p, const
 {
   if (end <= begin) return cudaSuccess;
   k_sort_keys<<<grid_for(end - begin, 256), 256, 0, s>>>(g, p, x, y, z, in, nullptr, begin, end,
-                                                        static_cast<uint32_t *>(ws));
+                                                        static_cast<uint32_t *>(ws), nullptr);
   return cudaGetLastError();
 }
 
 cudaError_t launch_nav_sort(const DevGeom &g, const SortKeyParams &p, const double *x, const double *y,
                             const double *z, const NavState *in, size_t n, void *ws, const uint32_t **order,
-                            cudaStream_t s, const uint32_t *list, bool keys_done)
+                            cudaStream_t s, const uint32_t *list, bool keys_done, const unsigned int *n_dev)
 {
   *order = nullptr;
   if (n == 0) return cudaSuccess;
@@ -227,16 +233,17 @@ cudaError_t launch_nav_sort(const DevGeom &g, const SortKeyParams &p, const doub
   uint32_t *v0 = reinterpret_cast<uint32_t *>(w + 2 * a), *v1 = reinterpret_cast<uint32_t *>(w + 3 * a);
   uint32_t *hist   = reinterpret_cast<uint32_t *>(w + 4 * a);
   uint32_t *totals = reinterpret_cast<uint32_t *>(w + 4 * a + align256(256 * (size_t)ntiles * sizeof(uint32_t)));
-  if (!keys_done) k_sort_keys<<<grid_for(n, 256), 256, 0, s>>>(g, p, x, y, z, in, list, 0, n, k0);
+  if (!keys_done) k_sort_keys<<<grid_for(n, 256), 256, 0, s>>>(g, p, x, y, z, in, list, 0, n, k0, n_dev);
   // Digits above the key's width are all zero (invalid states carry all-ones keys, which
   // sort last within every pass), so only the passes that cover the key bits are run.
   const int bits   = sort_key_bits(p);
   const int passes = (bits + 7) / 8;
   uint32_t *kin = k0, *kout = k1, *vin = nullptr, *vout = v0;
   for (int ps = 0; ps < passes; ++ps) {
-    k_radix_hist<<<ntiles, kSortBlock, 0, s>>>(kin, n, 8 * ps, hist, ntiles);
+    k_radix_hist<<<ntiles, kSortBlock, 0, s>>>(kin, n, 8 * ps, hist, ntiles, n_dev);
     k_scan_rows<<<256, 1024, 0, s>>>(hist, ntiles, totals);
-    k_radix_scatter<<<ntiles, kSortBlock, 0, s>>>(kin, vin, kout, vout, n, 8 * ps, hist, totals, ntiles, list);
+    k_radix_scatter<<<ntiles, kSortBlock, 0, s>>>(kin, vin, kout, vout, n, 8 * ps, hist, totals, ntiles, list,
+                                                  n_dev);
     uint32_t *tk = kin;
     kin          = kout;
     kout         = tk;
