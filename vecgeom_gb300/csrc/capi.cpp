@@ -241,7 +241,7 @@ int shape_query(const vg_geom *g, int32_t shape, const vg::Xform &xf, int apply_
   const bool composite = type == vg::kShapePolycone || type == vg::kShapePolyhedron || type == vg::kShapeBoolMinus;
   const bool mixed      = (flags & VG_PREC_MIXED) != 0;
   const float *lbd      = mixed ? geo.shape_lbd_host.data() + 8 * (size_t)shape : nullptr;
-  const cudaError_t e   = composite ? vg::launch_shape_query_dyn_fp64(geo.dev, shape, xf, apply_xf, q, a,
+  const cudaError_t e   = composite ? vg::launch_shape_query_dyn_fp64(geo.dev, shape, type, xf, apply_xf, q, a,
                                                                     (cudaStream_t)stream, mixed)
                                   : vg::launch_shape_query_fp64(type, geo.shape_rec(shape), xf, apply_xf, q, a,
                                                                 (cudaStream_t)stream, lbd);

@@ -261,6 +261,47 @@ __global__ void __launch_bounds__(256) k_shape_query_dyn(const DevGeom g, const 
   }
 }
 
+// Polycone DistanceToOut with lane refill. The section loop of PolyconeImplementation.h
+// runs 1 to nsec passes per ray, so in the plain kernel a warp waits for its longest ray.
+// Here each lane walks its own grid-stride sequence of queries: every round, a lane without
+// a query in progress sets up its next one (which may end at once), and every lane with a
+// section loop in progress runs one pass of it. The passes of a round run together, and a
+// lane whose ray is done starts the next instead of idling. Each query runs the same setup
+// and passes as polycone_dist_out, so the results are its results.
+__global__ void __launch_bounds__(256) k_polycone_dist_out_refill(const DevGeom g, const int shape,
+                                                                  const double *__restrict__ x,
+                                                                  const double *__restrict__ y,
+                                                                  const double *__restrict__ z,
+                                                                  const double *__restrict__ dx,
+                                                                  const double *__restrict__ dy,
+                                                                  const double *__restrict__ dz, size_t n,
+                                                                  double *__restrict__ out)
+{
+  const f64::PolyconeView v(f64::rec_at<PolyconeRec>(g, g.shape_off[shape]));
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t i            = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  f64::PolyconeOutLoop L;
+  bool busy = false;
+  for (;;) {
+    double r;
+    if (!busy && i < n) {
+      if (f64::polycone_out_setup(v, V3{__ldg(x + i), __ldg(y + i), __ldg(z + i)},
+                                  V3{__ldg(dx + i), __ldg(dy + i), __ldg(dz + i)}, r, L)) {
+        out[i] = r;
+        i += stride;
+      } else {
+        busy = true;
+      }
+    }
+    if (busy && f64::polycone_out_pass(v, L, r)) {
+      out[i] = r;
+      i += stride;
+      busy = false;
+    }
+    if (!__any_sync(0xffffffffu, busy || i < n)) break;
+  }
+}
+
 } // namespace
 
 cudaError_t launch_shape_query_fp64(int type, const double *rec, const Xform &xf, int apply_xf, int q,
@@ -282,11 +323,16 @@ cudaError_t launch_shape_query_fp64(int type, const double *rec, const Xform &xf
   }
 }
 
-cudaError_t launch_shape_query_dyn_fp64(const DevGeom &g, int shape, const Xform &xf, int apply_xf, int q,
+cudaError_t launch_shape_query_dyn_fp64(const DevGeom &g, int shape, int type, const Xform &xf, int apply_xf, int q,
                                         const QueryArgs &a, cudaStream_t s, bool mixed)
 {
   if (a.n == 0) return cudaSuccess;
   const unsigned grid = grid_for(a.n, 256);
+  if (q == 3 && type == kShapePolycone) { // DistanceToOut takes local points: no transform
+    k_polycone_dist_out_refill<<<grid, 256, 0, s>>>(g, shape, a.x, a.y, a.z, a.dx, a.dy, a.dz, a.n,
+                                                    static_cast<double *>(a.out));
+    return cudaGetLastError();
+  }
 #define VG_DYN(Q)                                                                                                   \
   (mixed ? k_shape_query_dyn<Q, true><<<grid, 256, 0, s>>>(g, shape, xf, apply_xf, a.x, a.y, a.z, a.dx, a.dy, a.dz, \
                                                            a.n, a.out)                                             \

@@ -38,7 +38,8 @@ struct SortKeyParams {
 // mixed-precision variant (VG_PREC_MIXED).
 cudaError_t launch_shape_query_fp64(int type, const double *rec, const Xform &xf, int apply_xf, int q,
                                     const QueryArgs &a, cudaStream_t s, const float *lbd = nullptr);
-cudaError_t launch_shape_query_dyn_fp64(const DevGeom &g, int shape, const Xform &xf, int apply_xf, int q,
+// `type`: the shape's type tag (host copy), which selects Polycone DistanceToOut's refill kernel.
+cudaError_t launch_shape_query_dyn_fp64(const DevGeom &g, int shape, int type, const Xform &xf, int apply_xf, int q,
                                         const QueryArgs &a, cudaStream_t s, bool mixed = false);
 cudaError_t launch_locate_fp64(const DevGeom &g, const double *x, const double *y, const double *z, size_t n,
                                NavState *out, cudaStream_t s);

@@ -353,59 +353,102 @@ static __device__ __noinline__ double polycone_dist_in(const PolyconeRec &rec, V
   } while (index >= 0 && index < v.nsec);
   return distance;
 }
-// PolyconeImplementation.h:181-300
-static __device__ __noinline__ double polycone_dist_out(const PolyconeRec &rec, V3 point, V3 dir)
+// PolyconeImplementation.h:181-300, in two parts so that a kernel can interleave the
+// section loops of different queries on one lane (k_polycone_dist_out_refill): the setup
+// before the loop, and one pass of the loop. polycone_dist_out runs them back to back.
+struct PolyconeOutLoop {
+  V3 point, dir, pn;
+  double total;
+  int index, increment, istep;
+};
+// Setup: true with the result in r when the query ends before the section loop.
+__device__ __forceinline__ bool polycone_out_setup(const PolyconeView &v, V3 point, V3 dir, double &r,
+                                                   PolyconeOutLoop &L)
 {
-  const PolyconeView v(rec);
-  if (v.nsec == 1) return cone_dist_out(v.cone(0), v.local(point, 0), dir);
+  if (v.nsec == 1) {
+    r = cone_dist_out(v.cone(0), v.local(point, 0), dir);
+    return true;
+  }
   const int lo = v.index(point.z - kTolerance);
   const int hi = v.index(point.z + kTolerance);
   int index    = 0;
-  if (lo < 0 && hi < 0) return -1;
+  r            = -1.;
+  if (lo < 0 && hi < 0) return true;
   if (lo < 0 && hi >= 0) {
     index = hi;
-    if (cone_inside(v.cone(index), v.local(point, index)) == kOutside) return -1;
+    if (cone_inside(v.cone(index), v.local(point, index)) == kOutside) return true;
   } else if (lo != hi && lo >= 0) {
     index = (cone_inside(v.cone(lo), v.local(point, lo)) == kOutside) ? hi : lo;
   } else {
     index = lo;
     if (index < 0) index = v.index(point.z);
   }
-  if (index < 0) return 0.;
-  if (cone_inside(v.cone(index), v.local(point, index)) == kOutside) return -1;
-  double total  = 0.;
-  int increment = dgt(dir.z, 0.) ? 1 : -1;
-  if (dabs_lt(dir.z, kTolerance)) increment = 0;
-  int istep = 0;
-  V3 pn     = point;
-  do {
-    if (dne(total, 0.) || (istep < 2)) {
-      pn = V3{point.x + total * dir.x, point.y + total * dir.y, point.z + total * dir.z};
-      pn.z -= v.shift(index);
-      if (cone_inside(v.cone(index), pn) == kOutside) break;
+  if (index < 0) {
+    r = 0.;
+    return true;
+  }
+  if (cone_inside(v.cone(index), v.local(point, index)) == kOutside) return true;
+  L.point     = point;
+  L.dir       = dir;
+  L.pn        = point;
+  L.total     = 0.;
+  L.index     = index;
+  L.increment = dgt(dir.z, 0.) ? 1 : -1;
+  if (dabs_lt(dir.z, kTolerance)) L.increment = 0;
+  L.istep = 0;
+  return false;
+}
+// One pass of the section loop: true with the result in r when the query ends.
+__device__ __forceinline__ bool polycone_out_pass(const PolyconeView &v, PolyconeOutLoop &L, double &r)
+{
+  const V3 point = L.point, dir = L.dir;
+  if (dne(L.total, 0.) || (L.istep < 2)) {
+    L.pn = V3{point.x + L.total * dir.x, point.y + L.total * dir.y, point.z + L.total * dir.z};
+    L.pn.z -= v.shift(L.index);
+    if (cone_inside(v.cone(L.index), L.pn) == kOutside) {
+      r = L.total;
+      return true;
+    }
+  } else {
+    L.pn.z -= v.shift(L.index);
+  }
+  L.istep++;
+  const double dist = cone_dist_out(v.cone(L.index), L.pn, dir);
+  if (deq(dist, -1.)) {
+    r = kInfLength;
+    return true;
+  }
+  if (dabs_lt(dist, 0.5 * kTolerance)) {
+    int index1 = L.index;
+    if ((L.index > 0) && (L.index < v.nsec - 1)) {
+      index1 += L.increment;
     } else {
-      pn.z -= v.shift(index);
+      if ((L.index == 0) && (L.increment > 0)) index1 += L.increment;
+      if ((L.index == v.nsec - 1) && (L.increment < 0)) index1 += L.increment;
     }
-    istep++;
-    const double dist = cone_dist_out(v.cone(index), pn, dir);
-    if (deq(dist, -1.)) return kInfLength;
-    if (dabs_lt(dist, 0.5 * kTolerance)) {
-      int index1 = index;
-      if ((index > 0) && (index < v.nsec - 1)) {
-        index1 += increment;
-      } else {
-        if ((index == 0) && (increment > 0)) index1 += increment;
-        if ((index == v.nsec - 1) && (increment < 0)) index1 += increment;
-      }
-      const double s = total + dist;
-      V3 pte{point.x + s * dir.x, point.y + s * dir.y, point.z + s * dir.z};
-      pte.z -= v.shift(index1);
-      if (cone_inside(v.cone(index1), pte) == 3 || increment == 0) break;
+    const double s = L.total + dist;
+    V3 pte{point.x + s * dir.x, point.y + s * dir.y, point.z + s * dir.z};
+    pte.z -= v.shift(index1);
+    if (cone_inside(v.cone(index1), pte) == 3 || L.increment == 0) {
+      r = L.total;
+      return true;
     }
-    total += dist;
-    index += increment;
-  } while (increment != 0 && index >= 0 && index < v.nsec);
-  return total;
+  }
+  L.total += dist;
+  L.index += L.increment;
+  if (L.increment != 0 && L.index >= 0 && L.index < v.nsec) return false;
+  r = L.total;
+  return true;
+}
+static __device__ __noinline__ double polycone_dist_out(const PolyconeRec &rec, V3 point, V3 dir)
+{
+  const PolyconeView v(rec);
+  double r;
+  PolyconeOutLoop L;
+  if (polycone_out_setup(v, point, dir, r, L)) return r;
+  while (!polycone_out_pass(v, L, r)) {
+  }
+  return r;
 }
 // PolyconeImplementation.h:301-354
 static __device__ __noinline__ double polycone_safety_in(const PolyconeRec &rec, V3 p)
