@@ -730,12 +730,13 @@ def nav_parity(gpu_out, gpu_step, o_out, o_step):
 
 def shape_parity_summary(rows):
     """Totals of the shape rows' oracle comparison, per precision, with the largest error
-    per shape; mixed Box safeties are lowered by their proven bound on purpose and are
-    listed apart."""
+    per shape; the mixed full-phi Tube safeties are lowered by their proven bound on purpose
+    and are listed apart."""
     out = {}
     for prec in ("fp64", "mixed"):
         sel = [r for r in rows if r["precision"] == prec]
-        bounded = [r for r in sel if prec == "mixed" and r["shape"] == "box" and r["query"].startswith("safety")]
+        # FP32 safeties with a proven bound below the FP64 value: the full-phi Tube's
+        bounded = [r for r in sel if prec == "mixed" and r["shape"] == "tube" and r["query"].startswith("safety")]
         strict = [r for r in sel if r not in bounded]
         per_shape = {}
         for r in strict:
@@ -747,7 +748,9 @@ def shape_parity_summary(rows):
                      "beyond_tol": sum(r.get("beyond_tol_vs_oracle", 0) for r in strict),
                      "max_abs_err_per_shape": per_shape}
         if bounded:
-            out[prec]["box_safety_bounded_max_err"] = max(r["max_abs_err_vs_oracle"] for r in bounded)
+            out[prec]["fp32_safety_bounded_max_err"] = {
+                k: max(r["max_abs_err_vs_oracle"] for r in bounded if r["shape"] == k)
+                for k in sorted({r["shape"] for r in bounded})}
     return out
 
 

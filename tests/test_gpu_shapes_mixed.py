@@ -1,7 +1,8 @@
 """Mixed-precision shape queries (VG_PREC_MIXED on the placed SoA queries) against the FP64
 kernels on the same points: Inside, Contains, DistanceToIn and DistanceToOut are identical
-for every shape; safeties are identical except Box, whose FP32 safeties never exceed the
-FP64 value and stay within the stated bound 2^-21 (max|p| + max half-length) below it."""
+for every shape; safeties are identical except the full-phi Tube's, whose FP32 safeties
+never exceed the FP64 value and stay within the stated bound 2^-20 (max(r, |z|) +
+max(dz, rmax)) below it."""
 import numpy as np
 import pytest
 
@@ -51,12 +52,13 @@ def test_mixed_shape_queries(cuda, case):
     b = _run(cuda, g, pv, pts, dirs, vg.PREC_MIXED)
     for q in QUERIES[:4]:
         assert np.array_equal(a[q], b[q]), (q, int((a[q] != b[q]).sum()))
-    if kind == "box":
-        p = np.abs(np.stack(pts))
-        bound = 2.0 ** -21 * (p.max(axis=0) + max(params))
+    if kind == "tube" and params[4] >= 2 * np.pi:
+        r = np.hypot(pts[0], pts[1])
+        bound = 2.0 ** -20 * (np.maximum(r, np.abs(pts[2])) + max(params[1], params[2]))
         for q in ("safety_to_in", "safety_to_out"):
-            assert (b[q] <= a[q]).all()
+            assert (b[q] <= a[q]).all(), q
             assert (a[q] - b[q] <= bound * 1.0001 + 1e-300).all(), q
+            assert (a[q] != b[q]).any(), q  # the FP32 form ran
     else:
         for q in ("safety_to_in", "safety_to_out"):
             assert np.array_equal(a[q], b[q]), q

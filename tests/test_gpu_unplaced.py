@@ -2,7 +2,7 @@
 kernels untransformed (VUnplacedVolume), so signed zeros reach the kernels as given. Against
 the oracle's unplaced queries: bit-exact in FP64 (Torus2 distances within 1e-9 mm + 1e-12
 relative), and the
-mixed-precision results equal to FP64 (Box safeties excepted: their FP32 form has a stated
+mixed-precision results equal to FP64 (full-phi Tube safeties excepted: their FP32 form has a stated
 bound)."""
 import numpy as np
 import pytest
@@ -69,5 +69,5 @@ def test_unplaced_queries_match_oracle(cuda, name):
         else:
             bad = ~((got == ref) | (np.isnan(got) & np.isnan(ref)))
         assert not bad.any(), (name, QUERIES[qi], int(bad.sum()), got[bad][:3], ref[bad][:3])
-        if not (kind == "box" and qi >= 4):
+        if not (kind == "tube" and params[4] >= 2 * np.pi and qi >= 4):
             assert np.array_equal(res[vg.PREC_MIXED, qi], got, equal_nan=True), (name, QUERIES[qi])

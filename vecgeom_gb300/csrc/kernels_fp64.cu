@@ -77,8 +77,9 @@ __global__ void __launch_bounds__(256) k_shape_query(const R rec, const Xform xf
     }
     if (Q == 4 || Q == 5) {
       double r;
-      if (M && std::is_same<R, BoxRec>::value && mixed::in_range(mixed::f3(p)))
-        r = mixed::box_safety_mixed(reinterpret_cast<const BoxRec &>(rec), p, Q == 5);
+      if (M && std::is_same<R, TubeRec>::value && !f64::tube_phi(reinterpret_cast<const TubeRec &>(rec)) &&
+               mixed::in_range(mixed::f3(p)))
+        r = mixed::tube_safety_mixed(reinterpret_cast<const TubeRec &>(rec), p, Q == 5);
       else
         r = (Q == 4) ? ShapeOps<R>::safety_in(rec, p) : ShapeOps<R>::safety_out(rec, p);
       static_cast<double *>(out)[i] = r;

@@ -204,19 +204,35 @@ __device__ __forceinline__ bool f32_certain_miss(const ShapeLB &s, F3 l, F3 d)
   return shell_lb(rmin, rmax, s.a2 - kBoxPad, s.a3 + kBoxPad, l, d) == INFINITY;
 }
 
-// Box safeties entirely in FP32 (no FP64 operation), with directed rounding. Each FP32 term
-// |p_k| - h_k carries at most 2^-23 (|p_k| + h_k) of rounding (input conversions and the
-// subtraction) and the FP64 reference's own at most 2^-53 of it; max/min are 1-Lipschitz.
-// So the FP32 safety s is within (2^-23 + 2^-53) M of the FP64 safety S, M = max_k |p_k| +
-// max_k h_k, and s - 2^-22 M (bound rounded up, subtraction rounded down) never exceeds S
-// and lies at most 2^-21 M below it.
-__device__ __forceinline__ double box_safety_mixed(const BoxRec &b, V3 p, bool out)
+// Full-phi Tube safeties in FP32 (the SafetyToInOld / SafetyToOutOld forms of
+// TubeImplementation.h:758-802 that tube_safety_in / tube_safety_out follow: the z term
+// |z| - dz, the radial terms r - rmax and rmin - r, combined by max, or their negatives by
+// min), lowered by a proven bound so that they never exceed the FP64 value. With u = 2^-24,
+// inputs rounded to nearest, sqrtf and every FP32 operation correctly rounded:
+// r32 = sqrtf(fmaf(x, x, y * y)) lies within 3.1 u r of r (u r from the inputs, 2 u from the
+// sum and the root); each FP32 term within 4.2 u (R + D) of the exact one, R = max(r, |z|),
+// D = max(dz, rmax) (r32's error, the rounding of the constant and of the subtraction); the
+// FP64 terms within 2^-50 (R + D) of the exact ones. max and min are 1-Lipschitz, so the FP32
+// safety s is within (4.2 u + 2^-50)(R + D) < 2^-21 (R + D) of the FP64 one, and
+// s - 2^-21 (R + D) (bound rounded up, subtraction rounded down) never exceeds it and lies at
+// most 2^-20 (R + D) below it. Phi sections keep the FP64 kernel. (The Box's FP64 safety
+// is three subtractions; an FP32 form of it measured slower than that, so the Box keeps it.)
+__device__ __forceinline__ double tube_safety_mixed(const TubeRec &t, V3 p, bool out)
 {
-  const float x = fabsf((float)p.x), y = fabsf((float)p.y), z = fabsf((float)p.z);
-  const float dx = (float)b.dx, dy = (float)b.dy, dz = (float)b.dz;
-  const float s  = out ? fminf(fminf(dx - x, dy - y), dz - z) : fmaxf(fmaxf(x - dx, y - dy), z - dz);
-  const float m  = __fadd_ru(fmaxf(fmaxf(x, y), z), fmaxf(fmaxf(dx, dy), dz));
-  return (double)__fsub_rd(s, __fmul_ru(2.384185791015625e-07f, m));
+  const float x = (float)p.x, y = (float)p.y, z = fabsf((float)p.z);
+  const float r  = sqrtf(fmaf(x, x, y * y));
+  const float dz = (float)t.z, rmax = (float)t.rmax, rmin = (float)t.rmin;
+  const bool hasmin = f64::tube_rmin(t);
+  float s;
+  if (out) {
+    s = fminf(dz - z, rmax - r);
+    if (hasmin) s = fminf(s, r - rmin);
+  } else {
+    s = fmaxf(z - dz, r - rmax);
+    if (hasmin) s = fmaxf(s, rmin - r);
+  }
+  const float m = __fadd_ru(fmaxf(r, z), fmaxf(dz, rmax));
+  return (double)__fsub_rd(s, __fmul_ru(4.76837158203125e-07f, m));
 }
 
 } // namespace mixed
