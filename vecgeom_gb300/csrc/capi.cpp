@@ -135,16 +135,18 @@ constexpr uint32_t kNavFlags = VG_PREC_MIXED | VG_NAV_SORT | VG_NAV_QUEUE | VG_N
 size_t step_workspace_bytes(size_t n, uint32_t flags)
 {
   size_t b = 0;
-  if (flags & VG_NAV_QUEUE) b += 256;
+  if (flags & VG_NAV_QUEUE) b += 256 + ((3 * n * sizeof(double) + 255) & ~size_t(255));
   if (flags & VG_NAV_LEARNED) b += (n + 255) & ~size_t(255);
   if (flags & VG_NAV_SORT) b += vg::nav_sort_workspace_bytes(n);
   return b;
 }
 
-// Workspace of a scheduled step: work-queue counter (256 bytes), proposal slots (n bytes,
-// with VG_NAV_LEARNED), then the sort arrays (keys first).
+// Workspace of a scheduled step: work-queue counter (256 bytes) and the relocation points
+// of the split step (3 n doubles, in visiting order) with VG_NAV_QUEUE, proposal slots (n
+// bytes) with VG_NAV_LEARNED, then the sort arrays (keys first).
 struct StepWs {
   unsigned long long *counter = nullptr;
+  double *reloc               = nullptr;
   int8_t *slots               = nullptr;
   unsigned char *sort         = nullptr;
 };
@@ -155,6 +157,8 @@ StepWs step_ws(void *ws, size_t n, uint32_t flags)
   if (flags & VG_NAV_QUEUE) {
     r.counter = reinterpret_cast<unsigned long long *>(w);
     w += 256;
+    r.reloc = reinterpret_cast<double *>(w);
+    w += (3 * n * sizeof(double) + 255) & ~size_t(255);
   }
   if (flags & VG_NAV_LEARNED) {
     r.slots = reinterpret_cast<int8_t *>(w);
@@ -204,8 +208,10 @@ int step_launch(const vg_geom *g, vg::StepArgs a, uint32_t flags, void *ws, size
     }
     a.proposal = w.slots;
   }
-  if (flags & VG_NAV_QUEUE)
-    e = vg::launch_step_mixed_queue(g->geo.dev, a, counter, g->queue_blocks, s);
+  if (flags & VG_NAV_QUEUE) {
+    a.reloc = w.reloc;
+    e       = vg::launch_step_mixed_queue(g->geo.dev, a, counter, g->queue_blocks, s);
+  }
   else
     e = vg::launch_step(g->geo.dev, a, flags & VG_PREC_MIXED, s);
   return e == cudaSuccess ? VG_OK : cuda_fail(e, "navigation step launch");

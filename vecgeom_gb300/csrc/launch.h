@@ -23,6 +23,8 @@ struct StepArgs {
   const uint32_t *order = nullptr; // optional visiting order (track indices); null: 0..n-1
   const int8_t *proposal = nullptr; // optional learned first subtree per track (-1: none)
   const unsigned int *n_dev = nullptr; // optional device count: only the first min(n, *n_dev) entries
+  double *reloc = nullptr; // split step (work-queue configurations 5-8): 3 n doubles, the
+                           // relocation point of the i-th visited track at i, n + i, 2n + i
 };
 
 // Sort key of a track: logical volume of its state above 3*cell_bits Morton bits of its

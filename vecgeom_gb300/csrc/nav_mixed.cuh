@@ -529,13 +529,19 @@ __device__ __forceinline__ double step_before_relocation_mixed(const DevGeom &g,
   return step;
 }
 
-// The relocation of a step: lp, ld and step as step_before_relocation_mixed saw and returned
-// them, `out` as it left it.
-__device__ __forceinline__ void relocate_after_step_mixed(const DevGeom &g, const ShapeLB *lbs, V3 lp, V3 ld,
-                                                          double step, int reloc, NavState &out, int &status)
+// The point a step's relocation starts from: lp, ld and step as step_before_relocation_mixed
+// saw and returned them (VNavigator.h:478-490, the point pushed 1e-6 mm past the boundary).
+__device__ __forceinline__ V3 relocation_point(V3 lp, V3 ld, double step)
 {
   const double s = step + 1E-6;
-  const V3 after{lp.x + s * ld.x, lp.y + s * ld.y, lp.z + s * ld.z};
+  return V3{lp.x + s * ld.x, lp.y + s * ld.y, lp.z + s * ld.z};
+}
+
+// The relocation of a step from its relocation point, `out` as step_before_relocation_mixed
+// left it.
+__device__ __forceinline__ void relocate_from_point_mixed(const DevGeom &g, const ShapeLB *lbs, V3 after, int reloc,
+                                                          NavState &out, int &status)
+{
   if (reloc == kRelocExit) {
     relocate_force_different_mixed(g, lbs, after, out.navInd, status);
   } else {
@@ -543,6 +549,12 @@ __device__ __forceinline__ void relocate_after_step_mixed(const DevGeom &g, cons
     out.navInd    = f64::nav_pop(g, out.navInd);
     locate_global_point_mixed(g, lbs, hit, f64::to_local(g.pv_xf[hit], after), out.navInd, false, status);
   }
+}
+
+__device__ __forceinline__ void relocate_after_step_mixed(const DevGeom &g, const ShapeLB *lbs, V3 lp, V3 ld,
+                                                          double step, int reloc, NavState &out, int &status)
+{
+  relocate_from_point_mixed(g, lbs, relocation_point(lp, ld, step), reloc, out, status);
 }
 
 __device__ __forceinline__ double compute_step_mixed(const DevGeom &g, const ShapeLB *lbs, V3 gp, V3 gd, double limit,

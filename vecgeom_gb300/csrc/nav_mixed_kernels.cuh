@@ -72,12 +72,13 @@ __global__ void __launch_bounds__(Threads, MinBlocks) k_step_mixed_queue(const D
 }
 
 // Split step (queue configurations 5-8): the first kernel computes each step up to its
-// relocation and leaves the relocation code in the out-state's first pad byte; the second
-// kernel relocates those tracks over the same visiting order, recomputing the local point
-// and direction from the input state, and clears the byte. Each kernel's body is about half
-// of the fused one (fewer instruction-cache misses, its own register budget). Results are
-// those of the fused kernel: the same operations on the same values.
-__device__ __forceinline__ void step_one_mixed_split(const DevGeom &g, const StepArgs &a, size_t t)
+// relocation, leaves the relocation code in the out-state's first pad byte and the
+// relocation point (FP64) in a.reloc at the track's visiting position; the second kernel
+// relocates those tracks over the same visiting order, reading that point back with
+// coalesced loads, and clears the byte. Each kernel's body is about half of the fused one
+// (fewer instruction-cache misses, its own register budget). Results are those of the fused
+// kernel: the same operations on the same values.
+__device__ __forceinline__ void step_one_mixed_split(const DevGeom &g, const StepArgs &a, size_t t, size_t i)
 {
   const NavState s = a.in[t];
   NavState o       = s;
@@ -92,6 +93,12 @@ __device__ __forceinline__ void step_one_mixed_split(const DevGeom &g, const Ste
     const f64::V3 ld = f64::rotate(m, f64::V3{__ldg(a.dx + t), __ldg(a.dy + t), __ldg(a.dz + t)});
     step = mixed::step_before_relocation_mixed(g, lp, ld, lim, s, o, st, a.nvisited ? &nv : nullptr,
                                                a.proposal ? (int)__ldg(a.proposal + t) : -1, reloc);
+    if (reloc != mixed::kRelocNone) {
+      const f64::V3 q = mixed::relocation_point(lp, ld, step);
+      a.reloc[i]           = q.x;
+      a.reloc[a.n + i]     = q.y;
+      a.reloc[2 * a.n + i] = q.z;
+    }
   }
   o.pad[0]  = (uint8_t)reloc;
   a.step[t] = step;
@@ -101,18 +108,15 @@ __device__ __forceinline__ void step_one_mixed_split(const DevGeom &g, const Ste
 }
 
 __device__ __forceinline__ void relocate_one_mixed(const DevGeom &g, const mixed::ShapeLB *lbs, const StepArgs &a,
-                                                   size_t t)
+                                                   size_t t, size_t i)
 {
   NavState o = a.out[t];
   if (o.pad[0] == mixed::kRelocNone) return;
-  const int reloc  = o.pad[0];
-  o.pad[0]         = 0;
-  const NavState s = a.in[t];
-  const Xform m    = f64::nav_top_matrix(g, s.navInd);
-  const f64::V3 lp = f64::to_local(m, f64::V3{__ldg(a.x + t), __ldg(a.y + t), __ldg(a.z + t)});
-  const f64::V3 ld = f64::rotate(m, f64::V3{__ldg(a.dx + t), __ldg(a.dy + t), __ldg(a.dz + t)});
-  int st           = kTrackOk;
-  mixed::relocate_after_step_mixed(g, lbs, lp, ld, a.step[t], reloc, o, st);
+  const int reloc = o.pad[0];
+  o.pad[0]        = 0;
+  const f64::V3 q{a.reloc[i], a.reloc[a.n + i], a.reloc[2 * a.n + i]};
+  int st = kTrackOk;
+  mixed::relocate_from_point_mixed(g, lbs, q, reloc, o, st);
   a.out[t] = o;
   if (a.status) a.status[t] = st;
 }
@@ -132,9 +136,9 @@ __global__ void __launch_bounds__(Threads, MinBlocks) k_step_mixed_split(const D
     if (i >= a.n) continue;
     const size_t t = a.order ? (size_t)__ldg(a.order + i) : i;
     if (Relocate)
-      relocate_one_mixed(g, lbs, a, t);
+      relocate_one_mixed(g, lbs, a, t, i);
     else
-      step_one_mixed_split(g, a, t);
+      step_one_mixed_split(g, a, t, i);
   }
 }
 

@@ -11,6 +11,7 @@ cudaError_t launch_step_mixed_queue(const DevGeom &g, const StepArgs &a, unsigne
                                     int blocks_per_sm, cudaStream_t s)
 {
   if (a.n == 0) return cudaSuccess;
+  if (blocks_per_sm > 4 && !a.reloc) blocks_per_sm -= 4; // no relocation buffer: the fused kernel
   if (blocks_per_sm == 8) return launch_queue_split<128, 5>(g, a, counter, s);
   if (blocks_per_sm == 7) return launch_queue_split<128, 3>(g, a, counter, s);
   if (blocks_per_sm == 6) return launch_queue_split<256, 2>(g, a, counter, s);

@@ -1,9 +1,9 @@
 // Fixed device scratch for vg_nav_compute_step_and_next_volume_noalloc: the work-queue
-// counter, the per-track proposal slots, and the sort keys, track order and radix counts of
-// a scheduled navigation step, held in one file-scope device array instead of a
-// caller-supplied or allocated workspace.
+// counter, the relocation points of the split step, the per-track proposal slots, and the
+// sort keys, track order and radix counts of a scheduled navigation step, held in one
+// file-scope device array instead of a caller-supplied or allocated workspace.
 //
-// Capacity: kNoAllocMaxTracks tracks per call (17.3 MiB of scratch per device). The array
+// Capacity: kNoAllocMaxTracks tracks per call (41.3 MiB of scratch per device). The array
 // exists once per device, so calls that overlap in time (on different streams or host
 // threads) share it and race; callers serialise them. The first call on a device looks up
 // the array's address (cudaGetSymbolAddress, which may load this module), so it belongs
@@ -18,13 +18,13 @@ namespace {
 
 constexpr size_t kNoAllocMaxTracks = size_t(1) << 20;
 // The layout of a step workspace with every scheduling flag at kNoAllocMaxTracks tracks:
-// 256-byte counter block, one proposal slot byte per track (256-aligned), four track
-// arrays of 4 bytes per track (keys and values, twice), 256 digit counts per 4096-track
-// tile and 256 digit totals. noalloc_check_capacity() compares this with the workspace
+// 256-byte counter block, three relocation coordinates (doubles) per track, one proposal
+// slot byte per track (256-aligned), four track arrays of 4 bytes per track (keys and
+// values, twice), 256 digit counts per 4096-track tile and 256 digit totals. noalloc_check_capacity() compares this with the workspace
 // size the step launch asks for, so the two cannot drift apart unnoticed.
 constexpr size_t kNoAllocTiles        = (kNoAllocMaxTracks + 4095) / 4096;
-constexpr size_t kNoAllocScratchBytes = 256 + kNoAllocMaxTracks + 4 * (kNoAllocMaxTracks * 4) +
-                                        256 * kNoAllocTiles * 4 + 256 * 4;
+constexpr size_t kNoAllocScratchBytes = 256 + 3 * 8 * kNoAllocMaxTracks + kNoAllocMaxTracks +
+                                        4 * (kNoAllocMaxTracks * 4) + 256 * kNoAllocTiles * 4 + 256 * 4;
 static_assert(kNoAllocMaxTracks % 256 == 0 && (256 * kNoAllocTiles * 4) % 256 == 0,
               "no-allocation scratch segments must stay 256-byte aligned");
 
