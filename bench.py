@@ -46,6 +46,10 @@ FP64_OPS_PER_STEP = {"fused": 3.0 + 10.2 + 289.4, "split": 3.0 + 10.2 + 279.1 + 
 # relocation kernel 119.2 + 4.9 MB. Configurations not captured report null.
 STEP_TRAFFIC_PER_STEP = {4: (727.3e6 + 297.5e6) / (1 << 20),
                          6: (464.9e6 + 141.6e6 + 119.2e6 + 4.9e6) / (1 << 20)}
+# name -> (precision | scheduling flags): 1 = VG_PREC_MIXED, 2 = VG_NAV_SORT, 4 = VG_NAV_QUEUE
+# 8 = VG_NAV_LEARNED (explore the BVH subtree proposed by the trained model first)
+SCHEDULES = {"fp64": 0, "fp64_sort": 2, "mixed": 1, "mixed_sort": 3, "mixed_queue": 5, "mixed_sort_queue": 7,
+             "mixed_sort_queue_learned": 15}
 
 
 def parse():

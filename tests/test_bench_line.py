@@ -80,3 +80,15 @@ def test_nav_parity_compares_all_state_fields():
     g["pad"][2] = 9  # padding is not part of the state
     r = bench.nav_parity(g, np.zeros(3), o, np.zeros(3))
     assert r["state_mismatch"] == 1 and r["next_volume_mismatch"] == 0
+
+
+def test_arguments_parse(monkeypatch):
+    """The command lines the benchmark is run with parse (the driver's, the reference arm's,
+    the profiling one), and every schedule the parser offers is defined."""
+    import sys
+    for argv in (["--gpus", "1", "--steps", "20", "--warmup", "5"], ["--impl", "reference"],
+                 ["--tracks", "1048576", "--variants", "0", "--tune", "0", "--queue-blocks", "6"]):
+        monkeypatch.setattr(sys, "argv", ["bench.py", *argv])
+        a = bench.parse()
+        assert a.schedule in bench.SCHEDULES
+    assert set(bench.SCHEDULES) >= {"fp64", "fp64_sort", "mixed_sort_queue", "mixed_sort_queue_learned"}
