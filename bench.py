@@ -656,6 +656,7 @@ def main():
         "value": value, "ms_per_step": ms_head, "n": n, "ws": ws, "args": args, "pool": pool,
         "ms_fp64": ms_fp64, "ms_fp64_sort": variants.get("fp64_sort"), "ids_equal": ids_equal, "step_err": step_err,
         "e2e_value": ws * n / e2e_s, "e2e_calls": e2e_calls, "head": head, "passes": passes,
+        "step_kernels": 2 if (split and head & 4) else 1,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak,
                      "traffic": STEP_TRAFFIC_PER_STEP[queue_cfg] * n
@@ -777,7 +778,8 @@ def headline_line(m):
         "e2e": {"value": m["e2e_value"], "unit": UNIT, "h2d_bytes_per_step": n * (48 + 12),
                 "d2h_bytes_per_step": n * (12 + 8), "ms_per_call": m["e2e_calls"]},
         "roofline": m["roofline"], "roofline_fp64": m["roofline_fp64"],
-        "gpu_launches": args.steps * (1 + ((1 + 3 * m["passes"]) if m["head"] & 2 else 0) + (1 if m["head"] & 8 else 0)),
+        "gpu_launches": args.steps * (m.get("step_kernels", 1) + ((1 + 3 * m["passes"]) if m["head"] & 2 else 0)
+                                      + (1 if m["head"] & 8 else 0)),
         "track_errors": m["n_err"], "clocks": m["clocks"],
     }
     par = m.get("parity")
