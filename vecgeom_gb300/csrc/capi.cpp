@@ -33,11 +33,14 @@ struct vg_geom {
   static constexpr int kCopyChunks = 4;
   cudaStream_t copy_stream           = nullptr;
   cudaEvent_t chunk_ready[kCopyChunks] = {};
+  cudaEvent_t steps_ready = nullptr, steps_copied = nullptr; // step lengths back while the relocation runs
   ~vg_geom()
   {
     if (staging) cudaFree(staging);
     for (cudaEvent_t ev : chunk_ready)
       if (ev) cudaEventDestroy(ev);
+    if (steps_ready) cudaEventDestroy(steps_ready);
+    if (steps_copied) cudaEventDestroy(steps_copied);
     if (copy_stream) cudaStreamDestroy(copy_stream);
   }
 };
@@ -918,6 +921,8 @@ int vg_nav_compute_step_and_next_volume_host(vg_geom *g, const double *x, const 
       e = cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking);
       for (int c = 0; c < vg_geom::kCopyChunks && e == cudaSuccess; ++c)
         e = cudaEventCreateWithFlags(&g->chunk_ready[c], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->steps_ready, cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->steps_copied, cudaEventDisableTiming);
       if (e != cudaSuccess) return cuda_fail(e, "copy stream setup");
     }
     const StepWs w = step_ws(dws, n, flags);
@@ -949,10 +954,23 @@ int vg_nav_compute_step_and_next_volume_host(vg_geom *g, const double *x, const 
     if (e == cudaSuccess) e = cudaMemcpyAsync(din, in, ns, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return cuda_fail(e, "host-to-device copy");
   }
+  // With the work queue the launcher records steps_ready once the step lengths are final
+  // (before a split step's relocation kernel), so they travel back on the copy stream while
+  // the relocation still runs; the out-states follow the whole step.
+  const bool early_steps = pipelined && (flags & VG_NAV_QUEUE);
+  if (early_steps) a.steps_done = g->steps_ready;
   const int rc = step_launch(g, a, flags, dws, wsb, s, pipelined);
   if (rc != VG_OK) return rc;
-  e = cudaMemcpyAsync(out, dout, ns, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(step, d[7], nd, cudaMemcpyDeviceToHost, s);
+  if (early_steps) {
+    e = cudaStreamWaitEvent(g->copy_stream, g->steps_ready, 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(step, d[7], nd, cudaMemcpyDeviceToHost, g->copy_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(g->steps_copied, g->copy_stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, ns, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, g->steps_copied, 0);
+  } else {
+    e = cudaMemcpyAsync(out, dout, ns, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(step, d[7], nd, cudaMemcpyDeviceToHost, s);
+  }
   if (e == cudaSuccess && status) e = cudaMemcpyAsync(status, dst, ni, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   return e == cudaSuccess ? VG_OK : cuda_fail(e, "device-to-host copy");

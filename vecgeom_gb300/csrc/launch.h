@@ -25,6 +25,8 @@ struct StepArgs {
   const unsigned int *n_dev = nullptr; // optional device count: only the first min(n, *n_dev) entries
   double *reloc = nullptr; // split step (work-queue configurations 5-8): 3 n doubles, the
                            // relocation point of the i-th visited track at i, n + i, 2n + i
+  cudaEvent_t steps_done = nullptr; // optional: recorded once step[] is final (the work-queue
+                                    // launcher records it before a split step's relocation)
 };
 
 // Sort key of a track: logical volume of its state above 3*cell_bits Morton bits of its

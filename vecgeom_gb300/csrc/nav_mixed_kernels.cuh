@@ -121,8 +121,11 @@ __device__ __forceinline__ void relocate_one_mixed(const DevGeom &g, const mixed
   if (a.status) a.status[t] = st;
 }
 
+// The relocation kernel (72 registers unbounded) waits on memory: it gets a 64-register
+// budget, for 32 resident warps per SM.
 template <int Threads, int MinBlocks, bool Relocate>
-__global__ void __launch_bounds__(Threads, MinBlocks) k_step_mixed_split(const DevGeom g, const StepArgs a,
+__global__ void __launch_bounds__(Threads, Relocate ? 1024 / Threads : MinBlocks)
+    k_step_mixed_split(const DevGeom g, const StepArgs a,
                                                                          unsigned long long *__restrict__ counter)
 {
   const mixed::ShapeLB *lbs = reinterpret_cast<const mixed::ShapeLB *>(g.shape_lbd);
@@ -357,6 +360,7 @@ template <int Threads, int MinBlocks>
 cudaError_t launch_queue_split(const DevGeom &g, const StepArgs &a, unsigned long long *counter, cudaStream_t s)
 {
   cudaError_t e = launch_split<Threads, MinBlocks, false>(g, a, counter, s);
+  if (e == cudaSuccess && a.steps_done) e = cudaEventRecord(a.steps_done, s); // step[] is final
   if (e == cudaSuccess) e = launch_split<Threads, MinBlocks, true>(g, a, counter, s);
   return e;
 }

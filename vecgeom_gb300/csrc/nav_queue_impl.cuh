@@ -16,9 +16,15 @@ cudaError_t launch_step_mixed_queue(const DevGeom &g, const StepArgs &a, unsigne
   if (blocks_per_sm == 7) return launch_queue_split<128, 3>(g, a, counter, s);
   if (blocks_per_sm == 6) return launch_queue_split<256, 2>(g, a, counter, s);
   if (blocks_per_sm == 5) return launch_queue_split<256, 1>(g, a, counter, s);
-  if (blocks_per_sm == 4) return launch_queue<128, 5>(g, a, counter, s);
-  if (blocks_per_sm == 3) return launch_queue<128, 3>(g, a, counter, s);
-  return blocks_per_sm == 2 ? launch_queue<256, 2>(g, a, counter, s) : launch_queue<256, 1>(g, a, counter, s);
+  cudaError_t e;
+  if (blocks_per_sm == 4)
+    e = launch_queue<128, 5>(g, a, counter, s);
+  else if (blocks_per_sm == 3)
+    e = launch_queue<128, 3>(g, a, counter, s);
+  else
+    e = blocks_per_sm == 2 ? launch_queue<256, 2>(g, a, counter, s) : launch_queue<256, 1>(g, a, counter, s);
+  if (e == cudaSuccess && a.steps_done) e = cudaEventRecord(a.steps_done, s);
+  return e;
 }
 
 } // namespace VG_NAV_SET
