@@ -125,8 +125,7 @@ __device__ __forceinline__ void relocate_one_mixed(const DevGeom &g, const mixed
 // budget, for 32 resident warps per SM.
 template <int Threads, int MinBlocks, bool Relocate>
 __global__ void __launch_bounds__(Threads, Relocate ? 1024 / Threads : MinBlocks)
-    k_step_mixed_split(const DevGeom g, const StepArgs a,
-                                                                         unsigned long long *__restrict__ counter)
+    k_step_mixed_split(const DevGeom g, const StepArgs a, unsigned long long *__restrict__ counter)
 {
   const mixed::ShapeLB *lbs = reinterpret_cast<const mixed::ShapeLB *>(g.shape_lbd);
   const int lane            = threadIdx.x & 31;
