@@ -587,7 +587,7 @@ def main():
         torch.cuda.synchronize()
         ms_sort = e0.elapsed_time(e1) / args.steps
         _, _, cb, lb = geo.sort_key_params()
-        passes = (lb + 3 * cb + 7) // 8
+        passes = (lb + 3 * cb + 8) // 9  # 9-bit radix digits
     # the learned proposal alone (features + MLP inference), also part of the headline step
     ms_propose = 0.0
     if head & vg.NAV_LEARNED:

@@ -293,7 +293,7 @@ int vg_nav_compute_step_and_next_volume_ws(const vg_geom *g, const double *x, co
                                            uint32_t flags, void *workspace, size_t workspace_bytes, void *stream);
 
 /* The scheduled step without any allocation and without a caller workspace: scratch is a
- * fixed 41.3 MiB device array inside the library (capacity 2^20 tracks per call with any
+ * fixed 41.5 MiB device array inside the library (capacity 2^20 tracks per call with any
  * flags, VG_NAV_LEARNED's proposal slots included; larger n is rejected with VG_EINVAL).
  * No reference counterpart: it exists for callers that may not allocate device memory on
  * the step path. Calls that overlap in time share the scratch and race, so callers

@@ -3,7 +3,7 @@
 // sort keys, track order and radix counts of a scheduled navigation step, held in one
 // file-scope device array instead of a caller-supplied or allocated workspace.
 //
-// Capacity: kNoAllocMaxTracks tracks per call (41.3 MiB of scratch per device). The array
+// Capacity: kNoAllocMaxTracks tracks per call (41.5 MiB of scratch per device). The array
 // exists once per device, so calls that overlap in time (on different streams or host
 // threads) share it and race; callers serialise them. The first call on a device looks up
 // the array's address (cudaGetSymbolAddress, which may load this module), so it belongs
@@ -20,12 +20,12 @@ constexpr size_t kNoAllocMaxTracks = size_t(1) << 20;
 // The layout of a step workspace with every scheduling flag at kNoAllocMaxTracks tracks:
 // 256-byte counter block, three relocation coordinates (doubles) per track, one proposal
 // slot byte per track (256-aligned), four track arrays of 4 bytes per track (keys and
-// values, twice), 256 digit counts per 4096-track tile and 256 digit totals. noalloc_check_capacity() compares this with the workspace
+// values, twice), 512 digit counts per 4096-track tile and 512 digit totals. noalloc_check_capacity() compares this with the workspace
 // size the step launch asks for, so the two cannot drift apart unnoticed.
 constexpr size_t kNoAllocTiles        = (kNoAllocMaxTracks + 4095) / 4096;
 constexpr size_t kNoAllocScratchBytes = 256 + 3 * 8 * kNoAllocMaxTracks + kNoAllocMaxTracks +
-                                        4 * (kNoAllocMaxTracks * 4) + 256 * kNoAllocTiles * 4 + 256 * 4;
-static_assert(kNoAllocMaxTracks % 256 == 0 && (256 * kNoAllocTiles * 4) % 256 == 0,
+                                        4 * (kNoAllocMaxTracks * 4) + 512 * kNoAllocTiles * 4 + 512 * 4;
+static_assert(kNoAllocMaxTracks % 256 == 0 && (512 * kNoAllocTiles * 4) % 256 == 0,
               "no-allocation scratch segments must stay 256-byte aligned");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];

@@ -3,7 +3,9 @@
 // LSD radix sort of (key, track index) pairs with 8-bit digits. The step kernels then walk
 // tracks in key order, so a warp's 32 lanes share the mother shape, the BVH and mostly the
 // BVH path. The sort only permutes work: every track's result is computed exactly as in
-// the unsorted launch and written at the track's own index.
+// the unsorted launch and written at the track's own index. Digits are 9 bits wide (512
+// buckets), so the 26-bit keys of the tuned detector sort (7 Morton bits per axis beside the
+// logical volume) take three passes instead of four.
 #include "launch.h"
 
 namespace vg {
@@ -13,6 +15,9 @@ constexpr int kSortBlock = 256;
 constexpr int kSortItems = 16;
 constexpr int kSortTile  = kSortBlock * kSortItems;
 constexpr int kSortWarps = kSortBlock / 32;
+constexpr int kDigitBits = 9;
+constexpr int kRadix     = 1 << kDigitBits; // buckets per pass: two per thread of a block
+static_assert(kRadix == 2 * kSortBlock, "each thread scans two digits");
 
 inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
@@ -66,18 +71,18 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_hist(const uint32_t *__res
                                                            const unsigned int *__restrict__ n_dev)
 {
   if (n_dev && *n_dev < n) n = *n_dev;
-  __shared__ uint32_t h[256];
-  h[threadIdx.x] = 0u;
+  __shared__ uint32_t h[kRadix];
+  for (int k = threadIdx.x; k < kRadix; k += kSortBlock) h[k] = 0u;
   __syncthreads();
   const size_t base = (size_t)blockIdx.x * kSortTile;
   for (int r = 0; r < kSortItems; ++r) {
     const size_t i    = base + (size_t)r * kSortBlock + threadIdx.x;
-    const uint32_t d  = i < n ? (__ldg(keys + i) >> shift) & 255u : 256u;
+    const uint32_t d  = i < n ? (__ldg(keys + i) >> shift) & (kRadix - 1u) : (uint32_t)kRadix;
     const uint32_t pm = __match_any_sync(0xffffffffu, d);
-    if (d < 256u && (pm & ((1u << (threadIdx.x & 31)) - 1u)) == 0u) atomicAdd(&h[d], (uint32_t)__popc(pm));
+    if (d < (uint32_t)kRadix && (pm & ((1u << (threadIdx.x & 31)) - 1u)) == 0u) atomicAdd(&h[d], (uint32_t)__popc(pm));
   }
   __syncthreads();
-  hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+  for (int k = threadIdx.x; k < kRadix; k += kSortBlock) hist[(size_t)k * ntiles + blockIdx.x] = h[k];
 }
 
 // Exclusive block-wide scan of one value per thread (blockDim.x a multiple of 32, <= 1024);
@@ -139,10 +144,10 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_scatter(const uint32_t *__
                                                               const unsigned int *__restrict__ n_dev)
 {
   if (n_dev && *n_dev < n) n = *n_dev;
-  __shared__ uint32_t cnt[kSortWarps][256];
+  __shared__ uint32_t cnt[kSortWarps][kRadix];
   __shared__ uint32_t wsum[33];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int k = threadIdx.x; k < kSortWarps * 256; k += kSortBlock) (&cnt[0][0])[k] = 0u;
+  for (int k = threadIdx.x; k < kSortWarps * kRadix; k += kSortBlock) (&cnt[0][0])[k] = 0u;
   __syncthreads();
   const size_t base = (size_t)blockIdx.x * kSortTile + (size_t)w * (32 * kSortItems);
   const uint32_t lt = (1u << lane) - 1u;
@@ -153,7 +158,7 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_scatter(const uint32_t *__
     const bool ok   = i < n;
     key[r]          = ok ? __ldg(kin + i) : 0u;
     val[r]          = ok ? (vin ? __ldg(vin + i) : (list ? __ldg(list + i) : (uint32_t)i)) : 0u;
-    const uint32_t d  = ok ? (key[r] >> shift) & 255u : 256u;
+    const uint32_t d  = ok ? (key[r] >> shift) & (kRadix - 1u) : (uint32_t)kRadix;
     const uint32_t pm = __match_any_sync(0xffffffffu, d);
     const uint32_t before = ok ? cnt[w][d] : 0u;
     __syncwarp();
@@ -163,13 +168,20 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_scatter(const uint32_t *__
   }
   __syncthreads();
   {
-    const uint32_t d = threadIdx.x;
+    // digits 2t and 2t + 1: their start = the totals of all lower digits + this row's
+    // count in the tiles before this one, then each warp's share in warp order
+    const uint32_t d0 = 2u * threadIdx.x, d1 = d0 + 1u;
+    const uint32_t t0 = __ldg(totals + d0), t1 = __ldg(totals + d1);
     uint32_t tot;
-    uint32_t run = block_exclusive_scan(__ldg(totals + d), wsum, &tot) + __ldg(hist + (size_t)d * ntiles + blockIdx.x);
+    const uint32_t below = block_exclusive_scan(t0 + t1, wsum, &tot);
+    uint32_t run0        = below + __ldg(hist + (size_t)d0 * ntiles + blockIdx.x);
+    uint32_t run1        = below + t0 + __ldg(hist + (size_t)d1 * ntiles + blockIdx.x);
     for (int ww = 0; ww < kSortWarps; ++ww) {
-      const uint32_t c = cnt[ww][d];
-      cnt[ww][d]       = run;
-      run += c;
+      const uint32_t c0 = cnt[ww][d0], c1 = cnt[ww][d1];
+      cnt[ww][d0]       = run0;
+      cnt[ww][d1]       = run1;
+      run0 += c0;
+      run1 += c1;
     }
   }
   __syncthreads();
@@ -177,7 +189,7 @@ __global__ void __launch_bounds__(kSortBlock) k_radix_scatter(const uint32_t *__
   for (int r = 0; r < kSortItems; ++r) {
     const size_t i = base + (size_t)r * 32 + lane;
     if (i < n) {
-      const uint32_t pos = cnt[w][(key[r] >> shift) & 255u] + rank[r];
+      const uint32_t pos = cnt[w][(key[r] >> shift) & (kRadix - 1u)] + rank[r];
       kout[pos]          = key[r];
       vout[pos]          = val[r];
     }
@@ -197,7 +209,7 @@ inline unsigned grid_for(size_t n, int block)
 size_t nav_sort_workspace_bytes(size_t n)
 {
   const size_t ntiles = (n + kSortTile - 1) / kSortTile;
-  return 4 * align256(n * sizeof(uint32_t)) + align256(256 * ntiles * sizeof(uint32_t)) + 256 * sizeof(uint32_t);
+  return 4 * align256(n * sizeof(uint32_t)) + align256(kRadix * ntiles * sizeof(uint32_t)) + kRadix * sizeof(uint32_t);
 }
 
 const uint32_t *nav_sort_keys_of(const uint32_t *order, const void *ws, size_t n)
@@ -232,18 +244,18 @@ cudaError_t launch_nav_sort(const DevGeom &g, const SortKeyParams &p, const doub
   uint32_t *k0 = reinterpret_cast<uint32_t *>(w), *k1 = reinterpret_cast<uint32_t *>(w + a);
   uint32_t *v0 = reinterpret_cast<uint32_t *>(w + 2 * a), *v1 = reinterpret_cast<uint32_t *>(w + 3 * a);
   uint32_t *hist   = reinterpret_cast<uint32_t *>(w + 4 * a);
-  uint32_t *totals = reinterpret_cast<uint32_t *>(w + 4 * a + align256(256 * (size_t)ntiles * sizeof(uint32_t)));
+  uint32_t *totals = reinterpret_cast<uint32_t *>(w + 4 * a + align256(kRadix * (size_t)ntiles * sizeof(uint32_t)));
   if (!keys_done) k_sort_keys<<<grid_for(n, 256), 256, 0, s>>>(g, p, x, y, z, in, list, 0, n, k0, n_dev);
   // Digits above the key's width are all zero (invalid states carry all-ones keys, which
   // sort last within every pass), so only the passes that cover the key bits are run.
   const int bits   = sort_key_bits(p);
-  const int passes = (bits + 7) / 8;
+  const int passes = (bits + kDigitBits - 1) / kDigitBits;
   uint32_t *kin = k0, *kout = k1, *vin = nullptr, *vout = v0;
   for (int ps = 0; ps < passes; ++ps) {
-    k_radix_hist<<<ntiles, kSortBlock, 0, s>>>(kin, n, 8 * ps, hist, ntiles, n_dev);
-    k_scan_rows<<<256, 1024, 0, s>>>(hist, ntiles, totals);
-    k_radix_scatter<<<ntiles, kSortBlock, 0, s>>>(kin, vin, kout, vout, n, 8 * ps, hist, totals, ntiles, list,
-                                                  n_dev);
+    k_radix_hist<<<ntiles, kSortBlock, 0, s>>>(kin, n, kDigitBits * ps, hist, ntiles, n_dev);
+    k_scan_rows<<<kRadix, 1024, 0, s>>>(hist, ntiles, totals);
+    k_radix_scatter<<<ntiles, kSortBlock, 0, s>>>(kin, vin, kout, vout, n, kDigitBits * ps, hist, totals, ntiles,
+                                                  list, n_dev);
     uint32_t *tk = kin;
     kin          = kout;
     kout         = tk;
