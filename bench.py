@@ -545,7 +545,7 @@ def main():
     tuning = None
     if args.tune and head & (vg.NAV_SORT | vg.NAV_QUEUE):
         from vecgeom_gb300.tune import autotune
-        cands = [(head, b, q) for b in (0, 7, 5) for q in (tuple(range(1, 9)) if head & vg.NAV_QUEUE else (1,))]
+        cands = [(head, b, q) for b in (0, 7, 6, 5) for q in (tuple(range(1, 9)) if head & vg.NAV_QUEUE else (1,))]
         tuning = autotune(geo, t, st, candidates=cands, cache=None)
     elif args.cell_bits or args.queue_blocks:
         geo.set_tuning(args.cell_bits, args.queue_blocks)
