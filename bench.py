@@ -42,10 +42,10 @@ STEP_BYTES = 24 + 24 + 12 + 12 + 8  # p, d, state in, state out, step (FP64 SoA 
 FP64_OPS_PER_STEP = {"fused": 3.0 + 10.2 + 289.4, "split": 3.0 + 10.2 + 279.1 + 14.5}
 # DRAM bytes per step of the step kernel launch(es) by work-queue configuration, from one ncu
 # capture each on 2^20 steps (spills included), scaled to the bench launch by its steps:
-# fused 128 x 5: read 727.3 MB + write 297.5 MB; split 256 x 2: step kernel 464.9 + 141.6 MB,
-# relocation kernel 119.2 + 4.9 MB. Configurations not captured report null.
+# fused 128 x 5: read 727.3 MB + write 297.5 MB; split 256 x 2: step kernel 464.5 + 141.1 MB,
+# relocation kernel 122.1 + 5.5 MB. Configurations not captured report null.
 STEP_TRAFFIC_PER_STEP = {4: (727.3e6 + 297.5e6) / (1 << 20),
-                         6: (464.9e6 + 141.6e6 + 119.2e6 + 4.9e6) / (1 << 20)}
+                         6: (464.5e6 + 141.1e6 + 122.1e6 + 5.5e6) / (1 << 20)}
 # name -> (precision | scheduling flags): 1 = VG_PREC_MIXED, 2 = VG_NAV_SORT, 4 = VG_NAV_QUEUE
 # 8 = VG_NAV_LEARNED (explore the BVH subtree proposed by the trained model first)
 SCHEDULES = {"fp64": 0, "fp64_sort": 2, "mixed": 1, "mixed_sort": 3, "mixed_queue": 5, "mixed_sort_queue": 7,
