@@ -214,3 +214,22 @@ def test_geometry_save_and_load_replay(tmp_path):
     bad.write_bytes(b"not a geometry file at all")
     with pytest.raises(vg.VGError):
         vg.Geometry.load(str(bad))
+
+
+def test_workspace_sizes_and_no_allocation_capacity():
+    """Workspace sizes are host arithmetic (no GPU): the scheduled step's workspace grows by
+    its parts (work-queue counter and relocation points, proposal slots, sort arrays), and
+    the no-allocation entry point's fixed scratch (documented as 41.5 MiB) holds the
+    workspace of its largest call, 2^20 tracks with every scheduling flag."""
+    lib = vg.load_library()
+    ws = lib.vg_nav_step_workspace_bytes
+    n = 1 << 20
+    align = lambda b: (b + 255) & ~255
+    every = vg.PREC_MIXED | vg.NAV_SORT | vg.NAV_QUEUE | vg.NAV_LEARNED
+    assert ws(n, vg.PREC_FP64) == 0 and ws(n, vg.PREC_MIXED) == 0
+    assert ws(n, vg.PREC_MIXED | vg.NAV_QUEUE) == 256 + align(3 * 8 * n)
+    assert ws(n, every) - ws(n, every & ~vg.NAV_LEARNED) == align(n)
+    sort_only = ws(n, vg.NAV_SORT)
+    assert ws(n, every) == 256 + align(3 * 8 * n) + align(n) + sort_only
+    assert 4 * 4 * n < sort_only < 4 * 4 * n + 2 * 512 * 4 * (n // 4096 + 1) + 4096
+    assert round(ws(n, every) / 2 ** 20, 1) == 41.5  # the size the header and noalloc.cu state
