@@ -240,9 +240,68 @@ static __device__ __noinline__ bool level_locate_far(const DevGeom &g, int lv, i
   return f64::bvh_level_locate(g, lv, excl_pv, lp, pv, dlp, status);
 }
 
+// Second pass of check_daughters_mixed (rare, out of line to keep the step kernel's body
+// small): traverses the whole tree again under the current bound and evaluates in FP64, at
+// once, every candidate whose lower bound lies from `floor_lb` (the lowest bound the first
+// pass left out of its full buffer; every lower bound the first pass kept and evaluated is
+// at most that) up to the bound. A kept candidate with a bound equal to floor_lb is
+// evaluated again, which cannot change the result.
+static __device__ __noinline__ int check_daughters_second_pass(const DevGeom &g, int node0, V3 lp, V3 ld, F3 pf, F3 ldf,
+                                                              F3 inv, float floor_lb, int last_pv, double &step,
+                                                              float &bound, int &hit_pv, int &visits)
+{
+  unsigned stack[32];
+  int sp   = 1;
+  stack[0] = 0;
+  do {
+    const unsigned id = stack[--sp];
+    ++visits;
+    const NodeF nd = g.node_f[node0 + id];
+    if (nd.nchild >= 0) {
+      for (int i = 0; i < nd.nchild; ++i) {
+        const int slot    = nd.offset + i;
+        const LeafRec *rp = g.leaf_rec + slot;
+        float blo[3], bhi[3];
+        int vol;
+        leaf_box(rp, blo, bhi, vol);
+        float tmin, tmax;
+        slab_f(blo, bhi, pf, inv, tmin, tmax);
+        if (!(tmin <= tmax && tmax >= 0.f && tmin < bound)) continue;
+        float ub;
+        const float lb = daughter_lb(rp, pf, ldf, ub);
+        if (!(lb < bound) || lb < floor_lb) continue;
+        const Xform &m    = g.pv_xf[vol];
+        const double dist =
+            f64::shape_dist_in_to(g, __ldg(&rp->type), __ldg(&rp->off), f64::to_local(m, lp), f64::rotate(m, ld));
+        if (dlt(dist, step) && !(dle(dist, 0.0) && vol == last_pv)) {
+          step   = dist;
+          hit_pv = vol;
+          bound  = fminf(bound, __double2float_ru(step));
+        }
+      }
+    } else {
+      const unsigned cl_ = 2 * id + 1, cr_ = 2 * id + 2;
+      const NodeF L = g.node_f[node0 + cl_], R = g.node_f[node0 + cr_];
+      float tminL, tmaxL, tminR, tmaxR;
+      slab_f(L.lo, L.hi, pf, inv, tminL, tmaxL);
+      slab_f(R.lo, R.hi, pf, inv, tminR, tmaxR);
+      if (sp + 2 > 32) return kTrackErrStack;
+      if (tminL <= tmaxL && tmaxL >= 0.f && tminL < bound) stack[sp++] = cl_;
+      if (tminR <= tmaxR && tmaxR >= 0.f && tminR < bound) stack[sp++] = cr_;
+    }
+  } while (sp > 0);
+  return kTrackOk;
+}
+
 // BVH::CheckDaughterIntersections with FP32 pruning (see file comment). Candidates wait in
-// a small buffer sorted by lower bound; when it is full the lowest is evaluated in FP64,
-// which tightens the step and drops every candidate that can no longer win.
+// a small buffer sorted by lower bound and are evaluated in FP64 at the end of the
+// traversal, lowest bound first, each evaluation tightening the step and dropping every
+// candidate that can no longer win. A full buffer keeps the kCandBuf lowest bounds and
+// remembers the lowest bound it left out; if that one is still below the step once the
+// buffer is evaluated, a second traversal evaluates every candidate from there up to the
+// step directly. (Evaluating the lowest buffered candidate as soon as the buffer filled, as
+// before, ran FP64 evaluations of far candidates in the middle of the traversal for tracks
+// whose daughters' boxes all contain them, such as the world volume's nested layers.)
 constexpr int kCandBuf = 8;
 
 __device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, int lv, int node0, V3 lp, V3 ld, double &step,
@@ -257,15 +316,7 @@ __device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, int lv, i
   float cl[kCandBuf] = {};
   int cp[kCandBuf]   = {}; // prim slots of the candidates
   int nc = 0;
-  auto evaluate_first = [&]() {
-    const float lb = cl[0];
-    const int slot = cp[0];
-    for (int k = 1; k < nc; ++k) cl[k - 1] = cl[k], cp[k - 1] = cp[k];
-    --nc;
-    if (lb >= bound) {
-      nc = 0;
-      return;
-    }
+  auto evaluate = [&](int slot) {
     const LeafRec *rp = g.leaf_rec + slot;
     const int vol     = __ldg(&rp->pv);
     const Xform &m    = g.pv_xf[vol];
@@ -278,11 +329,27 @@ __device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, int lv, i
       while (nc > 0 && cl[nc - 1] >= bound) --nc;
     }
   };
+  auto evaluate_first = [&]() {
+    const float lb = cl[0];
+    const int slot = cp[0];
+    for (int k = 1; k < nc; ++k) cl[k - 1] = cl[k], cp[k - 1] = cp[k];
+    --nc;
+    if (lb >= bound) {
+      nc = 0;
+      return;
+    }
+    evaluate(slot);
+  };
+  float dropped = INFINITY; // lowest lower bound left out of the full buffer
   auto add = [&](float lb, int slot) {
     if (!(lb < bound)) return;
     if (nc == kCandBuf) {
-      evaluate_first();
-      if (!(lb < bound)) return;
+      if (lb >= cl[nc - 1]) {
+        dropped = fminf(dropped, lb);
+        return;
+      }
+      dropped = fminf(dropped, cl[nc - 1]);
+      --nc;
     }
     int k = nc++;
     while (k > 0 && cl[k - 1] > lb) cl[k] = cl[k - 1], cp[k] = cp[k - 1], --k;
@@ -349,6 +416,14 @@ __device__ __forceinline__ int check_daughters_mixed(const DevGeom &g, int lv, i
     }
   } while (sp > 0);
   while (nc > 0) evaluate_first();
+  if (dropped < bound) { // the candidates left out of the full buffer may still win
+    const int st = check_daughters_second_pass(g, node0, lp, ld, pf, ldf, inv, dropped, last_pv, step, bound, hit_pv,
+                                               visits);
+    if (st != kTrackOk) {
+      if (nvisited) *nvisited = visits;
+      return st;
+    }
+  }
   if (nvisited) *nvisited = visits;
   return kTrackOk;
 }
