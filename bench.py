@@ -39,7 +39,7 @@ STEP_BYTES = 24 + 24 + 12 + 12 + 8  # p, d, state in, state out, step (FP64 SoA 
 # the step kernel, which also writes each track's relocation point, and the relocation
 # kernel that reads it (configurations 5-8). Per-thread counts do not depend on how lanes
 # group into warps, so they hold at 2^22. Counted before the candidate buffer kept its
-# lowest bounds when full; that build evaluates fewer candidates per step, so for it these
+# lowest bounds when full; the kernels now evaluate fewer candidates per step, so these
 # counts, and the FP64 fraction computed from them, are upper bounds.
 FP64_OPS_PER_STEP = {"fused": 3.0 + 10.2 + 289.4, "split": 3.0 + 10.2 + 279.1 + 14.5}
 # DRAM bytes per step of the step kernel launch(es) by work-queue configuration, from one ncu
@@ -654,7 +654,7 @@ def main():
                          "unit": "FP64 thread-ops/s", "frac": ops * n / (ms_head * 1e-3) / fp64_peak,
                          "ops_per_step": ops,
                          "note": "ncu-counted ops per step of the build before the candidate-buffer change "
-                                 "(an upper bound for this build); peak = DFMA probe timed in this run"}
+                                 "(an upper bound for the current kernels); peak = DFMA probe timed in this run"}
     m = {
         "value": value, "ms_per_step": ms_head, "n": n, "ws": ws, "args": args, "pool": pool,
         "ms_fp64": ms_fp64, "ms_fp64_sort": variants.get("fp64_sort"), "ids_equal": ids_equal, "step_err": step_err,

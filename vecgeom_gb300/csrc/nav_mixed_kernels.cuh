@@ -311,7 +311,7 @@ cudaError_t launch_transport(const DevGeom &g, const TransportArgs &a, unsigned 
 template <int Threads, int MinBlocks>
 cudaError_t launch_queue(const DevGeom &g, const StepArgs &a, unsigned long long *counter, cudaStream_t s)
 {
-  static int resident = 0; // blocks per SM (same for every device of this build)
+  static int resident = 0; // blocks per SM (the same on every device the library targets)
   if (resident == 0) {
     int r = 0;
     const cudaError_t e =
