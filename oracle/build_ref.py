@@ -1,0 +1,84 @@
+"""Build the compiled-reference oracle (test infrastructure; see compiled_ref/harness.cpp).
+
+Compiles the reference's own C++ sources in place, where they lie in the reference tree
+(VecGeom/ headers, source/*.cpp), against the scalar VecCore stand-in and the configuration
+header in oracle/compiled_ref/shim/, together with oracle/compiled_ref/harness.cpp, into
+oracle/_ref/libvgref.so. Nothing of the reference is copied into this repository and the
+reference's own build system (CMake) is not run. The flags are the hand-written oracle's
+(oracle/build.py): -O2 -std=c++17 -ffp-contract=off, so every +, -, *, / and sqrt rounds
+as in the reference's scalar FP64 build on x86-64, plus -DNDEBUG as in the reference's
+default Release build (CMakeLists.txt:40-42); its asserts are not meant to run there (the
+one at source/NavIndexTable.cpp:81 fails whenever a node's matrix needs alignment padding).
+
+Run only where the reference tree exists (VG_REFERENCE_DIR, default the sibling checkout
+named below); elsewhere `available()` is False and the tests that use it skip.
+"""
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = os.environ.get("VG_REFERENCE_DIR", "/root/reference")
+SHIM = os.path.join(HERE, "compiled_ref", "shim")
+HARNESS = os.path.join(HERE, "compiled_ref", "harness.cpp")
+OUT_DIR = os.path.join(HERE, "_ref")
+LIB = os.path.join(OUT_DIR, "libvgref.so")
+FLAGS = ["-O2", "-DNDEBUG", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-w"]
+
+# The reference's translation units on the path: geometry (logical and placed volumes,
+# transformations, the geometry manager, bounding boxes, BVHs, the navigation index table
+# and states) and the shapes the builders make, with their helpers.
+SOURCES = [
+    "GeoManager", "LogicalVolume", "PlacedVolume", "UnplacedVolume", "Transformation3D", "ABBoxManager", "BVH",
+    "BVHManager", "NavIndexTable", "NavStateIndex", "NavStatePath", "MessageLogger", "SOA3D", "AOS3D", "Vector",
+    "Scale3D", "Wedge", "Wedge_Evolution", "Planes", "Plane", "Quadrilaterals", "Rectangles", "Utils3D",
+    "ReducedPolycone", "CutPlanes", "TessellatedHelpers", "Tile", "SolidMesh", "HybridManager2",
+    "UnplacedBox", "PlacedBox", "UnplacedTube", "PlacedTube", "UnplacedCone", "PlacedCone", "UnplacedPolycone",
+    "PlacedPolycone", "UnplacedPolyhedron", "PlacedPolyhedron", "UnplacedTorus2", "PlacedTorus2", "UnplacedTrd",
+    "PlacedTrd", "UnplacedBooleanVolume", "PlacedBooleanVolume", "UnplacedTrapezoid", "PlacedTrapezoid",
+    "UnplacedSphere", "PlacedSphere", "UnplacedHype", "PlacedHype", "UnplacedGenTrap", "PlacedGenTrap",
+    "UnplacedCutTube", "PlacedCutTube", "UnplacedAssembly", "PlacedAssembly", "UnplacedScaledShape",
+    "PlacedScaledShape", "UnplacedOrb", "PlacedOrb", "UnplacedParallelepiped", "PlacedParallelepiped",
+    "UnplacedMultiUnion", "PlacedMultiUnion", "UnplacedTessellated", "PlacedTessellated", "UnplacedExtruded",
+    "PlacedExtruded", "UnplacedSExtruVolume", "PlacedSExtru", "UnplacedGenericPolycone", "PlacedGenericPolycone",
+    "UnplacedCoaxialCones", "PlacedCoaxialCones", "UnplacedEllipticalTube", "PlacedEllipticalTube",
+    "UnplacedEllipticalCone", "PlacedEllipticalCone", "UnplacedEllipsoid", "PlacedEllipsoid", "UnplacedParaboloid",
+    "PlacedParaboloid", "UnplacedTet", "PlacedTet",
+]
+
+
+def available():
+    return os.path.isdir(os.path.join(REF, "VecGeom")) and os.path.isdir(os.path.join(REF, "source"))
+
+
+def build(force=False, verbose=False):
+    if not available():
+        raise FileNotFoundError("reference tree not found at %s (set VG_REFERENCE_DIR)" % REF)
+    os.makedirs(OUT_DIR, exist_ok=True)
+    inc = ["-I", SHIM, "-I", REF]
+    shim_files = [os.path.join(d, f) for d, _, fs in os.walk(SHIM) for f in fs]
+    newest_dep = max(os.path.getmtime(f) for f in shim_files + [__file__])
+    units = [(os.path.join(REF, "source", s + ".cpp"), os.path.join(OUT_DIR, s + ".o")) for s in SOURCES]
+    units.append((HARNESS, os.path.join(OUT_DIR, "harness.o")))
+    jobs = []
+    for src, obj in units:
+        if force or not os.path.exists(obj) or os.path.getmtime(obj) < max(os.path.getmtime(src), newest_dep):
+            jobs.append(["g++", *FLAGS, *inc, "-c", src, "-o", obj])
+
+    def run(cmd):
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("compiled-reference build failed: %s\n%s" % (" ".join(cmd), r.stderr[-4000:]))
+
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        list(ex.map(run, jobs))
+    if jobs or not os.path.exists(LIB):
+        run(["g++", "-shared", "-o", LIB, *[o for _, o in units], "-pthread", "-Wl,--no-undefined"])
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

@@ -18,49 +18,60 @@ _vp = ctypes.c_void_p
 NAVSTATE_DTYPE = np.dtype([("nav_ind", "<u4"), ("last_exited", "<u4"), ("on_boundary", "u1"), ("pad", "u1", 3)])
 
 
+_SIGNATURES = {
+    "oracle_geom_create": (_vp, []),
+    "oracle_geom_destroy": (None, [_vp]),
+    "oracle_add_shape": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.c_int]),
+    "oracle_add_lv": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "oracle_place": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp]),
+    "oracle_place_daughter": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp, _dp]),
+    "oracle_set_world": (None, [_vp, ctypes.c_int]),
+    "oracle_close": (ctypes.c_int, [_vp]),
+    "oracle_shape_extent": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp]),
+    "oracle_shape_normal": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp]),
+    "oracle_gentrap_valid": (ctypes.c_int, [_dp, _dp, ctypes.c_double]),
+    "oracle_placed_query": (ctypes.c_double, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_size_t] + [_vp] * 6 +
+                            [ctypes.c_double, _vp, _vp, ctypes.c_int]),
+    "oracle_nav_table_words": (ctypes.c_size_t, [_vp]),
+    "oracle_nav_table": (None, [_vp, _vp]),
+    "oracle_max_depth": (ctypes.c_int, [_vp]),
+    "oracle_bvh_sizes": (ctypes.c_int, [_vp, ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 3),
+    "oracle_bvh_arrays": (ctypes.c_int, [_vp, ctypes.c_int] + [_vp] * 5),
+    "oracle_nav_locate": (ctypes.c_double, [_vp, ctypes.c_size_t, _vp, _vp, _vp, _vp, ctypes.c_int]),
+    "oracle_nav_step": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 11 + [ctypes.c_int]),
+    "oracle_nav_step_safety": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 11 + [ctypes.c_int]),
+    "oracle_shape_query": (ctypes.c_double, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_size_t] + [_vp] * 6 +
+                           [ctypes.c_double, _vp, _vp, ctypes.c_int]),
+    "oracle_nav_approach": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 8 + [ctypes.c_int]),
+    "oracle_nav_transport": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 7 +
+                             [ctypes.c_int, _vp, _vp, _vp, _vp, ctypes.c_int]),
+    "oracle_nav_step_simple": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 10 + [ctypes.c_int]),
+    "oracle_nav_locate_simple": (ctypes.c_double, [_vp, ctypes.c_size_t, _vp, _vp, _vp, _vp, ctypes.c_int]),
+    "oracle_nav_crosscheck": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 6 +
+                              [ctypes.c_int, _vp, ctypes.c_int]),
+    "oracle_check_nav_index": (ctypes.c_int, [_vp, _vp, ctypes.c_size_t, _vp]),
+}
+
+
+def bind(lib, required=True):
+    """Set the ctypes signatures of the oracle's extern "C" surface on `lib`; with
+    required=False, functions `lib` does not export are skipped."""
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            if required:
+                raise AttributeError(name)
+            continue
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
 def load():
     global _lib
     if _lib is None:
         path = _build.LIB if os.path.exists(_build.LIB) else _build.build()
-        lib = ctypes.CDLL(path)
-        sig = {
-            "oracle_geom_create": (_vp, []),
-            "oracle_geom_destroy": (None, [_vp]),
-            "oracle_add_shape": (ctypes.c_int, [_vp, ctypes.c_int, _dp, ctypes.c_int]),
-            "oracle_add_lv": (ctypes.c_int, [_vp, ctypes.c_int]),
-            "oracle_place": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp]),
-            "oracle_place_daughter": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp, _dp]),
-            "oracle_set_world": (None, [_vp, ctypes.c_int]),
-            "oracle_close": (ctypes.c_int, [_vp]),
-            "oracle_shape_extent": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp]),
-            "oracle_shape_normal": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp]),
-            "oracle_gentrap_valid": (ctypes.c_int, [_dp, _dp, ctypes.c_double]),
-            "oracle_placed_query": (ctypes.c_double, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_size_t] + [_vp] * 6 +
-                                    [ctypes.c_double, _vp, _vp, ctypes.c_int]),
-            "oracle_nav_table_words": (ctypes.c_size_t, [_vp]),
-            "oracle_nav_table": (None, [_vp, _vp]),
-            "oracle_max_depth": (ctypes.c_int, [_vp]),
-            "oracle_bvh_sizes": (ctypes.c_int, [_vp, ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 3),
-            "oracle_bvh_arrays": (ctypes.c_int, [_vp, ctypes.c_int] + [_vp] * 5),
-            "oracle_nav_locate": (ctypes.c_double, [_vp, ctypes.c_size_t, _vp, _vp, _vp, _vp, ctypes.c_int]),
-            "oracle_nav_step": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 11 + [ctypes.c_int]),
-            "oracle_nav_step_safety": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 11 + [ctypes.c_int]),
-            "oracle_shape_query": (ctypes.c_double, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_size_t] + [_vp] * 6 +
-                                   [ctypes.c_double, _vp, _vp, ctypes.c_int]),
-            "oracle_nav_approach": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 8 + [ctypes.c_int]),
-            "oracle_nav_transport": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 7 +
-                                     [ctypes.c_int, _vp, _vp, _vp, _vp, ctypes.c_int]),
-            "oracle_nav_step_simple": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 10 + [ctypes.c_int]),
-            "oracle_nav_locate_simple": (ctypes.c_double, [_vp, ctypes.c_size_t, _vp, _vp, _vp, _vp, ctypes.c_int]),
-            "oracle_nav_crosscheck": (ctypes.c_double, [_vp, ctypes.c_size_t] + [_vp] * 6 +
-                                      [ctypes.c_int, _vp, ctypes.c_int]),
-            "oracle_check_nav_index": (ctypes.c_int, [_vp, _vp, ctypes.c_size_t, _vp]),
-        }
-        for name, (res, args) in sig.items():
-            fn = getattr(lib, name)
-            fn.restype = res
-            fn.argtypes = args
-        _lib = lib
+        _lib = bind(ctypes.CDLL(path))
     return _lib
 
 
@@ -77,17 +88,17 @@ class OracleGeometry:
     """Same construction surface as vecgeom_gb300.Geometry, evaluated on the CPU."""
 
     def __init__(self):
-        load()
-        self._h = _lib.oracle_geom_create()
+        self._lib = load()
+        self._h = self._lib.oracle_geom_create()
 
     def __del__(self):
-        if getattr(self, "_h", None) and _lib is not None:
-            _lib.oracle_geom_destroy(self._h)
+        if getattr(self, "_h", None) and getattr(self, "_lib", None) is not None:
+            self._lib.oracle_geom_destroy(self._h)
             self._h = None
 
     def _shape(self, t, params):
         a, p = _d(params)
-        r = _lib.oracle_add_shape(self._h, t, p, a.size)
+        r = self._lib.oracle_add_shape(self._h, t, p, a.size)
         if r < 0:
             raise RuntimeError("oracle: unsupported shape type %d" % t)
         return r
@@ -140,7 +151,7 @@ class OracleGeometry:
         """VUnplacedVolume::Normal at p (shape frame): (normal, valid)."""
         n = np.zeros(3)
         a, pp = _d(p)
-        ok = _lib.oracle_shape_normal(self._h, shape, pp, n.ctypes.data_as(_dp))
+        ok = self._lib.oracle_shape_normal(self._h, shape, pp, n.ctypes.data_as(_dp))
         return n, bool(ok)
 
     def add_cut_tube(self, rmin, rmax, dz, sphi, dphi, bottom_normal, top_normal):
@@ -161,29 +172,29 @@ class OracleGeometry:
         return self._shape(9, list(c))
 
     def add_logical_volume(self, shape):
-        return _lib.oracle_add_lv(self._h, shape)
+        return self._lib.oracle_add_lv(self._h, shape)
 
     def place(self, lv, trans=(0.0, 0.0, 0.0), rot=(1.0, 0, 0, 0, 1.0, 0, 0, 0, 1.0)):
         t, tp = _d(trans)
         r, rp = _d(rot)
-        return _lib.oracle_place(self._h, lv, tp, rp)
+        return self._lib.oracle_place(self._h, lv, tp, rp)
 
     def place_daughter(self, mother_lv, lv, trans=(0.0, 0.0, 0.0), rot=(1.0, 0, 0, 0, 1.0, 0, 0, 0, 1.0)):
         t, tp = _d(trans)
         r, rp = _d(rot)
-        return _lib.oracle_place_daughter(self._h, mother_lv, lv, tp, rp)
+        return self._lib.oracle_place_daughter(self._h, mother_lv, lv, tp, rp)
 
     def set_world(self, pv):
-        _lib.oracle_set_world(self._h, pv)
+        self._lib.oracle_set_world(self._h, pv)
 
     def close(self):
-        if _lib.oracle_close(self._h) != 0:
+        if self._lib.oracle_close(self._h) != 0:
             raise RuntimeError("oracle close failed")
 
     def shape_extent(self, shape):
         lo, lp = _d(np.zeros(3))
         hi, hp = _d(np.zeros(3))
-        _lib.oracle_shape_extent(self._h, shape, lp, hp)
+        self._lib.oracle_shape_extent(self._h, shape, lp, hp)
         return lo, hi
 
     # ------------------------------------------------------------ queries (numpy, CPU)
@@ -193,7 +204,7 @@ class OracleGeometry:
         n = len(x)
         outd = np.empty(n, np.float64)
         outi = np.empty(n, np.int32)
-        t = _lib.oracle_placed_query(self._h, pv, q, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), step_max,
+        t = self._lib.oracle_placed_query(self._h, pv, q, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), step_max,
                                      _p(outd), _p(outi), nthreads)
         return (outi if q in (0, 1) else outd), t
 
@@ -203,36 +214,36 @@ class OracleGeometry:
         n = len(x)
         outd = np.empty(n, np.float64)
         outi = np.empty(n, np.int32)
-        _lib.oracle_shape_query(self._h, shape, q, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), step_max,
+        self._lib.oracle_shape_query(self._h, shape, q, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), step_max,
                                 _p(outd), _p(outi), nthreads)
         return outi if q in (0, 1) else outd
 
     def nav_table(self):
-        n = _lib.oracle_nav_table_words(self._h)
+        n = self._lib.oracle_nav_table_words(self._h)
         out = np.zeros(n, np.uint32)
-        _lib.oracle_nav_table(self._h, _p(out))
+        self._lib.oracle_nav_table(self._h, _p(out))
         return out
 
     def max_depth(self):
-        return _lib.oracle_max_depth(self._h)
+        return self._lib.oracle_max_depth(self._h)
 
     def bvh(self, lv):
         nn, npr, dep = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-        if _lib.oracle_bvh_sizes(self._h, lv, ctypes.byref(nn), ctypes.byref(npr), ctypes.byref(dep)) != 0:
+        if self._lib.oracle_bvh_sizes(self._h, lv, ctypes.byref(nn), ctypes.byref(npr), ctypes.byref(dep)) != 0:
             return None
         prim = np.zeros(npr.value, np.int32)
         off = np.zeros(nn.value, np.int32)
         nch = np.zeros(nn.value, np.int32)
         nodes = np.zeros((nn.value, 6))
         boxes = np.zeros((npr.value, 6))
-        _lib.oracle_bvh_arrays(self._h, lv, _p(prim), _p(off), _p(nch), _p(nodes), _p(boxes))
+        self._lib.oracle_bvh_arrays(self._h, lv, _p(prim), _p(off), _p(nch), _p(nodes), _p(boxes))
         return dict(depth=dep.value, prim=prim, offset=off, nchild=nch, nodes=nodes, boxes=boxes)
 
     def locate(self, x, y, z, nthreads=1, navigator="bvh"):
         """GlobalLocator::LocateGlobalPoint from the world with BVHLevelLocator, or with
         navigator="simple" the brute-force SimpleLevelLocator."""
         out = np.zeros(len(x), NAVSTATE_DTYPE)
-        fn = _lib.oracle_nav_locate_simple if navigator == "simple" else _lib.oracle_nav_locate
+        fn = self._lib.oracle_nav_locate_simple if navigator == "simple" else self._lib.oracle_nav_locate
         t = fn(self._h, len(x), _p(x), _p(y), _p(z), _p(out), nthreads)
         return out, t
 
@@ -245,11 +256,11 @@ class OracleGeometry:
         out = np.zeros(n, NAVSTATE_DTYPE)
         step = np.zeros(n)
         if navigator == "simple":
-            t = _lib.oracle_nav_step_simple(self._h, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(step_limit),
+            t = self._lib.oracle_nav_step_simple(self._h, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(step_limit),
                                             _p(states), _p(out), _p(step), nthreads)
             return out, step, None, t
         nv = np.zeros(n, np.int32) if count_nodes else None
-        t = _lib.oracle_nav_step(self._h, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(step_limit),
+        t = self._lib.oracle_nav_step(self._h, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(step_limit),
                                  _p(states), _p(out), _p(step), _p(nv), nthreads)
         return out, step, nv, t
 
@@ -259,7 +270,7 @@ class OracleGeometry:
         state. Returns counts: steps, not_nearly_equal, bit_different, state_different,
         start_state_different."""
         c = np.zeros(5, np.int64)
-        _lib.oracle_nav_crosscheck(self._h, len(x), _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), max_steps, _p(c),
+        self._lib.oracle_nav_crosscheck(self._h, len(x), _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), max_steps, _p(c),
                                    nthreads)
         return dict(zip(("steps", "not_nearly_equal", "bit_different", "state_different",
                          "start_state_different"), (int(v) for v in c)))
@@ -269,10 +280,10 @@ class OracleGeometry:
         when `table` is None) over every placed-volume path: (error code, paths visited)."""
         paths = np.zeros(1, np.int64)
         if table is None:
-            err = _lib.oracle_check_nav_index(self._h, None, 0, _p(paths))
+            err = self._lib.oracle_check_nav_index(self._h, None, 0, _p(paths))
         else:
             tab = np.ascontiguousarray(table, dtype=np.uint32)
-            err = _lib.oracle_check_nav_index(self._h, _p(tab), tab.size, _p(paths))
+            err = self._lib.oracle_check_nav_index(self._h, _p(tab), tab.size, _p(paths))
         return int(err), int(paths[0])
 
     def step_safety(self, x, y, z, dx, dy, dz, states, step_limit=None, nthreads=1):
@@ -282,7 +293,7 @@ class OracleGeometry:
         out = np.zeros(n, NAVSTATE_DTYPE)
         step = np.zeros(n)
         saf = np.zeros(n)
-        t = _lib.oracle_nav_step_safety(self._h, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(step_limit),
+        t = self._lib.oracle_nav_step_safety(self._h, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(step_limit),
                                         _p(states), _p(out), _p(step), _p(saf), nthreads)
         return out, step, saf, t
 
@@ -290,7 +301,7 @@ class OracleGeometry:
         """BVH::ApproachNextDaughter per track; returns the new step array (a copy of `step`
         lowered to the first daughter bounding box the ray reaches)."""
         out = np.array(step, dtype=np.float64, copy=True)
-        _lib.oracle_nav_approach(self._h, len(x), _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(states), _p(out),
+        self._lib.oracle_nav_approach(self._h, len(x), _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(states), _p(out),
                                  nthreads)
         return out
 
@@ -300,7 +311,7 @@ class OracleGeometry:
         final = np.zeros(n, NAVSTATE_DTYPE)
         tr = np.zeros((n, max_steps), np.uint32) if trace else None
         trs = np.zeros((n, max_steps)) if trace else None
-        t = _lib.oracle_nav_transport(self._h, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(states),
+        t = self._lib.oracle_nav_transport(self._h, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(states),
                                       max_steps, _p(nsteps), _p(final), _p(tr), _p(trs), nthreads)
         return nsteps, final, tr, trs, t
 

@@ -1,0 +1,162 @@
+"""The hand-written oracle against the reference's own code, compiled here (CPU only).
+
+oracle/build_ref.py compiles the reference's sources in place (source/*.cpp and the VecGeom/
+headers) against a scalar stand-in for the VecCore library (oracle/compiled_ref/shim), and
+oracle/reference.py drives the result through the oracle's own interface, one geometry per
+process. Every navigation geometry of the tests and every shape the product builds is then
+run on both, on the same inputs:
+
+* the NavIndex table word for word (padding words, which the reference leaves unwritten,
+  masked);
+* LocateGlobalPoint from the world on the config-5 track starts;
+* whole transport histories (ComputeStepAndPropagatedState with BVHNavigator, the point
+  moved by each step): every step's out-state and step length, bit for bit;
+* 2^16 single steps and step + safety (ComputeStepAndSafetyAndPropagatedState) from
+  pre-step states drawn from transport histories;
+* the six queries of every unplaced shape (Inside, Contains, DistanceToIn/Out, SafetyToIn/
+  Out) on points in the 1.2x extent box and on faces, edges and far points.
+
+All of it is bit-identical, with one stated exception: for GenTraps whose lateral faces are
+all planar, the reference's host build evaluates a TessellatedSection helper
+(VecGeom/volumes/kernel/GenTrapImplementation.h:339-345 and the other `#ifndef VECCORE_CUDA`
+branches) while its CUDA build, which the product and the oracle reproduce, evaluates the
+generic second-order-surface kernels. Those shapes' queries are not compared; in the GenTrap
+ring the next volumes and states are identical, the step lengths agree within 1e-9 mm +
+1e-12 relative (5.7e-14 mm measured), and the safeties are not compared.
+
+Skipped where the reference tree is absent (the checker is built from it)."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import reference as R
+from oracle.oracle import OracleGeometry, transport_step_sample
+from test_cuttube import CUTS
+from test_gpu_shapes import POLYHEDRA, edge_points
+from test_gpu_sphere import SPHERES
+from vecgeom_gb300 import workloads as W
+
+pytestmark = pytest.mark.skipif(not R.available(), reason="the reference tree is not present")
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DETECTOR_GDML = os.path.join(HERE, "golden", "gdml", "detector.gdml")
+NT = os.cpu_count() or 1
+
+WL = "vecgeom_gb300.workloads"
+GEOMETRIES = {
+    "barrel": (WL, "build_barrel", {}),
+    "detector": (WL, "build_detector", {}),
+    "trap_ring": (WL, "build_trap_ring", {}),
+    "gdml_detector": ("oracle.reference", "build_gdml", {"path": DETECTOR_GDML}),
+    "cut_tube_ring": (WL, "build_cut_tube_ring", {}),
+    "sphere_shells": (WL, "build_sphere_shells", {}),
+    "gentrap_ring": (WL, "build_gentrap_ring", {}),
+    "hype_ring": (WL, "build_hype_ring", {}),
+}
+# config-5 tracks transported to the world's edge, primaries whose histories give the 2^16
+# sampled pre-step states, and the half-lengths of the box in which restarting tracks start
+TRACKS = {"barrel": 1 << 14, "detector": 1 << 13, "gdml_detector": 1 << 14}
+PRIMARIES = {"barrel": 16384, "detector": 2048, "gdml_detector": 32768, "sphere_shells": 1 << 15}
+HALF = {"barrel": (2000.0, 2000.0, 3000.0), "detector": (2000.0, 2000.0, 3000.0),
+        "gdml_detector": (1500.0, 1500.0, 2000.0), "sphere_shells": (600.0, 600.0, 600.0)}
+PLANAR_GENTRAPS = ("planar", "pyramid", "anticlockwise")
+
+
+def table_padding(t):
+    """Mask of the NavIndex table words that hold nothing: the word that rounds a node's
+    daughter list to an even count, and the word that aligns a cached matrix to 8 bytes
+    (source/NavIndexTable.cpp:24-80; the reference allocates but never writes them)."""
+    pad = np.zeros(t.size, bool)
+    i = 1
+    while i < t.size:
+        nd = int(t[i + 2]) >> 16
+        hasm = (int(t[i + 2]) >> 8) & 0xFF
+        j = i + 3 + nd
+        if (nd + 1) & 1:
+            pad[j] = True
+            j += 1
+        if hasm & 0x04:
+            if j & 1:
+                pad[j] = True
+                j += 1
+            j += 24
+        i = j
+    return pad
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint8)
+
+
+@pytest.mark.parametrize("name", sorted(GEOMETRIES))
+def test_navigation_equals_compiled_reference(name):
+    mod, fn, kw = GEOMETRIES[name]
+    o = OracleGeometry()
+    getattr(__import__(mod, fromlist=[fn]), fn)(o, **kw)
+    n = TRACKS.get(name, 1 << 15)
+    (x, y, z), (dx, dy, dz), _ = W.stream_tracks(n, 0xC4EC, world_half=HALF.get(name, (600.0, 600.0, 400.0)))
+    st, _ = o.locate(x, y, z, nthreads=NT)
+    ns, fin, tr, trs, _ = o.transport(x, y, z, dx, dy, dz, st, 1000, trace=True, nthreads=NT)
+    cols, sst, _ = transport_step_sample(o, 1 << 16, 0x5A11, PRIMARIES.get(name, 1 << 16), nthreads=NT)
+    s_out, s_step, _, _ = o.step(*cols, sst, nthreads=NT)
+    ss_out, ss_step, ss_saf, _ = o.step_safety(*cols, sst, nthreads=NT)
+
+    ref = R.run((mod, fn), [
+        ("nav_table", (), {}),
+        ("locate", (x, y, z), {"nthreads": NT}),
+        ("transport", (x, y, z, dx, dy, dz, st, 1000), {"trace": True, "nthreads": NT}),
+        ("step", (*cols, sst), {"nthreads": NT}),
+        ("step_safety", (*cols, sst), {"nthreads": NT}),
+    ], kw)
+    table = o.nav_table()
+    assert ref[0].size == table.size
+    used = ~table_padding(table)
+    assert np.array_equal(ref[0][used], table[used]), "NavIndex table"
+    assert np.array_equal(ref[1][0], st), "LocateGlobalPoint"
+    r_ns, r_fin, r_tr, r_trs, _ = ref[2]
+    assert ns.sum() > n
+    assert np.array_equal(r_ns, ns) and np.array_equal(r_fin, fin) and np.array_equal(r_tr, tr), "transport states"
+    assert np.array_equal(ref[3][0], s_out), "step out-states"
+    assert np.array_equal(ref[4][0], ss_out), "step + safety out-states"
+    if name == "gentrap_ring":
+        # planar GenTraps: a different host algorithm in the reference (module docstring);
+        # the safeties, which the world's include, are not compared
+        for a, b in ((r_trs, trs), (ref[3][1], s_step), (ref[4][1], ss_step)):
+            assert np.all(np.abs(a - b) <= 1e-9 + 1e-12 * np.abs(b))
+    else:
+        assert np.array_equal(bits(r_trs), bits(trs)), "transport step lengths"
+        assert np.array_equal(bits(ref[3][1]), bits(s_step)), "step lengths"
+        assert np.array_equal(bits(ref[4][1]), bits(ss_step)), "step + safety step lengths"
+        assert np.array_equal(bits(ref[4][2]), bits(ss_saf)), "safety"
+
+
+def _shapes():
+    out = [(n, k, p) for n, (k, p) in {**W.SHAPES_CFG1, **W.SHAPES_CFG2}.items()]
+    out += [("polyhedron_%d" % i, "polyhedron", p) for i, p in enumerate(POLYHEDRA)]
+    out += [("sphere_%d" % i, "sphere", p) for i, p in enumerate(SPHERES)]
+    out += [("cut_tube_%d" % i, "cut_tube", p) for i, p in enumerate(CUTS)]
+    out += [("hype_" + n, "hype", p) for n, p in W.HYPES.items()]
+    out += [("gentrap_" + n, "gentrap", p) for n, p in W.GENTRAPS.items()]
+    out += [("trap_wedge", "trap", W.TRAP_WEDGE)]
+    return out
+
+
+def test_shape_queries_equal_compiled_reference():
+    shapes = _shapes()
+    o = OracleGeometry()
+    ids = [W.add_shape(o, k, p) for _, k, p in shapes]
+    calls, expect = [], []
+    for i, ((name, _, _), sid) in enumerate(zip(shapes, ids)):
+        if name in ["gentrap_" + k for k in PLANAR_GENTRAPS]:
+            continue
+        lo, hi = o.shape_extent(sid)
+        for pts, dirs in (W.shape_points_box(lo, hi, 1 << 14, seed=77 + i), edge_points(lo, hi, 4096, 99 + i)):
+            for q in range(6):
+                d = dirs if q in (2, 3) else (None, None, None)
+                calls.append(("shape_query", (sid, q, *pts, *d), {"nthreads": NT}))
+                expect.append(((name, q), o.shape_query(sid, q, *pts, *d, nthreads=NT)))
+    got = R.run(("oracle.reference", "build_shapes"), calls, {"shapes": [(k, p) for _, k, p in shapes]})
+    bad = [key for (key, e), g in zip(expect, got) if not np.array_equal(bits(g), bits(e))]
+    assert len(got) > 300
+    assert not bad, bad
