@@ -22,6 +22,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF = os.environ.get("VG_REFERENCE_DIR", "/root/reference")
 SHIM = os.path.join(HERE, "compiled_ref", "shim")
 HARNESS = os.path.join(HERE, "compiled_ref", "harness.cpp")
+ROOT = os.path.dirname(HERE)
+PRODUCT_INCLUDE = os.path.join(ROOT, "include")  # the C-ABI and the reference-side bridge
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
 OUT_DIR = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT_DIR, "libvgref.so")
 FLAGS = ["-O2", "-DNDEBUG", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-w"]
@@ -56,14 +60,20 @@ def build(force=False, verbose=False):
     if not available():
         raise FileNotFoundError("reference tree not found at %s (set VG_REFERENCE_DIR)" % REF)
     os.makedirs(OUT_DIR, exist_ok=True)
-    inc = ["-I", SHIM, "-I", REF]
+    from vecgeom_gb300 import build as product_build
+
+    product_lib = product_build.LIB if os.path.exists(product_build.LIB) else product_build.build()
+    inc = ["-I", SHIM, "-I", REF, "-I", PRODUCT_INCLUDE]
     shim_files = [os.path.join(d, f) for d, _, fs in os.walk(SHIM) for f in fs]
     newest_dep = max(os.path.getmtime(f) for f in shim_files + [__file__])
+    bridge = [os.path.join(PRODUCT_INCLUDE, f) for f in ("vecgeom_gb300.h", "vecgeom_gb300_mirror.hpp")]
+    newest_bridge = max(os.path.getmtime(f) for f in bridge)
     units = [(os.path.join(REF, "source", s + ".cpp"), os.path.join(OUT_DIR, s + ".o")) for s in SOURCES]
     units.append((HARNESS, os.path.join(OUT_DIR, "harness.o")))
     jobs = []
     for src, obj in units:
-        if force or not os.path.exists(obj) or os.path.getmtime(obj) < max(os.path.getmtime(src), newest_dep):
+        dep = max(os.path.getmtime(src), newest_dep, newest_bridge if src == HARNESS else 0.0)
+        if force or not os.path.exists(obj) or os.path.getmtime(obj) < dep:
             jobs.append(["g++", *FLAGS, *inc, "-c", src, "-o", obj])
 
     def run(cmd):
@@ -75,8 +85,10 @@ def build(force=False, verbose=False):
 
     with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
         list(ex.map(run, jobs))
-    if jobs or not os.path.exists(LIB):
-        run(["g++", "-shared", "-o", LIB, *[o for _, o in units], "-pthread", "-Wl,--no-undefined"])
+    libdir = os.path.dirname(product_lib)
+    if jobs or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(product_lib):
+        run(["g++", "-shared", "-o", LIB, *[o for _, o in units], "-L", libdir, "-lvecgeom_gb300",
+             "-Wl,-rpath," + libdir, "-pthread", "-Wl,--no-undefined"])
     return LIB
 
 

@@ -32,6 +32,7 @@
 #include "VecGeom/volumes/UnplacedTrapezoid.h"
 #include "VecGeom/volumes/UnplacedTrd.h"
 #include "VecGeom/volumes/UnplacedTube.h"
+#include "vecgeom_gb300_mirror.hpp"
 
 #include <chrono>
 #include <cstdint>
@@ -363,6 +364,13 @@ double oracle_nav_transport(void *, size_t n, const double *x, const double *y, 
       from_state(s, fp + 12 * i);
     }
   });
+}
+
+// The reference-side bridge (include/vecgeom_gb300_mirror.hpp) on the closed geometry:
+// mirror it into the product geometry `g` (a vg_geom handle created by the caller).
+int oracle_mirror_to_product(void *g, int32_t *failed_pv)
+{
+  return vecgeom_gb300::MirrorGeometry(static_cast<vg_geom *>(g), failed_pv);
 }
 
 } // extern "C"

@@ -10,7 +10,12 @@ requested calls in a fresh process and returns their results.
 import ctypes
 import importlib
 import multiprocessing as mp
+import os
+import struct
+import tempfile
 from concurrent.futures import ProcessPoolExecutor
+
+import numpy as np
 
 from . import build_ref
 from .oracle import OracleGeometry, bind
@@ -28,6 +33,8 @@ def load():
     global _lib
     if _lib is None:
         _lib = bind(ctypes.CDLL(build_ref.build()), required=False)
+        _lib.oracle_mirror_to_product.restype = ctypes.c_int
+        _lib.oracle_mirror_to_product.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]
     return _lib
 
 
@@ -44,6 +51,77 @@ class ReferenceGeometry(OracleGeometry):
 
     def __del__(self):
         self._h = None
+
+    def mirror_to_product(self):
+        """The reference-side bridge (include/vecgeom_gb300_mirror.hpp) on this closed
+        geometry: a product geometry built from it on the host (vg_geom_build, no GPU).
+        Returns the product's info, NavIndex table, BVH arrays per logical volume and shape
+        extents, or raises with the placed volume that could not be mirrored."""
+        import vecgeom_gb300 as vg
+
+        p = vg.Geometry()
+        failed = ctypes.c_int32(-1)
+        rc = self._lib.oracle_mirror_to_product(p._h, ctypes.byref(failed))
+        if rc != 0:
+            raise RuntimeError("mirror failed (%d) at placed volume %d" % (rc, failed.value))
+        p.build()
+        out = product_summary(p)
+        with tempfile.TemporaryDirectory() as d:
+            path = os.path.join(d, "mirror.geom")
+            p.save(path)
+            with open(path, "rb") as f:
+                out["builder_log"] = f.read()
+        return out
+
+
+def product_summary(p):
+    """Host-side contents of a built product geometry, for comparing two builds."""
+    def bvh(lv):
+        try:
+            return p.bvh(lv)
+        except Exception:  # a logical volume without daughters has no BVH
+            return None
+
+    info = p.info()
+    return {"info": info, "nav_table": p.nav_table(), "bvh": [bvh(lv) for lv in range(info["n_lv"])],
+            "extents": [p.shape_extent(s) for s in range(info["n_shapes"])]}
+
+
+# shape codes of the product's builder log (vecgeom_gb300/csrc/vg_types.h ShapeType) where
+# the oracle's extern "C" surface numbers them differently (ref_api.cpp oracle_add_shape)
+_LOG_TO_ORACLE_SHAPE = {10: 11, 11: 12, 12: 13, 13: 14}
+
+
+def replay_builder_log(data, geo):
+    """Replay a product geometry's saved builder log (vg_geom_save: magic, version, count,
+    then (op, arguments...) records as doubles) on an OracleGeometry and close it."""
+    n = struct.unpack_from("<Q", data, 12)[0]
+    log = np.frombuffer(data, dtype="<f8", count=n, offset=20)
+    i = 0
+    while i < n:
+        op = int(log[i])
+        if op == 1:
+            t, np_ = int(log[i + 1]), int(log[i + 2])
+            geo._shape(_LOG_TO_ORACLE_SHAPE.get(t, t), log[i + 3:i + 3 + np_])
+            i += 3 + np_
+        elif op == 2:
+            geo.add_logical_volume(int(log[i + 1]))
+            i += 2
+        elif op == 3:
+            lv, mother = int(log[i + 1]), int(log[i + 2])
+            tr, rot = log[i + 3:i + 6], log[i + 6:i + 15]
+            if mother < 0:
+                geo.place(lv, tr, rot)
+            else:
+                geo.place_daughter(mother, lv, tr, rot)
+            i += 15
+        elif op == 4:
+            geo.set_world(int(log[i + 1]))
+            i += 2
+        else:
+            raise ValueError("corrupt builder log")
+    geo.close()
+    return geo
 
 
 def _worker(builder, builder_kwargs, calls):
