@@ -157,3 +157,13 @@ def build_shapes(geo, shapes):
 
     for kind, params in shapes:
         W.add_shape(geo, kind, params)
+
+
+def build_placed_shapes(geo, shapes, placements):
+    """Builder for run(): each (kind, params) of `shapes` made as build_shapes does, then
+    placed once with the matching (translation, rotation) of `placements`; not closed.
+    Returns (shape id, placed-volume id) per shape."""
+    from vecgeom_gb300 import workloads as W
+
+    ids = [W.add_shape(geo, kind, params) for kind, params in shapes]
+    return [(s, geo.place(geo.add_logical_volume(s), t, r)) for s, (t, r) in zip(ids, placements)]

@@ -14,7 +14,9 @@ run on both, on the same inputs:
 * 2^16 single steps and step + safety (ComputeStepAndSafetyAndPropagatedState) from
   pre-step states drawn from transport histories;
 * the six queries of every unplaced shape (Inside, Contains, DistanceToIn/Out, SafetyToIn/
-  Out) on points in the 1.2x extent box and on faces, edges and far points.
+  Out) on points in the 1.2x extent box and on faces, edges and far points, and the same
+  queries plus PlacedDistanceToOut through the VPlacedVolume interface of each shape placed
+  with a rotation and a translation.
 
 All of it is bit-identical, with one stated exception: for GenTraps whose lateral faces are
 all planar, the reference's host build evaluates a TessellatedSection helper
@@ -201,3 +203,33 @@ def test_mirror_of_reference_geometry_equals_builder(name):
     assert a[0].sum() > 1 << 13
     for u, v in zip(a[:4], b[:4]):
         assert np.array_equal(bits(u), bits(v))
+
+
+def test_placed_queries_equal_compiled_reference():
+    from vecgeom_gb300.workloads import rot_z
+
+    shapes = [(n, k, p) for n, k, p in _shapes() if n not in ["gentrap_" + g for g in PLANAR_GENTRAPS]]
+    g = np.random.default_rng(5)
+    placements = []
+    for i in range(len(shapes)):
+        c, s_ = np.cos(0.3 * i + 0.1), np.sin(0.3 * i + 0.1)
+        rx = (1.0, 0.0, 0.0, 0.0, c, -s_, 0.0, s_, c)  # a tilt about x, then a turn about z
+        rz = np.asarray(rot_z(0.7 * i)).reshape(3, 3)
+        rot = tuple((rz @ np.asarray(rx).reshape(3, 3)).reshape(9))
+        placements.append((tuple(g.uniform(-50.0, 50.0, 3)), rot))
+    o = OracleGeometry()
+    made = R.build_placed_shapes(o, [(k, p) for _, k, p in shapes], placements)
+    calls, expect = [], []
+    for i, ((name, _, _), (sid, pv), (t, _)) in enumerate(zip(shapes, made, placements)):
+        lo, hi = o.shape_extent(sid)
+        (px, py, pz), dirs = W.shape_points_box(lo, hi, 1 << 13, seed=500 + i, scale=1.5)
+        pts = (px + t[0], py + t[1], pz + t[2])  # about the placed shape, in the mother's frame
+        for q in range(7):
+            d = dirs if q in (2, 3, 6) else (None, None, None)
+            calls.append(("query", (pv, q, *pts, *d), {"nthreads": NT}))
+            expect.append(((name, q), o.query(pv, q, *pts, *d, nthreads=NT)[0]))
+    got = R.run(("oracle.reference", "build_placed_shapes"), calls,
+                {"shapes": [(k, p) for _, k, p in shapes], "placements": placements})
+    assert len(got) == 7 * len(shapes) > 200
+    bad = [key for (key, e), r in zip(expect, got) if not np.array_equal(bits(r[0]), bits(e))]
+    assert not bad, bad
