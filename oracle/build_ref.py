@@ -66,7 +66,8 @@ def build(force=False, verbose=False):
     inc = ["-I", SHIM, "-I", REF, "-I", PRODUCT_INCLUDE]
     shim_files = [os.path.join(d, f) for d, _, fs in os.walk(SHIM) for f in fs]
     newest_dep = max(os.path.getmtime(f) for f in shim_files + [__file__])
-    bridge = [os.path.join(PRODUCT_INCLUDE, f) for f in ("vecgeom_gb300.h", "vecgeom_gb300_mirror.hpp")]
+    bridge = [os.path.join(PRODUCT_INCLUDE, f)
+              for f in ("vecgeom_gb300.h", "vecgeom_gb300_mirror.hpp", "vecgeom_gb300_navigator.hpp")]
     newest_bridge = max(os.path.getmtime(f) for f in bridge)
     units = [(os.path.join(REF, "source", s + ".cpp"), os.path.join(OUT_DIR, s + ".o")) for s in SOURCES]
     units.append((HARNESS, os.path.join(OUT_DIR, "harness.o")))

@@ -33,6 +33,7 @@
 #include "VecGeom/volumes/UnplacedTrd.h"
 #include "VecGeom/volumes/UnplacedTube.h"
 #include "vecgeom_gb300_mirror.hpp"
+#include "vecgeom_gb300_navigator.hpp"
 
 #include <chrono>
 #include <cstdint>
@@ -371,6 +372,36 @@ double oracle_nav_transport(void *, size_t n, const double *x, const double *y, 
 int oracle_mirror_to_product(void *g, int32_t *failed_pv)
 {
   return vecgeom_gb300::MirrorGeometry(static_cast<vg_geom *>(g), failed_pv);
+}
+
+// The reference-side navigator adapter (include/vecgeom_gb300_navigator.hpp) installed on
+// every volume with daughters, in place of BVHNavigator, with no product geometry: its
+// per-track methods (the ones that stay on the host) step the tracks, one
+// ComputeStepAndPropagatedState each, as oracle_nav_step does with the reference navigator.
+double oracle_adapter_step(size_t n, const double *x, const double *y, const double *z, const double *dx,
+                           const double *dy, const double *dz, const double *step_limit, const void *in, void *out,
+                           double *step)
+{
+  static vecgeom_gb300::GPUNavigator adapter(nullptr, 0);
+  for (auto &lvol : GeoManager::Instance().GetLogicalVolumesMap())
+    if (lvol.second->GetDaughters().size() > 0) lvol.second->SetNavigator(&adapter);
+  const char *ip = static_cast<const char *>(in);
+  char *op       = static_cast<char *>(out);
+  for (size_t i = 0; i < n; ++i) {
+    NavigationState si = to_state(ip + 12 * i), so;
+    if (si.IsOutside()) {
+      from_state(si, op + 12 * i);
+      step[i] = 0.;
+      continue;
+    }
+    VNavigator const *nav = si.Top()->GetLogicalVolume()->GetNavigator();
+    step[i] = nav->ComputeStepAndPropagatedState(Vector3D<Precision>(x[i], y[i], z[i]),
+                                                 Vector3D<Precision>(dx[i], dy[i], dz[i]), step_limit[i], si, so);
+    from_state(so, op + 12 * i);
+  }
+  for (auto &lvol : GeoManager::Instance().GetLogicalVolumesMap())
+    if (lvol.second->GetDaughters().size() > 0) lvol.second->SetNavigator(BVHNavigator<>::Instance());
+  return 0.0;
 }
 
 } // extern "C"

@@ -35,6 +35,8 @@ def load():
         _lib = bind(ctypes.CDLL(build_ref.build()), required=False)
         _lib.oracle_mirror_to_product.restype = ctypes.c_int
         _lib.oracle_mirror_to_product.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]
+        _lib.oracle_adapter_step.restype = ctypes.c_double
+        _lib.oracle_adapter_step.argtypes = [ctypes.c_size_t] + [ctypes.c_void_p] * 10
     return _lib
 
 
@@ -51,6 +53,21 @@ class ReferenceGeometry(OracleGeometry):
 
     def __del__(self):
         self._h = None
+
+    def adapter_step(self, x, y, z, dx, dy, dz, states, step_limit=None):
+        """One step per track with the reference-side navigator adapter
+        (include/vecgeom_gb300_navigator.hpp) installed on every volume with daughters, through
+        its per-track methods (no GPU); returns (out-states, steps)."""
+        from .oracle import NAVSTATE_DTYPE, _p
+
+        n = len(x)
+        if step_limit is None:
+            step_limit = np.full(n, np.finfo(np.float64).max)
+        out = np.zeros(n, NAVSTATE_DTYPE)
+        step = np.zeros(n)
+        self._lib.oracle_adapter_step(n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(step_limit), _p(states),
+                                      _p(out), _p(step))
+        return out, step
 
     def mirror_to_product(self):
         """The reference-side bridge (include/vecgeom_gb300_mirror.hpp) on this closed

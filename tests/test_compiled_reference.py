@@ -233,3 +233,17 @@ def test_placed_queries_equal_compiled_reference():
     assert len(got) == 7 * len(shapes) > 200
     bad = [key for (key, e), r in zip(expect, got) if not np.array_equal(bits(r[0]), bits(e))]
     assert not bad, bad
+
+
+def test_navigator_adapter_host_path_equals_reference():
+    """The reference-side navigator adapter compiles against the reference's headers and,
+    installed on every volume in place of BVHNavigator, steps the tracks as the reference
+    does on the methods it keeps on the host (its vector entry point is the GPU call)."""
+    mod, fn, kw = GEOMETRIES["detector"]
+    o = OracleGeometry()
+    getattr(__import__(mod, fromlist=[fn]), fn)(o, **kw)
+    cols, sst, _ = transport_step_sample(o, 1 << 14, 0x5A11, PRIMARIES["detector"], nthreads=NT)
+    out, step, _, _ = o.step(*cols, sst, nthreads=NT)
+    r_out, r_step = R.run((mod, fn), [("adapter_step", (*cols, sst), {})], kw)[0]
+    assert np.array_equal(r_out, out)
+    assert np.array_equal(bits(r_step), bits(step))
