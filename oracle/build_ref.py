@@ -52,6 +52,15 @@ SOURCES = [
 ]
 
 
+# The reference's own unit tests of the shapes and navigation states on the path
+# (test/unit_tests/*.cpp, each a program of asserts), built against the same library: their
+# passing pins the VecCore stand-in and the configuration header.
+UNIT_TESTS = ["TestBox", "TestTube", "TestCons", "TestPolycone", "TestPolyhedra", "TestTorus2", "TestTrd",
+              "TestBooleans", "TestTrap", "TestSphere", "TestHype", "TestGenTrap", "TestNavStateIndex",
+              "TestReducedPolycone", "TestVecGeomPolycone"]
+UNIT_DIR = os.path.join(OUT_DIR, "unit_tests")
+
+
 def available():
     return os.path.isdir(os.path.join(REF, "VecGeom")) and os.path.isdir(os.path.join(REF, "source"))
 
@@ -91,6 +100,34 @@ def build(force=False, verbose=False):
         run(["g++", "-shared", "-o", LIB, *[o for _, o in units], "-L", libdir, "-lvecgeom_gb300",
              "-Wl,-rpath," + libdir, "-pthread", "-Wl,--no-undefined"])
     return LIB
+
+
+def build_unit_tests(verbose=False):
+    """Compile UNIT_TESTS (asserts enabled: no -DNDEBUG in these translation units) against
+    the library; returns {name: executable path}."""
+    lib = build(verbose=verbose)
+    os.makedirs(UNIT_DIR, exist_ok=True)
+    src_dir = os.path.join(REF, "test", "unit_tests")
+    flags = [f for f in FLAGS if f not in ("-DNDEBUG", "-fPIC")]
+    inc = ["-I", SHIM, "-I", REF, "-I", src_dir]
+    libdir = os.path.dirname(lib)
+    jobs, exes = [], {}
+    for t in UNIT_TESTS:
+        src, exe = os.path.join(src_dir, t + ".cpp"), os.path.join(UNIT_DIR, t)
+        exes[t] = exe
+        if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(src), os.path.getmtime(lib)):
+            jobs.append(["g++", *flags, *inc, src, "-o", exe, "-L", libdir, "-lvgref", "-Wl,-rpath," + libdir])
+
+    def run(cmd):
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("unit-test build failed: %s\n%s" % (" ".join(cmd), r.stderr[-4000:]))
+
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        list(ex.map(run, jobs))
+    return exes
 
 
 if __name__ == "__main__":

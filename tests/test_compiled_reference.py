@@ -32,6 +32,10 @@ equals the product geometry the builder makes directly (placed-volume and logica
 counts, NavIndex table, every BVH, the shapes' extents), and the oracle built from the
 mirror's builder log transports the config-5 tracks exactly as the directly built one.
 
+The compiled reference is itself pinned: the reference's own unit tests of every shape on the
+path and of the navigation states (test/unit_tests/Test*.cpp, asserts enabled) are built
+against the same library and pass.
+
 Skipped where the reference tree is absent (the checker is built from it)."""
 import os
 
@@ -71,6 +75,17 @@ PRIMARIES = {"barrel": 16384, "detector": 2048, "gdml_detector": 32768, "sphere_
 HALF = {"barrel": (2000.0, 2000.0, 3000.0), "detector": (2000.0, 2000.0, 3000.0),
         "gdml_detector": (1500.0, 1500.0, 2000.0), "sphere_shells": (600.0, 600.0, 600.0)}
 PLANAR_GENTRAPS = ("planar", "pyramid", "anticlockwise")
+
+
+@pytest.mark.parametrize("name", __import__("oracle.build_ref", fromlist=["UNIT_TESTS"]).UNIT_TESTS)
+def test_reference_unit_tests_pass_on_the_stand_in(name):
+    import subprocess
+
+    from oracle import build_ref
+
+    exe = build_ref.build_unit_tests()[name]
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, (r.stdout[-2000:], r.stderr[-2000:])
 
 
 def table_padding(t):
