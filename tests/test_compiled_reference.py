@@ -13,6 +13,7 @@ run on both, on the same inputs:
   moved by each step): every step's out-state and step length, bit for bit;
 * 2^16 single steps and step + safety (ComputeStepAndSafetyAndPropagatedState) from
   pre-step states drawn from transport histories;
+* whole transport histories in the reference's own example GDML files;
 * the six queries of every unplaced shape (Inside, Contains, DistanceToIn/Out, SafetyToIn/
   Out) on points in the 1.2x extent box and on faces, edges and far points, and the same
   queries plus PlacedDistanceToOut through the VPlacedVolume interface of each shape placed
@@ -262,3 +263,33 @@ def test_navigator_adapter_host_path_equals_reference():
     r_out, r_step = R.run((mod, fn), [("adapter_step", (*cols, sst), {})], kw)[0]
     assert np.array_equal(r_out, out)
     assert np.array_equal(bits(r_step), bits(step))
+
+
+@pytest.mark.parametrize("name", __import__("test_gdml").SUPPORTED_REF)
+def test_reference_example_gdml_navigation_equals_compiled_reference(name):
+    """The reference's own example GDML files (persistency/gdml/gdmls) read by the product's
+    reader into the oracle and into the reference's own classes: whole transport histories
+    bit-identical (planar GenTraps excepted, as above)."""
+    from test_gdml import REF_GDMLS
+    from vecgeom_gb300 import gdml
+
+    path = os.path.join(REF_GDMLS, name + ".gdml")
+    o = OracleGeometry()
+    r = gdml.load(path, o)
+    ext = [o.shape_extent(s) for s in sorted(set(r.solids.values()))]
+    lo = np.min([e[0] for e in ext], axis=0)
+    hi = np.max([e[1] for e in ext], axis=0)
+    (x, y, z), (dx, dy, dz) = W.shape_points_box(lo, hi, 1 << 13, seed=0x6D1, scale=1.0)
+    st, _ = o.locate(x, y, z, nthreads=NT)
+    a = o.transport(x, y, z, dx, dy, dz, st, 1000, trace=True, nthreads=NT)
+    ref = R.run(("oracle.reference", "build_gdml"), [
+        ("locate", (x, y, z), {"nthreads": NT}),
+        ("transport", (x, y, z, dx, dy, dz, st, 1000), {"trace": True, "nthreads": NT})], {"path": path})
+    assert np.array_equal(ref[0][0], st)
+    assert a[0].sum() > 300
+    b = ref[1]
+    assert np.array_equal(b[0], a[0]) and np.array_equal(b[1], a[1]) and np.array_equal(b[2], a[2])
+    if name == "oneGeneralTrapezoid":
+        assert np.all(np.abs(b[3] - a[3]) <= 1e-9 + 1e-12 * np.abs(a[3]))
+    else:
+        assert np.array_equal(bits(b[3]), bits(a[3]))

@@ -12,13 +12,15 @@ import pytest
 import vecgeom_gb300 as vg
 from oracle.oracle import OracleGeometry
 from test_cpu_build import HostOnly
+from oracle import build_ref
 from vecgeom_gb300 import gdml
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 DETECTOR = os.path.join(HERE, "golden", "gdml", "detector.gdml")
-# the reference's own example GDML files, where a VecGeom source tree is named by
-# VECGEOM_SOURCE_DIR (the tests that read them are skipped otherwise)
-REF_GDMLS = os.path.join(os.environ.get("VECGEOM_SOURCE_DIR", "/nonexistent"), "persistency", "gdml", "gdmls")
+# the reference's own example GDML files, where a VecGeom source tree is present (named by
+# VECGEOM_SOURCE_DIR, else the tree the compiled-reference recipe reads); the tests that
+# read them are skipped otherwise
+REF_GDMLS = os.path.join(os.environ.get("VECGEOM_SOURCE_DIR", build_ref.REF), "persistency", "gdml", "gdmls")
 
 
 def compare(path):
