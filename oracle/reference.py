@@ -54,6 +54,12 @@ class ReferenceGeometry(OracleGeometry):
     def __del__(self):
         self._h = None
 
+    def locate_transport(self, x, y, z, dx, dy, dz, max_steps, nthreads=1):
+        """LocateGlobalPoint from the world, then every track transported to the world's
+        edge: (located states, the transport() tuple with traces)."""
+        st, _ = self.locate(x, y, z, nthreads=nthreads)
+        return st, self.transport(x, y, z, dx, dy, dz, st, max_steps, trace=True, nthreads=nthreads)
+
     def adapter_step(self, x, y, z, dx, dy, dz, states, step_limit=None):
         """One step per track with the reference-side navigator adapter
         (include/vecgeom_gb300_navigator.hpp) installed on every volume with daughters, through
