@@ -3,8 +3,13 @@ sources compiled by oracle/build_ref.py against the scalar VecCore stand-in), fo
 tests to compare with directly (tests/test_gpu_reference_outputs.py) and the CPU tests to
 check the oracle against (tests/test_reference_outputs.py).
 
-Inputs are not stored: they are regenerated from the seeds and boxes recorded here with
-vecgeom_gb300.workloads, so the fixture holds only the reference's answers.
+The inputs are stored with the answers: the track directions pass through numpy's
+transcendental functions, whose last bit can differ between machines (x86-64 here, aarch64
+on the GPU machine), which would move the steps by ulps. For the same reason the GDML
+detector is stored as the product's builder log (vg_geom_save) of the calls that built the
+reference's copy: the GDML reader's angle conversions go through the C library. The barrel
+and the detector are rebuilt by their builders (their rotations are identical on both
+machines, and the detector's log would be megabytes).
 
 * Navigation (GEOMETRIES): the config-5 track starts (stream_tracks(n, seed, world_half)),
   LocateGlobalPoint from the world, then every track transported to the world's edge with
@@ -34,9 +39,23 @@ GEOMETRIES = {
     "detector": (WL, "build_detector", {}, 256, 0xD2, (2000.0, 2000.0, 3000.0), 1000),
     "gdml_detector": ("oracle.reference", "build_gdml", {"path": GDML}, 256, 0xD3, (1500.0, 1500.0, 2000.0), 1000),
 }
+STORED_GEOMETRIES = ("gdml_detector",)
 SHAPES = ["box", "tube", "cone", "tube_phi", "polycone", "polyhedron", "torus2", "trd", "box_minus_tube"]
 SHAPE_POINTS = 256
 SHAPE_SEED = 0x5A
+
+
+class _Open:
+    """A product geometry whose close() is skipped: only the builder log is wanted."""
+
+    def __init__(self, g):
+        self.g = g
+
+    def __getattr__(self, n):
+        return getattr(self.g, n)
+
+    def close(self):
+        pass
 
 
 def main():
@@ -44,12 +63,24 @@ def main():
     from oracle.oracle import OracleGeometry
     from vecgeom_gb300 import workloads as W
 
+    import tempfile
+
+    import vecgeom_gb300 as vg
+
     out = {}
     for name, (mod, fn, kw, n, seed, half, max_steps) in GEOMETRIES.items():
+        if name in STORED_GEOMETRIES:
+            p = vg.Geometry()
+            getattr(__import__(mod, fromlist=[fn]), fn)(_Open(p), **kw)
+            with tempfile.TemporaryDirectory() as d:
+                p.save(os.path.join(d, "g.geom"))
+                with open(os.path.join(d, "g.geom"), "rb") as fh:
+                    out[name + "/builder_log"] = np.frombuffer(fh.read(), dtype=np.uint8)
         (x, y, z), (dx, dy, dz), _ = W.stream_tracks(n, seed, world_half=half)
         st, (ns, final, tr, trs, _) = R.run((mod, fn), [("locate_transport", (x, y, z, dx, dy, dz, max_steps), {})],
                                             kw)[0]
         mask = np.arange(max_steps)[None, :] < ns[:, None]
+        out[name + "/inputs"] = np.stack([x, y, z, dx, dy, dz])
         out[name + "/start"] = st.view(np.uint8).reshape(n, 12)
         out[name + "/nsteps"] = ns.astype(np.int32)
         out[name + "/final"] = final.view(np.uint8).reshape(n, 12)
@@ -64,6 +95,7 @@ def main():
         c, h = 0.5 * (lo + hi), 0.6 * (hi - lo)  # the 1.2x extent box
         out[name + "/box"] = np.stack([c - h, c + h])
         pts, dirs = W.shape_points_box(c - h, c + h, SHAPE_POINTS, seed=SHAPE_SEED, scale=1.0)
+        out[name + "/inputs"] = np.stack([*pts, *dirs])
         for q in range(6):
             d = dirs if q in (2, 3) else (None, None, None)
             calls.append(("shape_query", (sid, q, *pts, *d), {}))

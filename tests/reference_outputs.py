@@ -1,6 +1,5 @@
-"""Loader of tests/golden/reference_outputs.npz (outputs of the reference's own code; see
-tests/golden/make_reference_outputs.py) and the inputs it was made from, regenerated from
-the recorded seeds."""
+"""Loader of tests/golden/reference_outputs.npz (outputs of the reference's own code, with
+the inputs they were computed from; see tests/golden/make_reference_outputs.py)."""
 import os
 import sys
 
@@ -8,7 +7,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "golden"))
-from make_reference_outputs import GEOMETRIES, OUT, SHAPE_POINTS, SHAPE_SEED, SHAPES  # noqa: E402
+from make_reference_outputs import GEOMETRIES, OUT, SHAPES  # noqa: E402
 
 _cache = {}
 
@@ -21,15 +20,48 @@ def fixture():
 
 
 def geometry_inputs(name):
-    from vecgeom_gb300 import workloads as W
-
-    _, _, _, n, seed, half, _ = GEOMETRIES[name]
-    pts, dirs, _ = W.stream_tracks(n, seed, world_half=half)
-    return pts, dirs
+    a = fixture()[name + "/inputs"]
+    return tuple(np.ascontiguousarray(v) for v in a[:3]), tuple(np.ascontiguousarray(v) for v in a[3:])
 
 
 def shape_inputs(name):
-    from vecgeom_gb300 import workloads as W
+    return geometry_inputs(name)
 
-    lo, hi = fixture()[name + "/box"]
-    return W.shape_points_box(lo, hi, SHAPE_POINTS, seed=SHAPE_SEED, scale=1.0)
+
+def _builder(name):
+    mod, fn, kw = GEOMETRIES[name][:3]
+    return getattr(__import__(mod, fromlist=[fn]), fn), kw
+
+
+def product_geometry(name):
+    """The product geometry of navigation geometry `name`, closed: replayed from the stored
+    builder log (the calls that built the reference's copy) where one is stored, else built
+    by its builder."""
+    import tempfile
+
+    import vecgeom_gb300 as vg
+
+    if name + "/builder_log" not in fixture():
+        fn, kw = _builder(name)
+        g = vg.Geometry()
+        fn(g, **kw)
+        return g
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "g.geom")
+        fixture()[name + "/builder_log"].tofile(path)
+        g = vg.Geometry.load(path)
+    g.close()
+    return g
+
+
+def oracle_geometry(name):
+    """The oracle geometry of navigation geometry `name`, made as product_geometry makes it."""
+    from oracle.oracle import OracleGeometry
+    from oracle.reference import replay_builder_log
+
+    if name + "/builder_log" not in fixture():
+        fn, kw = _builder(name)
+        o = OracleGeometry()
+        fn(o, **kw)
+        return o
+    return replay_builder_log(fixture()[name + "/builder_log"].tobytes(), OracleGeometry())

@@ -4,8 +4,11 @@ against the VecCore stand-in; tests/test_reference_outputs.py checks the oracle 
 same fixture on the CPU):
 
 * LocateGlobalPoint and whole transport histories (vg_nav_transport, plain FP64 and the mixed
-  + sorted + work-queue schedule) in the barrel, the config-4 detector and the GDML detector:
-  steps per track, final states, every step's next nav index and length, bit for bit;
+  + sorted + work-queue schedule) in the barrel, the config-4 detector and the GDML detector
+  (replayed from the stored builder log of the reference's copy): steps per track, final
+  states, every step's next nav index and length, bit for bit, except the steps into or out
+  of the GDML detector's Torus2 ring (within 1e-9 mm + 1e-12 relative: the device's
+  cbrt/pow/cos/atan2);
 * the six unplaced queries of the config-1 and config-2 shapes, FP64 and mixed precision:
   bit for bit, except Torus2's distances (within 1e-9 mm + 1e-12 relative: its cubic
   resolvent calls the device's cbrt/pow/cos/atan2) and the full-phi Tube's mixed-precision
@@ -13,24 +16,11 @@ same fixture on the CPU):
 import numpy as np
 import pytest
 
-from reference_outputs import GEOMETRIES, SHAPES, fixture, geometry_inputs, shape_inputs
+from reference_outputs import GEOMETRIES, SHAPES, fixture, geometry_inputs, oracle_geometry, product_geometry, shape_inputs
 
 pytestmark = pytest.mark.gpu
 
 QUERIES = ["inside", "contains", "distance_to_in", "distance_to_out", "safety_to_in", "safety_to_out"]
-
-
-def _build(name):
-    import vecgeom_gb300 as vg
-    from vecgeom_gb300 import gdml
-
-    mod, fn, kw = GEOMETRIES[name][:3]
-    g = vg.Geometry()
-    if "path" in kw:
-        gdml.load(kw["path"], g)
-    else:
-        getattr(__import__(mod, fromlist=[fn]), fn)(g, **kw)
-    return g
 
 
 @pytest.mark.parametrize("name", sorted(GEOMETRIES))
@@ -38,7 +28,7 @@ def test_transport_equals_reference_outputs(cuda, name):
     import vecgeom_gb300 as vg
     f = fixture()
     n, max_steps = GEOMETRIES[name][3], GEOMETRIES[name][6]
-    g = _build(name)
+    g = product_geometry(name)  # the builder calls of the reference's copy, replayed
     pts, dirs = geometry_inputs(name)
     mask = np.arange(max_steps)[None, :] < f[name + "/nsteps"][:, None]
     for flags in (vg.PREC_FP64, vg.PREC_MIXED | vg.NAV_SORT | vg.NAV_QUEUE):
@@ -53,7 +43,23 @@ def test_transport_equals_reference_outputs(cuda, name):
         trs = tst.cpu().numpy().view(vg.NAVSTATE_DTYPE).reshape(n, max_steps)["nav_ind"]
         tsl = tsp.cpu().numpy().reshape(n, max_steps)
         assert np.array_equal(trs[mask], f[name + "/trace_nav"]), flags
-        assert np.array_equal(tsl[mask].view(np.uint64), f[name + "/trace_step"].view(np.uint64)), flags
+        got, ref = tsl[mask], f[name + "/trace_step"]
+        if name != "gdml_detector":
+            assert np.array_equal(got.view(np.uint64), ref.view(np.uint64)), flags
+            continue
+        # the GDML detector holds a Torus2 ring: steps into or out of it are compared at
+        # 1e-9 mm + 1e-12 relative (the device's cbrt/pow/cos/atan2), every other step bit
+        # for bit
+        torus = oracle_geometry(name).locate(np.array([1000.0]), np.array([0.0]), np.array([1500.0]))[0]["nav_ind"][0]
+        nav = f[name + "/trace_nav"]
+        first = np.concatenate([[0], np.cumsum(f[name + "/nsteps"])[:-1]])
+        prev = np.concatenate([[0], nav[:-1]])
+        moved = f[name + "/nsteps"] > 0
+        prev[first[moved]] = f[name + "/start"].reshape(-1).view(vg.NAVSTATE_DTYPE)["nav_ind"][moved]
+        differ = got != ref
+        assert (np.abs(got - ref)[differ] <= 1e-9 + 1e-12 * np.abs(ref[differ])).all(), flags
+        assert ((nav == torus) | (prev == torus))[differ].all(), flags
+        assert differ.sum() < 0.02 * got.size, flags
 
 
 @pytest.mark.parametrize("name", SHAPES)
