@@ -15,8 +15,10 @@ machines, and the detector's log would be megabytes).
   LocateGlobalPoint from the world, then every track transported to the world's edge with
   ComputeStepAndPropagatedState (BVHNavigator): steps per track, final states, and each
   step's next nav index and length (the valid steps of all tracks, concatenated).
-* Shapes (SHAPES): the six queries of each config-1 and config-2 shape (unplaced, the shape's
-  own frame) on points uniform in the recorded box (its 1.2x extent) with isotropic directions.
+* Shapes (SHAPES): the six queries of each config-1 and config-2 shape and of a Polyhedron
+  with a phi cut, a Trapezoid, two Spheres, two Hypes, a CutTube and two twisted GenTraps
+  (unplaced, the shape's own frame) on points uniform in the 1.2x extent box with isotropic
+  directions.
 
 Run here, where the reference tree is present:  python tests/golden/make_reference_outputs.py
 """
@@ -40,7 +42,29 @@ GEOMETRIES = {
     "gdml_detector": ("oracle.reference", "build_gdml", {"path": GDML}, 256, 0xD3, (1500.0, 1500.0, 2000.0), 1000),
 }
 STORED_GEOMETRIES = ("gdml_detector",)
-SHAPES = ["box", "tube", "cone", "tube_phi", "polycone", "polyhedron", "torus2", "trd", "box_minus_tube"]
+SHAPES = ["box", "tube", "cone", "tube_phi", "polycone", "polyhedron", "torus2", "trd", "box_minus_tube",
+          "polyhedron_phi", "trap_wedge", "sphere_phi", "sphere_theta", "hype_hollow", "hype_cone_in", "cut_tube",
+          "gentrap_twisted", "gentrap_one_twisted"]
+_PI = 3.141592653589793
+# the shapes beyond configs 1-2: (kind, parameters) as vecgeom_gb300.workloads.add_shape takes them
+EXTRA_SHAPES = {
+    "polyhedron_phi": ("polyhedron", (0.3, 1.8, 5, (-100.0, 0.0, 0.0, 50.0), (0.0, 10.0, 20.0, 5.0),
+                                      (40.0, 60.0, 50.0, 30.0))),
+    "trap_wedge": ("trap", (60.0, 0.1, 0.4, 40.0, 20.0, 30.0, 0.15, 50.0, 25.0, 35.0, 0.15)),
+    "sphere_phi": ("sphere", (20.0, 50.0, 0.3, 1.8, 0.0, _PI)),
+    "sphere_theta": ("sphere", (10.0, 50.0, 0.5, 2.5, 1.8, 0.9)),
+    "cut_tube": ("cut_tube", (10.0, 20.0, 30.0, 0.0, 4.0, (0.2, 0.3, -1.0), (-0.1, 0.5, 1.0))),
+}
+
+
+def shape_spec(name):
+    from vecgeom_gb300 import workloads as W
+
+    if name.startswith("hype_"):
+        return ("hype", W.HYPES[name[5:]])
+    if name.startswith("gentrap_"):
+        return ("gentrap", W.GENTRAPS[name[8:]])
+    return EXTRA_SHAPES.get(name) or W.SHAPES_CFG1.get(name) or W.SHAPES_CFG2[name]
 SHAPE_POINTS = 256
 SHAPE_SEED = 0x5A
 
@@ -86,7 +110,7 @@ def main():
         out[name + "/final"] = final.view(np.uint8).reshape(n, 12)
         out[name + "/trace_nav"] = tr[mask].astype(np.uint32)
         out[name + "/trace_step"] = trs[mask]
-    shapes = [W.SHAPES_CFG1.get(s) or W.SHAPES_CFG2[s] for s in SHAPES]
+    shapes = [shape_spec(s) for s in SHAPES]
     o = OracleGeometry()
     ids = [W.add_shape(o, k, p) for k, p in shapes]
     calls, keys = [], []

@@ -7,7 +7,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "golden"))
-from make_reference_outputs import GEOMETRIES, OUT, SHAPES  # noqa: E402
+from make_reference_outputs import GEOMETRIES, OUT, SHAPES, shape_spec  # noqa: E402
 
 _cache = {}
 

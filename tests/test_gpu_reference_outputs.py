@@ -9,14 +9,15 @@ same fixture on the CPU):
   states, every step's next nav index and length, bit for bit, except the steps into or out
   of the GDML detector's Torus2 ring (within 1e-9 mm + 1e-12 relative: the device's
   cbrt/pow/cos/atan2);
-* the six unplaced queries of the config-1 and config-2 shapes, FP64 and mixed precision:
+* the six unplaced queries of 18 shapes (configs 1-2, a phi-cut Polyhedron, a Trapezoid,
+  two Spheres, two Hypes, a CutTube, two twisted GenTraps), FP64 and mixed precision:
   bit for bit, except Torus2's distances (within 1e-9 mm + 1e-12 relative: its cubic
   resolvent calls the device's cbrt/pow/cos/atan2) and the full-phi Tube's mixed-precision
   safeties (the stated FP32 bound)."""
 import numpy as np
 import pytest
 
-from reference_outputs import GEOMETRIES, SHAPES, fixture, geometry_inputs, oracle_geometry, product_geometry, shape_inputs
+from reference_outputs import GEOMETRIES, SHAPES, fixture, geometry_inputs, shape_spec, oracle_geometry, product_geometry, shape_inputs
 
 pytestmark = pytest.mark.gpu
 
@@ -68,7 +69,7 @@ def test_shape_queries_equal_reference_outputs(cuda, name):
     from vecgeom_gb300 import workloads as W
     f = fixture()
     g = vg.Geometry()
-    s, _ = W.build_single_shape(g, *(W.SHAPES_CFG1.get(name) or W.SHAPES_CFG2[name]))
+    s, _ = W.build_single_shape(g, *shape_spec(name))
     pts, dirs = shape_inputs(name)
     t = [cuda.from_numpy(np.ascontiguousarray(a)).to("cuda:0") for a in (*pts, *dirs)]
     n = len(pts[0])

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from oracle.oracle import NAVSTATE_DTYPE, OracleGeometry
-from reference_outputs import GEOMETRIES, SHAPES, fixture, geometry_inputs, oracle_geometry, shape_inputs
+from reference_outputs import GEOMETRIES, SHAPES, fixture, geometry_inputs, shape_spec, oracle_geometry, shape_inputs
 from vecgeom_gb300 import workloads as W
 
 NT = os.cpu_count() or 1
@@ -35,7 +35,7 @@ def test_oracle_transport_equals_reference_outputs(name):
 def test_oracle_shape_queries_equal_reference_outputs(name):
     f = fixture()
     o = OracleGeometry()
-    sid = W.add_shape(o, *(W.SHAPES_CFG1.get(name) or W.SHAPES_CFG2[name]))
+    sid = W.add_shape(o, *shape_spec(name))
     pts, dirs = shape_inputs(name)
     for q in range(6):
         d = dirs if q in (2, 3) else (None, None, None)
