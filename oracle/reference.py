@@ -60,6 +60,14 @@ class ReferenceGeometry(OracleGeometry):
         st, _ = self.locate(x, y, z, nthreads=nthreads)
         return st, self.transport(x, y, z, dx, dy, dz, st, max_steps, trace=True, nthreads=nthreads)
 
+    def timed_shape_query(self, shape, q, x, y, z, dx=None, dy=None, dz=None, nthreads=1):
+        """Wall time (s) of one shape_query call (the batched loop, as the oracle reports)."""
+        import time
+
+        t0 = time.perf_counter()
+        self.shape_query(shape, q, x, y, z, dx, dy, dz, nthreads=nthreads)
+        return time.perf_counter() - t0
+
     def adapter_step(self, x, y, z, dx, dy, dz, states, step_limit=None):
         """One step per track with the reference-side navigator adapter
         (include/vecgeom_gb300_navigator.hpp) installed on every volume with daughters, through
