@@ -25,6 +25,7 @@
 #include "VecGeom/volumes/UnplacedCutTube.h"
 #include "VecGeom/volumes/UnplacedGenTrap.h"
 #include "VecGeom/volumes/UnplacedHype.h"
+#include "VecGeom/volumes/UnplacedOrb.h"
 #include "VecGeom/volumes/UnplacedPolycone.h"
 #include "VecGeom/volumes/UnplacedPolyhedron.h"
 #include "VecGeom/volumes/UnplacedSphere.h"
@@ -111,7 +112,8 @@ void *oracle_geom_create()
 }
 void oracle_geom_destroy(void *) {}
 
-// Shape codes and parameter layouts as in ref_api.cpp; every shape is made the way the
+// Shape codes and parameter layouts as in ref_api.cpp (plus 15, an Orb of radius p[0], which
+// only this harness makes: a shape outside the product's set); every shape is made the way the
 // reference's own factories make it (GeoManager::MakeInstance where a Maker exists, which
 // with volume specialisation off gives the universal kernels).
 int oracle_add_shape(void *, int type, const double *p, int np)
@@ -161,6 +163,7 @@ int oracle_add_shape(void *, int type, const double *p, int np)
       return -1; // the 17-value (dz, four planes) form is the product's own mirror constructor
     }
     break;
+  case 15: s = new UnplacedOrb(p[0]); break; // reference only: a shape the product does not build
   default: return -1;
   }
   g->shapes.push_back(s);

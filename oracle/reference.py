@@ -198,3 +198,13 @@ def build_placed_shapes(geo, shapes, placements):
 
     ids = [W.add_shape(geo, kind, params) for kind, params in shapes]
     return [(s, geo.place(geo.add_logical_volume(s), t, r)) for s, (t, r) in zip(ids, placements)]
+
+
+def build_with_orb(geo):
+    """Builder for run(), reference only: a world box holding a box and an Orb (a shape the
+    product does not build), closed."""
+    world = geo.add_logical_volume(geo.add_box(100.0, 100.0, 100.0))
+    geo.place_daughter(world, geo.add_logical_volume(geo.add_box(10.0, 10.0, 10.0)), (-50.0, 0.0, 0.0))
+    geo.place_daughter(world, geo.add_logical_volume(geo._shape(15, [20.0])), (50.0, 0.0, 0.0))
+    geo.set_world(geo.place(world))
+    geo.close()

@@ -293,3 +293,11 @@ def test_reference_example_gdml_navigation_equals_compiled_reference(name):
         assert np.all(np.abs(b[3] - a[3]) <= 1e-9 + 1e-12 * np.abs(a[3]))
     else:
         assert np.array_equal(bits(b[3]), bits(a[3]))
+
+
+def test_mirror_rejects_a_shape_outside_the_product_set():
+    """A closed reference geometry holding an Orb: MirrorGeometry returns VG_EINVAL and names
+    the first placed volume it cannot mirror (the Orb, id 1), so the caller keeps that
+    geometry on the reference's path."""
+    with pytest.raises(RuntimeError, match=r"mirror failed \(-1\) at placed volume 1"):
+        R.run(("oracle.reference", "build_with_orb"), [("mirror_to_product", (), {})])
