@@ -41,6 +41,10 @@ STEP_BYTES = 24 + 24 + 12 + 12 + 8  # p, d, state in, state out, step (FP64 SoA 
 # group into warps, so they hold at 2^22. Counted before the candidate buffer kept its
 # lowest bounds when full; the kernels now evaluate fewer candidates per step, so these
 # counts, and the FP64 fraction computed from them, are upper bounds.
+# What the CPU figures are: the oracle port stands in for the reference's CPU code, whose
+# sources are not on the GPU machine.
+PORT_NOTE = ("oracle port; bit-identical to the reference's own code compiled in the development container, "
+             "where that code ran 1.07-1.23x as fast on the same inputs")
 FP64_OPS_PER_STEP = {"fused": 3.0 + 10.2 + 289.4, "split": 3.0 + 10.2 + 279.1 + 14.5}
 # DRAM bytes per step of the step kernel launch(es) by work-queue configuration, from one ncu
 # capture each on 2^20 steps (spills included), scaled to the bench launch by its steps:
@@ -463,7 +467,7 @@ def run_reference(args, ws, rank):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": config_of(args), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
-                             "sample": sample + ", every step"},
+                             "sample": sample + ", every step", "note": PORT_NOTE},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -708,7 +712,7 @@ def main():
         cv, cv1 = cpu_time_steps(args, [a[:k] for a in hin], hst_np[:k], nthreads)
         m["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": nthreads, "kind": "port",
                              "single_thread_value": cv1,
-                             "sample": "the first %d of the %d step inputs, median of 5 after a warm-up" % (k, n)}
+                             "sample": "the first %d of the %d step inputs, median of 5 after a warm-up" % (k, n), "note": PORT_NOTE}
         emit(headline_line(m))
     if ws > 1:
         import torch.distributed as dist
