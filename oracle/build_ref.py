@@ -61,6 +61,14 @@ UNIT_TESTS = ["TestBox", "TestTube", "TestCons", "TestPolycone", "TestPolyhedra"
 UNIT_DIR = os.path.join(OUT_DIR, "unit_tests")
 
 
+# The reference's shape testers (test/shape_tester/shape_test*.cpp with ShapeTester.cpp and
+# ConventionChecker.cpp: random inside, outside and surface points, the conventions of every
+# query, distance accuracy), for the shapes on the path.
+SHAPE_TESTERS = ["shape_testBox", "shape_testTube", "shape_testCone", "shape_testPolycone", "shape_testPolyhedron",
+                 "shape_testTorus2", "shape_testTrd", "shape_testTrapezoid", "shape_testSphere", "shape_testHype",
+                 "shape_testGenTrap", "shape_testCutTube"]
+
+
 def available():
     return os.path.isdir(os.path.join(REF, "VecGeom")) and os.path.isdir(os.path.join(REF, "source"))
 
@@ -124,6 +132,34 @@ def build_unit_tests(verbose=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("unit-test build failed: %s\n%s" % (" ".join(cmd), r.stderr[-4000:]))
+
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        list(ex.map(run, jobs))
+    return exes
+
+
+def build_shape_testers(verbose=False):
+    """Compile SHAPE_TESTERS against the library; returns {name: executable path}."""
+    lib = build(verbose=verbose)
+    os.makedirs(UNIT_DIR, exist_ok=True)
+    src_dir = os.path.join(REF, "test", "shape_tester")
+    flags = [f for f in FLAGS if f not in ("-DNDEBUG", "-fPIC")]
+    inc = ["-I", SHIM, "-I", REF, "-I", src_dir]
+    libdir = os.path.dirname(lib)
+    common = [os.path.join(src_dir, f) for f in ("ShapeTester.cpp", "ConventionChecker.cpp")]
+    jobs, exes = [], {}
+    for t in SHAPE_TESTERS:
+        src, exe = os.path.join(src_dir, t + ".cpp"), os.path.join(UNIT_DIR, t)
+        exes[t] = exe
+        newest = max(os.path.getmtime(f) for f in [src, lib] + common)
+        if not os.path.exists(exe) or os.path.getmtime(exe) < newest:
+            jobs.append(["g++", *flags, *inc, src, *common, "-o", exe, "-L", libdir, "-lvgref",
+                         "-Wl,-rpath," + libdir])
+
+    def run(cmd):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("shape-tester build failed: %s\n%s" % (" ".join(cmd), r.stderr[-4000:]))
 
     with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
         list(ex.map(run, jobs))

@@ -89,6 +89,31 @@ def test_reference_unit_tests_pass_on_the_stand_in(name):
     assert r.returncode == 0, (r.stdout[-2000:], r.stderr[-2000:])
 
 
+def test_reference_shape_testers_on_the_stand_in(tmp_path):
+    """The reference's shape testers on the stand-in build (run in parallel): every one
+    reports 0 errors except Torus2's, which reports 3 misclassified random points (2 inside,
+    1 outside) on this build; the reference builds its shape testers but registers none of
+    them as a test (test/CMakeLists.txt:300-350), so it states no expected outcome for them."""
+    import subprocess
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import build_ref
+
+    exes = build_ref.build_shape_testers()
+
+    def run(name):
+        d = tmp_path / name
+        d.mkdir()
+        r = subprocess.run([exes[name]], capture_output=True, text=True, timeout=600, cwd=d)
+        last = [ln for ln in r.stdout.splitlines() if "Final Error count" in ln]
+        return name, (int(last[-1].split("=")[-1]) if last else None), r.stdout[-2000:]
+
+    with ThreadPoolExecutor(max_workers=NT) as ex:
+        results = list(ex.map(run, build_ref.SHAPE_TESTERS))
+    for name, errors, tail in results:
+        assert errors == (3 if name == "shape_testTorus2" else 0), (name, tail)
+
+
 def table_padding(t):
     """Mask of the NavIndex table words that hold nothing: the word that rounds a node's
     daughter list to an even count, and the word that aligns a cached matrix to 8 bytes
